@@ -1,0 +1,588 @@
+// api.cu — the C-ABI of include/gbh.h: contexts, grow-only device buffers, and the host side
+// of the force and step path (bh.Solver.Accelerations, Simulation.Step) over the kernels of
+// tree.cu and walk.cu.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "gbh_internal.cuh"
+
+using gbh::DevInfo;
+using gbh::Launch;
+
+struct gbh_ctx {
+    int device = 0;
+    int num_sms = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev[6] = {};
+    gbh::TreeBufs tb;
+    // resident state (state order)
+    int64_t cap = 0, n = 0;
+    bool have_state = false, acc_valid = false;
+    int32_t state_holes = 0;
+    bool state_has_kind = false, state_has_alive = false;
+    double *px = nullptr, *py = nullptr, *pz = nullptr, *vx = nullptr, *vy = nullptr, *vz = nullptr;
+    double *ax = nullptr, *ay = nullptr, *az = nullptr, *mass = nullptr;
+    uint8_t *kind = nullptr, *alive = nullptr;
+    // scratch of the potential and direct-sum calls
+    double *part = nullptr;
+    int64_t part_cap = 0;
+    double *scalar = nullptr;
+    int32_t *holes = nullptr;
+    int64_t holes_cap = 0;
+    int64_t *targets = nullptr;
+    double *tout = nullptr;
+    int64_t targets_cap = 0;
+    float *probe = nullptr;
+    // bookkeeping
+    int64_t launches = 0;
+    int64_t h2d = 0, d2h = 0;
+    DevInfo info_host = {};
+    gbh_timings last = {};
+    std::string err;
+};
+
+namespace {
+
+int fail(gbh_ctx *c, int code, const char *fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    c->err = buf;
+    return code;
+}
+
+#define CK(call)                                                                                  \
+    do {                                                                                          \
+        cudaError_t e_ = (call);                                                                  \
+        if (e_ != cudaSuccess)                                                                    \
+            return fail(ctx, e_ == cudaErrorMemoryAllocation ? GBH_ERR_NOMEM : GBH_ERR_CUDA, "%s: %s (%s:%d)", \
+                        #call, cudaGetErrorString(e_), __FILE__, __LINE__);                       \
+    } while (0)
+
+template <class T>
+cudaError_t grow(T *&p, int64_t &cap, int64_t need) {
+    if (need <= cap && p) return cudaSuccess;
+    if (p) cudaFree(p);
+    p = nullptr;
+    int64_t c = std::max<int64_t>(need + need / 4, 16);
+    cudaError_t e = cudaMalloc(&p, sizeof(T) * size_t(c));
+    cap = e == cudaSuccess ? c : 0;
+    return e;
+}
+
+void free_state(gbh_ctx *c) {
+    void *ptrs[] = {c->px, c->py, c->pz, c->vx, c->vy, c->vz, c->ax, c->ay, c->az, c->mass, c->kind, c->alive};
+    for (void *p : ptrs)
+        if (p) cudaFree(p);
+    c->px = c->py = c->pz = c->vx = c->vy = c->vz = c->ax = c->ay = c->az = c->mass = nullptr;
+    c->kind = c->alive = nullptr;
+    c->cap = 0;
+}
+
+cudaError_t ensure_state(gbh_ctx *c, int64_t n) {
+    if (n <= c->cap && c->px) return cudaSuccess;
+    free_state(c);
+    int64_t cap = std::max<int64_t>(n + n / 4, 16);
+    cudaError_t e = cudaSuccess;
+    double **d[] = {&c->px, &c->py, &c->pz, &c->vx, &c->vy, &c->vz, &c->ax, &c->ay, &c->az, &c->mass};
+    for (double **p : d)
+        if (e == cudaSuccess) e = cudaMalloc(p, sizeof(double) * size_t(cap));
+    if (e == cudaSuccess) e = cudaMalloc(&c->kind, size_t(cap));
+    if (e == cudaSuccess) e = cudaMalloc(&c->alive, size_t(cap));
+    if (e != cudaSuccess) {
+        free_state(c);
+        return e;
+    }
+    c->cap = cap;
+    return cudaSuccess;
+}
+
+int check_params(gbh_ctx *ctx, const gbh_params *p) {
+    if (!p) return fail(ctx, GBH_ERR_ARG, "params is NULL");
+    if (!(p->theta >= 0 && p->theta <= 1)) return fail(ctx, GBH_ERR_ARG, "theta %g outside [0, 1]", p->theta);
+    if (!(p->softening >= 0)) return fail(ctx, GBH_ERR_ARG, "softening %g < 0", p->softening);
+    if (p->leaf_size < 0 || p->leaf_size > 1 << 20) return fail(ctx, GBH_ERR_ARG, "leaf_size %d", p->leaf_size);
+    if (p->walk < GBH_WALK_MIXED || p->walk > GBH_WALK_FP64) return fail(ctx, GBH_ERR_ARG, "walk %d", p->walk);
+    return GBH_OK;
+}
+
+double theta_of(const gbh_params *p) { return p->theta == 0 ? 0.9 : p->theta; }  // bh.go:118-123
+int leaf_of(const gbh_params *p) { return p->leaf_size > 0 ? p->leaf_size : 24; }  // bh.go:67-68
+
+int begin(gbh_ctx *ctx) {
+    if (!ctx) return GBH_ERR_ARG;
+    ctx->err.clear();
+    ctx->launches = 0;
+    ctx->h2d = ctx->d2h = 0;
+    ctx->last = gbh_timings{};
+    cudaError_t e = cudaSetDevice(ctx->device);  // cgo callers may migrate between OS threads
+    if (e != cudaSuccess) return fail(ctx, GBH_ERR_CUDA, "cudaSetDevice: %s", cudaGetErrorString(e));
+    return GBH_OK;
+}
+
+Launch launch_of(gbh_ctx *ctx) { return Launch{ctx->stream, &ctx->launches, ctx->num_sms}; }
+
+int h2d(gbh_ctx *ctx, void *dst, const void *src, size_t bytes) {
+    if (!bytes) return GBH_OK;
+    CK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, ctx->stream));
+    ctx->h2d += int64_t(bytes);
+    return GBH_OK;
+}
+
+int d2h(gbh_ctx *ctx, void *dst, const void *src, size_t bytes) {
+    if (!bytes) return GBH_OK;
+    CK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    ctx->d2h += int64_t(bytes);
+    return GBH_OK;
+}
+
+// Tree build + walk on device arrays; accelerations of alive non-hole bodies, holes zeroed.
+int forces(gbh_ctx *ctx, const gbh_params *p, int64_t n, const double *px, const double *py, const double *pz,
+           const double *mass, const uint8_t *kind, const uint8_t *alive, double *ax, double *ay, double *az,
+           double theta, float *build_ms_slot, float *walk_ms_slot) {
+    (void)build_ms_slot;
+    (void)walk_ms_slot;
+    Launch L = launch_of(ctx);
+    int leaf = leaf_of(p);
+    CK(gbh::tree_alloc(ctx->tb, n, leaf));
+    CK(gbh::tree_build(L, ctx->tb, n, px, py, pz, mass, kind, alive, ax, ay, az, theta, leaf, p->dark_matter_off));
+    CK(cudaEventRecord(ctx->ev[1], ctx->stream));
+    double eps2 = p->softening * p->softening;
+    int quad = !p->monopole_only;
+    switch (p->walk) {
+        case GBH_WALK_FP64:
+            CK(gbh::walk_fp64(L, ctx->tb, n, eps2, quad, ax, ay, az));
+            break;
+        case GBH_WALK_PLAIN:
+            if (!quad) return fail(ctx, GBH_ERR_ARG, "the plain FP32 walk always uses quadrupoles (as the Metal kernel)");
+            CK(gbh::walk_plain(L, ctx->tb, ctx->tb.cap_n, float(eps2), ax, ay, az));
+            break;
+        default:
+            CK(gbh::walk_mixed(L, ctx->tb, ctx->tb.cap_n, float(eps2), quad, ax, ay, az));
+            break;
+    }
+    CK(cudaEventRecord(ctx->ev[2], ctx->stream));
+    return GBH_OK;
+}
+
+// Waits for the stream, reads the device scalars and fills the timings of the call.
+int finish(gbh_ctx *ctx, bool tree, bool staged) {
+    CK(cudaEventRecord(ctx->ev[5], ctx->stream));
+    if (tree && ctx->tb.info) {
+        CK(cudaMemcpyAsync(&ctx->info_host, ctx->tb.info, sizeof(DevInfo), cudaMemcpyDeviceToHost, ctx->stream));
+    }
+    CK(cudaStreamSynchronize(ctx->stream));
+    float ms = 0;
+    gbh_timings &t = ctx->last;
+    if (cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[5]) == cudaSuccess) t.total_ms = ms;
+    if (staged) {
+        if (cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[1]) == cudaSuccess) t.build_ms = ms;
+        if (cudaEventElapsedTime(&ms, ctx->ev[1], ctx->ev[2]) == cudaSuccess) t.walk_ms = ms;
+    }
+    t.launches = ctx->launches;
+    t.h2d_bytes = ctx->h2d;
+    t.d2h_bytes = ctx->d2h;
+    if (tree) {
+        t.nstars = ctx->info_host.nstars;
+        t.nnodes = ctx->info_host.nnodes;
+        if (ctx->info_host.err)
+            return fail(ctx, GBH_ERR_LIMIT, "device walk exceeded its step bound (kernel %d)", ctx->info_host.err_where);
+    }
+    return GBH_OK;
+}
+
+int count_holes(const uint8_t *kind, const uint8_t *alive, int64_t n) {
+    if (!kind) return 0;
+    int64_t h = 0;
+    for (int64_t i = 0; i < n; ++i)
+        if ((alive ? alive[i] : 1) && kind[i] == GBH_BLACK_HOLE) ++h;
+    return int(std::min<int64_t>(h, 1 << 30));
+}
+
+// Steps on the resident state (sim.go:252-288, no holes, no hydro).
+int run_steps(gbh_ctx *ctx, const gbh_params *p, double dt, int64_t nsteps) {
+    Launch L = launch_of(ctx);
+    int64_t n = ctx->n;
+    const uint8_t *kind = ctx->state_has_kind ? ctx->kind : nullptr;
+    const uint8_t *alive = ctx->state_has_alive ? ctx->alive : nullptr;
+    double theta = theta_of(p);
+    float dummy = 0;
+    if (!ctx->acc_valid) {  // initForces (gas.go:14-17)
+        int rc = forces(ctx, p, n, ctx->px, ctx->py, ctx->pz, ctx->mass, kind, alive, ctx->ax, ctx->ay, ctx->az, theta,
+                        &dummy, &dummy);
+        if (rc) return rc;
+        ctx->acc_valid = true;
+    }
+    double h = 0.5 * dt;
+    for (int64_t s = 0; s < nsteps; ++s) {
+        CK(gbh::kick_drift(L, n, h, dt, ctx->px, ctx->py, ctx->pz, ctx->vx, ctx->vy, ctx->vz, ctx->ax, ctx->ay,
+                           ctx->az));
+        int rc = forces(ctx, p, n, ctx->px, ctx->py, ctx->pz, ctx->mass, kind, alive, ctx->ax, ctx->ay, ctx->az, theta,
+                        &dummy, &dummy);
+        if (rc) return rc;
+        CK(gbh::kick(L, n, h, ctx->vx, ctx->vy, ctx->vz, ctx->ax, ctx->ay, ctx->az));
+    }
+    return GBH_OK;
+}
+
+int upload_state(gbh_ctx *ctx, int64_t n, const double *px, const double *py, const double *pz, const double *vx,
+                 const double *vy, const double *vz, const double *ax, const double *ay, const double *az,
+                 const double *mass, const uint8_t *kind, const uint8_t *alive) {
+    if (n < 0 || n > (int64_t(1) << 30)) return fail(ctx, GBH_ERR_ARG, "n = %lld out of range", (long long)n);
+    if (n > 0 && (!px || !py || !pz || !vx || !vy || !vz || !mass))
+        return fail(ctx, GBH_ERR_ARG, "state arrays must not be NULL");
+    CK(ensure_state(ctx, n));
+    size_t b = sizeof(double) * size_t(n);
+    int rc;
+    const double *src[] = {px, py, pz, vx, vy, vz, mass};
+    double *dst[] = {ctx->px, ctx->py, ctx->pz, ctx->vx, ctx->vy, ctx->vz, ctx->mass};
+    for (int k = 0; k < 7; ++k)
+        if ((rc = h2d(ctx, dst[k], src[k], b))) return rc;
+    bool acc = ax && ay && az;
+    if (acc) {
+        if ((rc = h2d(ctx, ctx->ax, ax, b)) || (rc = h2d(ctx, ctx->ay, ay, b)) || (rc = h2d(ctx, ctx->az, az, b)))
+            return rc;
+    } else if (n > 0) {
+        CK(cudaMemsetAsync(ctx->ax, 0, b, ctx->stream));
+        CK(cudaMemsetAsync(ctx->ay, 0, b, ctx->stream));
+        CK(cudaMemsetAsync(ctx->az, 0, b, ctx->stream));
+    }
+    ctx->state_has_kind = kind != nullptr;
+    ctx->state_has_alive = alive != nullptr;
+    if (kind && (rc = h2d(ctx, ctx->kind, kind, size_t(n)))) return rc;
+    if (alive && (rc = h2d(ctx, ctx->alive, alive, size_t(n)))) return rc;
+    ctx->n = n;
+    ctx->have_state = true;
+    ctx->acc_valid = acc;
+    ctx->state_holes = count_holes(kind, alive, n);
+    return GBH_OK;
+}
+
+int download_state(gbh_ctx *ctx, double *px, double *py, double *pz, double *vx, double *vy, double *vz, double *ax,
+                   double *ay, double *az) {
+    size_t b = sizeof(double) * size_t(ctx->n);
+    double *dst[] = {px, py, pz, vx, vy, vz, ax, ay, az};
+    const double *src[] = {ctx->px, ctx->py, ctx->pz, ctx->vx, ctx->vy, ctx->vz, ctx->ax, ctx->ay, ctx->az};
+    for (int k = 0; k < 9; ++k)
+        if (dst[k]) {
+            int rc = d2h(ctx, dst[k], src[k], b);
+            if (rc) return rc;
+        }
+    return GBH_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int gbh_create(const gbh_config *cfg, gbh_ctx **out, char *err, int errlen) {
+    auto report = [&](int code, const char *msg) {
+        if (err && errlen > 0) {
+            std::strncpy(err, msg, size_t(errlen) - 1);
+            err[errlen - 1] = 0;
+        }
+        return code;
+    };
+    if (!out) return report(GBH_ERR_ARG, "out is NULL");
+    *out = nullptr;
+    int dev = cfg ? cfg->device : 0;
+    int count = 0;
+    cudaError_t e = cudaGetDeviceCount(&count);
+    if (e != cudaSuccess) return report(GBH_ERR_CUDA, cudaGetErrorString(e));
+    if (dev < 0 || dev >= count) return report(GBH_ERR_ARG, "no such CUDA device");
+    if ((e = cudaSetDevice(dev)) != cudaSuccess) return report(GBH_ERR_CUDA, cudaGetErrorString(e));
+    cudaDeviceProp prop;
+    if ((e = cudaGetDeviceProperties(&prop, dev)) != cudaSuccess) return report(GBH_ERR_CUDA, cudaGetErrorString(e));
+    if (prop.major < 10) return report(GBH_ERR_UNSUPPORTED, "libgbh is built for sm_103a (GB300)");
+    gbh_ctx *c = new gbh_ctx();
+    c->device = dev;
+    c->num_sms = prop.multiProcessorCount;
+    if ((e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking)) != cudaSuccess) {
+        delete c;
+        return report(GBH_ERR_CUDA, cudaGetErrorString(e));
+    }
+    for (auto &ev : c->ev) {
+        if ((e = cudaEventCreate(&ev)) != cudaSuccess) {
+            gbh_destroy(c);
+            return report(GBH_ERR_CUDA, cudaGetErrorString(e));
+        }
+    }
+    *out = c;
+    return report(GBH_OK, "");
+}
+
+void gbh_destroy(gbh_ctx *c) {
+    if (!c) return;
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    gbh::tree_free(c->tb);
+    free_state(c);
+    void *ptrs[] = {c->part, c->scalar, c->holes, c->targets, c->tout, c->probe};
+    for (void *p : ptrs)
+        if (p) cudaFree(p);
+    for (auto &ev : c->ev)
+        if (ev) cudaEventDestroy(ev);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+}
+
+const char *gbh_last_error(const gbh_ctx *ctx) { return ctx ? ctx->err.c_str() : "NULL context"; }
+
+int gbh_device_name(gbh_ctx *ctx, char *out, int len) {
+    int rc = begin(ctx);
+    if (rc) return rc;
+    if (!out || len <= 0) return fail(ctx, GBH_ERR_ARG, "bad output buffer");
+    cudaDeviceProp prop;
+    CK(cudaGetDeviceProperties(&prop, ctx->device));
+    std::strncpy(out, prop.name, size_t(len) - 1);
+    out[len - 1] = 0;
+    return GBH_OK;
+}
+
+int gbh_accelerations(gbh_ctx *ctx, const gbh_params *p, int64_t n, const double *px, const double *py,
+                      const double *pz, const double *mass, const uint8_t *kind, const uint8_t *alive, double *ax,
+                      double *ay, double *az) {
+    int rc = begin(ctx);
+    if (rc || (rc = check_params(ctx, p))) return rc;
+    if (n < 0 || n > (int64_t(1) << 30)) return fail(ctx, GBH_ERR_ARG, "n = %lld out of range", (long long)n);
+    if (n == 0) return GBH_OK;
+    if (!px || !py || !pz || !mass || !ax || !ay || !az) return fail(ctx, GBH_ERR_ARG, "array argument is NULL");
+    CK(ensure_state(ctx, n));
+    ctx->have_state = false;  // the state buffers now hold this call's arrays
+    CK(cudaEventRecord(ctx->ev[0], ctx->stream));
+    size_t b = sizeof(double) * size_t(n);
+    if ((rc = h2d(ctx, ctx->px, px, b)) || (rc = h2d(ctx, ctx->py, py, b)) || (rc = h2d(ctx, ctx->pz, pz, b)) ||
+        (rc = h2d(ctx, ctx->mass, mass, b)))
+        return rc;
+    // Dead bodies keep their entries (bh.go:141-150 writes only stars and holes).
+    if ((rc = h2d(ctx, ctx->ax, ax, b)) || (rc = h2d(ctx, ctx->ay, ay, b)) || (rc = h2d(ctx, ctx->az, az, b))) return rc;
+    if (kind && (rc = h2d(ctx, ctx->kind, kind, size_t(n)))) return rc;
+    if (alive && (rc = h2d(ctx, ctx->alive, alive, size_t(n)))) return rc;
+    float dummy;
+    rc = forces(ctx, p, n, ctx->px, ctx->py, ctx->pz, ctx->mass, kind ? ctx->kind : nullptr,
+                alive ? ctx->alive : nullptr, ctx->ax, ctx->ay, ctx->az, theta_of(p), &dummy, &dummy);
+    if (rc) return rc;
+    if ((rc = d2h(ctx, ax, ctx->ax, b)) || (rc = d2h(ctx, ay, ctx->ay, b)) || (rc = d2h(ctx, az, ctx->az, b))) return rc;
+    return finish(ctx, true, false);
+}
+
+int gbh_potential_energy(gbh_ctx *ctx, const gbh_params *p, int64_t n, const double *px, const double *py,
+                         const double *pz, const double *mass, const uint8_t *kind, const uint8_t *alive, double c,
+                         double *u) {
+    int rc = begin(ctx);
+    if (rc || (rc = check_params(ctx, p))) return rc;
+    if (!u) return fail(ctx, GBH_ERR_ARG, "u is NULL");
+    *u = 0;
+    if (n < 0 || n > (int64_t(1) << 30)) return fail(ctx, GBH_ERR_ARG, "n out of range");
+    if (n == 0) return GBH_OK;
+    if (!px || !py || !pz || !mass) return fail(ctx, GBH_ERR_ARG, "array argument is NULL");
+    CK(ensure_state(ctx, n));
+    ctx->have_state = false;
+    CK(cudaEventRecord(ctx->ev[0], ctx->stream));
+    size_t b = sizeof(double) * size_t(n);
+    if ((rc = h2d(ctx, ctx->px, px, b)) || (rc = h2d(ctx, ctx->py, py, b)) || (rc = h2d(ctx, ctx->pz, pz, b)) ||
+        (rc = h2d(ctx, ctx->mass, mass, b)))
+        return rc;
+    if (kind && (rc = h2d(ctx, ctx->kind, kind, size_t(n)))) return rc;
+    if (alive && (rc = h2d(ctx, ctx->alive, alive, size_t(n)))) return rc;
+    // Holes in state order (collect, build.go:65-69).
+    std::vector<int32_t> holes;
+    if (kind)
+        for (int64_t i = 0; i < n; ++i)
+            if ((alive ? alive[i] : 1) && kind[i] == GBH_BLACK_HOLE) holes.push_back(int32_t(i));
+    CK(grow(ctx->holes, ctx->holes_cap, int64_t(holes.size()) + 1));
+    if (!holes.empty() && (rc = h2d(ctx, ctx->holes, holes.data(), holes.size() * sizeof(int32_t)))) return rc;
+    Launch L = launch_of(ctx);
+    int leaf = leaf_of(p);
+    double theta = std::min(theta_of(p), 0.9);  // diagTheta, potential.go:12-14
+    CK(gbh::tree_alloc(ctx->tb, n, leaf));
+    CK(gbh::tree_build(L, ctx->tb, n, ctx->px, ctx->py, ctx->pz, ctx->mass, kind ? ctx->kind : nullptr,
+                       alive ? ctx->alive : nullptr, ctx->ax, ctx->ay, ctx->az, theta, leaf, p->dark_matter_off));
+    int64_t nparts = (ctx->tb.cap_n + 255) / 256;
+    CK(grow(ctx->part, ctx->part_cap, nparts));
+    if (!ctx->scalar) CK(cudaMalloc(&ctx->scalar, 64));
+    double eps2 = p->softening * p->softening;
+    CK(gbh::potential_fp64(L, ctx->tb, n, ctx->px, ctx->py, ctx->pz, ctx->mass, kind ? ctx->kind : nullptr,
+                           alive ? ctx->alive : nullptr, ctx->holes, int32_t(holes.size()), eps2, c,
+                           p->dark_matter_off, !p->monopole_only, ctx->part, ctx->scalar));
+    if ((rc = d2h(ctx, u, ctx->scalar, sizeof(double)))) return rc;
+    return finish(ctx, true, false);
+}
+
+int gbh_direct_accelerations(gbh_ctx *ctx, const gbh_params *p, int64_t n, const double *px, const double *py,
+                             const double *pz, const double *mass, const uint8_t *kind, const int64_t *targets,
+                             int64_t ntargets, double *ax, double *ay, double *az) {
+    int rc = begin(ctx);
+    if (rc || (rc = check_params(ctx, p))) return rc;
+    if (n < 0 || n > (int64_t(1) << 30)) return fail(ctx, GBH_ERR_ARG, "n out of range");
+    if (!targets) ntargets = n;
+    if (ntargets < 0) return fail(ctx, GBH_ERR_ARG, "ntargets < 0");
+    if (n == 0 || ntargets == 0) return GBH_OK;
+    if (!px || !py || !pz || !mass || !ax || !ay || !az) return fail(ctx, GBH_ERR_ARG, "array argument is NULL");
+    if (targets)
+        for (int64_t q = 0; q < ntargets; ++q)
+            if (targets[q] < 0 || targets[q] >= n) return fail(ctx, GBH_ERR_ARG, "target %lld out of range", (long long)q);
+    CK(ensure_state(ctx, n));
+    ctx->have_state = false;
+    CK(cudaEventRecord(ctx->ev[0], ctx->stream));
+    size_t b = sizeof(double) * size_t(n);
+    if ((rc = h2d(ctx, ctx->px, px, b)) || (rc = h2d(ctx, ctx->py, py, b)) || (rc = h2d(ctx, ctx->pz, pz, b)) ||
+        (rc = h2d(ctx, ctx->mass, mass, b)))
+        return rc;
+    if (kind && (rc = h2d(ctx, ctx->kind, kind, size_t(n)))) return rc;
+    CK(grow(ctx->targets, ctx->targets_cap, ntargets));
+    CK(cudaFree(ctx->tout));
+    ctx->tout = nullptr;
+    CK(cudaMalloc(&ctx->tout, sizeof(double) * 3 * size_t(ctx->targets_cap)));
+    if (targets && (rc = h2d(ctx, ctx->targets, targets, sizeof(int64_t) * size_t(ntargets)))) return rc;
+    double *tx = ctx->tout, *ty = tx + ctx->targets_cap, *tz = ty + ctx->targets_cap;
+    Launch L = launch_of(ctx);
+    CK(gbh::direct_fp64(L, n, ctx->px, ctx->py, ctx->pz, ctx->mass, kind ? ctx->kind : nullptr,
+                        p->softening * p->softening, p->dark_matter_off, targets ? ctx->targets : nullptr, ntargets,
+                        tx, ty, tz));
+    size_t tb = sizeof(double) * size_t(ntargets);
+    if ((rc = d2h(ctx, ax, tx, tb)) || (rc = d2h(ctx, ay, ty, tb)) || (rc = d2h(ctx, az, tz, tb))) return rc;
+    return finish(ctx, false, false);
+}
+
+int gbh_step_kdk(gbh_ctx *ctx, const gbh_params *p, double dt, int64_t nsteps, int32_t acc_valid, int64_t n,
+                 double *px, double *py, double *pz, double *vx, double *vy, double *vz, double *ax, double *ay,
+                 double *az, const double *mass, const uint8_t *kind, const uint8_t *alive) {
+    int rc = begin(ctx);
+    if (rc || (rc = check_params(ctx, p))) return rc;
+    if (nsteps < 0) return fail(ctx, GBH_ERR_ARG, "nsteps < 0");
+    if (!ax || !ay || !az) return fail(ctx, GBH_ERR_ARG, "acceleration arrays must not be NULL");
+    if (count_holes(kind, alive, n))
+        return fail(ctx, GBH_ERR_UNSUPPORTED,
+                    "alive black holes need the hole-aware split step (sim.stepSplit), which this path does not cover");
+    CK(cudaEventRecord(ctx->ev[0], ctx->stream));
+    rc = upload_state(ctx, n, px, py, pz, vx, vy, vz, acc_valid ? ax : nullptr, acc_valid ? ay : nullptr,
+                      acc_valid ? az : nullptr, mass, kind, alive);
+    if (rc) return rc;
+    if (n > 0 && (rc = run_steps(ctx, p, dt, nsteps))) return rc;
+    if ((rc = download_state(ctx, px, py, pz, vx, vy, vz, ax, ay, az))) return rc;
+    return finish(ctx, n > 0, false);
+}
+
+int gbh_state_upload(gbh_ctx *ctx, int64_t n, const double *px, const double *py, const double *pz, const double *vx,
+                     const double *vy, const double *vz, const double *ax, const double *ay, const double *az,
+                     const double *mass, const uint8_t *kind, const uint8_t *alive) {
+    int rc = begin(ctx);
+    if (rc) return rc;
+    CK(cudaEventRecord(ctx->ev[0], ctx->stream));
+    if ((rc = upload_state(ctx, n, px, py, pz, vx, vy, vz, ax, ay, az, mass, kind, alive))) return rc;
+    return finish(ctx, false, false);
+}
+
+int gbh_state_download(gbh_ctx *ctx, double *px, double *py, double *pz, double *vx, double *vy, double *vz, double *ax,
+                       double *ay, double *az) {
+    int rc = begin(ctx);
+    if (rc) return rc;
+    if (!ctx->have_state) return fail(ctx, GBH_ERR_STATE, "no resident state");
+    CK(cudaEventRecord(ctx->ev[0], ctx->stream));
+    if ((rc = download_state(ctx, px, py, pz, vx, vy, vz, ax, ay, az))) return rc;
+    return finish(ctx, false, false);
+}
+
+int gbh_state_step(gbh_ctx *ctx, const gbh_params *p, double dt, int64_t nsteps) {
+    int rc = begin(ctx);
+    if (rc || (rc = check_params(ctx, p))) return rc;
+    if (!ctx->have_state) return fail(ctx, GBH_ERR_STATE, "no resident state (gbh_state_upload first)");
+    if (nsteps < 0) return fail(ctx, GBH_ERR_ARG, "nsteps < 0");
+    if (ctx->state_holes)
+        return fail(ctx, GBH_ERR_UNSUPPORTED,
+                    "alive black holes need the hole-aware split step (sim.stepSplit), which this path does not cover");
+    CK(cudaEventRecord(ctx->ev[0], ctx->stream));
+    if (ctx->n > 0 && (rc = run_steps(ctx, p, dt, nsteps))) return rc;
+    return finish(ctx, ctx->n > 0, false);
+}
+
+int gbh_state_accelerations(gbh_ctx *ctx, const gbh_params *p) {
+    int rc = begin(ctx);
+    if (rc || (rc = check_params(ctx, p))) return rc;
+    if (!ctx->have_state) return fail(ctx, GBH_ERR_STATE, "no resident state (gbh_state_upload first)");
+    if (ctx->n == 0) return GBH_OK;
+    CK(cudaEventRecord(ctx->ev[0], ctx->stream));
+    float dummy;
+    rc = forces(ctx, p, ctx->n, ctx->px, ctx->py, ctx->pz, ctx->mass, ctx->state_has_kind ? ctx->kind : nullptr,
+                ctx->state_has_alive ? ctx->alive : nullptr, ctx->ax, ctx->ay, ctx->az, theta_of(p), &dummy, &dummy);
+    if (rc) return rc;
+    ctx->acc_valid = true;
+    return finish(ctx, true, true);
+}
+
+int gbh_tree_size(gbh_ctx *ctx, int64_t *nstars, int64_t *nnodes) {
+    int rc = begin(ctx);
+    if (rc) return rc;
+    if (!ctx->tb.info) return fail(ctx, GBH_ERR_STATE, "no tree built yet");
+    CK(cudaMemcpy(&ctx->info_host, ctx->tb.info, sizeof(DevInfo), cudaMemcpyDeviceToHost));
+    if (nstars) *nstars = ctx->info_host.nstars;
+    if (nnodes) *nnodes = ctx->info_host.nnodes;
+    return GBH_OK;
+}
+
+int gbh_tree_export(gbh_ctx *ctx, uint64_t *keys, int32_t *order, gbh_node *nodes, int64_t node_cap) {
+    int rc = begin(ctx);
+    if (rc) return rc;
+    if (!ctx->tb.info) return fail(ctx, GBH_ERR_STATE, "no tree built yet");
+    CK(cudaMemcpy(&ctx->info_host, ctx->tb.info, sizeof(DevInfo), cudaMemcpyDeviceToHost));
+    int64_t ns = ctx->info_host.nstars, nn = ctx->info_host.nnodes;
+    if (keys && ns) CK(cudaMemcpy(keys, ctx->tb.keys, sizeof(uint64_t) * size_t(ns), cudaMemcpyDeviceToHost));
+    if (order && ns) CK(cudaMemcpy(order, ctx->tb.order, sizeof(int32_t) * size_t(ns), cudaMemcpyDeviceToHost));
+    int64_t cnt = std::min(nn, node_cap);
+    if (nodes && cnt > 0) CK(cudaMemcpy(nodes, ctx->tb.nodes, sizeof(gbh_node) * size_t(cnt), cudaMemcpyDeviceToHost));
+    return GBH_OK;
+}
+
+int gbh_last_timings(gbh_ctx *ctx, gbh_timings *t) {
+    if (!ctx || !t) return GBH_ERR_ARG;
+    *t = ctx->last;
+    return GBH_OK;
+}
+
+int gbh_probe_fp32_peak(gbh_ctx *ctx, double ms, double *tflops) {
+    int rc = begin(ctx);
+    if (rc) return rc;
+    if (!tflops) return fail(ctx, GBH_ERR_ARG, "tflops is NULL");
+    if (!ctx->probe) CK(cudaMalloc(&ctx->probe, sizeof(float) * 65536));
+    Launch L = launch_of(ctx);
+    int blocks = ctx->num_sms * 8;  // 8 x 256 threads = 64 warps per SM
+    int iters = 64;
+    // Calibrate the iteration count so one launch lasts about ms.
+    for (int round = 0; round < 8; ++round) {
+        CK(cudaEventRecord(ctx->ev[0], ctx->stream));
+        CK(gbh::fp32_fma_probe(L, blocks, iters, ctx->probe));
+        CK(cudaEventRecord(ctx->ev[1], ctx->stream));
+        CK(cudaEventSynchronize(ctx->ev[1]));
+        float t = 0;
+        CK(cudaEventElapsedTime(&t, ctx->ev[0], ctx->ev[1]));
+        if (t >= ms * 0.5 || iters > (1 << 24)) {
+            double flops = 2.0 * 8 * 16 * double(iters) * double(blocks) * 256;
+            // best of 3 at this size
+            float best = t;
+            for (int r = 0; r < 3; ++r) {
+                CK(cudaEventRecord(ctx->ev[0], ctx->stream));
+                CK(gbh::fp32_fma_probe(L, blocks, iters, ctx->probe));
+                CK(cudaEventRecord(ctx->ev[1], ctx->stream));
+                CK(cudaEventSynchronize(ctx->ev[1]));
+                CK(cudaEventElapsedTime(&t, ctx->ev[0], ctx->ev[1]));
+                best = std::min(best, t);
+            }
+            *tflops = flops / (double(best) * 1e-3) / 1e12;
+            return GBH_OK;
+        }
+        double scale = t > 0 ? ms / t : 8.0;
+        iters = int(std::min<double>(double(iters) * std::min(scale, 16.0), double(1 << 25)));
+    }
+    return fail(ctx, GBH_ERR_CUDA, "probe did not converge");
+}
+
+}  // extern "C"

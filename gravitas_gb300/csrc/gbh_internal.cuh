@@ -1,0 +1,127 @@
+// Internal declarations shared by the CUDA translation units of libgbh.
+//
+// Layout in HBM (one context, one tree at a time):
+//   state, state order (SoA FP64): px py pz vx vy vz ax ay az mass, kind/alive u8
+//   sorted stars: keys u64, order i32, sx sy sz sm FP64, st_hi/st_lo float4
+//   nodes, reference serial index layout: gbh_node (104 B) + walk records
+//     PNode (64 B, FP32, the Metal GNode) and MNode (64 B, hi/lo FP32) + int2 ranges
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/gbh.h"
+
+namespace gbh {
+
+constexpr int kMortonBits = 21;           // morton.go:4
+constexpr int kMaxLevel = kMortonBits;    // buildNode splits only below level 21 (build.go:136)
+constexpr int kNoCell = 22;               // "starts no cell": duplicate of the previous key
+
+// Per-build scalars kept on the device, so a step needs no host round trip.
+struct DevInfo {
+    double minx, miny, minz;  // bbox min of the stars (build.go:12)
+    double side;              // root cube side (build.go:19-20)
+    double scale;             // 2^21 / side (build.go:21)
+    double theta;             // opening angle used for crit2
+    int64_t nstars;           // alive non-hole bodies
+    int64_t nnodes;           // nodes of the tree
+    int32_t err;              // device-side limit hit (walk step bound, stack bound)
+    int32_t err_where;        // which kernel set err
+    uint32_t work;            // work counter of persistent kernels
+    uint32_t pad;
+};
+
+// The Metal kernel's GNode (gpu_darwin.go:79,121-124): com (x,y,z,m), q1 (qxx,qyy,qzz,qxy),
+// q2 (qxz,qyz,crit2,0), links (first,next,lo,hi).
+struct __align__(16) PNode {
+    float4 com, q1, q2;
+    int4 links;
+};
+
+// Mixed-walk node: a = (com_hi.xyz, crit2), b = (com_lo.xyz, m), c = (qxx,qyy,qzz,qxy),
+// d = (qxz, qyz, first as bits, next as bits). com = com_hi + com_lo (FP64 split in two FP32).
+struct __align__(16) MNode {
+    float4 a, b, c, d;
+};
+
+// Device buffers of the tree path (all owned by the context).
+struct TreeBufs {
+    int64_t cap_n = 0;      // bodies
+    int64_t cap_nodes = 0;  // nodes
+    // compaction / bbox
+    uint32_t *flag = nullptr;     // star flags, then their exclusive scan
+    double *bbox_part = nullptr;  // per-block partial min/max (6 per block)
+    // sort
+    uint64_t *keys = nullptr, *keys_alt = nullptr;
+    int32_t *order = nullptr, *order_alt = nullptr;
+    uint32_t *hist = nullptr;     // radix digit table
+    // sorted stars
+    double *sx = nullptr, *sy = nullptr, *sz = nullptr, *sm = nullptr;
+    float4 *st_hi = nullptr, *st_lo = nullptr;
+    // chain topology, indexed by sorted position
+    uint32_t *chain_cnt = nullptr;  // nodes starting at each position, then the scan
+    // pre-order node arrays (index p)
+    int32_t *pre_parent = nullptr;
+    uint32_t *pre_info = nullptr;   // level | oct << 8 | mask << 16
+    uint32_t *pre_nchild = nullptr; // then its exclusive scan
+    int32_t *pre_ref = nullptr;     // reference index of pre-order node p
+    // reference-layout node arrays (index r)
+    gbh_node *nodes = nullptr;
+    int32_t *n_parent = nullptr;
+    uint32_t *n_info = nullptr;     // level | nchild << 8
+    int32_t *n_arrive = nullptr;
+    PNode *pnodes = nullptr;
+    MNode *mnodes = nullptr;
+    int2 *mrange = nullptr;
+    // scan temporaries
+    uint32_t *scan_tmp = nullptr;
+    int64_t scan_tmp_cap = 0;
+    DevInfo *info = nullptr;
+};
+
+// Launch helper context: stream and launch counter.
+struct Launch {
+    cudaStream_t stream;
+    int64_t *count;
+    int num_sms;
+};
+
+// ---- tree.cu (FP64 parts compiled without FMA contraction) ----
+cudaError_t tree_alloc(TreeBufs &b, int64_t n, int leaf_size);
+void tree_free(TreeBufs &b);
+// Builds the tree of the alive non-hole bodies; zeroes alive holes' accelerations.
+cudaError_t tree_build(const Launch &L, TreeBufs &b, int64_t n, const double *px, const double *py,
+                       const double *pz, const double *mass, const uint8_t *kind,
+                       const uint8_t *alive, double *ax, double *ay, double *az, double theta,
+                       int leaf_size, int dm_off);
+cudaError_t walk_fp64(const Launch &L, const TreeBufs &b, int64_t n, double eps2, int quad,
+                      double *ax, double *ay, double *az);
+cudaError_t kick(const Launch &L, int64_t n, double h, double *vx, double *vy, double *vz,
+                 const double *ax, const double *ay, const double *az);
+cudaError_t kick_drift(const Launch &L, int64_t n, double h, double dt, double *px, double *py,
+                       double *pz, double *vx, double *vy, double *vz, const double *ax,
+                       const double *ay, const double *az);
+cudaError_t direct_fp64(const Launch &L, int64_t n, const double *px, const double *py,
+                        const double *pz, const double *mass, const uint8_t *kind, double eps2,
+                        int dm_off, const int64_t *targets, int64_t ntargets, double *ax,
+                        double *ay, double *az);
+// Potential: psi sums of the FP64 walk plus hole terms; result in *u_dev.
+cudaError_t potential_fp64(const Launch &L, const TreeBufs &b, int64_t n, const double *px,
+                           const double *py, const double *pz, const double *mass,
+                           const uint8_t *kind, const uint8_t *alive, const int32_t *holes,
+                           int32_t nholes, double eps2, double c, int dm_off, int quad,
+                           double *part, double *u_dev);
+// Exclusive scan of n uint32 in place (in may equal out).
+cudaError_t scan_u32(const Launch &L, const uint32_t *in, uint32_t *out, int64_t n,
+                     uint32_t *tmp, int64_t tmp_cap);
+int64_t scan_tmp_size(int64_t n);
+
+// ---- walk.cu (FP32 walks, FMA contraction on) ----
+cudaError_t walk_plain(const Launch &L, const TreeBufs &b, int64_t nstars_cap, float eps2,
+                       double *ax, double *ay, double *az);
+cudaError_t walk_mixed(const Launch &L, const TreeBufs &b, int64_t nstars_cap, float eps2,
+                       int quad, double *ax, double *ay, double *az);
+cudaError_t fp32_fma_probe(const Launch &L, int blocks, int iters, float *out);
+
+}  // namespace gbh

@@ -1,0 +1,1174 @@
+// tree.cu — octree construction and the FP64 kernels of the Barnes-Hut step.
+//
+// Compiled with -fmad=false: every FP64 a*b+c is a rounded multiply and a rounded add, as in
+// the reference's arithmetic, so keys, node moments, the FP64 walk, the direct sum and the
+// kick/drift are bit identical to it.
+//
+// Pipeline of tree_build (one stream, no host round trip):
+//   k_flags_bbox -> scan -> k_bbox_final -> k_compact_keys          (collect + keys, build.go:11-31, 62-113)
+//   8 x (k_rs_hist -> scan -> k_rs_scatter)                         (stable LSD radix sort, morton.go:25-49)
+//   k_gather                                                        (sorted copies, build.go:34-41)
+//   k_chain_count -> scan -> k_chain_emit -> scan -> k_ref_index -> k_emit_nodes
+//                                                                   (node set and links of buildNode, build.go:134-172)
+//   k_upsweep                                                       (finish, build.go:176-217)
+//
+// Node set without recursion. A cell at level L is the set of sorted stars whose keys share
+// their top 3L bits. The reference creates a node for the root and for every non-empty octant
+// of a node that splits (count > leaf and level < 21). Counts shrink down the tree, so a
+// non-root cell is a node exactly when its parent cell holds more than leaf stars. Every node
+// starts at some sorted position i; the nodes starting at i form a chain of consecutive levels
+// (a node and its first child share their first star). Sorting nodes by (first star, level) is
+// the walk's pre-order, so the skip pointer of a node is the shallowest node that starts where
+// it ends. The reference's serial build allocates each node's children as one block when the
+// node is visited in that pre-order, so a prefix sum of child counts over pre-order gives every
+// node its index in the reference's own serial layout.
+#include <cuda_runtime.h>
+
+#include "gbh_internal.cuh"
+
+namespace gbh {
+
+namespace {
+
+constexpr int kScanThreads = 256;
+constexpr int kScanItems = 8;
+constexpr int kScanTile = kScanThreads * kScanItems;
+
+constexpr int kRsThreads = 256;
+constexpr int kRsItems = 8;
+constexpr int kRsTile = kRsThreads * kRsItems;
+constexpr int kRsWarps = kRsThreads / 32;
+constexpr int kRsBins = 256;
+
+constexpr int kThreads = 256;
+
+inline unsigned blocks_for(int64_t n, int threads) {
+    int64_t b = (n + threads - 1) / threads;
+    return unsigned(b < 1 ? 1 : b);
+}
+
+// ---------------------------------------------------------------- exclusive scan (uint32)
+
+__device__ __forceinline__ uint32_t warp_incl_scan(uint32_t v) {
+    int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t t = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o) v += t;
+    }
+    return v;
+}
+
+// Block-wide exclusive scan of one value per thread; returns the exclusive prefix and the total.
+__device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t *s_warp, uint32_t &total) {
+    int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t incl = warp_incl_scan(v);
+    if (lane == 31) s_warp[warp] = incl;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t w = lane < (kScanThreads / 32) ? s_warp[lane] : 0;
+        uint32_t wi = warp_incl_scan(w);
+        if (lane < (kScanThreads / 32)) s_warp[lane] = wi - w;
+        if (lane == (kScanThreads / 32) - 1) s_warp[kScanThreads / 32] = wi;
+    }
+    __syncthreads();
+    uint32_t r = s_warp[warp] + incl - v;
+    total = s_warp[kScanThreads / 32];
+    __syncthreads();
+    return r;
+}
+
+__device__ __forceinline__ int64_t dyn_len(int64_t n, const int64_t *ndyn) {
+    if (ndyn) {
+        int64_t m = *ndyn;
+        return m < n ? m : n;
+    }
+    return n;
+}
+
+__global__ __launch_bounds__(kScanThreads) void k_scan_reduce(const uint32_t *__restrict__ in, int64_t n,
+                                                              const int64_t *ndyn, uint32_t *__restrict__ sums) {
+    __shared__ uint32_t s_warp[kScanThreads / 32 + 1];
+    int64_t ne = dyn_len(n, ndyn);
+    int64_t base = int64_t(blockIdx.x) * kScanTile + int64_t(threadIdx.x) * kScanItems;
+    uint32_t v = 0;
+    if (int64_t(blockIdx.x) * kScanTile < ne) {
+#pragma unroll
+        for (int k = 0; k < kScanItems; ++k)
+            if (base + k < ne) v += in[base + k];
+    }
+    uint32_t total;
+    block_excl_scan(v, s_warp, total);
+    if (threadIdx.x == 0) sums[blockIdx.x] = total;
+}
+
+__global__ __launch_bounds__(kScanThreads) void k_scan_apply(const uint32_t *in, uint32_t *out, int64_t n,
+                                                             const int64_t *ndyn, const uint32_t *__restrict__ sums) {
+    __shared__ uint32_t s_warp[kScanThreads / 32 + 1];
+    int64_t ne = dyn_len(n, ndyn);
+    if (int64_t(blockIdx.x) * kScanTile >= ne) return;
+    int64_t base = int64_t(blockIdx.x) * kScanTile + int64_t(threadIdx.x) * kScanItems;
+    uint32_t v[kScanItems];
+    uint32_t s = 0;
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+        v[k] = base + k < ne ? in[base + k] : 0;
+        s += v[k];
+    }
+    uint32_t total;
+    uint32_t run = block_excl_scan(s, s_warp, total) + (sums ? sums[blockIdx.x] : 0);
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+        if (base + k < ne) out[base + k] = run;
+        run += v[k];
+    }
+}
+
+cudaError_t scan_rec(const Launch &L, const uint32_t *in, uint32_t *out, int64_t n, const int64_t *ndyn,
+                     uint32_t *tmp, int64_t tmp_cap) {
+    int64_t tiles = (n + kScanTile - 1) / kScanTile;
+    if (tiles <= 1) {
+        k_scan_apply<<<1, kScanThreads, 0, L.stream>>>(in, out, n, ndyn, nullptr);
+        ++*L.count;
+        return cudaGetLastError();
+    }
+    if (tiles > tmp_cap) return cudaErrorInvalidValue;
+    k_scan_reduce<<<unsigned(tiles), kScanThreads, 0, L.stream>>>(in, n, ndyn, tmp);
+    ++*L.count;
+    cudaError_t e = scan_rec(L, tmp, tmp, tiles, nullptr, tmp + tiles, tmp_cap - tiles);
+    if (e != cudaSuccess) return e;
+    k_scan_apply<<<unsigned(tiles), kScanThreads, 0, L.stream>>>(in, out, n, ndyn, tmp);
+    ++*L.count;
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------- collect + bbox + keys
+
+__device__ __forceinline__ bool is_star(uint8_t alive, uint8_t kind) { return alive && kind != GBH_BLACK_HOLE; }
+
+// Star flags, per-block bbox partials; alive holes get zero acceleration (bh.go:148-150).
+__global__ __launch_bounds__(kThreads) void k_flags_bbox(int64_t n, const double *__restrict__ px,
+                                                         const double *__restrict__ py, const double *__restrict__ pz,
+                                                         const uint8_t *__restrict__ kind,
+                                                         const uint8_t *__restrict__ alive, uint32_t *__restrict__ flag,
+                                                         double *__restrict__ part, double *ax, double *ay, double *az) {
+    double mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
+        uint8_t al = alive ? alive[i] : 1, kd = kind ? kind[i] : 0;
+        bool st = is_star(al, kd);
+        flag[i] = st;
+        if (st) {
+            double x = px[i], y = py[i], z = pz[i];
+            mn[0] = fmin(mn[0], x);
+            mx[0] = fmax(mx[0], x);
+            mn[1] = fmin(mn[1], y);
+            mx[1] = fmax(mx[1], y);
+            mn[2] = fmin(mn[2], z);
+            mx[2] = fmax(mx[2], z);
+        } else if (al && kd == GBH_BLACK_HOLE) {
+            ax[i] = 0;
+            ay[i] = 0;
+            az[i] = 0;
+        }
+    }
+    __shared__ double s[6][kThreads / 32];
+    int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        for (int o = 16; o > 0; o >>= 1) {
+            mn[c] = fmin(mn[c], __shfl_xor_sync(0xffffffffu, mn[c], o));
+            mx[c] = fmax(mx[c], __shfl_xor_sync(0xffffffffu, mx[c], o));
+        }
+        if (lane == 0) {
+            s[c][warp] = mn[c];
+            s[3 + c][warp] = mx[c];
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x < 6) {
+        bool isMin = threadIdx.x < 3;
+        double v = s[threadIdx.x][0];
+        for (int w = 1; w < kThreads / 32; ++w) v = isMin ? fmin(v, s[threadIdx.x][w]) : fmax(v, s[threadIdx.x][w]);
+        part[blockIdx.x * 6 + threadIdx.x] = v;
+    }
+}
+
+// Root cube (build.go:19-21): side = max(max extent * (1+1e-9), 1e-12), scale = 2^21 / side.
+__global__ void k_bbox_final(int nparts, const double *__restrict__ part, int64_t n, const uint32_t *__restrict__ scan,
+                             const uint8_t *kind, const uint8_t *alive, double theta, DevInfo *info) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    double mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (int b = 0; b < nparts; ++b)
+        for (int c = 0; c < 3; ++c) {
+            mn[c] = fmin(mn[c], part[b * 6 + c]);
+            mx[c] = fmax(mx[c], part[b * 6 + 3 + c]);
+        }
+    int64_t ns = 0;
+    if (n > 0) ns = int64_t(scan[n - 1]) + (is_star(alive ? alive[n - 1] : 1, kind ? kind[n - 1] : 0) ? 1 : 0);
+    double side = fmax(mx[0] - mn[0], fmax(mx[1] - mn[1], mx[2] - mn[2]));
+    side = fmax(side * (1 + 1e-9), 1e-12);
+    info->minx = mn[0];
+    info->miny = mn[1];
+    info->minz = mn[2];
+    info->side = side;
+    info->scale = double(1 << kMortonBits) / side;
+    info->theta = theta;
+    info->nstars = ns;
+    info->nnodes = 0;
+    info->err = 0;
+    info->err_where = 0;
+    info->work = 0;
+}
+
+// morton.go:7-15.
+__device__ __forceinline__ uint64_t spread(uint64_t v) {
+    v &= (uint64_t(1) << kMortonBits) - 1;
+    v = (v | v << 32) & 0x1f00000000ffffull;
+    v = (v | v << 16) & 0x1f0000ff0000ffull;
+    v = (v | v << 8) & 0x100f00f00f00f00full;
+    v = (v | v << 4) & 0x10c30c30c30c30c3ull;
+    v = (v | v << 2) & 0x1249249249249249ull;
+    return v;
+}
+
+// cell(), build.go:23-25: uint64(min(2^21-1, max(0, (v-lo)*scale))).
+__device__ __forceinline__ uint64_t cell(double v, double lo, double scale) {
+    double t = fmin(double((1 << kMortonBits) - 1), fmax(0.0, (v - lo) * scale));
+    return uint64_t(t);
+}
+
+// order[k] = i for the k-th star in state order; keys[k] = mortonKey(cells) (build.go:26-31).
+__global__ __launch_bounds__(kThreads) void k_compact_keys(int64_t n, const double *__restrict__ px,
+                                                           const double *__restrict__ py, const double *__restrict__ pz,
+                                                           const uint8_t *__restrict__ kind,
+                                                           const uint8_t *__restrict__ alive,
+                                                           const uint32_t *__restrict__ scan, const DevInfo *info,
+                                                           uint64_t *__restrict__ keys, int32_t *__restrict__ order) {
+    int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    if (!is_star(alive ? alive[i] : 1, kind ? kind[i] : 0)) return;
+    double sc = info->scale;
+    uint64_t k = spread(cell(px[i], info->minx, sc)) << 2 | spread(cell(py[i], info->miny, sc)) << 1 |
+                 spread(cell(pz[i], info->minz, sc));
+    uint32_t pos = scan[i];
+    keys[pos] = k;
+    order[pos] = int32_t(i);
+}
+
+// ---------------------------------------------------------------- stable LSD radix sort
+
+__global__ __launch_bounds__(kRsThreads) void k_rs_hist(const uint64_t *__restrict__ keys, const DevInfo *info,
+                                                        int shift, uint32_t ntiles, uint32_t *__restrict__ hist) {
+    __shared__ uint32_t h[kRsBins];
+    int64_t n = info->nstars;
+    h[threadIdx.x] = 0;
+    __syncthreads();
+    int64_t base = int64_t(blockIdx.x) * kRsTile;
+    if (base < n) {
+#pragma unroll
+        for (int it = 0; it < kRsItems; ++it) {
+            int64_t idx = base + it * kRsThreads + threadIdx.x;
+            if (idx < n) atomicAdd(&h[(keys[idx] >> shift) & (kRsBins - 1)], 1u);
+        }
+    }
+    __syncthreads();
+    hist[size_t(threadIdx.x) * ntiles + blockIdx.x] = h[threadIdx.x];
+}
+
+// Stable scatter of one tile. Rank of a key = keys of the same digit earlier in the tile, in
+// the order (item round, warp, lane) used to load them; offs holds the digit-major exclusive
+// scan of the tile histograms, so equal digits keep their input order across tiles too.
+__global__ __launch_bounds__(kRsThreads) void k_rs_scatter(const uint64_t *__restrict__ kin,
+                                                           const int32_t *__restrict__ vin,
+                                                           uint64_t *__restrict__ kout, int32_t *__restrict__ vout,
+                                                           const DevInfo *info, int shift, uint32_t ntiles,
+                                                           const uint32_t *__restrict__ offs) {
+    __shared__ uint32_t s_run[kRsBins];
+    __shared__ uint32_t s_goff[kRsBins];
+    __shared__ uint32_t s_w[2][kRsWarps][kRsBins];
+    int64_t n = info->nstars;
+    int64_t base = int64_t(blockIdx.x) * kRsTile;
+    if (base >= n) return;  // uniform over the block
+    int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    s_run[tid] = 0;
+    s_goff[tid] = offs[size_t(tid) * ntiles + blockIdx.x];
+#pragma unroll
+    for (int w = 0; w < kRsWarps; ++w) {
+        s_w[0][w][tid] = 0;
+        s_w[1][w][tid] = 0;
+    }
+    uint64_t k[kRsItems];
+    int32_t v[kRsItems];
+#pragma unroll
+    for (int it = 0; it < kRsItems; ++it) {
+        int64_t idx = base + it * kRsThreads + tid;
+        if (idx < n) {
+            k[it] = kin[idx];
+            v[it] = vin[idx];
+        }
+    }
+    __syncthreads();
+    const uint32_t lt = (1u << lane) - 1u;
+#pragma unroll
+    for (int it = 0; it < kRsItems; ++it) {
+        const int buf = it & 1;
+        int64_t idx = base + it * kRsThreads + tid;
+        bool valid = idx < n;
+        uint32_t d = valid ? uint32_t(k[it] >> shift) & (kRsBins - 1) : 0u;
+        uint32_t peers = __match_any_sync(0xffffffffu, valid ? d : uint32_t(kRsBins + lane));
+        uint32_t rank = __popc(peers & lt);
+        if (valid && rank == 0) s_w[buf][warp][d] = __popc(peers);
+        __syncthreads();
+        uint32_t run = s_run[tid];
+#pragma unroll
+        for (int w = 0; w < kRsWarps; ++w) {
+            uint32_t c = s_w[buf][w][tid];
+            s_w[buf][w][tid] = run;
+            run += c;
+            s_w[buf ^ 1][w][tid] = 0;  // readers of the other buffer finished before this round's first barrier
+        }
+        s_run[tid] = run;
+        __syncthreads();
+        if (valid) {
+            uint32_t pos = s_goff[d] + s_w[buf][warp][d] + rank;
+            kout[pos] = k[it];
+            vout[pos] = v[it];
+        }
+    }
+}
+
+// ---------------------------------------------------------------- sorted copies
+
+// build.go:34-41 with SourceMass (sim.go:93-98); FP32 hi/lo split for the walks.
+__global__ __launch_bounds__(kThreads) void k_gather(const DevInfo *info, const int32_t *__restrict__ order,
+                                                     const double *__restrict__ px, const double *__restrict__ py,
+                                                     const double *__restrict__ pz, const double *__restrict__ mass,
+                                                     const uint8_t *__restrict__ kind, int dm_off,
+                                                     double *__restrict__ sx, double *__restrict__ sy,
+                                                     double *__restrict__ sz, double *__restrict__ sm,
+                                                     float4 *__restrict__ st_hi, float4 *__restrict__ st_lo) {
+    int64_t k = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (k >= info->nstars) return;
+    int32_t i = order[k];
+    double x = px[i], y = py[i], z = pz[i];
+    double m = mass[i];
+    if (dm_off && kind && kind[i] == GBH_DARK_MATTER) m = 0;
+    sx[k] = x;
+    sy[k] = y;
+    sz[k] = z;
+    sm[k] = m;
+    float hx = __double2float_rn(x), hy = __double2float_rn(y), hz = __double2float_rn(z);
+    st_hi[k] = make_float4(hx, hy, hz, __double2float_rn(m));
+    st_lo[k] = make_float4(__double2float_rn(x - double(hx)), __double2float_rn(y - double(hy)),
+                           __double2float_rn(z - double(hz)), 0.f);
+}
+
+// ---------------------------------------------------------------- node set (chains)
+
+// Shallowest level at which sorted position i starts a new cell (0 for i == 0, kNoCell if its
+// key equals the previous one).
+__device__ __forceinline__ int start_level(const uint64_t *__restrict__ keys, int64_t i) {
+    if (i == 0) return 0;
+    uint64_t x = keys[i] ^ keys[i - 1];
+    if (x == 0) return kNoCell;
+    int h = 63 - __clzll(static_cast<long long>(x));
+    return kMaxLevel - h / 3;
+}
+
+__device__ __forceinline__ uint64_t prefix(uint64_t k, int L) { return L == 0 ? 0 : k >> (3 * (kMaxLevel - L)); }
+
+// First position after i whose level-L cell differs from i's (galloping, then binary search).
+__device__ int64_t cell_end(const uint64_t *__restrict__ keys, int64_t n, int64_t i, int L) {
+    if (L == 0) return n;
+    uint64_t P = prefix(keys[i], L);
+    int64_t lo = i + 1, hi = n, step = 1;
+    for (;;) {
+        int64_t probe = i + step;
+        if (probe >= n) break;
+        if (prefix(keys[probe], L) != P) {
+            hi = probe;
+            break;
+        }
+        lo = probe + 1;
+        step <<= 1;
+    }
+    while (lo < hi) {
+        int64_t mid = (lo + hi) >> 1;
+        if (prefix(keys[mid], L) == P) lo = mid + 1;
+        else hi = mid;
+    }
+    return lo;
+}
+
+// First position of i's level-L cell.
+__device__ int64_t cell_start(const uint64_t *__restrict__ keys, int64_t i, int L) {
+    if (L == 0) return 0;
+    uint64_t P = prefix(keys[i], L);
+    int64_t lo = 0, hi = i, step = 1;
+    for (;;) {
+        int64_t probe = i - step;
+        if (probe < 0) break;
+        if (prefix(keys[probe], L) != P) {
+            lo = probe + 1;
+            break;
+        }
+        hi = probe;
+        step <<= 1;
+    }
+    while (lo < hi) {
+        int64_t mid = (lo + hi) >> 1;
+        if (prefix(keys[mid], L) == P) hi = mid;
+        else lo = mid + 1;
+    }
+    return lo;
+}
+
+// Number of nodes that start at sorted position i.
+__global__ __launch_bounds__(kThreads) void k_chain_count(const uint64_t *__restrict__ keys, const DevInfo *info,
+                                                          int leaf, uint32_t *__restrict__ cnt) {
+    int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    int64_t n = info->nstars;
+    if (i >= n) return;
+    int L0 = start_level(keys, i);
+    uint32_t c = 0;
+    if (L0 <= kMaxLevel) {
+        bool exists = true;
+        if (i > 0) {  // the parent cell (level L0-1) contains i-1 and i; it splits iff it holds > leaf stars
+            int Lp = L0 - 1;
+            exists = cell_end(keys, n, i, Lp) - cell_start(keys, i, Lp) > leaf;
+        }
+        if (exists) {
+            for (int L = L0;; ++L) {
+                int64_t e = cell_end(keys, n, i, L);
+                ++c;
+                if (!(e - i > leaf && L < kMaxLevel)) break;
+            }
+        }
+    }
+    cnt[i] = c;
+}
+
+// Pre-order node arrays: parent (pre-order index), level | octant << 8 | child mask << 16,
+// child count. base = exclusive scan of cnt: the pre-order index of the first node at i.
+__global__ __launch_bounds__(kThreads) void k_chain_emit(const uint64_t *__restrict__ keys, DevInfo *info,
+                                                         const uint32_t *__restrict__ cnt,
+                                                         const uint32_t *__restrict__ base,
+                                                         int32_t *__restrict__ pre_parent,
+                                                         uint32_t *__restrict__ pre_info,
+                                                         uint32_t *__restrict__ pre_nchild) {
+    int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    int64_t n = info->nstars;
+    if (i >= n) return;
+    uint32_t c = cnt[i];
+    if (i == n - 1) info->nnodes = int64_t(base[i]) + c;
+    if (c == 0) return;
+    int L0 = start_level(keys, i);
+    int32_t parent_pre = -1;
+    if (i > 0) {
+        int Lp = L0 - 1;
+        int64_t ps = cell_start(keys, i, Lp);
+        int Lps = start_level(keys, ps);  // ps starts its chain at this level; the parent is Lp - Lps deeper
+        parent_pre = int32_t(base[ps]) + (Lp - Lps);
+    }
+    uint64_t key = keys[i];
+    uint32_t p = base[i];
+    for (uint32_t t = 0; t < c; ++t, ++p) {
+        int L = L0 + int(t);
+        uint32_t oct = L == 0 ? 0u : uint32_t(key >> (3 * (kMaxLevel - L))) & 7u;
+        uint32_t mask = 0;
+        if (t + 1 < c) {  // the node splits: occupied octants of level L+1 inside it
+            int64_t e = cell_end(keys, n, i, L);
+            int sh = 3 * (kMaxLevel - L - 1);
+            for (int64_t j = i; j < e; j = cell_end(keys, n, j, L + 1)) mask |= 1u << (uint32_t(keys[j] >> sh) & 7u);
+        }
+        pre_parent[p] = t == 0 ? parent_pre : int32_t(p) - 1;
+        pre_info[p] = uint32_t(L) | oct << 8 | mask << 16;
+        pre_nchild[p] = __popc(mask);
+    }
+}
+
+// Reference index of every node: 1 + (children allocated before its parent's block) + rank
+// among the parent's non-empty octants. child_base = exclusive scan of child counts.
+__global__ __launch_bounds__(kThreads) void k_ref_index(const DevInfo *info, const uint32_t *__restrict__ cnt,
+                                                        const uint32_t *__restrict__ base,
+                                                        const int32_t *__restrict__ pre_parent,
+                                                        const uint32_t *__restrict__ pre_info,
+                                                        const uint32_t *__restrict__ child_base,
+                                                        int32_t *__restrict__ pre_ref) {
+    int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= info->nstars) return;
+    uint32_t c = cnt[i];
+    uint32_t p = base[i];
+    for (uint32_t t = 0; t < c; ++t, ++p) {
+        int32_t pp = pre_parent[p];
+        if (pp < 0) {
+            pre_ref[p] = 0;
+            continue;
+        }
+        uint32_t oct = (pre_info[p] >> 8) & 0xffu;
+        uint32_t pmask = pre_info[pp] >> 16;
+        pre_ref[p] = int32_t(1 + child_base[pp] + __popc(pmask & ((1u << oct) - 1u)));
+    }
+}
+
+// Links and ranges of every node in the reference layout (bh.go:108-116).
+__global__ __launch_bounds__(kThreads) void k_emit_nodes(const uint64_t *__restrict__ keys, const DevInfo *info,
+                                                         const uint32_t *__restrict__ cnt,
+                                                         const uint32_t *__restrict__ base,
+                                                         const int32_t *__restrict__ pre_parent,
+                                                         const uint32_t *__restrict__ pre_info,
+                                                         const uint32_t *__restrict__ child_base,
+                                                         const int32_t *__restrict__ pre_ref, gbh_node *__restrict__ nodes,
+                                                         int32_t *__restrict__ n_parent, uint32_t *__restrict__ n_info,
+                                                         int32_t *__restrict__ n_arrive) {
+    int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    int64_t n = info->nstars;
+    if (i >= n) return;
+    uint32_t c = cnt[i];
+    uint32_t p = base[i];
+    for (uint32_t t = 0; t < c; ++t, ++p) {
+        uint32_t inf = pre_info[p];
+        int L = int(inf & 0xffu);
+        uint32_t mask = inf >> 16;
+        int64_t hi = cell_end(keys, n, i, L);
+        int32_t r = pre_ref[p];
+        gbh_node &nd = nodes[r];
+        nd.first = mask ? int32_t(1 + child_base[p]) : -1;
+        nd.next = hi == n ? -1 : pre_ref[base[hi]];
+        nd.lo = int32_t(i);
+        nd.hi = int32_t(hi);
+        int32_t pp = pre_parent[p];
+        n_parent[r] = pp < 0 ? -1 : pre_ref[pp];
+        n_info[r] = uint32_t(L) | uint32_t(__popc(mask)) << 8;
+        n_arrive[r] = 0;
+    }
+}
+
+// ---------------------------------------------------------------- moments (finish, build.go:176-217)
+
+struct Moments {
+    double x, y, z, m, qxx, qyy, qzz, qxy, qxz, qyz;
+};
+
+// quadrupole.add, build.go:329-337.
+__device__ __forceinline__ void quad_add(Moments &q, double m, double dx, double dy, double dz) {
+    double r2 = dx * dx + dy * dy + dz * dz;
+    q.qxx += m * (3 * dx * dx - r2);
+    q.qyy += m * (3 * dy * dy - r2);
+    q.qzz += m * (3 * dz * dz - r2);
+    q.qxy += m * 3 * dx * dy;
+    q.qxz += m * 3 * dx * dz;
+    q.qyz += m * 3 * dy * dz;
+}
+
+// Geometric centre and half side of the level-L cell containing key, through the same
+// rounded additions as the recursion c_child = c + offset(oct, bit) * half/2 (build.go:142-152).
+__device__ __forceinline__ void cell_center(const DevInfo &inf, uint64_t key, int L, double &cx, double &cy,
+                                            double &cz, double &half) {
+    double h = inf.side / 2;
+    cx = inf.minx + h;
+    cy = inf.miny + h;
+    cz = inf.minz + h;
+    for (int l = 1; l <= L; ++l) {
+        h = h / 2;
+        uint32_t oct = uint32_t(key >> (3 * (kMaxLevel - l))) & 7u;
+        cx = cx + ((oct >> 2 & 1u) ? h : -h);
+        cy = cy + ((oct >> 1 & 1u) ? h : -h);
+        cz = cz + ((oct & 1u) ? h : -h);
+    }
+    half = h;
+}
+
+__device__ __forceinline__ void write_node(gbh_node *nodes, PNode *pn, MNode *mn, int2 *mr, int32_t r, const Moments &q,
+                                           double crit2) {
+    gbh_node &nd = nodes[r];
+    nd.x = q.x;
+    nd.y = q.y;
+    nd.z = q.z;
+    nd.m = q.m;
+    nd.qxx = q.qxx;
+    nd.qyy = q.qyy;
+    nd.qzz = q.qzz;
+    nd.qxy = q.qxy;
+    nd.qxz = q.qxz;
+    nd.qyz = q.qyz;
+    nd.crit2 = crit2;
+    int32_t first = nd.first, next = nd.next, lo = nd.lo, hi = nd.hi;
+    float fx = __double2float_rn(q.x), fy = __double2float_rn(q.y), fz = __double2float_rn(q.z);
+    float fm = __double2float_rn(q.m), fc = __double2float_rn(crit2);
+    PNode p;
+    p.com = make_float4(fx, fy, fz, fm);
+    p.q1 = make_float4(__double2float_rn(q.qxx), __double2float_rn(q.qyy), __double2float_rn(q.qzz),
+                       __double2float_rn(q.qxy));
+    p.q2 = make_float4(__double2float_rn(q.qxz), __double2float_rn(q.qyz), fc, 0.f);
+    p.links = make_int4(first, next, lo, hi);
+    pn[r] = p;
+    MNode m;
+    m.a = make_float4(fx, fy, fz, fc);
+    m.b = make_float4(__double2float_rn(q.x - double(fx)), __double2float_rn(q.y - double(fy)),
+                      __double2float_rn(q.z - double(fz)), fm);
+    m.c = p.q1;
+    m.d = make_float4(p.q2.x, p.q2.y, __int_as_float(first), __int_as_float(next));
+    mn[r] = m;
+    mr[r] = make_int2(lo, hi);
+}
+
+__device__ __forceinline__ double crit2_of(const DevInfo &inf, const Moments &q, double cx, double cy, double cz,
+                                           double half) {
+    double delta = sqrt((q.x - cx) * (q.x - cx) + (q.y - cy) * (q.y - cy) + (q.z - cz) * (q.z - cz));
+    double crit = 2 * half / inf.theta + delta;
+    return crit * crit;
+}
+
+// Bottom-up moments: one thread per leaf; the last child to finish computes its parent.
+__global__ __launch_bounds__(kThreads) void k_upsweep(const uint64_t *__restrict__ keys, const DevInfo *info,
+                                                      const uint32_t *__restrict__ cnt, const uint32_t *__restrict__ base,
+                                                      const int32_t *__restrict__ pre_ref, const double *__restrict__ sx,
+                                                      const double *__restrict__ sy, const double *__restrict__ sz,
+                                                      const double *__restrict__ sm, gbh_node *nodes,
+                                                      const int32_t *__restrict__ n_parent,
+                                                      const uint32_t *__restrict__ n_info, int32_t *n_arrive, PNode *pn,
+                                                      MNode *mn, int2 *mr) {
+    int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= info->nstars) return;
+    uint32_t c = cnt[i];
+    if (c == 0) return;
+    const DevInfo inf = *info;
+    int32_t r = pre_ref[base[i] + c - 1];  // the last node of a chain never splits: a leaf
+    {
+        int32_t lo = nodes[r].lo, hi = nodes[r].hi;
+        int L = int(n_info[r] & 0xffu);
+        Moments q = {};
+        for (int32_t j = lo; j < hi; ++j) {
+            double mj = sm[j];
+            q.x = q.x + mj * sx[j];
+            q.y = q.y + mj * sy[j];
+            q.z = q.z + mj * sz[j];
+            q.m = q.m + mj;
+        }
+        double cx, cy, cz, half;
+        cell_center(inf, keys[lo], L, cx, cy, cz, half);
+        if (q.m > 0) {
+            q.x = q.x / q.m;
+            q.y = q.y / q.m;
+            q.z = q.z / q.m;
+        } else {
+            q.x = cx;
+            q.y = cy;
+            q.z = cz;
+        }
+        for (int32_t j = lo; j < hi; ++j) quad_add(q, sm[j], sx[j] - q.x, sy[j] - q.y, sz[j] - q.z);
+        write_node(nodes, pn, mn, mr, r, q, crit2_of(inf, q, cx, cy, cz, half));
+    }
+    int32_t cur = r;
+    for (int guard = 0; guard <= kMaxLevel + 1; ++guard) {
+        int32_t par = n_parent[cur];
+        if (par < 0) break;
+        uint32_t nch = (n_info[par] >> 8) & 0xffu;
+        __threadfence();
+        int old = atomicAdd(&n_arrive[par], 1);
+        if (old != int(nch) - 1) break;
+        __threadfence();
+        int32_t first = nodes[par].first;
+        Moments q = {};
+        for (int32_t ch = first; ch < first + int32_t(nch); ++ch) {
+            double cm = __ldcg(&nodes[ch].m);
+            q.x = q.x + cm * __ldcg(&nodes[ch].x);
+            q.y = q.y + cm * __ldcg(&nodes[ch].y);
+            q.z = q.z + cm * __ldcg(&nodes[ch].z);
+            q.m = q.m + cm;
+        }
+        int L = int(n_info[par] & 0xffu);
+        double cx, cy, cz, half;
+        cell_center(inf, keys[nodes[par].lo], L, cx, cy, cz, half);
+        if (q.m > 0) {
+            q.x = q.x / q.m;
+            q.y = q.y / q.m;
+            q.z = q.z / q.m;
+        } else {
+            q.x = cx;
+            q.y = cy;
+            q.z = cz;
+        }
+        for (int32_t ch = first; ch < first + int32_t(nch); ++ch) {
+            q.qxx = q.qxx + __ldcg(&nodes[ch].qxx);
+            q.qyy = q.qyy + __ldcg(&nodes[ch].qyy);
+            q.qzz = q.qzz + __ldcg(&nodes[ch].qzz);
+            q.qxy = q.qxy + __ldcg(&nodes[ch].qxy);
+            q.qxz = q.qxz + __ldcg(&nodes[ch].qxz);
+            q.qyz = q.qyz + __ldcg(&nodes[ch].qyz);
+            quad_add(q, __ldcg(&nodes[ch].m), __ldcg(&nodes[ch].x) - q.x, __ldcg(&nodes[ch].y) - q.y,
+                     __ldcg(&nodes[ch].z) - q.z);
+        }
+        write_node(nodes, pn, mn, mr, par, q, crit2_of(inf, q, cx, cy, cz, half));
+        cur = par;
+    }
+}
+
+// ---------------------------------------------------------------- FP64 walk (bh.go:155-204)
+
+__global__ __launch_bounds__(kThreads) void k_walk_fp64(const DevInfo *info, const gbh_node *__restrict__ nodes,
+                                                        const double *__restrict__ sx, const double *__restrict__ sy,
+                                                        const double *__restrict__ sz, const double *__restrict__ sm,
+                                                        const int32_t *__restrict__ order, double eps2, int quad,
+                                                        double *ax, double *ay, double *az, DevInfo *err_info) {
+    int64_t k = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    int64_t ns = info->nstars;
+    if (k >= ns) return;
+    int64_t nn = info->nnodes;
+    double x = sx[k], y = sy[k], z = sz[k];
+    double fax = 0, fay = 0, faz = 0;
+    int64_t steps = 0;
+    for (int32_t i = nn > 0 ? 0 : -1; i >= 0;) {
+        if (++steps > nn) {  // each node is visited at most once
+            atomicExch(&err_info->err, 1);
+            err_info->err_where = 1;
+            break;
+        }
+        const gbh_node &nd = nodes[i];
+        double dx = nd.x - x, dy = nd.y - y, dz = nd.z - z;
+        double d2 = dx * dx + dy * dy + dz * dz;
+        if (d2 >= nd.crit2) {
+            double inv = 1 / (d2 + eps2);
+            double inv3 = inv * sqrt(inv);
+            double f = nd.m * inv3;
+            if (quad) {
+                double qx = nd.qxx * dx + nd.qxy * dy + nd.qxz * dz;
+                double qy = nd.qxy * dx + nd.qyy * dy + nd.qyz * dz;
+                double qz = nd.qxz * dx + nd.qyz * dy + nd.qzz * dz;
+                double inv5 = inv3 * inv;
+                f += 2.5 * (dx * qx + dy * qy + dz * qz) * inv5 * inv;
+                fax -= qx * inv5;
+                fay -= qy * inv5;
+                faz -= qz * inv5;
+            }
+            fax += f * dx;
+            fay += f * dy;
+            faz += f * dz;
+            i = nd.next;
+            continue;
+        }
+        if (nd.first >= 0) {
+            i = nd.first;
+            continue;
+        }
+        for (int32_t j = nd.lo; j < nd.hi; ++j) {
+            if (j == k) continue;
+            double ddx = sx[j] - x, ddy = sy[j] - y, ddz = sz[j] - z;
+            double r2 = ddx * ddx + ddy * ddy + ddz * ddz + eps2;
+            double f = sm[j] / (r2 * sqrt(r2));
+            fax += f * ddx;
+            fay += f * ddy;
+            faz += f * ddz;
+        }
+        i = nd.next;
+    }
+    int32_t o = order[k];
+    ax[o] = fax;
+    ay[o] = fay;
+    az[o] = faz;
+}
+
+// ---------------------------------------------------------------- KDK (sim.go:302-343)
+
+__global__ __launch_bounds__(kThreads) void k_kick(int64_t n, double h, double *vx, double *vy, double *vz,
+                                                   const double *__restrict__ ax, const double *__restrict__ ay,
+                                                   const double *__restrict__ az) {
+    int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    vx[i] += h * ax[i];
+    vy[i] += h * ay[i];
+    vz[i] += h * az[i];
+}
+
+__global__ __launch_bounds__(kThreads) void k_kick_drift(int64_t n, double h, double dt, double *px, double *py,
+                                                         double *pz, double *vx, double *vy, double *vz,
+                                                         const double *__restrict__ ax, const double *__restrict__ ay,
+                                                         const double *__restrict__ az) {
+    int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double x = vx[i] + h * ax[i], y = vy[i] + h * ay[i], z = vz[i] + h * az[i];
+    vx[i] = x;
+    vy[i] = y;
+    vz[i] = z;
+    px[i] += dt * x;
+    py[i] += dt * y;
+    pz[i] += dt * z;
+}
+
+// ---------------------------------------------------------------- direct sum (direct.go:18-48)
+
+constexpr int kDirThreads = 128;
+
+__global__ __launch_bounds__(kDirThreads) void k_direct_fp64(int64_t n, const double *__restrict__ px,
+                                                             const double *__restrict__ py, const double *__restrict__ pz,
+                                                             const double *__restrict__ mass,
+                                                             const uint8_t *__restrict__ kind, double eps2, int dm_off,
+                                                             const int64_t *__restrict__ targets, int64_t ntargets,
+                                                             double *ax, double *ay, double *az) {
+    __shared__ double s_x[kDirThreads], s_y[kDirThreads], s_z[kDirThreads], s_m[kDirThreads];
+    __shared__ uint8_t s_skip[kDirThreads];
+    int64_t q = int64_t(blockIdx.x) * kDirThreads + threadIdx.x;
+    bool valid = q < ntargets;
+    int64_t i = valid ? (targets ? targets[q] : q) : 0;
+    double xi = px[i], yi = py[i], zi = pz[i];
+    double fax = 0, fay = 0, faz = 0;
+    for (int64_t j0 = 0; j0 < n; j0 += kDirThreads) {
+        int64_t j = j0 + threadIdx.x;
+        if (j < n) {
+            uint8_t kd = kind ? kind[j] : 0;
+            s_x[threadIdx.x] = px[j];
+            s_y[threadIdx.x] = py[j];
+            s_z[threadIdx.x] = pz[j];
+            s_m[threadIdx.x] = mass[j];
+            s_skip[threadIdx.x] = kd == GBH_BLACK_HOLE || (dm_off && kd == GBH_DARK_MATTER);
+        }
+        __syncthreads();
+        int64_t cnt = n - j0 < kDirThreads ? n - j0 : kDirThreads;
+        for (int t = 0; t < cnt; ++t) {
+            if (j0 + t == i || s_skip[t]) continue;
+            double dx = s_x[t] - xi, dy = s_y[t] - yi, dz = s_z[t] - zi;
+            double re2 = dx * dx + dy * dy + dz * dz + eps2;
+            double f = s_m[t] / (re2 * sqrt(re2));
+            fax += f * dx;
+            fay += f * dy;
+            faz += f * dz;
+        }
+        __syncthreads();
+    }
+    if (!valid) return;
+    bool hole = kind && kind[i] == GBH_BLACK_HOLE;
+    ax[q] = hole ? 0 : fax;
+    ay[q] = hole ? 0 : fay;
+    az[q] = hole ? 0 : faz;
+}
+
+// ---------------------------------------------------------------- potential (potential.go:16-81)
+
+__device__ __forceinline__ double schwarzschild(double m, double c) { return c <= 0 ? 0 : 2 * m / (c * c); }
+
+__device__ __forceinline__ double pair_rs(uint8_t ki, double mi, uint8_t kj, double mj, double c) {
+    bool hi = ki == GBH_BLACK_HOLE, hj = kj == GBH_BLACK_HOLE;
+    if (c <= 0 || hi == hj) return 0;
+    return hi ? schwarzschild(mi, c) : schwarzschild(mj, c);
+}
+
+__device__ __forceinline__ double pair_potential(double mi, double mj, double r2, double eps2, double rs) {
+    double re = sqrt(r2 + eps2);
+    if (rs == 0) return -mi * mj / re;
+    if (re >= 1.5 * rs) return -mi * mj / (re - rs);
+    return mi * mj * (-2 / rs + 4 / (rs * rs) * (re - 1.5 * rs));
+}
+
+// holePotential, potential.go:84-96.
+__device__ double hole_potential(int64_t i, const double *px, const double *py, const double *pz, const double *mass,
+                                 const uint8_t *kind, const int32_t *holes, int32_t nholes, double eps2, double c,
+                                 int dm_off) {
+    double x = px[i], y = py[i], z = pz[i], u = 0;
+    uint8_t ki = kind ? kind[i] : 0;
+    double smi = (dm_off && ki == GBH_DARK_MATTER) ? 0.0 : mass[i];
+    for (int32_t t = 0; t < nholes; ++t) {
+        int32_t h = holes[t];
+        if (h == i) continue;
+        double dx = px[h] - x, dy = py[h] - y, dz = pz[h] - z;
+        double rs = pair_rs(ki, mass[i], GBH_BLACK_HOLE, mass[h], c);
+        u += pair_potential(smi, mass[h], dx * dx + dy * dy + dz * dz, eps2, rs);
+    }
+    return u;
+}
+
+// Per sorted star: sm[k] * walkPotential(k) - holePotential(order[k]); block partial sums.
+__global__ __launch_bounds__(kThreads) void k_potential_walk(const DevInfo *info, const gbh_node *__restrict__ nodes,
+                                                             const double *__restrict__ sx, const double *__restrict__ sy,
+                                                             const double *__restrict__ sz, const double *__restrict__ sm,
+                                                             const int32_t *__restrict__ order, const double *px,
+                                                             const double *py, const double *pz, const double *mass,
+                                                             const uint8_t *kind, const int32_t *holes, int32_t nholes,
+                                                             double eps2, double c, int dm_off, int quad, double *part,
+                                                             DevInfo *err_info) {
+    int64_t k = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    int64_t ns = info->nstars, nn = info->nnodes;
+    double v = 0;
+    if (k < ns) {
+        double x = sx[k], y = sy[k], z = sz[k], psi = 0;
+        int64_t steps = 0;
+        for (int32_t i = nn > 0 ? 0 : -1; i >= 0;) {
+            if (++steps > nn) {
+                atomicExch(&err_info->err, 1);
+                err_info->err_where = 2;
+                break;
+            }
+            const gbh_node &nd = nodes[i];
+            double dx = nd.x - x, dy = nd.y - y, dz = nd.z - z;
+            double d2 = dx * dx + dy * dy + dz * dz;
+            if (d2 >= nd.crit2) {
+                double inv = 1 / (d2 + eps2);
+                psi += nd.m * sqrt(inv);
+                if (quad) {
+                    double dqd = nd.qxx * dx * dx + nd.qyy * dy * dy + nd.qzz * dz * dz +
+                                 2 * (nd.qxy * dx * dy + nd.qxz * dx * dz + nd.qyz * dy * dz);
+                    psi += 0.5 * dqd * inv * inv * sqrt(inv);
+                }
+                i = nd.next;
+                continue;
+            }
+            if (nd.first >= 0) {
+                i = nd.first;
+                continue;
+            }
+            for (int32_t j = nd.lo; j < nd.hi; ++j) {
+                if (j == k) continue;
+                double ddx = sx[j] - x, ddy = sy[j] - y, ddz = sz[j] - z;
+                psi += sm[j] / sqrt(ddx * ddx + ddy * ddy + ddz * ddz + eps2);
+            }
+            i = nd.next;
+        }
+        v = sm[k] * psi - (nholes ? hole_potential(order[k], px, py, pz, mass, kind, holes, nholes, eps2, c, dm_off) : 0.0);
+    }
+    // Deterministic block sum (tree order over threads).
+    __shared__ double s[kThreads];
+    s[threadIdx.x] = v;
+    __syncthreads();
+    for (int o = kThreads / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) s[threadIdx.x] += s[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) part[blockIdx.x] = s[0];
+}
+
+// Sum of the block parts plus the hole terms (potential.go:31-41); U = -sum / 2.
+__global__ void k_potential_final(int64_t nparts, const double *part, const DevInfo *info,
+                                  const double *__restrict__ sx, const double *__restrict__ sy,
+                                  const double *__restrict__ sz, const double *__restrict__ sm, const double *px,
+                                  const double *py, const double *pz, const double *mass, const uint8_t *kind,
+                                  const int32_t *holes, int32_t nholes, double eps2, double c, int dm_off, double *u) {
+    __shared__ double s[kThreads];
+    double v = 0;
+    for (int64_t b = threadIdx.x; b < nparts; b += blockDim.x) v += part[b];
+    int64_t ns = info->nstars;
+    for (int32_t t = 0; t < nholes; ++t) {
+        int32_t i = holes[t];
+        double x = px[i], y = py[i], z = pz[i];
+        double rs = schwarzschild(mass[i], c);
+        for (int64_t k = threadIdx.x; k < ns; k += blockDim.x) {
+            double dx = sx[k] - x, dy = sy[k] - y, dz = sz[k] - z;
+            v -= pair_potential(mass[i], sm[k], dx * dx + dy * dy + dz * dz, eps2, rs);
+        }
+        if (threadIdx.x == 0) v -= hole_potential(i, px, py, pz, mass, kind, holes, nholes, eps2, c, dm_off);
+    }
+    s[threadIdx.x] = v;
+    __syncthreads();
+    for (int o = kThreads / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) s[threadIdx.x] += s[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *u = -s[0] / 2;
+}
+
+constexpr int kFlagBlocksMax = 1024;
+
+}  // namespace
+
+int64_t scan_tmp_size(int64_t n) {
+    int64_t total = 0;
+    for (int64_t t = (n + kScanTile - 1) / kScanTile; t > 1; t = (t + kScanTile - 1) / kScanTile) total += t;
+    return total + 64;
+}
+
+cudaError_t scan_u32(const Launch &L, const uint32_t *in, uint32_t *out, int64_t n, uint32_t *tmp, int64_t tmp_cap) {
+    return scan_rec(L, in, out, n, nullptr, tmp, tmp_cap);
+}
+
+static cudaError_t scan_dyn(const Launch &L, const uint32_t *in, uint32_t *out, int64_t n, const int64_t *ndyn,
+                            uint32_t *tmp, int64_t tmp_cap) {
+    return scan_rec(L, in, out, n, ndyn, tmp, tmp_cap);
+}
+
+void tree_free(TreeBufs &b) {
+    void *ptrs[] = {b.flag, b.bbox_part, b.keys, b.keys_alt, b.order, b.order_alt, b.hist, b.sx, b.sy, b.sz, b.sm,
+                    b.st_hi, b.st_lo, b.chain_cnt, b.pre_parent, b.pre_info, b.pre_nchild, b.pre_ref, b.nodes,
+                    b.n_parent, b.n_info, b.n_arrive, b.pnodes, b.mnodes, b.mrange, b.scan_tmp, b.info};
+    for (void *p : ptrs)
+        if (p) cudaFree(p);
+    b = TreeBufs{};
+}
+
+// Worst-case node count: at most n leaves, and at each of the 22 levels at most n/(leaf+1)
+// cells hold more than leaf stars (only those have children).
+static int64_t node_capacity(int64_t n, int leaf) { return n + 22 * (n / (leaf + 1) + 1) + 1; }
+
+cudaError_t tree_alloc(TreeBufs &b, int64_t n, int leaf) {
+    int64_t need_nodes = node_capacity(n, leaf);
+    if (n <= b.cap_n && need_nodes <= b.cap_nodes) return cudaSuccess;
+    int64_t cn = n > b.cap_n ? n + n / 4 : b.cap_n;  // grow by 1.25x like gpuBuffers.ensure (gpu_darwin.go:164-177)
+    int64_t cnodes = need_nodes > b.cap_nodes ? node_capacity(cn, leaf) : b.cap_nodes;
+    if (cnodes < need_nodes) cnodes = need_nodes;
+    tree_free(b);
+    cn = cn < 1 ? 1 : cn;
+    int64_t rs_tiles = (cn + kRsTile - 1) / kRsTile;
+    int64_t scan_cap = scan_tmp_size(cnodes > cn * 1 ? cnodes : cn);
+    int64_t scan_cap2 = scan_tmp_size(rs_tiles * kRsBins);
+    if (scan_cap2 > scan_cap) scan_cap = scan_cap2;
+    b.scan_tmp_cap = scan_cap;
+    cudaError_t e = cudaSuccess;
+#define GBH_ALLOC(ptr, count)                                                     \
+    do {                                                                          \
+        if (e == cudaSuccess) e = cudaMalloc(&(ptr), sizeof(*(ptr)) * size_t(count)); \
+    } while (0)
+    GBH_ALLOC(b.flag, cn);
+    GBH_ALLOC(b.bbox_part, kFlagBlocksMax * 6);
+    GBH_ALLOC(b.keys, cn);
+    GBH_ALLOC(b.keys_alt, cn);
+    GBH_ALLOC(b.order, cn);
+    GBH_ALLOC(b.order_alt, cn);
+    GBH_ALLOC(b.hist, rs_tiles * kRsBins);
+    GBH_ALLOC(b.sx, cn);
+    GBH_ALLOC(b.sy, cn);
+    GBH_ALLOC(b.sz, cn);
+    GBH_ALLOC(b.sm, cn);
+    GBH_ALLOC(b.st_hi, cn);
+    GBH_ALLOC(b.st_lo, cn);
+    GBH_ALLOC(b.chain_cnt, cn * 2);  // counts, then their scan
+    GBH_ALLOC(b.pre_parent, cnodes);
+    GBH_ALLOC(b.pre_info, cnodes);
+    GBH_ALLOC(b.pre_nchild, cnodes);
+    GBH_ALLOC(b.pre_ref, cnodes);
+    GBH_ALLOC(b.nodes, cnodes);
+    GBH_ALLOC(b.n_parent, cnodes);
+    GBH_ALLOC(b.n_info, cnodes);
+    GBH_ALLOC(b.n_arrive, cnodes);
+    GBH_ALLOC(b.pnodes, cnodes);
+    GBH_ALLOC(b.mnodes, cnodes);
+    GBH_ALLOC(b.mrange, cnodes);
+    GBH_ALLOC(b.scan_tmp, scan_cap);
+    GBH_ALLOC(b.info, 1);
+#undef GBH_ALLOC
+    if (e != cudaSuccess) {
+        tree_free(b);
+        return e;
+    }
+    b.cap_n = cn;
+    b.cap_nodes = cnodes;
+    return cudaMemset(b.info, 0, sizeof(DevInfo));
+}
+
+#define GBH_LAUNCH_CHECK()                         \
+    do {                                           \
+        ++*L.count;                                \
+        cudaError_t e_ = cudaGetLastError();       \
+        if (e_ != cudaSuccess) return e_;          \
+    } while (0)
+
+cudaError_t tree_build(const Launch &L, TreeBufs &b, int64_t n, const double *px, const double *py, const double *pz,
+                       const double *mass, const uint8_t *kind, const uint8_t *alive, double *ax, double *ay,
+                       double *az, double theta, int leaf, int dm_off) {
+    cudaStream_t s = L.stream;
+    const int64_t cap = b.cap_n;
+    // collect + bbox (build.go:62-113)
+    unsigned fb = blocks_for(n, kThreads);
+    if (fb > unsigned(kFlagBlocksMax)) fb = kFlagBlocksMax;
+    k_flags_bbox<<<fb, kThreads, 0, s>>>(n, px, py, pz, kind, alive, b.flag, b.bbox_part, ax, ay, az);
+    GBH_LAUNCH_CHECK();
+    cudaError_t e = scan_u32(L, b.flag, b.flag, n, b.scan_tmp, b.scan_tmp_cap);
+    if (e != cudaSuccess) return e;
+    k_bbox_final<<<1, 32, 0, s>>>(int(fb), b.bbox_part, n, b.flag, kind, alive, theta, b.info);
+    GBH_LAUNCH_CHECK();
+    k_compact_keys<<<blocks_for(n, kThreads), kThreads, 0, s>>>(n, px, py, pz, kind, alive, b.flag, b.info, b.keys,
+                                                                b.order);
+    GBH_LAUNCH_CHECK();
+    // radix sort (morton.go:25-49): 8 stable passes, ping-pong, result back in keys/order
+    const uint32_t ntiles = uint32_t((cap + kRsTile - 1) / kRsTile);
+    uint64_t *kin = b.keys, *kout = b.keys_alt;
+    int32_t *vin = b.order, *vout = b.order_alt;
+    for (int shift = 0; shift < 64; shift += 8) {
+        k_rs_hist<<<ntiles, kRsThreads, 0, s>>>(kin, b.info, shift, ntiles, b.hist);
+        GBH_LAUNCH_CHECK();
+        e = scan_u32(L, b.hist, b.hist, int64_t(ntiles) * kRsBins, b.scan_tmp, b.scan_tmp_cap);
+        if (e != cudaSuccess) return e;
+        k_rs_scatter<<<ntiles, kRsThreads, 0, s>>>(kin, vin, kout, vout, b.info, shift, ntiles, b.hist);
+        GBH_LAUNCH_CHECK();
+        uint64_t *tk = kin;
+        kin = kout;
+        kout = tk;
+        int32_t *tv = vin;
+        vin = vout;
+        vout = tv;
+    }
+    // sorted copies (build.go:34-41)
+    const unsigned nb = blocks_for(cap, kThreads);
+    k_gather<<<nb, kThreads, 0, s>>>(b.info, b.order, px, py, pz, mass, kind, dm_off, b.sx, b.sy, b.sz, b.sm, b.st_hi,
+                                     b.st_lo);
+    GBH_LAUNCH_CHECK();
+    // node set
+    uint32_t *cnt = b.chain_cnt, *base = b.chain_cnt + cap;
+    k_chain_count<<<nb, kThreads, 0, s>>>(b.keys, b.info, leaf, cnt);
+    GBH_LAUNCH_CHECK();
+    e = scan_dyn(L, cnt, base, cap, &b.info->nstars, b.scan_tmp, b.scan_tmp_cap);
+    if (e != cudaSuccess) return e;
+    k_chain_emit<<<nb, kThreads, 0, s>>>(b.keys, b.info, cnt, base, b.pre_parent, b.pre_info, b.pre_nchild);
+    GBH_LAUNCH_CHECK();
+    e = scan_dyn(L, b.pre_nchild, b.pre_nchild, b.cap_nodes, &b.info->nnodes, b.scan_tmp, b.scan_tmp_cap);
+    if (e != cudaSuccess) return e;
+    k_ref_index<<<nb, kThreads, 0, s>>>(b.info, cnt, base, b.pre_parent, b.pre_info, b.pre_nchild, b.pre_ref);
+    GBH_LAUNCH_CHECK();
+    k_emit_nodes<<<nb, kThreads, 0, s>>>(b.keys, b.info, cnt, base, b.pre_parent, b.pre_info, b.pre_nchild, b.pre_ref,
+                                         b.nodes, b.n_parent, b.n_info, b.n_arrive);
+    GBH_LAUNCH_CHECK();
+    k_upsweep<<<nb, kThreads, 0, s>>>(b.keys, b.info, cnt, base, b.pre_ref, b.sx, b.sy, b.sz, b.sm, b.nodes,
+                                      b.n_parent, b.n_info, b.n_arrive, b.pnodes, b.mnodes, b.mrange);
+    GBH_LAUNCH_CHECK();
+    return cudaSuccess;
+}
+
+cudaError_t walk_fp64(const Launch &L, const TreeBufs &b, int64_t n, double eps2, int quad, double *ax, double *ay,
+                      double *az) {
+    (void)n;
+    k_walk_fp64<<<blocks_for(b.cap_n, kThreads), kThreads, 0, L.stream>>>(b.info, b.nodes, b.sx, b.sy, b.sz, b.sm,
+                                                                           b.order, eps2, quad, ax, ay, az, b.info);
+    GBH_LAUNCH_CHECK();
+    return cudaSuccess;
+}
+
+cudaError_t kick(const Launch &L, int64_t n, double h, double *vx, double *vy, double *vz, const double *ax,
+                 const double *ay, const double *az) {
+    if (n == 0) return cudaSuccess;
+    k_kick<<<blocks_for(n, kThreads), kThreads, 0, L.stream>>>(n, h, vx, vy, vz, ax, ay, az);
+    GBH_LAUNCH_CHECK();
+    return cudaSuccess;
+}
+
+cudaError_t kick_drift(const Launch &L, int64_t n, double h, double dt, double *px, double *py, double *pz, double *vx,
+                       double *vy, double *vz, const double *ax, const double *ay, const double *az) {
+    if (n == 0) return cudaSuccess;
+    k_kick_drift<<<blocks_for(n, kThreads), kThreads, 0, L.stream>>>(n, h, dt, px, py, pz, vx, vy, vz, ax, ay, az);
+    GBH_LAUNCH_CHECK();
+    return cudaSuccess;
+}
+
+cudaError_t direct_fp64(const Launch &L, int64_t n, const double *px, const double *py, const double *pz,
+                        const double *mass, const uint8_t *kind, double eps2, int dm_off, const int64_t *targets,
+                        int64_t ntargets, double *ax, double *ay, double *az) {
+    if (ntargets == 0 || n == 0) return cudaSuccess;
+    k_direct_fp64<<<blocks_for(ntargets, kDirThreads), kDirThreads, 0, L.stream>>>(n, px, py, pz, mass, kind, eps2,
+                                                                                  dm_off, targets, ntargets, ax, ay, az);
+    GBH_LAUNCH_CHECK();
+    return cudaSuccess;
+}
+
+cudaError_t potential_fp64(const Launch &L, const TreeBufs &b, int64_t n, const double *px, const double *py,
+                           const double *pz, const double *mass, const uint8_t *kind, const uint8_t *alive,
+                           const int32_t *holes, int32_t nholes, double eps2, double c, int dm_off, int quad,
+                           double *part, double *u_dev) {
+    (void)n;
+    (void)alive;
+    unsigned nb = blocks_for(b.cap_n, kThreads);
+    k_potential_walk<<<nb, kThreads, 0, L.stream>>>(b.info, b.nodes, b.sx, b.sy, b.sz, b.sm, b.order, px, py, pz, mass,
+                                                    kind, holes, nholes, eps2, c, dm_off, quad, part, b.info);
+    GBH_LAUNCH_CHECK();
+    k_potential_final<<<1, kThreads, 0, L.stream>>>(nb, part, b.info, b.sx, b.sy, b.sz, b.sm, px, py, pz, mass, kind,
+                                                    holes, nholes, eps2, c, dm_off, u_dev);
+    GBH_LAUNCH_CHECK();
+    return cudaSuccess;
+}
+
+}  // namespace gbh

@@ -1,0 +1,261 @@
+// walk.cu — the FP32 tree walks (compiled with FMA contraction and fast FP32 division/sqrt).
+//
+// walk_plain: one thread per sorted star, the CUDA twin of the Metal kernel
+//   internal/sim/bh/gpu_darwin.go:76-118 (all FP32, uncompensated, per-star opening).
+// walk_mixed: one warp per group of 32 consecutive Morton-sorted stars walking the skip-pointer
+//   tree in lockstep. A node is opened when any star of the group would open it under the
+//   reference criterion d2 < crit2 (bh.go:165), so every star sees each accepted node exactly
+//   where the reference would accept it or deeper. Positions enter as FP32 offsets from the
+//   group's anchor star, formed from FP64 positions split into hi + lo FP32 parts, so a
+//   separation is as precise as the offsets themselves however far the system is from the
+//   origin. Each star accumulates in FP32 blocks of 32 interactions folded into a Kahan sum.
+#include <cuda_runtime.h>
+
+#include "gbh_internal.cuh"
+
+namespace gbh {
+
+namespace {
+
+constexpr unsigned kFull = 0xffffffffu;
+constexpr int kPlainThreads = 256;
+constexpr int kMixedThreads = 128;
+
+inline unsigned blocks_for(int64_t n, int threads) {
+    int64_t b = (n + threads - 1) / threads;
+    return unsigned(b < 1 ? 1 : b);
+}
+
+__device__ __forceinline__ void set_err(DevInfo *info, int where) {
+    atomicExch(&info->err, 1);
+    info->err_where = where;
+}
+
+// gpu_darwin.go:84-117, with the same float4 node and star records.
+__global__ __launch_bounds__(kPlainThreads) void k_walk_plain(const DevInfo *info, const PNode *__restrict__ nodes,
+                                                              const float4 *__restrict__ stars,
+                                                              const int32_t *__restrict__ order, float eps2,
+                                                              double *ax, double *ay, double *az, DevInfo *err_info) {
+    int64_t k = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    int64_t ns = info->nstars;
+    if (k >= ns) return;
+    int64_t nn = info->nnodes;
+    float4 p = stars[k];
+    float fax = 0.f, fay = 0.f, faz = 0.f;
+    int64_t steps = 0;
+    int i = nn > 0 ? 0 : -1;
+    while (i >= 0) {
+        if (++steps > nn) {
+            set_err(err_info, 3);
+            break;
+        }
+        const PNode nd = nodes[i];
+        float dx = nd.com.x - p.x, dy = nd.com.y - p.y, dz = nd.com.z - p.z;
+        float d2 = dx * dx + dy * dy + dz * dz;
+        if (d2 >= nd.q2.z) {
+            float inv = 1.0f / (d2 + eps2);
+            float inv3 = inv * sqrtf(inv);
+            float qx = nd.q1.x * dx + nd.q1.w * dy + nd.q2.x * dz;
+            float qy = nd.q1.w * dx + nd.q1.y * dy + nd.q2.y * dz;
+            float qz = nd.q2.x * dx + nd.q2.y * dy + nd.q1.z * dz;
+            float inv5 = inv3 * inv;
+            float f = nd.com.w * inv3 + 2.5f * (dx * qx + dy * qy + dz * qz) * inv5 * inv;
+            fax += dx * f - qx * inv5;
+            fay += dy * f - qy * inv5;
+            faz += dz * f - qz * inv5;
+            i = nd.links.y;
+            continue;
+        }
+        if (nd.links.x >= 0) {
+            i = nd.links.x;
+            continue;
+        }
+        for (int j = nd.links.z; j < nd.links.w; ++j) {
+            if (j == int(k)) continue;
+            float4 s = stars[j];
+            float ddx = s.x - p.x, ddy = s.y - p.y, ddz = s.z - p.z;
+            float ir = rsqrtf(ddx * ddx + ddy * ddy + ddz * ddz + eps2);
+            float f = s.w * ir * ir * ir;
+            fax += ddx * f;
+            fay += ddy * f;
+            faz += ddz * f;
+        }
+        i = nd.links.y;
+    }
+    int32_t o = order[k];
+    ax[o] = fax;
+    ay[o] = fay;
+    az[o] = faz;
+}
+
+// Kahan fold of a block partial into the running sum (s, c): true sum = s - c.
+__device__ __forceinline__ void kahan_fold(float &s, float &c, float &part) {
+    float y = part - c;
+    float t = s + y;
+    c = (t - s) - y;
+    s = t;
+    part = 0.f;
+}
+
+template <bool kQuad, bool kSoft>
+__global__ __launch_bounds__(kMixedThreads) void k_walk_mixed(const DevInfo *info, const MNode *__restrict__ nodes,
+                                                              const int2 *__restrict__ ranges,
+                                                              const float4 *__restrict__ st_hi,
+                                                              const float4 *__restrict__ st_lo,
+                                                              const int32_t *__restrict__ order, float eps2,
+                                                              double *ax, double *ay, double *az, DevInfo *err_info) {
+    const int lane = threadIdx.x & 31;
+    const int64_t ns = info->nstars;
+    const int64_t nn = info->nnodes;
+    const int64_t group = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    const int64_t base = group * 32;
+    if (base >= ns) return;  // uniform over the warp
+    const int64_t k = base + lane;
+    const bool valid = k < ns;
+    const int64_t kk = valid ? k : base;
+    const float4 h = st_hi[kk], l = st_lo[kk];
+    const float gx = __shfl_sync(kFull, h.x, 0), gy = __shfl_sync(kFull, h.y, 0), gz = __shfl_sync(kFull, h.z, 0);
+    const float tx = (h.x - gx) + l.x, ty = (h.y - gy) + l.y, tz = (h.z - gz) + l.z;
+
+    float sx = 0.f, sy = 0.f, sz = 0.f, cx = 0.f, cy = 0.f, cz = 0.f;  // Kahan sums
+    float px = 0.f, py = 0.f, pz = 0.f;                                // block partials
+    int nint = 0;
+    int64_t steps = 0;
+    int i = nn > 0 ? 0 : -1;
+    while (i >= 0) {
+        if (++steps > nn) {
+            if (lane == 0) set_err(err_info, 4);
+            break;
+        }
+        const MNode nd = nodes[i];
+        const float dx = ((nd.a.x - gx) + nd.b.x) - tx;
+        const float dy = ((nd.a.y - gy) + nd.b.y) - ty;
+        const float dz = ((nd.a.z - gz) + nd.b.z) - tz;
+        const float d2 = dx * dx + dy * dy + dz * dz;
+        const bool open = __any_sync(kFull, d2 < nd.a.w);
+        const int first = __float_as_int(nd.d.z), next = __float_as_int(nd.d.w);
+        if (!open) {
+            const float ir = rsqrtf(d2 + eps2);
+            const float ir2 = ir * ir;
+            const float ir3 = ir * ir2;
+            float f = nd.b.w * ir3;
+            if (kQuad) {
+                const float qx = nd.c.x * dx + nd.c.w * dy + nd.d.x * dz;
+                const float qy = nd.c.w * dx + nd.c.y * dy + nd.d.y * dz;
+                const float qz = nd.d.x * dx + nd.d.y * dy + nd.c.z * dz;
+                const float ir5 = ir3 * ir2;
+                f += 2.5f * (dx * qx + dy * qy + dz * qz) * ir5 * ir2;
+                px -= qx * ir5;
+                py -= qy * ir5;
+                pz -= qz * ir5;
+            }
+            px += f * dx;
+            py += f * dy;
+            pz += f * dz;
+            if (++nint == 32) {
+                kahan_fold(sx, cx, px);
+                kahan_fold(sy, cy, py);
+                kahan_fold(sz, cz, pz);
+                nint = 0;
+            }
+            i = next;
+            continue;
+        }
+        if (first >= 0) {
+            i = first;
+            continue;
+        }
+        const int2 r = ranges[i];
+        for (int j = r.x; j < r.y; ++j) {
+            const float4 sh = st_hi[j], sl = st_lo[j];
+            const float ex = ((sh.x - gx) + sl.x) - tx;
+            const float ey = ((sh.y - gy) + sl.y) - ty;
+            const float ez = ((sh.z - gz) + sl.z) - tz;
+            const float r2 = ex * ex + ey * ey + ez * ez + eps2;
+            // The star itself gives ex = ey = ez = 0 exactly; with eps2 > 0 that adds 0, as
+            // skipping j == self does (bh.go:191-193). Without softening r2 = 0 is masked.
+            const float ir = kSoft ? rsqrtf(r2) : (r2 > 0.f ? rsqrtf(r2) : 0.f);
+            const float f = sh.w * ir * ir * ir;
+            px += f * ex;
+            py += f * ey;
+            pz += f * ez;
+            if (++nint == 32) {
+                kahan_fold(sx, cx, px);
+                kahan_fold(sy, cy, py);
+                kahan_fold(sz, cz, pz);
+                nint = 0;
+            }
+        }
+        i = next;
+    }
+    kahan_fold(sx, cx, px);
+    kahan_fold(sy, cy, py);
+    kahan_fold(sz, cz, pz);
+    if (valid) {
+        int32_t o = order[k];
+        ax[o] = double(sx) - double(cx);
+        ay[o] = double(sy) - double(cy);
+        az[o] = double(sz) - double(cz);
+    }
+}
+
+// Register-resident FMA chains: 8 independent chains per thread.
+__global__ __launch_bounds__(256) void k_fma_probe(int iters, float *out) {
+    float a0 = threadIdx.x * 1e-7f, a1 = a0 + 1e-7f, a2 = a0 + 2e-7f, a3 = a0 + 3e-7f;
+    float a4 = a0 + 4e-7f, a5 = a0 + 5e-7f, a6 = a0 + 6e-7f, a7 = a0 + 7e-7f;
+    const float m = 0.999999f, c = 1e-7f;
+    for (int it = 0; it < iters; ++it) {
+#pragma unroll
+        for (int u = 0; u < 16; ++u) {
+            a0 = fmaf(a0, m, c);
+            a1 = fmaf(a1, m, c);
+            a2 = fmaf(a2, m, c);
+            a3 = fmaf(a3, m, c);
+            a4 = fmaf(a4, m, c);
+            a5 = fmaf(a5, m, c);
+            a6 = fmaf(a6, m, c);
+            a7 = fmaf(a7, m, c);
+        }
+    }
+    float s = a0 + a1 + a2 + a3 + a4 + a5 + a6 + a7;
+    if (s == 12345.678f) out[blockIdx.x] = s;  // never true; keeps the chains live
+}
+
+}  // namespace
+
+cudaError_t walk_plain(const Launch &L, const TreeBufs &b, int64_t nstars_cap, float eps2, double *ax, double *ay,
+                       double *az) {
+    k_walk_plain<<<blocks_for(nstars_cap, kPlainThreads), kPlainThreads, 0, L.stream>>>(
+        b.info, b.pnodes, b.st_hi, b.order, eps2, ax, ay, az, b.info);
+    ++*L.count;
+    return cudaGetLastError();
+}
+
+cudaError_t walk_mixed(const Launch &L, const TreeBufs &b, int64_t nstars_cap, float eps2, int quad, double *ax,
+                       double *ay, double *az) {
+    int64_t groups = (nstars_cap + 31) / 32;
+    unsigned nb = blocks_for(groups * 32, kMixedThreads);
+    bool soft = eps2 > 0.f;
+    if (quad && soft)
+        k_walk_mixed<true, true><<<nb, kMixedThreads, 0, L.stream>>>(b.info, b.mnodes, b.mrange, b.st_hi, b.st_lo,
+                                                                     b.order, eps2, ax, ay, az, b.info);
+    else if (quad)
+        k_walk_mixed<true, false><<<nb, kMixedThreads, 0, L.stream>>>(b.info, b.mnodes, b.mrange, b.st_hi, b.st_lo,
+                                                                      b.order, eps2, ax, ay, az, b.info);
+    else if (soft)
+        k_walk_mixed<false, true><<<nb, kMixedThreads, 0, L.stream>>>(b.info, b.mnodes, b.mrange, b.st_hi, b.st_lo,
+                                                                      b.order, eps2, ax, ay, az, b.info);
+    else
+        k_walk_mixed<false, false><<<nb, kMixedThreads, 0, L.stream>>>(b.info, b.mnodes, b.mrange, b.st_hi, b.st_lo,
+                                                                       b.order, eps2, ax, ay, az, b.info);
+    ++*L.count;
+    return cudaGetLastError();
+}
+
+cudaError_t fp32_fma_probe(const Launch &L, int blocks, int iters, float *out) {
+    k_fma_probe<<<blocks, 256, 0, L.stream>>>(iters, out);
+    ++*L.count;
+    return cudaGetLastError();
+}
+
+}  // namespace gbh

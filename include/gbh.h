@@ -1,0 +1,193 @@
+/*
+ * gbh.h — C-ABI of the GB300 Barnes-Hut gravity step (libgbh.so).
+ *
+ * This is the drop-in boundary for gravitas' force and step path. The
+ * reference binds its force solver through the Go interface
+ *     type Solver interface { Accelerations(s *State, p Params) }
+ * (internal/sim/sim.go:100-105), implemented by bh.Solver
+ * (internal/sim/bh/bh.go:77-151), and reaches native code through cgo static C
+ * functions (internal/sim/bh/gpu_darwin.go:18-62: gpu_init / gpu_buffer /
+ * gpu_walk, synchronous, 0-or-error-code returns with a message buffer). The
+ * entry points below replace those; each cites the reference interface it
+ * stands in for. Plain pointers and sizes only; all host arrays are owned by
+ * the caller, all device memory by the context (grow-only, no allocation per
+ * call once sizes are stable).
+ *
+ * Threading: a context may be used from any OS thread (it makes its device
+ * current on every entry, as a cgo caller can migrate between threads), but
+ * by one thread at a time. Every call is synchronous: it returns after the
+ * device work it issued has finished, like gpu_walk's waitUntilCompleted.
+ *
+ * Errors: every function returns GBH_OK (0) or a GBH_ERR_* code; the message
+ * is available from gbh_last_error(). Nothing aborts the process.
+ */
+#ifndef GBH_H
+#define GBH_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GBH_ABI_VERSION 1
+
+enum {
+    GBH_OK = 0,
+    GBH_ERR_ARG = 1,         /* invalid argument (null pointer, negative size, bad enum) */
+    GBH_ERR_CUDA = 2,        /* a CUDA runtime call failed (message has the CUDA error) */
+    GBH_ERR_NOMEM = 3,       /* device allocation failed */
+    GBH_ERR_LIMIT = 4,       /* a device-side walk exceeded its step bound (corrupt input?) */
+    GBH_ERR_STATE = 5,       /* no resident state, or sizes do not match it */
+    GBH_ERR_UNSUPPORTED = 6  /* input outside this path (e.g. alive black holes in a step) */
+};
+
+/* Body kinds, internal/sim/state.go:12-21 (sim.Kind). */
+enum { GBH_STAR = 0, GBH_BLACK_HOLE = 1, GBH_DARK_MATTER = 2, GBH_GAS = 3 };
+
+/* Tree walk variants. */
+enum {
+    /* Warp-cooperative walk: FP32 group-relative coordinates split from FP64
+       positions, compensated per-particle accumulation. The default. */
+    GBH_WALK_MIXED = 0,
+    /* One thread per star, all FP32, uncompensated: the CUDA twin of the Metal
+       kernel internal/sim/bh/gpu_darwin.go:76-118. */
+    GBH_WALK_PLAIN = 1,
+    /* One thread per star in FP64 with the reference's operation order: bit
+       identical to bh.Solver.walk (internal/sim/bh/bh.go:155-204). */
+    GBH_WALK_FP64 = 2
+};
+
+/* Solver knobs: bh.Solver{Theta, MonopoleOnly} (bh.go:77-87) and the
+   sim.Params fields the force path reads (sim.go:9-23). */
+typedef struct {
+    double theta;            /* opening angle; 0 means 0.9 (bh.go:63-66, 118-123) */
+    double softening;        /* Plummer softening length eps (Params.Softening) */
+    int32_t leaf_size;       /* max stars per leaf; 0 means 24 (bh.go:67-68) */
+    int32_t monopole_only;   /* drop quadrupoles of accepted nodes (bh.go:82-83) */
+    int32_t dark_matter_off; /* dark matter pulls nothing (Params.DarkMatterOff, sim.go:92-98) */
+    int32_t walk;            /* GBH_WALK_* */
+} gbh_params;
+
+typedef struct {
+    int32_t device;          /* CUDA device ordinal */
+    int32_t reserved[7];     /* zero */
+} gbh_config;
+
+/* One tree node, field for field internal/sim/bh/bh.go:108-116 (104 bytes). */
+typedef struct {
+    double x, y, z, m;
+    double qxx, qyy, qzz, qxy, qxz, qyz;
+    double crit2;
+    int32_t first, next, lo, hi;
+} gbh_node;
+
+/* Device times of the last call, from CUDA events on the context's stream
+   (LastGPUSeconds, gpu_darwin.go:155, split by stage). */
+typedef struct {
+    double build_ms;   /* collect, keys, sort, node ranges, moments */
+    double walk_ms;    /* tree walk */
+    double step_ms;    /* kicks and drift */
+    double total_ms;   /* everything the call issued, copies included */
+    int64_t nstars;    /* stars in the last tree */
+    int64_t nnodes;    /* nodes in the last tree */
+    int64_t launches;  /* kernels launched by the last call */
+    int64_t h2d_bytes; /* host-to-device bytes copied by the last call */
+    int64_t d2h_bytes; /* device-to-host bytes copied by the last call */
+} gbh_timings;
+
+typedef struct gbh_ctx gbh_ctx;
+
+/* Creates a context on cfg->device (NULL: device 0). Replaces gpu_init /
+   GPUAvailable (gpu_darwin.go:18-29, 132-142): returns a code and writes a
+   message to err on failure. */
+int gbh_create(const gbh_config *cfg, gbh_ctx **out, char *err, int errlen);
+/* Frees the context and all its device memory. NULL is a no-op. */
+void gbh_destroy(gbh_ctx *ctx);
+/* Message of the last failed call on ctx ("" after a success). */
+const char *gbh_last_error(const gbh_ctx *ctx);
+/* Device name (GPUName, gpu_darwin.go:145-152). */
+int gbh_device_name(gbh_ctx *ctx, char *out, int len);
+
+/*
+ * bh.Solver.Accelerations (bh.go:125-151) on host arrays of one sim.State
+ * (state.go:33-52): fills ax/ay/az for every alive non-hole body from the
+ * star–star forces, sets alive black holes to 0 and leaves dead bodies'
+ * entries untouched. kind and alive may be NULL (all stars, all alive).
+ */
+int gbh_accelerations(gbh_ctx *ctx, const gbh_params *p, int64_t n, const double *px,
+                      const double *py, const double *pz, const double *mass,
+                      const uint8_t *kind, const uint8_t *alive, double *ax, double *ay,
+                      double *az);
+
+/*
+ * bh.Solver.PotentialEnergy (potential.go:12-42): U from an FP64 tree walk
+ * at min(theta, 0.9), with star–hole and hole–hole pairs in the pair model of
+ * internal/sim/pair.go at speed of light c (0: Newtonian).
+ */
+int gbh_potential_energy(gbh_ctx *ctx, const gbh_params *p, int64_t n, const double *px,
+                         const double *py, const double *pz, const double *mass,
+                         const uint8_t *kind, const uint8_t *alive, double c, double *u);
+
+/*
+ * direct.Solver.Accelerations (internal/sim/direct/direct.go:18-48) in FP64 on
+ * the GPU, for the ntargets state indices in targets (all bodies when targets
+ * is NULL; then ntargets is ignored and rows follow state order). Same
+ * operation order as the reference, so results are bit identical to it.
+ */
+int gbh_direct_accelerations(gbh_ctx *ctx, const gbh_params *p, int64_t n, const double *px,
+                             const double *py, const double *pz, const double *mass,
+                             const uint8_t *kind, const int64_t *targets, int64_t ntargets,
+                             double *ax, double *ay, double *az);
+
+/*
+ * sim.Simulation.Step (sim.go:248-288) repeated nsteps times for a state with
+ * no alive black holes and no gas hydro: kick(dt/2), drift(dt) (c = 0,
+ * sim.go:327-334), Solver.Accelerations, kick(dt/2). If acc_valid is 0 the
+ * forces are computed first (initForces, gas.go:14-17). Arrays are read and
+ * written in place; the state stays on the device between the steps.
+ */
+int gbh_step_kdk(gbh_ctx *ctx, const gbh_params *p, double dt, int64_t nsteps, int32_t acc_valid,
+                 int64_t n, double *px, double *py, double *pz, double *vx, double *vy,
+                 double *vz, double *ax, double *ay, double *az, const double *mass,
+                 const uint8_t *kind, const uint8_t *alive);
+
+/* ---- Resident state: the same step with the state kept in HBM between calls. ---- */
+
+/* Copies a state to the device (acc may be NULL: forces are then computed before the
+   first step). */
+int gbh_state_upload(gbh_ctx *ctx, int64_t n, const double *px, const double *py,
+                     const double *pz, const double *vx, const double *vy, const double *vz,
+                     const double *ax, const double *ay, const double *az, const double *mass,
+                     const uint8_t *kind, const uint8_t *alive);
+/* Copies the resident state back (any pointer may be NULL). */
+int gbh_state_download(gbh_ctx *ctx, double *px, double *py, double *pz, double *vx, double *vy,
+                       double *vz, double *ax, double *ay, double *az);
+/* nsteps KDK steps on the resident state (as gbh_step_kdk, no copies). */
+int gbh_state_step(gbh_ctx *ctx, const gbh_params *p, double dt, int64_t nsteps);
+/* Accelerations of the resident state (as gbh_accelerations, no copies). */
+int gbh_state_accelerations(gbh_ctx *ctx, const gbh_params *p);
+
+/* ---- Inspection of the last tree (b.nodes / b.order / b.keys in bh.Solver). ---- */
+
+/* Stars and nodes of the last built tree. */
+int gbh_tree_size(gbh_ctx *ctx, int64_t *nstars, int64_t *nnodes);
+/* Copies the last tree: Morton keys and state indices in sorted order (nstars each)
+   and the node table in the reference's serial index layout (up to node_cap nodes).
+   Any pointer may be NULL. */
+int gbh_tree_export(gbh_ctx *ctx, uint64_t *keys, int32_t *order, gbh_node *nodes,
+                    int64_t node_cap);
+/* Device times and counters of the last call. */
+int gbh_last_timings(gbh_ctx *ctx, gbh_timings *t);
+
+/* ---- Diagnostics. ---- */
+
+/* Measures this device's FP32 FMA throughput (TFLOP/s, 2 flops per FMA) with a
+   register-resident FMA loop of about ms milliseconds; the roofline denominator
+   of the walk. */
+int gbh_probe_fp32_peak(gbh_ctx *ctx, double ms, double *tflops);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

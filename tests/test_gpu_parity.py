@@ -1,0 +1,281 @@
+"""GPU parity: the CUDA path through the C-ABI against the CPU oracle and the golden fixtures.
+
+Bit-exact where the reference's arithmetic is integer or FP64 in a fixed order (Morton keys,
+sort order, node table, the FP64 walk, direct sum, potential terms, KDK); tolerances stated per
+test for the FP32 walks.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from gravitas_gb300 import abi, ics
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+P = abi.ptr
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    c = abi.Context(0)
+    yield c
+    c.close()
+
+
+def gpu_acc(ctx, s, theta, leaf, eps, walk, monopole=False, dm_off=False, acc=None):
+    n = len(s["px"])
+    ax, ay, az = (np.zeros(n) for _ in range(3)) if acc is None else (a.copy() for a in acc)
+    par = abi.make_params(theta, eps, leaf, monopole, dm_off, walk)
+    ctx.call("gbh_accelerations", par, n, P(s["px"]), P(s["py"]), P(s["pz"]), P(s["mass"]),
+             P(s.get("kind")), P(s.get("alive")), P(ax), P(ay), P(az))
+    return np.stack([ax, ay, az], axis=1)
+
+
+def oracle_tree(s, theta, leaf, dm_off=False):
+    return O.Tree(s["px"], s["py"], s["pz"], s["mass"], s.get("kind"), s.get("alive"), theta=theta, leaf=leaf,
+                  dm_off=dm_off, workers=1)
+
+
+def rel_err(got, want):
+    return np.linalg.norm(got - want, axis=1) / np.linalg.norm(want, axis=1)
+
+
+def random_state(n, seed, spread=1.0, kinds=False, dead=False):
+    rng = np.random.default_rng(seed)
+    p = rng.normal(size=(n, 3)) * spread
+    s = dict(px=p[:, 0].copy(), py=p[:, 1].copy(), pz=p[:, 2].copy(), mass=rng.uniform(0.5, 1.5, n))
+    s["kind"] = rng.choice([0, 2, 3], n).astype(np.uint8) if kinds else np.zeros(n, np.uint8)
+    s["alive"] = (rng.random(n) > 0.1).astype(np.uint8) if dead else np.ones(n, np.uint8)
+    return s
+
+
+def assert_tree_equal(ctx, s, theta, leaf, dm_off=False):
+    t = oracle_tree(s, theta, leaf, dm_off)
+    e = t.export()
+    g = ctx.tree_export()
+    assert np.array_equal(g["keys"], e["keys"]), "Morton keys differ"
+    assert np.array_equal(g["order"], e["order"]), "sort order differs"
+    assert len(g["nodes"]) == len(e["nodes"]), "node count differs"
+    for f in abi.NODE_DTYPE.names:
+        assert np.array_equal(g["nodes"][f], e["nodes"][f]), f"node field {f} differs"
+    return t
+
+
+# ---------------------------------------------------------------- known answer
+
+@pytest.mark.parametrize("walk", ["fp64", "plain", "mixed"])
+def test_known_answer(ctx, walk):  # bh_test.go:137-147
+    g = np.load(os.path.join(GOLDEN, "kat.npz"))
+    s = {k: g[k] for k in ("px", "py", "pz", "mass", "kind", "alive")}
+    a = gpu_acc(ctx, s, 0.0, 0, 0.0, walk)
+    if walk == "fp64":
+        assert np.array_equal(a, g["acc"])
+    else:
+        assert np.allclose(a, g["acc"], rtol=1e-6, atol=0)
+
+
+# ---------------------------------------------------------------- tree, bit exact
+
+@pytest.mark.parametrize("name", ["plummer", "disk"])
+def test_tree_and_fp64_walk_match_golden(ctx, name):
+    g = np.load(os.path.join(GOLDEN, f"{name}.npz"))
+    s = {k: g[k] for k in ("px", "py", "pz", "mass", "kind", "alive")}
+    a = gpu_acc(ctx, s, float(g["theta"]), int(g["leaf"]), float(g["eps"]), "fp64")
+    t = ctx.tree_export()
+    assert np.array_equal(t["keys"], g["keys"])
+    assert np.array_equal(t["order"], g["order"])
+    assert np.array_equal(t["nodes"], g["nodes"])
+    assert np.array_equal(a, g["acc"])
+
+
+@pytest.mark.parametrize("n,leaf,seed,theta", [
+    (1, 8, 0, 0.5), (2, 1, 1, 0.5), (7, 1, 2, 0.3), (100, 4, 3, 0.5), (1000, 8, 4, 0.5),
+    (5000, 24, 5, 0.9), (33_000, 32, 6, 0.7), (50_000, 8, 7, 0.5)])
+def test_tree_bit_exact_random(ctx, n, leaf, seed, theta):
+    s = random_state(n, seed)
+    a = gpu_acc(ctx, s, theta, leaf, 0.01, "fp64")
+    t = assert_tree_equal(ctx, s, theta, leaf)
+    assert np.array_equal(a, t.accelerations(0.01))
+
+
+def test_tree_bit_exact_kinds_dead_dm_off(ctx):
+    s = random_state(20_000, 11, kinds=True, dead=True)
+    s["kind"][::97] = O.BLACK_HOLE
+    rng = np.random.default_rng(3)
+    init = [rng.normal(size=len(s["px"])) for _ in range(3)]
+    a = gpu_acc(ctx, s, 0.6, 12, 0.02, "fp64", dm_off=True, acc=init)
+    t = assert_tree_equal(ctx, s, 0.6, 12, dm_off=True)
+    want = t.accelerations(0.02, acc=[x.copy() for x in init])
+    assert np.array_equal(a, want)
+    dead = s["alive"] == 0
+    assert np.array_equal(a[dead], np.stack(init, axis=1)[dead])  # dead bodies untouched
+    holes = (s["alive"] == 1) & (s["kind"] == O.BLACK_HOLE)
+    assert np.all(a[holes] == 0)
+
+
+def test_coincident_stars(ctx):  # bh_test.go:149-163
+    n = 101
+    s = dict(px=np.full(n, 1.0), py=np.full(n, 2.0), pz=np.full(n, 3.0), mass=np.ones(n))
+    s["px"][-1] = s["py"][-1] = s["pz"][-1] = 0.0
+    for walk in ("fp64", "plain", "mixed"):
+        a = gpu_acc(ctx, s, 0.0, 0, 0.01, walk)
+        assert not np.isnan(a).any()
+    assert_tree_equal(ctx, s, 0.9, 24)
+    nodes = ctx.tree_export()["nodes"]
+    assert (nodes["hi"] - nodes["lo"])[nodes["first"] < 0].max() == 100
+
+
+def test_clustered_and_far_apart(ctx):
+    """Extreme dynamic range: two tight clumps 1e6 apart (deep trees, large coordinates)."""
+    rng = np.random.default_rng(9)
+    p = np.concatenate([rng.normal(size=(3000, 3)) * 1e-3, rng.normal(size=(3000, 3)) * 1e-3 + 1e6])
+    s = dict(px=p[:, 0].copy(), py=p[:, 1].copy(), pz=p[:, 2].copy(), mass=np.ones(6000))
+    a = gpu_acc(ctx, s, 0.5, 8, 1e-4, "fp64")
+    t = assert_tree_equal(ctx, s, 0.5, 8)
+    assert np.array_equal(a, t.accelerations(1e-4))
+    # the mixed walk stays accurate far from the origin (group-relative coordinates)
+    am = gpu_acc(ctx, s, 0.5, 8, 1e-4, "mixed")
+    scale = np.linalg.norm(a, axis=1).mean()
+    e = np.linalg.norm(am - a, axis=1) / scale
+    assert np.median(e) < 1e-5 and e.max() < 1e-3
+
+
+# ---------------------------------------------------------------- FP32 walks
+
+def test_plain_walk_matches_cpu_walk(ctx):  # gpu_test.go:8-21
+    s = ics.test_disk(20000)
+    stars = s["kind"] == O.STAR
+    want = oracle_tree(s, 0.9, 24).accelerations(0.06)
+    got = gpu_acc(ctx, s, 0.0, 0, 0.06, "plain")
+    e = rel_err(got[stars], want[stars])
+    assert np.median(e) <= 1e-5 and e.max() <= 1e-3
+
+
+def test_mixed_walk_accuracy_vs_direct(ctx):
+    """The warp walk opens a node wherever any star of its group would, so against the FP64
+    direct sum it is at least as accurate as the reference's per-star walk."""
+    s = ics.plummer(16384, seed=0)
+    want = O.direct(s["px"], s["py"], s["pz"], s["mass"], eps=0.01)
+    ref = oracle_tree(s, 0.5, 8).accelerations(0.01)
+    e_ref = rel_err(ref, want)
+    for walk in ("mixed", "plain"):
+        got = gpu_acc(ctx, s, 0.5, 8, 0.01, walk)
+        e = rel_err(got, want)
+        rms, rms_ref = np.sqrt(np.mean(e ** 2)), np.sqrt(np.mean(e_ref ** 2))
+        p99, p99_ref = np.percentile(e, 99), np.percentile(e_ref, 99)
+        if walk == "mixed":
+            assert rms <= rms_ref * 1.001 + 1e-7 and p99 <= p99_ref * 1.001 + 1e-7
+        assert rms <= 2e-3
+        # against the reference walk itself: within its own approximation error
+        d = rel_err(got, ref)
+        assert np.median(d) <= np.median(e_ref) and d.max() <= 5 * e_ref.max()
+
+
+def test_mixed_walk_monopole_and_no_softening(ctx):
+    s = random_state(3000, 21)
+    want = O.direct(s["px"], s["py"], s["pz"], s["mass"], eps=0.0)
+    for mono in (False, True):
+        ref = oracle_tree(s, 0.5, 8).accelerations(0.0, monopole_only=mono)
+        got = gpu_acc(ctx, s, 0.5, 8, 0.0, "mixed", monopole=mono)
+        assert np.isfinite(got).all()
+        e, e_ref = rel_err(got, want), rel_err(ref, want)
+        assert np.sqrt(np.mean(e ** 2)) <= np.sqrt(np.mean(e_ref ** 2)) * 1.01 + 1e-6
+
+
+@pytest.mark.parametrize("walk", ["fp64", "plain", "mixed"])
+def test_walks_are_deterministic(ctx, walk):
+    s = ics.plummer(30000, seed=2)
+    a = gpu_acc(ctx, s, 0.5, 8, 0.01, walk)
+    b = gpu_acc(ctx, s, 0.5, 8, 0.01, walk)
+    assert np.array_equal(a, b)
+
+
+# ---------------------------------------------------------------- direct, potential, KDK
+
+def test_direct_sum_bit_exact(ctx):
+    s = random_state(3000, 5, kinds=True)
+    s["kind"][::50] = O.BLACK_HOLE
+    want = O.direct(s["px"], s["py"], s["pz"], s["mass"], s["kind"], eps=0.02, dm_off=True)
+    n = len(s["px"])
+    out = np.zeros((3, n))
+    par = abi.make_params(0, 0.02, 0, False, True, "fp64")
+    ctx.call("gbh_direct_accelerations", par, n, P(s["px"]), P(s["py"]), P(s["pz"]), P(s["mass"]), P(s["kind"]),
+             None, 0, P(out[0]), P(out[1]), P(out[2]))
+    assert np.array_equal(out.T, want)
+    tg = np.array([0, 17, 2999, 50], np.int64)
+    sub = np.zeros((3, 4))
+    ctx.call("gbh_direct_accelerations", par, n, P(s["px"]), P(s["py"]), P(s["pz"]), P(s["mass"]), P(s["kind"]),
+             P(tg), 4, P(sub[0]), P(sub[1]), P(sub[2]))
+    assert np.array_equal(sub.T, want[tg])
+
+
+def test_potential_matches_oracle(ctx):
+    g = np.load(os.path.join(GOLDEN, "disk.npz"))
+    s = {k: g[k] for k in ("px", "py", "pz", "mass", "kind", "alive")}
+    u = np.zeros(1)
+    par = abi.make_params(float(g["theta"]), float(g["eps"]), int(g["leaf"]), False, False, "fp64")
+    ctx.call("gbh_potential_energy", par, len(s["px"]), P(s["px"]), P(s["py"]), P(s["pz"]), P(s["mass"]),
+             P(s["kind"]), P(s["alive"]), float(g["c"]), P(u))
+    assert abs((u[0] - float(g["potential"])) / float(g["potential"])) <= 1e-12
+
+
+def test_kdk_fp64_bit_exact(ctx):
+    g = np.load(os.path.join(GOLDEN, "kdk.npz"))
+    st = {k: g[f"in_{k}"].copy() for k in ("px", "py", "pz", "vx", "vy", "vz", "mass")}
+    n = len(st["px"])
+    acc = [np.zeros(n) for _ in range(3)]
+    par = abi.make_params(float(g["theta"]), float(g["eps"]), int(g["leaf"]), False, False, "fp64")
+    ctx.call("gbh_step_kdk", par, float(g["dt"]), int(g["nsteps"]), 0, n, P(st["px"]), P(st["py"]), P(st["pz"]),
+             P(st["vx"]), P(st["vy"]), P(st["vz"]), P(acc[0]), P(acc[1]), P(acc[2]), P(st["mass"]), None, None)
+    for k in ("px", "py", "pz", "vx", "vy", "vz"):
+        assert np.array_equal(st[k], g[f"out_{k}"]), k
+    for k, a in zip(("ax", "ay", "az"), acc):
+        assert np.array_equal(a, g[f"out_{k}"]), k
+
+
+def test_resident_steps_match_host_steps(ctx):
+    s = ics.plummer(20000, seed=7)
+    n = len(s["px"])
+    par = abi.make_params(0.5, 0.01, 8, False, False, "mixed")
+    host = {k: s[k].copy() for k in ("px", "py", "pz", "vx", "vy", "vz", "ax", "ay", "az")}
+    ctx.call("gbh_step_kdk", par, 1e-3, 3, 0, n, *[P(host[k]) for k in ("px", "py", "pz", "vx", "vy", "vz", "ax",
+                                                                         "ay", "az")], P(s["mass"]), None, None)
+    ctx.call("gbh_state_upload", n, P(s["px"]), P(s["py"]), P(s["pz"]), P(s["vx"]), P(s["vy"]), P(s["vz"]), None,
+             None, None, P(s["mass"]), None, None)
+    ctx.call("gbh_state_step", par, 1e-3, 3)
+    dev = {k: np.zeros(n) for k in host}
+    ctx.call("gbh_state_download", *[P(dev[k]) for k in ("px", "py", "pz", "vx", "vy", "vz", "ax", "ay", "az")])
+    for k in host:
+        assert np.array_equal(host[k], dev[k]), k
+
+
+def test_step_rejects_holes(ctx):
+    s = ics.test_disk(500)
+    n = len(s["px"])
+    par = abi.make_params(0.5, 0.06, 8, False, False, "mixed")
+    with pytest.raises(abi.GbhError) as ei:
+        ctx.call("gbh_step_kdk", par, 1e-3, 1, 0, n, *[P(s[k]) for k in ("px", "py", "pz", "vx", "vy", "vz", "ax",
+                                                                          "ay", "az")], P(s["mass"]), P(s["kind"]),
+                 P(s["alive"]))
+    assert ei.value.code == abi.ERR_UNSUPPORTED
+
+
+def test_bad_arguments_are_errors(ctx):
+    s = random_state(10, 1)
+    with pytest.raises(abi.GbhError) as ei:
+        gpu_acc(ctx, s, 1.5, 8, 0.01, "mixed")
+    assert ei.value.code == abi.ERR_ARG
+    with pytest.raises(abi.GbhError):
+        gpu_acc(ctx, s, 0.5, 8, -1.0, "mixed")
+    # the context stays usable
+    a = gpu_acc(ctx, s, 0.5, 8, 0.01, "fp64")
+    assert np.isfinite(a).all()
+
+
+def test_empty_state(ctx):
+    s = dict(px=np.zeros(0), py=np.zeros(0), pz=np.zeros(0), mass=np.zeros(0))
+    assert gpu_acc(ctx, s, 0.5, 8, 0.01, "mixed").shape == (0, 3)
+    s = dict(px=np.zeros(5), py=np.zeros(5), pz=np.zeros(5), mass=np.ones(5), kind=np.full(5, 1, np.uint8))
+    assert np.all(gpu_acc(ctx, s, 0.5, 8, 0.01, "mixed") == 0)  # holes only: no stars, all zero

@@ -1,0 +1,237 @@
+"""CPU tests pinning the oracle (the checker) to the reference's own tests.
+
+The reference (Go) cannot run here and stores no golden vectors for this path; its tests are a
+known-answer test and relations. Each test below restates one of them against the C++ oracle
+(internal/sim/bh/bh_test.go, gpu_test.go, internal/sim/direct/direct_test.go), then checks the
+committed fixtures of tests/golden/ (made by tests/golden/make_golden.py).
+"""
+import os
+
+import numpy as np
+import pytest
+
+from gravitas_gb300 import ics
+from oracle import oracle as O
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def rel_errors(got, want):
+    """Median and max of |got - want| / |want| per body (bh_test.go:76-86)."""
+    e = np.linalg.norm(got - want, axis=1) / np.linalg.norm(want, axis=1)
+    e = np.sort(e)
+    return e[len(e) // 2], e[-1]
+
+
+def tree_of(s, **kw):
+    return O.Tree(s["px"], s["py"], s["pz"], s["mass"], s.get("kind"), s.get("alive"), **kw)
+
+
+def test_morton_key_interleaves_bits():  # bh_test.go:16-31
+    def naive(x, y, z):
+        k = 0
+        for b in range(21):
+            k |= ((x >> b) & 1) << (3 * b + 2) | ((y >> b) & 1) << (3 * b + 1) | ((z >> b) & 1) << (3 * b)
+        return k
+
+    rng = np.random.default_rng(12)
+    for x, y, z in rng.integers(0, 1 << 21, size=(1000, 3)):
+        assert O.morton_key(int(x), int(y), int(z)) == naive(int(x), int(y), int(z))
+
+
+def test_radix_sort():  # bh_test.go:33-52
+    rng = np.random.default_rng(34)
+    keys = rng.integers(0, 1 << 63, size=5000, dtype=np.uint64)
+    k, i = O.radix_sort(keys, np.arange(5000, dtype=np.int32))
+    assert np.all(k[1:] >= k[:-1])
+    assert np.array_equal(keys[i], k)
+
+
+def test_parallel_radix_sort_is_stable_and_correct():  # bh_test.go:353-367
+    rng = np.random.default_rng(89)
+    keys = rng.integers(0, 1 << 20, size=200_000, dtype=np.uint64) << np.uint64(40)
+    idx = np.arange(len(keys), dtype=np.int32)
+    k1, i1 = O.radix_sort(keys, idx, workers=1)
+    k7, i7 = O.radix_sort(keys, idx, workers=7)
+    assert np.array_equal(k1, k7) and np.array_equal(i1, i7)
+    # stable: equal keys keep index order
+    same = k1[1:] == k1[:-1]
+    assert np.all(i1[1:][same] > i1[:-1][same])
+    order = np.argsort(keys, kind="stable")
+    assert np.array_equal(i1, order)
+
+
+def test_solver_leaves_holes_to_the_integrator():  # bh_test.go:137-147 (known answer)
+    g = np.load(os.path.join(GOLDEN, "kat.npz"))
+    t = O.Tree(g["px"], g["py"], g["pz"], g["mass"], g["kind"], g["alive"])
+    assert np.array_equal(t.accelerations(0.0), g["acc"])
+    assert np.array_equal(g["acc"], [[2, 0, 0], [-1, 0, 0], [0, 0, 0]])
+
+
+def test_coincident_stars_do_not_recurse_forever():  # bh_test.go:149-163
+    n = 101
+    px, py, pz = np.full(n, 1.0), np.full(n, 2.0), np.full(n, 3.0)
+    px[-1] = py[-1] = pz[-1] = 0.0
+    t = O.Tree(px, py, pz, np.ones(n))
+    a = t.accelerations(0.01)
+    assert not np.isnan(a).any()
+    nodes = t.export()["nodes"]
+    leaves = nodes[nodes["first"] < 0]
+    assert (leaves["hi"] - leaves["lo"]).max() == 100  # oversize leaf at the depth cap
+
+
+def test_tiny_theta_matches_direct():  # bh_test.go:88-97
+    s = ics.test_disk(3000)
+    want = O.direct(s["px"], s["py"], s["pz"], s["mass"], s["kind"], eps=0.06)
+    got = tree_of(s, theta=1e-9).accelerations(0.06)
+    stars = s["kind"] != O.BLACK_HOLE
+    _, mx = rel_errors(got[stars], want[stars])
+    assert mx < 1e-10
+    assert np.all(got[~stars] == 0) and np.all(want[~stars] == 0)
+
+
+def test_default_theta_accuracy():  # bh_test.go:124-135 (star-star part; holes are summed outside)
+    s = ics.test_disk(5000)
+    stars = s["kind"] == O.STAR
+    want = O.direct(s["px"], s["py"], s["pz"], s["mass"], s["kind"], eps=0.06)[stars]
+    got = tree_of(s).accelerations(0.06)[stars]
+    med, mx = rel_errors(got, want)
+    assert med < 4e-3 and mx < 6e-2
+
+
+@pytest.mark.parametrize("n", [4000, 40_000, 60_000])
+def test_parallel_build_is_bit_identical(n):  # bh_test.go:192-199, 369-394
+    s = ics.test_disk(n)
+    t1, t8 = tree_of(s, workers=1), tree_of(s, workers=8)
+    assert t1.nnodes == t8.nnodes
+    assert np.array_equal(t1.accelerations(0.06, workers=1), t8.accelerations(0.06, workers=8))
+    u1, u8 = t1.potential(0.06, c=10), t8.potential(0.06, c=10)
+    assert abs((u1 - u8) / u1) <= 1e-12
+
+
+def test_potential_energy_matches_exact():  # bh_test.go:280-293
+    s = ics.test_disk(3000)
+    want = O.potential_exact(s["px"], s["py"], s["pz"], s["mass"], s["kind"], eps=0.06, c=10)
+    got = tree_of(s, theta=1e-9).potential(0.06, c=10)
+    assert abs((got - want) / want) < 1e-10
+    got = tree_of(s, theta=0.9).potential(0.06, c=10)
+    assert abs((got - want) / want) < 1e-3
+
+
+def test_quadrupole_improves_far_field():  # bh_test.go:309-330
+    s = ics.far_cluster()
+    want = O.direct(s["px"], s["py"], s["pz"], s["mass"], eps=1e-3)[0]
+    err = {}
+    for mono in (True, False):
+        got = tree_of(s, theta=0.95).accelerations(1e-3, monopole_only=mono)[0]
+        err[mono] = np.linalg.norm(got - want) / np.linalg.norm(want)
+    assert err[False] < err[True] / 5
+
+
+def test_quadrupole_force_is_gradient_of_potential():  # bh_test.go:332-351
+    s = ics.far_cluster()
+    t = tree_of(s, theta=0.95)
+    eps2, h = 1e-6, 1e-6
+    x, y, z = 0.0, 0.5, 0.2
+    a = t.walk_point(x, y, z, eps2)
+    g = [(t.walk_potential_point(x + h * (d == 0), y + h * (d == 1), z + h * (d == 2), eps2) -
+          t.walk_potential_point(x - h * (d == 0), y - h * (d == 1), z - h * (d == 2), eps2)) / (2 * h)
+         for d in range(3)]
+    assert np.all(np.abs(a - np.array(g)) <= 1e-6 * abs(a[0]))
+
+
+def test_fp32_walk_matches_fp64_walk():  # gpu_test.go:8-21, on the CPU restatement of the Metal walk
+    s = ics.test_disk(20000)
+    t = tree_of(s)
+    want = t.accelerations(0.06)
+    e = t.export()
+    got32 = t.walk_fp32(0.06).astype(np.float64)
+    stars = s["kind"] == O.STAR
+    got = np.zeros_like(want)
+    got[e["order"]] = got32
+    med, mx = rel_errors(got[stars], want[stars])
+    assert med <= 1e-5 and mx <= 1e-3
+
+
+def test_kepler_conservation():  # direct_test.go:37-63, KDK with the tree solver on two bodies
+    e = 0.3
+    st = dict(px=np.array([0.0, 1 - e]), py=np.zeros(2), pz=np.zeros(2), vx=np.zeros(2),
+              vy=np.array([0.0, np.sqrt((1 + e) / (1 - e))]), vz=np.zeros(2), ax=np.zeros(2), ay=np.zeros(2),
+              az=np.zeros(2), mass=np.array([1.0, 1e-12]))
+    # a fixed central mass: a massive body at rest with negligible pull from the test body
+    period = 2 * np.pi
+    steps_per_orbit = 2000
+    dt = period / steps_per_orbit
+
+    def energy(s):
+        dx, dy = s["px"][1] - s["px"][0], s["py"][1] - s["py"][0]
+        v2 = (s["vx"][1] - s["vx"][0]) ** 2 + (s["vy"][1] - s["vy"][0]) ** 2
+        return 0.5 * v2 - 1 / np.hypot(dx, dy)
+
+    def ang(s):
+        dx, dy = s["px"][1] - s["px"][0], s["py"][1] - s["py"][0]
+        return dx * (s["vy"][1] - s["vy"][0]) - dy * (s["vx"][1] - s["vx"][0])
+
+    e0, l0 = energy(st), ang(st)
+    O.kdk(st, dt=dt, eps=0.0, theta=0.5, leaf=24, nsteps=steps_per_orbit * 20, workers=1)
+    assert abs((energy(st) - e0) / e0) <= 1e-4
+    assert abs(ang(st) - l0) <= 1e-10
+    r = np.hypot(st["px"][1] - st["px"][0], st["py"][1] - st["py"][0])
+    assert abs(r - 0.7) < 0.05
+
+
+def test_momentum_conservation_direct():  # direct_test.go:65-75
+    rng = np.random.default_rng(7)
+    n = 1000
+    p = rng.normal(size=(n, 3))
+    m = rng.uniform(0.5, 1.5, n)
+    a = O.direct(p[:, 0], p[:, 1], p[:, 2], m, eps=0.05)
+    assert np.abs((m[:, None] * a).sum(axis=0)).max() <= 1e-12 * np.abs(m[:, None] * a).sum()
+
+
+@pytest.mark.parametrize("name", ["plummer", "disk"])
+def test_oracle_matches_golden(name):
+    g = np.load(os.path.join(GOLDEN, f"{name}.npz"))
+    t = O.Tree(g["px"], g["py"], g["pz"], g["mass"], g["kind"], g["alive"], theta=float(g["theta"]),
+               leaf=int(g["leaf"]), workers=1)
+    e = t.export()
+    assert np.array_equal(e["keys"], g["keys"])
+    assert np.array_equal(e["order"], g["order"])
+    assert np.array_equal(e["nodes"], g["nodes"])
+    assert np.array_equal(t.accelerations(float(g["eps"])), g["acc"])
+    assert np.array_equal(np.array(t.counts(float(g["eps"]))), g["counts"])
+    if "acc_fp32_sorted" in g:
+        assert np.array_equal(t.walk_fp32(float(g["eps"])), g["acc_fp32_sorted"])
+
+
+def test_oracle_kdk_matches_golden():
+    g = np.load(os.path.join(GOLDEN, "kdk.npz"))
+    st = {k: g[f"in_{k}"].copy() for k in ("px", "py", "pz", "vx", "vy", "vz", "mass")}
+    n = len(st["px"])
+    st.update(ax=np.zeros(n), ay=np.zeros(n), az=np.zeros(n))
+    O.kdk(st, dt=float(g["dt"]), eps=float(g["eps"]), theta=float(g["theta"]), leaf=int(g["leaf"]),
+          nsteps=int(g["nsteps"]), workers=1)
+    for k in ("px", "py", "pz", "vx", "vy", "vz", "ax", "ay", "az"):
+        assert np.array_equal(st[k], g[f"out_{k}"])
+
+
+def test_node_table_invariants():
+    """Structure of the reference's serial layout: children contiguous, skip pointers pre-order."""
+    g = np.load(os.path.join(GOLDEN, "plummer.npz"))
+    nodes = g["nodes"]
+    n = len(g["keys"])
+    assert nodes[0]["lo"] == 0 and nodes[0]["hi"] == n and nodes[0]["next"] == -1
+    for i, nd in enumerate(nodes):
+        if nd["first"] >= 0:
+            c = nd["first"]
+            lo = nd["lo"]
+            while True:  # children tile the parent's range in order
+                assert nodes[c]["lo"] == lo
+                lo = nodes[c]["hi"]
+                if nodes[c]["next"] != c + 1:
+                    assert nodes[c]["next"] == nd["next"]
+                    break
+                c += 1
+            assert lo == nd["hi"]
+        else:
+            assert nd["hi"] - nd["lo"] <= int(g["leaf"])
