@@ -1,0 +1,323 @@
+"""Benchmark of the Barnes-Hut gravity step: particle-steps/s at N = 1,048,576, theta = 0.5.
+
+Workload: a major merger of two disk + bulge + NFW-halo galaxies of 524,288 particles each
+(seeded synthetic stand-in, gravitas_gb300.ics.merger), theta 0.5 with quadrupoles, leaf 8,
+softening 0.02, global KDK steps of dt = 1e-3 (kick, drift, tree build, walk, kick). One step
+advances all N particles.
+
+  value       mixed walk (warp-cooperative FP32 + compensated sums, FP64 state), state resident
+              in HBM, device time of K steps from CUDA events on the library's stream, L2
+              flushed (256 MiB write) between steps
+  e2e         the same step through gbh_step_kdk with pinned host buffers: state copied in and
+              out inside every timed step (wall clock)
+  plain       the same step with the plain all-FP32 walk (the CUDA twin of the Metal kernel)
+  roofline    the walk kernel: algorithmic FLOP (50 per accepted quadrupole node, 18 per leaf
+              pair, 8 per opened node, counted by the reference per-star walk of the CPU oracle)
+              per launch / its CUDA-event duration, against this GPU's FP32 FMA peak measured
+              in the same run
+  errors      RMS and p99 relative force error of both walks against the FP64 direct sum on
+              4,096 seeded targets
+
+--impl reference times the CPU restatement of the reference's Barnes-Hut step (oracle/, FP64,
+all host threads) on the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "particle-steps/s @N=1M θ=0.5: mixed vs plain GPU walk at RMS force err ≤2e-3"
+N_DEFAULT = 1 << 20
+THETA, LEAF, EPS, DT = 0.5, 8, 0.02, 1e-3
+FIELDS = ("px", "py", "pz", "vx", "vy", "vz", "ax", "ay", "az")
+
+
+def workload_name(n, leaf):
+    return (f"merger N={n} (2 x {n // 2} disk+bulge+NFW-halo galaxies, pericentre 5, separation 40), "
+            f"theta={THETA}, leaf={leaf}, eps={EPS}, dt={DT}, global KDK steps")
+
+
+def dist_env():
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
+
+
+class Clocks:
+    """Samples nvidia-smi clocks and throttle reasons while the timed region runs."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device, self.rows, self.proc = device, [], None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            try:
+                sm.append(float(r[1]))
+                mx = float(r[2])
+            except (ValueError, IndexError):
+                continue
+            for name, v in zip(names, r[5:9]):
+                if v.strip().lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def make_workload(n, seed=0):
+    from gravitas_gb300 import ics
+    return ics.merger(n, seed=seed)
+
+
+def cpu_reference_steps(s, steps, leaf, workers=0, count=False):
+    """Times full KDK steps of the CPU oracle (the reference's algorithm, FP64) on a copy of s;
+    optionally also returns the reference walk's interaction counts at the initial state."""
+    from oracle import oracle as O
+    counts = None
+    if count:
+        t = O.Tree(s["px"], s["py"], s["pz"], s["mass"], theta=THETA, leaf=leaf, workers=workers)
+        counts = t.counts(EPS, workers=workers)
+        del t
+    st = {k: np.array(s[k], copy=True) for k in (*FIELDS, "mass")}
+    O.kdk(st, dt=DT, eps=EPS, theta=THETA, leaf=leaf, nsteps=0, workers=workers)  # initial forces
+    t0 = time.perf_counter()
+    O.kdk(st, dt=DT, eps=EPS, theta=THETA, leaf=leaf, nsteps=steps, acc_valid=True, workers=workers)
+    return time.perf_counter() - t0, counts
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    n = args.n
+    s = make_workload(n)
+    cores = os.cpu_count() or 1
+    # one warm-up step, then at most as many timed steps as fit in about a minute
+    warm, _ = cpu_reference_steps(s, max(1, min(args.warmup, 1)), args.leaf, workers=0)
+    k = max(1, min(args.steps, int(60.0 / max(warm, 1e-3))))
+    el, _ = cpu_reference_steps(s, k, args.leaf, workers=0)
+    value = n * k / el
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": args.gpus,
+        "steps": k, "warmup": 1, "ms_per_step": el / k * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": workload_name(n, args.leaf), "requested_steps": args.steps},
+        "cpu_baseline": {"value": value, "unit": "particle-steps/s", "cores": cores, "kind": "port",
+                         "sample": f"{k} full KDK steps of the {n}-particle workload (C++ restatement of the "
+                                   f"reference CPU Barnes-Hut, FP64, {cores} threads; Go is not available)"},
+        "e2e": {"value": value, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def rel_err_stats(got, want):
+    e = np.linalg.norm(got - want, axis=1) / np.linalg.norm(want, axis=1)
+    return {"rms": float(np.sqrt(np.mean(e ** 2))), "p99": float(np.percentile(e, 99)),
+            "median": float(np.median(e)), "max": float(e.max())}
+
+
+def run(args):
+    import torch
+
+    from gravitas_gb300 import abi
+
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    P = abi.ptr
+    n = args.n
+    s = make_workload(n, seed=0)
+    ctx = abi.Context(local)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{local}")
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    def upload(state):
+        ctx.call("gbh_state_upload", n, *[P(state[k]) for k in ("px", "py", "pz", "vx", "vy", "vz")],
+                 None, None, None, P(state["mass"]), None, None)
+
+    def timed_steps(walk, steps, warmup):
+        par = abi.make_params(THETA, EPS, args.leaf, False, False, walk)
+        upload(s)
+        for _ in range(warmup):
+            ctx.call("gbh_state_step", par, DT, 1)
+        barrier()
+        tot = walk_ms = build_ms = 0.0
+        launches = 0
+        for _ in range(steps):
+            flush.fill_(1)  # L2 flush (256 MiB) outside the step's events
+            torch.cuda.synchronize()
+            ctx.call("gbh_state_step", par, DT, 1)
+            t = ctx.timings()
+            tot += t["total_ms"]
+            walk_ms += t["walk_ms"]
+            build_ms += t["build_ms"]
+            launches += t["launches"]
+        barrier()
+        return tot, walk_ms, build_ms, launches, t["nnodes"]
+
+    peak = ctx.probe_fp32_peak(100.0)
+
+    # headline: mixed walk, resident state
+    with Clocks(local) as clk:
+        t_mixed, w_mixed, b_mixed, launches, nnodes = timed_steps("mixed", args.steps, args.warmup)
+    clocks = clk.summary()
+    t_plain, w_plain, b_plain, _, _ = timed_steps("plain", args.steps, args.warmup)
+
+    # max over ranks
+    def maxr(x):
+        if world == 1:
+            return x
+        tt = torch.tensor([x], dtype=torch.float64, device=f"cuda:{local}")
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        return float(tt.item())
+
+    t_mixed, t_plain = maxr(t_mixed), maxr(t_plain)
+    value = world * n * args.steps / (t_mixed * 1e-3)
+    plain_value = world * n * args.steps / (t_plain * 1e-3)
+
+    # end to end: host state in pinned memory, one gbh_step_kdk per step (copies inside)
+    host = {k: torch.from_numpy(np.array(s[k], copy=True)).pin_memory() for k in (*FIELDS, "mass")}
+    par = abi.make_params(THETA, EPS, args.leaf, False, False, "mixed")
+    hp = [host[k].data_ptr() for k in FIELDS]
+
+    def e2e_step(acc_valid):
+        ctx.call("gbh_step_kdk", par, DT, 1, acc_valid, n, *[P(x) for x in hp], P(host["mass"].data_ptr()),
+                 None, None)
+
+    e2e_step(0)
+    for _ in range(max(args.warmup - 1, 0)):
+        e2e_step(1)
+    barrier()
+    e2e_wall = 0.0
+    h2d = d2h = 0
+    for _ in range(args.steps):
+        flush.fill_(1)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e2e_step(1)
+        e2e_wall += time.perf_counter() - t0
+        tm = ctx.timings()
+        h2d, d2h = tm["h2d_bytes"], tm["d2h_bytes"]
+    e2e_wall = maxr(e2e_wall)
+    e2e_value = world * n * args.steps / e2e_wall
+
+    # force errors of both walks against the FP64 direct sum on 4096 seeded targets
+    rng = np.random.default_rng(1234)
+    targets = np.sort(rng.choice(n, 4096, replace=False)).astype(np.int64)
+    want = np.zeros((3, 4096))
+    ctx.call("gbh_direct_accelerations", abi.make_params(0, EPS, 0, False, False, "fp64"), n, P(s["px"]),
+             P(s["py"]), P(s["pz"]), P(s["mass"]), None, P(targets), 4096, P(want[0]), P(want[1]), P(want[2]))
+    want = want.T
+    errs = {}
+    for walk in ("mixed", "plain"):
+        a = [np.zeros(n) for _ in range(3)]
+        ctx.call("gbh_accelerations", abi.make_params(THETA, EPS, args.leaf, False, False, walk), n, P(s["px"]),
+                 P(s["py"]), P(s["pz"]), P(s["mass"]), None, None, P(a[0]), P(a[1]), P(a[2]))
+        errs[walk] = rel_err_stats(np.stack(a, axis=1)[targets], want)
+
+    line = None
+    if rank == 0:
+        # CPU baseline leg: the oracle (reference algorithm) on the host cores, bounded sample,
+        # plus the reference walk's interaction counts behind the algorithmic FLOP figure
+        cpu_steps = 1
+        el, counts = cpu_reference_steps(s, cpu_steps, args.leaf, workers=0, count=True)
+        cores = os.cpu_count() or 1
+        n_pn, n_pp, n_open = counts
+        flop = 50 * n_pn + 18 * n_pp + 8 * n_open
+        walk_s = w_mixed / args.steps * 1e-3
+        achieved = flop / walk_s / 1e12
+        line = {
+            "metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t_mixed / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 walk, f64 state", "data": "synthetic",
+            "config": {"workload": workload_name(n, args.leaf), "parallelism": "replicas" if world > 1 else "1 gpu",
+                       "l2": "flushed (256 MiB write) between timed steps; events cover each step only"},
+            "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                         "frac": achieved / peak, "traffic": None,
+                         "kernel": "k_walk_mixed", "flop_per_launch": flop,
+                         "peak_source": "FP32 FMA microbenchmark in this run (gbh_probe_fp32_peak); "
+                                        "MEASURED_PEAKS.json has no FP32 figure",
+                         "walk_ms": w_mixed / args.steps, "build_ms": b_mixed / args.steps},
+            "cpu_baseline": {"value": n * cpu_steps / el, "unit": "particle-steps/s", "cores": cores, "kind": "port",
+                             "sample": f"{cpu_steps} full KDK step of the {n}-particle workload, C++ restatement "
+                                       f"of the reference CPU Barnes-Hut (FP64), {cores} threads"},
+            "e2e": {"value": e2e_value, "unit": "particle-steps/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h, "api": "gbh_step_kdk on pinned host buffers, 1 step per call"},
+            "gpu_launches": launches,
+            "clocks": clocks,
+            "plain": {"value": plain_value, "ms_per_step": t_plain / args.steps, "walk_ms": w_plain / args.steps,
+                      "force_error": errs["plain"], "speedup_mixed_over_plain": value / plain_value},
+            "force_error": errs["mixed"],
+            "interactions": {"accepted_nodes": n_pn, "leaf_pairs": n_pp, "opened_nodes": n_open,
+                             "per_star": (n_pn + n_pp) / n, "nodes": nnodes},
+        }
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--n", type=int, default=N_DEFAULT)
+    ap.add_argument("--leaf", type=int, default=LEAF)
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "ours":
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

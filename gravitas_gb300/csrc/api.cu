@@ -39,6 +39,9 @@ struct gbh_ctx {
     double *tout = nullptr;
     int64_t targets_cap = 0;
     float *probe = nullptr;
+    // per-stage events of the current call: (build start, walk start, walk end) triples
+    std::vector<cudaEvent_t> evpool;
+    size_t evused = 0;
     // bookkeeping
     int64_t launches = 0;
     int64_t h2d = 0, d2h = 0;
@@ -120,6 +123,7 @@ int leaf_of(const gbh_params *p) { return p->leaf_size > 0 ? p->leaf_size : 24; 
 int begin(gbh_ctx *ctx) {
     if (!ctx) return GBH_ERR_ARG;
     ctx->err.clear();
+    ctx->evused = 0;
     ctx->launches = 0;
     ctx->h2d = ctx->d2h = 0;
     ctx->last = gbh_timings{};
@@ -129,6 +133,17 @@ int begin(gbh_ctx *ctx) {
 }
 
 Launch launch_of(gbh_ctx *ctx) { return Launch{ctx->stream, &ctx->launches, ctx->num_sms}; }
+
+// Records the next stage event of the call on the context's stream.
+cudaError_t stage_event(gbh_ctx *ctx) {
+    if (ctx->evused == ctx->evpool.size()) {
+        cudaEvent_t e;
+        cudaError_t r = cudaEventCreate(&e);
+        if (r != cudaSuccess) return r;
+        ctx->evpool.push_back(e);
+    }
+    return cudaEventRecord(ctx->evpool[ctx->evused++], ctx->stream);
+}
 
 int h2d(gbh_ctx *ctx, void *dst, const void *src, size_t bytes) {
     if (!bytes) return GBH_OK;
@@ -147,14 +162,13 @@ int d2h(gbh_ctx *ctx, void *dst, const void *src, size_t bytes) {
 // Tree build + walk on device arrays; accelerations of alive non-hole bodies, holes zeroed.
 int forces(gbh_ctx *ctx, const gbh_params *p, int64_t n, const double *px, const double *py, const double *pz,
            const double *mass, const uint8_t *kind, const uint8_t *alive, double *ax, double *ay, double *az,
-           double theta, float *build_ms_slot, float *walk_ms_slot) {
-    (void)build_ms_slot;
-    (void)walk_ms_slot;
+           double theta) {
     Launch L = launch_of(ctx);
     int leaf = leaf_of(p);
     CK(gbh::tree_alloc(ctx->tb, n, leaf));
+    CK(stage_event(ctx));
     CK(gbh::tree_build(L, ctx->tb, n, px, py, pz, mass, kind, alive, ax, ay, az, theta, leaf, p->dark_matter_off));
-    CK(cudaEventRecord(ctx->ev[1], ctx->stream));
+    CK(stage_event(ctx));
     double eps2 = p->softening * p->softening;
     int quad = !p->monopole_only;
     switch (p->walk) {
@@ -169,12 +183,12 @@ int forces(gbh_ctx *ctx, const gbh_params *p, int64_t n, const double *px, const
             CK(gbh::walk_mixed(L, ctx->tb, ctx->tb.cap_n, float(eps2), quad, ax, ay, az));
             break;
     }
-    CK(cudaEventRecord(ctx->ev[2], ctx->stream));
+    CK(stage_event(ctx));
     return GBH_OK;
 }
 
 // Waits for the stream, reads the device scalars and fills the timings of the call.
-int finish(gbh_ctx *ctx, bool tree, bool staged) {
+int finish(gbh_ctx *ctx, bool tree) {
     CK(cudaEventRecord(ctx->ev[5], ctx->stream));
     if (tree && ctx->tb.info) {
         CK(cudaMemcpyAsync(&ctx->info_host, ctx->tb.info, sizeof(DevInfo), cudaMemcpyDeviceToHost, ctx->stream));
@@ -183,10 +197,11 @@ int finish(gbh_ctx *ctx, bool tree, bool staged) {
     float ms = 0;
     gbh_timings &t = ctx->last;
     if (cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[5]) == cudaSuccess) t.total_ms = ms;
-    if (staged) {
-        if (cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[1]) == cudaSuccess) t.build_ms = ms;
-        if (cudaEventElapsedTime(&ms, ctx->ev[1], ctx->ev[2]) == cudaSuccess) t.walk_ms = ms;
+    for (size_t k = 0; k + 2 < ctx->evused; k += 3) {
+        if (cudaEventElapsedTime(&ms, ctx->evpool[k], ctx->evpool[k + 1]) == cudaSuccess) t.build_ms += ms;
+        if (cudaEventElapsedTime(&ms, ctx->evpool[k + 1], ctx->evpool[k + 2]) == cudaSuccess) t.walk_ms += ms;
     }
+    t.step_ms = t.total_ms - t.build_ms - t.walk_ms;
     t.launches = ctx->launches;
     t.h2d_bytes = ctx->h2d;
     t.d2h_bytes = ctx->d2h;
@@ -214,10 +229,8 @@ int run_steps(gbh_ctx *ctx, const gbh_params *p, double dt, int64_t nsteps) {
     const uint8_t *kind = ctx->state_has_kind ? ctx->kind : nullptr;
     const uint8_t *alive = ctx->state_has_alive ? ctx->alive : nullptr;
     double theta = theta_of(p);
-    float dummy = 0;
     if (!ctx->acc_valid) {  // initForces (gas.go:14-17)
-        int rc = forces(ctx, p, n, ctx->px, ctx->py, ctx->pz, ctx->mass, kind, alive, ctx->ax, ctx->ay, ctx->az, theta,
-                        &dummy, &dummy);
+        int rc = forces(ctx, p, n, ctx->px, ctx->py, ctx->pz, ctx->mass, kind, alive, ctx->ax, ctx->ay, ctx->az, theta);
         if (rc) return rc;
         ctx->acc_valid = true;
     }
@@ -225,8 +238,7 @@ int run_steps(gbh_ctx *ctx, const gbh_params *p, double dt, int64_t nsteps) {
     for (int64_t s = 0; s < nsteps; ++s) {
         CK(gbh::kick_drift(L, n, h, dt, ctx->px, ctx->py, ctx->pz, ctx->vx, ctx->vy, ctx->vz, ctx->ax, ctx->ay,
                            ctx->az));
-        int rc = forces(ctx, p, n, ctx->px, ctx->py, ctx->pz, ctx->mass, kind, alive, ctx->ax, ctx->ay, ctx->az, theta,
-                        &dummy, &dummy);
+        int rc = forces(ctx, p, n, ctx->px, ctx->py, ctx->pz, ctx->mass, kind, alive, ctx->ax, ctx->ay, ctx->az, theta);
         if (rc) return rc;
         CK(gbh::kick(L, n, h, ctx->vx, ctx->vy, ctx->vz, ctx->ax, ctx->ay, ctx->az));
     }
@@ -330,6 +342,7 @@ void gbh_destroy(gbh_ctx *c) {
         if (p) cudaFree(p);
     for (auto &ev : c->ev)
         if (ev) cudaEventDestroy(ev);
+    for (auto &ev : c->evpool) cudaEventDestroy(ev);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
 }
@@ -366,12 +379,11 @@ int gbh_accelerations(gbh_ctx *ctx, const gbh_params *p, int64_t n, const double
     if ((rc = h2d(ctx, ctx->ax, ax, b)) || (rc = h2d(ctx, ctx->ay, ay, b)) || (rc = h2d(ctx, ctx->az, az, b))) return rc;
     if (kind && (rc = h2d(ctx, ctx->kind, kind, size_t(n)))) return rc;
     if (alive && (rc = h2d(ctx, ctx->alive, alive, size_t(n)))) return rc;
-    float dummy;
     rc = forces(ctx, p, n, ctx->px, ctx->py, ctx->pz, ctx->mass, kind ? ctx->kind : nullptr,
-                alive ? ctx->alive : nullptr, ctx->ax, ctx->ay, ctx->az, theta_of(p), &dummy, &dummy);
+                alive ? ctx->alive : nullptr, ctx->ax, ctx->ay, ctx->az, theta_of(p));
     if (rc) return rc;
     if ((rc = d2h(ctx, ax, ctx->ax, b)) || (rc = d2h(ctx, ay, ctx->ay, b)) || (rc = d2h(ctx, az, ctx->az, b))) return rc;
-    return finish(ctx, true, false);
+    return finish(ctx, true);
 }
 
 int gbh_potential_energy(gbh_ctx *ctx, const gbh_params *p, int64_t n, const double *px, const double *py,
@@ -414,7 +426,7 @@ int gbh_potential_energy(gbh_ctx *ctx, const gbh_params *p, int64_t n, const dou
                            alive ? ctx->alive : nullptr, ctx->holes, int32_t(holes.size()), eps2, c,
                            p->dark_matter_off, !p->monopole_only, ctx->part, ctx->scalar));
     if ((rc = d2h(ctx, u, ctx->scalar, sizeof(double)))) return rc;
-    return finish(ctx, true, false);
+    return finish(ctx, true);
 }
 
 int gbh_direct_accelerations(gbh_ctx *ctx, const gbh_params *p, int64_t n, const double *px, const double *py,
@@ -450,7 +462,7 @@ int gbh_direct_accelerations(gbh_ctx *ctx, const gbh_params *p, int64_t n, const
                         tx, ty, tz));
     size_t tb = sizeof(double) * size_t(ntargets);
     if ((rc = d2h(ctx, ax, tx, tb)) || (rc = d2h(ctx, ay, ty, tb)) || (rc = d2h(ctx, az, tz, tb))) return rc;
-    return finish(ctx, false, false);
+    return finish(ctx, false);
 }
 
 int gbh_step_kdk(gbh_ctx *ctx, const gbh_params *p, double dt, int64_t nsteps, int32_t acc_valid, int64_t n,
@@ -469,7 +481,7 @@ int gbh_step_kdk(gbh_ctx *ctx, const gbh_params *p, double dt, int64_t nsteps, i
     if (rc) return rc;
     if (n > 0 && (rc = run_steps(ctx, p, dt, nsteps))) return rc;
     if ((rc = download_state(ctx, px, py, pz, vx, vy, vz, ax, ay, az))) return rc;
-    return finish(ctx, n > 0, false);
+    return finish(ctx, n > 0);
 }
 
 int gbh_state_upload(gbh_ctx *ctx, int64_t n, const double *px, const double *py, const double *pz, const double *vx,
@@ -479,7 +491,7 @@ int gbh_state_upload(gbh_ctx *ctx, int64_t n, const double *px, const double *py
     if (rc) return rc;
     CK(cudaEventRecord(ctx->ev[0], ctx->stream));
     if ((rc = upload_state(ctx, n, px, py, pz, vx, vy, vz, ax, ay, az, mass, kind, alive))) return rc;
-    return finish(ctx, false, false);
+    return finish(ctx, false);
 }
 
 int gbh_state_download(gbh_ctx *ctx, double *px, double *py, double *pz, double *vx, double *vy, double *vz, double *ax,
@@ -489,7 +501,7 @@ int gbh_state_download(gbh_ctx *ctx, double *px, double *py, double *pz, double 
     if (!ctx->have_state) return fail(ctx, GBH_ERR_STATE, "no resident state");
     CK(cudaEventRecord(ctx->ev[0], ctx->stream));
     if ((rc = download_state(ctx, px, py, pz, vx, vy, vz, ax, ay, az))) return rc;
-    return finish(ctx, false, false);
+    return finish(ctx, false);
 }
 
 int gbh_state_step(gbh_ctx *ctx, const gbh_params *p, double dt, int64_t nsteps) {
@@ -502,7 +514,7 @@ int gbh_state_step(gbh_ctx *ctx, const gbh_params *p, double dt, int64_t nsteps)
                     "alive black holes need the hole-aware split step (sim.stepSplit), which this path does not cover");
     CK(cudaEventRecord(ctx->ev[0], ctx->stream));
     if (ctx->n > 0 && (rc = run_steps(ctx, p, dt, nsteps))) return rc;
-    return finish(ctx, ctx->n > 0, false);
+    return finish(ctx, ctx->n > 0);
 }
 
 int gbh_state_accelerations(gbh_ctx *ctx, const gbh_params *p) {
@@ -511,12 +523,11 @@ int gbh_state_accelerations(gbh_ctx *ctx, const gbh_params *p) {
     if (!ctx->have_state) return fail(ctx, GBH_ERR_STATE, "no resident state (gbh_state_upload first)");
     if (ctx->n == 0) return GBH_OK;
     CK(cudaEventRecord(ctx->ev[0], ctx->stream));
-    float dummy;
     rc = forces(ctx, p, ctx->n, ctx->px, ctx->py, ctx->pz, ctx->mass, ctx->state_has_kind ? ctx->kind : nullptr,
-                ctx->state_has_alive ? ctx->alive : nullptr, ctx->ax, ctx->ay, ctx->az, theta_of(p), &dummy, &dummy);
+                ctx->state_has_alive ? ctx->alive : nullptr, ctx->ax, ctx->ay, ctx->az, theta_of(p));
     if (rc) return rc;
     ctx->acc_valid = true;
-    return finish(ctx, true, true);
+    return finish(ctx, true);
 }
 
 int gbh_tree_size(gbh_ctx *ctx, int64_t *nstars, int64_t *nnodes) {

@@ -47,6 +47,12 @@ inline unsigned blocks_for(int64_t n, int threads) {
     return unsigned(b < 1 ? 1 : b);
 }
 
+// Records a device-side consistency failure (checked by the host after the call).
+__device__ __forceinline__ void dev_error(DevInfo *info, int where) {
+    atomicExch(&info->err, 1);
+    info->err_where = where;
+}
+
 // ---------------------------------------------------------------- exclusive scan (uint32)
 
 __device__ __forceinline__ uint32_t warp_incl_scan(uint32_t v) {
@@ -281,7 +287,7 @@ __global__ __launch_bounds__(kRsThreads) void k_rs_hist(const uint64_t *__restri
 __global__ __launch_bounds__(kRsThreads) void k_rs_scatter(const uint64_t *__restrict__ kin,
                                                            const int32_t *__restrict__ vin,
                                                            uint64_t *__restrict__ kout, int32_t *__restrict__ vout,
-                                                           const DevInfo *info, int shift, uint32_t ntiles,
+                                                           DevInfo *info, int shift, uint32_t ntiles,
                                                            const uint32_t *__restrict__ offs) {
     __shared__ uint32_t s_run[kRsBins];
     __shared__ uint32_t s_goff[kRsBins];
@@ -331,8 +337,12 @@ __global__ __launch_bounds__(kRsThreads) void k_rs_scatter(const uint64_t *__res
         __syncthreads();
         if (valid) {
             uint32_t pos = s_goff[d] + s_w[buf][warp][d] + rank;
-            kout[pos] = k[it];
-            vout[pos] = v[it];
+            if (pos < n) {
+                kout[pos] = k[it];
+                vout[pos] = v[it];
+            } else {
+                dev_error(info, 10);
+            }
         }
     }
 }
@@ -512,7 +522,7 @@ __global__ __launch_bounds__(kThreads) void k_ref_index(const DevInfo *info, con
 }
 
 // Links and ranges of every node in the reference layout (bh.go:108-116).
-__global__ __launch_bounds__(kThreads) void k_emit_nodes(const uint64_t *__restrict__ keys, const DevInfo *info,
+__global__ __launch_bounds__(kThreads) void k_emit_nodes(const uint64_t *__restrict__ keys, DevInfo *info,
                                                          const uint32_t *__restrict__ cnt,
                                                          const uint32_t *__restrict__ base,
                                                          const int32_t *__restrict__ pre_parent,
@@ -524,6 +534,7 @@ __global__ __launch_bounds__(kThreads) void k_emit_nodes(const uint64_t *__restr
     int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     int64_t n = info->nstars;
     if (i >= n) return;
+    const int64_t nn = info->nnodes;
     uint32_t c = cnt[i];
     uint32_t p = base[i];
     for (uint32_t t = 0; t < c; ++t, ++p) {
@@ -532,9 +543,18 @@ __global__ __launch_bounds__(kThreads) void k_emit_nodes(const uint64_t *__restr
         uint32_t mask = inf >> 16;
         int64_t hi = cell_end(keys, n, i, L);
         int32_t r = pre_ref[p];
+        if (r < 0 || r >= nn) {
+            dev_error(info, 11);
+            continue;
+        }
         gbh_node &nd = nodes[r];
         nd.first = mask ? int32_t(1 + child_base[p]) : -1;
-        nd.next = hi == n ? -1 : pre_ref[base[hi]];
+        int32_t nx = hi == n ? -1 : pre_ref[base[hi]];
+        if (nx >= nn || (hi < n && cnt[hi] == 0)) {
+            dev_error(info, 12);
+            nx = -1;
+        }
+        nd.next = nx;
         nd.lo = int32_t(i);
         nd.hi = int32_t(hi);
         int32_t pp = pre_parent[p];
@@ -628,7 +648,7 @@ __global__ __launch_bounds__(kThreads) void k_upsweep(const uint64_t *__restrict
                                                       const double *__restrict__ sm, gbh_node *nodes,
                                                       const int32_t *__restrict__ n_parent,
                                                       const uint32_t *__restrict__ n_info, int32_t *n_arrive, PNode *pn,
-                                                      MNode *mn, int2 *mr) {
+                                                      MNode *mn, int2 *mr, DevInfo *err_info) {
     int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= info->nstars) return;
     uint32_t c = cnt[i];
@@ -670,6 +690,10 @@ __global__ __launch_bounds__(kThreads) void k_upsweep(const uint64_t *__restrict
         if (old != int(nch) - 1) break;
         __threadfence();
         int32_t first = nodes[par].first;
+        if (first < 0 || int64_t(first) + nch > inf.nnodes) {
+            dev_error(err_info, 13);
+            break;
+        }
         Moments q = {};
         for (int32_t ch = first; ch < first + int32_t(nch); ++ch) {
             double cm = __ldcg(&nodes[ch].m);
@@ -720,9 +744,8 @@ __global__ __launch_bounds__(kThreads) void k_walk_fp64(const DevInfo *info, con
     double fax = 0, fay = 0, faz = 0;
     int64_t steps = 0;
     for (int32_t i = nn > 0 ? 0 : -1; i >= 0;) {
-        if (++steps > nn) {  // each node is visited at most once
-            atomicExch(&err_info->err, 1);
-            err_info->err_where = 1;
+        if (++steps > nn || i >= nn) {  // each node is visited at most once
+            dev_error(err_info, 1);
             break;
         }
         const gbh_node &nd = nodes[i];
@@ -751,6 +774,10 @@ __global__ __launch_bounds__(kThreads) void k_walk_fp64(const DevInfo *info, con
         if (nd.first >= 0) {
             i = nd.first;
             continue;
+        }
+        if (nd.lo < 0 || nd.hi > ns || nd.lo > nd.hi) {
+            dev_error(err_info, 7);
+            break;
         }
         for (int32_t j = nd.lo; j < nd.hi; ++j) {
             if (j == k) continue;
@@ -893,9 +920,8 @@ __global__ __launch_bounds__(kThreads) void k_potential_walk(const DevInfo *info
         double x = sx[k], y = sy[k], z = sz[k], psi = 0;
         int64_t steps = 0;
         for (int32_t i = nn > 0 ? 0 : -1; i >= 0;) {
-            if (++steps > nn) {
-                atomicExch(&err_info->err, 1);
-                err_info->err_where = 2;
+            if (++steps > nn || i >= nn) {
+                dev_error(err_info, 2);
                 break;
             }
             const gbh_node &nd = nodes[i];
@@ -1115,7 +1141,7 @@ cudaError_t tree_build(const Launch &L, TreeBufs &b, int64_t n, const double *px
                                          b.nodes, b.n_parent, b.n_info, b.n_arrive);
     GBH_LAUNCH_CHECK();
     k_upsweep<<<nb, kThreads, 0, s>>>(b.keys, b.info, cnt, base, b.pre_ref, b.sx, b.sy, b.sz, b.sm, b.nodes,
-                                      b.n_parent, b.n_info, b.n_arrive, b.pnodes, b.mnodes, b.mrange);
+                                      b.n_parent, b.n_info, b.n_arrive, b.pnodes, b.mnodes, b.mrange, b.info);
     GBH_LAUNCH_CHECK();
     return cudaSuccess;
 }

@@ -5,10 +5,11 @@
 // walk_mixed: one warp per group of 32 consecutive Morton-sorted stars walking the skip-pointer
 //   tree in lockstep. A node is opened when any star of the group would open it under the
 //   reference criterion d2 < crit2 (bh.go:165), so every star sees each accepted node exactly
-//   where the reference would accept it or deeper. Positions enter as FP32 offsets from the
-//   group's anchor star, formed from FP64 positions split into hi + lo FP32 parts, so a
-//   separation is as precise as the offsets themselves however far the system is from the
-//   origin. Each star accumulates in FP32 blocks of 32 interactions folded into a Kahan sum.
+//   where the reference would accept it or deeper. Positions are FP64 split into hi + lo FP32
+//   parts; a separation is formed per star as (hi_a - hi_b) + (lo_a - lo_b), whose hi difference
+//   is exact for nearby points (Sterbenz) and relatively small for distant ones, so separations
+//   stay accurate however far a system lies from the origin. Each star accumulates in FP32
+//   blocks of 32 interactions folded into a Kahan sum.
 #include <cuda_runtime.h>
 
 #include "gbh_internal.cuh"
@@ -45,7 +46,7 @@ __global__ __launch_bounds__(kPlainThreads) void k_walk_plain(const DevInfo *inf
     int64_t steps = 0;
     int i = nn > 0 ? 0 : -1;
     while (i >= 0) {
-        if (++steps > nn) {
+        if (++steps > nn || i >= nn) {
             set_err(err_info, 3);
             break;
         }
@@ -69,6 +70,10 @@ __global__ __launch_bounds__(kPlainThreads) void k_walk_plain(const DevInfo *inf
         if (nd.links.x >= 0) {
             i = nd.links.x;
             continue;
+        }
+        if (nd.links.z < 0 || nd.links.w > ns || nd.links.z > nd.links.w) {
+            set_err(err_info, 6);
+            break;
         }
         for (int j = nd.links.z; j < nd.links.w; ++j) {
             if (j == int(k)) continue;
@@ -114,8 +119,6 @@ __global__ __launch_bounds__(kMixedThreads) void k_walk_mixed(const DevInfo *inf
     const bool valid = k < ns;
     const int64_t kk = valid ? k : base;
     const float4 h = st_hi[kk], l = st_lo[kk];
-    const float gx = __shfl_sync(kFull, h.x, 0), gy = __shfl_sync(kFull, h.y, 0), gz = __shfl_sync(kFull, h.z, 0);
-    const float tx = (h.x - gx) + l.x, ty = (h.y - gy) + l.y, tz = (h.z - gz) + l.z;
 
     float sx = 0.f, sy = 0.f, sz = 0.f, cx = 0.f, cy = 0.f, cz = 0.f;  // Kahan sums
     float px = 0.f, py = 0.f, pz = 0.f;                                // block partials
@@ -123,14 +126,14 @@ __global__ __launch_bounds__(kMixedThreads) void k_walk_mixed(const DevInfo *inf
     int64_t steps = 0;
     int i = nn > 0 ? 0 : -1;
     while (i >= 0) {
-        if (++steps > nn) {
+        if (++steps > nn || i >= nn) {
             if (lane == 0) set_err(err_info, 4);
             break;
         }
         const MNode nd = nodes[i];
-        const float dx = ((nd.a.x - gx) + nd.b.x) - tx;
-        const float dy = ((nd.a.y - gy) + nd.b.y) - ty;
-        const float dz = ((nd.a.z - gz) + nd.b.z) - tz;
+        const float dx = (nd.a.x - h.x) + (nd.b.x - l.x);
+        const float dy = (nd.a.y - h.y) + (nd.b.y - l.y);
+        const float dz = (nd.a.z - h.z) + (nd.b.z - l.z);
         const float d2 = dx * dx + dy * dy + dz * dz;
         const bool open = __any_sync(kFull, d2 < nd.a.w);
         const int first = __float_as_int(nd.d.z), next = __float_as_int(nd.d.w);
@@ -166,11 +169,15 @@ __global__ __launch_bounds__(kMixedThreads) void k_walk_mixed(const DevInfo *inf
             continue;
         }
         const int2 r = ranges[i];
+        if (r.x < 0 || r.y > ns || r.x > r.y) {
+            if (lane == 0) set_err(err_info, 5);
+            break;
+        }
         for (int j = r.x; j < r.y; ++j) {
             const float4 sh = st_hi[j], sl = st_lo[j];
-            const float ex = ((sh.x - gx) + sl.x) - tx;
-            const float ey = ((sh.y - gy) + sl.y) - ty;
-            const float ez = ((sh.z - gz) + sl.z) - tz;
+            const float ex = (sh.x - h.x) + (sl.x - l.x);
+            const float ey = (sh.y - h.y) + (sl.y - l.y);
+            const float ez = (sh.z - h.z) + (sl.z - l.z);
             const float r2 = ex * ex + ey * ey + ez * ez + eps2;
             // The star itself gives ex = ey = ez = 0 exactly; with eps2 > 0 that adds 0, as
             // skipping j == self does (bh.go:191-193). Without softening r2 = 0 is masked.
