@@ -76,6 +76,7 @@ SIGNATURES = {
     "gbh_tree_export": (ctypes.c_int, [_P, _P, _P, _P, _I64]),
     "gbh_last_timings": (ctypes.c_int, [_P, ctypes.POINTER(Timings)]),
     "gbh_probe_fp32_peak": (ctypes.c_int, [_P, _D, _P]),
+    "gbh_morton_order_noalloc": (ctypes.c_int, [_I32, _P, _I64] + [_P] * 8 + [ctypes.c_char_p, ctypes.c_int]),
 }
 
 _lib = None

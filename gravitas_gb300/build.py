@@ -4,7 +4,8 @@ Each translation unit gets its own floating-point flags:
   tree.cu  -fmad=false   FP64 keys, moments, FP64 walk, direct sum and kick/drift keep the
                          reference's rounded multiply-then-add order (bit-exact parity);
   walk.cu  fast FP32     FMA contraction on, approximate FP32 division and square root;
-  api.cu                 host code.
+  api.cu                 host code;
+  noalloc.cu             the entry point whose temporaries live in a static device array.
 Objects compile in parallel; the shared library links the CUDA runtime statically.
 """
 from __future__ import annotations
@@ -25,6 +26,7 @@ UNITS = {
     "tree.cu": ["-fmad=false"],
     "walk.cu": ["-prec-div=false", "-prec-sqrt=false", "-ftz=true"],
     "api.cu": [],
+    "noalloc.cu": [],
 }
 
 

@@ -117,6 +117,14 @@ cudaError_t scan_u32(const Launch &L, const uint32_t *in, uint32_t *out, int64_t
                      uint32_t *tmp, int64_t tmp_cap);
 int64_t scan_tmp_size(int64_t n);
 
+// Stable Morton order of the alive non-hole bodies (collect, keys and radix sort of tree_build)
+// with all temporaries in one caller-provided device block of scratch_bytes; keys/order get the
+// sorted keys and state indices, *info_out points at the DevInfo inside the block.
+size_t morton_sort_scratch_bytes(int64_t nmax);
+cudaError_t morton_sort(const Launch &L, int64_t n, const double *px, const double *py, const double *pz,
+                        const uint8_t *kind, const uint8_t *alive, uint64_t *keys, int32_t *order, void *scratch,
+                        size_t scratch_bytes, DevInfo **info_out);
+
 // ---- walk.cu (FP32 walks, FMA contraction on) ----
 cudaError_t walk_plain(const Launch &L, const TreeBufs &b, int64_t nstars_cap, float eps2,
                        double *ax, double *ay, double *az);

@@ -1198,3 +1198,122 @@ cudaError_t potential_fp64(const Launch &L, const TreeBufs &b, int64_t n, const 
 }
 
 }  // namespace gbh
+
+namespace gbh {
+
+// ---------------------------------------------------------------- Morton order into caller-owned scratch
+
+namespace {
+inline size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+
+// Star flags and per-block bbox partials, as k_flags_bbox but writing no accelerations.
+__global__ __launch_bounds__(kThreads) void k_flags_bbox_noacc(int64_t n, const double *__restrict__ px,
+                                                               const double *__restrict__ py,
+                                                               const double *__restrict__ pz,
+                                                               const uint8_t *__restrict__ kind,
+                                                               const uint8_t *__restrict__ alive,
+                                                               uint32_t *__restrict__ flag, double *__restrict__ part) {
+    double mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
+        bool st = is_star(alive ? alive[i] : 1, kind ? kind[i] : 0);
+        flag[i] = st;
+        if (st) {
+            double x = px[i], y = py[i], z = pz[i];
+            mn[0] = fmin(mn[0], x);
+            mx[0] = fmax(mx[0], x);
+            mn[1] = fmin(mn[1], y);
+            mx[1] = fmax(mx[1], y);
+            mn[2] = fmin(mn[2], z);
+            mx[2] = fmax(mx[2], z);
+        }
+    }
+    __shared__ double s[6][kThreads / 32];
+    int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        for (int o = 16; o > 0; o >>= 1) {
+            mn[c] = fmin(mn[c], __shfl_xor_sync(0xffffffffu, mn[c], o));
+            mx[c] = fmax(mx[c], __shfl_xor_sync(0xffffffffu, mx[c], o));
+        }
+        if (lane == 0) {
+            s[c][warp] = mn[c];
+            s[3 + c][warp] = mx[c];
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x < 6) {
+        bool isMin = threadIdx.x < 3;
+        double v = s[threadIdx.x][0];
+        for (int w = 1; w < kThreads / 32; ++w) v = isMin ? fmin(v, s[threadIdx.x][w]) : fmax(v, s[threadIdx.x][w]);
+        part[blockIdx.x * 6 + threadIdx.x] = v;
+    }
+}
+}  // namespace
+
+size_t morton_sort_scratch_bytes(int64_t nmax) {
+    int64_t tiles = (nmax + kRsTile - 1) / kRsTile;
+    size_t b = align256(sizeof(DevInfo));
+    b += align256(sizeof(double) * kFlagBlocksMax * 6);
+    b += align256(sizeof(uint32_t) * size_t(nmax));
+    b += align256(sizeof(uint64_t) * size_t(nmax));
+    b += align256(sizeof(int32_t) * size_t(nmax));
+    b += align256(sizeof(uint32_t) * size_t(tiles) * kRsBins);
+    b += align256(sizeof(uint32_t) * size_t(scan_tmp_size(nmax > tiles * kRsBins ? nmax : tiles * kRsBins)));
+    return b;
+}
+
+// The collect, key and stable-sort stages of tree_build (the same kernels), with every
+// temporary carved out of one caller-provided device block instead of TreeBufs.
+cudaError_t morton_sort(const Launch &L, int64_t n, const double *px, const double *py, const double *pz,
+                        const uint8_t *kind, const uint8_t *alive, uint64_t *keys, int32_t *order, void *scratch,
+                        size_t scratch_bytes, DevInfo **info_out) {
+    if (morton_sort_scratch_bytes(n) > scratch_bytes) return cudaErrorInvalidValue;
+    char *p = static_cast<char *>(scratch);
+    DevInfo *info = reinterpret_cast<DevInfo *>(p);
+    p += align256(sizeof(DevInfo));
+    double *bbox_part = reinterpret_cast<double *>(p);
+    p += align256(sizeof(double) * kFlagBlocksMax * 6);
+    uint32_t *flag = reinterpret_cast<uint32_t *>(p);
+    p += align256(sizeof(uint32_t) * size_t(n));
+    uint64_t *keys_alt = reinterpret_cast<uint64_t *>(p);
+    p += align256(sizeof(uint64_t) * size_t(n));
+    int32_t *order_alt = reinterpret_cast<int32_t *>(p);
+    p += align256(sizeof(int32_t) * size_t(n));
+    const uint32_t ntiles = uint32_t((n + kRsTile - 1) / kRsTile);
+    uint32_t *hist = reinterpret_cast<uint32_t *>(p);
+    p += align256(sizeof(uint32_t) * size_t(ntiles) * kRsBins);
+    uint32_t *tmp = reinterpret_cast<uint32_t *>(p);
+    int64_t tmp_cap = int64_t((static_cast<char *>(scratch) + scratch_bytes - p) / sizeof(uint32_t));
+    *info_out = info;
+    cudaStream_t s = L.stream;
+    cudaError_t e = cudaMemsetAsync(info, 0, sizeof(DevInfo), s);
+    if (e != cudaSuccess || n == 0) return e;
+    unsigned fb = blocks_for(n, kThreads);
+    if (fb > unsigned(kFlagBlocksMax)) fb = kFlagBlocksMax;
+    k_flags_bbox_noacc<<<fb, kThreads, 0, s>>>(n, px, py, pz, kind, alive, flag, bbox_part);
+    GBH_LAUNCH_CHECK();
+    if ((e = scan_u32(L, flag, flag, n, tmp, tmp_cap)) != cudaSuccess) return e;
+    k_bbox_final<<<1, 32, 0, s>>>(int(fb), bbox_part, n, flag, kind, alive, 0.9, info);
+    GBH_LAUNCH_CHECK();
+    k_compact_keys<<<blocks_for(n, kThreads), kThreads, 0, s>>>(n, px, py, pz, kind, alive, flag, info, keys, order);
+    GBH_LAUNCH_CHECK();
+    uint64_t *kin = keys, *kout = keys_alt;
+    int32_t *vin = order, *vout = order_alt;
+    for (int shift = 0; shift < 64; shift += 8) {
+        k_rs_hist<<<ntiles ? ntiles : 1, kRsThreads, 0, s>>>(kin, info, shift, ntiles ? ntiles : 1, hist);
+        GBH_LAUNCH_CHECK();
+        if ((e = scan_u32(L, hist, hist, int64_t(ntiles ? ntiles : 1) * kRsBins, tmp, tmp_cap)) != cudaSuccess) return e;
+        k_rs_scatter<<<ntiles ? ntiles : 1, kRsThreads, 0, s>>>(kin, vin, kout, vout, info, shift, ntiles ? ntiles : 1,
+                                                                 hist);
+        GBH_LAUNCH_CHECK();
+        uint64_t *tk = kin;
+        kin = kout;
+        kout = tk;
+        int32_t *tv = vin;
+        vin = vout;
+        vout = tv;
+    }
+    return cudaSuccess;  // eight passes: the result is back in keys/order
+}
+
+}  // namespace gbh

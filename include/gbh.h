@@ -187,6 +187,34 @@ int gbh_last_timings(gbh_ctx *ctx, gbh_timings *t);
    of the walk. */
 int gbh_probe_fp32_peak(gbh_ctx *ctx, double ms, double *tflops);
 
+/* ---- Without device allocation. ---- */
+
+/*
+ * No counterpart in the reference. For callers that must not call cudaMalloc: code whose
+ * device memory belongs to another framework's allocator that has already reserved most of
+ * the GPU, code that cannot take the device-wide synchronisation cudaMalloc/cudaFree may
+ * imply while other streams run, and loops that must never allocate after start-up.
+ *
+ * Sorted Morton keys and state indices of the alive non-hole bodies, exactly the keys and
+ * order gbh_tree_export returns after gbh_accelerations on the same arrays (collect, keys
+ * and the stable radix sort of the tree build). All pointers except nstars, err and stream
+ * are device pointers owned by the caller: px/py/pz hold n doubles, kind/alive n bytes (each
+ * may be NULL: all stars, all alive), keys and order room for n entries; *nstars (host)
+ * receives the number of sorted bodies. stream is a cudaStream_t (NULL: the legacy default
+ * stream); the call returns after the work on it has finished.
+ *
+ * It allocates nothing: its temporaries live in one static device array of 4.5 MiB that
+ * every GPU which loads the library holds until the process exits, enough for at most
+ * 262,144 bodies; larger n returns GBH_ERR_ARG. The first call on a device looks up that
+ * array's device address, so make it before any stream capture. All calls share the array:
+ * calls that overlap on the GPU (for instance on two streams of one device) race and must
+ * be serialised by the caller. Errors are returned as a code with a message in err.
+ */
+int gbh_morton_order_noalloc(int32_t device, void *stream, int64_t n, const double *px,
+                             const double *py, const double *pz, const uint8_t *kind,
+                             const uint8_t *alive, uint64_t *keys, int32_t *order,
+                             int64_t *nstars, char *err, int errlen);
+
 #ifdef __cplusplus
 }
 #endif
