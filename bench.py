@@ -303,6 +303,26 @@ def run(args):
     return 0
 
 
+def run_profile(args):
+    """A short launch sequence for ncu captures: upload the workload, then two force
+    evaluations with the chosen walk (tree build + walk each)."""
+    from gravitas_gb300 import abi
+    P = abi.ptr
+    n = args.n
+    s = make_workload(n, seed=0)
+    ctx = abi.Context(0)
+    ctx.call("gbh_state_upload", n, *[P(s[k]) for k in ("px", "py", "pz", "vx", "vy", "vz")], None, None, None,
+             P(s["mass"]), None, None)
+    par = abi.make_params(THETA, EPS, args.leaf, False, False, args.profile)
+    for _ in range(2):
+        ctx.call("gbh_state_accelerations", par)
+    t = ctx.timings()
+    print(json.dumps({"profile": args.profile, "n": n, "leaf": args.leaf, "build_ms": t["build_ms"],
+                      "walk_ms": t["walk_ms"], "nnodes": t["nnodes"], "launches": t["launches"]}))
+    ctx.close()
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
@@ -311,7 +331,11 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--n", type=int, default=N_DEFAULT)
     ap.add_argument("--leaf", type=int, default=LEAF)
+    ap.add_argument("--profile", choices=["mixed", "plain", "fp64"], default=None,
+                    help="run only two force evaluations with this walk (for ncu captures)")
     args = ap.parse_args()
+    if args.profile:
+        return run_profile(args)
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3
     if args.impl == "reference":

@@ -167,7 +167,8 @@ int forces(gbh_ctx *ctx, const gbh_params *p, int64_t n, const double *px, const
     int leaf = leaf_of(p);
     CK(gbh::tree_alloc(ctx->tb, n, leaf));
     CK(stage_event(ctx));
-    CK(gbh::tree_build(L, ctx->tb, n, px, py, pz, mass, kind, alive, ax, ay, az, theta, leaf, p->dark_matter_off));
+    CK(gbh::tree_build(L, ctx->tb, n, px, py, pz, mass, kind, alive, ax, ay, az, theta, leaf, p->dark_matter_off,
+                       p->walk == GBH_WALK_FP64, p->walk == GBH_WALK_PLAIN));
     CK(stage_event(ctx));
     double eps2 = p->softening * p->softening;
     int quad = !p->monopole_only;
@@ -417,7 +418,7 @@ int gbh_potential_energy(gbh_ctx *ctx, const gbh_params *p, int64_t n, const dou
     double theta = std::min(theta_of(p), 0.9);  // diagTheta, potential.go:12-14
     CK(gbh::tree_alloc(ctx->tb, n, leaf));
     CK(gbh::tree_build(L, ctx->tb, n, ctx->px, ctx->py, ctx->pz, ctx->mass, kind ? ctx->kind : nullptr,
-                       alive ? ctx->alive : nullptr, ctx->ax, ctx->ay, ctx->az, theta, leaf, p->dark_matter_off));
+                       alive ? ctx->alive : nullptr, ctx->ax, ctx->ay, ctx->az, theta, leaf, p->dark_matter_off, true));
     int64_t nparts = (ctx->tb.cap_n + 255) / 256;
     CK(grow(ctx->part, ctx->part_cap, nparts));
     if (!ctx->scalar) CK(cudaMalloc(&ctx->scalar, 64));
@@ -549,7 +550,14 @@ int gbh_tree_export(gbh_ctx *ctx, uint64_t *keys, int32_t *order, gbh_node *node
     if (keys && ns) CK(cudaMemcpy(keys, ctx->tb.keys, sizeof(uint64_t) * size_t(ns), cudaMemcpyDeviceToHost));
     if (order && ns) CK(cudaMemcpy(order, ctx->tb.order, sizeof(int32_t) * size_t(ns), cudaMemcpyDeviceToHost));
     int64_t cnt = std::min(nn, node_cap);
-    if (nodes && cnt > 0) CK(cudaMemcpy(nodes, ctx->tb.nodes, sizeof(gbh_node) * size_t(cnt), cudaMemcpyDeviceToHost));
+    if (nodes && cnt > 0) {
+        if (!ctx->tb.moments_exact) {  // FP32 upsweep: fill the FP64 fields from the walk records
+            Launch L = launch_of(ctx);
+            CK(gbh::export_fast_moments(L, ctx->tb));
+            CK(cudaStreamSynchronize(ctx->stream));
+        }
+        CK(cudaMemcpy(nodes, ctx->tb.nodes, sizeof(gbh_node) * size_t(cnt), cudaMemcpyDeviceToHost));
+    }
     return GBH_OK;
 }
 

@@ -29,7 +29,12 @@ struct DevInfo {
     int32_t err;              // device-side limit hit (walk step bound, stack bound)
     int32_t err_where;        // which kernel set err
     uint32_t work;            // work counter of persistent kernels
-    uint32_t pad;
+    uint32_t nleaves;         // leaves appended to the leaf list
+    // FP32 views for the FP32 upsweep: min corner and side as hi + lo pairs, and the
+    // opening base 2 * half_L / theta per level L
+    float min_hi[3], min_lo[3];
+    float side_hi, side_lo;
+    float crit_base[kMaxLevel + 1];
 };
 
 // The Metal kernel's GNode (gpu_darwin.go:79,121-124): com (x,y,z,m), q1 (qxx,qyy,qzz,qxy),
@@ -74,6 +79,8 @@ struct TreeBufs {
     PNode *pnodes = nullptr;
     MNode *mnodes = nullptr;
     int2 *mrange = nullptr;
+    int32_t *leaves = nullptr;      // sorted position of every leaf's first star
+    bool moments_exact = false;     // the last build ran the bit-exact FP64 upsweep
     // scan temporaries
     uint32_t *scan_tmp = nullptr;
     int64_t scan_tmp_cap = 0;
@@ -90,11 +97,18 @@ struct Launch {
 // ---- tree.cu (FP64 parts compiled without FMA contraction) ----
 cudaError_t tree_alloc(TreeBufs &b, int64_t n, int leaf_size);
 void tree_free(TreeBufs &b);
-// Builds the tree of the alive non-hole bodies; zeroes alive holes' accelerations.
+// Builds the tree of the alive non-hole bodies; zeroes alive holes' accelerations. exact:
+// FP64 moments bit identical to the reference (the FP64 walk); otherwise the FP32 upsweep of
+// moments.cu, which feeds the FP32 walks.
 cudaError_t tree_build(const Launch &L, TreeBufs &b, int64_t n, const double *px, const double *py,
                        const double *pz, const double *mass, const uint8_t *kind,
                        const uint8_t *alive, double *ax, double *ay, double *az, double theta,
-                       int leaf_size, int dm_off);
+                       int leaf_size, int dm_off, bool exact, bool plain_records = true);
+// ---- moments.cu ----
+// FP32 upsweep; writes the walk records of the plain walk (PNode) and/or the mixed walk (MNode).
+cudaError_t upsweep_fast(const Launch &L, TreeBufs &b, bool plain_records);
+// Fills the FP64 moment fields of the node table from the MNode records (after an FP32 upsweep).
+cudaError_t export_fast_moments(const Launch &L, TreeBufs &b);
 cudaError_t walk_fp64(const Launch &L, const TreeBufs &b, int64_t n, double eps2, int quad,
                       double *ax, double *ay, double *az);
 cudaError_t kick(const Launch &L, int64_t n, double h, double *vx, double *vy, double *vz,

@@ -200,15 +200,40 @@ __global__ __launch_bounds__(kThreads) void k_flags_bbox(int64_t n, const double
 }
 
 // Root cube (build.go:19-21): side = max(max extent * (1+1e-9), 1e-12), scale = 2^21 / side.
-__global__ void k_bbox_final(int nparts, const double *__restrict__ part, int64_t n, const uint32_t *__restrict__ scan,
-                             const uint8_t *kind, const uint8_t *alive, double theta, DevInfo *info) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+// One block reduces the per-block partials (min/max are exact, so the order does not matter).
+constexpr int kFinalThreads = 1024;
+__global__ __launch_bounds__(kFinalThreads) void k_bbox_final(int nparts, const double *__restrict__ part, int64_t n,
+                                                              const uint32_t *__restrict__ scan, const uint8_t *kind,
+                                                              const uint8_t *alive, double theta, DevInfo *info) {
     double mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
-    for (int b = 0; b < nparts; ++b)
+    for (int b = threadIdx.x; b < nparts; b += blockDim.x)
         for (int c = 0; c < 3; ++c) {
             mn[c] = fmin(mn[c], part[b * 6 + c]);
             mx[c] = fmax(mx[c], part[b * 6 + 3 + c]);
         }
+    __shared__ double s[6][kFinalThreads / 32];
+    int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int c = 0; c < 3; ++c) {
+        for (int o = 16; o > 0; o >>= 1) {
+            mn[c] = fmin(mn[c], __shfl_xor_sync(0xffffffffu, mn[c], o));
+            mx[c] = fmax(mx[c], __shfl_xor_sync(0xffffffffu, mx[c], o));
+        }
+        if (lane == 0) {
+            s[c][warp] = mn[c];
+            s[3 + c][warp] = mx[c];
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x != 0) return;
+    for (int w = 1; w < int(blockDim.x / 32); ++w)
+        for (int c = 0; c < 3; ++c) {
+            s[c][0] = fmin(s[c][0], s[c][w]);
+            s[3 + c][0] = fmax(s[3 + c][0], s[3 + c][w]);
+        }
+    for (int c = 0; c < 3; ++c) {
+        mn[c] = s[c][0];
+        mx[c] = s[3 + c][0];
+    }
     int64_t ns = 0;
     if (n > 0) ns = int64_t(scan[n - 1]) + (is_star(alive ? alive[n - 1] : 1, kind ? kind[n - 1] : 0) ? 1 : 0);
     double side = fmax(mx[0] - mn[0], fmax(mx[1] - mn[1], mx[2] - mn[2]));
@@ -224,6 +249,17 @@ __global__ void k_bbox_final(int nparts, const double *__restrict__ part, int64_
     info->err = 0;
     info->err_where = 0;
     info->work = 0;
+    info->nleaves = 0;
+    for (int c = 0; c < 3; ++c) {
+        float h = __double2float_rn(mn[c]);
+        info->min_hi[c] = h;
+        info->min_lo[c] = __double2float_rn(mn[c] - double(h));
+    }
+    float sh = __double2float_rn(side);
+    info->side_hi = sh;
+    info->side_lo = __double2float_rn(side - double(sh));
+    double half = side / 2;
+    for (int L = 0; L <= kMaxLevel; ++L, half = half / 2) info->crit_base[L] = __double2float_rn(2 * half / theta);
 }
 
 // morton.go:7-15.
@@ -465,11 +501,21 @@ __global__ __launch_bounds__(kThreads) void k_chain_emit(const uint64_t *__restr
                                                          const uint32_t *__restrict__ base,
                                                          int32_t *__restrict__ pre_parent,
                                                          uint32_t *__restrict__ pre_info,
-                                                         uint32_t *__restrict__ pre_nchild) {
+                                                         uint32_t *__restrict__ pre_nchild,
+                                                         int32_t *__restrict__ leaves) {
     int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     int64_t n = info->nstars;
+    uint32_t c = i < n ? cnt[i] : 0;
+    // every position with nodes ends its chain in exactly one leaf: append it to the leaf list
+    unsigned m = __ballot_sync(0xffffffffu, c > 0);
+    if (m) {
+        int lane = threadIdx.x & 31;
+        uint32_t off = 0;
+        if (lane == __ffs(m) - 1) off = atomicAdd(&info->nleaves, uint32_t(__popc(m)));
+        off = __shfl_sync(0xffffffffu, off, __ffs(m) - 1);
+        if (c > 0) leaves[off + __popc(m & ((1u << lane) - 1u))] = int32_t(i);
+    }
     if (i >= n) return;
-    uint32_t c = cnt[i];
     if (i == n - 1) info->nnodes = int64_t(base[i]) + c;
     if (c == 0) return;
     int L0 = start_level(keys, i);
@@ -1012,7 +1058,7 @@ static cudaError_t scan_dyn(const Launch &L, const uint32_t *in, uint32_t *out, 
 
 void tree_free(TreeBufs &b) {
     void *ptrs[] = {b.flag, b.bbox_part, b.keys, b.keys_alt, b.order, b.order_alt, b.hist, b.sx, b.sy, b.sz, b.sm,
-                    b.st_hi, b.st_lo, b.chain_cnt, b.pre_parent, b.pre_info, b.pre_nchild, b.pre_ref, b.nodes,
+                    b.st_hi, b.st_lo, b.chain_cnt, b.leaves, b.pre_parent, b.pre_info, b.pre_nchild, b.pre_ref, b.nodes,
                     b.n_parent, b.n_info, b.n_arrive, b.pnodes, b.mnodes, b.mrange, b.scan_tmp, b.info};
     for (void *p : ptrs)
         if (p) cudaFree(p);
@@ -1055,6 +1101,7 @@ cudaError_t tree_alloc(TreeBufs &b, int64_t n, int leaf) {
     GBH_ALLOC(b.st_hi, cn);
     GBH_ALLOC(b.st_lo, cn);
     GBH_ALLOC(b.chain_cnt, cn * 2);  // counts, then their scan
+    GBH_ALLOC(b.leaves, cn);
     GBH_ALLOC(b.pre_parent, cnodes);
     GBH_ALLOC(b.pre_info, cnodes);
     GBH_ALLOC(b.pre_nchild, cnodes);
@@ -1087,7 +1134,7 @@ cudaError_t tree_alloc(TreeBufs &b, int64_t n, int leaf) {
 
 cudaError_t tree_build(const Launch &L, TreeBufs &b, int64_t n, const double *px, const double *py, const double *pz,
                        const double *mass, const uint8_t *kind, const uint8_t *alive, double *ax, double *ay,
-                       double *az, double theta, int leaf, int dm_off) {
+                       double *az, double theta, int leaf, int dm_off, bool exact, bool plain_records) {
     cudaStream_t s = L.stream;
     const int64_t cap = b.cap_n;
     // collect + bbox (build.go:62-113)
@@ -1097,7 +1144,7 @@ cudaError_t tree_build(const Launch &L, TreeBufs &b, int64_t n, const double *px
     GBH_LAUNCH_CHECK();
     cudaError_t e = scan_u32(L, b.flag, b.flag, n, b.scan_tmp, b.scan_tmp_cap);
     if (e != cudaSuccess) return e;
-    k_bbox_final<<<1, 32, 0, s>>>(int(fb), b.bbox_part, n, b.flag, kind, alive, theta, b.info);
+    k_bbox_final<<<1, kFinalThreads, 0, s>>>(int(fb), b.bbox_part, n, b.flag, kind, alive, theta, b.info);
     GBH_LAUNCH_CHECK();
     k_compact_keys<<<blocks_for(n, kThreads), kThreads, 0, s>>>(n, px, py, pz, kind, alive, b.flag, b.info, b.keys,
                                                                 b.order);
@@ -1131,7 +1178,7 @@ cudaError_t tree_build(const Launch &L, TreeBufs &b, int64_t n, const double *px
     GBH_LAUNCH_CHECK();
     e = scan_dyn(L, cnt, base, cap, &b.info->nstars, b.scan_tmp, b.scan_tmp_cap);
     if (e != cudaSuccess) return e;
-    k_chain_emit<<<nb, kThreads, 0, s>>>(b.keys, b.info, cnt, base, b.pre_parent, b.pre_info, b.pre_nchild);
+    k_chain_emit<<<nb, kThreads, 0, s>>>(b.keys, b.info, cnt, base, b.pre_parent, b.pre_info, b.pre_nchild, b.leaves);
     GBH_LAUNCH_CHECK();
     e = scan_dyn(L, b.pre_nchild, b.pre_nchild, b.cap_nodes, &b.info->nnodes, b.scan_tmp, b.scan_tmp_cap);
     if (e != cudaSuccess) return e;
@@ -1140,6 +1187,8 @@ cudaError_t tree_build(const Launch &L, TreeBufs &b, int64_t n, const double *px
     k_emit_nodes<<<nb, kThreads, 0, s>>>(b.keys, b.info, cnt, base, b.pre_parent, b.pre_info, b.pre_nchild, b.pre_ref,
                                          b.nodes, b.n_parent, b.n_info, b.n_arrive);
     GBH_LAUNCH_CHECK();
+    b.moments_exact = exact;
+    if (!exact) return upsweep_fast(L, b, plain_records);
     k_upsweep<<<nb, kThreads, 0, s>>>(b.keys, b.info, cnt, base, b.pre_ref, b.sx, b.sy, b.sz, b.sm, b.nodes,
                                       b.n_parent, b.n_info, b.n_arrive, b.pnodes, b.mnodes, b.mrange, b.info);
     GBH_LAUNCH_CHECK();
@@ -1293,7 +1342,7 @@ cudaError_t morton_sort(const Launch &L, int64_t n, const double *px, const doub
     k_flags_bbox_noacc<<<fb, kThreads, 0, s>>>(n, px, py, pz, kind, alive, flag, bbox_part);
     GBH_LAUNCH_CHECK();
     if ((e = scan_u32(L, flag, flag, n, tmp, tmp_cap)) != cudaSuccess) return e;
-    k_bbox_final<<<1, 32, 0, s>>>(int(fb), bbox_part, n, flag, kind, alive, 0.9, info);
+    k_bbox_final<<<1, kFinalThreads, 0, s>>>(int(fb), bbox_part, n, flag, kind, alive, 0.9, info);
     GBH_LAUNCH_CHECK();
     k_compact_keys<<<blocks_for(n, kThreads), kThreads, 0, s>>>(n, px, py, pz, kind, alive, flag, info, keys, order);
     GBH_LAUNCH_CHECK();

@@ -2,14 +2,15 @@
 //
 // walk_plain: one thread per sorted star, the CUDA twin of the Metal kernel
 //   internal/sim/bh/gpu_darwin.go:76-118 (all FP32, uncompensated, per-star opening).
-// walk_mixed: one warp per group of 32 consecutive Morton-sorted stars walking the skip-pointer
-//   tree in lockstep. A node is opened when any star of the group would open it under the
+// walk_mixed: one warp per group of 64 consecutive Morton-sorted stars (two per lane, packed
+//   FP32x2 arithmetic; a one-star-per-lane kernel is kept behind GBH_MIXED_PAIRS=0) walking the
+//   skip-pointer tree in lockstep. A node is opened when any star of the group would open it under the
 //   reference criterion d2 < crit2 (bh.go:165), so every star sees each accepted node exactly
 //   where the reference would accept it or deeper. Positions are FP64 split into hi + lo FP32
 //   parts; a separation is formed per star as (hi_a - hi_b) + (lo_a - lo_b), whose hi difference
 //   is exact for nearby points (Sterbenz) and relatively small for distant ones, so separations
 //   stay accurate however far a system lies from the origin. Each star accumulates in FP32
-//   blocks of 32 interactions folded into a Kahan sum.
+//   blocks (the interactions of 32 node visits) folded into a Kahan sum.
 #include <cuda_runtime.h>
 
 #include "gbh_internal.cuh"
@@ -19,8 +20,21 @@ namespace gbh {
 namespace {
 
 constexpr unsigned kFull = 0xffffffffu;
+
 constexpr int kPlainThreads = 256;
-constexpr int kMixedThreads = 128;
+// Mixed-walk block size and the minimum resident blocks per SM asked of the compiler (which
+// caps its registers per thread); compile-time tuning knobs.
+#ifndef GBH_MIXED_THREADS
+#define GBH_MIXED_THREADS 128
+#endif
+#ifndef GBH_MIXED_MINBLOCKS
+#define GBH_MIXED_MINBLOCKS 1
+#endif
+// Stars per lane in the mixed walk: 1 (k_walk_mixed) or 2 (k_walk_mixed2, packed FP32x2).
+#ifndef GBH_MIXED_PAIRS
+#define GBH_MIXED_PAIRS 1
+#endif
+constexpr int kMixedThreads = GBH_MIXED_THREADS;
 
 inline unsigned blocks_for(int64_t n, int threads) {
     int64_t b = (n + threads - 1) / threads;
@@ -102,31 +116,33 @@ __device__ __forceinline__ void kahan_fold(float &s, float &c, float &part) {
     part = 0.f;
 }
 
+// One warp per group of 32 consecutive sorted stars; the warps of a block take consecutive
+// groups, which share most of their nodes in L1.
 template <bool kQuad, bool kSoft>
-__global__ __launch_bounds__(kMixedThreads) void k_walk_mixed(const DevInfo *info, const MNode *__restrict__ nodes,
+__global__ __launch_bounds__(kMixedThreads, GBH_MIXED_MINBLOCKS) void k_walk_mixed(const DevInfo *info,
+                                                                                  const MNode *__restrict__ nodes,
                                                               const int2 *__restrict__ ranges,
                                                               const float4 *__restrict__ st_hi,
                                                               const float4 *__restrict__ st_lo,
                                                               const int32_t *__restrict__ order, float eps2,
                                                               double *ax, double *ay, double *az, DevInfo *err_info) {
     const int lane = threadIdx.x & 31;
-    const int64_t ns = info->nstars;
-    const int64_t nn = info->nnodes;
-    const int64_t group = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
-    const int64_t base = group * 32;
+    const int32_t ns = int32_t(info->nstars);  // the C-ABI caps n at 2^30
+    const uint32_t nn = uint32_t(info->nnodes);
+    const int32_t base = int32_t((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32;
     if (base >= ns) return;  // uniform over the warp
-    const int64_t k = base + lane;
+    const int32_t k = base + lane;
     const bool valid = k < ns;
-    const int64_t kk = valid ? k : base;
+    const int32_t kk = valid ? k : base;
     const float4 h = st_hi[kk], l = st_lo[kk];
 
     float sx = 0.f, sy = 0.f, sz = 0.f, cx = 0.f, cy = 0.f, cz = 0.f;  // Kahan sums
     float px = 0.f, py = 0.f, pz = 0.f;                                // block partials
-    int nint = 0;
-    int64_t steps = 0;
+    uint32_t visits = 0;
     int i = nn > 0 ? 0 : -1;
+    // Control flow is uniform over the warp: i, first, next and the vote agree in all lanes.
     while (i >= 0) {
-        if (++steps > nn || i >= nn) {
+        if (uint32_t(i) >= nn) {
             if (lane == 0) set_err(err_info, 4);
             break;
         }
@@ -141,59 +157,59 @@ __global__ __launch_bounds__(kMixedThreads) void k_walk_mixed(const DevInfo *inf
             const float ir = rsqrtf(d2 + eps2);
             const float ir2 = ir * ir;
             const float ir3 = ir * ir2;
-            float f = nd.b.w * ir3;
             if (kQuad) {
                 const float qx = nd.c.x * dx + nd.c.w * dy + nd.d.x * dz;
                 const float qy = nd.c.w * dx + nd.c.y * dy + nd.d.y * dz;
                 const float qz = nd.d.x * dx + nd.d.y * dy + nd.c.z * dz;
                 const float ir5 = ir3 * ir2;
-                f += 2.5f * (dx * qx + dy * qy + dz * qz) * ir5 * ir2;
-                px -= qx * ir5;
-                py -= qy * ir5;
-                pz -= qz * ir5;
-            }
-            px += f * dx;
-            py += f * dy;
-            pz += f * dz;
-            if (++nint == 32) {
-                kahan_fold(sx, cx, px);
-                kahan_fold(sy, cy, py);
-                kahan_fold(sz, cz, pz);
-                nint = 0;
+                const float u = 2.5f * ir2 * (dx * qx + dy * qy + dz * qz);
+                const float f = fmaf(ir5, u, nd.b.w * ir3);
+                px = fmaf(f, dx, px);
+                py = fmaf(f, dy, py);
+                pz = fmaf(f, dz, pz);
+                px = fmaf(-ir5, qx, px);
+                py = fmaf(-ir5, qy, py);
+                pz = fmaf(-ir5, qz, pz);
+            } else {
+                const float f = nd.b.w * ir3;
+                px = fmaf(f, dx, px);
+                py = fmaf(f, dy, py);
+                pz = fmaf(f, dz, pz);
             }
             i = next;
-            continue;
-        }
-        if (first >= 0) {
+        } else if (first >= 0) {
             i = first;
-            continue;
+        } else {
+            const int2 r = ranges[i];
+            if (r.x < 0 || r.y > ns || r.x > r.y) {
+                if (lane == 0) set_err(err_info, 5);
+                break;
+            }
+            for (int j = r.x; j < r.y; ++j) {
+                const float4 sh = st_hi[j], sl = st_lo[j];
+                const float ex = (sh.x - h.x) + (sl.x - l.x);
+                const float ey = (sh.y - h.y) + (sl.y - l.y);
+                const float ez = (sh.z - h.z) + (sl.z - l.z);
+                const float r2 = fmaf(ex, ex, fmaf(ey, ey, fmaf(ez, ez, eps2)));
+                // The star itself gives ex = ey = ez = 0 exactly; with eps2 > 0 that adds 0, as
+                // skipping j == self does (bh.go:191-193). Without softening r2 = 0 is masked.
+                const float ir = kSoft ? rsqrtf(r2) : (r2 > 0.f ? rsqrtf(r2) : 0.f);
+                const float f = sh.w * ir * ir * ir;
+                px = fmaf(f, ex, px);
+                py = fmaf(f, ey, py);
+                pz = fmaf(f, ez, pz);
+            }
+            i = next;
         }
-        const int2 r = ranges[i];
-        if (r.x < 0 || r.y > ns || r.x > r.y) {
-            if (lane == 0) set_err(err_info, 5);
-            break;
-        }
-        for (int j = r.x; j < r.y; ++j) {
-            const float4 sh = st_hi[j], sl = st_lo[j];
-            const float ex = (sh.x - h.x) + (sl.x - l.x);
-            const float ey = (sh.y - h.y) + (sl.y - l.y);
-            const float ez = (sh.z - h.z) + (sl.z - l.z);
-            const float r2 = ex * ex + ey * ey + ez * ez + eps2;
-            // The star itself gives ex = ey = ez = 0 exactly; with eps2 > 0 that adds 0, as
-            // skipping j == self does (bh.go:191-193). Without softening r2 = 0 is masked.
-            const float ir = kSoft ? rsqrtf(r2) : (r2 > 0.f ? rsqrtf(r2) : 0.f);
-            const float f = sh.w * ir * ir * ir;
-            px += f * ex;
-            py += f * ey;
-            pz += f * ez;
-            if (++nint == 32) {
-                kahan_fold(sx, cx, px);
-                kahan_fold(sy, cy, py);
-                kahan_fold(sz, cz, pz);
-                nint = 0;
+        if ((++visits & 31u) == 0) {  // fold the block partial every 32 visits
+            kahan_fold(sx, cx, px);
+            kahan_fold(sy, cy, py);
+            kahan_fold(sz, cz, pz);
+            if (visits > nn + 32u) {  // each node is visited at most once
+                if (lane == 0) set_err(err_info, 4);
+                break;
             }
         }
-        i = next;
     }
     kahan_fold(sx, cx, px);
     kahan_fold(sy, cy, py);
@@ -203,6 +219,139 @@ __global__ __launch_bounds__(kMixedThreads) void k_walk_mixed(const DevInfo *inf
         ax[o] = double(sx) - double(cx);
         ay[o] = double(sy) - double(cy);
         az[o] = double(sz) - double(cz);
+    }
+}
+
+// Paired variant of the mixed walk: one warp per group of 64 consecutive sorted stars, each
+// lane owning two neighbouring stars; every separation, test and interaction is computed for
+// both stars at once with packed FP32x2 arithmetic (__fadd2_rn / __fmul2_rn / __ffma2_rn), so
+// the node load, vote and branch of a visit are shared by twice the stars and the math issues
+// half the instructions. Same opening rule (any star of the group opens the node), same
+// double-float separations and Kahan-folded block sums as k_walk_mixed.
+__device__ __forceinline__ float2 f2(float v) { return make_float2(v, v); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+
+__device__ __forceinline__ void kahan_fold2(float2 &s, float2 &c, float2 &part) {
+    kahan_fold(s.x, c.x, part.x);
+    kahan_fold(s.y, c.y, part.y);
+}
+
+template <bool kQuad, bool kSoft>
+__global__ __launch_bounds__(kMixedThreads) void k_walk_mixed2(const DevInfo *info, const MNode *__restrict__ nodes,
+                                                               const int2 *__restrict__ ranges,
+                                                               const float4 *__restrict__ st_hi,
+                                                               const float4 *__restrict__ st_lo,
+                                                               const int32_t *__restrict__ order, float eps2,
+                                                               double *ax, double *ay, double *az, DevInfo *err_info) {
+    const int lane = threadIdx.x & 31;
+    const int32_t ns = int32_t(info->nstars);  // the C-ABI caps n at 2^30
+    const uint32_t nn = uint32_t(info->nnodes);
+    const int32_t base = int32_t((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 64;
+    if (base >= ns) return;  // uniform over the warp
+    const int32_t k0 = base + 2 * lane, k1 = k0 + 1;
+    const bool v0 = k0 < ns, v1 = k1 < ns;
+    const float4 h0 = st_hi[v0 ? k0 : base], l0 = st_lo[v0 ? k0 : base];
+    const float4 h1 = st_hi[v1 ? k1 : base], l1 = st_lo[v1 ? k1 : base];
+    // negated target coordinates, so separations are sums
+    const float2 nhx = make_float2(-h0.x, -h1.x), nhy = make_float2(-h0.y, -h1.y), nhz = make_float2(-h0.z, -h1.z);
+    const float2 nlx = make_float2(-l0.x, -l1.x), nly = make_float2(-l0.y, -l1.y), nlz = make_float2(-l0.z, -l1.z);
+    const float2 e2 = f2(eps2);
+
+    float2 sx = f2(0.f), sy = f2(0.f), sz = f2(0.f), cx = f2(0.f), cy = f2(0.f), cz = f2(0.f);
+    float2 px = f2(0.f), py = f2(0.f), pz = f2(0.f);
+    uint32_t visits = 0;
+    int i = nn > 0 ? 0 : -1;
+    while (i >= 0) {
+        if (uint32_t(i) >= nn) {
+            if (lane == 0) set_err(err_info, 4);
+            break;
+        }
+        const MNode nd = nodes[i];
+        const float2 dx = add2(add2(f2(nd.a.x), nhx), add2(f2(nd.b.x), nlx));
+        const float2 dy = add2(add2(f2(nd.a.y), nhy), add2(f2(nd.b.y), nly));
+        const float2 dz = add2(add2(f2(nd.a.z), nhz), add2(f2(nd.b.z), nlz));
+        const float2 d2 = fma2(dz, dz, fma2(dy, dy, mul2(dx, dx)));
+        const bool open = __any_sync(kFull, (d2.x < nd.a.w) | (d2.y < nd.a.w));
+        const int first = __float_as_int(nd.d.z), next = __float_as_int(nd.d.w);
+        if (!open) {
+            const float2 r2 = add2(d2, e2);
+            const float2 ir = make_float2(rsqrtf(r2.x), rsqrtf(r2.y));
+            const float2 ir2 = mul2(ir, ir);
+            const float2 ir3 = mul2(ir, ir2);
+            if (kQuad) {
+                const float2 qx = fma2(f2(nd.d.x), dz, fma2(f2(nd.c.w), dy, mul2(f2(nd.c.x), dx)));
+                const float2 qy = fma2(f2(nd.d.y), dz, fma2(f2(nd.c.y), dy, mul2(f2(nd.c.w), dx)));
+                const float2 qz = fma2(f2(nd.c.z), dz, fma2(f2(nd.d.y), dy, mul2(f2(nd.d.x), dx)));
+                const float2 ir5 = mul2(ir3, ir2);
+                const float2 dqd = fma2(dz, qz, fma2(dy, qy, mul2(dx, qx)));
+                const float2 u = mul2(mul2(f2(2.5f), ir2), dqd);
+                const float2 f = fma2(ir5, u, mul2(f2(nd.b.w), ir3));
+                const float2 nir5 = mul2(f2(-1.f), ir5);
+                px = fma2(nir5, qx, fma2(f, dx, px));
+                py = fma2(nir5, qy, fma2(f, dy, py));
+                pz = fma2(nir5, qz, fma2(f, dz, pz));
+            } else {
+                const float2 f = mul2(f2(nd.b.w), ir3);
+                px = fma2(f, dx, px);
+                py = fma2(f, dy, py);
+                pz = fma2(f, dz, pz);
+            }
+            i = next;
+        } else if (first >= 0) {
+            i = first;
+        } else {
+            const int2 r = ranges[i];
+            if (r.x < 0 || r.y > ns || r.x > r.y) {
+                if (lane == 0) set_err(err_info, 5);
+                break;
+            }
+            for (int j = r.x; j < r.y; ++j) {
+                const float4 sh = st_hi[j], sl = st_lo[j];
+                const float2 ex = add2(add2(f2(sh.x), nhx), add2(f2(sl.x), nlx));
+                const float2 ey = add2(add2(f2(sh.y), nhy), add2(f2(sl.y), nly));
+                const float2 ez = add2(add2(f2(sh.z), nhz), add2(f2(sl.z), nlz));
+                const float2 r2 = fma2(ez, ez, fma2(ey, ey, fma2(ex, ex, e2)));
+                // A star paired with itself gives a zero separation: with eps2 > 0 that adds 0, as
+                // skipping j == self does (bh.go:191-193). Without softening r2 = 0 is masked.
+                float2 ir;
+                if (kSoft) {
+                    ir = make_float2(rsqrtf(r2.x), rsqrtf(r2.y));
+                } else {
+                    ir = make_float2(r2.x > 0.f ? rsqrtf(r2.x) : 0.f, r2.y > 0.f ? rsqrtf(r2.y) : 0.f);
+                }
+                const float2 f = mul2(mul2(f2(sh.w), ir), mul2(ir, ir));
+                px = fma2(f, ex, px);
+                py = fma2(f, ey, py);
+                pz = fma2(f, ez, pz);
+            }
+            i = next;
+        }
+        if ((++visits & 31u) == 0) {  // fold the block partials every 32 visits
+            kahan_fold2(sx, cx, px);
+            kahan_fold2(sy, cy, py);
+            kahan_fold2(sz, cz, pz);
+            if (visits > nn + 32u) {  // each node is visited at most once
+                if (lane == 0) set_err(err_info, 4);
+                break;
+            }
+        }
+    }
+    kahan_fold2(sx, cx, px);
+    kahan_fold2(sy, cy, py);
+    kahan_fold2(sz, cz, pz);
+    if (v0) {
+        int32_t o = order[k0];
+        ax[o] = double(sx.x) - double(cx.x);
+        ay[o] = double(sy.x) - double(cy.x);
+        az[o] = double(sz.x) - double(cz.x);
+    }
+    if (v1) {
+        int32_t o = order[k1];
+        ax[o] = double(sx.y) - double(cx.y);
+        ay[o] = double(sy.y) - double(cy.y);
+        az[o] = double(sz.y) - double(cz.y);
     }
 }
 
@@ -238,25 +387,29 @@ cudaError_t walk_plain(const Launch &L, const TreeBufs &b, int64_t nstars_cap, f
     return cudaGetLastError();
 }
 
-cudaError_t walk_mixed(const Launch &L, const TreeBufs &b, int64_t nstars_cap, float eps2, int quad, double *ax,
-                       double *ay, double *az) {
-    int64_t groups = (nstars_cap + 31) / 32;
-    unsigned nb = blocks_for(groups * 32, kMixedThreads);
-    bool soft = eps2 > 0.f;
-    if (quad && soft)
-        k_walk_mixed<true, true><<<nb, kMixedThreads, 0, L.stream>>>(b.info, b.mnodes, b.mrange, b.st_hi, b.st_lo,
-                                                                     b.order, eps2, ax, ay, az, b.info);
-    else if (quad)
-        k_walk_mixed<true, false><<<nb, kMixedThreads, 0, L.stream>>>(b.info, b.mnodes, b.mrange, b.st_hi, b.st_lo,
-                                                                      b.order, eps2, ax, ay, az, b.info);
-    else if (soft)
-        k_walk_mixed<false, true><<<nb, kMixedThreads, 0, L.stream>>>(b.info, b.mnodes, b.mrange, b.st_hi, b.st_lo,
-                                                                      b.order, eps2, ax, ay, az, b.info);
+template <bool kQuad, bool kSoft>
+static cudaError_t launch_mixed(const Launch &L, const TreeBufs &b, int64_t nstars_cap, float eps2, double *ax,
+                                double *ay, double *az) {
+    const int per_warp = GBH_MIXED_PAIRS ? 64 : 32;
+    int64_t groups = (nstars_cap + per_warp - 1) / per_warp;
+    int64_t blocks = (groups + kMixedThreads / 32 - 1) / (kMixedThreads / 32);
+    if (GBH_MIXED_PAIRS)
+        k_walk_mixed2<kQuad, kSoft><<<unsigned(blocks < 1 ? 1 : blocks), kMixedThreads, 0, L.stream>>>(
+            b.info, b.mnodes, b.mrange, b.st_hi, b.st_lo, b.order, eps2, ax, ay, az, b.info);
     else
-        k_walk_mixed<false, false><<<nb, kMixedThreads, 0, L.stream>>>(b.info, b.mnodes, b.mrange, b.st_hi, b.st_lo,
-                                                                       b.order, eps2, ax, ay, az, b.info);
+        k_walk_mixed<kQuad, kSoft><<<unsigned(blocks < 1 ? 1 : blocks), kMixedThreads, 0, L.stream>>>(
+            b.info, b.mnodes, b.mrange, b.st_hi, b.st_lo, b.order, eps2, ax, ay, az, b.info);
     ++*L.count;
     return cudaGetLastError();
+}
+
+cudaError_t walk_mixed(const Launch &L, const TreeBufs &b, int64_t nstars_cap, float eps2, int quad, double *ax,
+                       double *ay, double *az) {
+    bool soft = eps2 > 0.f;
+    if (quad && soft) return launch_mixed<true, true>(L, b, nstars_cap, eps2, ax, ay, az);
+    if (quad) return launch_mixed<true, false>(L, b, nstars_cap, eps2, ax, ay, az);
+    if (soft) return launch_mixed<false, true>(L, b, nstars_cap, eps2, ax, ay, az);
+    return launch_mixed<false, false>(L, b, nstars_cap, eps2, ax, ay, az);
 }
 
 cudaError_t fp32_fma_probe(const Launch &L, int blocks, int iters, float *out) {

@@ -47,8 +47,9 @@ enum { GBH_STAR = 0, GBH_BLACK_HOLE = 1, GBH_DARK_MATTER = 2, GBH_GAS = 3 };
 
 /* Tree walk variants. */
 enum {
-    /* Warp-cooperative walk: FP32 group-relative coordinates split from FP64
-       positions, compensated per-particle accumulation. The default. */
+    /* Warp-cooperative walk: one warp per 32 Morton-consecutive stars, FP32
+       separations formed from hi + lo splits of the FP64 positions, compensated
+       per-star accumulation. The default. */
     GBH_WALK_MIXED = 0,
     /* One thread per star, all FP32, uncompensated: the CUDA twin of the Metal
        kernel internal/sim/bh/gpu_darwin.go:76-118. */
@@ -174,7 +175,9 @@ int gbh_state_accelerations(gbh_ctx *ctx, const gbh_params *p);
 int gbh_tree_size(gbh_ctx *ctx, int64_t *nstars, int64_t *nnodes);
 /* Copies the last tree: Morton keys and state indices in sorted order (nstars each)
    and the node table in the reference's serial index layout (up to node_cap nodes).
-   Any pointer may be NULL. */
+   Any pointer may be NULL. Keys, order, ranges and links are always the reference's;
+   the moments are the reference's FP64 values, bit for bit, after a GBH_WALK_FP64 call,
+   and FP32-accurate values after a call with an FP32 walk. */
 int gbh_tree_export(gbh_ctx *ctx, uint64_t *keys, int32_t *order, gbh_node *nodes,
                     int64_t node_cap);
 /* Device times and counters of the last call. */

@@ -119,7 +119,7 @@ def test_coincident_stars(ctx):  # bh_test.go:149-163
     n = 101
     s = dict(px=np.full(n, 1.0), py=np.full(n, 2.0), pz=np.full(n, 3.0), mass=np.ones(n))
     s["px"][-1] = s["py"][-1] = s["pz"][-1] = 0.0
-    for walk in ("fp64", "plain", "mixed"):
+    for walk in ("plain", "mixed", "fp64"):
         a = gpu_acc(ctx, s, 0.0, 0, 0.01, walk)
         assert not np.isnan(a).any()
     assert_tree_equal(ctx, s, 0.9, 24)
@@ -143,6 +143,28 @@ def test_clustered_and_far_apart(ctx):
 
 
 # ---------------------------------------------------------------- FP32 walks
+
+@pytest.mark.parametrize("name,theta,leaf", [("plummer", 0.5, 8), ("disk", 0.9, 24)])
+def test_fast_moments_agree_with_exact(ctx, name, theta, leaf):
+    """The FP32 walks run on node moments formed in FP32 about a point inside each node; same
+    node set and links, values within FP32 rounding of the reference's FP64 moments."""
+    g = np.load(os.path.join(GOLDEN, f"{name}.npz"))
+    s = {k: g[k] for k in ("px", "py", "pz", "mass", "kind", "alive")}
+    gpu_acc(ctx, s, theta, leaf, float(g["eps"]), "mixed")
+    fast = ctx.tree_export()["nodes"]
+    ex = g["nodes"]
+    for f in ("first", "next", "lo", "hi"):
+        assert np.array_equal(fast[f], ex[f]), f
+    side = max(np.ptp(s[k][(s["alive"] == 1) & (s["kind"] != O.BLACK_HOLE)]) for k in ("px", "py", "pz"))
+    for f in ("x", "y", "z"):
+        assert np.abs(fast[f] - ex[f]).max() <= 1e-6 * side, f
+    assert np.allclose(fast["m"], ex["m"], rtol=1e-6, atol=0)
+    assert np.allclose(fast["crit2"], ex["crit2"], rtol=1e-5, atol=0)
+    qs = ("qxx", "qyy", "qzz", "qxy", "qxz", "qyz")
+    qmax = np.max(np.abs(np.stack([ex[q] for q in qs])), axis=0)
+    for q in qs:
+        assert np.all(np.abs(fast[q] - ex[q]) <= 1e-5 * qmax + 1e-30), q
+
 
 def test_plain_walk_matches_cpu_walk(ctx):  # gpu_test.go:8-21
     s = ics.test_disk(20000)
