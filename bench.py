@@ -40,6 +40,9 @@ sys.path.insert(0, ROOT)
 METRIC = "particle-steps/s @N=1M θ=0.5: mixed vs plain GPU walk at RMS force err ≤2e-3"
 N_DEFAULT = 1 << 20
 THETA, LEAF, EPS, DT = 0.5, 8, 0.02, 1e-3
+# DRAM bytes (read + write) of one k_walk_mixed2 launch on this workload, from the ncu capture
+# summarised in profiles/walk_mixed2_merger_1M_theta0.5_leaf8.md (72.90 MB + 6.48 MB).
+WALK_TRAFFIC_BYTES = 79_383_296
 FIELDS = ("px", "py", "pz", "vx", "vy", "vz", "ax", "ay", "az")
 
 
@@ -278,8 +281,9 @@ def run(args):
             "config": {"workload": workload_name(n, args.leaf), "parallelism": "replicas" if world > 1 else "1 gpu",
                        "l2": "flushed (256 MiB write) between timed steps; events cover each step only"},
             "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                         "frac": achieved / peak, "traffic": None,
-                         "kernel": "k_walk_mixed", "flop_per_launch": flop,
+                         "frac": achieved / peak, "traffic": WALK_TRAFFIC_BYTES,
+                         "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch",
+                         "kernel": "k_walk_mixed2", "flop_per_launch": flop,
                          "peak_source": "FP32 FMA microbenchmark in this run (gbh_probe_fp32_peak); "
                                         "MEASURED_PEAKS.json has no FP32 figure",
                          "walk_ms": w_mixed / args.steps, "build_ms": b_mixed / args.steps},
