@@ -34,8 +34,11 @@ class Params(ctypes.Structure):
                 ("monopole_only", ctypes.c_int32), ("dark_matter_off", ctypes.c_int32), ("walk", ctypes.c_int32)]
 
 
+CFG_NO_GRAPHS = 1
+
+
 class Config(ctypes.Structure):
-    _fields_ = [("device", ctypes.c_int32), ("reserved", ctypes.c_int32 * 7)]
+    _fields_ = [("device", ctypes.c_int32), ("flags", ctypes.c_int32), ("reserved", ctypes.c_int32 * 6)]
 
 
 class Timings(ctypes.Structure):
@@ -134,9 +137,9 @@ def make_params(theta=0.0, softening=0.0, leaf_size=0, monopole_only=False, dark
 class Context:
     """One gbh_ctx (one device, one stream)."""
 
-    def __init__(self, device: int = 0):
+    def __init__(self, device: int = 0, flags: int = 0):
         L = load()
-        cfg = Config(device, (ctypes.c_int32 * 7)())
+        cfg = Config(device, flags, (ctypes.c_int32 * 6)())
         h = _P()
         err = ctypes.create_string_buffer(512)
         rc = L.gbh_create(ctypes.byref(cfg), ctypes.byref(h), err, 512)

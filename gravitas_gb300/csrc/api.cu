@@ -15,6 +15,20 @@
 using gbh::DevInfo;
 using gbh::Launch;
 
+// One KDK step captured as a CUDA graph, valid for the sizes, parameters and buffers it was
+// captured with.
+struct StepGraph {
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    cudaGraphNode_t stage_nodes[3] = {};  // event-record nodes: build start, walk start, walk end
+    int64_t launches = 0;                 // kernels in one replay
+    // validity key
+    int64_t n = -1, tree_gen = -1, state_gen = -1;
+    gbh_params p = {};
+    double dt = 0;
+    const void *kind = nullptr, *alive = nullptr;
+};
+
 struct gbh_ctx {
     int device = 0;
     int num_sms = 0;
@@ -23,6 +37,7 @@ struct gbh_ctx {
     gbh::TreeBufs tb;
     // resident state (state order)
     int64_t cap = 0, n = 0;
+    int64_t state_gen = 0;  // incremented whenever the state buffers are reallocated
     bool have_state = false, acc_valid = false;
     int32_t state_holes = 0;
     bool state_has_kind = false, state_has_alive = false;
@@ -42,6 +57,9 @@ struct gbh_ctx {
     // per-stage events of the current call: (build start, walk start, walk end) triples
     std::vector<cudaEvent_t> evpool;
     size_t evused = 0;
+    StepGraph step_graph;
+    bool use_graphs = true;
+    bool capturing = false;  // stage events become graph event-record nodes
     // bookkeeping
     int64_t launches = 0;
     int64_t h2d = 0, d2h = 0;
@@ -105,6 +123,7 @@ cudaError_t ensure_state(gbh_ctx *c, int64_t n) {
         return e;
     }
     c->cap = cap;
+    ++c->state_gen;
     return cudaSuccess;
 }
 
@@ -134,15 +153,25 @@ int begin(gbh_ctx *ctx) {
 
 Launch launch_of(gbh_ctx *ctx) { return Launch{ctx->stream, &ctx->launches, ctx->num_sms}; }
 
-// Records the next stage event of the call on the context's stream.
-cudaError_t stage_event(gbh_ctx *ctx) {
+// Takes the next stage event of the call from the pool (creating it if needed).
+cudaError_t next_stage_event(gbh_ctx *ctx, cudaEvent_t *ev) {
     if (ctx->evused == ctx->evpool.size()) {
         cudaEvent_t e;
         cudaError_t r = cudaEventCreate(&e);
         if (r != cudaSuccess) return r;
         ctx->evpool.push_back(e);
     }
-    return cudaEventRecord(ctx->evpool[ctx->evused++], ctx->stream);
+    *ev = ctx->evpool[ctx->evused++];
+    return cudaSuccess;
+}
+
+// Records the next stage event of the call on the context's stream.
+cudaError_t stage_event(gbh_ctx *ctx) {
+    cudaEvent_t ev;
+    cudaError_t r = next_stage_event(ctx, &ev);
+    if (r != cudaSuccess) return r;
+    return ctx->capturing ? cudaEventRecordWithFlags(ev, ctx->stream, cudaEventRecordExternal)
+                          : cudaEventRecord(ev, ctx->stream);
 }
 
 int h2d(gbh_ctx *ctx, void *dst, const void *src, size_t bytes) {
@@ -223,6 +252,74 @@ int count_holes(const uint8_t *kind, const uint8_t *alive, int64_t n) {
     return int(std::min<int64_t>(h, 1 << 30));
 }
 
+void free_graph(StepGraph &g) {
+    if (g.exec) cudaGraphExecDestroy(g.exec);
+    if (g.graph) cudaGraphDestroy(g.graph);
+    g = StepGraph{};
+}
+
+bool same_params(const gbh_params &a, const gbh_params &b) {
+    return a.theta == b.theta && a.softening == b.softening && a.leaf_size == b.leaf_size &&
+           a.monopole_only == b.monopole_only && a.dark_matter_off == b.dark_matter_off && a.walk == b.walk;
+}
+
+// Captures one resident step (kick + drift, forces, kick) into ctx->step_graph.
+int capture_step(gbh_ctx *ctx, const gbh_params *p, double dt, const uint8_t *kind, const uint8_t *alive) {
+    StepGraph &g = ctx->step_graph;
+    free_graph(g);
+    Launch L = launch_of(ctx);
+    const int64_t n = ctx->n;
+    const double h = 0.5 * dt;
+    const size_t ev0 = ctx->evused;
+    const int64_t l0 = ctx->launches;
+    CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+    ctx->capturing = true;
+    int rc = GBH_OK;
+    cudaError_t e = gbh::kick_drift(L, n, h, dt, ctx->px, ctx->py, ctx->pz, ctx->vx, ctx->vy, ctx->vz, ctx->ax, ctx->ay,
+                                    ctx->az);
+    if (e == cudaSuccess)
+        rc = forces(ctx, p, n, ctx->px, ctx->py, ctx->pz, ctx->mass, kind, alive, ctx->ax, ctx->ay, ctx->az,
+                    theta_of(p));
+    if (e == cudaSuccess && rc == GBH_OK) e = gbh::kick(L, n, h, ctx->vx, ctx->vy, ctx->vz, ctx->ax, ctx->ay, ctx->az);
+    cudaGraph_t graph = nullptr;
+    cudaError_t e2 = cudaStreamEndCapture(ctx->stream, &graph);
+    ctx->capturing = false;
+    if (e != cudaSuccess || rc != GBH_OK || e2 != cudaSuccess) {
+        if (graph) cudaGraphDestroy(graph);
+        if (rc != GBH_OK) return rc;
+        return fail(ctx, GBH_ERR_CUDA, "step capture: %s", cudaGetErrorString(e != cudaSuccess ? e : e2));
+    }
+    g.graph = graph;
+    g.launches = ctx->launches - l0;
+    ctx->launches = l0;
+    // the event-record nodes of the three stage events recorded by forces()
+    size_t count = 0;
+    CK(cudaGraphGetNodes(graph, nullptr, &count));
+    std::vector<cudaGraphNode_t> nodes(count);
+    CK(cudaGraphGetNodes(graph, nodes.data(), &count));
+    for (cudaGraphNode_t nd : nodes) {
+        cudaGraphNodeType t;
+        CK(cudaGraphNodeGetType(nd, &t));
+        if (t != cudaGraphNodeTypeEventRecord) continue;
+        cudaEvent_t ev;
+        CK(cudaGraphEventRecordNodeGetEvent(nd, &ev));
+        for (int k = 0; k < 3; ++k)
+            if (ev == ctx->evpool[ev0 + k]) g.stage_nodes[k] = nd;
+    }
+    ctx->evused = ev0;  // the captured events were placeholders; replays get their own
+    for (auto nd : g.stage_nodes)
+        if (!nd) return fail(ctx, GBH_ERR_CUDA, "step capture: stage events not found in the graph");
+    CK(cudaGraphInstantiate(&g.exec, graph, 0));
+    g.n = n;
+    g.p = *p;
+    g.dt = dt;
+    g.tree_gen = ctx->tb.generation;
+    g.state_gen = ctx->state_gen;
+    g.kind = kind;
+    g.alive = alive;
+    return GBH_OK;
+}
+
 // Steps on the resident state (sim.go:252-288, no holes, no hydro).
 int run_steps(gbh_ctx *ctx, const gbh_params *p, double dt, int64_t nsteps) {
     Launch L = launch_of(ctx);
@@ -234,6 +331,26 @@ int run_steps(gbh_ctx *ctx, const gbh_params *p, double dt, int64_t nsteps) {
         int rc = forces(ctx, p, n, ctx->px, ctx->py, ctx->pz, ctx->mass, kind, alive, ctx->ax, ctx->ay, ctx->az, theta);
         if (rc) return rc;
         ctx->acc_valid = true;
+    }
+    if (ctx->use_graphs && nsteps > 0) {
+        // One captured step per replay: the ~50 kernels of a step launch as one graph.
+        CK(gbh::tree_alloc(ctx->tb, n, leaf_of(p)));  // any growth happens outside the capture
+        StepGraph &g = ctx->step_graph;
+        if (!(g.exec && g.n == n && same_params(g.p, *p) && g.dt == dt && g.tree_gen == ctx->tb.generation &&
+              g.state_gen == ctx->state_gen && g.kind == kind && g.alive == alive)) {
+            int rc = capture_step(ctx, p, dt, kind, alive);
+            if (rc) return rc;
+        }
+        for (int64_t s = 0; s < nsteps; ++s) {
+            for (int k = 0; k < 3; ++k) {
+                cudaEvent_t ev;
+                CK(next_stage_event(ctx, &ev));
+                CK(cudaGraphExecEventRecordNodeSetEvent(g.exec, g.stage_nodes[k], ev));
+            }
+            CK(cudaGraphLaunch(g.exec, ctx->stream));
+            ctx->launches += g.launches;
+        }
+        return GBH_OK;
     }
     double h = 0.5 * dt;
     for (int64_t s = 0; s < nsteps; ++s) {
@@ -317,6 +434,7 @@ int gbh_create(const gbh_config *cfg, gbh_ctx **out, char *err, int errlen) {
     if (prop.major < 10) return report(GBH_ERR_UNSUPPORTED, "libgbh is built for sm_103a (GB300)");
     gbh_ctx *c = new gbh_ctx();
     c->device = dev;
+    c->use_graphs = !(cfg && (cfg->flags & GBH_CFG_NO_GRAPHS));
     c->num_sms = prop.multiProcessorCount;
     if ((e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking)) != cudaSuccess) {
         delete c;
@@ -336,6 +454,7 @@ void gbh_destroy(gbh_ctx *c) {
     if (!c) return;
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
+    free_graph(c->step_graph);
     gbh::tree_free(c->tb);
     free_state(c);
     void *ptrs[] = {c->part, c->scalar, c->holes, c->targets, c->tout, c->probe};

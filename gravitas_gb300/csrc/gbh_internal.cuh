@@ -54,6 +54,7 @@ struct __align__(16) MNode {
 struct TreeBufs {
     int64_t cap_n = 0;      // bodies
     int64_t cap_nodes = 0;  // nodes
+    int64_t generation = 0; // incremented whenever the buffers are reallocated
     // compaction / bbox
     uint32_t *flag = nullptr;     // star flags, then their exclusive scan
     double *bbox_part = nullptr;  // per-block partial min/max (6 per block)
@@ -68,8 +69,9 @@ struct TreeBufs {
     uint32_t *chain_cnt = nullptr;  // nodes starting at each position, then the scan
     // pre-order node arrays (index p)
     int32_t *pre_parent = nullptr;
-    uint32_t *pre_info = nullptr;   // level | oct << 8 | mask << 16
-    uint32_t *pre_nchild = nullptr; // then its exclusive scan
+    uint32_t *pre_info = nullptr;   // level | octant << 8
+    uint32_t *pre_mask = nullptr;   // occupied child octants (bit per octant)
+    uint32_t *pre_nchild = nullptr; // child count, then its exclusive scan
     int32_t *pre_ref = nullptr;     // reference index of pre-order node p
     // reference-layout node arrays (index r)
     gbh_node *nodes = nullptr;

@@ -24,6 +24,8 @@
 // node its index in the reference's own serial layout.
 #include <cuda_runtime.h>
 
+#include <climits>
+
 #include "gbh_internal.cuh"
 
 namespace gbh {
@@ -152,38 +154,25 @@ cudaError_t scan_rec(const Launch &L, const uint32_t *in, uint32_t *out, int64_t
 
 __device__ __forceinline__ bool is_star(uint8_t alive, uint8_t kind) { return alive && kind != GBH_BLACK_HOLE; }
 
-// Star flags, per-block bbox partials; alive holes get zero acceleration (bh.go:148-150).
-__global__ __launch_bounds__(kThreads) void k_flags_bbox(int64_t n, const double *__restrict__ px,
-                                                         const double *__restrict__ py, const double *__restrict__ pz,
-                                                         const uint8_t *__restrict__ kind,
-                                                         const uint8_t *__restrict__ alive, uint32_t *__restrict__ flag,
-                                                         double *__restrict__ part, double *ax, double *ay, double *az) {
-    double mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
-    for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
-        uint8_t al = alive ? alive[i] : 1, kd = kind ? kind[i] : 0;
-        bool st = is_star(al, kd);
-        flag[i] = st;
-        if (st) {
-            double x = px[i], y = py[i], z = pz[i];
-            mn[0] = fmin(mn[0], x);
-            mx[0] = fmax(mx[0], x);
-            mn[1] = fmin(mn[1], y);
-            mx[1] = fmax(mx[1], y);
-            mn[2] = fmin(mn[2], z);
-            mx[2] = fmax(mx[2], z);
-        } else if (al && kd == GBH_BLACK_HOLE) {
-            ax[i] = 0;
-            ay[i] = 0;
-            az[i] = 0;
-        }
-    }
-    __shared__ double s[6][kThreads / 32];
+// Order-preserving map of a double to a signed 64-bit integer (an involution): min and max of
+// the keys are the keys of the min and max, computed on the integer ALU instead of the slow
+// FP64 pipe. (-0 orders before +0; the coordinates are not NaN.)
+__device__ __forceinline__ long long ord_key(double v) {
+    long long b = __double_as_longlong(v);
+    return b ^ ((b >> 63) & 0x7fffffffffffffffll);
+}
+__device__ __forceinline__ double ord_val(long long k) { return __longlong_as_double(k ^ ((k >> 63) & 0x7fffffffffffffffll)); }
+
+// Per-block min/max of the 6 ordered keys into part[6 * blockIdx.x ...] (as raw 64-bit words).
+template <int kBlock>
+__device__ __forceinline__ void block_minmax(long long mn[3], long long mx[3], double *part) {
+    __shared__ long long s[6][kBlock / 32];
     int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
         for (int o = 16; o > 0; o >>= 1) {
-            mn[c] = fmin(mn[c], __shfl_xor_sync(0xffffffffu, mn[c], o));
-            mx[c] = fmax(mx[c], __shfl_xor_sync(0xffffffffu, mx[c], o));
+            mn[c] = min(mn[c], __shfl_xor_sync(0xffffffffu, mn[c], o));
+            mx[c] = max(mx[c], __shfl_xor_sync(0xffffffffu, mx[c], o));
         }
         if (lane == 0) {
             s[c][warp] = mn[c];
@@ -193,10 +182,38 @@ __global__ __launch_bounds__(kThreads) void k_flags_bbox(int64_t n, const double
     __syncthreads();
     if (threadIdx.x < 6) {
         bool isMin = threadIdx.x < 3;
-        double v = s[threadIdx.x][0];
-        for (int w = 1; w < kThreads / 32; ++w) v = isMin ? fmin(v, s[threadIdx.x][w]) : fmax(v, s[threadIdx.x][w]);
-        part[blockIdx.x * 6 + threadIdx.x] = v;
+        long long v = s[threadIdx.x][0];
+        for (int w = 1; w < kBlock / 32; ++w) v = isMin ? min(v, s[threadIdx.x][w]) : max(v, s[threadIdx.x][w]);
+        part[blockIdx.x * 6 + threadIdx.x] = __longlong_as_double(v);
     }
+}
+
+// Star flags, per-block bbox partials; alive holes get zero acceleration (bh.go:148-150).
+__global__ __launch_bounds__(kThreads) void k_flags_bbox(int64_t n, const double *__restrict__ px,
+                                                         const double *__restrict__ py, const double *__restrict__ pz,
+                                                         const uint8_t *__restrict__ kind,
+                                                         const uint8_t *__restrict__ alive, uint32_t *__restrict__ flag,
+                                                         double *__restrict__ part, double *ax, double *ay, double *az) {
+    long long mn[3] = {LLONG_MAX, LLONG_MAX, LLONG_MAX}, mx[3] = {LLONG_MIN, LLONG_MIN, LLONG_MIN};
+    for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
+        uint8_t al = alive ? alive[i] : 1, kd = kind ? kind[i] : 0;
+        bool st = is_star(al, kd);
+        flag[i] = st;
+        if (st) {
+            long long x = ord_key(px[i]), y = ord_key(py[i]), z = ord_key(pz[i]);
+            mn[0] = min(mn[0], x);
+            mx[0] = max(mx[0], x);
+            mn[1] = min(mn[1], y);
+            mx[1] = max(mx[1], y);
+            mn[2] = min(mn[2], z);
+            mx[2] = max(mx[2], z);
+        } else if (al && kd == GBH_BLACK_HOLE) {
+            ax[i] = 0;
+            ay[i] = 0;
+            az[i] = 0;
+        }
+    }
+    block_minmax<kThreads>(mn, mx, part);
 }
 
 // Root cube (build.go:19-21): side = max(max extent * (1+1e-9), 1e-12), scale = 2^21 / side.
@@ -205,34 +222,35 @@ constexpr int kFinalThreads = 1024;
 __global__ __launch_bounds__(kFinalThreads) void k_bbox_final(int nparts, const double *__restrict__ part, int64_t n,
                                                               const uint32_t *__restrict__ scan, const uint8_t *kind,
                                                               const uint8_t *alive, double theta, DevInfo *info) {
-    double mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
+    long long kmn[3] = {LLONG_MAX, LLONG_MAX, LLONG_MAX}, kmx[3] = {LLONG_MIN, LLONG_MIN, LLONG_MIN};
     for (int b = threadIdx.x; b < nparts; b += blockDim.x)
         for (int c = 0; c < 3; ++c) {
-            mn[c] = fmin(mn[c], part[b * 6 + c]);
-            mx[c] = fmax(mx[c], part[b * 6 + 3 + c]);
+            kmn[c] = min(kmn[c], __double_as_longlong(part[b * 6 + c]));
+            kmx[c] = max(kmx[c], __double_as_longlong(part[b * 6 + 3 + c]));
         }
-    __shared__ double s[6][kFinalThreads / 32];
+    __shared__ long long s[6][kFinalThreads / 32];
     int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (int c = 0; c < 3; ++c) {
         for (int o = 16; o > 0; o >>= 1) {
-            mn[c] = fmin(mn[c], __shfl_xor_sync(0xffffffffu, mn[c], o));
-            mx[c] = fmax(mx[c], __shfl_xor_sync(0xffffffffu, mx[c], o));
+            kmn[c] = min(kmn[c], __shfl_xor_sync(0xffffffffu, kmn[c], o));
+            kmx[c] = max(kmx[c], __shfl_xor_sync(0xffffffffu, kmx[c], o));
         }
         if (lane == 0) {
-            s[c][warp] = mn[c];
-            s[3 + c][warp] = mx[c];
+            s[c][warp] = kmn[c];
+            s[3 + c][warp] = kmx[c];
         }
     }
     __syncthreads();
     if (threadIdx.x != 0) return;
     for (int w = 1; w < int(blockDim.x / 32); ++w)
         for (int c = 0; c < 3; ++c) {
-            s[c][0] = fmin(s[c][0], s[c][w]);
-            s[3 + c][0] = fmax(s[3 + c][0], s[3 + c][w]);
+            s[c][0] = min(s[c][0], s[c][w]);
+            s[3 + c][0] = max(s[3 + c][0], s[3 + c][w]);
         }
+    double mn[3], mx[3];
     for (int c = 0; c < 3; ++c) {
-        mn[c] = s[c][0];
-        mx[c] = s[3 + c][0];
+        mn[c] = ord_val(s[c][0]);
+        mx[c] = ord_val(s[3 + c][0]);
     }
     int64_t ns = 0;
     if (n > 0) ns = int64_t(scan[n - 1]) + (is_star(alive ? alive[n - 1] : 1, kind ? kind[n - 1] : 0) ? 1 : 0);
@@ -389,7 +407,7 @@ __global__ __launch_bounds__(kRsThreads) void k_rs_scatter(const uint64_t *__res
 __global__ __launch_bounds__(kThreads) void k_gather(const DevInfo *info, const int32_t *__restrict__ order,
                                                      const double *__restrict__ px, const double *__restrict__ py,
                                                      const double *__restrict__ pz, const double *__restrict__ mass,
-                                                     const uint8_t *__restrict__ kind, int dm_off,
+                                                     const uint8_t *__restrict__ kind, int dm_off, int fp64_copies,
                                                      double *__restrict__ sx, double *__restrict__ sy,
                                                      double *__restrict__ sz, double *__restrict__ sm,
                                                      float4 *__restrict__ st_hi, float4 *__restrict__ st_lo) {
@@ -399,10 +417,12 @@ __global__ __launch_bounds__(kThreads) void k_gather(const DevInfo *info, const 
     double x = px[i], y = py[i], z = pz[i];
     double m = mass[i];
     if (dm_off && kind && kind[i] == GBH_DARK_MATTER) m = 0;
-    sx[k] = x;
-    sy[k] = y;
-    sz[k] = z;
-    sm[k] = m;
+    if (fp64_copies) {  // read by the FP64 upsweep, walk and potential only
+        sx[k] = x;
+        sy[k] = y;
+        sz[k] = z;
+        sm[k] = m;
+    }
     float hx = __double2float_rn(x), hy = __double2float_rn(y), hz = __double2float_rn(z);
     st_hi[k] = make_float4(hx, hy, hz, __double2float_rn(m));
     st_lo[k] = make_float4(__double2float_rn(x - double(hx)), __double2float_rn(y - double(hy)),
@@ -502,6 +522,7 @@ __global__ __launch_bounds__(kThreads) void k_chain_emit(const uint64_t *__restr
                                                          int32_t *__restrict__ pre_parent,
                                                          uint32_t *__restrict__ pre_info,
                                                          uint32_t *__restrict__ pre_nchild,
+                                                         uint32_t *__restrict__ pre_mask,
                                                          int32_t *__restrict__ leaves) {
     int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     int64_t n = info->nstars;
@@ -531,15 +552,13 @@ __global__ __launch_bounds__(kThreads) void k_chain_emit(const uint64_t *__restr
     for (uint32_t t = 0; t < c; ++t, ++p) {
         int L = L0 + int(t);
         uint32_t oct = L == 0 ? 0u : uint32_t(key >> (3 * (kMaxLevel - L))) & 7u;
-        uint32_t mask = 0;
-        if (t + 1 < c) {  // the node splits: occupied octants of level L+1 inside it
-            int64_t e = cell_end(keys, n, i, L);
-            int sh = 3 * (kMaxLevel - L - 1);
-            for (int64_t j = i; j < e; j = cell_end(keys, n, j, L + 1)) mask |= 1u << (uint32_t(keys[j] >> sh) & 7u);
+        int32_t par = t == 0 ? parent_pre : int32_t(p) - 1;
+        pre_parent[p] = par;
+        pre_info[p] = uint32_t(L) | oct << 8;
+        if (par >= 0) {  // every node marks its octant in its parent's child mask (both zeroed first)
+            atomicOr(&pre_mask[par], 1u << oct);
+            atomicAdd(&pre_nchild[par], 1u);
         }
-        pre_parent[p] = t == 0 ? parent_pre : int32_t(p) - 1;
-        pre_info[p] = uint32_t(L) | oct << 8 | mask << 16;
-        pre_nchild[p] = __popc(mask);
     }
 }
 
@@ -549,6 +568,7 @@ __global__ __launch_bounds__(kThreads) void k_ref_index(const DevInfo *info, con
                                                         const uint32_t *__restrict__ base,
                                                         const int32_t *__restrict__ pre_parent,
                                                         const uint32_t *__restrict__ pre_info,
+                                                        const uint32_t *__restrict__ pre_mask,
                                                         const uint32_t *__restrict__ child_base,
                                                         int32_t *__restrict__ pre_ref) {
     int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
@@ -562,7 +582,7 @@ __global__ __launch_bounds__(kThreads) void k_ref_index(const DevInfo *info, con
             continue;
         }
         uint32_t oct = (pre_info[p] >> 8) & 0xffu;
-        uint32_t pmask = pre_info[pp] >> 16;
+        uint32_t pmask = pre_mask[pp];
         pre_ref[p] = int32_t(1 + child_base[pp] + __popc(pmask & ((1u << oct) - 1u)));
     }
 }
@@ -573,6 +593,7 @@ __global__ __launch_bounds__(kThreads) void k_emit_nodes(const uint64_t *__restr
                                                          const uint32_t *__restrict__ base,
                                                          const int32_t *__restrict__ pre_parent,
                                                          const uint32_t *__restrict__ pre_info,
+                                                         const uint32_t *__restrict__ pre_mask,
                                                          const uint32_t *__restrict__ child_base,
                                                          const int32_t *__restrict__ pre_ref, gbh_node *__restrict__ nodes,
                                                          int32_t *__restrict__ n_parent, uint32_t *__restrict__ n_info,
@@ -586,7 +607,7 @@ __global__ __launch_bounds__(kThreads) void k_emit_nodes(const uint64_t *__restr
     for (uint32_t t = 0; t < c; ++t, ++p) {
         uint32_t inf = pre_info[p];
         int L = int(inf & 0xffu);
-        uint32_t mask = inf >> 16;
+        uint32_t mask = pre_mask[p];
         int64_t hi = cell_end(keys, n, i, L);
         int32_t r = pre_ref[p];
         if (r < 0 || r >= nn) {
@@ -1058,7 +1079,7 @@ static cudaError_t scan_dyn(const Launch &L, const uint32_t *in, uint32_t *out, 
 
 void tree_free(TreeBufs &b) {
     void *ptrs[] = {b.flag, b.bbox_part, b.keys, b.keys_alt, b.order, b.order_alt, b.hist, b.sx, b.sy, b.sz, b.sm,
-                    b.st_hi, b.st_lo, b.chain_cnt, b.leaves, b.pre_parent, b.pre_info, b.pre_nchild, b.pre_ref, b.nodes,
+                    b.st_hi, b.st_lo, b.chain_cnt, b.leaves, b.pre_parent, b.pre_info, b.pre_nchild, b.pre_mask, b.pre_ref, b.nodes,
                     b.n_parent, b.n_info, b.n_arrive, b.pnodes, b.mnodes, b.mrange, b.scan_tmp, b.info};
     for (void *p : ptrs)
         if (p) cudaFree(p);
@@ -1075,7 +1096,9 @@ cudaError_t tree_alloc(TreeBufs &b, int64_t n, int leaf) {
     int64_t cn = n > b.cap_n ? n + n / 4 : b.cap_n;  // grow by 1.25x like gpuBuffers.ensure (gpu_darwin.go:164-177)
     int64_t cnodes = need_nodes > b.cap_nodes ? node_capacity(cn, leaf) : b.cap_nodes;
     if (cnodes < need_nodes) cnodes = need_nodes;
+    const int64_t gen = b.generation + 1;
     tree_free(b);
+    b.generation = gen;
     cn = cn < 1 ? 1 : cn;
     int64_t rs_tiles = (cn + kRsTile - 1) / kRsTile;
     int64_t scan_cap = scan_tmp_size(cnodes > cn * 1 ? cnodes : cn);
@@ -1105,6 +1128,7 @@ cudaError_t tree_alloc(TreeBufs &b, int64_t n, int leaf) {
     GBH_ALLOC(b.pre_parent, cnodes);
     GBH_ALLOC(b.pre_info, cnodes);
     GBH_ALLOC(b.pre_nchild, cnodes);
+    GBH_ALLOC(b.pre_mask, cnodes);
     GBH_ALLOC(b.pre_ref, cnodes);
     GBH_ALLOC(b.nodes, cnodes);
     GBH_ALLOC(b.n_parent, cnodes);
@@ -1169,8 +1193,8 @@ cudaError_t tree_build(const Launch &L, TreeBufs &b, int64_t n, const double *px
     }
     // sorted copies (build.go:34-41)
     const unsigned nb = blocks_for(cap, kThreads);
-    k_gather<<<nb, kThreads, 0, s>>>(b.info, b.order, px, py, pz, mass, kind, dm_off, b.sx, b.sy, b.sz, b.sm, b.st_hi,
-                                     b.st_lo);
+    k_gather<<<nb, kThreads, 0, s>>>(b.info, b.order, px, py, pz, mass, kind, dm_off, exact ? 1 : 0, b.sx, b.sy, b.sz,
+                                     b.sm, b.st_hi, b.st_lo);
     GBH_LAUNCH_CHECK();
     // node set
     uint32_t *cnt = b.chain_cnt, *base = b.chain_cnt + cap;
@@ -1178,14 +1202,19 @@ cudaError_t tree_build(const Launch &L, TreeBufs &b, int64_t n, const double *px
     GBH_LAUNCH_CHECK();
     e = scan_dyn(L, cnt, base, cap, &b.info->nstars, b.scan_tmp, b.scan_tmp_cap);
     if (e != cudaSuccess) return e;
-    k_chain_emit<<<nb, kThreads, 0, s>>>(b.keys, b.info, cnt, base, b.pre_parent, b.pre_info, b.pre_nchild, b.leaves);
+    e = cudaMemsetAsync(b.pre_mask, 0, sizeof(uint32_t) * size_t(b.cap_nodes), s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(b.pre_nchild, 0, sizeof(uint32_t) * size_t(b.cap_nodes), s);
+    if (e != cudaSuccess) return e;
+    k_chain_emit<<<nb, kThreads, 0, s>>>(b.keys, b.info, cnt, base, b.pre_parent, b.pre_info, b.pre_nchild, b.pre_mask,
+                                         b.leaves);
     GBH_LAUNCH_CHECK();
     e = scan_dyn(L, b.pre_nchild, b.pre_nchild, b.cap_nodes, &b.info->nnodes, b.scan_tmp, b.scan_tmp_cap);
     if (e != cudaSuccess) return e;
-    k_ref_index<<<nb, kThreads, 0, s>>>(b.info, cnt, base, b.pre_parent, b.pre_info, b.pre_nchild, b.pre_ref);
+    k_ref_index<<<nb, kThreads, 0, s>>>(b.info, cnt, base, b.pre_parent, b.pre_info, b.pre_mask, b.pre_nchild,
+                                        b.pre_ref);
     GBH_LAUNCH_CHECK();
-    k_emit_nodes<<<nb, kThreads, 0, s>>>(b.keys, b.info, cnt, base, b.pre_parent, b.pre_info, b.pre_nchild, b.pre_ref,
-                                         b.nodes, b.n_parent, b.n_info, b.n_arrive);
+    k_emit_nodes<<<nb, kThreads, 0, s>>>(b.keys, b.info, cnt, base, b.pre_parent, b.pre_info, b.pre_mask, b.pre_nchild,
+                                         b.pre_ref, b.nodes, b.n_parent, b.n_info, b.n_arrive);
     GBH_LAUNCH_CHECK();
     b.moments_exact = exact;
     if (!exact) return upsweep_fast(L, b, plain_records);
@@ -1262,40 +1291,21 @@ __global__ __launch_bounds__(kThreads) void k_flags_bbox_noacc(int64_t n, const 
                                                                const uint8_t *__restrict__ kind,
                                                                const uint8_t *__restrict__ alive,
                                                                uint32_t *__restrict__ flag, double *__restrict__ part) {
-    double mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
+    long long mn[3] = {LLONG_MAX, LLONG_MAX, LLONG_MAX}, mx[3] = {LLONG_MIN, LLONG_MIN, LLONG_MIN};
     for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
         bool st = is_star(alive ? alive[i] : 1, kind ? kind[i] : 0);
         flag[i] = st;
         if (st) {
-            double x = px[i], y = py[i], z = pz[i];
-            mn[0] = fmin(mn[0], x);
-            mx[0] = fmax(mx[0], x);
-            mn[1] = fmin(mn[1], y);
-            mx[1] = fmax(mx[1], y);
-            mn[2] = fmin(mn[2], z);
-            mx[2] = fmax(mx[2], z);
+            long long x = ord_key(px[i]), y = ord_key(py[i]), z = ord_key(pz[i]);
+            mn[0] = min(mn[0], x);
+            mx[0] = max(mx[0], x);
+            mn[1] = min(mn[1], y);
+            mx[1] = max(mx[1], y);
+            mn[2] = min(mn[2], z);
+            mx[2] = max(mx[2], z);
         }
     }
-    __shared__ double s[6][kThreads / 32];
-    int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
-        for (int o = 16; o > 0; o >>= 1) {
-            mn[c] = fmin(mn[c], __shfl_xor_sync(0xffffffffu, mn[c], o));
-            mx[c] = fmax(mx[c], __shfl_xor_sync(0xffffffffu, mx[c], o));
-        }
-        if (lane == 0) {
-            s[c][warp] = mn[c];
-            s[3 + c][warp] = mx[c];
-        }
-    }
-    __syncthreads();
-    if (threadIdx.x < 6) {
-        bool isMin = threadIdx.x < 3;
-        double v = s[threadIdx.x][0];
-        for (int w = 1; w < kThreads / 32; ++w) v = isMin ? fmin(v, s[threadIdx.x][w]) : fmax(v, s[threadIdx.x][w]);
-        part[blockIdx.x * 6 + threadIdx.x] = v;
-    }
+    block_minmax<kThreads>(mn, mx, part);
 }
 }  // namespace
 

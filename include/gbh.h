@@ -70,9 +70,15 @@ typedef struct {
     int32_t walk;            /* GBH_WALK_* */
 } gbh_params;
 
+enum {
+    /* Steps launch their kernels one by one instead of replaying a captured CUDA graph. */
+    GBH_CFG_NO_GRAPHS = 1
+};
+
 typedef struct {
     int32_t device;          /* CUDA device ordinal */
-    int32_t reserved[7];     /* zero */
+    int32_t flags;           /* GBH_CFG_* bits */
+    int32_t reserved[6];     /* zero */
 } gbh_config;
 
 /* One tree node, field for field internal/sim/bh/bh.go:108-116 (104 bytes). */
@@ -146,7 +152,10 @@ int gbh_direct_accelerations(gbh_ctx *ctx, const gbh_params *p, int64_t n, const
  * no alive black holes and no gas hydro: kick(dt/2), drift(dt) (c = 0,
  * sim.go:327-334), Solver.Accelerations, kick(dt/2). If acc_valid is 0 the
  * forces are computed first (initForces, gas.go:14-17). Arrays are read and
- * written in place; the state stays on the device between the steps.
+ * written in place; the state stays on the device between the steps. Each
+ * step replays one CUDA graph (captured on first use for the sizes and
+ * parameters given, re-captured when they change) unless the context was
+ * created with GBH_CFG_NO_GRAPHS; results are identical either way.
  */
 int gbh_step_kdk(gbh_ctx *ctx, const gbh_params *p, double dt, int64_t nsteps, int32_t acc_valid,
                  int64_t n, double *px, double *py, double *pz, double *vx, double *vy,

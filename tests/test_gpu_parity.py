@@ -273,6 +273,27 @@ def test_resident_steps_match_host_steps(ctx):
         assert np.array_equal(host[k], dev[k]), k
 
 
+@pytest.mark.parametrize("walk", ["mixed", "plain", "fp64"])
+def test_graph_replay_matches_plain_launches(ctx, walk):
+    """Steps replayed from a captured CUDA graph equal steps launched kernel by kernel."""
+    s = ics.plummer(30000, seed=11)
+    n = len(s["px"])
+    par = abi.make_params(0.5, 0.01, 8, False, False, walk)
+    out = []
+    for c in (ctx, abi.Context(0, abi.CFG_NO_GRAPHS)):
+        c.call("gbh_state_upload", n, *[P(s[k]) for k in ("px", "py", "pz", "vx", "vy", "vz")], None, None, None,
+               P(s["mass"]), None, None)
+        c.call("gbh_state_step", par, 1e-3, 2)
+        c.call("gbh_state_step", par, 1e-3, 1)
+        t = c.timings()
+        assert t["walk_ms"] > 0 and t["build_ms"] > 0
+        st = {k: np.zeros(n) for k in ("px", "py", "pz", "vx", "vy", "vz", "ax", "ay", "az")}
+        c.call("gbh_state_download", *[P(st[k]) for k in ("px", "py", "pz", "vx", "vy", "vz", "ax", "ay", "az")])
+        out.append(st)
+    for k in out[0]:
+        assert np.array_equal(out[0][k], out[1][k]), k
+
+
 def test_step_rejects_holes(ctx):
     s = ics.test_disk(500)
     n = len(s["px"])
