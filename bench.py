@@ -183,9 +183,11 @@ def run(args):
         ctx.call("gbh_state_upload", n, *[P(state[k]) for k in ("px", "py", "pz", "vx", "vy", "vz")],
                  None, None, None, P(state["mass"]), None, None)
 
-    def timed_steps(walk, steps, warmup):
+    def timed_steps(walk, steps, warmup, diag=None):
         par = abi.make_params(THETA, EPS, args.leaf, False, False, walk)
         upload(s)
+        if diag is not None:
+            diag.append(ctx.diagnostics(par))
         for _ in range(warmup):
             ctx.call("gbh_state_step", par, DT, 1)
         barrier()
@@ -201,14 +203,22 @@ def run(args):
             build_ms += t["build_ms"]
             launches += t["launches"]
         barrier()
+        if diag is not None:
+            diag.append(ctx.diagnostics(par))
         return tot, walk_ms, build_ms, launches, t["nnodes"]
 
     peak = ctx.probe_fp32_peak(100.0)
 
     # headline: mixed walk, resident state
+    diag = []
     with Clocks(local) as clk:
-        t_mixed, w_mixed, b_mixed, launches, nnodes = timed_steps("mixed", args.steps, args.warmup)
+        t_mixed, w_mixed, b_mixed, launches, nnodes = timed_steps("mixed", args.steps, args.warmup, diag)
     clocks = clk.summary()
+    e0, e1 = diag[0]["total"], diag[1]["total"]
+    l0, l1 = np.array(diag[0]["angular_momentum"]), np.array(diag[1]["angular_momentum"])
+    drift = {"steps": args.warmup + args.steps, "dt": DT, "energy_rel": abs((e1 - e0) / e0),
+             "angular_momentum_rel": float(np.linalg.norm(l1 - l0) / np.linalg.norm(l0)),
+             "energy_method": "FP64 tree potential at theta 0.5 + FP64 kinetic (gbh_state_diagnostics)"}
     t_plain, w_plain, b_plain, _, _ = timed_steps("plain", args.steps, args.warmup)
 
     # max over ranks
@@ -297,6 +307,7 @@ def run(args):
             "plain": {"value": plain_value, "ms_per_step": t_plain / args.steps, "walk_ms": w_plain / args.steps,
                       "force_error": errs["plain"], "speedup_mixed_over_plain": value / plain_value},
             "force_error": errs["mixed"],
+            "drift": drift,
             "interactions": {"accepted_nodes": n_pn, "leaf_pairs": n_pp, "opened_nodes": n_open,
                              "per_star": (n_pn + n_pp) / n, "nodes": nnodes},
         }

@@ -50,6 +50,24 @@ class Timings(ctypes.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class BlockStats(ctypes.Structure):
+    _fields_ = [("substeps", ctypes.c_int64), ("evaluations", ctypes.c_int64), ("min_substep_ticks", ctypes.c_int32),
+                ("reserved", ctypes.c_int32)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}
+
+
+class Diagnostics(ctypes.Structure):
+    _fields_ = [("kinetic", ctypes.c_double), ("potential", ctypes.c_double), ("total", ctypes.c_double),
+                ("momentum", ctypes.c_double * 3), ("angular_momentum", ctypes.c_double * 3),
+                ("center_of_mass", ctypes.c_double * 3), ("mass", ctypes.c_double)]
+
+    def as_dict(self):
+        return {k: (list(getattr(self, k)) if k in ("momentum", "angular_momentum", "center_of_mass")
+                    else getattr(self, k)) for k, _ in self._fields_}
+
+
 NODE_DTYPE = np.dtype(
     [("x", "f8"), ("y", "f8"), ("z", "f8"), ("m", "f8"),
      ("qxx", "f8"), ("qyy", "f8"), ("qzz", "f8"), ("qxy", "f8"), ("qxz", "f8"), ("qyz", "f8"),
@@ -79,6 +97,8 @@ SIGNATURES = {
     "gbh_tree_export": (ctypes.c_int, [_P, _P, _P, _P, _I64]),
     "gbh_last_timings": (ctypes.c_int, [_P, ctypes.POINTER(Timings)]),
     "gbh_probe_fp32_peak": (ctypes.c_int, [_P, _D, _P]),
+    "gbh_state_diagnostics": (ctypes.c_int, [_P, _PP, _D, _P]),
+    "gbh_state_step_block": (ctypes.c_int, [_P, _PP, _D, _D, _I32, _I64, _P]),
     "gbh_morton_order_noalloc": (ctypes.c_int, [_I32, _P, _I64] + [_P] * 8 + [ctypes.c_char_p, ctypes.c_int]),
 }
 
@@ -195,6 +215,16 @@ class Context:
         nodes = np.zeros(nn, NODE_DTYPE)
         self.call("gbh_tree_export", ptr(keys), ptr(order), ptr(nodes), nn)
         return dict(keys=keys, order=order, nodes=nodes)
+
+    def step_block(self, params: Params, dt: float, eta: float, levels: int, nsteps: int) -> dict:
+        st = BlockStats()
+        self.call("gbh_state_step_block", params, float(dt), float(eta), int(levels), int(nsteps), ctypes.byref(st))
+        return st.as_dict()
+
+    def diagnostics(self, params: Params, c: float = 0.0) -> dict:
+        d = Diagnostics()
+        self.call("gbh_state_diagnostics", params, float(c), ctypes.byref(d))
+        return d.as_dict()
 
     def probe_fp32_peak(self, ms: float = 50.0) -> float:
         out = np.zeros(1)

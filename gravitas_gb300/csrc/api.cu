@@ -54,6 +54,12 @@ struct gbh_ctx {
     double *tout = nullptr;
     int64_t targets_cap = 0;
     float *probe = nullptr;
+    double *scratch3 = nullptr;  // 3 x n doubles the diagnostics' tree build may write
+    int64_t scratch3_cap = 0;
+    uint8_t *rung = nullptr;     // block steps: rung and step-end tick per body
+    int64_t rung_cap = 0;
+    int32_t *end_tick = nullptr;
+    int64_t end_cap = 0;
     // per-stage events of the current call: (build start, walk start, walk end) triples
     std::vector<cudaEvent_t> evpool;
     size_t evused = 0;
@@ -363,6 +369,90 @@ int run_steps(gbh_ctx *ctx, const gbh_params *p, double dt, int64_t nsteps) {
     return GBH_OK;
 }
 
+// Forces on the stars whose step ends at tick (block steps): tree of all stars, walk of the
+// active ones only.
+int forces_active(gbh_ctx *ctx, const gbh_params *p, const uint8_t *kind, const uint8_t *alive, const int32_t *end,
+                  int32_t tick) {
+    Launch L = launch_of(ctx);
+    int leaf = leaf_of(p);
+    int64_t n = ctx->n;
+    CK(gbh::tree_alloc(ctx->tb, n, leaf));
+    CK(stage_event(ctx));
+    CK(gbh::tree_build(L, ctx->tb, n, ctx->px, ctx->py, ctx->pz, ctx->mass, kind, alive, ctx->ax, ctx->ay, ctx->az,
+                       theta_of(p), leaf, p->dark_matter_off, p->walk == GBH_WALK_FP64, p->walk == GBH_WALK_PLAIN));
+    CK(gbh::select_targets(L, ctx->tb, end, tick));
+    CK(stage_event(ctx));
+    double eps2 = p->softening * p->softening;
+    int quad = !p->monopole_only;
+    switch (p->walk) {
+        case GBH_WALK_FP64:
+            CK(gbh::walk_fp64(L, ctx->tb, n, eps2, quad, ctx->ax, ctx->ay, ctx->az, true));
+            break;
+        case GBH_WALK_PLAIN:
+            if (!quad) return fail(ctx, GBH_ERR_ARG, "the plain FP32 walk always uses quadrupoles (as the Metal kernel)");
+            CK(gbh::walk_plain(L, ctx->tb, ctx->tb.cap_n, float(eps2), ctx->ax, ctx->ay, ctx->az, true));
+            break;
+        default:
+            CK(gbh::walk_mixed(L, ctx->tb, ctx->tb.cap_n, float(eps2), quad, ctx->ax, ctx->ay, ctx->az, true));
+            break;
+    }
+    CK(stage_event(ctx));
+    return GBH_OK;
+}
+
+// Reads the device scalars (next event tick, active count) after the work issued so far.
+int read_info(gbh_ctx *ctx) {
+    CK(cudaMemcpyAsync(&ctx->info_host, ctx->tb.info, sizeof(DevInfo), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    if (ctx->info_host.err)
+        return fail(ctx, GBH_ERR_LIMIT, "device walk exceeded its step bound (kernel %d)", ctx->info_host.err_where);
+    return GBH_OK;
+}
+
+// Block-step KDK on the resident state (see block_open in tree.cu for the scheme).
+int run_block_steps(gbh_ctx *ctx, const gbh_params *p, double T, double eta, int levels, int64_t nsteps,
+                    gbh_blockstats *st) {
+    Launch L = launch_of(ctx);
+    const int64_t n = ctx->n;
+    const uint8_t *kind = ctx->state_has_kind ? ctx->kind : nullptr;
+    const uint8_t *alive = ctx->state_has_alive ? ctx->alive : nullptr;
+    const int32_t ticks = 1 << (levels - 1);
+    const double eps = p->softening;
+    CK(grow(ctx->rung, ctx->rung_cap, n));
+    CK(grow(ctx->end_tick, ctx->end_cap, n));
+    if (!ctx->acc_valid) {  // initForces (gas.go:14-17)
+        int rc = forces(ctx, p, n, ctx->px, ctx->py, ctx->pz, ctx->mass, kind, alive, ctx->ax, ctx->ay, ctx->az,
+                        theta_of(p));
+        if (rc) return rc;
+        ctx->acc_valid = true;
+    }
+    CK(gbh::tree_alloc(ctx->tb, n, leaf_of(p)));
+    int rc;
+    for (int64_t s = 0; s < nsteps; ++s) {
+        CK(gbh::block_open(L, ctx->tb, n, T, levels, eta, eps, ctx->ax, ctx->ay, ctx->az, ctx->vx, ctx->vy, ctx->vz,
+                           ctx->rung, ctx->end_tick));
+        if ((rc = read_info(ctx))) return rc;
+        int32_t t = 0;
+        while (t < ticks) {
+            int32_t tn = ctx->info_host.next_tick;
+            if (tn <= t || tn > ticks) return fail(ctx, GBH_ERR_LIMIT, "block steps: next event %d after %d", tn, t);
+            if (st && (st->min_substep_ticks == 0 || tn - t < st->min_substep_ticks)) st->min_substep_ticks = tn - t;
+            CK(gbh::block_drift(L, n, double(tn - t) * (T / double(ticks)), ctx->px, ctx->py, ctx->pz, ctx->vx,
+                                ctx->vy, ctx->vz));
+            t = tn;
+            if ((rc = forces_active(ctx, p, kind, alive, ctx->end_tick, t))) return rc;
+            CK(gbh::block_close(L, ctx->tb, n, t, T, levels, eta, eps, ctx->ax, ctx->ay, ctx->az, ctx->vx, ctx->vy,
+                                ctx->vz, ctx->rung, ctx->end_tick));
+            if ((rc = read_info(ctx))) return rc;
+            if (st) {
+                st->substeps += 1;
+                st->evaluations += ctx->info_host.ntargets;
+            }
+        }
+    }
+    return GBH_OK;
+}
+
 int upload_state(gbh_ctx *ctx, int64_t n, const double *px, const double *py, const double *pz, const double *vx,
                  const double *vy, const double *vz, const double *ax, const double *ay, const double *az,
                  const double *mass, const uint8_t *kind, const uint8_t *alive) {
@@ -457,7 +547,7 @@ void gbh_destroy(gbh_ctx *c) {
     free_graph(c->step_graph);
     gbh::tree_free(c->tb);
     free_state(c);
-    void *ptrs[] = {c->part, c->scalar, c->holes, c->targets, c->tout, c->probe};
+    void *ptrs[] = {c->part, c->scalar, c->holes, c->targets, c->tout, c->probe, c->scratch3, c->rung, c->end_tick};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     for (auto &ev : c->ev)
@@ -540,7 +630,7 @@ int gbh_potential_energy(gbh_ctx *ctx, const gbh_params *p, int64_t n, const dou
                        alive ? ctx->alive : nullptr, ctx->ax, ctx->ay, ctx->az, theta, leaf, p->dark_matter_off, true));
     int64_t nparts = (ctx->tb.cap_n + 255) / 256;
     CK(grow(ctx->part, ctx->part_cap, nparts));
-    if (!ctx->scalar) CK(cudaMalloc(&ctx->scalar, 64));
+    if (!ctx->scalar) CK(cudaMalloc(&ctx->scalar, 256));
     double eps2 = p->softening * p->softening;
     CK(gbh::potential_fp64(L, ctx->tb, n, ctx->px, ctx->py, ctx->pz, ctx->mass, kind ? ctx->kind : nullptr,
                            alive ? ctx->alive : nullptr, ctx->holes, int32_t(holes.size()), eps2, c,
@@ -637,6 +727,24 @@ int gbh_state_step(gbh_ctx *ctx, const gbh_params *p, double dt, int64_t nsteps)
     return finish(ctx, ctx->n > 0);
 }
 
+int gbh_state_step_block(gbh_ctx *ctx, const gbh_params *p, double dt, double eta, int32_t levels, int64_t nsteps,
+                         gbh_blockstats *stats) {
+    int rc = begin(ctx);
+    if (rc || (rc = check_params(ctx, p))) return rc;
+    if (!ctx->have_state) return fail(ctx, GBH_ERR_STATE, "no resident state (gbh_state_upload first)");
+    if (nsteps < 0) return fail(ctx, GBH_ERR_ARG, "nsteps < 0");
+    if (levels < 1 || levels > 16) return fail(ctx, GBH_ERR_ARG, "levels %d outside [1, 16]", levels);
+    if (!(eta > 0)) return fail(ctx, GBH_ERR_ARG, "eta must be > 0");
+    if (!(dt > 0)) return fail(ctx, GBH_ERR_ARG, "dt must be > 0");
+    if (ctx->state_holes)
+        return fail(ctx, GBH_ERR_UNSUPPORTED,
+                    "alive black holes need the hole-aware split step (sim.stepSplit), which this path does not cover");
+    if (stats) *stats = gbh_blockstats{};
+    CK(cudaEventRecord(ctx->ev[0], ctx->stream));
+    if (ctx->n > 0 && (rc = run_block_steps(ctx, p, dt, eta, levels, nsteps, stats))) return rc;
+    return finish(ctx, ctx->n > 0);
+}
+
 int gbh_state_accelerations(gbh_ctx *ctx, const gbh_params *p) {
     int rc = begin(ctx);
     if (rc || (rc = check_params(ctx, p))) return rc;
@@ -648,6 +756,65 @@ int gbh_state_accelerations(gbh_ctx *ctx, const gbh_params *p) {
     if (rc) return rc;
     ctx->acc_valid = true;
     return finish(ctx, true);
+}
+
+int gbh_state_diagnostics(gbh_ctx *ctx, const gbh_params *p, double c, gbh_diagnostics *out) {
+    int rc = begin(ctx);
+    if (rc || (rc = check_params(ctx, p))) return rc;
+    if (!out) return fail(ctx, GBH_ERR_ARG, "out is NULL");
+    if (!ctx->have_state) return fail(ctx, GBH_ERR_STATE, "no resident state (gbh_state_upload first)");
+    *out = gbh_diagnostics{};
+    if (ctx->n == 0) return GBH_OK;
+    CK(cudaEventRecord(ctx->ev[0], ctx->stream));
+    const int64_t n = ctx->n;
+    const uint8_t *kind = ctx->state_has_kind ? ctx->kind : nullptr;
+    const uint8_t *alive = ctx->state_has_alive ? ctx->alive : nullptr;
+    Launch L = launch_of(ctx);
+    CK(grow(ctx->part, ctx->part_cap, std::max<int64_t>((ctx->cap + 255) / 256, int64_t(gbh::diag_parts()) * 11)));
+    if (!ctx->scalar) CK(cudaMalloc(&ctx->scalar, 256));
+    // potential: the tree at min(theta, 0.9) with the FP64 walk (potential.go:12-42)
+    std::vector<uint8_t> hkind, halive;
+    std::vector<int32_t> holes;
+    if (ctx->state_holes) {  // hole list in state order
+        hkind.resize(size_t(n));
+        halive.assign(size_t(n), 1);
+        CK(cudaMemcpy(hkind.data(), ctx->kind, size_t(n), cudaMemcpyDeviceToHost));
+        if (alive) CK(cudaMemcpy(halive.data(), ctx->alive, size_t(n), cudaMemcpyDeviceToHost));
+        for (int64_t i = 0; i < n; ++i)
+            if (halive[size_t(i)] && hkind[size_t(i)] == GBH_BLACK_HOLE) holes.push_back(int32_t(i));
+    }
+    CK(grow(ctx->holes, ctx->holes_cap, int64_t(holes.size()) + 1));
+    if (!holes.empty()) CK(cudaMemcpy(ctx->holes, holes.data(), holes.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
+    int leaf = leaf_of(p);
+    double theta = std::min(theta_of(p), 0.9);
+    // the build zeroes alive holes' accelerations: use the force scratch of the potential path
+    CK(gbh::tree_alloc(ctx->tb, n, leaf));
+    CK(grow(ctx->scratch3, ctx->scratch3_cap, 3 * n));
+    double *sa = ctx->scratch3;
+    CK(gbh::tree_build(L, ctx->tb, n, ctx->px, ctx->py, ctx->pz, ctx->mass, kind, alive, sa, sa + n, sa + 2 * n, theta,
+                       leaf, p->dark_matter_off, true));
+    CK(gbh::potential_fp64(L, ctx->tb, n, ctx->px, ctx->py, ctx->pz, ctx->mass, kind, alive, ctx->holes,
+                           int32_t(holes.size()), p->softening * p->softening, c, p->dark_matter_off,
+                           !p->monopole_only, ctx->part, ctx->scalar));
+    double u = 0;
+    CK(cudaMemcpyAsync(&u, ctx->scalar, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    double sums[11];
+    CK(gbh::diagnostics(L, n, ctx->px, ctx->py, ctx->pz, ctx->vx, ctx->vy, ctx->vz, ctx->mass, kind, c,
+                        p->dark_matter_off, ctx->part, ctx->scalar));
+    CK(cudaMemcpyAsync(sums, ctx->scalar, sizeof sums, cudaMemcpyDeviceToHost, ctx->stream));
+    rc = finish(ctx, true);
+    if (rc) return rc;
+    out->kinetic = sums[0];
+    out->potential = u;
+    out->total = sums[0] + u;
+    for (int k = 0; k < 3; ++k) {
+        out->momentum[k] = sums[1 + k];
+        out->angular_momentum[k] = sums[4 + k];
+        out->center_of_mass[k] = sums[10] != 0 ? sums[7 + k] / sums[10] : 0.0;
+    }
+    out->mass = sums[10];
+    return GBH_OK;
 }
 
 int gbh_tree_size(gbh_ctx *ctx, int64_t *nstars, int64_t *nnodes) {

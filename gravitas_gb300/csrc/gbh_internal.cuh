@@ -30,6 +30,8 @@ struct DevInfo {
     int32_t err_where;        // which kernel set err
     uint32_t work;            // work counter of persistent kernels
     uint32_t nleaves;         // leaves appended to the leaf list
+    uint32_t ntargets;        // entries of the target list (walks restricted to active stars)
+    int32_t next_tick;        // block steps: the earliest step end over all bodies
     // FP32 views for the FP32 upsweep: min corner and side as hi + lo pairs, and the
     // opening base 2 * half_L / theta per level L
     float min_hi[3], min_lo[3];
@@ -82,6 +84,7 @@ struct TreeBufs {
     MNode *mnodes = nullptr;
     int2 *mrange = nullptr;
     int32_t *leaves = nullptr;      // sorted position of every leaf's first star
+    int32_t *targets = nullptr;     // sorted positions of the stars a restricted walk evaluates
     bool moments_exact = false;     // the last build ran the bit-exact FP64 upsweep
     // scan temporaries
     uint32_t *scan_tmp = nullptr;
@@ -106,13 +109,27 @@ cudaError_t tree_build(const Launch &L, TreeBufs &b, int64_t n, const double *px
                        const double *pz, const double *mass, const uint8_t *kind,
                        const uint8_t *alive, double *ax, double *ay, double *az, double theta,
                        int leaf_size, int dm_off, bool exact, bool plain_records = true);
+// Block time steps (see tree.cu): tick-0 opening kicks and rungs, drift of all bodies, and the
+// closing/opening kicks of the bodies whose step ends at tick. DevInfo.next_tick receives the
+// earliest step end over all bodies.
+cudaError_t block_open(const Launch &L, const TreeBufs &b, int64_t n, double T, int levels, double eta, double eps,
+                       const double *ax, const double *ay, const double *az, double *vx, double *vy, double *vz,
+                       uint8_t *rung, int32_t *end);
+cudaError_t block_drift(const Launch &L, int64_t n, double dt, double *px, double *py, double *pz, const double *vx,
+                        const double *vy, const double *vz);
+cudaError_t block_close(const Launch &L, const TreeBufs &b, int64_t n, int32_t tick, double T, int levels, double eta,
+                        double eps, const double *ax, const double *ay, const double *az, double *vx, double *vy,
+                        double *vz, uint8_t *rung, int32_t *end);
 // ---- moments.cu ----
 // FP32 upsweep; writes the walk records of the plain walk (PNode) and/or the mixed walk (MNode).
 cudaError_t upsweep_fast(const Launch &L, TreeBufs &b, bool plain_records);
 // Fills the FP64 moment fields of the node table from the MNode records (after an FP32 upsweep).
 cudaError_t export_fast_moments(const Launch &L, TreeBufs &b);
+// Walks: every star, or (targets = true) the stars listed in b.targets (count in DevInfo.ntargets).
 cudaError_t walk_fp64(const Launch &L, const TreeBufs &b, int64_t n, double eps2, int quad,
-                      double *ax, double *ay, double *az);
+                      double *ax, double *ay, double *az, bool targets = false);
+// Lists in b.targets the sorted positions whose body has end[order[k]] == tick.
+cudaError_t select_targets(const Launch &L, TreeBufs &b, const int32_t *end, int32_t tick);
 cudaError_t kick(const Launch &L, int64_t n, double h, double *vx, double *vy, double *vz,
                  const double *ax, const double *ay, const double *az);
 cudaError_t kick_drift(const Launch &L, int64_t n, double h, double dt, double *px, double *py,
@@ -128,6 +145,12 @@ cudaError_t potential_fp64(const Launch &L, const TreeBufs &b, int64_t n, const 
                            const uint8_t *kind, const uint8_t *alive, const int32_t *holes,
                            int32_t nholes, double eps2, double c, int dm_off, int quad,
                            double *part, double *u_dev);
+// Sums of diag.go: out[0] kinetic (bodies that gravitate), out[1..3] momentum, out[4..6]
+// angular momentum, out[7..9] sum m x, out[10] mass. part holds diag_parts() x 11 doubles.
+int diag_parts();
+cudaError_t diagnostics(const Launch &L, int64_t n, const double *px, const double *py, const double *pz,
+                        const double *vx, const double *vy, const double *vz, const double *mass, const uint8_t *kind,
+                        double c, int dm_off, double *part, double *out);
 // Exclusive scan of n uint32 in place (in may equal out).
 cudaError_t scan_u32(const Launch &L, const uint32_t *in, uint32_t *out, int64_t n,
                      uint32_t *tmp, int64_t tmp_cap);
@@ -143,9 +166,9 @@ cudaError_t morton_sort(const Launch &L, int64_t n, const double *px, const doub
 
 // ---- walk.cu (FP32 walks, FMA contraction on) ----
 cudaError_t walk_plain(const Launch &L, const TreeBufs &b, int64_t nstars_cap, float eps2,
-                       double *ax, double *ay, double *az);
+                       double *ax, double *ay, double *az, bool targets = false);
 cudaError_t walk_mixed(const Launch &L, const TreeBufs &b, int64_t nstars_cap, float eps2,
-                       int quad, double *ax, double *ay, double *az);
+                       int quad, double *ax, double *ay, double *az, bool targets = false);
 cudaError_t fp32_fma_probe(const Launch &L, int blocks, int iters, float *out);
 
 }  // namespace gbh

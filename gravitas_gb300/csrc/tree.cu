@@ -802,10 +802,12 @@ __global__ __launch_bounds__(kThreads) void k_walk_fp64(const DevInfo *info, con
                                                         const double *__restrict__ sx, const double *__restrict__ sy,
                                                         const double *__restrict__ sz, const double *__restrict__ sm,
                                                         const int32_t *__restrict__ order, double eps2, int quad,
-                                                        double *ax, double *ay, double *az, DevInfo *err_info) {
-    int64_t k = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+                                                        double *ax, double *ay, double *az,
+                                                        const int32_t *__restrict__ targets, DevInfo *err_info) {
+    int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     int64_t ns = info->nstars;
-    if (k >= ns) return;
+    if (t >= (targets ? int64_t(info->ntargets) : ns)) return;
+    int64_t k = targets ? int64_t(targets[t]) : t;
     int64_t nn = info->nnodes;
     double x = sx[k], y = sy[k], z = sz[k];
     double fax = 0, fay = 0, faz = 0;
@@ -1079,7 +1081,7 @@ static cudaError_t scan_dyn(const Launch &L, const uint32_t *in, uint32_t *out, 
 
 void tree_free(TreeBufs &b) {
     void *ptrs[] = {b.flag, b.bbox_part, b.keys, b.keys_alt, b.order, b.order_alt, b.hist, b.sx, b.sy, b.sz, b.sm,
-                    b.st_hi, b.st_lo, b.chain_cnt, b.leaves, b.pre_parent, b.pre_info, b.pre_nchild, b.pre_mask, b.pre_ref, b.nodes,
+                    b.st_hi, b.st_lo, b.chain_cnt, b.leaves, b.targets, b.pre_parent, b.pre_info, b.pre_nchild, b.pre_mask, b.pre_ref, b.nodes,
                     b.n_parent, b.n_info, b.n_arrive, b.pnodes, b.mnodes, b.mrange, b.scan_tmp, b.info};
     for (void *p : ptrs)
         if (p) cudaFree(p);
@@ -1125,6 +1127,7 @@ cudaError_t tree_alloc(TreeBufs &b, int64_t n, int leaf) {
     GBH_ALLOC(b.st_lo, cn);
     GBH_ALLOC(b.chain_cnt, cn * 2);  // counts, then their scan
     GBH_ALLOC(b.leaves, cn);
+    GBH_ALLOC(b.targets, cn);
     GBH_ALLOC(b.pre_parent, cnodes);
     GBH_ALLOC(b.pre_info, cnodes);
     GBH_ALLOC(b.pre_nchild, cnodes);
@@ -1225,10 +1228,10 @@ cudaError_t tree_build(const Launch &L, TreeBufs &b, int64_t n, const double *px
 }
 
 cudaError_t walk_fp64(const Launch &L, const TreeBufs &b, int64_t n, double eps2, int quad, double *ax, double *ay,
-                      double *az) {
+                      double *az, bool targets) {
     (void)n;
-    k_walk_fp64<<<blocks_for(b.cap_n, kThreads), kThreads, 0, L.stream>>>(b.info, b.nodes, b.sx, b.sy, b.sz, b.sm,
-                                                                           b.order, eps2, quad, ax, ay, az, b.info);
+    k_walk_fp64<<<blocks_for(b.cap_n, kThreads), kThreads, 0, L.stream>>>(
+        b.info, b.nodes, b.sx, b.sy, b.sz, b.sm, b.order, eps2, quad, ax, ay, az, targets ? b.targets : nullptr, b.info);
     GBH_LAUNCH_CHECK();
     return cudaSuccess;
 }
@@ -1373,6 +1376,245 @@ cudaError_t morton_sort(const Launch &L, int64_t n, const double *px, const doub
         vout = tv;
     }
     return cudaSuccess;  // eight passes: the result is back in keys/order
+}
+
+}  // namespace gbh
+
+namespace gbh {
+
+// ---------------------------------------------------------------- diagnostics (diag.go:31-135)
+
+namespace {
+
+constexpr int kDiagSums = 11;  // kinetic, p(3), L(3), m x (3), m
+
+// Per-block sums over bodies i (all bodies, as Momentum/AngularMomentum/CenterOfMass iterate
+// s.Len(); kinetic over the bodies that gravitate, sourceKinetic diag.go:80-88).
+__global__ __launch_bounds__(kThreads) void k_diag_partial(int64_t n, const double *__restrict__ px,
+                                                           const double *__restrict__ py, const double *__restrict__ pz,
+                                                           const double *__restrict__ vx, const double *__restrict__ vy,
+                                                           const double *__restrict__ vz,
+                                                           const double *__restrict__ mass,
+                                                           const uint8_t *__restrict__ kind, double c, int dm_off,
+                                                           double *__restrict__ part) {
+    double acc[kDiagSums] = {};
+    for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
+        double m = mass[i], x = px[i], y = py[i], z = pz[i], ux = vx[i], uy = vy[i], uz = vz[i];
+        uint8_t kd = kind ? kind[i] : 0;
+        bool source = !(dm_off && kd == GBH_DARK_MATTER);
+        double u2 = ux * ux + uy * uy + uz * uz;
+        double g = c <= 0 ? 1.0 : sqrt(1 + u2 / (c * c));  // gamma, relativity.go:15-20
+        if (source) acc[0] += m * u2 / (g + 1);           // kinetic, relativity.go:22-26
+        acc[1] += m * ux;
+        acc[2] += m * uy;
+        acc[3] += m * uz;
+        acc[4] += m * (y * uz - z * uy);
+        acc[5] += m * (z * ux - x * uz);
+        acc[6] += m * (x * uy - y * ux);
+        acc[7] += m * x;
+        acc[8] += m * y;
+        acc[9] += m * z;
+        acc[10] += m;
+    }
+    __shared__ double s[kThreads];
+    for (int q = 0; q < kDiagSums; ++q) {
+        s[threadIdx.x] = acc[q];
+        __syncthreads();
+        for (int o = kThreads / 2; o > 0; o >>= 1) {
+            if (threadIdx.x < o) s[threadIdx.x] += s[threadIdx.x + o];
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) part[blockIdx.x * kDiagSums + q] = s[0];
+        __syncthreads();
+    }
+}
+
+__global__ void k_diag_final(int nparts, const double *__restrict__ part, double *out) {
+    if (threadIdx.x >= kDiagSums) return;
+    double v = 0;
+    for (int b = 0; b < nparts; ++b) v += part[b * kDiagSums + threadIdx.x];
+    out[threadIdx.x] = v;
+}
+
+}  // namespace
+
+int diag_parts() { return kFlagBlocksMax; }
+
+cudaError_t diagnostics(const Launch &L, int64_t n, const double *px, const double *py, const double *pz,
+                        const double *vx, const double *vy, const double *vz, const double *mass, const uint8_t *kind,
+                        double c, int dm_off, double *part, double *out) {
+    unsigned nb = blocks_for(n, kThreads);
+    if (nb > unsigned(kFlagBlocksMax)) nb = kFlagBlocksMax;
+    k_diag_partial<<<nb, kThreads, 0, L.stream>>>(n, px, py, pz, vx, vy, vz, mass, kind, c, dm_off, part);
+    GBH_LAUNCH_CHECK();
+    k_diag_final<<<1, 32, 0, L.stream>>>(int(nb), part, out);
+    GBH_LAUNCH_CHECK();
+    return cudaSuccess;
+}
+
+}  // namespace gbh
+
+namespace gbh {
+
+// ---------------------------------------------------------------- active-star lists (block steps)
+
+namespace {
+
+__global__ __launch_bounds__(kThreads) void k_target_flags(const DevInfo *info, const int32_t *__restrict__ order,
+                                                           const int32_t *__restrict__ end, int32_t tick,
+                                                           uint32_t *__restrict__ flag) {
+    int64_t k = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (k >= info->nstars) return;
+    flag[k] = end[order[k]] == tick;
+}
+
+__global__ __launch_bounds__(kThreads) void k_target_write(DevInfo *info, const int32_t *__restrict__ order,
+                                                           const int32_t *__restrict__ end, int32_t tick,
+                                                           const uint32_t *__restrict__ pos, int32_t *__restrict__ targets) {
+    int64_t k = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    int64_t ns = info->nstars;
+    if (k >= ns) return;
+    bool on = end[order[k]] == tick;
+    if (on) targets[pos[k]] = int32_t(k);
+    if (k == ns - 1) info->ntargets = pos[k] + (on ? 1u : 0u);
+}
+
+}  // namespace
+
+cudaError_t select_targets(const Launch &L, TreeBufs &b, const int32_t *end, int32_t tick) {
+    const unsigned nb = blocks_for(b.cap_n, kThreads);
+    k_target_flags<<<nb, kThreads, 0, L.stream>>>(b.info, b.order, end, tick, b.flag);
+    GBH_LAUNCH_CHECK();
+    cudaError_t e = scan_dyn(L, b.flag, b.flag, b.cap_n, &b.info->nstars, b.scan_tmp, b.scan_tmp_cap);
+    if (e != cudaSuccess) return e;
+    k_target_write<<<nb, kThreads, 0, L.stream>>>(b.info, b.order, end, tick, b.flag, b.targets);
+    GBH_LAUNCH_CHECK();
+    return cudaSuccess;
+}
+
+}  // namespace gbh
+
+namespace gbh {
+
+// ---------------------------------------------------------------- block time steps
+//
+// Gravity has no block steps in the reference; these follow its gas block steps
+// (internal/sim/blockstep.go:22-90): a global step T is split into 2^(levels-1) ticks, a body
+// on rung r steps T / 2^r, its rung is the smallest r with T / 2^r <= dt_i (rungFor,
+// blockstep.go:38-45) capped at levels - 1, with dt_i = eta sqrt(eps / |a_i|), and a step may
+// start only at a multiple of its length (blockstep.go:84-86). Kick-drift-kick per body: an
+// opening half kick when its step starts, all bodies drift together from event to event, and
+// at the end of its step a body gets its new acceleration, the closing half kick, a new rung
+// and the next opening kick. With one level this is exactly the global KDK of sim.go.
+
+namespace {
+
+__device__ __forceinline__ int rung_for(double dt, double T, int rmax) {
+    int r = 0;
+    double x = T;
+    while (x > dt && r < rmax) {
+        x *= 0.5;
+        ++r;
+    }
+    return r;
+}
+
+__device__ __forceinline__ double body_dt(double ax, double ay, double az, double eta, double eps) {
+    double a = sqrt(ax * ax + ay * ay + az * az);
+    return a > 0 ? eta * sqrt(eps / a) : INFINITY;
+}
+
+// Tick 0 of a global step: every body starts a step (rung from its acceleration) with the
+// opening half kick.
+__global__ __launch_bounds__(kThreads) void k_block_open(int64_t n, double T, int32_t ticks, int levels, double eta,
+                                                         double eps, const double *__restrict__ ax,
+                                                         const double *__restrict__ ay, const double *__restrict__ az,
+                                                         double *vx, double *vy, double *vz, uint8_t *rung,
+                                                         int32_t *end, DevInfo *info) {
+    int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double a0 = ax[i], a1 = ay[i], a2 = az[i];
+    int r = rung_for(body_dt(a0, a1, a2, eta, eps), T, levels - 1);
+    rung[i] = uint8_t(r);
+    int32_t e = ticks >> r;
+    end[i] = e;
+    double h = 0.5 * (T / double(1 << r));
+    vx[i] += h * a0;
+    vy[i] += h * a1;
+    vz[i] += h * a2;
+    atomicMin(&info->next_tick, e);
+}
+
+__global__ __launch_bounds__(kThreads) void k_block_drift(int64_t n, double dt, double *px, double *py, double *pz,
+                                                          const double *__restrict__ vx, const double *__restrict__ vy,
+                                                          const double *__restrict__ vz) {
+    int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    px[i] += dt * vx[i];
+    py[i] += dt * vy[i];
+    pz[i] += dt * vz[i];
+}
+
+// Bodies whose step ends at tick: closing half kick with the new acceleration, then (before
+// the end of the global step) a new rung aligned to tick and the opening half kick.
+__global__ __launch_bounds__(kThreads) void k_block_close(int64_t n, int32_t tick, int32_t ticks, double T, int levels,
+                                                          double eta, double eps, const double *__restrict__ ax,
+                                                          const double *__restrict__ ay, const double *__restrict__ az,
+                                                          double *vx, double *vy, double *vz, uint8_t *rung,
+                                                          int32_t *end, DevInfo *info) {
+    int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int32_t e = end[i];
+    if (e == tick) {
+        double a0 = ax[i], a1 = ay[i], a2 = az[i];
+        double h = 0.5 * (T / double(1 << rung[i]));
+        vx[i] += h * a0;
+        vy[i] += h * a1;
+        vz[i] += h * a2;
+        if (tick < ticks) {
+            int r = rung_for(body_dt(a0, a1, a2, eta, eps), T, levels - 1);
+            while (tick % (ticks >> r) != 0) ++r;
+            rung[i] = uint8_t(r);
+            e = tick + (ticks >> r);
+            end[i] = e;
+            double h2 = 0.5 * (T / double(1 << r));
+            vx[i] += h2 * a0;
+            vy[i] += h2 * a1;
+            vz[i] += h2 * a2;
+        }
+    }
+    atomicMin(&info->next_tick, e);
+}
+
+}  // namespace
+
+cudaError_t block_open(const Launch &L, const TreeBufs &b, int64_t n, double T, int levels, double eta, double eps,
+                       const double *ax, const double *ay, const double *az, double *vx, double *vy, double *vz,
+                       uint8_t *rung, int32_t *end) {
+    cudaError_t e = cudaMemsetAsync(&b.info->next_tick, 0x7f, sizeof(int32_t), L.stream);
+    if (e != cudaSuccess) return e;
+    k_block_open<<<blocks_for(n, kThreads), kThreads, 0, L.stream>>>(n, T, 1 << (levels - 1), levels, eta, eps, ax, ay,
+                                                                     az, vx, vy, vz, rung, end, b.info);
+    GBH_LAUNCH_CHECK();
+    return cudaSuccess;
+}
+
+cudaError_t block_drift(const Launch &L, int64_t n, double dt, double *px, double *py, double *pz, const double *vx,
+                        const double *vy, const double *vz) {
+    k_block_drift<<<blocks_for(n, kThreads), kThreads, 0, L.stream>>>(n, dt, px, py, pz, vx, vy, vz);
+    GBH_LAUNCH_CHECK();
+    return cudaSuccess;
+}
+
+cudaError_t block_close(const Launch &L, const TreeBufs &b, int64_t n, int32_t tick, double T, int levels, double eta,
+                        double eps, const double *ax, const double *ay, const double *az, double *vx, double *vy,
+                        double *vz, uint8_t *rung, int32_t *end) {
+    cudaError_t e = cudaMemsetAsync(&b.info->next_tick, 0x7f, sizeof(int32_t), L.stream);
+    if (e != cudaSuccess) return e;
+    k_block_close<<<blocks_for(n, kThreads), kThreads, 0, L.stream>>>(n, tick, 1 << (levels - 1), T, levels, eta, eps,
+                                                                      ax, ay, az, vx, vy, vz, rung, end, b.info);
+    GBH_LAUNCH_CHECK();
+    return cudaSuccess;
 }
 
 }  // namespace gbh

@@ -3,8 +3,7 @@
 // walk_plain: one thread per sorted star, the CUDA twin of the Metal kernel
 //   internal/sim/bh/gpu_darwin.go:76-118 (all FP32, uncompensated, per-star opening).
 // walk_mixed: one warp per group of 64 consecutive Morton-sorted stars (two per lane, packed
-//   FP32x2 arithmetic; a one-star-per-lane kernel is kept behind GBH_MIXED_PAIRS=0) walking the
-//   skip-pointer tree in lockstep. A node is opened when any star of the group would open it under the
+//   FP32x2 arithmetic) walking the skip-pointer tree in lockstep. A node is opened when any star of the group would open it under the
 //   reference criterion d2 < crit2 (bh.go:165), so every star sees each accepted node exactly
 //   where the reference would accept it or deeper. Positions are FP64 split into hi + lo FP32
 //   parts; a separation is formed per star as (hi_a - hi_b) + (lo_a - lo_b), whose hi difference
@@ -22,17 +21,9 @@ namespace {
 constexpr unsigned kFull = 0xffffffffu;
 
 constexpr int kPlainThreads = 256;
-// Mixed-walk block size and the minimum resident blocks per SM asked of the compiler (which
-// caps its registers per thread); compile-time tuning knobs.
+// Mixed-walk block size (a compile-time tuning knob; 64 and 128 measured equal).
 #ifndef GBH_MIXED_THREADS
 #define GBH_MIXED_THREADS 128
-#endif
-#ifndef GBH_MIXED_MINBLOCKS
-#define GBH_MIXED_MINBLOCKS 1
-#endif
-// Stars per lane in the mixed walk: 1 (k_walk_mixed) or 2 (k_walk_mixed2, packed FP32x2).
-#ifndef GBH_MIXED_PAIRS
-#define GBH_MIXED_PAIRS 1
 #endif
 constexpr int kMixedThreads = GBH_MIXED_THREADS;
 
@@ -50,10 +41,12 @@ __device__ __forceinline__ void set_err(DevInfo *info, int where) {
 __global__ __launch_bounds__(kPlainThreads) void k_walk_plain(const DevInfo *info, const PNode *__restrict__ nodes,
                                                               const float4 *__restrict__ stars,
                                                               const int32_t *__restrict__ order, float eps2,
-                                                              double *ax, double *ay, double *az, DevInfo *err_info) {
-    int64_t k = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+                                                              double *ax, double *ay, double *az,
+                                                              const int32_t *__restrict__ targets, DevInfo *err_info) {
+    int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     int64_t ns = info->nstars;
-    if (k >= ns) return;
+    if (t >= (targets ? int64_t(info->ntargets) : ns)) return;
+    int64_t k = targets ? int64_t(targets[t]) : t;
     int64_t nn = info->nnodes;
     float4 p = stars[k];
     float fax = 0.f, fay = 0.f, faz = 0.f;
@@ -116,118 +109,11 @@ __device__ __forceinline__ void kahan_fold(float &s, float &c, float &part) {
     part = 0.f;
 }
 
-// One warp per group of 32 consecutive sorted stars; the warps of a block take consecutive
-// groups, which share most of their nodes in L1.
-template <bool kQuad, bool kSoft>
-__global__ __launch_bounds__(kMixedThreads, GBH_MIXED_MINBLOCKS) void k_walk_mixed(const DevInfo *info,
-                                                                                  const MNode *__restrict__ nodes,
-                                                              const int2 *__restrict__ ranges,
-                                                              const float4 *__restrict__ st_hi,
-                                                              const float4 *__restrict__ st_lo,
-                                                              const int32_t *__restrict__ order, float eps2,
-                                                              double *ax, double *ay, double *az, DevInfo *err_info) {
-    const int lane = threadIdx.x & 31;
-    const int32_t ns = int32_t(info->nstars);  // the C-ABI caps n at 2^30
-    const uint32_t nn = uint32_t(info->nnodes);
-    const int32_t base = int32_t((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32;
-    if (base >= ns) return;  // uniform over the warp
-    const int32_t k = base + lane;
-    const bool valid = k < ns;
-    const int32_t kk = valid ? k : base;
-    const float4 h = st_hi[kk], l = st_lo[kk];
-
-    float sx = 0.f, sy = 0.f, sz = 0.f, cx = 0.f, cy = 0.f, cz = 0.f;  // Kahan sums
-    float px = 0.f, py = 0.f, pz = 0.f;                                // block partials
-    uint32_t visits = 0;
-    int i = nn > 0 ? 0 : -1;
-    // Control flow is uniform over the warp: i, first, next and the vote agree in all lanes.
-    while (i >= 0) {
-        if (uint32_t(i) >= nn) {
-            if (lane == 0) set_err(err_info, 4);
-            break;
-        }
-        const MNode nd = nodes[i];
-        const float dx = (nd.a.x - h.x) + (nd.b.x - l.x);
-        const float dy = (nd.a.y - h.y) + (nd.b.y - l.y);
-        const float dz = (nd.a.z - h.z) + (nd.b.z - l.z);
-        const float d2 = dx * dx + dy * dy + dz * dz;
-        const bool open = __any_sync(kFull, d2 < nd.a.w);
-        const int first = __float_as_int(nd.d.z), next = __float_as_int(nd.d.w);
-        if (!open) {
-            const float ir = rsqrtf(d2 + eps2);
-            const float ir2 = ir * ir;
-            const float ir3 = ir * ir2;
-            if (kQuad) {
-                const float qx = nd.c.x * dx + nd.c.w * dy + nd.d.x * dz;
-                const float qy = nd.c.w * dx + nd.c.y * dy + nd.d.y * dz;
-                const float qz = nd.d.x * dx + nd.d.y * dy + nd.c.z * dz;
-                const float ir5 = ir3 * ir2;
-                const float u = 2.5f * ir2 * (dx * qx + dy * qy + dz * qz);
-                const float f = fmaf(ir5, u, nd.b.w * ir3);
-                px = fmaf(f, dx, px);
-                py = fmaf(f, dy, py);
-                pz = fmaf(f, dz, pz);
-                px = fmaf(-ir5, qx, px);
-                py = fmaf(-ir5, qy, py);
-                pz = fmaf(-ir5, qz, pz);
-            } else {
-                const float f = nd.b.w * ir3;
-                px = fmaf(f, dx, px);
-                py = fmaf(f, dy, py);
-                pz = fmaf(f, dz, pz);
-            }
-            i = next;
-        } else if (first >= 0) {
-            i = first;
-        } else {
-            const int2 r = ranges[i];
-            if (r.x < 0 || r.y > ns || r.x > r.y) {
-                if (lane == 0) set_err(err_info, 5);
-                break;
-            }
-            for (int j = r.x; j < r.y; ++j) {
-                const float4 sh = st_hi[j], sl = st_lo[j];
-                const float ex = (sh.x - h.x) + (sl.x - l.x);
-                const float ey = (sh.y - h.y) + (sl.y - l.y);
-                const float ez = (sh.z - h.z) + (sl.z - l.z);
-                const float r2 = fmaf(ex, ex, fmaf(ey, ey, fmaf(ez, ez, eps2)));
-                // The star itself gives ex = ey = ez = 0 exactly; with eps2 > 0 that adds 0, as
-                // skipping j == self does (bh.go:191-193). Without softening r2 = 0 is masked.
-                const float ir = kSoft ? rsqrtf(r2) : (r2 > 0.f ? rsqrtf(r2) : 0.f);
-                const float f = sh.w * ir * ir * ir;
-                px = fmaf(f, ex, px);
-                py = fmaf(f, ey, py);
-                pz = fmaf(f, ez, pz);
-            }
-            i = next;
-        }
-        if ((++visits & 31u) == 0) {  // fold the block partial every 32 visits
-            kahan_fold(sx, cx, px);
-            kahan_fold(sy, cy, py);
-            kahan_fold(sz, cz, pz);
-            if (visits > nn + 32u) {  // each node is visited at most once
-                if (lane == 0) set_err(err_info, 4);
-                break;
-            }
-        }
-    }
-    kahan_fold(sx, cx, px);
-    kahan_fold(sy, cy, py);
-    kahan_fold(sz, cz, pz);
-    if (valid) {
-        int32_t o = order[k];
-        ax[o] = double(sx) - double(cx);
-        ay[o] = double(sy) - double(cy);
-        az[o] = double(sz) - double(cz);
-    }
-}
-
-// Paired variant of the mixed walk: one warp per group of 64 consecutive sorted stars, each
-// lane owning two neighbouring stars; every separation, test and interaction is computed for
-// both stars at once with packed FP32x2 arithmetic (__fadd2_rn / __fmul2_rn / __ffma2_rn), so
-// the node load, vote and branch of a visit are shared by twice the stars and the math issues
-// half the instructions. Same opening rule (any star of the group opens the node), same
-// double-float separations and Kahan-folded block sums as k_walk_mixed.
+// The mixed walk: one warp per group of 64 consecutive sorted stars (or 64 consecutive entries
+// of a target list), each lane owning two neighbouring stars; every separation, test and
+// interaction is computed for both stars at once with packed FP32x2 arithmetic
+// (__fadd2_rn / __fmul2_rn / __ffma2_rn), so the node load, vote and branch of a visit are shared
+// by 64 stars and the math issues half the instructions of one star per lane (measured 1.3x).
 __device__ __forceinline__ float2 f2(float v) { return make_float2(v, v); }
 __device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
 __device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
@@ -244,16 +130,21 @@ __global__ __launch_bounds__(kMixedThreads) void k_walk_mixed2(const DevInfo *in
                                                                const float4 *__restrict__ st_hi,
                                                                const float4 *__restrict__ st_lo,
                                                                const int32_t *__restrict__ order, float eps2,
-                                                               double *ax, double *ay, double *az, DevInfo *err_info) {
+                                                               double *ax, double *ay, double *az,
+                                                               const int32_t *__restrict__ targets, DevInfo *err_info) {
     const int lane = threadIdx.x & 31;
     const int32_t ns = int32_t(info->nstars);  // the C-ABI caps n at 2^30
+    const int32_t nt = targets ? int32_t(info->ntargets) : ns;
     const uint32_t nn = uint32_t(info->nnodes);
     const int32_t base = int32_t((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 64;
-    if (base >= ns) return;  // uniform over the warp
-    const int32_t k0 = base + 2 * lane, k1 = k0 + 1;
-    const bool v0 = k0 < ns, v1 = k1 < ns;
-    const float4 h0 = st_hi[v0 ? k0 : base], l0 = st_lo[v0 ? k0 : base];
-    const float4 h1 = st_hi[v1 ? k1 : base], l1 = st_lo[v1 ? k1 : base];
+    if (base >= nt) return;  // uniform over the warp
+    const int32_t t0 = base + 2 * lane, t1 = t0 + 1;
+    const bool v0 = t0 < nt, v1 = t1 < nt;
+    const int32_t first_k = targets ? targets[base] : base;
+    const int32_t k0 = v0 ? (targets ? targets[t0] : t0) : first_k;
+    const int32_t k1 = v1 ? (targets ? targets[t1] : t1) : first_k;
+    const float4 h0 = st_hi[k0], l0 = st_lo[k0];
+    const float4 h1 = st_hi[k1], l1 = st_lo[k1];
     // negated target coordinates, so separations are sums
     const float2 nhx = make_float2(-h0.x, -h1.x), nhy = make_float2(-h0.y, -h1.y), nhz = make_float2(-h0.z, -h1.z);
     const float2 nlx = make_float2(-l0.x, -l1.x), nly = make_float2(-l0.y, -l1.y), nlz = make_float2(-l0.z, -l1.z);
@@ -380,36 +271,32 @@ __global__ __launch_bounds__(256) void k_fma_probe(int iters, float *out) {
 }  // namespace
 
 cudaError_t walk_plain(const Launch &L, const TreeBufs &b, int64_t nstars_cap, float eps2, double *ax, double *ay,
-                       double *az) {
+                       double *az, bool targets) {
     k_walk_plain<<<blocks_for(nstars_cap, kPlainThreads), kPlainThreads, 0, L.stream>>>(
-        b.info, b.pnodes, b.st_hi, b.order, eps2, ax, ay, az, b.info);
+        b.info, b.pnodes, b.st_hi, b.order, eps2, ax, ay, az, targets ? b.targets : nullptr, b.info);
     ++*L.count;
     return cudaGetLastError();
 }
 
 template <bool kQuad, bool kSoft>
 static cudaError_t launch_mixed(const Launch &L, const TreeBufs &b, int64_t nstars_cap, float eps2, double *ax,
-                                double *ay, double *az) {
-    const int per_warp = GBH_MIXED_PAIRS ? 64 : 32;
-    int64_t groups = (nstars_cap + per_warp - 1) / per_warp;
+                                double *ay, double *az, bool targets) {
+    int64_t groups = (nstars_cap + 63) / 64;
     int64_t blocks = (groups + kMixedThreads / 32 - 1) / (kMixedThreads / 32);
-    if (GBH_MIXED_PAIRS)
-        k_walk_mixed2<kQuad, kSoft><<<unsigned(blocks < 1 ? 1 : blocks), kMixedThreads, 0, L.stream>>>(
-            b.info, b.mnodes, b.mrange, b.st_hi, b.st_lo, b.order, eps2, ax, ay, az, b.info);
-    else
-        k_walk_mixed<kQuad, kSoft><<<unsigned(blocks < 1 ? 1 : blocks), kMixedThreads, 0, L.stream>>>(
-            b.info, b.mnodes, b.mrange, b.st_hi, b.st_lo, b.order, eps2, ax, ay, az, b.info);
+    k_walk_mixed2<kQuad, kSoft><<<unsigned(blocks < 1 ? 1 : blocks), kMixedThreads, 0, L.stream>>>(
+        b.info, b.mnodes, b.mrange, b.st_hi, b.st_lo, b.order, eps2, ax, ay, az, targets ? b.targets : nullptr,
+        b.info);
     ++*L.count;
     return cudaGetLastError();
 }
 
 cudaError_t walk_mixed(const Launch &L, const TreeBufs &b, int64_t nstars_cap, float eps2, int quad, double *ax,
-                       double *ay, double *az) {
+                       double *ay, double *az, bool targets) {
     bool soft = eps2 > 0.f;
-    if (quad && soft) return launch_mixed<true, true>(L, b, nstars_cap, eps2, ax, ay, az);
-    if (quad) return launch_mixed<true, false>(L, b, nstars_cap, eps2, ax, ay, az);
-    if (soft) return launch_mixed<false, true>(L, b, nstars_cap, eps2, ax, ay, az);
-    return launch_mixed<false, false>(L, b, nstars_cap, eps2, ax, ay, az);
+    if (quad && soft) return launch_mixed<true, true>(L, b, nstars_cap, eps2, ax, ay, az, targets);
+    if (quad) return launch_mixed<true, false>(L, b, nstars_cap, eps2, ax, ay, az, targets);
+    if (soft) return launch_mixed<false, true>(L, b, nstars_cap, eps2, ax, ay, az, targets);
+    return launch_mixed<false, false>(L, b, nstars_cap, eps2, ax, ay, az, targets);
 }
 
 cudaError_t fp32_fma_probe(const Launch &L, int blocks, int iters, float *out) {

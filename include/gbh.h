@@ -175,8 +175,44 @@ int gbh_state_download(gbh_ctx *ctx, double *px, double *py, double *pz, double 
                        double *vz, double *ax, double *ay, double *az);
 /* nsteps KDK steps on the resident state (as gbh_step_kdk, no copies). */
 int gbh_state_step(gbh_ctx *ctx, const gbh_params *p, double dt, int64_t nsteps);
+/* Statistics of block steps. */
+typedef struct {
+    int64_t substeps;          /* events: tree builds and walks of the active stars */
+    int64_t evaluations;       /* stars walked, summed over the events */
+    int32_t min_substep_ticks; /* shortest interval between events, in ticks of dt / 2^(levels-1) */
+    int32_t reserved;
+} gbh_blockstats;
+
+/*
+ * nsteps global steps of length dt with power-of-two block time steps on the resident state.
+ * The reference steps gravity with one global dt; this follows its gas block steps
+ * (internal/sim/blockstep.go:22-90): a body's rung is the smallest r with dt / 2^r <= dt_i
+ * (rungFor, blockstep.go:38-45), capped at levels - 1, with dt_i = eta * sqrt(softening / |a_i|),
+ * and a step may start only at a multiple of its length (blockstep.go:84-86). Kick-drift-kick
+ * per body: opening half kick when its step starts, all bodies drift together from event to
+ * event, the tree of all stars is rebuilt at each event and only the bodies whose step ends
+ * are walked, kicked and given a new rung. levels = 1 is exactly gbh_state_step. stats may be
+ * NULL.
+ */
+int gbh_state_step_block(gbh_ctx *ctx, const gbh_params *p, double dt, double eta, int32_t levels,
+                         int64_t nsteps, gbh_blockstats *stats);
 /* Accelerations of the resident state (as gbh_accelerations, no copies). */
 int gbh_state_accelerations(gbh_ctx *ctx, const gbh_params *p);
+
+/* Conserved quantities of the resident state (internal/sim/diag.go:31-120), FP64 on the
+   GPU. */
+typedef struct {
+    double kinetic;             /* sourceKinetic: sum of m u^2 / (gamma + 1) over bodies that gravitate (diag.go:80-88) */
+    double potential;           /* tree potential at min(theta, 0.9) (potential.go:12-42) */
+    double total;               /* kinetic + potential (TotalEnergy without gas, diag.go:43-51) */
+    double momentum[3];         /* Momentum, all bodies (diag.go:89-96) */
+    double angular_momentum[3]; /* AngularMomentum about the origin (diag.go:98-105) */
+    double center_of_mass[3];   /* CenterOfMass (diag.go:107-120) */
+    double mass;                /* its total mass */
+} gbh_diagnostics;
+
+/* Diagnostics of the resident state; c is the speed of light of the pair model (0: Newtonian). */
+int gbh_state_diagnostics(gbh_ctx *ctx, const gbh_params *p, double c, gbh_diagnostics *out);
 
 /* ---- Inspection of the last tree (b.nodes / b.order / b.keys in bh.Solver). ---- */
 

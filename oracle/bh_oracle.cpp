@@ -870,6 +870,99 @@ void orc_kdk(int64_t n, double *px, double *py, double *pz, double *vx, double *
     }
 }
 
+void orc_block_kdk(int64_t n, double *px, double *py, double *pz, double *vx, double *vy, double *vz, double *ax,
+                   double *ay, double *az, const double *mass, const uint8_t *kind, const uint8_t *alive, double T,
+                   double eta, int levels, double eps, double theta, int leaf_size, int monopole_only, int dm_off,
+                   int acc_valid, int64_t nsteps, int workers, int64_t *substeps, int64_t *evals) {
+    orc_tree t;
+    t.theta = theta == 0 ? 0.9 : theta;
+    t.leaf = leaf_size > 0 ? leaf_size : 24;
+    t.workers = workers;
+    double eps2 = eps * eps;
+    bool quad = !monopole_only;
+    if (!acc_valid) {
+        t.build(n, px, py, pz, mass, kind, alive, dm_off);
+        orc_tree_accelerations(&t, n, eps, monopole_only, workers, ax, ay, az);
+    }
+    const int32_t ticks = 1 << (levels - 1);
+    auto rung_for = [&](double dt) {  // blockstep.go:38-45
+        int r = 0;
+        double x = T;
+        while (x > dt && r < levels - 1) {
+            x *= 0.5;
+            ++r;
+        }
+        return r;
+    };
+    auto body_dt = [&](int64_t i) {
+        double a = std::sqrt(ax[i] * ax[i] + ay[i] * ay[i] + az[i] * az[i]);
+        return a > 0 ? eta * std::sqrt(eps / a) : std::numeric_limits<double>::infinity();
+    };
+    std::vector<int> rung(n);
+    std::vector<int32_t> end(n);
+    int64_t ns = 0, ne = 0;
+    for (int64_t s = 0; s < nsteps; ++s) {
+        int32_t next = std::numeric_limits<int32_t>::max();
+        for (int64_t i = 0; i < n; ++i) {  // tick 0: every body opens a step
+            int r = rung_for(body_dt(i));
+            rung[i] = r;
+            end[i] = ticks >> r;
+            double h = 0.5 * (T / double(1 << r));
+            vx[i] += h * ax[i];
+            vy[i] += h * ay[i];
+            vz[i] += h * az[i];
+            next = std::min(next, end[i]);
+        }
+        int32_t tk = 0;
+        while (tk < ticks) {
+            int32_t tn = next;
+            double d = double(tn - tk) * (T / double(ticks));
+            for (int64_t i = 0; i < n; ++i) {
+                px[i] += d * vx[i];
+                py[i] += d * vy[i];
+                pz[i] += d * vz[i];
+            }
+            tk = tn;
+            t.build(n, px, py, pz, mass, kind, alive, dm_off);
+            for (int32_t h : t.holes) ax[h] = ay[h] = az[h] = 0;
+            std::vector<int64_t> act;
+            for (int64_t k = 0; k < int64_t(t.order.size()); ++k)
+                if (end[t.order[k]] == tk) act.push_back(k);
+            parallel_for(int64_t(act.size()), kGrain, workers, [&](int64_t lo, int64_t hi) {
+                for (int64_t q = lo; q < hi; ++q) {
+                    int64_t k = act[q];
+                    int32_t i = t.order[k];
+                    t.walk<false>(t.sx[k], t.sy[k], t.sz[k], int32_t(k), eps2, quad, ax[i], ay[i], az[i], nullptr);
+                }
+            });
+            ++ns;
+            ne += int64_t(act.size());
+            next = std::numeric_limits<int32_t>::max();
+            for (int64_t i = 0; i < n; ++i) {
+                if (end[i] == tk) {
+                    double h = 0.5 * (T / double(1 << rung[i]));
+                    vx[i] += h * ax[i];
+                    vy[i] += h * ay[i];
+                    vz[i] += h * az[i];
+                    if (tk < ticks) {
+                        int r = rung_for(body_dt(i));
+                        while (tk % (ticks >> r) != 0) ++r;
+                        rung[i] = r;
+                        end[i] = tk + (ticks >> r);
+                        double h2 = 0.5 * (T / double(1 << r));
+                        vx[i] += h2 * ax[i];
+                        vy[i] += h2 * ay[i];
+                        vz[i] += h2 * az[i];
+                    }
+                }
+                next = std::min(next, end[i]);
+            }
+        }
+    }
+    if (substeps) *substeps = ns;
+    if (evals) *evals = ne;
+}
+
 double orc_potential_exact(int64_t n, const double *px, const double *py, const double *pz,
                            const double *mass, const uint8_t *kind, double eps, double c, int dm_off,
                            int workers) {

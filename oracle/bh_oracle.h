@@ -123,6 +123,20 @@ void orc_kdk(int64_t n, double *px, double *py, double *pz, double *vx, double *
              int leaf_size, int monopole_only, int dark_matter_off, int acc_valid,
              int64_t nsteps, int workers);
 
+/*
+ * Block time steps for gravity, on the scheme of the reference's gas block steps
+ * (internal/sim/blockstep.go:22-90; gravity itself has no block steps in the reference):
+ * rung r = smallest with dt/2^r <= eta*sqrt(eps/|a|) (rungFor, blockstep.go:38-45), capped at
+ * levels-1, steps start at multiples of their length (blockstep.go:84-86), per-body KDK, all
+ * bodies drift from event to event, tree rebuilt at each event, only bodies whose step ends
+ * are walked and kicked. Counts of events and walked stars go to *substeps / *evals.
+ */
+void orc_block_kdk(int64_t n, double *px, double *py, double *pz, double *vx, double *vy,
+                   double *vz, double *ax, double *ay, double *az, const double *mass,
+                   const uint8_t *kind, const uint8_t *alive, double dt, double eta, int levels,
+                   double eps, double theta, int leaf_size, int monopole_only, int dark_matter_off,
+                   int acc_valid, int64_t nsteps, int workers, int64_t *substeps, int64_t *evals);
+
 /* diag.go:44-64 exact pair potential (no holes: plain softened Newtonian). */
 double orc_potential_exact(int64_t n, const double *px, const double *py, const double *pz,
                            const double *mass, const uint8_t *kind, double eps, double c,

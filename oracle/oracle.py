@@ -66,6 +66,8 @@ def lib():
             "orc_direct_targets": (None, [_I64, _P, _P, _P, _P, _P, _D, _INT, _P, _I64, _INT, _P, _P, _P]),
             "orc_kdk": (None, [_I64] + [_P] * 12 + [_D, _D, _D, _INT, _INT, _INT, _INT, _I64, _INT]),
             "orc_potential_exact": (_D, [_I64, _P, _P, _P, _P, _P, _D, _D, _INT, _INT]),
+            "orc_block_kdk": (None, [_I64] + [_P] * 12 + [_D, _D, _INT, _D, _D, _INT, _INT, _INT, _INT, _I64, _INT,
+                                                         _P, _P]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -217,3 +219,18 @@ def kdk(state: dict, dt, eps, theta, leaf, nsteps, monopole_only=False, dm_off=F
                   _ptr(kind), _ptr(alive), dt, eps, theta, leaf, int(monopole_only), int(dm_off),
                   int(acc_valid), nsteps, workers)
     return s
+
+
+def block_kdk(state: dict, dt, eta, levels, eps, theta, leaf, nsteps, monopole_only=False, dm_off=False,
+              acc_valid=False, workers=0):
+    """Block-step KDK (the scheme of gbh_state_step_block) on a dict of SoA arrays, in place;
+    returns (events, walked stars)."""
+    s = state
+    n = len(s["px"])
+    kind = _u8(s.get("kind", np.zeros(n, np.uint8)))
+    alive = _u8(s.get("alive", np.ones(n, np.uint8)))
+    a, b = np.zeros(1, np.int64), np.zeros(1, np.int64)
+    lib().orc_block_kdk(n, *[_ptr(s[k]) for k in ("px", "py", "pz", "vx", "vy", "vz", "ax", "ay", "az", "mass")],
+                        _ptr(kind), _ptr(alive), dt, eta, levels, eps, theta, leaf, int(monopole_only), int(dm_off),
+                        int(acc_valid), nsteps, workers, _ptr(a), _ptr(b))
+    return int(a[0]), int(b[0])

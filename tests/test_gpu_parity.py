@@ -294,6 +294,91 @@ def test_graph_replay_matches_plain_launches(ctx, walk):
         assert np.array_equal(out[0][k], out[1][k]), k
 
 
+def test_diagnostics_match_oracle_and_sums(ctx):  # diag.go:31-120, potential.go:12-42
+    g = np.load(os.path.join(GOLDEN, "disk.npz"))
+    s = {k: g[k].copy() for k in ("px", "py", "pz", "vx", "vy", "vz", "mass", "kind", "alive")}
+    n = len(s["px"])
+    ctx.call("gbh_state_upload", n, *[P(s[k]) for k in ("px", "py", "pz", "vx", "vy", "vz")], None, None, None,
+             P(s["mass"]), P(s["kind"]), P(s["alive"]))
+    par = abi.make_params(float(g["theta"]), float(g["eps"]), int(g["leaf"]), False, False, "fp64")
+    d = ctx.diagnostics(par, c=float(g["c"]))
+    m, v = s["mass"], np.stack([s["vx"], s["vy"], s["vz"]], 1)
+    x = np.stack([s["px"], s["py"], s["pz"]], 1)
+    c = float(g["c"])
+    u2 = (v * v).sum(1)
+    kin = (m * u2 / (np.sqrt(1 + u2 / c ** 2) + 1)).sum()
+    assert abs(d["kinetic"] - kin) <= 1e-12 * abs(kin)
+    assert abs((d["potential"] - float(g["potential"])) / float(g["potential"])) <= 1e-12
+    assert abs(d["total"] - (d["kinetic"] + d["potential"])) <= 1e-15 * abs(d["total"]) + 1e-300
+    assert np.allclose(d["momentum"], (m[:, None] * v).sum(0), rtol=1e-12, atol=1e-14)
+    assert np.allclose(d["angular_momentum"], (m[:, None] * np.cross(x, v)).sum(0), rtol=1e-12, atol=1e-14)
+    assert np.allclose(d["center_of_mass"], (m[:, None] * x).sum(0) / m.sum(), rtol=1e-12, atol=1e-14)
+    assert abs(d["mass"] - m.sum()) <= 1e-12 * m.sum()
+
+
+BLOCK_FIELDS = ("px", "py", "pz", "vx", "vy", "vz", "ax", "ay", "az")
+
+
+def upload_state(ctx, s):
+    ctx.call("gbh_state_upload", len(s["px"]), *[P(s[k]) for k in ("px", "py", "pz", "vx", "vy", "vz")], None, None,
+             None, P(s["mass"]), None, None)
+
+
+def download_state(ctx, n):
+    st = {k: np.zeros(n) for k in BLOCK_FIELDS}
+    ctx.call("gbh_state_download", *[P(st[k]) for k in BLOCK_FIELDS])
+    return st
+
+
+@pytest.mark.parametrize("walk", ["fp64", "mixed"])
+def test_block_steps_one_level_is_global_step(ctx, walk):
+    s = ics.plummer(20000, seed=12)
+    n = len(s["px"])
+    par = abi.make_params(0.5, 0.01, 8, False, False, walk)
+    upload_state(ctx, s)
+    ctx.call("gbh_state_step", par, 1e-2, 3)
+    want = download_state(ctx, n)
+    upload_state(ctx, s)
+    st = ctx.step_block(par, 1e-2, 0.025, 1, 3)
+    got = download_state(ctx, n)
+    assert st["substeps"] == 3 and st["evaluations"] == 3 * n
+    for k in BLOCK_FIELDS:
+        assert np.array_equal(want[k], got[k]), k
+
+
+def test_block_steps_fp64_bit_exact_with_oracle(ctx):
+    s = ics.plummer(4096, seed=13)
+    n = len(s["px"])
+    par = abi.make_params(0.5, 0.01, 8, False, False, "fp64")
+    upload_state(ctx, s)
+    st = ctx.step_block(par, 2e-2, 0.025, 6, 2)
+    got = download_state(ctx, n)
+    ref = {k: s[k].copy() for k in (*BLOCK_FIELDS, "mass")}
+    events, walked = O.block_kdk(ref, dt=2e-2, eta=0.025, levels=6, eps=0.01, theta=0.5, leaf=8, nsteps=2, workers=1)
+    assert (st["substeps"], st["evaluations"]) == (events, walked)
+    for k in BLOCK_FIELDS:
+        assert np.array_equal(got[k], ref[k]), k
+
+
+def test_block_steps_conserve_energy_at_fewer_evaluations(ctx):
+    """Plummer sphere, mixed walk: block steps with 6 levels conserve energy about as well as
+    global steps at the finest step, while walking far fewer stars."""
+    s = ics.plummer(16384, seed=0)
+    n = len(s["px"])
+    par = abi.make_params(0.5, 0.01, 8, False, False, "mixed")
+    T = 1.6e-2
+    upload_state(ctx, s)
+    e0 = ctx.diagnostics(par)["total"]
+    st = ctx.step_block(par, T, 0.025, 6, 10)
+    e_block = ctx.diagnostics(par)["total"]
+    upload_state(ctx, s)
+    ctx.call("gbh_state_step", par, T / 32, 320)
+    e_fine = ctx.diagnostics(par)["total"]
+    d_block, d_fine = abs((e_block - e0) / e0), abs((e_fine - e0) / e0)
+    assert st["evaluations"] < 0.5 * 320 * n
+    assert d_block <= max(5 * d_fine, 2e-5)
+
+
 def test_step_rejects_holes(ctx):
     s = ics.test_disk(500)
     n = len(s["px"])

@@ -235,3 +235,24 @@ def test_node_table_invariants():
             assert lo == nd["hi"]
         else:
             assert nd["hi"] - nd["lo"] <= int(g["leaf"])
+
+
+def test_block_steps_one_level_is_global_kdk():
+    s = ics.plummer(1024, seed=5)
+    g = {k: s[k].copy() for k in ("px", "py", "pz", "vx", "vy", "vz", "ax", "ay", "az", "mass")}
+    b = {k: s[k].copy() for k in g}
+    O.kdk(g, dt=1e-2, eps=0.01, theta=0.5, leaf=8, nsteps=3, workers=1)
+    events, walked = O.block_kdk(b, dt=1e-2, eta=0.025, levels=1, eps=0.01, theta=0.5, leaf=8, nsteps=3, workers=1)
+    assert (events, walked) == (3, 3 * 1024)
+    for k in g:
+        assert np.array_equal(g[k], b[k]), k
+
+
+def test_block_steps_rungs_follow_accelerations():
+    """Denser regions take shorter steps: with 6 levels the walked stars per global step lie
+    between one (all on rung 0) and 32 (all on the finest rung) per star."""
+    s = ics.plummer(2048, seed=6)
+    b = {k: s[k].copy() for k in ("px", "py", "pz", "vx", "vy", "vz", "ax", "ay", "az", "mass")}
+    events, walked = O.block_kdk(b, dt=2e-2, eta=0.025, levels=6, eps=0.01, theta=0.5, leaf=8, nsteps=2, workers=1)
+    assert 2 < events <= 2 * 32
+    assert 2 * 2048 < walked < 2 * 32 * 2048
