@@ -99,6 +99,8 @@ SIGNATURES = {
     "gbh_probe_fp32_peak": (ctypes.c_int, [_P, _D, _P]),
     "gbh_state_diagnostics": (ctypes.c_int, [_P, _PP, _D, _P]),
     "gbh_state_step_block": (ctypes.c_int, [_P, _PP, _D, _D, _I32, _I64, _P]),
+    "gbh_forest_upload": (ctypes.c_int, [_P, _I32, _P] + [_P] * 12),
+    "gbh_forest_layout": (ctypes.c_int, [_P, _I32, _P, _P]),
     "gbh_morton_order_noalloc": (ctypes.c_int, [_I32, _P, _I64] + [_P] * 8 + [ctypes.c_char_p, ctypes.c_int]),
 }
 
@@ -215,6 +217,18 @@ class Context:
         nodes = np.zeros(nn, NODE_DTYPE)
         self.call("gbh_tree_export", ptr(keys), ptr(order), ptr(nodes), nn)
         return dict(keys=keys, order=order, nodes=nodes)
+
+    def forest_upload(self, offsets, px, py, pz, vx, vy, vz, mass, kind=None, alive=None, acc=None):
+        off = np.ascontiguousarray(offsets, np.int64)
+        ax, ay, az = (None, None, None) if acc is None else acc
+        self.call("gbh_forest_upload", len(off) - 1, ptr(off), ptr(px), ptr(py), ptr(pz), ptr(vx), ptr(vy), ptr(vz),
+                  ptr(ax), ptr(ay), ptr(az), ptr(mass), ptr(kind), ptr(alive))
+
+    def forest_layout(self, nsys: int):
+        stars = np.zeros(2 * nsys, np.int64)
+        nodes = np.zeros(2 * nsys, np.int64)
+        self.call("gbh_forest_layout", nsys, ptr(stars), ptr(nodes))
+        return stars.reshape(nsys, 2), nodes.reshape(nsys, 2)
 
     def step_block(self, params: Params, dt: float, eta: float, levels: int, nsteps: int) -> dict:
         st = BlockStats()

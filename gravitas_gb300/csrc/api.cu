@@ -23,7 +23,7 @@ struct StepGraph {
     cudaGraphNode_t stage_nodes[3] = {};  // event-record nodes: build start, walk start, walk end
     int64_t launches = 0;                 // kernels in one replay
     // validity key
-    int64_t n = -1, tree_gen = -1, state_gen = -1;
+    int64_t n = -1, tree_gen = -1, state_gen = -1, sys_gen = -1;
     gbh_params p = {};
     double dt = 0;
     const void *kind = nullptr, *alive = nullptr;
@@ -38,6 +38,13 @@ struct gbh_ctx {
     // resident state (state order)
     int64_t cap = 0, n = 0;
     int64_t state_gen = 0;  // incremented whenever the state buffers are reallocated
+    // forest: systems of the resident state (nsys == 1: a plain state)
+    int32_t nsys = 1;
+    int64_t sys_gen = 0;      // incremented whenever the systems change
+    uint16_t *sys_of = nullptr;
+    int64_t sys_of_cap = 0;
+    int64_t *sys_off = nullptr;
+    int64_t sys_off_cap = 0;
     bool have_state = false, acc_valid = false;
     int32_t state_holes = 0;
     bool state_has_kind = false, state_has_alive = false;
@@ -195,15 +202,18 @@ int d2h(gbh_ctx *ctx, void *dst, const void *src, size_t bytes) {
 }
 
 // Tree build + walk on device arrays; accelerations of alive non-hole bodies, holes zeroed.
+// forest: the resident state's systems (each its own tree) instead of one system.
 int forces(gbh_ctx *ctx, const gbh_params *p, int64_t n, const double *px, const double *py, const double *pz,
            const double *mass, const uint8_t *kind, const uint8_t *alive, double *ax, double *ay, double *az,
-           double theta) {
+           double theta, bool forest = false) {
     Launch L = launch_of(ctx);
     int leaf = leaf_of(p);
-    CK(gbh::tree_alloc(ctx->tb, n, leaf));
+    forest = forest && ctx->nsys > 1;
+    CK(gbh::tree_alloc(ctx->tb, n, leaf, forest ? ctx->nsys : 1));
     CK(stage_event(ctx));
     CK(gbh::tree_build(L, ctx->tb, n, px, py, pz, mass, kind, alive, ax, ay, az, theta, leaf, p->dark_matter_off,
-                       p->walk == GBH_WALK_FP64, p->walk == GBH_WALK_PLAIN));
+                       p->walk == GBH_WALK_FP64, p->walk == GBH_WALK_PLAIN, forest ? ctx->sys_of : nullptr,
+                       forest ? ctx->sys_off : nullptr));
     CK(stage_event(ctx));
     double eps2 = p->softening * p->softening;
     int quad = !p->monopole_only;
@@ -285,7 +295,7 @@ int capture_step(gbh_ctx *ctx, const gbh_params *p, double dt, const uint8_t *ki
                                     ctx->az);
     if (e == cudaSuccess)
         rc = forces(ctx, p, n, ctx->px, ctx->py, ctx->pz, ctx->mass, kind, alive, ctx->ax, ctx->ay, ctx->az,
-                    theta_of(p));
+                    theta_of(p), true);
     if (e == cudaSuccess && rc == GBH_OK) e = gbh::kick(L, n, h, ctx->vx, ctx->vy, ctx->vz, ctx->ax, ctx->ay, ctx->az);
     cudaGraph_t graph = nullptr;
     cudaError_t e2 = cudaStreamEndCapture(ctx->stream, &graph);
@@ -321,6 +331,7 @@ int capture_step(gbh_ctx *ctx, const gbh_params *p, double dt, const uint8_t *ki
     g.dt = dt;
     g.tree_gen = ctx->tb.generation;
     g.state_gen = ctx->state_gen;
+    g.sys_gen = ctx->sys_gen;
     g.kind = kind;
     g.alive = alive;
     return GBH_OK;
@@ -334,16 +345,17 @@ int run_steps(gbh_ctx *ctx, const gbh_params *p, double dt, int64_t nsteps) {
     const uint8_t *alive = ctx->state_has_alive ? ctx->alive : nullptr;
     double theta = theta_of(p);
     if (!ctx->acc_valid) {  // initForces (gas.go:14-17)
-        int rc = forces(ctx, p, n, ctx->px, ctx->py, ctx->pz, ctx->mass, kind, alive, ctx->ax, ctx->ay, ctx->az, theta);
+        int rc = forces(ctx, p, n, ctx->px, ctx->py, ctx->pz, ctx->mass, kind, alive, ctx->ax, ctx->ay, ctx->az, theta,
+                        true);
         if (rc) return rc;
         ctx->acc_valid = true;
     }
     if (ctx->use_graphs && nsteps > 0) {
         // One captured step per replay: the ~50 kernels of a step launch as one graph.
-        CK(gbh::tree_alloc(ctx->tb, n, leaf_of(p)));  // any growth happens outside the capture
+        CK(gbh::tree_alloc(ctx->tb, n, leaf_of(p), ctx->nsys));  // any growth happens outside the capture
         StepGraph &g = ctx->step_graph;
         if (!(g.exec && g.n == n && same_params(g.p, *p) && g.dt == dt && g.tree_gen == ctx->tb.generation &&
-              g.state_gen == ctx->state_gen && g.kind == kind && g.alive == alive)) {
+              g.state_gen == ctx->state_gen && g.sys_gen == ctx->sys_gen && g.kind == kind && g.alive == alive)) {
             int rc = capture_step(ctx, p, dt, kind, alive);
             if (rc) return rc;
         }
@@ -362,7 +374,8 @@ int run_steps(gbh_ctx *ctx, const gbh_params *p, double dt, int64_t nsteps) {
     for (int64_t s = 0; s < nsteps; ++s) {
         CK(gbh::kick_drift(L, n, h, dt, ctx->px, ctx->py, ctx->pz, ctx->vx, ctx->vy, ctx->vz, ctx->ax, ctx->ay,
                            ctx->az));
-        int rc = forces(ctx, p, n, ctx->px, ctx->py, ctx->pz, ctx->mass, kind, alive, ctx->ax, ctx->ay, ctx->az, theta);
+        int rc = forces(ctx, p, n, ctx->px, ctx->py, ctx->pz, ctx->mass, kind, alive, ctx->ax, ctx->ay, ctx->az, theta,
+                        true);
         if (rc) return rc;
         CK(gbh::kick(L, n, h, ctx->vx, ctx->vy, ctx->vz, ctx->ax, ctx->ay, ctx->az));
     }
@@ -483,6 +496,10 @@ int upload_state(gbh_ctx *ctx, int64_t n, const double *px, const double *py, co
     ctx->have_state = true;
     ctx->acc_valid = acc;
     ctx->state_holes = count_holes(kind, alive, n);
+    if (ctx->nsys != 1) {
+        ctx->nsys = 1;
+        ++ctx->sys_gen;
+    }
     return GBH_OK;
 }
 
@@ -547,7 +564,8 @@ void gbh_destroy(gbh_ctx *c) {
     free_graph(c->step_graph);
     gbh::tree_free(c->tb);
     free_state(c);
-    void *ptrs[] = {c->part, c->scalar, c->holes, c->targets, c->tout, c->probe, c->scratch3, c->rung, c->end_tick};
+    void *ptrs[] = {c->part,  c->scalar,   c->holes, c->targets,  c->tout,   c->probe,
+                    c->scratch3, c->rung, c->end_tick, c->sys_of, c->sys_off};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     for (auto &ev : c->ev)
@@ -625,7 +643,7 @@ int gbh_potential_energy(gbh_ctx *ctx, const gbh_params *p, int64_t n, const dou
     Launch L = launch_of(ctx);
     int leaf = leaf_of(p);
     double theta = std::min(theta_of(p), 0.9);  // diagTheta, potential.go:12-14
-    CK(gbh::tree_alloc(ctx->tb, n, leaf));
+    CK(gbh::tree_alloc(ctx->tb, n, leaf, 1));
     CK(gbh::tree_build(L, ctx->tb, n, ctx->px, ctx->py, ctx->pz, ctx->mass, kind ? ctx->kind : nullptr,
                        alive ? ctx->alive : nullptr, ctx->ax, ctx->ay, ctx->az, theta, leaf, p->dark_matter_off, true));
     int64_t nparts = (ctx->tb.cap_n + 255) / 256;
@@ -739,6 +757,7 @@ int gbh_state_step_block(gbh_ctx *ctx, const gbh_params *p, double dt, double et
     if (ctx->state_holes)
         return fail(ctx, GBH_ERR_UNSUPPORTED,
                     "alive black holes need the hole-aware split step (sim.stepSplit), which this path does not cover");
+    if (ctx->nsys > 1) return fail(ctx, GBH_ERR_UNSUPPORTED, "block steps of a forest are not supported");
     if (stats) *stats = gbh_blockstats{};
     CK(cudaEventRecord(ctx->ev[0], ctx->stream));
     if (ctx->n > 0 && (rc = run_block_steps(ctx, p, dt, eta, levels, nsteps, stats))) return rc;
@@ -752,7 +771,7 @@ int gbh_state_accelerations(gbh_ctx *ctx, const gbh_params *p) {
     if (ctx->n == 0) return GBH_OK;
     CK(cudaEventRecord(ctx->ev[0], ctx->stream));
     rc = forces(ctx, p, ctx->n, ctx->px, ctx->py, ctx->pz, ctx->mass, ctx->state_has_kind ? ctx->kind : nullptr,
-                ctx->state_has_alive ? ctx->alive : nullptr, ctx->ax, ctx->ay, ctx->az, theta_of(p));
+                ctx->state_has_alive ? ctx->alive : nullptr, ctx->ax, ctx->ay, ctx->az, theta_of(p), true);
     if (rc) return rc;
     ctx->acc_valid = true;
     return finish(ctx, true);
@@ -788,11 +807,13 @@ int gbh_state_diagnostics(gbh_ctx *ctx, const gbh_params *p, double c, gbh_diagn
     int leaf = leaf_of(p);
     double theta = std::min(theta_of(p), 0.9);
     // the build zeroes alive holes' accelerations: use the force scratch of the potential path
-    CK(gbh::tree_alloc(ctx->tb, n, leaf));
+    const bool forest = ctx->nsys > 1;
+    CK(gbh::tree_alloc(ctx->tb, n, leaf, ctx->nsys));
     CK(grow(ctx->scratch3, ctx->scratch3_cap, 3 * n));
     double *sa = ctx->scratch3;
     CK(gbh::tree_build(L, ctx->tb, n, ctx->px, ctx->py, ctx->pz, ctx->mass, kind, alive, sa, sa + n, sa + 2 * n, theta,
-                       leaf, p->dark_matter_off, true));
+                       leaf, p->dark_matter_off, true, true, forest ? ctx->sys_of : nullptr,
+                       forest ? ctx->sys_off : nullptr));
     CK(gbh::potential_fp64(L, ctx->tb, n, ctx->px, ctx->py, ctx->pz, ctx->mass, kind, alive, ctx->holes,
                            int32_t(holes.size()), p->softening * p->softening, c, p->dark_matter_off,
                            !p->monopole_only, ctx->part, ctx->scalar));
@@ -814,6 +835,65 @@ int gbh_state_diagnostics(gbh_ctx *ctx, const gbh_params *p, double c, gbh_diagn
         out->center_of_mass[k] = sums[10] != 0 ? sums[7 + k] / sums[10] : 0.0;
     }
     out->mass = sums[10];
+    return GBH_OK;
+}
+
+int gbh_forest_upload(gbh_ctx *ctx, int32_t nsys, const int64_t *offsets, const double *px, const double *py,
+                      const double *pz, const double *vx, const double *vy, const double *vz, const double *ax,
+                      const double *ay, const double *az, const double *mass, const uint8_t *kind,
+                      const uint8_t *alive) {
+    int rc = begin(ctx);
+    if (rc) return rc;
+    if (nsys < 1 || nsys > 65535) return fail(ctx, GBH_ERR_ARG, "nsys %d outside [1, 65535]", nsys);
+    if (!offsets) return fail(ctx, GBH_ERR_ARG, "offsets is NULL");
+    if (offsets[0] != 0) return fail(ctx, GBH_ERR_ARG, "offsets[0] must be 0");
+    for (int32_t q = 0; q < nsys; ++q)
+        if (offsets[q + 1] < offsets[q]) return fail(ctx, GBH_ERR_ARG, "offsets decrease at system %d", q);
+    const int64_t n = offsets[nsys];
+    CK(cudaEventRecord(ctx->ev[0], ctx->stream));
+    if ((rc = upload_state(ctx, n, px, py, pz, vx, vy, vz, ax, ay, az, mass, kind, alive))) return rc;
+    std::vector<uint16_t> sys(static_cast<size_t>(n));
+    for (int32_t q = 0; q < nsys; ++q)
+        for (int64_t i = offsets[q]; i < offsets[q + 1]; ++i) sys[size_t(i)] = uint16_t(q);
+    CK(grow(ctx->sys_of, ctx->sys_of_cap, n + 1));
+    CK(grow(ctx->sys_off, ctx->sys_off_cap, int64_t(nsys) + 1));
+    if (n > 0) CK(cudaMemcpy(ctx->sys_of, sys.data(), sizeof(uint16_t) * size_t(n), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(ctx->sys_off, offsets, sizeof(int64_t) * size_t(nsys + 1), cudaMemcpyHostToDevice));
+    ctx->h2d += int64_t(sizeof(uint16_t) * size_t(n) + sizeof(int64_t) * size_t(nsys + 1));
+    ctx->nsys = nsys;
+    ++ctx->sys_gen;
+    return finish(ctx, false);
+}
+
+int gbh_forest_layout(gbh_ctx *ctx, int32_t nsys, int64_t *star_range, int64_t *node_range) {
+    int rc = begin(ctx);
+    if (rc) return rc;
+    if (!ctx->tb.info || !ctx->tb.geo) return fail(ctx, GBH_ERR_STATE, "no tree built yet");
+    if (nsys != ctx->tb.nsys) return fail(ctx, GBH_ERR_ARG, "the last tree has %d systems", ctx->tb.nsys);
+    std::vector<gbh::SysGeo> geo(static_cast<size_t>(nsys));
+    CK(cudaMemcpy(geo.data(), ctx->tb.geo, sizeof(gbh::SysGeo) * size_t(nsys), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(&ctx->info_host, ctx->tb.info, sizeof(DevInfo), cudaMemcpyDeviceToHost));
+    for (int32_t q = 0; q < nsys; ++q) {
+        if (star_range) {
+            star_range[2 * q] = geo[size_t(q)].star_lo;
+            star_range[2 * q + 1] = geo[size_t(q)].star_hi;
+        }
+        if (node_range) {
+            int64_t lo = geo[size_t(q)].root, hi = lo;
+            if (lo >= 0) {  // the next non-empty system's root, or the end of the table
+                hi = ctx->info_host.nnodes;
+                for (int32_t r = q + 1; r < nsys; ++r)
+                    if (geo[size_t(r)].root >= 0) {
+                        hi = geo[size_t(r)].root;
+                        break;
+                    }
+            } else {
+                lo = hi = 0;
+            }
+            node_range[2 * q] = lo;
+            node_range[2 * q + 1] = hi;
+        }
+    }
     return GBH_OK;
 }
 

@@ -31,12 +31,28 @@ struct DevInfo {
     uint32_t work;            // work counter of persistent kernels
     uint32_t nleaves;         // leaves appended to the leaf list
     uint32_t ntargets;        // entries of the target list (walks restricted to active stars)
+    uint32_t ngroups;         // mixed-walk groups of a forest
     int32_t next_tick;        // block steps: the earliest step end over all bodies
     // FP32 views for the FP32 upsweep: min corner and side as hi + lo pairs, and the
     // opening base 2 * half_L / theta per level L
     float min_hi[3], min_lo[3];
     float side_hi, side_lo;
     float crit_base[kMaxLevel + 1];
+};
+
+// Geometry and layout of one system of a forest (a single state is a forest of one system):
+// its root cube, FP32 views of it, the opening bases per level, its sorted star range, its
+// root node and its first mixed-walk group.
+struct SysGeo {
+    double minx, miny, minz, side, scale;
+    float min_hi[3], min_lo[3];
+    float side_hi, side_lo;
+    float crit_base[kMaxLevel + 1];
+    long long kmin[3], kmax[3];  // ordered keys of the bbox (accumulated by atomics)
+    int32_t star_lo, star_hi;    // sorted range of its stars
+    int32_t root;                // index of its root node; its nodes follow in its own serial layout
+    int32_t group_lo, ngroups;   // its 64-star mixed-walk groups
+    int32_t pad;
 };
 
 // The Metal kernel's GNode (gpu_darwin.go:79,121-124): com (x,y,z,m), q1 (qxx,qyy,qzz,qxy),
@@ -85,6 +101,13 @@ struct TreeBufs {
     int2 *mrange = nullptr;
     int32_t *leaves = nullptr;      // sorted position of every leaf's first star
     int32_t *targets = nullptr;     // sorted positions of the stars a restricted walk evaluates
+    // forest: systems, their geometry, the system of every sorted star, mixed-walk groups
+    int32_t nsys = 1;
+    int32_t cap_sys = 0;
+    SysGeo *geo = nullptr;
+    int32_t *sid_sorted = nullptr;  // only when nsys > 1
+    int4 *groups = nullptr;         // (first sorted star, count, root, 0); only when nsys > 1
+    int64_t cap_groups = 0;
     bool moments_exact = false;     // the last build ran the bit-exact FP64 upsweep
     // scan temporaries
     uint32_t *scan_tmp = nullptr;
@@ -100,15 +123,18 @@ struct Launch {
 };
 
 // ---- tree.cu (FP64 parts compiled without FMA contraction) ----
-cudaError_t tree_alloc(TreeBufs &b, int64_t n, int leaf_size);
+cudaError_t tree_alloc(TreeBufs &b, int64_t n, int leaf_size, int32_t nsys = 1);
 void tree_free(TreeBufs &b);
 // Builds the tree of the alive non-hole bodies; zeroes alive holes' accelerations. exact:
 // FP64 moments bit identical to the reference (the FP64 walk); otherwise the FP32 upsweep of
 // moments.cu, which feeds the FP32 walks.
+// Forests: sys_of (state order, nsys > 1 only) is each body's system, sys_off (nsys + 1 entries,
+// state order) the first body of each system; bodies of a system are contiguous.
 cudaError_t tree_build(const Launch &L, TreeBufs &b, int64_t n, const double *px, const double *py,
                        const double *pz, const double *mass, const uint8_t *kind,
                        const uint8_t *alive, double *ax, double *ay, double *az, double theta,
-                       int leaf_size, int dm_off, bool exact, bool plain_records = true);
+                       int leaf_size, int dm_off, bool exact, bool plain_records = true,
+                       const uint16_t *sys_of = nullptr, const int64_t *sys_off = nullptr);
 // Block time steps (see tree.cu): tick-0 opening kicks and rungs, drift of all bodies, and the
 // closing/opening kicks of the bodies whose step ends at tick. DevInfo.next_tick receives the
 // earliest step end over all bodies.

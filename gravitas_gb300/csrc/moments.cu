@@ -81,7 +81,7 @@ __device__ __forceinline__ void quad_add(FMom &q, float m, float ex, float ey, f
 
 // Finishes node r: centre of mass from the reference point and mean offset (or the geometric
 // centre for zero mass), crit2, and the walk records.
-__device__ __forceinline__ void finish_fast(const DevInfo &inf, FMom &q, float rhx, float rhy, float rhz, float rlx,
+__device__ __forceinline__ void finish_fast(const SysGeo &inf, FMom &q, float rhx, float rhy, float rhz, float rlx,
                                             float rly, float rlz, float ox, float oy, float oz, uint64_t key, int L,
                                             const gbh_node *nodes, int32_t r, PNode *pn, MNode *mn, int2 *mr,
                                             bool plain_records) {
@@ -129,7 +129,8 @@ __global__ __launch_bounds__(kThreads) void k_upsweep_fast(const uint64_t *__res
                                                            const int32_t *__restrict__ n_parent,
                                                            const uint32_t *__restrict__ n_info, int32_t *n_arrive,
                                                            PNode *pn, MNode *mn, int2 *mr, bool plain_records,
-                                                           DevInfo *err_info) {
+                                                           const int32_t *__restrict__ sid_sorted,
+                                                           const SysGeo *__restrict__ geo, DevInfo *err_info) {
     int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (t >= int64_t(info->nleaves)) return;
     const DevInfo inf = *info;
@@ -175,8 +176,8 @@ __global__ __launch_bounds__(kThreads) void k_upsweep_fast(const uint64_t *__res
                 quad_add(q, h.w, ex, ey, ez);
             }
         }
-        finish_fast(inf, q, rh.x, rh.y, rh.z, rl.x, rl.y, rl.z, ox, oy, oz, keys[lo], int(n_info[r] & 0xffu), nodes,
-                    r, pn, mn, mr, plain_records);
+        finish_fast(geo[sid_sorted ? sid_sorted[lo] : 0], q, rh.x, rh.y, rh.z, rl.x, rl.y, rl.z, ox, oy, oz, keys[lo],
+                    int(n_info[r] & 0xffu), nodes, r, pn, mn, mr, plain_records);
     }
     int32_t cur = r;
     for (int guard = 0; guard <= kMaxLevel + 1; ++guard) {
@@ -224,7 +225,8 @@ __global__ __launch_bounds__(kThreads) void k_upsweep_fast(const uint64_t *__res
             float ez = ((a.z - ra.z) + (b.z - rb.z)) - oz;
             quad_add(q, b.w, ex, ey, ez);
         }
-        finish_fast(inf, q, ra.x, ra.y, ra.z, rb.x, rb.y, rb.z, ox, oy, oz, keys[nodes[par].lo],
+        const int32_t plo = nodes[par].lo;
+        finish_fast(geo[sid_sorted ? sid_sorted[plo] : 0], q, ra.x, ra.y, ra.z, rb.x, rb.y, rb.z, ox, oy, oz, keys[plo],
                     int(n_info[par] & 0xffu), nodes, par, pn, mn, mr, plain_records);
         cur = par;
     }
@@ -257,7 +259,7 @@ cudaError_t upsweep_fast(const Launch &L, TreeBufs &b, bool plain_records) {
     int64_t nb = (b.cap_n + kThreads - 1) / kThreads;
     k_upsweep_fast<<<unsigned(nb < 1 ? 1 : nb), kThreads, 0, L.stream>>>(
         b.keys, b.info, b.leaves, cnt, base, b.pre_ref, b.st_hi, b.st_lo, b.nodes, b.n_parent, b.n_info, b.n_arrive,
-        b.pnodes, b.mnodes, b.mrange, plain_records, b.info);
+        b.pnodes, b.mnodes, b.mrange, plain_records, b.nsys > 1 ? b.sid_sorted : nullptr, b.geo, b.info);
     ++*L.count;
     return cudaGetLastError();
 }

@@ -221,7 +221,8 @@ __global__ __launch_bounds__(kThreads) void k_flags_bbox(int64_t n, const double
 constexpr int kFinalThreads = 1024;
 __global__ __launch_bounds__(kFinalThreads) void k_bbox_final(int nparts, const double *__restrict__ part, int64_t n,
                                                               const uint32_t *__restrict__ scan, const uint8_t *kind,
-                                                              const uint8_t *alive, double theta, DevInfo *info) {
+                                                              const uint8_t *alive, double theta, DevInfo *info,
+                                                              SysGeo *geo) {
     long long kmn[3] = {LLONG_MAX, LLONG_MAX, LLONG_MAX}, kmx[3] = {LLONG_MIN, LLONG_MIN, LLONG_MIN};
     for (int b = threadIdx.x; b < nparts; b += blockDim.x)
         for (int c = 0; c < 3; ++c) {
@@ -278,6 +279,26 @@ __global__ __launch_bounds__(kFinalThreads) void k_bbox_final(int nparts, const 
     info->side_lo = __double2float_rn(side - double(sh));
     double half = side / 2;
     for (int L = 0; L <= kMaxLevel; ++L, half = half / 2) info->crit_base[L] = __double2float_rn(2 * half / theta);
+    if (geo) {  // the single system of a plain state
+        SysGeo &g = geo[0];
+        g.minx = info->minx;
+        g.miny = info->miny;
+        g.minz = info->minz;
+        g.side = side;
+        g.scale = info->scale;
+        for (int c = 0; c < 3; ++c) {
+            g.min_hi[c] = info->min_hi[c];
+            g.min_lo[c] = info->min_lo[c];
+        }
+        g.side_hi = info->side_hi;
+        g.side_lo = info->side_lo;
+        for (int L = 0; L <= kMaxLevel; ++L) g.crit_base[L] = info->crit_base[L];
+        g.star_lo = 0;
+        g.star_hi = int32_t(ns);
+        g.root = 0;
+        g.group_lo = 0;
+        g.ngroups = int32_t((ns + 63) / 64);
+    }
 }
 
 // morton.go:7-15.
@@ -317,7 +338,11 @@ __global__ __launch_bounds__(kThreads) void k_compact_keys(int64_t n, const doub
 
 // ---------------------------------------------------------------- stable LSD radix sort
 
-__global__ __launch_bounds__(kRsThreads) void k_rs_hist(const uint64_t *__restrict__ keys, const DevInfo *info,
+// kSid: the digit is taken from the system id of the element's body (forest sorts by system
+// after the 8 key passes) instead of the key.
+template <bool kSid>
+__global__ __launch_bounds__(kRsThreads) void k_rs_hist(const uint64_t *__restrict__ keys, const int32_t *__restrict__ vals,
+                                                        const uint16_t *__restrict__ sys_of, const DevInfo *info,
                                                         int shift, uint32_t ntiles, uint32_t *__restrict__ hist) {
     __shared__ uint32_t h[kRsBins];
     int64_t n = info->nstars;
@@ -328,7 +353,10 @@ __global__ __launch_bounds__(kRsThreads) void k_rs_hist(const uint64_t *__restri
 #pragma unroll
         for (int it = 0; it < kRsItems; ++it) {
             int64_t idx = base + it * kRsThreads + threadIdx.x;
-            if (idx < n) atomicAdd(&h[(keys[idx] >> shift) & (kRsBins - 1)], 1u);
+            if (idx < n) {
+                uint32_t d = kSid ? uint32_t(sys_of[vals[idx]] >> shift) : uint32_t(keys[idx] >> shift);
+                atomicAdd(&h[d & (kRsBins - 1)], 1u);
+            }
         }
     }
     __syncthreads();
@@ -338,11 +366,12 @@ __global__ __launch_bounds__(kRsThreads) void k_rs_hist(const uint64_t *__restri
 // Stable scatter of one tile. Rank of a key = keys of the same digit earlier in the tile, in
 // the order (item round, warp, lane) used to load them; offs holds the digit-major exclusive
 // scan of the tile histograms, so equal digits keep their input order across tiles too.
+template <bool kSid>
 __global__ __launch_bounds__(kRsThreads) void k_rs_scatter(const uint64_t *__restrict__ kin,
                                                            const int32_t *__restrict__ vin,
                                                            uint64_t *__restrict__ kout, int32_t *__restrict__ vout,
-                                                           DevInfo *info, int shift, uint32_t ntiles,
-                                                           const uint32_t *__restrict__ offs) {
+                                                           const uint16_t *__restrict__ sys_of, DevInfo *info, int shift,
+                                                           uint32_t ntiles, const uint32_t *__restrict__ offs) {
     __shared__ uint32_t s_run[kRsBins];
     __shared__ uint32_t s_goff[kRsBins];
     __shared__ uint32_t s_w[2][kRsWarps][kRsBins];
@@ -374,7 +403,8 @@ __global__ __launch_bounds__(kRsThreads) void k_rs_scatter(const uint64_t *__res
         const int buf = it & 1;
         int64_t idx = base + it * kRsThreads + tid;
         bool valid = idx < n;
-        uint32_t d = valid ? uint32_t(k[it] >> shift) & (kRsBins - 1) : 0u;
+        uint32_t d = 0u;
+        if (valid) d = (kSid ? uint32_t(sys_of[v[it]] >> shift) : uint32_t(k[it] >> shift)) & (kRsBins - 1);
         uint32_t peers = __match_any_sync(0xffffffffu, valid ? d : uint32_t(kRsBins + lane));
         uint32_t rank = __popc(peers & lt);
         if (valid && rank == 0) s_w[buf][warp][d] = __popc(peers);
@@ -410,10 +440,13 @@ __global__ __launch_bounds__(kThreads) void k_gather(const DevInfo *info, const 
                                                      const uint8_t *__restrict__ kind, int dm_off, int fp64_copies,
                                                      double *__restrict__ sx, double *__restrict__ sy,
                                                      double *__restrict__ sz, double *__restrict__ sm,
-                                                     float4 *__restrict__ st_hi, float4 *__restrict__ st_lo) {
+                                                     float4 *__restrict__ st_hi, float4 *__restrict__ st_lo,
+                                                     const uint16_t *__restrict__ sys_of,
+                                                     int32_t *__restrict__ sid_sorted) {
     int64_t k = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (k >= info->nstars) return;
     int32_t i = order[k];
+    if (sys_of) sid_sorted[k] = sys_of[i];
     double x = px[i], y = py[i], z = pz[i];
     double m = mass[i];
     if (dm_off && kind && kind[i] == GBH_DARK_MATTER) m = 0;
@@ -431,10 +464,22 @@ __global__ __launch_bounds__(kThreads) void k_gather(const DevInfo *info, const 
 
 // ---------------------------------------------------------------- node set (chains)
 
-// Shallowest level at which sorted position i starts a new cell (0 for i == 0, kNoCell if its
-// key equals the previous one).
-__device__ __forceinline__ int start_level(const uint64_t *__restrict__ keys, int64_t i) {
-    if (i == 0) return 0;
+// Sorted star range [lo, hi) of the system that sorted position i belongs to (the whole array
+// for a plain state).
+struct SysRange {
+    int64_t lo, hi;
+};
+__device__ __forceinline__ SysRange sys_range(const int32_t *__restrict__ sid_sorted, const SysGeo *__restrict__ geo,
+                                              int64_t i, int64_t n) {
+    if (!sid_sorted) return SysRange{0, n};
+    const SysGeo &g = geo[sid_sorted[i]];
+    return SysRange{g.star_lo, g.star_hi};
+}
+
+// Shallowest level at which sorted position i starts a new cell (0 at the first star of its
+// system, kNoCell if its key equals the previous one).
+__device__ __forceinline__ int start_level(const uint64_t *__restrict__ keys, int64_t i, int64_t lo = 0) {
+    if (i == lo) return 0;
     uint64_t x = keys[i] ^ keys[i - 1];
     if (x == 0) return kNoCell;
     int h = 63 - __clzll(static_cast<long long>(x));
@@ -466,14 +511,14 @@ __device__ int64_t cell_end(const uint64_t *__restrict__ keys, int64_t n, int64_
     return lo;
 }
 
-// First position of i's level-L cell.
-__device__ int64_t cell_start(const uint64_t *__restrict__ keys, int64_t i, int L) {
-    if (L == 0) return 0;
+// First position of i's level-L cell (not before lo_bound, the first star of its system).
+__device__ int64_t cell_start(const uint64_t *__restrict__ keys, int64_t lo_bound, int64_t i, int L) {
+    if (L == 0) return lo_bound;
     uint64_t P = prefix(keys[i], L);
-    int64_t lo = 0, hi = i, step = 1;
+    int64_t lo = lo_bound, hi = i, step = 1;
     for (;;) {
         int64_t probe = i - step;
-        if (probe < 0) break;
+        if (probe < lo_bound) break;
         if (prefix(keys[probe], L) != P) {
             lo = probe + 1;
             break;
@@ -491,21 +536,24 @@ __device__ int64_t cell_start(const uint64_t *__restrict__ keys, int64_t i, int 
 
 // Number of nodes that start at sorted position i.
 __global__ __launch_bounds__(kThreads) void k_chain_count(const uint64_t *__restrict__ keys, const DevInfo *info,
-                                                          int leaf, uint32_t *__restrict__ cnt) {
+                                                          const int32_t *__restrict__ sid_sorted,
+                                                          const SysGeo *__restrict__ geo, int leaf,
+                                                          uint32_t *__restrict__ cnt) {
     int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     int64_t n = info->nstars;
     if (i >= n) return;
-    int L0 = start_level(keys, i);
+    const SysRange R = sys_range(sid_sorted, geo, i, n);
+    int L0 = start_level(keys, i, R.lo);
     uint32_t c = 0;
     if (L0 <= kMaxLevel) {
         bool exists = true;
-        if (i > 0) {  // the parent cell (level L0-1) contains i-1 and i; it splits iff it holds > leaf stars
+        if (i > R.lo) {  // the parent cell (level L0-1) contains i-1 and i; it splits iff it holds > leaf stars
             int Lp = L0 - 1;
-            exists = cell_end(keys, n, i, Lp) - cell_start(keys, i, Lp) > leaf;
+            exists = cell_end(keys, R.hi, i, Lp) - cell_start(keys, R.lo, i, Lp) > leaf;
         }
         if (exists) {
             for (int L = L0;; ++L) {
-                int64_t e = cell_end(keys, n, i, L);
+                int64_t e = cell_end(keys, R.hi, i, L);
                 ++c;
                 if (!(e - i > leaf && L < kMaxLevel)) break;
             }
@@ -523,7 +571,9 @@ __global__ __launch_bounds__(kThreads) void k_chain_emit(const uint64_t *__restr
                                                          uint32_t *__restrict__ pre_info,
                                                          uint32_t *__restrict__ pre_nchild,
                                                          uint32_t *__restrict__ pre_mask,
-                                                         int32_t *__restrict__ leaves) {
+                                                         int32_t *__restrict__ leaves,
+                                                         const int32_t *__restrict__ sid_sorted,
+                                                         const SysGeo *__restrict__ geo) {
     int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     int64_t n = info->nstars;
     uint32_t c = i < n ? cnt[i] : 0;
@@ -539,12 +589,13 @@ __global__ __launch_bounds__(kThreads) void k_chain_emit(const uint64_t *__restr
     if (i >= n) return;
     if (i == n - 1) info->nnodes = int64_t(base[i]) + c;
     if (c == 0) return;
-    int L0 = start_level(keys, i);
+    const SysRange R = sys_range(sid_sorted, geo, i, n);
+    int L0 = start_level(keys, i, R.lo);
     int32_t parent_pre = -1;
-    if (i > 0) {
+    if (i > R.lo) {
         int Lp = L0 - 1;
-        int64_t ps = cell_start(keys, i, Lp);
-        int Lps = start_level(keys, ps);  // ps starts its chain at this level; the parent is Lp - Lps deeper
+        int64_t ps = cell_start(keys, R.lo, i, Lp);
+        int Lps = start_level(keys, ps, R.lo);  // ps starts its chain at this level; the parent is Lp - Lps deeper
         parent_pre = int32_t(base[ps]) + (Lp - Lps);
     }
     uint64_t key = keys[i];
@@ -570,20 +621,27 @@ __global__ __launch_bounds__(kThreads) void k_ref_index(const DevInfo *info, con
                                                         const uint32_t *__restrict__ pre_info,
                                                         const uint32_t *__restrict__ pre_mask,
                                                         const uint32_t *__restrict__ child_base,
-                                                        int32_t *__restrict__ pre_ref) {
+                                                        int32_t *__restrict__ pre_ref,
+                                                        const int32_t *__restrict__ sid_sorted,
+                                                        const SysGeo *__restrict__ geo) {
     int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (i >= info->nstars) return;
+    int64_t n = info->nstars;
+    if (i >= n) return;
     uint32_t c = cnt[i];
+    if (c == 0) return;
+    // a system's nodes are the pre-order block starting at its root (pre-order index of its
+    // first star's chain); its reference layout fills the same block
+    const uint32_t root = base[sys_range(sid_sorted, geo, i, n).lo];
     uint32_t p = base[i];
     for (uint32_t t = 0; t < c; ++t, ++p) {
         int32_t pp = pre_parent[p];
         if (pp < 0) {
-            pre_ref[p] = 0;
+            pre_ref[p] = int32_t(root);
             continue;
         }
         uint32_t oct = (pre_info[p] >> 8) & 0xffu;
         uint32_t pmask = pre_mask[pp];
-        pre_ref[p] = int32_t(1 + child_base[pp] + __popc(pmask & ((1u << oct) - 1u)));
+        pre_ref[p] = int32_t(root + 1 + (child_base[pp] - child_base[root]) + __popc(pmask & ((1u << oct) - 1u)));
     }
 }
 
@@ -597,27 +655,32 @@ __global__ __launch_bounds__(kThreads) void k_emit_nodes(const uint64_t *__restr
                                                          const uint32_t *__restrict__ child_base,
                                                          const int32_t *__restrict__ pre_ref, gbh_node *__restrict__ nodes,
                                                          int32_t *__restrict__ n_parent, uint32_t *__restrict__ n_info,
-                                                         int32_t *__restrict__ n_arrive) {
+                                                         int32_t *__restrict__ n_arrive,
+                                                         const int32_t *__restrict__ sid_sorted,
+                                                         const SysGeo *__restrict__ geo) {
     int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     int64_t n = info->nstars;
     if (i >= n) return;
     const int64_t nn = info->nnodes;
     uint32_t c = cnt[i];
+    if (c == 0) return;
+    const SysRange R = sys_range(sid_sorted, geo, i, n);
+    const uint32_t root = base[R.lo];
     uint32_t p = base[i];
     for (uint32_t t = 0; t < c; ++t, ++p) {
         uint32_t inf = pre_info[p];
         int L = int(inf & 0xffu);
         uint32_t mask = pre_mask[p];
-        int64_t hi = cell_end(keys, n, i, L);
+        int64_t hi = cell_end(keys, R.hi, i, L);
         int32_t r = pre_ref[p];
         if (r < 0 || r >= nn) {
             dev_error(info, 11);
             continue;
         }
         gbh_node &nd = nodes[r];
-        nd.first = mask ? int32_t(1 + child_base[p]) : -1;
-        int32_t nx = hi == n ? -1 : pre_ref[base[hi]];
-        if (nx >= nn || (hi < n && cnt[hi] == 0)) {
+        nd.first = mask ? int32_t(root + 1 + (child_base[p] - child_base[root])) : -1;
+        int32_t nx = hi == R.hi ? -1 : pre_ref[base[hi]];  // a system's walk ends at its own last node
+        if (nx >= nn || (hi < R.hi && cnt[hi] == 0)) {
             dev_error(info, 12);
             nx = -1;
         }
@@ -650,7 +713,7 @@ __device__ __forceinline__ void quad_add(Moments &q, double m, double dx, double
 
 // Geometric centre and half side of the level-L cell containing key, through the same
 // rounded additions as the recursion c_child = c + offset(oct, bit) * half/2 (build.go:142-152).
-__device__ __forceinline__ void cell_center(const DevInfo &inf, uint64_t key, int L, double &cx, double &cy,
+__device__ __forceinline__ void cell_center(const SysGeo &inf, uint64_t key, int L, double &cx, double &cy,
                                             double &cz, double &half) {
     double h = inf.side / 2;
     cx = inf.minx + h;
@@ -700,10 +763,10 @@ __device__ __forceinline__ void write_node(gbh_node *nodes, PNode *pn, MNode *mn
     mr[r] = make_int2(lo, hi);
 }
 
-__device__ __forceinline__ double crit2_of(const DevInfo &inf, const Moments &q, double cx, double cy, double cz,
+__device__ __forceinline__ double crit2_of(double theta, const Moments &q, double cx, double cy, double cz,
                                            double half) {
     double delta = sqrt((q.x - cx) * (q.x - cx) + (q.y - cy) * (q.y - cy) + (q.z - cz) * (q.z - cz));
-    double crit = 2 * half / inf.theta + delta;
+    double crit = 2 * half / theta + delta;
     return crit * crit;
 }
 
@@ -715,7 +778,8 @@ __global__ __launch_bounds__(kThreads) void k_upsweep(const uint64_t *__restrict
                                                       const double *__restrict__ sm, gbh_node *nodes,
                                                       const int32_t *__restrict__ n_parent,
                                                       const uint32_t *__restrict__ n_info, int32_t *n_arrive, PNode *pn,
-                                                      MNode *mn, int2 *mr, DevInfo *err_info) {
+                                                      MNode *mn, int2 *mr, const int32_t *__restrict__ sid_sorted,
+                                                      const SysGeo *__restrict__ geo, DevInfo *err_info) {
     int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= info->nstars) return;
     uint32_t c = cnt[i];
@@ -734,7 +798,8 @@ __global__ __launch_bounds__(kThreads) void k_upsweep(const uint64_t *__restrict
             q.m = q.m + mj;
         }
         double cx, cy, cz, half;
-        cell_center(inf, keys[lo], L, cx, cy, cz, half);
+        const SysGeo &g = geo[sid_sorted ? sid_sorted[lo] : 0];
+        cell_center(g, keys[lo], L, cx, cy, cz, half);
         if (q.m > 0) {
             q.x = q.x / q.m;
             q.y = q.y / q.m;
@@ -745,7 +810,7 @@ __global__ __launch_bounds__(kThreads) void k_upsweep(const uint64_t *__restrict
             q.z = cz;
         }
         for (int32_t j = lo; j < hi; ++j) quad_add(q, sm[j], sx[j] - q.x, sy[j] - q.y, sz[j] - q.z);
-        write_node(nodes, pn, mn, mr, r, q, crit2_of(inf, q, cx, cy, cz, half));
+        write_node(nodes, pn, mn, mr, r, q, crit2_of(inf.theta, q, cx, cy, cz, half));
     }
     int32_t cur = r;
     for (int guard = 0; guard <= kMaxLevel + 1; ++guard) {
@@ -771,7 +836,8 @@ __global__ __launch_bounds__(kThreads) void k_upsweep(const uint64_t *__restrict
         }
         int L = int(n_info[par] & 0xffu);
         double cx, cy, cz, half;
-        cell_center(inf, keys[nodes[par].lo], L, cx, cy, cz, half);
+        const int32_t plo = nodes[par].lo;
+        cell_center(geo[sid_sorted ? sid_sorted[plo] : 0], keys[plo], L, cx, cy, cz, half);
         if (q.m > 0) {
             q.x = q.x / q.m;
             q.y = q.y / q.m;
@@ -791,7 +857,7 @@ __global__ __launch_bounds__(kThreads) void k_upsweep(const uint64_t *__restrict
             quad_add(q, __ldcg(&nodes[ch].m), __ldcg(&nodes[ch].x) - q.x, __ldcg(&nodes[ch].y) - q.y,
                      __ldcg(&nodes[ch].z) - q.z);
         }
-        write_node(nodes, pn, mn, mr, par, q, crit2_of(inf, q, cx, cy, cz, half));
+        write_node(nodes, pn, mn, mr, par, q, crit2_of(inf.theta, q, cx, cy, cz, half));
         cur = par;
     }
 }
@@ -803,7 +869,9 @@ __global__ __launch_bounds__(kThreads) void k_walk_fp64(const DevInfo *info, con
                                                         const double *__restrict__ sz, const double *__restrict__ sm,
                                                         const int32_t *__restrict__ order, double eps2, int quad,
                                                         double *ax, double *ay, double *az,
-                                                        const int32_t *__restrict__ targets, DevInfo *err_info) {
+                                                        const int32_t *__restrict__ targets,
+                                                        const int32_t *__restrict__ sid_sorted,
+                                                        const SysGeo *__restrict__ geo, DevInfo *err_info) {
     int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     int64_t ns = info->nstars;
     if (t >= (targets ? int64_t(info->ntargets) : ns)) return;
@@ -812,7 +880,8 @@ __global__ __launch_bounds__(kThreads) void k_walk_fp64(const DevInfo *info, con
     double x = sx[k], y = sy[k], z = sz[k];
     double fax = 0, fay = 0, faz = 0;
     int64_t steps = 0;
-    for (int32_t i = nn > 0 ? 0 : -1; i >= 0;) {
+    const int32_t root = sid_sorted ? geo[sid_sorted[k]].root : 0;  // the star's own system
+    for (int32_t i = nn > 0 ? root : -1; i >= 0;) {
         if (++steps > nn || i >= nn) {  // each node is visited at most once
             dev_error(err_info, 1);
             break;
@@ -981,14 +1050,16 @@ __global__ __launch_bounds__(kThreads) void k_potential_walk(const DevInfo *info
                                                              const double *py, const double *pz, const double *mass,
                                                              const uint8_t *kind, const int32_t *holes, int32_t nholes,
                                                              double eps2, double c, int dm_off, int quad, double *part,
-                                                             DevInfo *err_info) {
+                                                             const int32_t *__restrict__ sid_sorted,
+                                                             const SysGeo *__restrict__ geo, DevInfo *err_info) {
     int64_t k = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     int64_t ns = info->nstars, nn = info->nnodes;
     double v = 0;
     if (k < ns) {
         double x = sx[k], y = sy[k], z = sz[k], psi = 0;
         int64_t steps = 0;
-        for (int32_t i = nn > 0 ? 0 : -1; i >= 0;) {
+        const int32_t root = sid_sorted ? geo[sid_sorted[k]].root : 0;
+        for (int32_t i = nn > 0 ? root : -1; i >= 0;) {
             if (++steps > nn || i >= nn) {
                 dev_error(err_info, 2);
                 break;
@@ -1064,6 +1135,167 @@ constexpr int kFlagBlocksMax = 1024;
 
 }  // namespace
 
+// ---------------------------------------------------------------- forests (many systems)
+
+namespace {
+
+__global__ void k_sys_init(int32_t nsys, SysGeo *geo) {
+    int32_t s = int32_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (s >= nsys) return;
+    for (int c = 0; c < 3; ++c) {
+        geo[s].kmin[c] = LLONG_MAX;
+        geo[s].kmax[c] = LLONG_MIN;
+    }
+}
+
+// Star flags, alive holes' accelerations zeroed, and each system's bbox (ordered keys, one
+// warp-wide atomic per quantity when the warp's stars share a system).
+__global__ __launch_bounds__(kThreads) void k_flags_sys(int64_t n, const double *__restrict__ px,
+                                                        const double *__restrict__ py, const double *__restrict__ pz,
+                                                        const uint8_t *__restrict__ kind,
+                                                        const uint8_t *__restrict__ alive,
+                                                        const uint16_t *__restrict__ sys_of, uint32_t *__restrict__ flag,
+                                                        SysGeo *geo, double *ax, double *ay, double *az) {
+    int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    bool st = false;
+    int s = -1;
+    long long k[3] = {LLONG_MAX, LLONG_MAX, LLONG_MAX};
+    if (i < n) {
+        uint8_t al = alive ? alive[i] : 1, kd = kind ? kind[i] : 0;
+        st = is_star(al, kd);
+        flag[i] = st;
+        if (st) {
+            s = sys_of[i];
+            k[0] = ord_key(px[i]);
+            k[1] = ord_key(py[i]);
+            k[2] = ord_key(pz[i]);
+        } else if (al && kd == GBH_BLACK_HOLE) {
+            ax[i] = 0;
+            ay[i] = 0;
+            az[i] = 0;
+        }
+    }
+    unsigned m = __match_any_sync(0xffffffffu, s);
+    int lane = threadIdx.x & 31;
+    bool uniform = m == 0xffffffffu;
+    if (uniform) {
+        if (s < 0) return;
+        long long mn[3] = {k[0], k[1], k[2]}, mx[3] = {k[0], k[1], k[2]};
+        for (int c = 0; c < 3; ++c)
+            for (int o = 16; o > 0; o >>= 1) {
+                mn[c] = min(mn[c], __shfl_xor_sync(0xffffffffu, mn[c], o));
+                mx[c] = max(mx[c], __shfl_xor_sync(0xffffffffu, mx[c], o));
+            }
+        if (lane == 0)
+            for (int c = 0; c < 3; ++c) {
+                atomicMin(&geo[s].kmin[c], mn[c]);
+                atomicMax(&geo[s].kmax[c], mx[c]);
+            }
+    } else if (s >= 0) {
+        for (int c = 0; c < 3; ++c) {
+            atomicMin(&geo[s].kmin[c], k[c]);
+            atomicMax(&geo[s].kmax[c], k[c]);
+        }
+    }
+}
+
+// Per system: root cube (build.go:19-21), FP32 views, opening bases, sorted star range.
+// Thread 0 also resets the per-build scalars.
+__global__ void k_sys_final(int32_t nsys, int64_t n, const int64_t *__restrict__ sys_off,
+                            const uint32_t *__restrict__ scan, const uint8_t *kind, const uint8_t *alive, double theta,
+                            SysGeo *geo, DevInfo *info) {
+    int32_t s = int32_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    int64_t total = n > 0 ? int64_t(scan[n - 1]) + (is_star(alive ? alive[n - 1] : 1, kind ? kind[n - 1] : 0) ? 1 : 0)
+                          : 0;
+    if (s == 0) {
+        info->theta = theta;
+        info->nstars = total;
+        info->nnodes = 0;
+        info->err = 0;
+        info->err_where = 0;
+        info->work = 0;
+        info->nleaves = 0;
+    }
+    if (s >= nsys) return;
+    SysGeo &g = geo[s];
+    double mn[3], mx[3];
+    for (int c = 0; c < 3; ++c) {
+        mn[c] = ord_val(g.kmin[c]);
+        mx[c] = ord_val(g.kmax[c]);
+    }
+    double side = fmax(mx[0] - mn[0], fmax(mx[1] - mn[1], mx[2] - mn[2]));
+    side = fmax(side * (1 + 1e-9), 1e-12);
+    g.minx = mn[0];
+    g.miny = mn[1];
+    g.minz = mn[2];
+    g.side = side;
+    g.scale = double(1 << kMortonBits) / side;
+    for (int c = 0; c < 3; ++c) {
+        float h = __double2float_rn(mn[c]);
+        g.min_hi[c] = h;
+        g.min_lo[c] = __double2float_rn(mn[c] - double(h));
+    }
+    float sh = __double2float_rn(side);
+    g.side_hi = sh;
+    g.side_lo = __double2float_rn(side - double(sh));
+    double half = side / 2;
+    for (int L = 0; L <= kMaxLevel; ++L, half = half / 2) g.crit_base[L] = __double2float_rn(2 * half / theta);
+    int64_t a = sys_off[s], b = sys_off[s + 1];
+    g.star_lo = int32_t(a < n ? int64_t(scan[a]) : total);
+    g.star_hi = int32_t(b < n ? int64_t(scan[b]) : total);
+}
+
+// Each star's Morton key in its own system's cube (build.go:19-31).
+__global__ __launch_bounds__(kThreads) void k_compact_keys_sys(int64_t n, const double *__restrict__ px,
+                                                               const double *__restrict__ py,
+                                                               const double *__restrict__ pz,
+                                                               const uint8_t *__restrict__ kind,
+                                                               const uint8_t *__restrict__ alive,
+                                                               const uint16_t *__restrict__ sys_of,
+                                                               const uint32_t *__restrict__ scan,
+                                                               const SysGeo *__restrict__ geo,
+                                                               uint64_t *__restrict__ keys, int32_t *__restrict__ order) {
+    int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    if (!is_star(alive ? alive[i] : 1, kind ? kind[i] : 0)) return;
+    const SysGeo &g = geo[sys_of[i]];
+    double sc = g.scale;
+    uint64_t k = spread(cell(px[i], g.minx, sc)) << 2 | spread(cell(py[i], g.miny, sc)) << 1 |
+                 spread(cell(pz[i], g.minz, sc));
+    uint32_t pos = scan[i];
+    keys[pos] = k;
+    order[pos] = int32_t(i);
+}
+
+// Roots (the pre-order index of a system's first star chain) and the 64-star groups of the
+// mixed walk, which never straddle two systems.
+__global__ void k_sys_layout(int32_t nsys, const uint32_t *__restrict__ base, SysGeo *geo, DevInfo *info) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    int32_t groups = 0;
+    for (int32_t s = 0; s < nsys; ++s) {
+        SysGeo &g = geo[s];
+        int32_t cnt = g.star_hi - g.star_lo;
+        g.root = cnt > 0 ? int32_t(base[g.star_lo]) : -1;
+        g.group_lo = groups;
+        g.ngroups = (cnt + 63) / 64;
+        groups += g.ngroups;
+    }
+    info->ngroups = uint32_t(groups);
+}
+
+__global__ void k_sys_groups(int32_t nsys, const SysGeo *__restrict__ geo, int4 *__restrict__ groups) {
+    int32_t s = int32_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (s >= nsys) return;
+    const SysGeo &g = geo[s];
+    for (int32_t q = 0; q < g.ngroups; ++q) {
+        int32_t start = g.star_lo + 64 * q;
+        int32_t cnt = g.star_hi - start < 64 ? g.star_hi - start : 64;
+        groups[g.group_lo + q] = make_int4(start, cnt, g.root, 0);
+    }
+}
+
+}  // namespace
+
 int64_t scan_tmp_size(int64_t n) {
     int64_t total = 0;
     for (int64_t t = (n + kScanTile - 1) / kScanTile; t > 1; t = (t + kScanTile - 1) / kScanTile) total += t;
@@ -1081,7 +1313,7 @@ static cudaError_t scan_dyn(const Launch &L, const uint32_t *in, uint32_t *out, 
 
 void tree_free(TreeBufs &b) {
     void *ptrs[] = {b.flag, b.bbox_part, b.keys, b.keys_alt, b.order, b.order_alt, b.hist, b.sx, b.sy, b.sz, b.sm,
-                    b.st_hi, b.st_lo, b.chain_cnt, b.leaves, b.targets, b.pre_parent, b.pre_info, b.pre_nchild, b.pre_mask, b.pre_ref, b.nodes,
+                    b.st_hi, b.st_lo, b.chain_cnt, b.leaves, b.targets, b.geo, b.sid_sorted, b.groups, b.pre_parent, b.pre_info, b.pre_nchild, b.pre_mask, b.pre_ref, b.nodes,
                     b.n_parent, b.n_info, b.n_arrive, b.pnodes, b.mnodes, b.mrange, b.scan_tmp, b.info};
     for (void *p : ptrs)
         if (p) cudaFree(p);
@@ -1092,9 +1324,14 @@ void tree_free(TreeBufs &b) {
 // cells hold more than leaf stars (only those have children).
 static int64_t node_capacity(int64_t n, int leaf) { return n + 22 * (n / (leaf + 1) + 1) + 1; }
 
-cudaError_t tree_alloc(TreeBufs &b, int64_t n, int leaf) {
+cudaError_t tree_alloc(TreeBufs &b, int64_t n, int leaf, int32_t nsys) {
     int64_t need_nodes = node_capacity(n, leaf);
-    if (n <= b.cap_n && need_nodes <= b.cap_nodes) return cudaSuccess;
+    if (nsys < 1) nsys = 1;
+    if (n <= b.cap_n && need_nodes <= b.cap_nodes && nsys <= b.cap_sys && n / 64 + nsys + 1 <= b.cap_groups) {
+        b.nsys = nsys;
+        return cudaSuccess;
+    }
+    if (nsys > b.cap_sys) b.cap_sys = 0;
     int64_t cn = n > b.cap_n ? n + n / 4 : b.cap_n;  // grow by 1.25x like gpuBuffers.ensure (gpu_darwin.go:164-177)
     int64_t cnodes = need_nodes > b.cap_nodes ? node_capacity(cn, leaf) : b.cap_nodes;
     if (cnodes < need_nodes) cnodes = need_nodes;
@@ -1128,6 +1365,11 @@ cudaError_t tree_alloc(TreeBufs &b, int64_t n, int leaf) {
     GBH_ALLOC(b.chain_cnt, cn * 2);  // counts, then their scan
     GBH_ALLOC(b.leaves, cn);
     GBH_ALLOC(b.targets, cn);
+    const int32_t csys = nsys + nsys / 4 + 1;
+    const int64_t cgroups = cn / 64 + csys + 1;
+    GBH_ALLOC(b.geo, csys);
+    GBH_ALLOC(b.sid_sorted, cn);
+    GBH_ALLOC(b.groups, cgroups);
     GBH_ALLOC(b.pre_parent, cnodes);
     GBH_ALLOC(b.pre_info, cnodes);
     GBH_ALLOC(b.pre_nchild, cnodes);
@@ -1149,6 +1391,9 @@ cudaError_t tree_alloc(TreeBufs &b, int64_t n, int leaf) {
     }
     b.cap_n = cn;
     b.cap_nodes = cnodes;
+    b.cap_sys = csys;
+    b.cap_groups = cgroups;
+    b.nsys = nsys;
     return cudaMemset(b.info, 0, sizeof(DevInfo));
 }
 
@@ -1161,31 +1406,52 @@ cudaError_t tree_alloc(TreeBufs &b, int64_t n, int leaf) {
 
 cudaError_t tree_build(const Launch &L, TreeBufs &b, int64_t n, const double *px, const double *py, const double *pz,
                        const double *mass, const uint8_t *kind, const uint8_t *alive, double *ax, double *ay,
-                       double *az, double theta, int leaf, int dm_off, bool exact, bool plain_records) {
+                       double *az, double theta, int leaf, int dm_off, bool exact, bool plain_records,
+                       const uint16_t *sys_of, const int64_t *sys_off) {
     cudaStream_t s = L.stream;
     const int64_t cap = b.cap_n;
-    // collect + bbox (build.go:62-113)
-    unsigned fb = blocks_for(n, kThreads);
-    if (fb > unsigned(kFlagBlocksMax)) fb = kFlagBlocksMax;
-    k_flags_bbox<<<fb, kThreads, 0, s>>>(n, px, py, pz, kind, alive, b.flag, b.bbox_part, ax, ay, az);
-    GBH_LAUNCH_CHECK();
-    cudaError_t e = scan_u32(L, b.flag, b.flag, n, b.scan_tmp, b.scan_tmp_cap);
-    if (e != cudaSuccess) return e;
-    k_bbox_final<<<1, kFinalThreads, 0, s>>>(int(fb), b.bbox_part, n, b.flag, kind, alive, theta, b.info);
-    GBH_LAUNCH_CHECK();
-    k_compact_keys<<<blocks_for(n, kThreads), kThreads, 0, s>>>(n, px, py, pz, kind, alive, b.flag, b.info, b.keys,
-                                                                b.order);
-    GBH_LAUNCH_CHECK();
+    const bool forest = b.nsys > 1;
+    if (forest && (!sys_of || !sys_off)) return cudaErrorInvalidValue;
+    cudaError_t e;
+    if (!forest) {
+        // collect + bbox (build.go:62-113)
+        unsigned fb = blocks_for(n, kThreads);
+        if (fb > unsigned(kFlagBlocksMax)) fb = kFlagBlocksMax;
+        k_flags_bbox<<<fb, kThreads, 0, s>>>(n, px, py, pz, kind, alive, b.flag, b.bbox_part, ax, ay, az);
+        GBH_LAUNCH_CHECK();
+        e = scan_u32(L, b.flag, b.flag, n, b.scan_tmp, b.scan_tmp_cap);
+        if (e != cudaSuccess) return e;
+        k_bbox_final<<<1, kFinalThreads, 0, s>>>(int(fb), b.bbox_part, n, b.flag, kind, alive, theta, b.info, b.geo);
+        GBH_LAUNCH_CHECK();
+        k_compact_keys<<<blocks_for(n, kThreads), kThreads, 0, s>>>(n, px, py, pz, kind, alive, b.flag, b.info, b.keys,
+                                                                    b.order);
+        GBH_LAUNCH_CHECK();
+    } else {
+        // collect per system: each system gets its own root cube and keys (build.go:11-31)
+        const unsigned sb = blocks_for(b.nsys, 128);
+        k_sys_init<<<sb, 128, 0, s>>>(b.nsys, b.geo);
+        GBH_LAUNCH_CHECK();
+        k_flags_sys<<<blocks_for(n, kThreads), kThreads, 0, s>>>(n, px, py, pz, kind, alive, sys_of, b.flag, b.geo, ax,
+                                                                 ay, az);
+        GBH_LAUNCH_CHECK();
+        e = scan_u32(L, b.flag, b.flag, n, b.scan_tmp, b.scan_tmp_cap);
+        if (e != cudaSuccess) return e;
+        k_sys_final<<<sb, 128, 0, s>>>(b.nsys, n, sys_off, b.flag, kind, alive, theta, b.geo, b.info);
+        GBH_LAUNCH_CHECK();
+        k_compact_keys_sys<<<blocks_for(n, kThreads), kThreads, 0, s>>>(n, px, py, pz, kind, alive, sys_of, b.flag,
+                                                                        b.geo, b.keys, b.order);
+        GBH_LAUNCH_CHECK();
+    }
     // radix sort (morton.go:25-49): 8 stable passes, ping-pong, result back in keys/order
     const uint32_t ntiles = uint32_t((cap + kRsTile - 1) / kRsTile);
     uint64_t *kin = b.keys, *kout = b.keys_alt;
     int32_t *vin = b.order, *vout = b.order_alt;
     for (int shift = 0; shift < 64; shift += 8) {
-        k_rs_hist<<<ntiles, kRsThreads, 0, s>>>(kin, b.info, shift, ntiles, b.hist);
+        k_rs_hist<false><<<ntiles, kRsThreads, 0, s>>>(kin, vin, nullptr, b.info, shift, ntiles, b.hist);
         GBH_LAUNCH_CHECK();
         e = scan_u32(L, b.hist, b.hist, int64_t(ntiles) * kRsBins, b.scan_tmp, b.scan_tmp_cap);
         if (e != cudaSuccess) return e;
-        k_rs_scatter<<<ntiles, kRsThreads, 0, s>>>(kin, vin, kout, vout, b.info, shift, ntiles, b.hist);
+        k_rs_scatter<false><<<ntiles, kRsThreads, 0, s>>>(kin, vin, kout, vout, nullptr, b.info, shift, ntiles, b.hist);
         GBH_LAUNCH_CHECK();
         uint64_t *tk = kin;
         kin = kout;
@@ -1194,14 +1460,32 @@ cudaError_t tree_build(const Launch &L, TreeBufs &b, int64_t n, const double *px
         vin = vout;
         vout = tv;
     }
+    if (forest) {  // then stably by system: (system, key) order, each system's stars contiguous
+        for (int shift = 0; shift < 16; shift += 8) {
+            k_rs_hist<true><<<ntiles, kRsThreads, 0, s>>>(kin, vin, sys_of, b.info, shift, ntiles, b.hist);
+            GBH_LAUNCH_CHECK();
+            e = scan_u32(L, b.hist, b.hist, int64_t(ntiles) * kRsBins, b.scan_tmp, b.scan_tmp_cap);
+            if (e != cudaSuccess) return e;
+            k_rs_scatter<true><<<ntiles, kRsThreads, 0, s>>>(kin, vin, kout, vout, sys_of, b.info, shift, ntiles,
+                                                             b.hist);
+            GBH_LAUNCH_CHECK();
+            uint64_t *tk = kin;
+            kin = kout;
+            kout = tk;
+            int32_t *tv = vin;
+            vin = vout;
+            vout = tv;
+        }
+    }
     // sorted copies (build.go:34-41)
     const unsigned nb = blocks_for(cap, kThreads);
     k_gather<<<nb, kThreads, 0, s>>>(b.info, b.order, px, py, pz, mass, kind, dm_off, exact ? 1 : 0, b.sx, b.sy, b.sz,
-                                     b.sm, b.st_hi, b.st_lo);
+                                     b.sm, b.st_hi, b.st_lo, forest ? sys_of : nullptr, b.sid_sorted);
     GBH_LAUNCH_CHECK();
     // node set
     uint32_t *cnt = b.chain_cnt, *base = b.chain_cnt + cap;
-    k_chain_count<<<nb, kThreads, 0, s>>>(b.keys, b.info, leaf, cnt);
+    const int32_t *sid = forest ? b.sid_sorted : nullptr;
+    k_chain_count<<<nb, kThreads, 0, s>>>(b.keys, b.info, sid, b.geo, leaf, cnt);
     GBH_LAUNCH_CHECK();
     e = scan_dyn(L, cnt, base, cap, &b.info->nstars, b.scan_tmp, b.scan_tmp_cap);
     if (e != cudaSuccess) return e;
@@ -1209,20 +1493,27 @@ cudaError_t tree_build(const Launch &L, TreeBufs &b, int64_t n, const double *px
     if (e == cudaSuccess) e = cudaMemsetAsync(b.pre_nchild, 0, sizeof(uint32_t) * size_t(b.cap_nodes), s);
     if (e != cudaSuccess) return e;
     k_chain_emit<<<nb, kThreads, 0, s>>>(b.keys, b.info, cnt, base, b.pre_parent, b.pre_info, b.pre_nchild, b.pre_mask,
-                                         b.leaves);
+                                         b.leaves, sid, b.geo);
     GBH_LAUNCH_CHECK();
     e = scan_dyn(L, b.pre_nchild, b.pre_nchild, b.cap_nodes, &b.info->nnodes, b.scan_tmp, b.scan_tmp_cap);
     if (e != cudaSuccess) return e;
     k_ref_index<<<nb, kThreads, 0, s>>>(b.info, cnt, base, b.pre_parent, b.pre_info, b.pre_mask, b.pre_nchild,
-                                        b.pre_ref);
+                                        b.pre_ref, sid, b.geo);
     GBH_LAUNCH_CHECK();
     k_emit_nodes<<<nb, kThreads, 0, s>>>(b.keys, b.info, cnt, base, b.pre_parent, b.pre_info, b.pre_mask, b.pre_nchild,
-                                         b.pre_ref, b.nodes, b.n_parent, b.n_info, b.n_arrive);
+                                         b.pre_ref, b.nodes, b.n_parent, b.n_info, b.n_arrive, sid, b.geo);
     GBH_LAUNCH_CHECK();
+    if (forest) {
+        k_sys_layout<<<1, 32, 0, s>>>(b.nsys, base, b.geo, b.info);
+        GBH_LAUNCH_CHECK();
+        k_sys_groups<<<blocks_for(b.nsys, 128), 128, 0, s>>>(b.nsys, b.geo, b.groups);
+        GBH_LAUNCH_CHECK();
+    }
     b.moments_exact = exact;
     if (!exact) return upsweep_fast(L, b, plain_records);
     k_upsweep<<<nb, kThreads, 0, s>>>(b.keys, b.info, cnt, base, b.pre_ref, b.sx, b.sy, b.sz, b.sm, b.nodes,
-                                      b.n_parent, b.n_info, b.n_arrive, b.pnodes, b.mnodes, b.mrange, b.info);
+                                      b.n_parent, b.n_info, b.n_arrive, b.pnodes, b.mnodes, b.mrange, sid, b.geo,
+                                      b.info);
     GBH_LAUNCH_CHECK();
     return cudaSuccess;
 }
@@ -1231,7 +1522,8 @@ cudaError_t walk_fp64(const Launch &L, const TreeBufs &b, int64_t n, double eps2
                       double *az, bool targets) {
     (void)n;
     k_walk_fp64<<<blocks_for(b.cap_n, kThreads), kThreads, 0, L.stream>>>(
-        b.info, b.nodes, b.sx, b.sy, b.sz, b.sm, b.order, eps2, quad, ax, ay, az, targets ? b.targets : nullptr, b.info);
+        b.info, b.nodes, b.sx, b.sy, b.sz, b.sm, b.order, eps2, quad, ax, ay, az, targets ? b.targets : nullptr,
+        b.nsys > 1 ? b.sid_sorted : nullptr, b.geo, b.info);
     GBH_LAUNCH_CHECK();
     return cudaSuccess;
 }
@@ -1270,7 +1562,8 @@ cudaError_t potential_fp64(const Launch &L, const TreeBufs &b, int64_t n, const 
     (void)alive;
     unsigned nb = blocks_for(b.cap_n, kThreads);
     k_potential_walk<<<nb, kThreads, 0, L.stream>>>(b.info, b.nodes, b.sx, b.sy, b.sz, b.sm, b.order, px, py, pz, mass,
-                                                    kind, holes, nholes, eps2, c, dm_off, quad, part, b.info);
+                                                    kind, holes, nholes, eps2, c, dm_off, quad, part,
+                                                    b.nsys > 1 ? b.sid_sorted : nullptr, b.geo, b.info);
     GBH_LAUNCH_CHECK();
     k_potential_final<<<1, kThreads, 0, L.stream>>>(nb, part, b.info, b.sx, b.sy, b.sz, b.sm, px, py, pz, mass, kind,
                                                     holes, nholes, eps2, c, dm_off, u_dev);
@@ -1355,18 +1648,19 @@ cudaError_t morton_sort(const Launch &L, int64_t n, const double *px, const doub
     k_flags_bbox_noacc<<<fb, kThreads, 0, s>>>(n, px, py, pz, kind, alive, flag, bbox_part);
     GBH_LAUNCH_CHECK();
     if ((e = scan_u32(L, flag, flag, n, tmp, tmp_cap)) != cudaSuccess) return e;
-    k_bbox_final<<<1, kFinalThreads, 0, s>>>(int(fb), bbox_part, n, flag, kind, alive, 0.9, info);
+    k_bbox_final<<<1, kFinalThreads, 0, s>>>(int(fb), bbox_part, n, flag, kind, alive, 0.9, info, nullptr);
     GBH_LAUNCH_CHECK();
     k_compact_keys<<<blocks_for(n, kThreads), kThreads, 0, s>>>(n, px, py, pz, kind, alive, flag, info, keys, order);
     GBH_LAUNCH_CHECK();
     uint64_t *kin = keys, *kout = keys_alt;
     int32_t *vin = order, *vout = order_alt;
     for (int shift = 0; shift < 64; shift += 8) {
-        k_rs_hist<<<ntiles ? ntiles : 1, kRsThreads, 0, s>>>(kin, info, shift, ntiles ? ntiles : 1, hist);
+        k_rs_hist<false><<<ntiles ? ntiles : 1, kRsThreads, 0, s>>>(kin, vin, nullptr, info, shift, ntiles ? ntiles : 1,
+                                                                    hist);
         GBH_LAUNCH_CHECK();
         if ((e = scan_u32(L, hist, hist, int64_t(ntiles ? ntiles : 1) * kRsBins, tmp, tmp_cap)) != cudaSuccess) return e;
-        k_rs_scatter<<<ntiles ? ntiles : 1, kRsThreads, 0, s>>>(kin, vin, kout, vout, info, shift, ntiles ? ntiles : 1,
-                                                                 hist);
+        k_rs_scatter<false><<<ntiles ? ntiles : 1, kRsThreads, 0, s>>>(kin, vin, kout, vout, nullptr, info, shift,
+                                                                        ntiles ? ntiles : 1, hist);
         GBH_LAUNCH_CHECK();
         uint64_t *tk = kin;
         kin = kout;

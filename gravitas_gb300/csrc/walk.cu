@@ -42,7 +42,9 @@ __global__ __launch_bounds__(kPlainThreads) void k_walk_plain(const DevInfo *inf
                                                               const float4 *__restrict__ stars,
                                                               const int32_t *__restrict__ order, float eps2,
                                                               double *ax, double *ay, double *az,
-                                                              const int32_t *__restrict__ targets, DevInfo *err_info) {
+                                                              const int32_t *__restrict__ targets,
+                                                              const int32_t *__restrict__ sid_sorted,
+                                                              const SysGeo *__restrict__ geo, DevInfo *err_info) {
     int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     int64_t ns = info->nstars;
     if (t >= (targets ? int64_t(info->ntargets) : ns)) return;
@@ -51,7 +53,7 @@ __global__ __launch_bounds__(kPlainThreads) void k_walk_plain(const DevInfo *inf
     float4 p = stars[k];
     float fax = 0.f, fay = 0.f, faz = 0.f;
     int64_t steps = 0;
-    int i = nn > 0 ? 0 : -1;
+    int i = nn > 0 ? (sid_sorted ? geo[sid_sorted[k]].root : 0) : -1;  // the star's own system
     while (i >= 0) {
         if (++steps > nn || i >= nn) {
             set_err(err_info, 3);
@@ -131,13 +133,24 @@ __global__ __launch_bounds__(kMixedThreads) void k_walk_mixed2(const DevInfo *in
                                                                const float4 *__restrict__ st_lo,
                                                                const int32_t *__restrict__ order, float eps2,
                                                                double *ax, double *ay, double *az,
-                                                               const int32_t *__restrict__ targets, DevInfo *err_info) {
+                                                               const int32_t *__restrict__ targets,
+                                                               const int4 *__restrict__ groups, DevInfo *err_info) {
     const int lane = threadIdx.x & 31;
     const int32_t ns = int32_t(info->nstars);  // the C-ABI caps n at 2^30
-    const int32_t nt = targets ? int32_t(info->ntargets) : ns;
     const uint32_t nn = uint32_t(info->nnodes);
-    const int32_t base = int32_t((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 64;
-    if (base >= nt) return;  // uniform over the warp
+    const int32_t g = int32_t((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    int32_t base, nt, root = 0;
+    if (groups) {  // a forest: group g = up to 64 stars of one system, walked from its root
+        if (uint32_t(g) >= info->ngroups) return;
+        const int4 e = groups[g];
+        base = e.x;
+        nt = e.x + e.y;
+        root = e.z;
+    } else {
+        base = g * 64;
+        nt = targets ? int32_t(info->ntargets) : ns;
+        if (base >= nt) return;  // uniform over the warp
+    }
     const int32_t t0 = base + 2 * lane, t1 = t0 + 1;
     const bool v0 = t0 < nt, v1 = t1 < nt;
     const int32_t first_k = targets ? targets[base] : base;
@@ -153,7 +166,7 @@ __global__ __launch_bounds__(kMixedThreads) void k_walk_mixed2(const DevInfo *in
     float2 sx = f2(0.f), sy = f2(0.f), sz = f2(0.f), cx = f2(0.f), cy = f2(0.f), cz = f2(0.f);
     float2 px = f2(0.f), py = f2(0.f), pz = f2(0.f);
     uint32_t visits = 0;
-    int i = nn > 0 ? 0 : -1;
+    int i = nn > 0 ? root : -1;
     while (i >= 0) {
         if (uint32_t(i) >= nn) {
             if (lane == 0) set_err(err_info, 4);
@@ -273,7 +286,8 @@ __global__ __launch_bounds__(256) void k_fma_probe(int iters, float *out) {
 cudaError_t walk_plain(const Launch &L, const TreeBufs &b, int64_t nstars_cap, float eps2, double *ax, double *ay,
                        double *az, bool targets) {
     k_walk_plain<<<blocks_for(nstars_cap, kPlainThreads), kPlainThreads, 0, L.stream>>>(
-        b.info, b.pnodes, b.st_hi, b.order, eps2, ax, ay, az, targets ? b.targets : nullptr, b.info);
+        b.info, b.pnodes, b.st_hi, b.order, eps2, ax, ay, az, targets ? b.targets : nullptr,
+        b.nsys > 1 ? b.sid_sorted : nullptr, b.geo, b.info);
     ++*L.count;
     return cudaGetLastError();
 }
@@ -281,11 +295,12 @@ cudaError_t walk_plain(const Launch &L, const TreeBufs &b, int64_t nstars_cap, f
 template <bool kQuad, bool kSoft>
 static cudaError_t launch_mixed(const Launch &L, const TreeBufs &b, int64_t nstars_cap, float eps2, double *ax,
                                 double *ay, double *az, bool targets) {
-    int64_t groups = (nstars_cap + 63) / 64;
+    const bool forest = b.nsys > 1;
+    int64_t groups = forest ? b.cap_groups : (nstars_cap + 63) / 64;
     int64_t blocks = (groups + kMixedThreads / 32 - 1) / (kMixedThreads / 32);
     k_walk_mixed2<kQuad, kSoft><<<unsigned(blocks < 1 ? 1 : blocks), kMixedThreads, 0, L.stream>>>(
         b.info, b.mnodes, b.mrange, b.st_hi, b.st_lo, b.order, eps2, ax, ay, az, targets ? b.targets : nullptr,
-        b.info);
+        forest ? b.groups : nullptr, b.info);
     ++*L.count;
     return cudaGetLastError();
 }

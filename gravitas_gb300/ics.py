@@ -14,6 +14,7 @@ arrays, so parity never depends on the generator.
                         velocities from Eddington's formula in the total potential
   merger(n)             two galaxy(n/2) on a parabolic orbit
   far_cluster()         the clumpy cluster plus probe of bh_test.go:294-307
+  forest(nsys)          independent Plummer or galaxy systems of log-uniform sizes, one state
 """
 from __future__ import annotations
 
@@ -315,3 +316,22 @@ def merger(n: int, seed: int = 0, pericentre: float = 5.0, separation: float = 4
     for key in ("ax", "ay", "az", "mass", "kind", "alive"):
         out[key] = np.concatenate([g1[key], g2[key]])
     return out
+
+
+def forest(nsys: int = 64, seed: int = 0, nmin: int = 2048, nmax: int = 65536, scale=(0.5, 2.0)):
+    """nsys independent systems concatenated into one state: each N log-uniform in [nmin, nmax],
+    scale radius uniform in `scale`, a Plummer sphere or a disk+bulge+halo galaxy by its seed.
+    Returns (state, offsets) with offsets[s] the first body of system s."""
+    rng = np.random.default_rng(seed)
+    parts, offsets = [], [0]
+    for q in range(nsys):
+        n = int(round(np.exp(rng.uniform(np.log(nmin), np.log(nmax)))))
+        a = rng.uniform(*scale)
+        if rng.random() < 0.5:
+            s = plummer(n, seed=seed * 1000 + q, a=a)
+        else:
+            s = galaxy(max(n, 16), seed=seed * 1000 + q, r_d=a, z0=0.1 * a, a_b=0.2 * a, r_s=5 * a)
+        parts.append(s)
+        offsets.append(offsets[-1] + len(s["px"]))
+    out = {k: np.concatenate([p[k] for p in parts]) for k in parts[0]}
+    return out, np.array(offsets, np.int64)

@@ -214,6 +214,26 @@ typedef struct {
 /* Diagnostics of the resident state; c is the speed of light of the pair model (0: Newtonian). */
 int gbh_state_diagnostics(gbh_ctx *ctx, const gbh_params *p, double c, gbh_diagnostics *out);
 
+/* ---- Batched forest: many independent systems in one resident state. ---- */
+
+/*
+ * Uploads nsys independent systems (at most 65,535) as one resident state: the bodies of
+ * system s are [offsets[s], offsets[s+1]) (offsets[0] = 0, n = offsets[nsys]); the other
+ * arrays are as in gbh_state_upload. Each system gets its own tree, exactly the tree
+ * bh.Solver builds for that system alone (its own root cube, keys, node layout); one build
+ * and one walk launch serve all systems. gbh_state_step, gbh_state_accelerations,
+ * gbh_state_diagnostics and gbh_state_download then act on the forest; gbh_state_upload
+ * returns to a single system. Block steps are not available for forests.
+ */
+int gbh_forest_upload(gbh_ctx *ctx, int32_t nsys, const int64_t *offsets, const double *px,
+                      const double *py, const double *pz, const double *vx, const double *vy,
+                      const double *vz, const double *ax, const double *ay, const double *az,
+                      const double *mass, const uint8_t *kind, const uint8_t *alive);
+/* Layout of the last forest tree: for system s, star_range[2s..2s+1] is its sorted star range
+   in gbh_tree_export's keys/order and node_range[2s..2s+1] its node range in the node table
+   (links inside are table indices; a system's root is node_range[2s]). Either may be NULL. */
+int gbh_forest_layout(gbh_ctx *ctx, int32_t nsys, int64_t *star_range, int64_t *node_range);
+
 /* ---- Inspection of the last tree (b.nodes / b.order / b.keys in bh.Solver). ---- */
 
 /* Stars and nodes of the last built tree. */
