@@ -338,6 +338,97 @@ def run_profile(args):
     return 0
 
 
+ADJ_N, ADJ_STEPS, ADJ_EVERY, ADJ_EPS, ADJ_DT = 32768, 1000, 50, 0.01, 1e-3
+ADJ_FLOP_FORCE, ADJ_FLOP_VJP = 18, 51  # algorithmic FLOP per ordered pair (force; kick adjoint)
+
+
+def run_adjoint(args):
+    """The differentiable workload: gradient of L = mean |x_T - target|^2 with respect to the
+    initial positions, velocities and masses through gbh_fwd_save / gbh_bwd, on a Plummer
+    sphere of 32,768 lognormal-mass bodies, 1,000 KDK steps of 1e-3, softening 0.01, checkpoints
+    every 50 steps, FP32 pair kernels. Checked against central differences (h = 1e-4) of the
+    same forward on --fd-coords coordinates. One line of JSON; not the headline workload."""
+    from gravitas_gb300 import abi, ics, sim
+    from oracle import oracle as O
+    rank, world, local = dist_env()
+    n, T, K = args.n if args.n != N_DEFAULT else ADJ_N, ADJ_STEPS, ADJ_EVERY
+    s, targets = ics.adjoint_problem(n, seed=0)
+    ctx = abi.Context(local)
+    x0 = np.stack([s["px"], s["py"], s["pz"]], 1)
+    v0 = np.stack([s["vx"], s["vy"], s["vz"]], 1)
+    peak = ctx.probe_fp32_peak(50.0)
+    for _ in range(args.warmup):
+        sim.trajectory_loss_gradient(s, targets, ADJ_DT, ADJ_EPS, T, K, abi.ADJ_FP32, ctx)
+    walls, dev, pair = [], [], []
+    with Clocks(local) as clk:
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            loss, dx, dv, dm = sim.trajectory_loss_gradient(s, targets, ADJ_DT, ADJ_EPS, T, K, abi.ADJ_FP32, ctx)
+            walls.append(time.perf_counter() - t0)
+            tf = ctx.timings()  # of gbh_bwd; the forward's were read below
+            dev.append(tf["total_ms"])
+            pair.append(tf["walk_ms"])
+    # device and pair-kernel time of one forward, read separately
+    ctx.fwd_save(x0, v0, s["mass"], ADJ_DT, ADJ_EPS, T, K, abi.ADJ_FP32)
+    tfw = ctx.timings()
+    ms_grad = statistics.median(walls) * 1e3
+    dev_ms = tfw["total_ms"] + statistics.median(dev)
+    pair_ms = tfw["walk_ms"] + statistics.median(pair)
+    nck = (T + K - 1) // K
+    pairs = n * (n - 1)
+    flop = pairs * (ADJ_FLOP_FORCE * (2 * T + 1 - nck) + ADJ_FLOP_VJP * (T + 1))
+    achieved = flop / (pair_ms * 1e-3) / 1e12
+    # central differences of the same forward on random velocity and mass coordinates
+    rng = np.random.default_rng(5)
+    h, errs, scale = 1e-4, [], float(np.abs(np.concatenate([dv.ravel(), dm])).max())
+    for q in range(args.fd_coords):
+        i, c = int(rng.integers(n)), int(rng.integers(3))
+        vals = []
+        for sign in (1.0, -1.0):
+            v, m = v0.copy(), s["mass"].copy()
+            if q % 2 == 0:
+                v[i, c] += sign * h
+            else:
+                m[i] += sign * h
+            xT, _ = ctx.fwd_save(x0, v, m, ADJ_DT, ADJ_EPS, T, T, abi.ADJ_FP32)
+            vals.append(float(np.sum((xT - targets) ** 2) / n))
+        fd = (vals[0] - vals[1]) / (2 * h)
+        g = dv[i, c] if q % 2 == 0 else dm[i]
+        errs.append(abs(g - fd) / max(abs(fd), 1e-3 * scale))
+    # CPU baseline: the oracle's FP64 adjoint on a bounded sample (all bodies, 4 steps)
+    cpu = None
+    if rank == 0:
+        xT4 = {k: s[k].copy() for k in ("px", "py", "pz", "vx", "vy", "vz", "mass")}
+        t0 = time.perf_counter()
+        O.kdk_direct(xT4, ADJ_DT, ADJ_EPS, 4)
+        gx4 = 2 * (np.stack([xT4["px"], xT4["py"], xT4["pz"]], 1) - targets) / n
+        O.adjoint_direct(s, ADJ_DT, ADJ_EPS, 4, 2, gx4, np.zeros_like(gx4))
+        el = time.perf_counter() - t0
+        cpu = {"value": n * 4 / el, "unit": "particle-steps/s", "cores": os.cpu_count() or 1, "kind": "port",
+               "sample": f"FP64 direct-sum adjoint of the oracle, all {n} bodies, 4 steps, checkpoints every 2 "
+                         f"(forward + backward), {os.cpu_count()} threads"}
+    line = {
+        "metric": f"adjoint particle-steps/s @N={n}: gradient of a final-position loss, {T} KDK steps",
+        "value": n * T / (ms_grad * 1e-3), "unit": "particle-steps/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_grad, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 pairs, f64 state", "data": "synthetic",
+        "config": {"workload": f"Plummer N={n}, lognormal(0.3) masses, eps={ADJ_EPS}, dt={ADJ_DT}, {T} steps, "
+                               f"checkpoints every {K}, targets = x0 rotated 30 deg about z + N(0, 0.01^2)",
+                   "loss": loss},
+        "device_ms_per_gradient": dev_ms, "pair_kernel_ms": pair_ms,
+        "roofline": {"bound": "fp32", "kernels": "k_force32 + k_vjp32", "achieved": achieved, "peak": peak,
+                     "unit": "TFLOP/s", "frac": achieved / peak, "flop_per_pair": [ADJ_FLOP_FORCE, ADJ_FLOP_VJP],
+                     "peak_source": "FP32 FMA probe of this run"},
+        "fd_check": {"coords": len(errs), "h": h, "max_rel": float(max(errs)) if errs else None,
+                     "median_rel": float(np.median(errs)) if errs else None},
+        "cpu_baseline": cpu, "clocks": clk.summary(),
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
@@ -348,7 +439,12 @@ def main():
     ap.add_argument("--leaf", type=int, default=LEAF)
     ap.add_argument("--profile", choices=["mixed", "plain", "fp64"], default=None,
                     help="run only two force evaluations with this walk (for ncu captures)")
+    ap.add_argument("--workload", choices=["merger", "adjoint"], default="merger",
+                    help="adjoint: the differentiable workload (gbh_fwd_save / gbh_bwd), its own JSON line")
+    ap.add_argument("--fd-coords", type=int, default=16, help="adjoint: coordinates checked by central differences")
     args = ap.parse_args()
+    if args.workload == "adjoint":
+        return run_adjoint(args)
     if args.profile:
         return run_profile(args)
     if args.warmup < 3 and args.impl == "ours":

@@ -68,6 +68,14 @@ class Diagnostics(ctypes.Structure):
                     else getattr(self, k)) for k, _ in self._fields_}
 
 
+class AdjointParams(ctypes.Structure):
+    _fields_ = [("dt", ctypes.c_double), ("softening", ctypes.c_double), ("nsteps", ctypes.c_int64),
+                ("every", ctypes.c_int64), ("precision", ctypes.c_int32), ("reserved", ctypes.c_int32 * 3)]
+
+
+ADJ_FP32 = 0
+ADJ_FP64 = 1
+
 NODE_DTYPE = np.dtype(
     [("x", "f8"), ("y", "f8"), ("z", "f8"), ("m", "f8"),
      ("qxx", "f8"), ("qyy", "f8"), ("qzz", "f8"), ("qxy", "f8"), ("qxz", "f8"), ("qyz", "f8"),
@@ -102,6 +110,8 @@ SIGNATURES = {
     "gbh_forest_upload": (ctypes.c_int, [_P, _I32, _P] + [_P] * 12),
     "gbh_forest_layout": (ctypes.c_int, [_P, _I32, _P, _P]),
     "gbh_morton_order_noalloc": (ctypes.c_int, [_I32, _P, _I64] + [_P] * 8 + [ctypes.c_char_p, ctypes.c_int]),
+    "gbh_fwd_save": (ctypes.c_int, [_P, ctypes.POINTER(AdjointParams), _I64] + [_P] * 13),
+    "gbh_bwd": (ctypes.c_int, [_P] + [_P] * 13),
 }
 
 _lib = None
@@ -239,6 +249,36 @@ class Context:
         d = Diagnostics()
         self.call("gbh_state_diagnostics", params, float(c), ctypes.byref(d))
         return d.as_dict()
+
+    def fwd_save(self, x0: np.ndarray, v0: np.ndarray, mass: np.ndarray, dt: float, softening: float,
+                 nsteps: int, every: int, precision: int = ADJ_FP32):
+        """Forward half of the adjoint pair: (x_T, v_T), each n x 3, with the tape kept on the device."""
+        x0 = np.ascontiguousarray(np.asarray(x0, np.float64).T)
+        v0 = np.ascontiguousarray(np.asarray(v0, np.float64).T)
+        m = np.ascontiguousarray(mass, np.float64)
+        n = m.shape[0]
+        out = np.empty((6, n))
+        ap = AdjointParams(float(dt), float(softening), int(nsteps), int(every), int(precision))
+        self.call("gbh_fwd_save", ctypes.byref(ap), n, *[ptr(x0[k]) for k in range(3)],
+                  *[ptr(v0[k]) for k in range(3)], ptr(m), *[ptr(out[k]) for k in range(6)])
+        return out[0:3].T.copy(), out[3:6].T.copy()
+
+    def bwd(self, gx: np.ndarray | None, gv: np.ndarray | None):
+        """Backward half: (dL/dx_0, dL/dv_0) as n x 3 and dL/dm, from dL/dx_T and dL/dv_T."""
+        g = [None] * 6
+        keep = []
+        for k, a in ((0, gx), (3, gv)):
+            if a is not None:
+                a = np.ascontiguousarray(np.asarray(a, np.float64).T)
+                keep.append(a)
+                for c in range(3):
+                    g[k + c] = ptr(a[c])
+        n = keep[0].shape[1] if keep else None
+        if n is None:
+            raise ValueError("bwd needs gx or gv")
+        out = np.empty((7, n))
+        self.call("gbh_bwd", *g, *[ptr(out[k]) for k in range(7)])
+        return out[0:3].T.copy(), out[3:6].T.copy(), out[6].copy()
 
     def probe_fp32_peak(self, ms: float = 50.0) -> float:
         out = np.zeros(1)

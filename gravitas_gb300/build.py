@@ -6,7 +6,9 @@ Each translation unit gets its own floating-point flags:
   walk.cu  fast FP32     FMA contraction on, approximate FP32 division and square root;
   moments.cu             FP32 node moments for the FP32 walks (FMA on, IEEE FP32 division);
   api.cu                 host code;
-  noalloc.cu             the entry point whose temporaries live in a static device array.
+  noalloc.cu             the entry point whose temporaries live in a static device array;
+  adjoint.cu -fmad=false the adjoint pair: FP64 pair kernels bit-exact with the CPU
+                         restatement, FP32 pair kernels with explicit fmaf/rsqrtf.
 Objects compile in parallel; the shared library links the CUDA runtime statically.
 """
 from __future__ import annotations
@@ -29,6 +31,7 @@ UNITS = {
     "moments.cu": [],
     "api.cu": [],
     "noalloc.cu": [],
+    "adjoint.cu": ["-fmad=false"],
 }
 
 

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
@@ -71,6 +72,7 @@ struct gbh_ctx {
     std::vector<cudaEvent_t> evpool;
     size_t evused = 0;
     StepGraph step_graph;
+    gbh::AdjTape adj;  // tape of gbh_fwd_save
     bool use_graphs = true;
     bool capturing = false;  // stage events become graph event-record nodes
     // bookkeeping
@@ -563,6 +565,7 @@ void gbh_destroy(gbh_ctx *c) {
     if (c->stream) cudaStreamSynchronize(c->stream);
     free_graph(c->step_graph);
     gbh::tree_free(c->tb);
+    gbh::adj_free(c->adj);
     free_state(c);
     void *ptrs[] = {c->part,  c->scalar,   c->holes, c->targets,  c->tout,   c->probe,
                     c->scratch3, c->rung, c->end_tick, c->sys_of, c->sys_off};
@@ -925,6 +928,66 @@ int gbh_tree_export(gbh_ctx *ctx, uint64_t *keys, int32_t *order, gbh_node *node
         CK(cudaMemcpy(nodes, ctx->tb.nodes, sizeof(gbh_node) * size_t(cnt), cudaMemcpyDeviceToHost));
     }
     return GBH_OK;
+}
+
+int gbh_fwd_save(gbh_ctx *ctx, const gbh_adjoint_params *ap, int64_t n, const double *px, const double *py,
+                 const double *pz, const double *vx, const double *vy, const double *vz, const double *mass,
+                 double *out_px, double *out_py, double *out_pz, double *out_vx, double *out_vy, double *out_vz) {
+    int rc = begin(ctx);
+    if (rc) return rc;
+    ctx->adj.valid = false;
+    if (!ap) return fail(ctx, GBH_ERR_ARG, "adjoint params are NULL");
+    if (!(ap->softening > 0)) return fail(ctx, GBH_ERR_ARG, "softening %g must be > 0", ap->softening);
+    if (!(std::isfinite(ap->dt))) return fail(ctx, GBH_ERR_ARG, "dt is not finite");
+    if (ap->nsteps < 1 || ap->every < 1) return fail(ctx, GBH_ERR_ARG, "nsteps and every must be >= 1");
+    if (ap->precision != GBH_ADJ_FP32 && ap->precision != GBH_ADJ_FP64)
+        return fail(ctx, GBH_ERR_ARG, "precision %d", ap->precision);
+    if (n < 1 || n > (int64_t(1) << 26)) return fail(ctx, GBH_ERR_ARG, "n = %lld out of range", (long long)n);
+    if (!px || !py || !pz || !vx || !vy || !vz || !mass) return fail(ctx, GBH_ERR_ARG, "array argument is NULL");
+    gbh::AdjTape &t = ctx->adj;
+    CK(cudaEventRecord(ctx->ev[0], ctx->stream));
+    CK(gbh::adj_reserve(t, n, ap->nsteps, ap->every, ap->dt, ap->softening, ap->precision == GBH_ADJ_FP32,
+                        ctx->num_sms));
+    size_t b = sizeof(double) * size_t(n);
+    if ((rc = h2d(ctx, t.x, px, b)) || (rc = h2d(ctx, t.x + n, py, b)) || (rc = h2d(ctx, t.x + 2 * n, pz, b)) ||
+        (rc = h2d(ctx, t.v, vx, b)) || (rc = h2d(ctx, t.v + n, vy, b)) || (rc = h2d(ctx, t.v + 2 * n, vz, b)) ||
+        (rc = h2d(ctx, t.m, mass, b)))
+        return rc;
+    t.mark = [](void *c) { return stage_event(static_cast<gbh_ctx *>(c)); };
+    t.mark_arg = ctx;
+    CK(gbh::adj_forward(launch_of(ctx), t));
+    double *outs[6] = {out_px, out_py, out_pz, out_vx, out_vy, out_vz};
+    for (int k = 0; k < 6; ++k)
+        if (outs[k] && (rc = d2h(ctx, outs[k], (k < 3 ? t.x : t.v) + (k % 3) * n, b))) return rc;
+    t.valid = false;
+    if ((rc = finish(ctx, false))) return rc;
+    t.valid = true;
+    return GBH_OK;
+}
+
+int gbh_bwd(gbh_ctx *ctx, const double *gx, const double *gy, const double *gz, const double *gvx, const double *gvy,
+            const double *gvz, double *dx, double *dy, double *dz, double *dvx, double *dvy, double *dvz, double *dm) {
+    int rc = begin(ctx);
+    if (rc) return rc;
+    gbh::AdjTape &t = ctx->adj;
+    if (!t.valid) return fail(ctx, GBH_ERR_STATE, "no adjoint tape: call gbh_fwd_save first");
+    const int64_t n = t.n;
+    size_t b = sizeof(double) * size_t(n);
+    CK(cudaEventRecord(ctx->ev[0], ctx->stream));
+    const double *gin[6] = {gx, gy, gz, gvx, gvy, gvz};
+    for (int k = 0; k < 6; ++k) {
+        if (gin[k]) {
+            if ((rc = h2d(ctx, t.lam + k * n, gin[k], b))) return rc;
+        } else {
+            CK(cudaMemsetAsync(t.lam + k * n, 0, b, ctx->stream));
+        }
+    }
+    CK(cudaMemsetAsync(t.lam + 6 * n, 0, b, ctx->stream));
+    CK(gbh::adj_backward(launch_of(ctx), t));
+    double *outs[7] = {dx, dy, dz, dvx, dvy, dvz, dm};
+    for (int k = 0; k < 7; ++k)
+        if (outs[k] && (rc = d2h(ctx, outs[k], t.lam + k * n, b))) return rc;
+    return finish(ctx, false);
 }
 
 int gbh_last_timings(gbh_ctx *ctx, gbh_timings *t) {

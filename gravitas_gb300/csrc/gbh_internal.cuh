@@ -190,6 +190,35 @@ cudaError_t morton_sort(const Launch &L, int64_t n, const double *px, const doub
                         const uint8_t *kind, const uint8_t *alive, uint64_t *keys, int32_t *order, void *scratch,
                         size_t scratch_bytes, DevInfo **info_out);
 
+// ---- adjoint.cu (gradient of the KDK leapfrog with the softened direct-sum force) ----
+struct AdjTape {
+    void *block = nullptr;  // one grow-only allocation holding every array below
+    size_t bytes = 0;
+    int64_t n = 0, nsteps = 0, every = 1, nck = 0, chunk = 0;
+    int nsplit = 1;
+    double dt = 0, eps2 = 0;
+    bool fp32 = false, valid = false;
+    double *x = nullptr, *v = nullptr, *a = nullptr;  // 3n each: the working state (x_T after the forward)
+    double *m = nullptr;                              // n
+    double *lam = nullptr;                            // 7n: lambda_x (3n), lambda_v (3n), lambda_m (n)
+    double *ck = nullptr;                             // nck x 9n: (x, v, a) at steps 0, K, 2K, ...
+    double *seg = nullptr;                            // K x 3n: positions of one replayed segment
+    double *rv = nullptr, *ra = nullptr;              // 3n each: velocities and accelerations of the replay
+    double *part = nullptr;                           // nsplit x 4n: FP32 pair sums per source split
+    float4 *hi = nullptr, *lo = nullptr, *w = nullptr;  // n each: FP32 positions + mass, remainders, weights
+    // Optional stage marks around each pair-kernel launch: (prep start, pair start, pair end).
+    cudaError_t (*mark)(void *) = nullptr;
+    void *mark_arg = nullptr;
+};
+// Carves the tape for n bodies, nsteps steps and checkpoints every `every` steps (grow-only).
+cudaError_t adj_reserve(AdjTape &t, int64_t n, int64_t nsteps, int64_t every, double dt, double eps, bool fp32,
+                        int num_sms);
+void adj_free(AdjTape &t);
+// nsteps KDK steps from (t.x, t.v) with masses t.m, saving checkpoints; leaves x_T, v_T in t.x, t.v.
+cudaError_t adj_forward(const Launch &L, AdjTape &t);
+// From t.lam = (dL/dx_T, dL/dv_T, 0) to (dL/dx_0, dL/dv_0, dL/dm) in place.
+cudaError_t adj_backward(const Launch &L, AdjTape &t);
+
 // ---- walk.cu (FP32 walks, FMA contraction on) ----
 cudaError_t walk_plain(const Launch &L, const TreeBufs &b, int64_t nstars_cap, float eps2,
                        double *ax, double *ay, double *az, bool targets = false);

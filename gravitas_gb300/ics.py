@@ -15,6 +15,8 @@ arrays, so parity never depends on the generator.
   merger(n)             two galaxy(n/2) on a parabolic orbit
   far_cluster()         the clumpy cluster plus probe of bh_test.go:294-307
   forest(nsys)          independent Plummer or galaxy systems of log-uniform sizes, one state
+  adjoint_problem(n)    Plummer sphere with lognormal masses and rotated, noisy target positions
+                        (the differentiable workload)
 """
 from __future__ import annotations
 
@@ -335,3 +337,19 @@ def forest(nsys: int = 64, seed: int = 0, nmin: int = 2048, nmax: int = 65536, s
         offsets.append(offsets[-1] + len(s["px"]))
     out = {k: np.concatenate([p[k] for p in parts]) for k in parts[0]}
     return out, np.array(offsets, np.int64)
+
+
+def adjoint_problem(n: int, seed: int = 0, sigma: float = 0.3, angle_deg: float = 30.0, noise: float = 0.01):
+    """A Plummer sphere (positions and velocities as plummer(n, seed), in FP64) with masses
+    lognormal(0, sigma) normalised to a total of 1, and targets = initial positions rotated by
+    angle_deg about z plus N(0, noise^2) per coordinate. Returns (state, targets n x 3)."""
+    s = plummer(n, seed=seed, float32=False)
+    rng = np.random.default_rng(seed + 7919)
+    m = np.exp(rng.normal(0.0, sigma, n))
+    s["mass"] = m / m.sum()
+    t = np.radians(angle_deg)
+    c, si = np.cos(t), np.sin(t)
+    x0 = np.stack([s["px"], s["py"], s["pz"]], 1)
+    rot = np.array([[c, -si, 0.0], [si, c, 0.0], [0.0, 0.0, 1.0]])
+    targets = x0 @ rot.T + rng.normal(0.0, noise, (n, 3))
+    return s, targets

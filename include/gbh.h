@@ -234,6 +234,39 @@ int gbh_forest_upload(gbh_ctx *ctx, int32_t nsys, const int64_t *offsets, const 
    (links inside are table indices; a system's root is node_range[2s]). Either may be NULL. */
 int gbh_forest_layout(gbh_ctx *ctx, int32_t nsys, int64_t *star_range, int64_t *node_range);
 
+/* ---- Adjoint pair: gradient of a loss on the final phase-space coordinates. ---- */
+
+/*
+ * No counterpart in the reference (it has no differentiable path). Differentiates N KDK steps
+ * (the step of gbh_step_kdk, sim.go:302-343) with the softened O(N^2) direct-sum force
+ * (direct.go:27-47), every body a star: the force whose gradient finite differences can check,
+ * because the tree force jumps where a node's opening test or a star's cell changes.
+ */
+enum { GBH_ADJ_FP32 = 0, GBH_ADJ_FP64 = 1 };
+typedef struct {
+    double dt;         /* step length */
+    double softening;  /* Plummer epsilon; must be > 0 */
+    int64_t nsteps;    /* >= 1 */
+    int64_t every;     /* checkpoint interval K >= 1: (x, v, a) saved every K steps */
+    int32_t precision; /* GBH_ADJ_FP64: pair sums bit-identical to the FP64 checker;
+                          GBH_ADJ_FP32: FP32 pairs, double-float separations, compensated sums */
+    int32_t reserved[3];
+} gbh_adjoint_params;
+
+/* Forward half: runs the steps from (x0, v0) with masses m, keeping checkpoints on the
+   device, and returns the final positions and velocities (any out pointer may be NULL).
+   The tape stays in the context until the next gbh_fwd_save or gbh_destroy. */
+int gbh_fwd_save(gbh_ctx *ctx, const gbh_adjoint_params *ap, int64_t n, const double *px,
+                 const double *py, const double *pz, const double *vx, const double *vy,
+                 const double *vz, const double *mass, double *out_px, double *out_py,
+                 double *out_pz, double *out_vx, double *out_vy, double *out_vz);
+/* Backward half: given dL/dx_T and dL/dv_T (NULL arrays are zero), returns dL/dx_0, dL/dv_0
+   and dL/dm (any out pointer may be NULL) by replaying each checkpoint segment. It may be
+   called again on the same tape with another loss. GBH_ERR_STATE without a tape. */
+int gbh_bwd(gbh_ctx *ctx, const double *gx, const double *gy, const double *gz, const double *gvx,
+            const double *gvy, const double *gvz, double *dx, double *dy, double *dz, double *dvx,
+            double *dvy, double *dvz, double *dm);
+
 /* ---- Inspection of the last tree (b.nodes / b.order / b.keys in bh.Solver). ---- */
 
 /* Stars and nodes of the last built tree. */

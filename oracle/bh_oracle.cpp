@@ -963,6 +963,157 @@ void orc_block_kdk(int64_t n, double *px, double *py, double *pz, double *vx, do
     if (evals) *evals = ne;
 }
 
+namespace {
+
+// Direct-sum accelerations of all bodies (all stars), j in index order (direct.go:27-47).
+void direct_all(int64_t n, const double *px, const double *py, const double *pz, const double *m, double eps2,
+                int workers, double *ax, double *ay, double *az) {
+    parallel_for(n, 64, workers, [&](int64_t lo, int64_t hi) {
+        for (int64_t i = lo; i < hi; ++i) {
+            double xi = px[i], yi = py[i], zi = pz[i], fx = 0, fy = 0, fz = 0;
+            for (int64_t j = 0; j < n; ++j) {
+                if (j == i) continue;
+                double dx = px[j] - xi, dy = py[j] - yi, dz = pz[j] - zi;
+                double re2 = dx * dx + dy * dy + dz * dz + eps2;
+                double f = m[j] / (re2 * std::sqrt(re2));
+                fx += f * dx;
+                fy += f * dy;
+                fz += f * dz;
+            }
+            ax[i] = fx;
+            ay[i] = fy;
+            az[i] = fz;
+        }
+    });
+}
+
+// Vector-Jacobian product of the direct-sum accelerations a(x; m) with weights w:
+//   g_x[i] = sum_j (da_j/dx_i)^T w_j = sum_{j != i} K(d) (m_i w_j - m_j w_i),
+//   g_m[i] = sum_j (da_j/dm_i) . w_j = -sum_{j != i} (w_j . d) / s^3,
+// with d = x_j - x_i, s^2 = |d|^2 + eps^2, K(d) = I / s^3 - 3 d d^T / s^5. Adds c * g to (gx, gm).
+void vjp_all(int64_t n, const double *px, const double *py, const double *pz, const double *m, const double *wx,
+             const double *wy, const double *wz, double eps2, double c, int workers, double *gx, double *gy,
+             double *gz, double *gm) {
+    parallel_for(n, 64, workers, [&](int64_t lo, int64_t hi) {
+        for (int64_t i = lo; i < hi; ++i) {
+            double xi = px[i], yi = py[i], zi = pz[i], mi = m[i];
+            double wix = wx[i], wiy = wy[i], wiz = wz[i];
+            double sx = 0, sy = 0, sz = 0, sm = 0;
+            for (int64_t j = 0; j < n; ++j) {
+                if (j == i) continue;
+                double dx = px[j] - xi, dy = py[j] - yi, dz = pz[j] - zi;
+                double s2 = dx * dx + dy * dy + dz * dz + eps2;
+                double inv3 = 1 / (s2 * std::sqrt(s2));
+                double inv5 = inv3 / s2;
+                double ux = mi * wx[j] - m[j] * wix, uy = mi * wy[j] - m[j] * wiy, uz = mi * wz[j] - m[j] * wiz;
+                double du = dx * ux + dy * uy + dz * uz;
+                sx += ux * inv3 - 3 * dx * du * inv5;
+                sy += uy * inv3 - 3 * dy * du * inv5;
+                sz += uz * inv3 - 3 * dz * du * inv5;
+                sm -= (wx[j] * dx + wy[j] * dy + wz[j] * dz) * inv3;
+            }
+            gx[i] += c * sx;
+            gy[i] += c * sy;
+            gz[i] += c * sz;
+            gm[i] += c * sm;
+        }
+    });
+}
+
+}  // namespace
+
+void orc_kdk_direct(int64_t n, double *px, double *py, double *pz, double *vx, double *vy, double *vz,
+                    const double *mass, double eps, double dt, int64_t nsteps, int workers) {
+    std::vector<double> ax(n), ay(n), az(n);
+    double eps2 = eps * eps, h = 0.5 * dt;
+    direct_all(n, px, py, pz, mass, eps2, workers, ax.data(), ay.data(), az.data());
+    for (int64_t s = 0; s < nsteps; ++s) {
+        for (int64_t i = 0; i < n; ++i) {
+            vx[i] += h * ax[i];
+            vy[i] += h * ay[i];
+            vz[i] += h * az[i];
+            px[i] += dt * vx[i];
+            py[i] += dt * vy[i];
+            pz[i] += dt * vz[i];
+        }
+        direct_all(n, px, py, pz, mass, eps2, workers, ax.data(), ay.data(), az.data());
+        for (int64_t i = 0; i < n; ++i) {
+            vx[i] += h * ax[i];
+            vy[i] += h * ay[i];
+            vz[i] += h * az[i];
+        }
+    }
+}
+
+void orc_adjoint_direct(int64_t n, const double *px, const double *py, const double *pz, const double *vx,
+                        const double *vy, const double *vz, const double *mass, double eps, double dt, int64_t nsteps,
+                        int64_t every, const double *gx, const double *gy, const double *gz, const double *gvx,
+                        const double *gvy, const double *gvz, double *dx, double *dy, double *dz, double *dvx,
+                        double *dvy, double *dvz, double *dm, int workers) {
+    const double eps2 = eps * eps, h = 0.5 * dt;
+    if (every < 1) every = 1;
+    // forward: checkpoints of (x, v) at steps 0, every, 2 every, ...
+    std::vector<std::vector<double>> ck;
+    std::vector<double> x(px, px + n), y(py, py + n), z(pz, pz + n), u(vx, vx + n), v(vy, vy + n), w(vz, vz + n);
+    for (int64_t s0 = 0; s0 < nsteps; s0 += every) {
+        std::vector<double> c(6 * n);
+        for (int64_t i = 0; i < n; ++i) {
+            c[i] = x[i];
+            c[n + i] = y[i];
+            c[2 * n + i] = z[i];
+            c[3 * n + i] = u[i];
+            c[4 * n + i] = v[i];
+            c[5 * n + i] = w[i];
+        }
+        ck.push_back(std::move(c));
+        int64_t k = std::min(every, nsteps - s0);
+        orc_kdk_direct(n, x.data(), y.data(), z.data(), u.data(), v.data(), w.data(), mass, eps, dt, k, workers);
+    }
+    // backward
+    std::vector<double> lx(gx, gx + n), ly(gy, gy + n), lz(gz, gz + n), lu(gvx, gvx + n), lv(gvy, gvy + n),
+        lw(gvz, gvz + n), lm(n, 0.0);
+    // closing kick of the last step, at the final positions
+    vjp_all(n, x.data(), y.data(), z.data(), mass, lu.data(), lv.data(), lw.data(), eps2, h, workers, lx.data(),
+            ly.data(), lz.data(), lm.data());
+    for (int64_t c = int64_t(ck.size()) - 1; c >= 0; --c) {
+        int64_t s0 = c * every, k = std::min(every, nsteps - s0);
+        // replay the segment, keeping the positions at its step starts
+        std::vector<std::vector<double>> pos(k);
+        std::vector<double> sx(ck[c].begin(), ck[c].begin() + n), sy(ck[c].begin() + n, ck[c].begin() + 2 * n),
+            sz(ck[c].begin() + 2 * n, ck[c].begin() + 3 * n), su(ck[c].begin() + 3 * n, ck[c].begin() + 4 * n),
+            sv(ck[c].begin() + 4 * n, ck[c].begin() + 5 * n), sw(ck[c].begin() + 5 * n, ck[c].end());
+        for (int64_t q = 0; q < k; ++q) {
+            pos[q].resize(3 * n);
+            std::copy(sx.begin(), sx.end(), pos[q].begin());
+            std::copy(sy.begin(), sy.end(), pos[q].begin() + n);
+            std::copy(sz.begin(), sz.end(), pos[q].begin() + 2 * n);
+            if (q + 1 < k)
+                orc_kdk_direct(n, sx.data(), sy.data(), sz.data(), su.data(), sv.data(), sw.data(), mass, eps, dt, 1,
+                               workers);
+        }
+        for (int64_t q = k - 1; q >= 0; --q) {
+            int64_t s = s0 + q;
+            for (int64_t i = 0; i < n; ++i) {  // drift x_{s+1} = x_s + dt v_half
+                lu[i] += dt * lx[i];
+                lv[i] += dt * ly[i];
+                lw[i] += dt * lz[i];
+            }
+            // opening kick of step s and closing kick of step s-1 act at x_s with the same weights
+            double cf = s > 0 ? dt : h;
+            const double *P = pos[q].data();
+            vjp_all(n, P, P + n, P + 2 * n, mass, lu.data(), lv.data(), lw.data(), eps2, cf, workers, lx.data(),
+                    ly.data(), lz.data(), lm.data());
+        }
+    }
+    std::copy(lx.begin(), lx.end(), dx);
+    std::copy(ly.begin(), ly.end(), dy);
+    std::copy(lz.begin(), lz.end(), dz);
+    std::copy(lu.begin(), lu.end(), dvx);
+    std::copy(lv.begin(), lv.end(), dvy);
+    std::copy(lw.begin(), lw.end(), dvz);
+    std::copy(lm.begin(), lm.end(), dm);
+}
+
 double orc_potential_exact(int64_t n, const double *px, const double *py, const double *pz,
                            const double *mass, const uint8_t *kind, double eps, double c, int dm_off,
                            int workers) {

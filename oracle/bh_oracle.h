@@ -137,6 +137,25 @@ void orc_block_kdk(int64_t n, double *px, double *py, double *pz, double *vx, do
                    double eps, double theta, int leaf_size, int monopole_only, int dark_matter_off,
                    int acc_valid, int64_t nsteps, int workers, int64_t *substeps, int64_t *evals);
 
+/*
+ * Adjoint of the KDK leapfrog (sim.go:302-343) with the softened direct-sum force
+ * (direct.go:27-47, all bodies stars): the gradient of a loss with respect to the initial
+ * positions, velocities and masses, given its gradient (gx.., gv..) with respect to the final
+ * positions and velocities after nsteps steps of dt from the state (x0, v0). FP64. The forward
+ * trajectory is replayed from checkpoints every `every` steps. No counterpart in the
+ * reference: the checker of gbh_adjoint_*.
+ */
+void orc_adjoint_direct(int64_t n, const double *px, const double *py, const double *pz,
+                        const double *vx, const double *vy, const double *vz, const double *mass,
+                        double eps, double dt, int64_t nsteps, int64_t every, const double *gx,
+                        const double *gy, const double *gz, const double *gvx, const double *gvy,
+                        const double *gvz, double *dx, double *dy, double *dz, double *dvx,
+                        double *dvy, double *dvz, double *dm, int workers);
+/* The forward of orc_adjoint_direct: nsteps KDK steps with the direct-sum force, in place. */
+void orc_kdk_direct(int64_t n, double *px, double *py, double *pz, double *vx, double *vy,
+                    double *vz, const double *mass, double eps, double dt, int64_t nsteps,
+                    int workers);
+
 /* diag.go:44-64 exact pair potential (no holes: plain softened Newtonian). */
 double orc_potential_exact(int64_t n, const double *px, const double *py, const double *pz,
                            const double *mass, const uint8_t *kind, double eps, double c,

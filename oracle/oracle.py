@@ -66,6 +66,8 @@ def lib():
             "orc_direct_targets": (None, [_I64, _P, _P, _P, _P, _P, _D, _INT, _P, _I64, _INT, _P, _P, _P]),
             "orc_kdk": (None, [_I64] + [_P] * 12 + [_D, _D, _D, _INT, _INT, _INT, _INT, _I64, _INT]),
             "orc_potential_exact": (_D, [_I64, _P, _P, _P, _P, _P, _D, _D, _INT, _INT]),
+            "orc_adjoint_direct": (None, [_I64] + [_P] * 7 + [_D, _D, _I64, _I64] + [_P] * 13 + [_INT]),
+            "orc_kdk_direct": (None, [_I64] + [_P] * 7 + [_D, _D, _I64, _INT]),
             "orc_block_kdk": (None, [_I64] + [_P] * 12 + [_D, _D, _INT, _D, _D, _INT, _INT, _INT, _INT, _I64, _INT,
                                                          _P, _P]),
         }
@@ -234,3 +236,26 @@ def block_kdk(state: dict, dt, eta, levels, eps, theta, leaf, nsteps, monopole_o
                         _ptr(kind), _ptr(alive), dt, eta, levels, eps, theta, leaf, int(monopole_only), int(dm_off),
                         int(acc_valid), nsteps, workers, _ptr(a), _ptr(b))
     return int(a[0]), int(b[0])
+
+
+def kdk_direct(state: dict, dt, eps, nsteps, workers=0):
+    """nsteps KDK steps with the FP64 direct-sum force, in place on px..vz (mass read)."""
+    s = state
+    n = len(s["px"])
+    lib().orc_kdk_direct(n, *[_ptr(s[k]) for k in ("px", "py", "pz", "vx", "vy", "vz", "mass")], eps, dt, nsteps,
+                         workers)
+    return s
+
+
+def adjoint_direct(state: dict, dt, eps, nsteps, every, gx, gv, workers=0):
+    """Gradient w.r.t. initial (x, v, m) of a loss whose gradient w.r.t. the final positions and
+    velocities is (gx, gv) (each n x 3), for the KDK trajectory with the direct-sum force."""
+    s = state
+    n = len(s["px"])
+    gx = np.ascontiguousarray(np.asarray(gx, np.float64).T)
+    gv = np.ascontiguousarray(np.asarray(gv, np.float64).T)
+    out = np.zeros((7, n))
+    lib().orc_adjoint_direct(n, *[_ptr(_f64(s[k])) for k in ("px", "py", "pz", "vx", "vy", "vz", "mass")], eps, dt,
+                             nsteps, every, _ptr(gx[0]), _ptr(gx[1]), _ptr(gx[2]), _ptr(gv[0]), _ptr(gv[1]),
+                             _ptr(gv[2]), *[_ptr(out[k]) for k in range(7)], workers)
+    return out[0:3].T.copy(), out[3:6].T.copy(), out[6].copy()

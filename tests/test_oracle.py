@@ -256,3 +256,49 @@ def test_block_steps_rungs_follow_accelerations():
     events, walked = O.block_kdk(b, dt=2e-2, eta=0.025, levels=6, eps=0.01, theta=0.5, leaf=8, nsteps=2, workers=1)
     assert 2 < events <= 2 * 32
     assert 2 * 2048 < walked < 2 * 32 * 2048
+
+
+# ---- adjoint of the KDK leapfrog with the direct-sum force (no reference counterpart; pinned by
+# central finite differences in FP64, the pattern of pair_test.go:8 and bh_test.go:332-351) ----
+
+def _adjoint_case(n=48, seed=3):
+    s, targets = ics.adjoint_problem(n, seed=seed)
+    return s, targets
+
+
+def _loss_fd(s, targets, key, idx, h, dt, eps, nsteps):
+    vals = []
+    for sign in (1.0, -1.0):
+        st = {k: s[k].copy() for k in ("px", "py", "pz", "vx", "vy", "vz", "mass")}
+        st[key][idx] += sign * h
+        O.kdk_direct(st, dt, eps, nsteps, workers=1)
+        x = np.stack([st["px"], st["py"], st["pz"]], 1)
+        vals.append(np.sum((x - targets) ** 2) / len(x))
+    return (vals[0] - vals[1]) / (2 * h)
+
+
+def test_adjoint_oracle_matches_central_differences():
+    s, targets = _adjoint_case()
+    dt, eps, nsteps = 1e-2, 0.05, 40
+    st = {k: s[k].copy() for k in ("px", "py", "pz", "vx", "vy", "vz", "mass")}
+    O.kdk_direct(st, dt, eps, nsteps, workers=1)
+    x = np.stack([st["px"], st["py"], st["pz"]], 1)
+    gx = 2 * (x - targets) / len(x)
+    dx, dv, dm = O.adjoint_direct(s, dt, eps, nsteps, 7, gx, np.zeros_like(gx), workers=1)
+    rng = np.random.default_rng(0)
+    grads = {"px": dx[:, 0], "py": dx[:, 1], "vx": dv[:, 0], "vz": dv[:, 2], "mass": dm}
+    for key, g in grads.items():
+        for idx in rng.choice(len(g), 4, replace=False):
+            fd = _loss_fd(s, targets, key, idx, 1e-4, dt, eps, nsteps)
+            assert abs(g[idx] - fd) <= 1e-6 * max(abs(fd), 1e-3 * np.abs(g).max()), (key, idx, g[idx], fd)
+
+
+def test_adjoint_oracle_checkpoint_interval_does_not_change_bits():
+    s, targets = _adjoint_case(n=40, seed=4)
+    gx = np.random.default_rng(1).normal(size=(40, 3))
+    gv = np.random.default_rng(2).normal(size=(40, 3))
+    ref = O.adjoint_direct(s, 5e-3, 0.02, 23, 1, gx, gv, workers=1)
+    for every in (4, 7, 23, 100):
+        got = O.adjoint_direct(s, 5e-3, 0.02, 23, every, gx, gv, workers=1)
+        for a, b in zip(ref, got):
+            assert np.array_equal(a, b), every
