@@ -429,6 +429,94 @@ def run_adjoint(args):
     return 0
 
 
+def run_forest(args):
+    """The batched workload: 64 independent Plummer or disk+bulge+halo systems of log-uniform
+    N in [2048, 65536] and scale radius in [0.5, 2], one state (gbh_forest_upload). The autotuner
+    (gbh_autotune) sweeps theta {0.4, 0.5, 0.7} x leaf {4, 8, 16, 32} x group {32, 64} for the
+    fastest force evaluation with RMS error <= 2e-3; then K graph-captured KDK steps run with the
+    chosen parameters (one build and one walk launch per step for all systems), and every system
+    is checked against its own FP64 direct sum on sampled stars. One line of JSON."""
+    import torch
+
+    from gravitas_gb300 import abi, ics
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    P = abi.ptr
+    s, off = ics.forest(nsys=64, seed=0)
+    n, nsys = int(off[-1]), len(off) - 1
+    ctx = abi.Context(local)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{local}")
+
+    def upload():
+        ctx.forest_upload(off, s["px"], s["py"], s["pz"], s["vx"], s["vy"], s["vz"], s["mass"], s["kind"],
+                          s["alive"])
+
+    upload()
+    base = abi.make_params(0.5, EPS, 8, False, False, "mixed")
+    t0 = time.perf_counter()
+    best, table = ctx.autotune(base, rms_bound=2e-3, sample=2048, reps=3)
+    tune_s = time.perf_counter() - t0
+    default = [e for e in table if (e["theta"], e["leaf_size"], e["group_size"]) == (0.5, 8, 64)][0]
+    upload()
+    for _ in range(args.warmup):
+        ctx.call("gbh_state_step", best, DT, 1)
+    torch.cuda.synchronize()
+    tot = walk_ms = build_ms = 0.0
+    launches = 0
+    with Clocks(local) as clk:
+        for _ in range(args.steps):
+            flush.fill_(1)
+            torch.cuda.synchronize()
+            ctx.call("gbh_state_step", best, DT, 1)
+            t = ctx.timings()
+            tot += t["total_ms"]
+            walk_ms += t["walk_ms"]
+            build_ms += t["build_ms"]
+            launches += t["launches"]
+    # per-system check of the stepped state's forces against each system's own FP64 direct sum
+    ctx.call("gbh_state_accelerations", best)
+    st = {k: np.zeros(n) for k in FIELDS}
+    ctx.call("gbh_state_download", *[P(st[k]) for k in FIELDS])
+    a = np.stack([st["ax"], st["ay"], st["az"]], 1)
+    rms, p99 = [], []
+    fp64 = abi.make_params(0, EPS, 0, False, False, "fp64")
+    for q in range(nsys):
+        lo, hi = int(off[q]), int(off[q + 1])
+        tg = np.arange(0, hi - lo, max(1, (hi - lo) // 256), dtype=np.int64)
+        want = np.zeros((3, len(tg)))
+        sub = {k: np.ascontiguousarray(st[k][lo:hi]) for k in ("px", "py", "pz")}
+        m = np.ascontiguousarray(s["mass"][lo:hi])
+        kd = np.ascontiguousarray(s["kind"][lo:hi])
+        ctx.call("gbh_direct_accelerations", fp64, hi - lo, P(sub["px"]), P(sub["py"]), P(sub["pz"]), P(m), P(kd),
+                 P(tg), len(tg), P(want[0]), P(want[1]), P(want[2]))
+        e = np.linalg.norm(a[lo:hi][tg] - want.T, axis=1) / np.linalg.norm(want.T, axis=1)
+        rms.append(float(np.sqrt(np.mean(e ** 2))))
+        p99.append(float(np.percentile(e, 99)))
+    value = n * args.steps / (tot * 1e-3)
+    line = {
+        "metric": f"forest particle-steps/s: {nsys} systems, N={n}, autotuned at RMS force err <= 2e-3",
+        "value": value, "unit": "particle-steps/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": tot / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 walk, f64 state", "data": "synthetic",
+        "config": {"workload": f"forest of {nsys} Plummer or disk+bulge+halo systems, N_i log-uniform in "
+                               f"[2048, 65536], scale U[0.5, 2], eps={EPS}, dt={DT}, global KDK steps",
+                   "l2": "flushed (256 MiB write) between timed steps"},
+        "chosen": {"theta": best.theta, "leaf_size": best.leaf_size, "group_size": best.group_size},
+        "autotune": {"seconds": tune_s, "candidates": len(table),
+                     "chosen_force_ms": min(e["ms"] for e in table if e["meets"]) if any(e["meets"] for e in table)
+                     else None, "default_force_ms": default["ms"], "default_rms_err": default["rms_err"],
+                     "table": [{k: (round(v, 6) if isinstance(v, float) else v) for k, v in e.items()} for e in table]},
+        "walk_ms": walk_ms / args.steps, "build_ms": build_ms / args.steps, "gpu_launches": launches,
+        "launches_per_step": launches / args.steps,
+        "force_error_per_system": {"max_rms": max(rms), "median_rms": float(np.median(rms)), "max_p99": max(p99)},
+        "clocks": clk.summary(),
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
@@ -439,12 +527,15 @@ def main():
     ap.add_argument("--leaf", type=int, default=LEAF)
     ap.add_argument("--profile", choices=["mixed", "plain", "fp64"], default=None,
                     help="run only two force evaluations with this walk (for ncu captures)")
-    ap.add_argument("--workload", choices=["merger", "adjoint"], default="merger",
-                    help="adjoint: the differentiable workload (gbh_fwd_save / gbh_bwd), its own JSON line")
+    ap.add_argument("--workload", choices=["merger", "adjoint", "forest"], default="merger",
+                    help="adjoint: the differentiable workload (gbh_fwd_save / gbh_bwd); forest: 64 systems in "
+                         "one state with the autotuner; each prints its own JSON line")
     ap.add_argument("--fd-coords", type=int, default=16, help="adjoint: coordinates checked by central differences")
     args = ap.parse_args()
     if args.workload == "adjoint":
         return run_adjoint(args)
+    if args.workload == "forest":
+        return run_forest(args)
     if args.profile:
         return run_profile(args)
     if args.warmup < 3 and args.impl == "ours":

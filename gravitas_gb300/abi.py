@@ -31,7 +31,8 @@ class GbhError(RuntimeError):
 
 class Params(ctypes.Structure):
     _fields_ = [("theta", ctypes.c_double), ("softening", ctypes.c_double), ("leaf_size", ctypes.c_int32),
-                ("monopole_only", ctypes.c_int32), ("dark_matter_off", ctypes.c_int32), ("walk", ctypes.c_int32)]
+                ("monopole_only", ctypes.c_int32), ("dark_matter_off", ctypes.c_int32), ("walk", ctypes.c_int32),
+                ("group_size", ctypes.c_int32), ("reserved", ctypes.c_int32)]
 
 
 CFG_NO_GRAPHS = 1
@@ -76,6 +77,16 @@ class AdjointParams(ctypes.Structure):
 ADJ_FP32 = 0
 ADJ_FP64 = 1
 
+
+class TuneEntry(ctypes.Structure):
+    _fields_ = [("theta", ctypes.c_double), ("leaf_size", ctypes.c_int32), ("group_size", ctypes.c_int32),
+                ("ms", ctypes.c_double), ("build_ms", ctypes.c_double), ("walk_ms", ctypes.c_double),
+                ("rms_err", ctypes.c_double), ("p99_err", ctypes.c_double), ("meets", ctypes.c_int32),
+                ("reserved", ctypes.c_int32)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}
+
 NODE_DTYPE = np.dtype(
     [("x", "f8"), ("y", "f8"), ("z", "f8"), ("m", "f8"),
      ("qxx", "f8"), ("qyy", "f8"), ("qzz", "f8"), ("qxy", "f8"), ("qxz", "f8"), ("qyz", "f8"),
@@ -112,6 +123,7 @@ SIGNATURES = {
     "gbh_morton_order_noalloc": (ctypes.c_int, [_I32, _P, _I64] + [_P] * 8 + [ctypes.c_char_p, ctypes.c_int]),
     "gbh_fwd_save": (ctypes.c_int, [_P, ctypes.POINTER(AdjointParams), _I64] + [_P] * 13),
     "gbh_bwd": (ctypes.c_int, [_P] + [_P] * 13),
+    "gbh_autotune": (ctypes.c_int, [_P, _PP, _P, _I32, _P, _I32, _P, _I32, _D, _I32, _I32, _PP, _P, _I32, _P]),
 }
 
 _lib = None
@@ -160,10 +172,10 @@ def ptr(a):
 
 
 def make_params(theta=0.0, softening=0.0, leaf_size=0, monopole_only=False, dark_matter_off=False,
-                walk="mixed") -> Params:
+                walk="mixed", group_size=0) -> Params:
     w = WALKS[walk] if isinstance(walk, str) else int(walk)
     return Params(float(theta), float(softening), int(leaf_size), int(bool(monopole_only)),
-                  int(bool(dark_matter_off)), w)
+                  int(bool(dark_matter_off)), w, int(group_size), 0)
 
 
 class Context:
@@ -279,6 +291,25 @@ class Context:
         out = np.empty((7, n))
         self.call("gbh_bwd", *g, *[ptr(out[k]) for k in range(7)])
         return out[0:3].T.copy(), out[3:6].T.copy(), out[6].copy()
+
+    def autotune(self, params: Params, thetas=None, leaves=None, groups=None, rms_bound: float = 2e-3,
+                 sample: int = 1024, reps: int = 3, strict: bool = False):
+        """gbh_autotune on the resident state: (best Params, candidates as dicts). With strict,
+        a sweep in which no candidate meets rms_bound raises; otherwise the most accurate wins."""
+        th = None if thetas is None else np.ascontiguousarray(thetas, np.float64)
+        lv = None if leaves is None else np.ascontiguousarray(leaves, np.int32)
+        gr = None if groups is None else np.ascontiguousarray(groups, np.int32)
+        cap = 4096
+        table = (TuneEntry * cap)()
+        best = Params()
+        cnt = np.zeros(1, np.int32)
+        rc = self._L.gbh_autotune(self._h, ctypes.byref(params), ptr(th), 0 if th is None else len(th), ptr(lv),
+                                   0 if lv is None else len(lv), ptr(gr), 0 if gr is None else len(gr),
+                                   float(rms_bound), int(sample), int(reps), ctypes.byref(best),
+                                   ctypes.cast(table, ctypes.c_void_p), cap, ptr(cnt))
+        if rc != OK and (strict or rc != ERR_LIMIT):
+            raise GbhError(rc, self._L.gbh_last_error(self._h).decode())
+        return best, [table[k].as_dict() for k in range(min(int(cnt[0]), cap))]
 
     def probe_fp32_peak(self, ms: float = 50.0) -> float:
         out = np.zeros(1)

@@ -148,6 +148,8 @@ int check_params(gbh_ctx *ctx, const gbh_params *p) {
     if (!(p->softening >= 0)) return fail(ctx, GBH_ERR_ARG, "softening %g < 0", p->softening);
     if (p->leaf_size < 0 || p->leaf_size > 1 << 20) return fail(ctx, GBH_ERR_ARG, "leaf_size %d", p->leaf_size);
     if (p->walk < GBH_WALK_MIXED || p->walk > GBH_WALK_FP64) return fail(ctx, GBH_ERR_ARG, "walk %d", p->walk);
+    if (p->group_size != 0 && p->group_size != 32 && p->group_size != 64)
+        return fail(ctx, GBH_ERR_ARG, "group_size %d (0, 32 or 64)", p->group_size);
     return GBH_OK;
 }
 
@@ -212,6 +214,7 @@ int forces(gbh_ctx *ctx, const gbh_params *p, int64_t n, const double *px, const
     int leaf = leaf_of(p);
     forest = forest && ctx->nsys > 1;
     CK(gbh::tree_alloc(ctx->tb, n, leaf, forest ? ctx->nsys : 1));
+    ctx->tb.group = p->group_size == 32 ? 32 : 64;
     CK(stage_event(ctx));
     CK(gbh::tree_build(L, ctx->tb, n, px, py, pz, mass, kind, alive, ax, ay, az, theta, leaf, p->dark_matter_off,
                        p->walk == GBH_WALK_FP64, p->walk == GBH_WALK_PLAIN, forest ? ctx->sys_of : nullptr,
@@ -278,7 +281,19 @@ void free_graph(StepGraph &g) {
 
 bool same_params(const gbh_params &a, const gbh_params &b) {
     return a.theta == b.theta && a.softening == b.softening && a.leaf_size == b.leaf_size &&
-           a.monopole_only == b.monopole_only && a.dark_matter_off == b.dark_matter_off && a.walk == b.walk;
+           a.monopole_only == b.monopole_only && a.dark_matter_off == b.dark_matter_off && a.walk == b.walk &&
+           (a.group_size == 32) == (b.group_size == 32);
+}
+
+// out[q] = a[idx[q]] for the three arrays of a (n doubles apart in out).
+__global__ void k_gather3(int64_t cnt, const int64_t *__restrict__ idx, const double *__restrict__ ax,
+                          const double *__restrict__ ay, const double *__restrict__ az, double *out) {
+    int64_t q = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (q >= cnt) return;
+    int64_t i = idx[q];
+    out[q] = ax[i];
+    out[cnt + q] = ay[i];
+    out[2 * cnt + q] = az[i];
 }
 
 // Captures one resident step (kick + drift, forces, kick) into ctx->step_graph.
@@ -988,6 +1003,164 @@ int gbh_bwd(gbh_ctx *ctx, const double *gx, const double *gy, const double *gz, 
     for (int k = 0; k < 7; ++k)
         if (outs[k] && (rc = d2h(ctx, outs[k], t.lam + k * n, b))) return rc;
     return finish(ctx, false);
+}
+
+int gbh_autotune(gbh_ctx *ctx, const gbh_params *base, const double *thetas, int32_t nthetas, const int32_t *leaves,
+                 int32_t nleaves, const int32_t *groups, int32_t ngroups, double rms_bound, int32_t sample,
+                 int32_t reps, gbh_params *best, gbh_tune_entry *table, int32_t table_cap, int32_t *ntable) {
+    int rc = begin(ctx);
+    if (rc || (rc = check_params(ctx, base))) return rc;
+    if (!best) return fail(ctx, GBH_ERR_ARG, "best is NULL");
+    if (!ctx->have_state || ctx->n <= 0) return fail(ctx, GBH_ERR_STATE, "no resident state to tune on");
+    static const double kThetas[] = {0.4, 0.5, 0.7};
+    static const int32_t kLeaves[] = {4, 8, 16, 32};
+    static const int32_t kGroups[] = {64, 32};
+    if (!thetas || nthetas <= 0) thetas = kThetas, nthetas = 3;
+    if (!leaves || nleaves <= 0) leaves = kLeaves, nleaves = 4;
+    if (!groups || ngroups <= 0) groups = kGroups, ngroups = base->walk == GBH_WALK_MIXED ? 2 : 1;
+    if (base->walk != GBH_WALK_MIXED) ngroups = 1;  // only the mixed walk has groups
+    for (int32_t a = 0; a < nthetas; ++a)
+        if (!(thetas[a] > 0 && thetas[a] <= 1)) return fail(ctx, GBH_ERR_ARG, "theta %g outside (0, 1]", thetas[a]);
+    for (int32_t a = 0; a < nleaves; ++a)
+        if (leaves[a] < 1 || leaves[a] > 1 << 20) return fail(ctx, GBH_ERR_ARG, "leaf size %d", leaves[a]);
+    for (int32_t a = 0; a < ngroups; ++a)
+        if (groups[a] != 32 && groups[a] != 64) return fail(ctx, GBH_ERR_ARG, "group size %d (32 or 64)", groups[a]);
+    if (!(rms_bound > 0)) return fail(ctx, GBH_ERR_ARG, "rms_bound must be > 0");
+    if (sample <= 0) sample = 1024;
+    if (reps <= 0) reps = 3;
+    const int64_t n = ctx->n;
+    const bool forest = ctx->nsys > 1;
+    // sample targets: evenly spaced alive non-hole bodies (state indices)
+    std::vector<uint8_t> kind, alive;
+    if (ctx->state_has_kind) {
+        kind.resize(size_t(n));
+        CK(cudaMemcpy(kind.data(), ctx->kind, size_t(n), cudaMemcpyDeviceToHost));
+    }
+    if (ctx->state_has_alive) {
+        alive.resize(size_t(n));
+        CK(cudaMemcpy(alive.data(), ctx->alive, size_t(n), cudaMemcpyDeviceToHost));
+    }
+    std::vector<int64_t> elig;
+    for (int64_t i = 0; i < n; ++i)
+        if ((kind.empty() || kind[size_t(i)] != GBH_BLACK_HOLE) && (alive.empty() || alive[size_t(i)]))
+            elig.push_back(i);
+    if (elig.empty()) return fail(ctx, GBH_ERR_STATE, "no alive stars to tune on");
+    const int64_t ns = std::min<int64_t>(sample, int64_t(elig.size()));
+    std::vector<int64_t> idx(static_cast<size_t>(ns));
+    for (int64_t q = 0; q < ns; ++q) idx[size_t(q)] = elig[size_t(q * int64_t(elig.size()) / ns)];
+    // systems: the FP64 direct sum of each target runs over its own system only
+    std::vector<int64_t> off{0, n};
+    if (forest) {
+        off.resize(size_t(ctx->nsys) + 1);
+        CK(cudaMemcpy(off.data(), ctx->sys_off, sizeof(int64_t) * off.size(), cudaMemcpyDeviceToHost));
+    }
+    CK(grow(ctx->targets, ctx->targets_cap, 2 * ns));
+    CK(cudaFree(ctx->tout));
+    ctx->tout = nullptr;
+    CK(cudaMalloc(&ctx->tout, sizeof(double) * 3 * size_t(ctx->targets_cap)));
+    Launch L = launch_of(ctx);
+    const double eps2 = base->softening * base->softening;
+    std::vector<int64_t> rel(static_cast<size_t>(ns));
+    std::vector<double> ref(3 * static_cast<size_t>(ns)), got(3 * static_cast<size_t>(ns));
+    {
+        size_t s = 0, q0 = 0;
+        for (size_t q = 0; q < size_t(ns); ++q) {
+            while (idx[q] >= off[s + 1]) ++s;
+            rel[q] = idx[q] - off[s];
+        }
+        CK(cudaMemcpyAsync(ctx->targets, rel.data(), sizeof(int64_t) * size_t(ns), cudaMemcpyHostToDevice, ctx->stream));
+        double *tx = ctx->tout, *ty = tx + ns, *tz = ty + ns;
+        for (s = 0; q0 < size_t(ns); ++s) {
+            size_t q1 = q0;
+            while (q1 < size_t(ns) && idx[q1] < off[s + 1]) ++q1;
+            if (q1 > q0) {
+                int64_t o = off[s];
+                CK(gbh::direct_fp64(L, off[s + 1] - o, ctx->px + o, ctx->py + o, ctx->pz + o, ctx->mass + o,
+                                    ctx->state_has_kind ? ctx->kind + o : nullptr, eps2, base->dark_matter_off,
+                                    ctx->targets + q0, int64_t(q1 - q0), tx + q0, ty + q0, tz + q0));
+            }
+            q0 = q1;
+        }
+        CK(cudaMemcpyAsync(ref.data(), ctx->tout, sizeof(double) * 3 * size_t(ns), cudaMemcpyDeviceToHost,
+                           ctx->stream));
+        CK(cudaMemcpyAsync(ctx->targets + ns, idx.data(), sizeof(int64_t) * size_t(ns), cudaMemcpyHostToDevice,
+                           ctx->stream));
+        CK(cudaStreamSynchronize(ctx->stream));
+    }
+    const uint8_t *kd = ctx->state_has_kind ? ctx->kind : nullptr, *al = ctx->state_has_alive ? ctx->alive : nullptr;
+    int32_t count = 0, best_k = -1, best_any = -1;
+    double best_ms = 0, best_err = 0;
+    gbh_tune_entry cur_best = {}, any_best = {};
+    for (int32_t a = 0; a < nthetas; ++a)
+        for (int32_t b = 0; b < nleaves; ++b)
+            for (int32_t c = 0; c < ngroups; ++c) {
+                gbh_params p = *base;
+                p.theta = thetas[a];
+                p.leaf_size = leaves[b];
+                p.group_size = groups[c];
+                gbh_tune_entry e = {};
+                e.theta = p.theta;
+                e.leaf_size = p.leaf_size;
+                e.group_size = base->walk == GBH_WALK_MIXED ? (p.group_size == 32 ? 32 : 64) : 0;
+                std::vector<double> tot, bld, wlk;
+                for (int32_t r = -1; r < reps; ++r) {  // r = -1: untimed warm-up (allocation)
+                    ctx->evused = 0;
+                    rc = forces(ctx, &p, n, ctx->px, ctx->py, ctx->pz, ctx->mass, kd, al, ctx->ax, ctx->ay, ctx->az,
+                                theta_of(&p), forest);
+                    if (rc) return rc;
+                    CK(cudaStreamSynchronize(ctx->stream));
+                    if (r < 0) continue;
+                    float b0 = 0, w0 = 0;
+                    CK(cudaEventElapsedTime(&b0, ctx->evpool[0], ctx->evpool[1]));
+                    CK(cudaEventElapsedTime(&w0, ctx->evpool[1], ctx->evpool[2]));
+                    bld.push_back(b0);
+                    wlk.push_back(w0);
+                    tot.push_back(double(b0) + double(w0));
+                }
+                auto median = [](std::vector<double> v) {
+                    std::sort(v.begin(), v.end());
+                    return v[v.size() / 2];
+                };
+                e.ms = median(tot);
+                e.build_ms = median(bld);
+                e.walk_ms = median(wlk);
+                k_gather3<<<unsigned((ns + 255) / 256), 256, 0, ctx->stream>>>(ns, ctx->targets + ns, ctx->ax, ctx->ay,
+                                                                              ctx->az, ctx->tout);
+                ++ctx->launches;
+                CK(cudaGetLastError());
+                CK(cudaMemcpyAsync(got.data(), ctx->tout, sizeof(double) * 3 * size_t(ns), cudaMemcpyDeviceToHost,
+                                   ctx->stream));
+                CK(cudaStreamSynchronize(ctx->stream));
+                std::vector<double> rerr;
+                for (int64_t q = 0; q < ns; ++q) {
+                    double rx = ref[size_t(q)], ry = ref[size_t(ns + q)], rz = ref[size_t(2 * ns + q)];
+                    double dx = got[size_t(q)] - rx, dy = got[size_t(ns + q)] - ry, dz = got[size_t(2 * ns + q)] - rz;
+                    double nr = std::sqrt(rx * rx + ry * ry + rz * rz);
+                    if (nr > 0) rerr.push_back(std::sqrt(dx * dx + dy * dy + dz * dz) / nr);
+                }
+                double s2 = 0;
+                for (double x : rerr) s2 += x * x;
+                e.rms_err = rerr.empty() ? 0 : std::sqrt(s2 / double(rerr.size()));
+                std::sort(rerr.begin(), rerr.end());
+                e.p99_err = rerr.empty() ? 0 : rerr[std::min(rerr.size() - 1, size_t(0.99 * double(rerr.size())))];
+                e.meets = e.rms_err <= rms_bound;
+                if (e.meets && (best_k < 0 || e.ms < best_ms)) best_k = count, best_ms = e.ms, cur_best = e;
+                if (best_any < 0 || e.rms_err < best_err) best_any = count, best_err = e.rms_err, any_best = e;
+                if (table && count < table_cap) table[count] = e;
+                ++count;
+            }
+    ctx->acc_valid = false;  // the accelerations are those of the last candidate
+    const gbh_tune_entry &w = best_k >= 0 ? cur_best : any_best;
+    *best = *base;
+    best->theta = w.theta;
+    best->leaf_size = w.leaf_size;
+    best->group_size = w.group_size;
+    if (ntable) *ntable = count;
+    ctx->evused = 0;
+    CK(cudaEventRecord(ctx->ev[0], ctx->stream));
+    rc = finish(ctx, false);
+    if (rc) return rc;
+    return best_k >= 0 ? GBH_OK : fail(ctx, GBH_ERR_LIMIT, "no candidate meets rms %g (best %g)", rms_bound, best_err);
 }
 
 int gbh_last_timings(gbh_ctx *ctx, gbh_timings *t) {

@@ -73,6 +73,7 @@ struct TreeBufs {
     int64_t cap_n = 0;      // bodies
     int64_t cap_nodes = 0;  // nodes
     int64_t generation = 0; // incremented whenever the buffers are reallocated
+    int32_t group = 64;     // stars per mixed-walk group (32 or 64), set before tree_build
     // compaction / bbox
     uint32_t *flag = nullptr;     // star flags, then their exclusive scan
     double *bbox_part = nullptr;  // per-block partial min/max (6 per block)

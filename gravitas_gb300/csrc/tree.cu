@@ -1267,9 +1267,10 @@ __global__ __launch_bounds__(kThreads) void k_compact_keys_sys(int64_t n, const 
     order[pos] = int32_t(i);
 }
 
-// Roots (the pre-order index of a system's first star chain) and the 64-star groups of the
+// Roots (the pre-order index of a system's first star chain) and the gsize-star groups of the
 // mixed walk, which never straddle two systems.
-__global__ void k_sys_layout(int32_t nsys, const uint32_t *__restrict__ base, SysGeo *geo, DevInfo *info) {
+__global__ void k_sys_layout(int32_t nsys, int32_t gsize, const uint32_t *__restrict__ base, SysGeo *geo,
+                             DevInfo *info) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
     int32_t groups = 0;
     for (int32_t s = 0; s < nsys; ++s) {
@@ -1277,19 +1278,19 @@ __global__ void k_sys_layout(int32_t nsys, const uint32_t *__restrict__ base, Sy
         int32_t cnt = g.star_hi - g.star_lo;
         g.root = cnt > 0 ? int32_t(base[g.star_lo]) : -1;
         g.group_lo = groups;
-        g.ngroups = (cnt + 63) / 64;
+        g.ngroups = (cnt + gsize - 1) / gsize;
         groups += g.ngroups;
     }
     info->ngroups = uint32_t(groups);
 }
 
-__global__ void k_sys_groups(int32_t nsys, const SysGeo *__restrict__ geo, int4 *__restrict__ groups) {
+__global__ void k_sys_groups(int32_t nsys, int32_t gsize, const SysGeo *__restrict__ geo, int4 *__restrict__ groups) {
     int32_t s = int32_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (s >= nsys) return;
     const SysGeo &g = geo[s];
     for (int32_t q = 0; q < g.ngroups; ++q) {
-        int32_t start = g.star_lo + 64 * q;
-        int32_t cnt = g.star_hi - start < 64 ? g.star_hi - start : 64;
+        int32_t start = g.star_lo + gsize * q;
+        int32_t cnt = g.star_hi - start < gsize ? g.star_hi - start : gsize;
         groups[g.group_lo + q] = make_int4(start, cnt, g.root, 0);
     }
 }
@@ -1327,7 +1328,7 @@ static int64_t node_capacity(int64_t n, int leaf) { return n + 22 * (n / (leaf +
 cudaError_t tree_alloc(TreeBufs &b, int64_t n, int leaf, int32_t nsys) {
     int64_t need_nodes = node_capacity(n, leaf);
     if (nsys < 1) nsys = 1;
-    if (n <= b.cap_n && need_nodes <= b.cap_nodes && nsys <= b.cap_sys && n / 64 + nsys + 1 <= b.cap_groups) {
+    if (n <= b.cap_n && need_nodes <= b.cap_nodes && nsys <= b.cap_sys && n / 32 + nsys + 1 <= b.cap_groups) {
         b.nsys = nsys;
         return cudaSuccess;
     }
@@ -1366,7 +1367,7 @@ cudaError_t tree_alloc(TreeBufs &b, int64_t n, int leaf, int32_t nsys) {
     GBH_ALLOC(b.leaves, cn);
     GBH_ALLOC(b.targets, cn);
     const int32_t csys = nsys + nsys / 4 + 1;
-    const int64_t cgroups = cn / 64 + csys + 1;
+    const int64_t cgroups = cn / 32 + csys + 1;  // groups of 32 or 64 stars
     GBH_ALLOC(b.geo, csys);
     GBH_ALLOC(b.sid_sorted, cn);
     GBH_ALLOC(b.groups, cgroups);
@@ -1504,9 +1505,9 @@ cudaError_t tree_build(const Launch &L, TreeBufs &b, int64_t n, const double *px
                                          b.pre_ref, b.nodes, b.n_parent, b.n_info, b.n_arrive, sid, b.geo);
     GBH_LAUNCH_CHECK();
     if (forest) {
-        k_sys_layout<<<1, 32, 0, s>>>(b.nsys, base, b.geo, b.info);
+        k_sys_layout<<<1, 32, 0, s>>>(b.nsys, b.group == 32 ? 32 : 64, base, b.geo, b.info);
         GBH_LAUNCH_CHECK();
-        k_sys_groups<<<blocks_for(b.nsys, 128), 128, 0, s>>>(b.nsys, b.geo, b.groups);
+        k_sys_groups<<<blocks_for(b.nsys, 128), 128, 0, s>>>(b.nsys, b.group == 32 ? 32 : 64, b.geo, b.groups);
         GBH_LAUNCH_CHECK();
     }
     b.moments_exact = exact;

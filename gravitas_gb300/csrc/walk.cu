@@ -134,25 +134,28 @@ __global__ __launch_bounds__(kMixedThreads) void k_walk_mixed2(const DevInfo *in
                                                                const int32_t *__restrict__ order, float eps2,
                                                                double *ax, double *ay, double *az,
                                                                const int32_t *__restrict__ targets,
-                                                               const int4 *__restrict__ groups, DevInfo *err_info) {
+                                                               const int4 *__restrict__ groups, int pair,
+                                                               DevInfo *err_info) {
+    // pair: 64-star groups, lane l walks stars 2l and 2l + 1; else 32-star groups, one star per
+    // lane (the second FP32x2 slot then repeats the first and is not written)
     const int lane = threadIdx.x & 31;
     const int32_t ns = int32_t(info->nstars);  // the C-ABI caps n at 2^30
     const uint32_t nn = uint32_t(info->nnodes);
     const int32_t g = int32_t((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
     int32_t base, nt, root = 0;
-    if (groups) {  // a forest: group g = up to 64 stars of one system, walked from its root
+    if (groups) {  // a forest: group g = up to 64 (32) stars of one system, walked from its root
         if (uint32_t(g) >= info->ngroups) return;
         const int4 e = groups[g];
         base = e.x;
         nt = e.x + e.y;
         root = e.z;
     } else {
-        base = g * 64;
+        base = g * (pair ? 64 : 32);
         nt = targets ? int32_t(info->ntargets) : ns;
         if (base >= nt) return;  // uniform over the warp
     }
-    const int32_t t0 = base + 2 * lane, t1 = t0 + 1;
-    const bool v0 = t0 < nt, v1 = t1 < nt;
+    const int32_t t0 = base + (pair ? 2 * lane : lane), t1 = t0 + 1;
+    const bool v0 = t0 < nt, v1 = pair && t1 < nt;
     const int32_t first_k = targets ? targets[base] : base;
     const int32_t k0 = v0 ? (targets ? targets[t0] : t0) : first_k;
     const int32_t k1 = v1 ? (targets ? targets[t1] : t1) : first_k;
@@ -296,11 +299,12 @@ template <bool kQuad, bool kSoft>
 static cudaError_t launch_mixed(const Launch &L, const TreeBufs &b, int64_t nstars_cap, float eps2, double *ax,
                                 double *ay, double *az, bool targets) {
     const bool forest = b.nsys > 1;
-    int64_t groups = forest ? b.cap_groups : (nstars_cap + 63) / 64;
+    const int gsize = b.group == 32 ? 32 : 64;
+    int64_t groups = forest ? b.cap_groups : (nstars_cap + gsize - 1) / gsize;
     int64_t blocks = (groups + kMixedThreads / 32 - 1) / (kMixedThreads / 32);
     k_walk_mixed2<kQuad, kSoft><<<unsigned(blocks < 1 ? 1 : blocks), kMixedThreads, 0, L.stream>>>(
         b.info, b.mnodes, b.mrange, b.st_hi, b.st_lo, b.order, eps2, ax, ay, az, targets ? b.targets : nullptr,
-        forest ? b.groups : nullptr, b.info);
+        forest ? b.groups : nullptr, gsize == 64 ? 1 : 0, b.info);
     ++*L.count;
     return cudaGetLastError();
 }

@@ -47,7 +47,8 @@ enum { GBH_STAR = 0, GBH_BLACK_HOLE = 1, GBH_DARK_MATTER = 2, GBH_GAS = 3 };
 
 /* Tree walk variants. */
 enum {
-    /* Warp-cooperative walk: one warp per 32 Morton-consecutive stars, FP32
+    /* Warp-cooperative walk: one warp per group of 64 (or 32, see group_size)
+       Morton-consecutive stars, two per lane in packed FP32x2 arithmetic, FP32
        separations formed from hi + lo splits of the FP64 positions, compensated
        per-star accumulation. The default. */
     GBH_WALK_MIXED = 0,
@@ -68,6 +69,8 @@ typedef struct {
     int32_t monopole_only;   /* drop quadrupoles of accepted nodes (bh.go:82-83) */
     int32_t dark_matter_off; /* dark matter pulls nothing (Params.DarkMatterOff, sim.go:92-98) */
     int32_t walk;            /* GBH_WALK_* */
+    int32_t group_size;      /* stars per warp of GBH_WALK_MIXED: 64 (0 means 64) or 32 */
+    int32_t reserved;        /* zero */
 } gbh_params;
 
 enum {
@@ -266,6 +269,39 @@ int gbh_fwd_save(gbh_ctx *ctx, const gbh_adjoint_params *ap, int64_t n, const do
 int gbh_bwd(gbh_ctx *ctx, const double *gx, const double *gy, const double *gz, const double *gvx,
             const double *gvy, const double *gvz, double *dx, double *dy, double *dz, double *dvx,
             double *dvy, double *dvz, double *dm);
+
+/* ---- Autotuner. ---- */
+
+/* One candidate of gbh_autotune. */
+typedef struct {
+    double theta;
+    int32_t leaf_size;
+    int32_t group_size; /* 32 or 64 for GBH_WALK_MIXED, 0 for the other walks */
+    double ms;          /* median device time of one force evaluation (build + walk) */
+    double build_ms;    /* its tree build */
+    double walk_ms;     /* its walk */
+    double rms_err;     /* RMS of the per-body relative force error on the sample */
+    double p99_err;     /* 99th percentile of the same */
+    int32_t meets;      /* rms_err <= rms_bound */
+    int32_t reserved;
+} gbh_tune_entry;
+
+/*
+ * No counterpart in the reference (its internal/perf/calibrate.go only picks CPU or GPU).
+ * Sweeps theta x leaf size x group size on the resident state (gbh_state_upload or
+ * gbh_forest_upload) with the other fields of *base, and writes to *best the candidate with
+ * the shortest median force evaluation (reps timed runs, CUDA events) among those whose RMS
+ * relative force error, on `sample` evenly spaced alive stars against the FP64 direct sum
+ * over each star's own system, is at most rms_bound. NULL or empty lists take the defaults
+ * theta {0.4, 0.5, 0.7}, leaf {4, 8, 16, 32}, group {64, 32}; sample <= 0 means 1024 and
+ * reps <= 0 means 3. Every candidate is written to table (up to table_cap) and counted in
+ * *ntable. If none meets the bound, *best is the most accurate one and the call returns
+ * GBH_ERR_LIMIT. The resident accelerations are left stale (the next step recomputes them).
+ */
+int gbh_autotune(gbh_ctx *ctx, const gbh_params *base, const double *thetas, int32_t nthetas,
+                 const int32_t *leaves, int32_t nleaves, const int32_t *groups, int32_t ngroups,
+                 double rms_bound, int32_t sample, int32_t reps, gbh_params *best,
+                 gbh_tune_entry *table, int32_t table_cap, int32_t *ntable);
 
 /* ---- Inspection of the last tree (b.nodes / b.order / b.keys in bh.Solver). ---- */
 

@@ -49,7 +49,9 @@ def test_null_context_is_rejected():
 
 
 def test_params_layout_matches_header():
-    assert ctypes.sizeof(abi.Params) == 32
+    assert ctypes.sizeof(abi.Params) == 40
+    assert ctypes.sizeof(abi.AdjointParams) == 48
+    assert ctypes.sizeof(abi.TuneEntry) == 64
     assert ctypes.sizeof(abi.Config) == 32
     assert ctypes.sizeof(abi.Timings) == 72
     assert abi.NODE_DTYPE.itemsize == 104

@@ -84,12 +84,12 @@ def test_forest_trees_and_fp64_forces_equal_each_system_alone(ctx, theta, leaf):
             assert np.array_equal(got[k][lo:hi][alive], want[:, j][alive]), (q, k)
 
 
-@pytest.mark.parametrize("walk", ["mixed", "plain", "fp64"])
-def test_forest_steps_equal_each_system_stepped_alone(ctx, walk):
-    """Bit-identical: the same per-system trees, the same 64-star groups, the same kernels."""
+@pytest.mark.parametrize("walk,group", [("mixed", 64), ("mixed", 32), ("plain", 0), ("fp64", 0)])
+def test_forest_steps_equal_each_system_stepped_alone(ctx, walk, group):
+    """Bit-identical: the same per-system trees, the same 64- (32-) star groups, the same kernels."""
     s, off = ics.forest(nsys=6, seed=3, nmin=500, nmax=4000)
     nsys, n = len(off) - 1, int(off[-1])
-    par = abi.make_params(0.5, 0.02, 8, False, False, walk)
+    par = abi.make_params(0.5, 0.02, 8, False, False, walk, group_size=group)
     upload_forest(ctx, s, off)
     ctx.call("gbh_state_step", par, 1e-3, 3)
     forest = download(ctx, n)
@@ -129,3 +129,29 @@ def test_forest_upload_validates_offsets(ctx):
     with pytest.raises(abi.GbhError) as ei:
         ctx.step_block(abi.make_params(0.5, 0.01, 8), 1e-3, 0.025, 3, 1)
     assert ei.value.code == abi.ERR_UNSUPPORTED
+
+
+def test_autotune_on_a_forest_meets_the_bound(ctx):
+    s, off = ics.forest(nsys=5, seed=8, nmin=800, nmax=5000)
+    n = int(off[-1])
+    upload_forest(ctx, s, off)
+    base = abi.make_params(0.5, 0.01, 8, False, False, "mixed")
+    best, table = ctx.autotune(base, thetas=[0.4, 0.7], leaves=[8, 16], groups=[64, 32], rms_bound=2e-3,
+                               sample=512, reps=2, strict=True)
+    assert len(table) == 8
+    meets = [e for e in table if e["meets"]]
+    assert meets and min(e["ms"] for e in meets) == min(
+        e["ms"] for e in meets if (e["theta"], e["leaf_size"], e["group_size"]) ==
+        (best.theta, best.leaf_size, best.group_size))
+    # the chosen parameters step the forest, and its forces meet the bound per system
+    ctx.call("gbh_state_step", best, 1e-3, 1)
+    ctx.call("gbh_state_accelerations", best)
+    got = download(ctx, n)
+    a = np.stack([got["ax"], got["ay"], got["az"]], 1)
+    for q in range(len(off) - 1):
+        lo, hi = int(off[q]), int(off[q + 1])
+        t = np.arange(0, hi - lo, max(1, (hi - lo) // 200))
+        want = O.direct(got["px"][lo:hi], got["py"][lo:hi], got["pz"][lo:hi], s["mass"][lo:hi], s["kind"][lo:hi],
+                        eps=0.01, targets=t)
+        e = np.linalg.norm(a[lo:hi][t] - want, axis=1) / np.linalg.norm(want, axis=1)
+        assert np.sqrt(np.mean(e ** 2)) < 4e-3, q

@@ -407,3 +407,65 @@ def test_empty_state(ctx):
     assert gpu_acc(ctx, s, 0.5, 8, 0.01, "mixed").shape == (0, 3)
     s = dict(px=np.zeros(5), py=np.zeros(5), pz=np.zeros(5), mass=np.ones(5), kind=np.full(5, 1, np.uint8))
     assert np.all(gpu_acc(ctx, s, 0.5, 8, 0.01, "mixed") == 0)  # holes only: no stars, all zero
+
+
+def test_mixed_walk_group_32_accuracy_and_determinism(ctx):
+    """32-star groups: one star per lane. Same accuracy class as 64-star groups against the FP64
+    direct sum, deterministic, and never less accurate per star than the group-64 bound allows."""
+    s = ics.plummer(20000, seed=21)
+    n = len(s["px"])
+    want = O.direct(s["px"], s["py"], s["pz"], s["mass"], eps=0.01, targets=np.arange(0, n, 7))
+    out = {}
+    for g in (64, 32):
+        a = [np.zeros(n) for _ in range(3)]
+        par = abi.make_params(0.5, 0.01, 8, False, False, "mixed", group_size=g)
+        for _ in range(2):
+            b = [np.zeros(n) for _ in range(3)]
+            ctx.call("gbh_accelerations", par, n, P(s["px"]), P(s["py"]), P(s["pz"]), P(s["mass"]), None, None,
+                     P(b[0]), P(b[1]), P(b[2]))
+            if a[0].any():
+                assert all(np.array_equal(x, y) for x, y in zip(a, b)), g
+            a = b
+        got = np.stack(a, 1)[::7]
+        e = np.linalg.norm(got - want, axis=1) / np.linalg.norm(want, axis=1)
+        out[g] = np.sqrt(np.mean(e ** 2))
+    assert out[32] < 2e-3 and out[64] < 2e-3, out
+    with pytest.raises(abi.GbhError) as ei:
+        ctx.call("gbh_accelerations", abi.make_params(0.5, 0.01, 8, group_size=48), n, P(s["px"]), P(s["py"]),
+                 P(s["pz"]), P(s["mass"]), None, None, P(np.zeros(n)), P(np.zeros(n)), P(np.zeros(n)))
+    assert ei.value.code == abi.ERR_ARG
+
+
+def test_autotune_single_system(ctx):
+    s = ics.plummer(30000, seed=22)
+    n = len(s["px"])
+    ctx.call("gbh_state_upload", n, *[P(s[k]) for k in ("px", "py", "pz", "vx", "vy", "vz")], None, None, None,
+             P(s["mass"]), None, None)
+    base = abi.make_params(0.5, 0.01, 8, False, False, "mixed")
+    best, table = ctx.autotune(base, rms_bound=2e-3, sample=1024, reps=2, strict=True)
+    assert len(table) == 3 * 4 * 2
+    assert {(e["theta"], e["leaf_size"], e["group_size"]) for e in table} == {
+        (t, l, g) for t in (0.4, 0.5, 0.7) for l in (4, 8, 16, 32) for g in (32, 64)}
+    for e in table:  # the error estimate does not depend on the timing
+        assert 0 < e["rms_err"] < 2e-2 and e["ms"] > 0 and e["build_ms"] > 0 and e["walk_ms"] > 0
+    chosen = [e for e in table if (e["theta"], e["leaf_size"], e["group_size"]) ==
+              (best.theta, best.leaf_size, best.group_size)][0]
+    assert chosen["meets"] and chosen["ms"] == min(e["ms"] for e in table if e["meets"])
+    # an unreachable bound: the most accurate candidate and GBH_ERR_LIMIT
+    best2, table2 = ctx.autotune(base, thetas=[0.7], leaves=[16], groups=[64], rms_bound=1e-9, sample=64, reps=1)
+    assert len(table2) == 1 and not table2[0]["meets"] and best2.theta == 0.7
+    with pytest.raises(abi.GbhError) as ei:
+        ctx.autotune(base, thetas=[0.7], leaves=[16], groups=[64], rms_bound=1e-9, sample=64, reps=1, strict=True)
+    assert ei.value.code == abi.ERR_LIMIT
+    # the state still steps with the chosen parameters
+    ctx.call("gbh_state_step", best, 1e-3, 2)
+
+
+def test_autotune_needs_a_state():
+    c = abi.Context(0)
+    try:
+        with pytest.raises(abi.GbhError) as ei:
+            c.autotune(abi.make_params(0.5, 0.01, 8))
+        assert ei.value.code == abi.ERR_STATE
+    finally:
+        c.close()
