@@ -1,9 +1,11 @@
 """Benchmark of the Barnes-Hut gravity step: particle-steps/s at N = 1,048,576, theta = 0.5.
 
 Workload: a major merger of two disk + bulge + NFW-halo galaxies of 524,288 particles each
-(seeded synthetic stand-in, gravitas_gb300.ics.merger), theta 0.5 with quadrupoles, leaf 8,
-softening 0.02, global KDK steps of dt = 1e-3 (kick, drift, tree build, walk, kick). One step
-advances all N particles.
+(seeded synthetic stand-in, gravitas_gb300.ics.merger), theta 0.5 with quadrupoles, softening
+0.02, global KDK steps of dt = 1e-3 (kick, drift, tree build, walk, kick). One step advances all
+N particles. The leaf size (and the mixed walk's group size) of each walk is chosen first by the
+library's autotuner (gbh_autotune) at theta 0.5 for the shortest force evaluation with RMS force
+error <= 2e-3; --leaf fixes it instead.
 
   value       mixed walk (warp-cooperative FP32 + compensated sums, FP64 state), state resident
               in HBM, device time of K steps from CUDA events on the library's stream, L2
@@ -19,7 +21,10 @@ advances all N particles.
               4,096 seeded targets
 
 --impl reference times the CPU restatement of the reference's Barnes-Hut step (oracle/, FP64,
-all host threads) on the same workload.
+all host threads) on the same workload at the reference solver's default leaf size, 24.
+
+--workload adjoint and --workload forest print the lines of the differentiable and the batched
+workloads instead (see run_adjoint and run_forest).
 """
 from __future__ import annotations
 
@@ -39,10 +44,13 @@ sys.path.insert(0, ROOT)
 
 METRIC = "particle-steps/s @N=1M θ=0.5: mixed vs plain GPU walk at RMS force err ≤2e-3"
 N_DEFAULT = 1 << 20
-THETA, LEAF, EPS, DT = 0.5, 8, 0.02, 1e-3
-# DRAM bytes (read + write) of one k_walk_mixed2 launch on this workload, from the ncu capture
-# summarised in profiles/walk_mixed2_merger_1M_theta0.5_leaf8.md (72.90 MB + 6.48 MB).
-WALK_TRAFFIC_BYTES = 79_383_296
+THETA, EPS, DT = 0.5, 0.02, 1e-3
+# DRAM bytes (read + write) of one k_walk_mixed2 launch on this workload by leaf size, from the
+# ncu captures summarised in profiles/walk_mixed2_merger_1M_theta0.5_leaf*.md.
+WALK_TRAFFIC_BYTES = {8: 79_383_296, 16: 63_032_576, 24: 58_338_304}
+TUNE_LEAVES = [8, 12, 16, 24, 32]
+RMS_BOUND = 2e-3
+REFERENCE_LEAF = 24  # bh.go:67-68, the reference solver's default leaf size
 FIELDS = ("px", "py", "pz", "vx", "vy", "vz", "ax", "ay", "az")
 
 
@@ -134,15 +142,17 @@ def run_reference(args):
     s = make_workload(n)
     cores = os.cpu_count() or 1
     # one warm-up step, then at most as many timed steps as fit in about a minute
-    warm, _ = cpu_reference_steps(s, max(1, min(args.warmup, 1)), args.leaf, workers=0)
+    leaf = args.leaf or REFERENCE_LEAF
+    warm, _ = cpu_reference_steps(s, max(1, min(args.warmup, 1)), leaf, workers=0)
     k = max(1, min(args.steps, int(60.0 / max(warm, 1e-3))))
-    el, _ = cpu_reference_steps(s, k, args.leaf, workers=0)
+    el, _ = cpu_reference_steps(s, k, leaf, workers=0)
     value = n * k / el
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": args.gpus,
         "steps": k, "warmup": 1, "ms_per_step": el / k * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": workload_name(n, args.leaf), "requested_steps": args.steps},
+        "config": {"workload": workload_name(n, leaf), "requested_steps": args.steps,
+                   "leaf_size": leaf, "tuning": "the reference solver's default leaf size (bh.go:67-68)"},
         "cpu_baseline": {"value": value, "unit": "particle-steps/s", "cores": cores, "kind": "port",
                          "sample": f"{k} full KDK steps of the {n}-particle workload (C++ restatement of the "
                                    f"reference CPU Barnes-Hut, FP64, {cores} threads; Go is not available)"},
@@ -183,8 +193,23 @@ def run(args):
         ctx.call("gbh_state_upload", n, *[P(state[k]) for k in ("px", "py", "pz", "vx", "vy", "vz")],
                  None, None, None, P(state["mass"]), None, None)
 
+    # leaf (and group) size of each walk: the autotuner at theta 0.5 under the RMS bound
+    upload(s)
+    tuned = {}
+    for walk in ("mixed", "plain"):
+        base = abi.make_params(THETA, EPS, args.leaf or 8, False, False, walk)
+        if args.leaf:
+            tuned[walk] = (base, None)
+            continue
+        best, table = ctx.autotune(base, thetas=[THETA], leaves=TUNE_LEAVES,
+                                   groups=[64, 32] if walk == "mixed" else [64], rms_bound=RMS_BOUND,
+                                   sample=4096, reps=3)
+        tuned[walk] = (best, [{k: (round(v, 6) if isinstance(v, float) else v) for k, v in e.items()
+                               if k in ("leaf_size", "group_size", "ms", "rms_err")} for e in table])
+    leaf = tuned["mixed"][0].leaf_size
+
     def timed_steps(walk, steps, warmup, diag=None):
-        par = abi.make_params(THETA, EPS, args.leaf, False, False, walk)
+        par = tuned[walk][0]
         upload(s)
         if diag is not None:
             diag.append(ctx.diagnostics(par))
@@ -235,7 +260,7 @@ def run(args):
 
     # end to end: host state in pinned memory, one gbh_step_kdk per step (copies inside)
     host = {k: torch.from_numpy(np.array(s[k], copy=True)).pin_memory() for k in (*FIELDS, "mass")}
-    par = abi.make_params(THETA, EPS, args.leaf, False, False, "mixed")
+    par = tuned["mixed"][0]
     hp = [host[k].data_ptr() for k in FIELDS]
 
     def e2e_step(acc_valid):
@@ -269,7 +294,7 @@ def run(args):
     errs = {}
     for walk in ("mixed", "plain"):
         a = [np.zeros(n) for _ in range(3)]
-        ctx.call("gbh_accelerations", abi.make_params(THETA, EPS, args.leaf, False, False, walk), n, P(s["px"]),
+        ctx.call("gbh_accelerations", tuned[walk][0], n, P(s["px"]),
                  P(s["py"]), P(s["pz"]), P(s["mass"]), None, None, P(a[0]), P(a[1]), P(a[2]))
         errs[walk] = rel_err_stats(np.stack(a, axis=1)[targets], want)
 
@@ -278,7 +303,7 @@ def run(args):
         # CPU baseline leg: the oracle (reference algorithm) on the host cores, bounded sample,
         # plus the reference walk's interaction counts behind the algorithmic FLOP figure
         cpu_steps = 1
-        el, counts = cpu_reference_steps(s, cpu_steps, args.leaf, workers=0, count=True)
+        el, counts = cpu_reference_steps(s, cpu_steps, leaf, workers=0, count=True)
         cores = os.cpu_count() or 1
         n_pn, n_pp, n_open = counts
         flop = 50 * n_pn + 18 * n_pp + 8 * n_open
@@ -288,11 +313,16 @@ def run(args):
             "metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_mixed / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32 walk, f64 state", "data": "synthetic",
-            "config": {"workload": workload_name(n, args.leaf), "parallelism": "replicas" if world > 1 else "1 gpu",
-                       "l2": "flushed (256 MiB write) between timed steps; events cover each step only"},
+            "config": {"workload": workload_name(n, leaf), "parallelism": "replicas" if world > 1 else "1 gpu",
+                       "l2": "flushed (256 MiB write) between timed steps; events cover each step only",
+                       "leaf_size": leaf, "group_size": tuned["mixed"][0].group_size or 64,
+                       "plain_leaf_size": tuned["plain"][0].leaf_size,
+                       "tuning": "gbh_autotune at theta 0.5, RMS force error <= 2e-3 on 4096 stars" if not args.leaf
+                       else "fixed by --leaf"},
             "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                         "frac": achieved / peak, "traffic": WALK_TRAFFIC_BYTES,
-                         "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch",
+                         "frac": achieved / peak, "traffic": WALK_TRAFFIC_BYTES.get(leaf),
+                         "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch at "
+                                           "this leaf size (null: not captured at this leaf size)",
                          "kernel": "k_walk_mixed2", "flop_per_launch": flop,
                          "peak_source": "FP32 FMA microbenchmark in this run (gbh_probe_fp32_peak); "
                                         "MEASURED_PEAKS.json has no FP32 figure",
@@ -306,6 +336,7 @@ def run(args):
             "clocks": clocks,
             "plain": {"value": plain_value, "ms_per_step": t_plain / args.steps, "walk_ms": w_plain / args.steps,
                       "force_error": errs["plain"], "speedup_mixed_over_plain": value / plain_value},
+            "autotune": {"mixed": tuned["mixed"][1], "plain": tuned["plain"][1]},
             "force_error": errs["mixed"],
             "drift": drift,
             "interactions": {"accepted_nodes": n_pn, "leaf_pairs": n_pp, "opened_nodes": n_open,
@@ -328,11 +359,12 @@ def run_profile(args):
     ctx = abi.Context(0)
     ctx.call("gbh_state_upload", n, *[P(s[k]) for k in ("px", "py", "pz", "vx", "vy", "vz")], None, None, None,
              P(s["mass"]), None, None)
-    par = abi.make_params(THETA, EPS, args.leaf, False, False, args.profile)
+    leaf = args.leaf or REFERENCE_LEAF
+    par = abi.make_params(THETA, EPS, leaf, False, False, args.profile)
     for _ in range(2):
         ctx.call("gbh_state_accelerations", par)
     t = ctx.timings()
-    print(json.dumps({"profile": args.profile, "n": n, "leaf": args.leaf, "build_ms": t["build_ms"],
+    print(json.dumps({"profile": args.profile, "n": n, "leaf": leaf, "build_ms": t["build_ms"],
                       "walk_ms": t["walk_ms"], "nnodes": t["nnodes"], "launches": t["launches"]}))
     ctx.close()
     return 0
@@ -524,7 +556,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--n", type=int, default=N_DEFAULT)
-    ap.add_argument("--leaf", type=int, default=LEAF)
+    ap.add_argument("--leaf", type=int, default=0,
+                    help="leaf size; 0 (default) lets the autotuner choose for each walk")
     ap.add_argument("--profile", choices=["mixed", "plain", "fp64"], default=None,
                     help="run only two force evaluations with this walk (for ncu captures)")
     ap.add_argument("--workload", choices=["merger", "adjoint", "forest"], default="merger",
