@@ -1,0 +1,137 @@
+"""GPU parity tests at the sizes of the reference workloads the benchmark configurations name:
+C1 (Plummer 16,384, 100 KDK steps), C2 (disk + bulge + NFW-halo galaxy of 131,072 bodies with
+6-rung block steps), C5 (the 1,048,576-body merger at theta 0.3, 0.5 and 0.8). C3 (forest) and
+C4 (adjoint) have their own files."""
+import numpy as np
+import pytest
+
+from gravitas_gb300 import abi, ics
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+P = abi.ptr
+F9 = ("px", "py", "pz", "vx", "vy", "vz", "ax", "ay", "az")
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    c = abi.Context(0)
+    yield c
+    c.close()
+
+
+def upload(ctx, s):
+    n = len(s["px"])
+    ctx.call("gbh_state_upload", n, *[P(s[k]) for k in ("px", "py", "pz", "vx", "vy", "vz")], None, None, None,
+             P(s["mass"]), P(s["kind"]), P(s["alive"]))
+
+
+def download(ctx, n):
+    st = {k: np.zeros(n) for k in F9}
+    ctx.call("gbh_state_download", *[P(st[k]) for k in F9])
+    return st
+
+
+def rms_p99(got, want):
+    e = np.linalg.norm(got - want, axis=1) / np.linalg.norm(want, axis=1)
+    return float(np.sqrt(np.mean(e ** 2))), float(np.percentile(e, 99))
+
+
+def accelerations(ctx, s, par):
+    n = len(s["px"])
+    a = [np.zeros(n) for _ in range(3)]
+    ctx.call("gbh_accelerations", par, n, P(s["px"]), P(s["py"]), P(s["pz"]), P(s["mass"]), P(s["kind"]),
+             P(s["alive"]), P(a[0]), P(a[1]), P(a[2]))
+    return np.stack(a, 1)
+
+
+def test_c1_plummer_100_steps_fp64_bit_exact(ctx):
+    """Config 1: equal-mass Plummer N = 16,384 (float32 positions and velocities), eps 0.01,
+    theta 0.5, leaf 8, 100 KDK steps of 1e-3: the FP64 walk's trajectory equals the oracle's."""
+    s = ics.plummer(16384, seed=0)
+    n = len(s["px"])
+    upload(ctx, s)
+    ctx.call("gbh_state_step", abi.make_params(0.5, 0.01, 8, False, False, "fp64"), 1e-3, 100)
+    got = download(ctx, n)
+    ref = {k: s[k].copy() for k in (*F9, "mass")}
+    O.kdk(ref, dt=1e-3, eps=0.01, theta=0.5, leaf=8, nsteps=100)
+    for k in F9:
+        assert np.array_equal(got[k], ref[k]), k
+
+
+def test_c1_fp32_walks_against_reference_tree_and_direct_sum(ctx):
+    """Config 1 forces: the plain walk against the reference CPU tree (gpu_test.go:8-21
+    tolerances), the mixed walk against the FP64 direct sum at equal or better RMS and p99
+    error than the reference per-star walk."""
+    s = ics.plummer(16384, seed=0)
+    tree = O.Tree(s["px"], s["py"], s["pz"], s["mass"], theta=0.5, leaf=8)
+    ref_tree = tree.accelerations(0.01)
+    direct = O.direct(s["px"], s["py"], s["pz"], s["mass"], eps=0.01)
+    plain = accelerations(ctx, s, abi.make_params(0.5, 0.01, 8, False, False, "plain"))
+    mixed = accelerations(ctx, s, abi.make_params(0.5, 0.01, 8, False, False, "mixed"))
+    e = np.linalg.norm(plain - ref_tree, axis=1) / np.linalg.norm(ref_tree, axis=1)
+    assert np.median(e) <= 1e-5 and e.max() <= 1e-3
+    r_tree, p_tree = rms_p99(ref_tree, direct)
+    r_mix, p_mix = rms_p99(mixed, direct)
+    assert r_mix <= 1.001 * r_tree and p_mix <= 1.001 * p_tree and r_mix <= 2e-3
+
+
+def test_c2_galaxy_block_steps(ctx):
+    """Config 2: the 131,072-body galaxy (40 % disk, 10 % bulge, 50 % NFW dark halo at 4x the
+    disk particle mass), eps 0.02, theta 0.5, 6 rungs, eta 0.025. Block steps conserve energy
+    as well as global steps at the finest rung, with far fewer star walks."""
+    g = ics.galaxy(131072, seed=0)
+    n = len(g["px"])
+    par = abi.make_params(0.5, 0.02, 8, False, False, "mixed")
+    T, steps = 1.6e-2, 4
+    upload(ctx, g)
+    e0 = ctx.diagnostics(par)["total"]
+    st = ctx.step_block(par, T, 0.025, 6, steps)
+    e_block = ctx.diagnostics(par)["total"]
+    upload(ctx, g)
+    ctx.call("gbh_state_step", par, T / 32, 32 * steps)
+    e_fine = ctx.diagnostics(par)["total"]
+    d_block, d_fine = abs((e_block - e0) / e0), abs((e_fine - e0) / e0)
+    assert st["substeps"] <= 32 * steps and st["evaluations"] < 0.5 * 32 * steps * n
+    assert d_block <= max(5 * d_fine, 2e-5), (d_block, d_fine)
+
+
+def test_c2_galaxy_block_steps_fp64_bit_exact_with_oracle(ctx):
+    """The same scheme on a smaller galaxy (dark matter included) through the FP64 walk equals
+    the oracle's restatement: trajectories, event count and walked stars."""
+    g = ics.galaxy(8192, seed=1)
+    n = len(g["px"])
+    upload(ctx, g)
+    st = ctx.step_block(abi.make_params(0.5, 0.02, 8, False, False, "fp64"), 1.6e-2, 0.025, 6, 2)
+    got = download(ctx, n)
+    ref = {k: g[k].copy() for k in (*F9, "mass", "kind", "alive")}
+    events, walked = O.block_kdk(ref, dt=1.6e-2, eta=0.025, levels=6, eps=0.02, theta=0.5, leaf=8, nsteps=2)
+    assert (st["substeps"], st["evaluations"]) == (events, walked)
+    for k in F9:
+        assert np.array_equal(got[k], ref[k]), k
+
+
+def test_c5_merger_1m_theta_sweep(ctx):
+    """Config 5: the 1,048,576-body merger at theta 0.3, 0.5 and 0.8. On 4,096 seeded stars the
+    mixed walk's RMS force error against the FP64 direct sum is at most the plain per-star
+    walk's, and within 2e-3 up to theta 0.5; one 6-rung block step keeps energy to 1e-5."""
+    s = ics.merger(1 << 20, seed=0)
+    n = len(s["px"])
+    rng = np.random.default_rng(1234)
+    tg = np.sort(rng.choice(n, 4096, replace=False)).astype(np.int64)
+    want = np.zeros((3, len(tg)))
+    ctx.call("gbh_direct_accelerations", abi.make_params(0, 0.02, 0, False, False, "fp64"), n, P(s["px"]),
+             P(s["py"]), P(s["pz"]), P(s["mass"]), P(s["kind"]), P(tg), len(tg), P(want[0]), P(want[1]), P(want[2]))
+    want = want.T
+    for theta in (0.3, 0.5, 0.8):
+        r_mix, _ = rms_p99(accelerations(ctx, s, abi.make_params(theta, 0.02, 8, False, False, "mixed"))[tg], want)
+        r_pl, _ = rms_p99(accelerations(ctx, s, abi.make_params(theta, 0.02, 8, False, False, "plain"))[tg], want)
+        assert r_mix <= r_pl, (theta, r_mix, r_pl)
+        if theta <= 0.5:
+            assert r_mix <= 2e-3, (theta, r_mix)
+    par = abi.make_params(0.5, 0.02, 8, False, False, "mixed")
+    upload(ctx, s)
+    e0 = ctx.diagnostics(par)["total"]
+    ctx.step_block(par, 4e-3, 0.025, 6, 1)
+    e1 = ctx.diagnostics(par)["total"]
+    assert abs((e1 - e0) / e0) < 1e-5
