@@ -45,7 +45,8 @@ class Config(ctypes.Structure):
 class Timings(ctypes.Structure):
     _fields_ = [("build_ms", ctypes.c_double), ("walk_ms", ctypes.c_double), ("step_ms", ctypes.c_double),
                 ("total_ms", ctypes.c_double), ("nstars", ctypes.c_int64), ("nnodes", ctypes.c_int64),
-                ("launches", ctypes.c_int64), ("h2d_bytes", ctypes.c_int64), ("d2h_bytes", ctypes.c_int64)]
+                ("launches", ctypes.c_int64), ("h2d_bytes", ctypes.c_int64), ("d2h_bytes", ctypes.c_int64),
+                ("substeps", ctypes.c_int64)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

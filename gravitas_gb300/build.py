@@ -7,6 +7,7 @@ Each translation unit gets its own floating-point flags:
   moments.cu             FP32 node moments for the FP32 walks (FMA on, IEEE FP32 division);
   api.cu                 host code;
   noalloc.cu             the entry point whose temporaries live in a static device array;
+  split.cu   -fmad=false the hole-aware split step (bit-exact with the CPU restatement);
   adjoint.cu -fmad=false the adjoint pair: FP64 pair kernels bit-exact with the CPU
                          restatement, FP32 pair kernels with explicit fmaf/rsqrtf.
 Objects compile in parallel; the shared library links the CUDA runtime statically.
@@ -32,6 +33,7 @@ UNITS = {
     "api.cu": [],
     "noalloc.cu": [],
     "adjoint.cu": ["-fmad=false"],
+    "split.cu": ["-fmad=false"],
 }
 
 

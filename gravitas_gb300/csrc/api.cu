@@ -73,11 +73,14 @@ struct gbh_ctx {
     size_t evused = 0;
     StepGraph step_graph;
     gbh::AdjTape adj;  // tape of gbh_fwd_save
+    gbh::SplitBufs split;             // buffers of the hole-aware step
+    std::vector<int32_t> hole_list;   // alive holes of the resident state, ascending
     bool use_graphs = true;
     bool capturing = false;  // stage events become graph event-record nodes
     // bookkeeping
     int64_t launches = 0;
     int64_t h2d = 0, d2h = 0;
+    int64_t last_substeps = 1;  // substeps of the last hole-aware step
     DevInfo info_host = {};
     gbh_timings last = {};
     std::string err;
@@ -254,6 +257,7 @@ int finish(gbh_ctx *ctx, bool tree) {
     }
     t.step_ms = t.total_ms - t.build_ms - t.walk_ms;
     t.launches = ctx->launches;
+    t.substeps = ctx->last_substeps;
     t.h2d_bytes = ctx->h2d;
     t.d2h_bytes = ctx->d2h;
     if (tree) {
@@ -355,6 +359,61 @@ int capture_step(gbh_ctx *ctx, const gbh_params *p, double dt, const uint8_t *ki
 }
 
 // Steps on the resident state (sim.go:252-288, no holes, no hydro).
+// The hole-aware step (split.go:161-204, stepSplit) with c = 0 and no gas: forces of pairs with a
+// hole summed directly, near stars and holes in power-of-two substeps, star-star forces from the
+// tree once per step. The substep count of the last step goes to ctx->last_substeps.
+int run_split_steps(gbh_ctx *ctx, const gbh_params *p, double dt, int64_t nsteps) {
+    Launch L = launch_of(ctx);
+    const int64_t n = ctx->n;
+    const uint8_t *kind = ctx->kind;  // holes imply kinds
+    const uint8_t *alive = ctx->state_has_alive ? ctx->alive : nullptr;
+    const double theta = theta_of(p), eps2 = p->softening * p->softening, h = 0.5 * dt;
+    const int dm = p->dark_matter_off;
+    gbh::SplitBufs &sb = ctx->split;
+    CK(gbh::split_reserve(sb, n, ctx->hole_list));
+    CK(cudaMemcpyAsync(sb.holes, ctx->hole_list.data(), sizeof(int32_t) * ctx->hole_list.size(),
+                       cudaMemcpyHostToDevice, ctx->stream));
+    double *px = ctx->px, *py = ctx->py, *pz = ctx->pz, *vx = ctx->vx, *vy = ctx->vy, *vz = ctx->vz;
+    auto slow = [&]() {  // Solver.Accelerations: star-star forces, holes get 0
+        return forces(ctx, p, n, px, py, pz, ctx->mass, kind, alive, ctx->ax, ctx->ay, ctx->az, theta, false);
+    };
+    if (!ctx->acc_valid) {  // initForces (gas.go:14-17)
+        int rc = slow();
+        if (rc) return rc;
+        ctx->acc_valid = true;
+    }
+    unsigned long long sc[2];
+    for (int64_t step = 0; step < nsteps; ++step) {
+        // classify (split.go:41-81): the host needs the substep count
+        CK(gbh::split_classify(L, sb, n, px, py, pz, ctx->mass, kind, eps2, 20.0 * dt));
+        CK(cudaMemcpyAsync(sc, sb.scalars, sizeof sc, cudaMemcpyDeviceToHost, ctx->stream));
+        CK(cudaStreamSynchronize(ctx->stream));
+        double tau_min;
+        std::memcpy(&tau_min, &sc[0], sizeof tau_min);
+        const int32_t nnear = int32_t(sc[1]);
+        int64_t k = 1;
+        if (!std::isinf(tau_min))
+            while (double(k) * tau_min < 20.0 * dt && k < 256) k *= 2;
+        ctx->last_substeps = k;
+        CK(gbh::split_outer(L, sb, n, px, py, pz, ctx->mass, kind, dm, eps2));
+        CK(gbh::split_kick_outer(L, sb, n, h, vx, vy, vz, ctx->ax, ctx->ay, ctx->az));
+        const double hs = dt / double(k);
+        CK(gbh::split_fast(L, sb, n, nnear, px, py, pz, ctx->mass, kind, dm, eps2));
+        for (int64_t q = 0; q < k; ++q) {
+            CK(gbh::split_fast_update(L, sb, n, nnear, false, 0.5 * hs, px, py, pz, vx, vy, vz));
+            CK(gbh::split_fast_update(L, sb, n, nnear, true, hs, px, py, pz, vx, vy, vz));
+            CK(gbh::split_fast(L, sb, n, nnear, px, py, pz, ctx->mass, kind, dm, eps2));
+            CK(gbh::split_fast_update(L, sb, n, nnear, false, 0.5 * hs, px, py, pz, vx, vy, vz));
+        }
+        CK(gbh::split_drift_far(L, sb, n, dt, kind, px, py, pz, vx, vy, vz));
+        int rc = slow();  // advanceGas without gas (blockstep.go:129-135)
+        if (rc) return rc;
+        CK(gbh::split_outer(L, sb, n, px, py, pz, ctx->mass, kind, dm, eps2));
+        CK(gbh::split_kick_outer(L, sb, n, h, vx, vy, vz, ctx->ax, ctx->ay, ctx->az));
+    }
+    return GBH_OK;
+}
+
 int run_steps(gbh_ctx *ctx, const gbh_params *p, double dt, int64_t nsteps) {
     Launch L = launch_of(ctx);
     int64_t n = ctx->n;
@@ -513,6 +572,10 @@ int upload_state(gbh_ctx *ctx, int64_t n, const double *px, const double *py, co
     ctx->have_state = true;
     ctx->acc_valid = acc;
     ctx->state_holes = count_holes(kind, alive, n);
+    ctx->hole_list.clear();
+    if (ctx->state_holes)  // collectHoles, sim.go:294-302 (kinds and liveness do not change in a step)
+        for (int64_t i = 0; i < n; ++i)
+            if ((alive ? alive[i] : 1) && kind[i] == GBH_BLACK_HOLE) ctx->hole_list.push_back(int32_t(i));
     if (ctx->nsys != 1) {
         ctx->nsys = 1;
         ++ctx->sys_gen;
@@ -581,6 +644,7 @@ void gbh_destroy(gbh_ctx *c) {
     free_graph(c->step_graph);
     gbh::tree_free(c->tb);
     gbh::adj_free(c->adj);
+    gbh::split_free(c->split);
     free_state(c);
     void *ptrs[] = {c->part,  c->scalar,   c->holes, c->targets,  c->tout,   c->probe,
                     c->scratch3, c->rung, c->end_tick, c->sys_of, c->sys_off};
@@ -718,14 +782,13 @@ int gbh_step_kdk(gbh_ctx *ctx, const gbh_params *p, double dt, int64_t nsteps, i
     if (rc || (rc = check_params(ctx, p))) return rc;
     if (nsteps < 0) return fail(ctx, GBH_ERR_ARG, "nsteps < 0");
     if (!ax || !ay || !az) return fail(ctx, GBH_ERR_ARG, "acceleration arrays must not be NULL");
-    if (count_holes(kind, alive, n))
-        return fail(ctx, GBH_ERR_UNSUPPORTED,
-                    "alive black holes need the hole-aware split step (sim.stepSplit), which this path does not cover");
     CK(cudaEventRecord(ctx->ev[0], ctx->stream));
     rc = upload_state(ctx, n, px, py, pz, vx, vy, vz, acc_valid ? ax : nullptr, acc_valid ? ay : nullptr,
                       acc_valid ? az : nullptr, mass, kind, alive);
     if (rc) return rc;
-    if (n > 0 && (rc = run_steps(ctx, p, dt, nsteps))) return rc;
+    ctx->last_substeps = 1;
+    if (n > 0 && (rc = ctx->state_holes ? run_split_steps(ctx, p, dt, nsteps) : run_steps(ctx, p, dt, nsteps)))
+        return rc;
     if ((rc = download_state(ctx, px, py, pz, vx, vy, vz, ax, ay, az))) return rc;
     return finish(ctx, n > 0);
 }
@@ -755,11 +818,13 @@ int gbh_state_step(gbh_ctx *ctx, const gbh_params *p, double dt, int64_t nsteps)
     if (rc || (rc = check_params(ctx, p))) return rc;
     if (!ctx->have_state) return fail(ctx, GBH_ERR_STATE, "no resident state (gbh_state_upload first)");
     if (nsteps < 0) return fail(ctx, GBH_ERR_ARG, "nsteps < 0");
-    if (ctx->state_holes)
-        return fail(ctx, GBH_ERR_UNSUPPORTED,
-                    "alive black holes need the hole-aware split step (sim.stepSplit), which this path does not cover");
+    if (ctx->state_holes && ctx->nsys > 1)
+        return fail(ctx, GBH_ERR_UNSUPPORTED, "alive black holes in a forest: the split step couples all systems");
     CK(cudaEventRecord(ctx->ev[0], ctx->stream));
-    if (ctx->n > 0 && (rc = run_steps(ctx, p, dt, nsteps))) return rc;
+    ctx->last_substeps = 1;
+    if (ctx->n > 0 &&
+        (rc = ctx->state_holes ? run_split_steps(ctx, p, dt, nsteps) : run_steps(ctx, p, dt, nsteps)))
+        return rc;
     return finish(ctx, ctx->n > 0);
 }
 
@@ -774,7 +839,7 @@ int gbh_state_step_block(gbh_ctx *ctx, const gbh_params *p, double dt, double et
     if (!(dt > 0)) return fail(ctx, GBH_ERR_ARG, "dt must be > 0");
     if (ctx->state_holes)
         return fail(ctx, GBH_ERR_UNSUPPORTED,
-                    "alive black holes need the hole-aware split step (sim.stepSplit), which this path does not cover");
+                    "block steps with alive black holes: use gbh_state_step (the hole-aware split step)");
     if (ctx->nsys > 1) return fail(ctx, GBH_ERR_UNSUPPORTED, "block steps of a forest are not supported");
     if (stats) *stats = gbh_blockstats{};
     CK(cudaEventRecord(ctx->ev[0], ctx->stream));

@@ -8,6 +8,8 @@
 #pragma once
 
 #include <cuda_runtime.h>
+
+#include <vector>
 #include <stdint.h>
 
 #include "../../include/gbh.h"
@@ -190,6 +192,39 @@ size_t morton_sort_scratch_bytes(int64_t nmax);
 cudaError_t morton_sort(const Launch &L, int64_t n, const double *px, const double *py, const double *pz,
                         const uint8_t *kind, const uint8_t *alive, uint64_t *keys, int32_t *order, void *scratch,
                         size_t scratch_bytes, DevInfo **info_out);
+
+// ---- split.cu (the hole-aware step of split.go with c = 0) ----
+struct SplitBufs {
+    int32_t *holes = nullptr;  // alive holes, ascending state index
+    int32_t nholes = 0, cap_holes = 0;
+    uint8_t *near8 = nullptr;   // near flags
+    uint32_t *near32 = nullptr; // near flags, then their exclusive scan
+    int32_t *near = nullptr;    // near stars, ascending
+    uint32_t *scan_tmp = nullptr;
+    int64_t scan_cap = 0;
+    double *far = nullptr, *fast = nullptr;  // 3n each (x, y, z blocks)
+    double *part = nullptr;                  // per 256-body chunk and hole: 3 partial sums
+    int64_t cap_n = 0, cap_part = 0;
+    unsigned long long *scalars = nullptr;   // [0] bits of the minimum timescale, [1] near count
+};
+cudaError_t split_reserve(SplitBufs &s, int64_t n, const std::vector<int32_t> &holes);
+void split_free(SplitBufs &s);
+// Near flags and list, minimum timescale (scalars) for the current positions.
+cudaError_t split_classify(const Launch &L, SplitBufs &s, int64_t n, const double *px, const double *py,
+                           const double *pz, const double *mass, const uint8_t *kind, double eps2, double limit);
+// far = hole pulls of the far stars and the far stars' pulls on the holes.
+cudaError_t split_outer(const Launch &L, SplitBufs &s, int64_t n, const double *px, const double *py,
+                        const double *pz, const double *mass, const uint8_t *kind, int dm_off, double eps2);
+cudaError_t split_kick_outer(const Launch &L, SplitBufs &s, int64_t n, double h, double *vx, double *vy, double *vz,
+                             const double *ax, const double *ay, const double *az);
+// fast = hole pulls of the near stars, and the holes' pulls from the other holes and the near stars.
+cudaError_t split_fast(const Launch &L, SplitBufs &s, int64_t n, int32_t nnear, const double *px, const double *py,
+                       const double *pz, const double *mass, const uint8_t *kind, int dm_off, double eps2);
+// Near stars and holes: v += h fast (drift = false) or x += h v (drift = true).
+cudaError_t split_fast_update(const Launch &L, SplitBufs &s, int64_t n, int32_t nnear, bool drift, double h,
+                              double *px, double *py, double *pz, double *vx, double *vy, double *vz);
+cudaError_t split_drift_far(const Launch &L, SplitBufs &s, int64_t n, double dt, const uint8_t *kind, double *px,
+                            double *py, double *pz, const double *vx, const double *vy, const double *vz);
 
 // ---- adjoint.cu (gradient of the KDK leapfrog with the softened direct-sum force) ----
 struct AdjTape {

@@ -104,6 +104,7 @@ typedef struct {
     int64_t launches;  /* kernels launched by the last call */
     int64_t h2d_bytes; /* host-to-device bytes copied by the last call */
     int64_t d2h_bytes; /* device-to-host bytes copied by the last call */
+    int64_t substeps;  /* hole substeps of the last step (Simulation.Substeps, split.go:168); 1 without holes */
 } gbh_timings;
 
 typedef struct gbh_ctx gbh_ctx;
@@ -151,14 +152,19 @@ int gbh_direct_accelerations(gbh_ctx *ctx, const gbh_params *p, int64_t n, const
                              double *ax, double *ay, double *az);
 
 /*
- * sim.Simulation.Step (sim.go:248-288) repeated nsteps times for a state with
- * no alive black holes and no gas hydro: kick(dt/2), drift(dt) (c = 0,
- * sim.go:327-334), Solver.Accelerations, kick(dt/2). If acc_valid is 0 the
- * forces are computed first (initForces, gas.go:14-17). Arrays are read and
- * written in place; the state stays on the device between the steps. Each
- * step replays one CUDA graph (captured on first use for the sizes and
- * parameters given, re-captured when they change) unless the context was
- * created with GBH_CFG_NO_GRAPHS; results are identical either way.
+ * sim.Simulation.Step (sim.go:248-288) repeated nsteps times, with c = 0 and no gas
+ * hydro. Without alive black holes: kick(dt/2), drift(dt) (sim.go:327-334),
+ * Solver.Accelerations, kick(dt/2); each step replays one CUDA graph (captured on
+ * first use for the sizes and parameters given, re-captured when they change) unless
+ * the context was created with GBH_CFG_NO_GRAPHS; results are identical either way.
+ * With alive black holes: the hole-aware split step (split.go:161-204, stepSplit):
+ * forces of pairs with a hole summed directly (pair.go:26-35, Newtonian for c = 0),
+ * stars whose timescale at a hole is below 20 dt and the holes advanced in 2^k
+ * substeps (classify, split.go:41-81; k of the last step in gbh_timings.substeps),
+ * star-star forces from the tree once per step; no graph (the substep count is read
+ * back every step). If acc_valid is 0 the forces are computed first (initForces,
+ * gas.go:14-17). Arrays are read and written in place; the state stays on the device
+ * between the steps.
  */
 int gbh_step_kdk(gbh_ctx *ctx, const gbh_params *p, double dt, int64_t nsteps, int32_t acc_valid,
                  int64_t n, double *px, double *py, double *pz, double *vx, double *vy,
@@ -176,7 +182,8 @@ int gbh_state_upload(gbh_ctx *ctx, int64_t n, const double *px, const double *py
 /* Copies the resident state back (any pointer may be NULL). */
 int gbh_state_download(gbh_ctx *ctx, double *px, double *py, double *pz, double *vx, double *vy,
                        double *vz, double *ax, double *ay, double *az);
-/* nsteps KDK steps on the resident state (as gbh_step_kdk, no copies). */
+/* nsteps KDK steps on the resident state (as gbh_step_kdk, no copies). A forest with alive
+   black holes returns GBH_ERR_UNSUPPORTED (the split step would couple its systems). */
 int gbh_state_step(gbh_ctx *ctx, const gbh_params *p, double dt, int64_t nsteps);
 /* Statistics of block steps. */
 typedef struct {

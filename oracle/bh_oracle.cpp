@@ -870,6 +870,206 @@ void orc_kdk(int64_t n, double *px, double *py, double *pz, double *vx, double *
     }
 }
 
+namespace {
+
+constexpr double kNearSteps = 20.0;      // split.go:18-19
+constexpr double kSubstepsPerTau = 20.0;  // split.go:20-21
+constexpr int kMaxSubsteps = 256;         // split.go:22-23
+constexpr int64_t kHoleChunk = 256;       // bodies per partial sum of a hole's far-star pull
+
+// pair.go:26-35 (PairForce) with rs = 0.
+inline double pair_force0(double m, double r2, double eps2) {
+    double re2 = r2 + eps2;
+    double re = std::sqrt(re2);
+    return m / (re2 * re);
+}
+
+}  // namespace
+
+void orc_split_kdk(int64_t n, double *px, double *py, double *pz, double *vx, double *vy, double *vz, double *ax,
+                   double *ay, double *az, const double *mass, const uint8_t *kind, const uint8_t *alive, double dt,
+                   double eps, double theta, int leaf_size, int monopole_only, int dm_off, int acc_valid,
+                   int64_t nsteps, int workers, int64_t *substeps, uint8_t *near_out) {
+    orc_tree t;
+    t.theta = theta == 0 ? 0.9 : theta;
+    t.leaf = leaf_size > 0 ? leaf_size : 24;
+    t.workers = workers;
+    auto forces = [&] {
+        t.build(n, px, py, pz, mass, kind, alive, dm_off);
+        orc_tree_accelerations(&t, n, eps, monopole_only, workers, ax, ay, az);
+    };
+    if (!acc_valid) forces();
+    const double eps2 = eps * eps, h = 0.5 * dt;
+    auto is_hole = [&](int64_t i) { return kind && kind[i] == ORC_BLACK_HOLE; };
+    auto src_mass = [&](int64_t i) { return dm_off && kind && kind[i] == ORC_DARK_MATTER ? 0.0 : mass[i]; };
+    std::vector<int64_t> holes, near;
+    std::vector<uint8_t> is_near(size_t(n), 0);
+    std::vector<double> far(3 * size_t(n)), fast(3 * size_t(n));
+    // split.go:27-36
+    auto timescale = [&](int64_t i, int64_t hh) {
+        double dx = px[i] - px[hh], dy = py[i] - py[hh], dz = pz[i] - pz[hh];
+        double r2 = dx * dx + dy * dy + dz * dz;
+        double a = pair_force0(mass[hh], r2, eps2) * std::sqrt(r2);
+        if (a == 0) return std::numeric_limits<double>::infinity();
+        return std::sqrt(std::sqrt(r2 + eps2) / a);
+    };
+    // holePull, split.go:119-137
+    auto hole_pull = [&](int64_t i, double &fx, double &fy, double &fz) {
+        fx = fy = fz = 0;
+        for (int64_t hh : holes) {
+            if (hh == i) continue;
+            double dx = px[hh] - px[i], dy = py[hh] - py[i], dz = pz[hh] - pz[i];
+            double f = pair_force0(mass[hh], dx * dx + dy * dy + dz * dz, eps2);
+            fx += f * dx;
+            fy += f * dy;
+            fz += f * dz;
+        }
+    };
+    // outerHoleForces, split.go:83-117
+    auto outer = [&] {
+        std::fill(far.begin(), far.end(), 0.0);
+        parallel_for(n, kGrain, workers, [&](int64_t lo, int64_t hi) {
+            for (int64_t i = lo; i < hi; ++i)
+                if (!is_hole(i) && !is_near[size_t(i)]) hole_pull(i, far[size_t(i)], far[size_t(n + i)], far[size_t(2 * n + i)]);
+        });
+        for (int64_t hh : holes) {
+            double x = px[hh], y = py[hh], z = pz[hh];
+            for (int64_t c0 = 0; c0 < n; c0 += kHoleChunk) {
+                double sx = 0, sy = 0, sz = 0;
+                for (int64_t i = c0; i < std::min(n, c0 + kHoleChunk); ++i) {
+                    if (is_hole(i) || is_near[size_t(i)]) continue;
+                    double dx = px[i] - x, dy = py[i] - y, dz = pz[i] - z;
+                    double f = pair_force0(src_mass(i), dx * dx + dy * dy + dz * dz, eps2);
+                    sx += f * dx;
+                    sy += f * dy;
+                    sz += f * dz;
+                }
+                far[size_t(hh)] += sx;
+                far[size_t(n + hh)] += sy;
+                far[size_t(2 * n + hh)] += sz;
+            }
+        }
+    };
+    // fastForces, split.go:139-159
+    auto fast_forces = [&] {
+        for (int64_t i : near) hole_pull(i, fast[size_t(i)], fast[size_t(n + i)], fast[size_t(2 * n + i)]);
+        for (int64_t hh : holes) {
+            double x = px[hh], y = py[hh], z = pz[hh];
+            double sx, sy, sz;
+            hole_pull(hh, sx, sy, sz);
+            for (int64_t i : near) {
+                double dx = px[i] - x, dy = py[i] - y, dz = pz[i] - z;
+                double f = pair_force0(src_mass(i), dx * dx + dy * dy + dz * dz, eps2);
+                sx += f * dx;
+                sy += f * dy;
+                sz += f * dz;
+            }
+            fast[size_t(hh)] = sx;
+            fast[size_t(n + hh)] = sy;
+            fast[size_t(2 * n + hh)] = sz;
+        }
+    };
+    auto kick_outer = [&](double k) {  // split.go:206-213
+        for (int64_t i = 0; i < n; ++i) {
+            vx[i] += k * (ax[i] + far[size_t(i)]);
+            vy[i] += k * (ay[i] + far[size_t(n + i)]);
+            vz[i] += k * (az[i] + far[size_t(2 * n + i)]);
+        }
+    };
+    auto kick_fast = [&](double k) {  // split.go:215-224
+        for (const auto *idx : {&near, &holes})
+            for (int64_t i : *idx) {
+                vx[i] += k * fast[size_t(i)];
+                vy[i] += k * fast[size_t(n + i)];
+                vz[i] += k * fast[size_t(2 * n + i)];
+            }
+    };
+    auto drift_idx = [&](const std::vector<int64_t> &idx, double d) {  // split.go:226-234, c = 0
+        for (int64_t i : idx) {
+            double f = d / 1.0;
+            px[i] += f * vx[i];
+            py[i] += f * vy[i];
+            pz[i] += f * vz[i];
+        }
+    };
+    int64_t last = 1;
+    for (int64_t step = 0; step < nsteps; ++step) {
+        holes.clear();
+        for (int64_t i = 0; i < n; ++i)  // collectHoles, sim.go:294-302
+            if ((!alive || alive[i]) && is_hole(i)) holes.push_back(i);
+        if (holes.empty()) {  // sim.go:266-280
+            std::fill(is_near.begin(), is_near.end(), 0);
+            for (int64_t i = 0; i < n; ++i) {
+                vx[i] += h * ax[i];
+                vy[i] += h * ay[i];
+                vz[i] += h * az[i];
+            }
+            for (int64_t i = 0; i < n; ++i) {
+                px[i] += dt * vx[i];
+                py[i] += dt * vy[i];
+                pz[i] += dt * vz[i];
+            }
+            forces();
+            for (int64_t i = 0; i < n; ++i) {
+                vx[i] += h * ax[i];
+                vy[i] += h * ay[i];
+                vz[i] += h * az[i];
+            }
+            last = 1;
+            continue;
+        }
+        // classify, split.go:41-81
+        const double limit = kNearSteps * dt;
+        double tau_min = std::numeric_limits<double>::infinity();
+        for (int64_t i = 0; i < n; ++i) {
+            bool nr = false;
+            if (!is_hole(i))
+                for (int64_t hh : holes) {
+                    double tau = timescale(i, hh);
+                    if (tau < limit) nr = true, tau_min = std::min(tau_min, tau);
+                }
+            is_near[size_t(i)] = nr;
+        }
+        for (size_t a = 0; a < holes.size(); ++a)
+            for (size_t b = a + 1; b < holes.size(); ++b) {
+                double tau = timescale(holes[a], holes[b]);
+                if (tau < limit) tau_min = std::min(tau_min, tau);
+            }
+        near.clear();
+        for (int64_t i = 0; i < n; ++i)
+            if (is_near[size_t(i)]) near.push_back(i);
+        int64_t k = 1;
+        if (!std::isinf(tau_min))
+            while (double(k) * tau_min < kSubstepsPerTau * dt && k < kMaxSubsteps) k *= 2;
+        last = k;
+        // stepSplit, split.go:161-204 (c = 0, no gas, no spin)
+        outer();
+        kick_outer(h);
+        const double hs = dt / double(k);
+        fast_forces();
+        for (int64_t q = 0; q < k; ++q) {
+            kick_fast(0.5 * hs);
+            drift_idx(near, hs);
+            drift_idx(holes, hs);
+            fast_forces();
+            kick_fast(0.5 * hs);
+        }
+        for (int64_t i = 0; i < n; ++i) {  // driftFar
+            if (is_hole(i) || is_near[size_t(i)]) continue;
+            double f = dt / 1.0;
+            px[i] += f * vx[i];
+            py[i] += f * vy[i];
+            pz[i] += f * vz[i];
+        }
+        forces();  // advanceGas without gas
+        outer();
+        kick_outer(h);
+    }
+    if (substeps) *substeps = last;
+    if (near_out)
+        for (int64_t i = 0; i < n; ++i) near_out[i] = is_near[size_t(i)];
+}
+
 void orc_block_kdk(int64_t n, double *px, double *py, double *pz, double *vx, double *vy, double *vz, double *ax,
                    double *ay, double *az, const double *mass, const uint8_t *kind, const uint8_t *alive, double T,
                    double eta, int levels, double eps, double theta, int leaf_size, int monopole_only, int dm_off,

@@ -138,6 +138,23 @@ void orc_block_kdk(int64_t n, double *px, double *py, double *pz, double *vx, do
                    int acc_valid, int64_t nsteps, int workers, int64_t *substeps, int64_t *evals);
 
 /*
+ * The hole-aware step of internal/sim/split.go:1-259 (stepSplit) with c = 0 (Newtonian pairs,
+ * pair.go:26-35 with rs = 0; no relativistic drift, frame dragging, retardation or accretion)
+ * and no gas: star-star forces from the tree once per step; every force involving an alive
+ * black hole summed directly; stars whose timescale at a hole is below 20 dt ("near") and the
+ * holes take n power-of-two substeps (classify, split.go:41-81). Steps without holes are the
+ * plain KDK of orc_kdk. A hole's pull from the far stars is summed in chunks of 256 bodies
+ * (sequential inside a chunk, chunks in index order); the reference sums its ParallelFor chunks
+ * in completion order, so its last bits vary from run to run there. *substeps gets n of the
+ * last step and near (n bytes, may be NULL) its near flags.
+ */
+void orc_split_kdk(int64_t n, double *px, double *py, double *pz, double *vx, double *vy,
+                   double *vz, double *ax, double *ay, double *az, const double *mass,
+                   const uint8_t *kind, const uint8_t *alive, double dt, double eps, double theta,
+                   int leaf_size, int monopole_only, int dark_matter_off, int acc_valid,
+                   int64_t nsteps, int workers, int64_t *substeps, uint8_t *near);
+
+/*
  * Adjoint of the KDK leapfrog (sim.go:302-343) with the softened direct-sum force
  * (direct.go:27-47, all bodies stars): the gradient of a loss with respect to the initial
  * positions, velocities and masses, given its gradient (gx.., gv..) with respect to the final

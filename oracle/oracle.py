@@ -66,6 +66,7 @@ def lib():
             "orc_direct_targets": (None, [_I64, _P, _P, _P, _P, _P, _D, _INT, _P, _I64, _INT, _P, _P, _P]),
             "orc_kdk": (None, [_I64] + [_P] * 12 + [_D, _D, _D, _INT, _INT, _INT, _INT, _I64, _INT]),
             "orc_potential_exact": (_D, [_I64, _P, _P, _P, _P, _P, _D, _D, _INT, _INT]),
+            "orc_split_kdk": (None, [_I64] + [_P] * 12 + [_D, _D, _D, _INT, _INT, _INT, _INT, _I64, _INT, _P, _P]),
             "orc_adjoint_direct": (None, [_I64] + [_P] * 7 + [_D, _D, _I64, _I64] + [_P] * 13 + [_INT]),
             "orc_kdk_direct": (None, [_I64] + [_P] * 7 + [_D, _D, _I64, _INT]),
             "orc_block_kdk": (None, [_I64] + [_P] * 12 + [_D, _D, _INT, _D, _D, _INT, _INT, _INT, _INT, _I64, _INT,
@@ -259,3 +260,21 @@ def adjoint_direct(state: dict, dt, eps, nsteps, every, gx, gv, workers=0):
                              nsteps, every, _ptr(gx[0]), _ptr(gx[1]), _ptr(gx[2]), _ptr(gv[0]), _ptr(gv[1]),
                              _ptr(gv[2]), *[_ptr(out[k]) for k in range(7)], workers)
     return out[0:3].T.copy(), out[3:6].T.copy(), out[6].copy()
+
+
+def split_kdk(state: dict, dt, eps, theta, leaf, nsteps, monopole_only=False, dm_off=False, acc_valid=False,
+              workers=0):
+    """The hole-aware step (split.go, c = 0, no gas) on a dict of SoA arrays, in place; returns
+    (substeps of the last step, near flags of the last step)."""
+    s = state
+    n = len(s["px"])
+    for k in ("px", "py", "pz", "vx", "vy", "vz", "ax", "ay", "az", "mass"):
+        assert s[k].dtype == np.float64 and s[k].flags.c_contiguous
+    kind = _u8(s.get("kind", np.zeros(n, np.uint8)))
+    alive = _u8(s.get("alive", np.ones(n, np.uint8)))
+    sub = np.zeros(1, np.int64)
+    near = np.zeros(n, np.uint8)
+    lib().orc_split_kdk(n, *[_ptr(s[k]) for k in ("px", "py", "pz", "vx", "vy", "vz", "ax", "ay", "az", "mass")],
+                        _ptr(kind), _ptr(alive), dt, eps, theta, leaf, int(monopole_only), int(dm_off),
+                        int(acc_valid), nsteps, workers, _ptr(sub), _ptr(near))
+    return int(sub[0]), near.astype(bool)

@@ -379,14 +379,15 @@ def test_block_steps_conserve_energy_at_fewer_evaluations(ctx):
     assert d_block <= max(5 * d_fine, 2e-5)
 
 
-def test_step_rejects_holes(ctx):
+def test_block_steps_reject_holes(ctx):
+    """Holes take the split step (tests/test_gpu_split.py); block steps do not cover them."""
     s = ics.test_disk(500)
     n = len(s["px"])
     par = abi.make_params(0.5, 0.06, 8, False, False, "mixed")
+    ctx.call("gbh_state_upload", n, *[P(s[k]) for k in ("px", "py", "pz", "vx", "vy", "vz")], None, None, None,
+             P(s["mass"]), P(s["kind"]), P(s["alive"]))
     with pytest.raises(abi.GbhError) as ei:
-        ctx.call("gbh_step_kdk", par, 1e-3, 1, 0, n, *[P(s[k]) for k in ("px", "py", "pz", "vx", "vy", "vz", "ax",
-                                                                          "ay", "az")], P(s["mass"]), P(s["kind"]),
-                 P(s["alive"]))
+        ctx.step_block(par, 1e-2, 0.025, 6, 1)
     assert ei.value.code == abi.ERR_UNSUPPORTED
 
 

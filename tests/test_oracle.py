@@ -302,3 +302,60 @@ def test_adjoint_oracle_checkpoint_interval_does_not_change_bits():
         got = O.adjoint_direct(s, 5e-3, 0.02, 23, every, gx, gv, workers=1)
         for a, b in zip(ref, got):
             assert np.array_equal(a, b), every
+
+
+# ---- hole-aware split step (split.go, c = 0) ----
+
+def _three_body(r):
+    z = np.zeros(3)
+    return dict(px=np.array([0.0, r, 50.0]), py=z.copy(), pz=z.copy(), vx=z.copy(), vy=z.copy(), vz=z.copy(),
+                ax=z.copy(), ay=z.copy(), az=z.copy(), mass=np.array([2.0, 1e-6, 1e-6]),
+                kind=np.array([O.BLACK_HOLE, 0, 0], np.uint8), alive=np.ones(3, np.uint8))
+
+
+def test_split_substeps_follow_closest_encounter():  # accrete_test.go:122-143
+    far, far_near = O.split_kdk(_three_body(5.0), 0.004, 0.01, 0.5, 8, 1, workers=1)
+    close, close_near = O.split_kdk(_three_body(0.05), 0.004, 0.01, 0.5, 8, 1, workers=1)
+    assert far == 1 and not far_near.any()
+    assert close == 16 and list(close_near) == [False, True, False]
+
+
+def _energy(s, eps):
+    ke = 0.5 * np.sum(s["mass"] * (s["vx"] ** 2 + s["vy"] ** 2 + s["vz"] ** 2))
+    return ke + O.potential_exact(s["px"], s["py"], s["pz"], s["mass"], s["kind"], eps=eps)
+
+
+def test_split_energy_drift_comparable_to_direct():
+    """bh_test.go:165-184 with c = 0: 500 steps of the disk with two holes; the Barnes-Hut drift
+    stays within 2x the drift of the (tiny-theta, i.e. direct) run + 1e-4. With c = 0 the holes
+    pass through each other instead of merging, and that passage sets the drift of both runs."""
+    drift = []
+    for theta, leaf in ((1e-9, 24), (0.0, 0)):
+        s = ics.test_disk(2000)
+        e0 = _energy(s, 0.06)
+        O.split_kdk(s, 0.004, 0.06, theta, leaf, 500)
+        drift.append(abs((_energy(s, 0.06) - e0) / e0))
+    ref, got = drift
+    assert ref < 2e-2 and got <= 2 * ref + 1e-4, drift
+
+
+def test_split_conserves_momentum_with_exact_pairs():
+    """Both partners of every pair are kicked at the same times with the same force
+    (split.go:8-15): with tiny theta the total momentum is conserved to rounding."""
+    s = ics.test_disk(1500)
+    p0 = np.array([np.sum(s["mass"] * s[k]) for k in ("vx", "vy", "vz")])
+    scale = np.sum(s["mass"] * np.sqrt(s["vx"] ** 2 + s["vy"] ** 2 + s["vz"] ** 2))
+    O.split_kdk(s, 0.004, 0.06, 1e-9, 8, 40)
+    p1 = np.array([np.sum(s["mass"] * s[k]) for k in ("vx", "vy", "vz")])
+    assert np.abs(p1 - p0).max() < 1e-12 * scale
+
+
+def test_split_without_holes_is_the_plain_step():
+    s = ics.plummer(3000, seed=9)
+    a = {k: s[k].copy() for k in ("px", "py", "pz", "vx", "vy", "vz", "ax", "ay", "az", "mass")}
+    b = {k: s[k].copy() for k in a}
+    O.kdk(a, dt=1e-3, eps=0.01, theta=0.5, leaf=8, nsteps=4, workers=1)
+    sub, near = O.split_kdk(b, 1e-3, 0.01, 0.5, 8, 4, workers=1)
+    assert sub == 1 and not near.any()
+    for k in a:
+        assert np.array_equal(a[k], b[k]), k
