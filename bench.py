@@ -59,6 +59,22 @@ def workload_name(n, leaf):
             f"theta={THETA}, leaf={leaf}, eps={EPS}, dt={DT}, global KDK steps")
 
 
+def max_over_ranks(x: float, world: int, device: str) -> float:
+    """The largest x over the ranks of the default process group (x itself on one rank)."""
+    if world == 1:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_value(n: int, steps: int, ms_max: float, world: int) -> float:
+    """Whole-job particle-steps/s of `world` independent replicas, each advancing n particles by
+    `steps` steps, timed by the slowest rank (ms_max milliseconds)."""
+    return world * n * steps / (ms_max * 1e-3)
+
+
 def dist_env():
     return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
 
@@ -246,17 +262,12 @@ def run(args):
              "energy_method": "FP64 tree potential at theta 0.5 + FP64 kinetic (gbh_state_diagnostics)"}
     t_plain, w_plain, b_plain, _, _ = timed_steps("plain", args.steps, args.warmup)
 
-    # max over ranks
     def maxr(x):
-        if world == 1:
-            return x
-        tt = torch.tensor([x], dtype=torch.float64, device=f"cuda:{local}")
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        return float(tt.item())
+        return max_over_ranks(x, world, f"cuda:{local}")
 
     t_mixed, t_plain = maxr(t_mixed), maxr(t_plain)
-    value = world * n * args.steps / (t_mixed * 1e-3)
-    plain_value = world * n * args.steps / (t_plain * 1e-3)
+    value = replica_value(n, args.steps, t_mixed, world)
+    plain_value = replica_value(n, args.steps, t_plain, world)
 
     # end to end: host state in pinned memory, one gbh_step_kdk per step (copies inside)
     host = {k: torch.from_numpy(np.array(s[k], copy=True)).pin_memory() for k in (*FIELDS, "mass")}
@@ -282,7 +293,7 @@ def run(args):
         tm = ctx.timings()
         h2d, d2h = tm["h2d_bytes"], tm["d2h_bytes"]
     e2e_wall = maxr(e2e_wall)
-    e2e_value = world * n * args.steps / e2e_wall
+    e2e_value = replica_value(n, args.steps, e2e_wall * 1e3, world)
 
     # force errors of both walks against the FP64 direct sum on 4096 seeded targets
     rng = np.random.default_rng(1234)
@@ -351,9 +362,36 @@ def run(args):
 
 def run_profile(args):
     """A short launch sequence for ncu captures: upload the workload, then two force
-    evaluations with the chosen walk (tree build + walk each)."""
+    evaluations with the chosen walk (tree build + walk each). --profile adjoint runs one
+    forward + backward of the 32,768-body adjoint workload over 4 steps (checkpoints every 2);
+    --profile forest two force evaluations of the 64-system forest at the autotuner's choice
+    (theta 0.7, leaf 16, group 64)."""
     from gravitas_gb300 import abi
     P = abi.ptr
+    if args.profile == "adjoint":
+        from gravitas_gb300 import ics, sim
+        s, targets = ics.adjoint_problem(ADJ_N, seed=0)
+        ctx = abi.Context(0)
+        loss, _, _, _ = sim.trajectory_loss_gradient(s, targets, ADJ_DT, ADJ_EPS, 4, 2, abi.ADJ_FP32, ctx)
+        t = ctx.timings()
+        print(json.dumps({"profile": "adjoint", "n": ADJ_N, "steps": 4, "loss": loss, "bwd_ms": t["total_ms"],
+                          "pair_ms": t["walk_ms"], "launches": t["launches"]}))
+        ctx.close()
+        return 0
+    if args.profile == "forest":
+        from gravitas_gb300 import ics
+        s, off = ics.forest(nsys=64, seed=0)
+        ctx = abi.Context(0)
+        ctx.forest_upload(off, s["px"], s["py"], s["pz"], s["vx"], s["vy"], s["vz"], s["mass"], s["kind"],
+                          s["alive"])
+        par = abi.make_params(0.7, EPS, 16, False, False, "mixed", group_size=64)
+        for _ in range(2):
+            ctx.call("gbh_state_accelerations", par)
+        t = ctx.timings()
+        print(json.dumps({"profile": "forest", "n": int(off[-1]), "build_ms": t["build_ms"], "walk_ms": t["walk_ms"],
+                          "nnodes": t["nnodes"], "launches": t["launches"]}))
+        ctx.close()
+        return 0
     n = args.n
     s = make_workload(n, seed=0)
     ctx = abi.Context(0)
@@ -558,7 +596,7 @@ def main():
     ap.add_argument("--n", type=int, default=N_DEFAULT)
     ap.add_argument("--leaf", type=int, default=0,
                     help="leaf size; 0 (default) lets the autotuner choose for each walk")
-    ap.add_argument("--profile", choices=["mixed", "plain", "fp64"], default=None,
+    ap.add_argument("--profile", choices=["mixed", "plain", "fp64", "adjoint", "forest"], default=None,
                     help="run only two force evaluations with this walk (for ncu captures)")
     ap.add_argument("--workload", choices=["merger", "adjoint", "forest"], default="merger",
                     help="adjoint: the differentiable workload (gbh_fwd_save / gbh_bwd); forest: 64 systems in "

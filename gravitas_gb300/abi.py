@@ -36,6 +36,7 @@ class Params(ctypes.Structure):
 
 
 CFG_NO_GRAPHS = 1
+CFG_BLOCKING_SYNC = 2
 
 
 class Config(ctypes.Structure):

@@ -76,6 +76,8 @@ struct gbh_ctx {
     gbh::SplitBufs split;             // buffers of the hole-aware step
     std::vector<int32_t> hole_list;   // alive holes of the resident state, ascending
     bool use_graphs = true;
+    cudaEvent_t wait_ev = nullptr;  // GBH_CFG_BLOCKING_SYNC: host waits sleep on this event
+    cudaEvent_t ahead[4] = {};      // GBH_CFG_BLOCKING_SYNC: ends of the last steps launched
     bool capturing = false;  // stage events become graph event-record nodes
     // bookkeeping
     int64_t launches = 0;
@@ -173,6 +175,25 @@ int begin(gbh_ctx *ctx) {
 
 Launch launch_of(gbh_ctx *ctx) { return Launch{ctx->stream, &ctx->launches, ctx->num_sms}; }
 
+// Waits for the context's stream: a spin in the driver by default, a sleep on a blocking-sync
+// event with GBH_CFG_BLOCKING_SYNC (the waiting thread then leaves its core to other work).
+cudaError_t wait_stream(gbh_ctx *ctx) {
+    if (!ctx->wait_ev) return cudaStreamSynchronize(ctx->stream);
+    cudaError_t e = cudaEventRecord(ctx->wait_ev, ctx->stream);
+    return e != cudaSuccess ? e : cudaEventSynchronize(ctx->wait_ev);
+}
+
+// Before launching step s: with GBH_CFG_BLOCKING_SYNC, sleep until step s - 4 has finished, so
+// that the driver's launch queue never fills (a full queue makes the launching thread spin).
+cudaError_t throttle_before(gbh_ctx *ctx, int64_t s) {
+    if (!ctx->wait_ev || s < 4) return cudaSuccess;
+    return cudaEventSynchronize(ctx->ahead[s % 4]);
+}
+
+cudaError_t throttle_after(gbh_ctx *ctx, int64_t s) {
+    return ctx->wait_ev ? cudaEventRecord(ctx->ahead[s % 4], ctx->stream) : cudaSuccess;
+}
+
 // Takes the next stage event of the call from the pool (creating it if needed).
 cudaError_t next_stage_event(gbh_ctx *ctx, cudaEvent_t *ev) {
     if (ctx->evused == ctx->evpool.size()) {
@@ -247,7 +268,7 @@ int finish(gbh_ctx *ctx, bool tree) {
     if (tree && ctx->tb.info) {
         CK(cudaMemcpyAsync(&ctx->info_host, ctx->tb.info, sizeof(DevInfo), cudaMemcpyDeviceToHost, ctx->stream));
     }
-    CK(cudaStreamSynchronize(ctx->stream));
+    CK(wait_stream(ctx));
     float ms = 0;
     gbh_timings &t = ctx->last;
     if (cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[5]) == cudaSuccess) t.total_ms = ms;
@@ -387,7 +408,7 @@ int run_split_steps(gbh_ctx *ctx, const gbh_params *p, double dt, int64_t nsteps
         // classify (split.go:41-81): the host needs the substep count
         CK(gbh::split_classify(L, sb, n, px, py, pz, ctx->mass, kind, eps2, 20.0 * dt));
         CK(cudaMemcpyAsync(sc, sb.scalars, sizeof sc, cudaMemcpyDeviceToHost, ctx->stream));
-        CK(cudaStreamSynchronize(ctx->stream));
+        CK(wait_stream(ctx));
         double tau_min;
         std::memcpy(&tau_min, &sc[0], sizeof tau_min);
         const int32_t nnear = int32_t(sc[1]);
@@ -436,6 +457,7 @@ int run_steps(gbh_ctx *ctx, const gbh_params *p, double dt, int64_t nsteps) {
             if (rc) return rc;
         }
         for (int64_t s = 0; s < nsteps; ++s) {
+            CK(throttle_before(ctx, s));
             for (int k = 0; k < 3; ++k) {
                 cudaEvent_t ev;
                 CK(next_stage_event(ctx, &ev));
@@ -443,17 +465,20 @@ int run_steps(gbh_ctx *ctx, const gbh_params *p, double dt, int64_t nsteps) {
             }
             CK(cudaGraphLaunch(g.exec, ctx->stream));
             ctx->launches += g.launches;
+            CK(throttle_after(ctx, s));
         }
         return GBH_OK;
     }
     double h = 0.5 * dt;
     for (int64_t s = 0; s < nsteps; ++s) {
+        CK(throttle_before(ctx, s));
         CK(gbh::kick_drift(L, n, h, dt, ctx->px, ctx->py, ctx->pz, ctx->vx, ctx->vy, ctx->vz, ctx->ax, ctx->ay,
                            ctx->az));
         int rc = forces(ctx, p, n, ctx->px, ctx->py, ctx->pz, ctx->mass, kind, alive, ctx->ax, ctx->ay, ctx->az, theta,
                         true);
         if (rc) return rc;
         CK(gbh::kick(L, n, h, ctx->vx, ctx->vy, ctx->vz, ctx->ax, ctx->ay, ctx->az));
+        CK(throttle_after(ctx, s));
     }
     return GBH_OK;
 }
@@ -492,7 +517,7 @@ int forces_active(gbh_ctx *ctx, const gbh_params *p, const uint8_t *kind, const 
 // Reads the device scalars (next event tick, active count) after the work issued so far.
 int read_info(gbh_ctx *ctx) {
     CK(cudaMemcpyAsync(&ctx->info_host, ctx->tb.info, sizeof(DevInfo), cudaMemcpyDeviceToHost, ctx->stream));
-    CK(cudaStreamSynchronize(ctx->stream));
+    CK(wait_stream(ctx));
     if (ctx->info_host.err)
         return fail(ctx, GBH_ERR_LIMIT, "device walk exceeded its step bound (kernel %d)", ctx->info_host.err_where);
     return GBH_OK;
@@ -622,6 +647,15 @@ int gbh_create(const gbh_config *cfg, gbh_ctx **out, char *err, int errlen) {
     gbh_ctx *c = new gbh_ctx();
     c->device = dev;
     c->use_graphs = !(cfg && (cfg->flags & GBH_CFG_NO_GRAPHS));
+    if (cfg && (cfg->flags & GBH_CFG_BLOCKING_SYNC)) {
+        e = cudaEventCreateWithFlags(&c->wait_ev, cudaEventBlockingSync | cudaEventDisableTiming);
+        for (auto &ev : c->ahead)
+            if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev, cudaEventBlockingSync | cudaEventDisableTiming);
+        if (e != cudaSuccess) {
+            gbh_destroy(c);
+            return report(GBH_ERR_CUDA, cudaGetErrorString(e));
+        }
+    }
     c->num_sms = prop.multiProcessorCount;
     if ((e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking)) != cudaSuccess) {
         delete c;
@@ -653,6 +687,9 @@ void gbh_destroy(gbh_ctx *c) {
     for (auto &ev : c->ev)
         if (ev) cudaEventDestroy(ev);
     for (auto &ev : c->evpool) cudaEventDestroy(ev);
+    if (c->wait_ev) cudaEventDestroy(c->wait_ev);
+    for (auto &ev : c->ahead)
+        if (ev) cudaEventDestroy(ev);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
 }
@@ -902,7 +939,7 @@ int gbh_state_diagnostics(gbh_ctx *ctx, const gbh_params *p, double c, gbh_diagn
                            !p->monopole_only, ctx->part, ctx->scalar));
     double u = 0;
     CK(cudaMemcpyAsync(&u, ctx->scalar, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
-    CK(cudaStreamSynchronize(ctx->stream));
+    CK(wait_stream(ctx));
     double sums[11];
     CK(gbh::diagnostics(L, n, ctx->px, ctx->py, ctx->pz, ctx->vx, ctx->vy, ctx->vz, ctx->mass, kind, c,
                         p->dark_matter_off, ctx->part, ctx->scalar));
@@ -1003,7 +1040,7 @@ int gbh_tree_export(gbh_ctx *ctx, uint64_t *keys, int32_t *order, gbh_node *node
         if (!ctx->tb.moments_exact) {  // FP32 upsweep: fill the FP64 fields from the walk records
             Launch L = launch_of(ctx);
             CK(gbh::export_fast_moments(L, ctx->tb));
-            CK(cudaStreamSynchronize(ctx->stream));
+            CK(wait_stream(ctx));
         }
         CK(cudaMemcpy(nodes, ctx->tb.nodes, sizeof(gbh_node) * size_t(cnt), cudaMemcpyDeviceToHost));
     }
@@ -1150,7 +1187,7 @@ int gbh_autotune(gbh_ctx *ctx, const gbh_params *base, const double *thetas, int
                            ctx->stream));
         CK(cudaMemcpyAsync(ctx->targets + ns, idx.data(), sizeof(int64_t) * size_t(ns), cudaMemcpyHostToDevice,
                            ctx->stream));
-        CK(cudaStreamSynchronize(ctx->stream));
+        CK(wait_stream(ctx));
     }
     const uint8_t *kd = ctx->state_has_kind ? ctx->kind : nullptr, *al = ctx->state_has_alive ? ctx->alive : nullptr;
     int32_t count = 0, best_k = -1, best_any = -1;
@@ -1173,7 +1210,7 @@ int gbh_autotune(gbh_ctx *ctx, const gbh_params *base, const double *thetas, int
                     rc = forces(ctx, &p, n, ctx->px, ctx->py, ctx->pz, ctx->mass, kd, al, ctx->ax, ctx->ay, ctx->az,
                                 theta_of(&p), forest);
                     if (rc) return rc;
-                    CK(cudaStreamSynchronize(ctx->stream));
+                    CK(wait_stream(ctx));
                     if (r < 0) continue;
                     float b0 = 0, w0 = 0;
                     CK(cudaEventElapsedTime(&b0, ctx->evpool[0], ctx->evpool[1]));
@@ -1195,7 +1232,7 @@ int gbh_autotune(gbh_ctx *ctx, const gbh_params *base, const double *thetas, int
                 CK(cudaGetLastError());
                 CK(cudaMemcpyAsync(got.data(), ctx->tout, sizeof(double) * 3 * size_t(ns), cudaMemcpyDeviceToHost,
                                    ctx->stream));
-                CK(cudaStreamSynchronize(ctx->stream));
+                CK(wait_stream(ctx));
                 std::vector<double> rerr;
                 for (int64_t q = 0; q < ns; ++q) {
                     double rx = ref[size_t(q)], ry = ref[size_t(ns + q)], rz = ref[size_t(2 * ns + q)];

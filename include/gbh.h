@@ -75,7 +75,11 @@ typedef struct {
 
 enum {
     /* Steps launch their kernels one by one instead of replaying a captured CUDA graph. */
-    GBH_CFG_NO_GRAPHS = 1
+    GBH_CFG_NO_GRAPHS = 1,
+    /* Host waits for the GPU sleep on a blocking-sync event instead of spinning, so a caller
+       thread blocked in a call (a goroutine running Accelerations while Hydro.Forces runs on
+       the other cores, gas.go:20-25) leaves its core free. */
+    GBH_CFG_BLOCKING_SYNC = 2
 };
 
 typedef struct {

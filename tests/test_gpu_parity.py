@@ -470,3 +470,31 @@ def test_autotune_needs_a_state():
         assert ei.value.code == abi.ERR_STATE
     finally:
         c.close()
+
+
+def test_blocking_sync_frees_the_waiting_thread():
+    """GBH_CFG_BLOCKING_SYNC: a thread waiting in a call sleeps instead of spinning (the process
+    uses far less CPU time than the call's wall time) and the results are unchanged."""
+    import time
+    s = ics.plummer(1 << 19, seed=31)
+    n = len(s["px"])
+    par = abi.make_params(0.5, 0.01, 8, False, False, "mixed")
+    out = {}
+    for flags in (0, abi.CFG_BLOCKING_SYNC):
+        c = abi.Context(0, flags)
+        try:
+            c.call("gbh_state_upload", n, *[P(s[k]) for k in ("px", "py", "pz", "vx", "vy", "vz")], None, None, None,
+                   P(s["mass"]), None, None)
+            c.call("gbh_state_step", par, 1e-3, 2)  # warm-up: allocation and graph capture
+            w0, c0 = time.perf_counter(), time.process_time()
+            c.call("gbh_state_step", par, 1e-3, 40)
+            wall, cpu = time.perf_counter() - w0, time.process_time() - c0
+            st = {k: np.zeros(n) for k in ("px", "vx", "ax")}
+            c.call("gbh_state_download", P(st["px"]), None, None, P(st["vx"]), None, None, P(st["ax"]), None, None)
+            out[flags] = (wall, cpu, st)
+        finally:
+            c.close()
+    wall, cpu, st = out[abi.CFG_BLOCKING_SYNC]
+    assert cpu < 0.5 * wall, (cpu, wall)
+    for k in st:
+        assert np.array_equal(st[k], out[0][2][k]), k
