@@ -86,6 +86,7 @@ struct TreeBufs {
     // sorted stars
     double *sx = nullptr, *sy = nullptr, *sz = nullptr, *sm = nullptr;
     float4 *st_hi = nullptr, *st_lo = nullptr;
+    float4 *st_off = nullptr;  // FP32 offset of each star from its leaf's centre of mass, and its mass
     // chain topology, indexed by sorted position
     uint32_t *chain_cnt = nullptr;  // nodes starting at each position, then the scan
     // pre-order node arrays (index p)

@@ -125,7 +125,8 @@ __global__ __launch_bounds__(kThreads) void k_upsweep_fast(const uint64_t *__res
                                                            const uint32_t *__restrict__ base,
                                                            const int32_t *__restrict__ pre_ref,
                                                            const float4 *__restrict__ st_hi,
-                                                           const float4 *__restrict__ st_lo, const gbh_node *nodes,
+                                                           const float4 *__restrict__ st_lo,
+                                                           float4 *__restrict__ st_off, const gbh_node *nodes,
                                                            const int32_t *__restrict__ n_parent,
                                                            const uint32_t *__restrict__ n_info, int32_t *n_arrive,
                                                            PNode *pn, MNode *mn, int2 *mr, bool plain_records,
@@ -178,6 +179,14 @@ __global__ __launch_bounds__(kThreads) void k_upsweep_fast(const uint64_t *__res
         }
         finish_fast(geo[sid_sorted ? sid_sorted[lo] : 0], q, rh.x, rh.y, rh.z, rl.x, rl.y, rl.z, ox, oy, oz, keys[lo],
                     int(n_info[r] & 0xffu), nodes, r, pn, mn, mr, plain_records);
+        // Each star's offset from the leaf's centre of mass, formed with the operations of the
+        // mixed walk's separation (com_hi - star_hi) + (com_lo - star_lo), negated: a star paired
+        // with itself then gets a separation of exactly 0 (IEEE addition is sign-symmetric).
+        for (int32_t j = lo; j < hi; ++j) {
+            float4 h = st_hi[j], l = st_lo[j];
+            st_off[j] = make_float4((h.x - q.hx) + (l.x - q.lx), (h.y - q.hy) + (l.y - q.ly),
+                                    (h.z - q.hz) + (l.z - q.lz), h.w);
+        }
     }
     int32_t cur = r;
     for (int guard = 0; guard <= kMaxLevel + 1; ++guard) {
@@ -258,7 +267,8 @@ cudaError_t upsweep_fast(const Launch &L, TreeBufs &b, bool plain_records) {
     const uint32_t *cnt = b.chain_cnt, *base = b.chain_cnt + b.cap_n;
     int64_t nb = (b.cap_n + kThreads - 1) / kThreads;
     k_upsweep_fast<<<unsigned(nb < 1 ? 1 : nb), kThreads, 0, L.stream>>>(
-        b.keys, b.info, b.leaves, cnt, base, b.pre_ref, b.st_hi, b.st_lo, b.nodes, b.n_parent, b.n_info, b.n_arrive,
+        b.keys, b.info, b.leaves, cnt, base, b.pre_ref, b.st_hi, b.st_lo, b.st_off, b.nodes, b.n_parent, b.n_info,
+        b.n_arrive,
         b.pnodes, b.mnodes, b.mrange, plain_records, b.nsys > 1 ? b.sid_sorted : nullptr, b.geo, b.info);
     ++*L.count;
     return cudaGetLastError();

@@ -1314,7 +1314,7 @@ static cudaError_t scan_dyn(const Launch &L, const uint32_t *in, uint32_t *out, 
 
 void tree_free(TreeBufs &b) {
     void *ptrs[] = {b.flag, b.bbox_part, b.keys, b.keys_alt, b.order, b.order_alt, b.hist, b.sx, b.sy, b.sz, b.sm,
-                    b.st_hi, b.st_lo, b.chain_cnt, b.leaves, b.targets, b.geo, b.sid_sorted, b.groups, b.pre_parent, b.pre_info, b.pre_nchild, b.pre_mask, b.pre_ref, b.nodes,
+                    b.st_hi, b.st_lo, b.st_off, b.chain_cnt, b.leaves, b.targets, b.geo, b.sid_sorted, b.groups, b.pre_parent, b.pre_info, b.pre_nchild, b.pre_mask, b.pre_ref, b.nodes,
                     b.n_parent, b.n_info, b.n_arrive, b.pnodes, b.mnodes, b.mrange, b.scan_tmp, b.info};
     for (void *p : ptrs)
         if (p) cudaFree(p);
@@ -1363,6 +1363,7 @@ cudaError_t tree_alloc(TreeBufs &b, int64_t n, int leaf, int32_t nsys) {
     GBH_ALLOC(b.sm, cn);
     GBH_ALLOC(b.st_hi, cn);
     GBH_ALLOC(b.st_lo, cn);
+    GBH_ALLOC(b.st_off, cn);
     GBH_ALLOC(b.chain_cnt, cn * 2);  // counts, then their scan
     GBH_ALLOC(b.leaves, cn);
     GBH_ALLOC(b.targets, cn);

@@ -127,10 +127,11 @@ __device__ __forceinline__ void kahan_fold2(float2 &s, float2 &c, float2 &part) 
 }
 
 template <bool kQuad, bool kSoft>
-__global__ __launch_bounds__(kMixedThreads) void k_walk_mixed2(const DevInfo *info, const MNode *__restrict__ nodes,
+__global__ __launch_bounds__(kMixedThreads, 8) void k_walk_mixed2(const DevInfo *info, const MNode *__restrict__ nodes,
                                                                const int2 *__restrict__ ranges,
                                                                const float4 *__restrict__ st_hi,
                                                                const float4 *__restrict__ st_lo,
+                                                               const float4 *__restrict__ st_off,
                                                                const int32_t *__restrict__ order, float eps2,
                                                                double *ax, double *ay, double *az,
                                                                const int32_t *__restrict__ targets,
@@ -214,21 +215,24 @@ __global__ __launch_bounds__(kMixedThreads) void k_walk_mixed2(const DevInfo *in
                 if (lane == 0) set_err(err_info, 5);
                 break;
             }
+            // Leaf stars: separation = (leaf com - star) + (leaf star - com), the first the visit's
+            // double-float separation, the second the star's FP32 offset stored by the upsweep.
             for (int j = r.x; j < r.y; ++j) {
-                const float4 sh = st_hi[j], sl = st_lo[j];
-                const float2 ex = add2(add2(f2(sh.x), nhx), add2(f2(sl.x), nlx));
-                const float2 ey = add2(add2(f2(sh.y), nhy), add2(f2(sl.y), nly));
-                const float2 ez = add2(add2(f2(sh.z), nhz), add2(f2(sl.z), nlz));
+                const float4 so = st_off[j];
+                const float2 ex = add2(dx, f2(so.x));
+                const float2 ey = add2(dy, f2(so.y));
+                const float2 ez = add2(dz, f2(so.z));
                 const float2 r2 = fma2(ez, ez, fma2(ey, ey, fma2(ex, ex, e2)));
-                // A star paired with itself gives a zero separation: with eps2 > 0 that adds 0, as
-                // skipping j == self does (bh.go:191-193). Without softening r2 = 0 is masked.
+                // A star paired with itself gives a separation of exactly 0 (its offset is the exact
+                // negative of the visit's separation): with eps2 > 0 that adds 0, as skipping
+                // j == self does (bh.go:191-193). Without softening r2 = 0 is masked.
                 float2 ir;
                 if (kSoft) {
                     ir = make_float2(rsqrtf(r2.x), rsqrtf(r2.y));
                 } else {
                     ir = make_float2(r2.x > 0.f ? rsqrtf(r2.x) : 0.f, r2.y > 0.f ? rsqrtf(r2.y) : 0.f);
                 }
-                const float2 f = mul2(mul2(f2(sh.w), ir), mul2(ir, ir));
+                const float2 f = mul2(mul2(f2(so.w), ir), mul2(ir, ir));
                 px = fma2(f, ex, px);
                 py = fma2(f, ey, py);
                 pz = fma2(f, ez, pz);
@@ -303,7 +307,8 @@ static cudaError_t launch_mixed(const Launch &L, const TreeBufs &b, int64_t nsta
     int64_t groups = forest ? b.cap_groups : (nstars_cap + gsize - 1) / gsize;
     int64_t blocks = (groups + kMixedThreads / 32 - 1) / (kMixedThreads / 32);
     k_walk_mixed2<kQuad, kSoft><<<unsigned(blocks < 1 ? 1 : blocks), kMixedThreads, 0, L.stream>>>(
-        b.info, b.mnodes, b.mrange, b.st_hi, b.st_lo, b.order, eps2, ax, ay, az, targets ? b.targets : nullptr,
+        b.info, b.mnodes, b.mrange, b.st_hi, b.st_lo, b.st_off, b.order, eps2, ax, ay, az,
+        targets ? b.targets : nullptr,
         forest ? b.groups : nullptr, gsize == 64 ? 1 : 0, b.info);
     ++*L.count;
     return cudaGetLastError();
