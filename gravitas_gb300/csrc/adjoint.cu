@@ -149,48 +149,71 @@ __global__ void k_prep32(int64_t n, const double *__restrict__ px, const double 
     if (w) w[i] = make_float4(__double2float_rn(wx[i]), __double2float_rn(wy[i]), __double2float_rn(wz[i]), 0.f);
 }
 
+__device__ __forceinline__ float2 f2(float v) { return make_float2(v, v); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+
+__device__ __forceinline__ void fold2(float2 &s, float2 &comp, float2 x) {
+    fold(s.x, comp.x, x.x);
+    fold(s.y, comp.y, x.y);
+}
+
+// Each thread owns two targets, i0 and i0 + kPairThreads, whose arithmetic runs as one packed
+// FP32x2 operation (__fadd2_rn / __fmul2_rn / __ffma2_rn); a block covers kPairTargets targets.
+constexpr int kPairTargets = 2 * kPairThreads;
+
 // part[(split * 3 + axis) * n + i]: the accelerations of target i from the sources of one split.
 __global__ void __launch_bounds__(kPairThreads) k_force32(int64_t n, int64_t chunk, const float4 *__restrict__ hi,
                                                           const float4 *__restrict__ lo, float eps2,
                                                           double *part) {
     __shared__ float4 shi[kPairThreads], slo[kPairThreads];
-    int64_t i = int64_t(blockIdx.x) * kPairThreads + threadIdx.x;
-    bool act = i < n;
-    float4 h = act ? hi[i] : make_float4(0.f, 0.f, 0.f, 0.f);
-    float4 l = act ? lo[i] : make_float4(0.f, 0.f, 0.f, 0.f);
-    float ax = 0.f, ay = 0.f, az = 0.f, cx = 0.f, cy = 0.f, cz = 0.f;
+    const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+    const int64_t i0 = int64_t(blockIdx.x) * kPairTargets + threadIdx.x, i1 = i0 + kPairThreads;
+    const bool a0 = i0 < n, a1 = i1 < n;
+    const float4 h0 = a0 ? hi[i0] : z4, h1 = a1 ? hi[i1] : z4, l0 = a0 ? lo[i0] : z4, l1 = a1 ? lo[i1] : z4;
+    // negated target coordinates, so separations are sums
+    const float2 nhx = make_float2(-h0.x, -h1.x), nhy = make_float2(-h0.y, -h1.y), nhz = make_float2(-h0.z, -h1.z);
+    const float2 nlx = make_float2(-l0.x, -l1.x), nly = make_float2(-l0.y, -l1.y), nlz = make_float2(-l0.z, -l1.z);
+    const float2 e2 = f2(eps2);
+    float2 ax = f2(0.f), ay = f2(0.f), az = f2(0.f), cx = f2(0.f), cy = f2(0.f), cz = f2(0.f);
     int64_t jb = int64_t(blockIdx.y) * chunk, je = jb + chunk < n ? jb + chunk : n;
     for (int64_t j0 = jb; j0 < je; j0 += kPairThreads) {
         int64_t j = j0 + threadIdx.x;
         // padding sources have zero mass at the origin: s^2 >= eps^2 > 0, so they add exactly 0
-        shi[threadIdx.x] = j < je ? hi[j] : make_float4(0.f, 0.f, 0.f, 0.f);
-        slo[threadIdx.x] = j < je ? lo[j] : make_float4(0.f, 0.f, 0.f, 0.f);
+        shi[threadIdx.x] = j < je ? hi[j] : z4;
+        slo[threadIdx.x] = j < je ? lo[j] : z4;
         __syncthreads();
-        float tx = 0.f, ty = 0.f, tz = 0.f;
+        float2 tx = f2(0.f), ty = f2(0.f), tz = f2(0.f);
 #pragma unroll 8
         for (int q = 0; q < kPairThreads; ++q) {
-            float4 sh = shi[q], sl = slo[q];
+            const float4 sh = shi[q], sl = slo[q];
             // j == i gives d == 0 exactly and adds nothing
-            float dx = (sh.x - h.x) + (sl.x - l.x);
-            float dy = (sh.y - h.y) + (sl.y - l.y);
-            float dz = (sh.z - h.z) + (sl.z - l.z);
-            float s2 = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, eps2)));
-            float r = rsqrtf(s2);
-            float f = (sh.w * r) * (r * r);
-            tx = fmaf(f, dx, tx);
-            ty = fmaf(f, dy, ty);
-            tz = fmaf(f, dz, tz);
+            const float2 dx = add2(add2(f2(sh.x), nhx), add2(f2(sl.x), nlx));
+            const float2 dy = add2(add2(f2(sh.y), nhy), add2(f2(sl.y), nly));
+            const float2 dz = add2(add2(f2(sh.z), nhz), add2(f2(sl.z), nlz));
+            const float2 s2 = fma2(dx, dx, fma2(dy, dy, fma2(dz, dz, e2)));
+            const float2 r = make_float2(rsqrtf(s2.x), rsqrtf(s2.y));
+            const float2 f = mul2(mul2(f2(sh.w), r), mul2(r, r));
+            tx = fma2(f, dx, tx);
+            ty = fma2(f, dy, ty);
+            tz = fma2(f, dz, tz);
         }
         __syncthreads();
-        fold(ax, cx, tx);
-        fold(ay, cy, ty);
-        fold(az, cz, tz);
+        fold2(ax, cx, tx);
+        fold2(ay, cy, ty);
+        fold2(az, cz, tz);
     }
-    if (act) {
-        double *p = part + int64_t(blockIdx.y) * 3 * n;
-        p[i] = double(ax) + double(cx);
-        p[n + i] = double(ay) + double(cy);
-        p[2 * n + i] = double(az) + double(cz);
+    double *p = part + int64_t(blockIdx.y) * 3 * n;
+    if (a0) {
+        p[i0] = double(ax.x) + double(cx.x);
+        p[n + i0] = double(ay.x) + double(cy.x);
+        p[2 * n + i0] = double(az.x) + double(cz.x);
+    }
+    if (a1) {
+        p[i1] = double(ax.y) + double(cx.y);
+        p[n + i1] = double(ay.y) + double(cy.y);
+        p[2 * n + i1] = double(az.y) + double(cz.y);
     }
 }
 
@@ -199,56 +222,69 @@ __global__ void __launch_bounds__(kPairThreads) k_vjp32(int64_t n, int64_t chunk
                                                         const float4 *__restrict__ lo,
                                                         const float4 *__restrict__ w, float eps2, double *part) {
     __shared__ float4 shi[kPairThreads], slo[kPairThreads], sw[kPairThreads];
-    int64_t i = int64_t(blockIdx.x) * kPairThreads + threadIdx.x;
-    bool act = i < n;
-    float4 h = act ? hi[i] : make_float4(0.f, 0.f, 0.f, 0.f);
-    float4 l = act ? lo[i] : make_float4(0.f, 0.f, 0.f, 0.f);
-    float4 wi = act ? w[i] : make_float4(0.f, 0.f, 0.f, 0.f);
-    float gx = 0.f, gy = 0.f, gz = 0.f, gm = 0.f, cx = 0.f, cy = 0.f, cz = 0.f, cm = 0.f;
+    const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+    const int64_t i0 = int64_t(blockIdx.x) * kPairTargets + threadIdx.x, i1 = i0 + kPairThreads;
+    const bool a0 = i0 < n, a1 = i1 < n;
+    const float4 h0 = a0 ? hi[i0] : z4, h1 = a1 ? hi[i1] : z4, l0 = a0 ? lo[i0] : z4, l1 = a1 ? lo[i1] : z4;
+    const float4 w0 = a0 ? w[i0] : z4, w1 = a1 ? w[i1] : z4;
+    const float2 nhx = make_float2(-h0.x, -h1.x), nhy = make_float2(-h0.y, -h1.y), nhz = make_float2(-h0.z, -h1.z);
+    const float2 nlx = make_float2(-l0.x, -l1.x), nly = make_float2(-l0.y, -l1.y), nlz = make_float2(-l0.z, -l1.z);
+    const float2 mi = make_float2(h0.w, h1.w);
+    const float2 wix = make_float2(w0.x, w1.x), wiy = make_float2(w0.y, w1.y), wiz = make_float2(w0.z, w1.z);
+    const float2 e2 = f2(eps2);
+    float2 gx = f2(0.f), gy = f2(0.f), gz = f2(0.f), gm = f2(0.f);
+    float2 cx = f2(0.f), cy = f2(0.f), cz = f2(0.f), cm = f2(0.f);
     int64_t jb = int64_t(blockIdx.y) * chunk, je = jb + chunk < n ? jb + chunk : n;
     for (int64_t j0 = jb; j0 < je; j0 += kPairThreads) {
         int64_t j = j0 + threadIdx.x;
         // padding sources: zero mass and zero weight, so u == 0 and w_j . d == 0
-        shi[threadIdx.x] = j < je ? hi[j] : make_float4(0.f, 0.f, 0.f, 0.f);
-        slo[threadIdx.x] = j < je ? lo[j] : make_float4(0.f, 0.f, 0.f, 0.f);
-        sw[threadIdx.x] = j < je ? w[j] : make_float4(0.f, 0.f, 0.f, 0.f);
+        shi[threadIdx.x] = j < je ? hi[j] : z4;
+        slo[threadIdx.x] = j < je ? lo[j] : z4;
+        sw[threadIdx.x] = j < je ? w[j] : z4;
         __syncthreads();
-        float tx = 0.f, ty = 0.f, tz = 0.f, tm = 0.f;
+        float2 tx = f2(0.f), ty = f2(0.f), tz = f2(0.f), tm = f2(0.f);
 #pragma unroll 4
         for (int q = 0; q < kPairThreads; ++q) {
-            float4 sh = shi[q], sl = slo[q], wj = sw[q];
-            float dx = (sh.x - h.x) + (sl.x - l.x);
-            float dy = (sh.y - h.y) + (sl.y - l.y);
-            float dz = (sh.z - h.z) + (sl.z - l.z);
-            float s2 = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, eps2)));
-            float r = rsqrtf(s2);
-            float r2 = r * r;
-            float inv3 = r2 * r;
-            float inv5 = inv3 * r2;
-            // separate products: for j == i both are equal and u is exactly 0
-            float ux = h.w * wj.x - sh.w * wi.x;
-            float uy = h.w * wj.y - sh.w * wi.y;
-            float uz = h.w * wj.z - sh.w * wi.z;
-            float du = fmaf(dx, ux, fmaf(dy, uy, dz * uz));
-            float t = 3.f * du * inv5;
-            tx = fmaf(-dx, t, fmaf(ux, inv3, tx));
-            ty = fmaf(-dy, t, fmaf(uy, inv3, ty));
-            tz = fmaf(-dz, t, fmaf(uz, inv3, tz));
-            float pw = fmaf(wj.x, dx, fmaf(wj.y, dy, wj.z * dz));
-            tm = fmaf(-pw, inv3, tm);
+            const float4 sh = shi[q], sl = slo[q], wj = sw[q];
+            const float2 dx = add2(add2(f2(sh.x), nhx), add2(f2(sl.x), nlx));
+            const float2 dy = add2(add2(f2(sh.y), nhy), add2(f2(sl.y), nly));
+            const float2 dz = add2(add2(f2(sh.z), nhz), add2(f2(sl.z), nlz));
+            const float2 s2 = fma2(dx, dx, fma2(dy, dy, fma2(dz, dz, e2)));
+            const float2 r = make_float2(rsqrtf(s2.x), rsqrtf(s2.y));
+            const float2 r2 = mul2(r, r);
+            const float2 inv3 = mul2(r2, r);
+            const float2 inv5 = mul2(inv3, r2);
+            // u = m_i w_j - m_j w_i from two rounded products: for j == i they cancel exactly
+            const float2 nmj = f2(-sh.w);
+            const float2 ux = add2(mul2(mi, f2(wj.x)), mul2(nmj, wix));
+            const float2 uy = add2(mul2(mi, f2(wj.y)), mul2(nmj, wiy));
+            const float2 uz = add2(mul2(mi, f2(wj.z)), mul2(nmj, wiz));
+            const float2 du = fma2(dx, ux, fma2(dy, uy, mul2(dz, uz)));
+            const float2 nt = mul2(mul2(f2(-3.f), du), inv5);
+            tx = fma2(dx, nt, fma2(ux, inv3, tx));
+            ty = fma2(dy, nt, fma2(uy, inv3, ty));
+            tz = fma2(dz, nt, fma2(uz, inv3, tz));
+            const float2 pw = fma2(f2(wj.x), dx, fma2(f2(wj.y), dy, mul2(f2(wj.z), dz)));
+            tm = fma2(pw, inv3, tm);  // the mass term is -sum pw inv3: negated at the end
         }
         __syncthreads();
-        fold(gx, cx, tx);
-        fold(gy, cy, ty);
-        fold(gz, cz, tz);
-        fold(gm, cm, tm);
+        fold2(gx, cx, tx);
+        fold2(gy, cy, ty);
+        fold2(gz, cz, tz);
+        fold2(gm, cm, tm);
     }
-    if (act) {
-        double *p = part + int64_t(blockIdx.y) * 4 * n;
-        p[i] = double(gx) + double(cx);
-        p[n + i] = double(gy) + double(cy);
-        p[2 * n + i] = double(gz) + double(cz);
-        p[3 * n + i] = double(gm) + double(cm);
+    double *p = part + int64_t(blockIdx.y) * 4 * n;
+    if (a0) {
+        p[i0] = double(gx.x) + double(cx.x);
+        p[n + i0] = double(gy.x) + double(cy.x);
+        p[2 * n + i0] = double(gz.x) + double(cz.x);
+        p[3 * n + i0] = -(double(gm.x) + double(cm.x));
+    }
+    if (a1) {
+        p[i1] = double(gx.y) + double(cx.y);
+        p[n + i1] = double(gy.y) + double(cy.y);
+        p[2 * n + i1] = double(gz.y) + double(cz.y);
+        p[3 * n + i1] = -(double(gm.y) + double(cm.y));
     }
 }
 
@@ -385,7 +421,7 @@ cudaError_t force(const Launch &L, AdjTape &t, const double *x, const double *y,
                                                           nullptr);
     ADJ_LAUNCH_CHECK();
     if ((e = mark(t))) return e;
-    dim3 grid(unsigned((t.n + kPairThreads - 1) / kPairThreads), unsigned(t.nsplit));
+    dim3 grid(unsigned((t.n + kPairTargets - 1) / kPairTargets), unsigned(t.nsplit));
     k_force32<<<grid, kPairThreads, 0, L.stream>>>(t.n, t.chunk, t.hi, t.lo, float(t.eps2), t.part);
     ADJ_LAUNCH_CHECK();
     return mark(t);
@@ -427,7 +463,7 @@ cudaError_t vjp(const Launch &L, AdjTape &t, const double *x, double c, bool dri
                                                         lam + 5 * n, t.hi, t.lo, t.w);
     ADJ_LAUNCH_CHECK();
     if ((e = mark(t))) return e;
-    dim3 grid(unsigned((n + kPairThreads - 1) / kPairThreads), unsigned(t.nsplit));
+    dim3 grid(unsigned((n + kPairTargets - 1) / kPairTargets), unsigned(t.nsplit));
     k_vjp32<<<grid, kPairThreads, 0, L.stream>>>(n, t.chunk, t.hi, t.lo, t.w, float(t.eps2), t.part);
     ADJ_LAUNCH_CHECK();
     if ((e = mark(t))) return e;
@@ -448,8 +484,8 @@ cudaError_t adj_reserve(AdjTape &t, int64_t n, int64_t nsteps, int64_t every, do
     t.valid = false;
     int64_t nck = (nsteps + every - 1) / every;
     int64_t seg = std::min(every, nsteps);
-    // j splits: about 8 blocks of kPairThreads per SM, each split at least 4 tiles long
-    int64_t nb = (n + kPairThreads - 1) / kPairThreads;
+    // j splits: about 8 blocks per SM, each split at least 4 tiles long
+    int64_t nb = (n + kPairTargets - 1) / kPairTargets;
     int64_t ns = fp32 ? std::max<int64_t>(1, (8 * int64_t(num_sms) + nb - 1) / nb) : 1;
     ns = std::min<int64_t>(ns, std::max<int64_t>(1, n / (4 * kPairThreads)));
     ns = std::min<int64_t>(ns, 64);
