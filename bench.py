@@ -587,6 +587,49 @@ def run_forest(args):
     return 0
 
 
+def run_scaling(args):
+    """Throughput against N on one GPU: equal-mass Plummer spheres of 1M, 4M, 16M and 64M bodies
+    (eps 0.01, theta 0.5, leaf 32, 64-star groups, dt 1e-3), global KDK steps of the mixed walk
+    with the state resident in HBM. For each N: device ms per step split into build and walk,
+    particle-steps/s, and the device memory the library holds. One line of JSON."""
+    import torch
+
+    from gravitas_gb300 import abi, ics
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    P = abi.ptr
+    rows = []
+    for n in args.sizes:
+        s = ics.plummer(n, seed=0)
+        ctx = abi.Context(local)
+        free0, total = torch.cuda.mem_get_info(local)
+        ctx.call("gbh_state_upload", n, *[P(s[k]) for k in ("px", "py", "pz", "vx", "vy", "vz")], None, None, None,
+                 P(s["mass"]), None, None)
+        par = abi.make_params(THETA, 0.01, 32, False, False, "mixed", group_size=64)
+        for _ in range(max(args.warmup, 1)):
+            ctx.call("gbh_state_step", par, DT, 1)
+        tot = walk = build = 0.0
+        for _ in range(args.steps):
+            ctx.call("gbh_state_step", par, DT, 1)
+            t = ctx.timings()
+            tot += t["total_ms"]
+            walk += t["walk_ms"]
+            build += t["build_ms"]
+        free1, _ = torch.cuda.mem_get_info(local)
+        rows.append({"n": n, "ms_per_step": tot / args.steps, "walk_ms": walk / args.steps,
+                     "build_ms": build / args.steps, "particle_steps_per_s": n * args.steps / (tot * 1e-3),
+                     "device_gb": (free0 - free1) / 1e9, "nodes": t["nnodes"]})
+        ctx.close()
+        del s
+        if rank == 0:
+            print(json.dumps({"scaling_row": rows[-1]}), flush=True)
+    if rank == 0:
+        print(json.dumps({"metric": "particle-steps/s vs N, Plummer, theta 0.5, mixed walk", "unit": "particle-steps/s",
+                          "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "data": "synthetic",
+                          "rows": rows, "hbm_total_gb": total / 1e9}), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
@@ -598,15 +641,19 @@ def main():
                     help="leaf size; 0 (default) lets the autotuner choose for each walk")
     ap.add_argument("--profile", choices=["mixed", "plain", "fp64", "adjoint", "forest"], default=None,
                     help="run only two force evaluations with this walk (for ncu captures)")
-    ap.add_argument("--workload", choices=["merger", "adjoint", "forest"], default="merger",
+    ap.add_argument("--workload", choices=["merger", "adjoint", "forest", "scaling"], default="merger",
                     help="adjoint: the differentiable workload (gbh_fwd_save / gbh_bwd); forest: 64 systems in "
                          "one state with the autotuner; each prints its own JSON line")
     ap.add_argument("--fd-coords", type=int, default=16, help="adjoint: coordinates checked by central differences")
+    ap.add_argument("--sizes", type=int, nargs="+", default=[1 << 20, 1 << 22, 1 << 24, 1 << 26],
+                    help="scaling: body counts")
     args = ap.parse_args()
     if args.workload == "adjoint":
         return run_adjoint(args)
     if args.workload == "forest":
         return run_forest(args)
+    if args.workload == "scaling":
+        return run_scaling(args)
     if args.profile:
         return run_profile(args)
     if args.warmup < 3 and args.impl == "ours":
