@@ -34,6 +34,8 @@ struct gbh_ctx {
     int device = 0;
     int num_sms = 0;
     cudaStream_t stream = nullptr;
+    cudaStream_t copy_stream = nullptr;  // device-to-host copies that overlap the walk
+    cudaEvent_t copy_done = nullptr;
     cudaEvent_t ev[6] = {};
     gbh::TreeBufs tb;
     // resident state (state order)
@@ -667,6 +669,11 @@ int gbh_create(const gbh_config *cfg, gbh_ctx **out, char *err, int errlen) {
             return report(GBH_ERR_CUDA, cudaGetErrorString(e));
         }
     }
+    if ((e = cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking)) != cudaSuccess ||
+        (e = cudaEventCreateWithFlags(&c->copy_done, cudaEventDisableTiming)) != cudaSuccess) {
+        gbh_destroy(c);
+        return report(GBH_ERR_CUDA, cudaGetErrorString(e));
+    }
     *out = c;
     return report(GBH_OK, "");
 }
@@ -688,6 +695,11 @@ void gbh_destroy(gbh_ctx *c) {
         if (ev) cudaEventDestroy(ev);
     for (auto &ev : c->evpool) cudaEventDestroy(ev);
     if (c->wait_ev) cudaEventDestroy(c->wait_ev);
+    if (c->copy_stream) {
+        cudaStreamSynchronize(c->copy_stream);
+        cudaStreamDestroy(c->copy_stream);
+    }
+    if (c->copy_done) cudaEventDestroy(c->copy_done);
     for (auto &ev : c->ahead)
         if (ev) cudaEventDestroy(ev);
     if (c->stream) cudaStreamDestroy(c->stream);
@@ -826,7 +838,27 @@ int gbh_step_kdk(gbh_ctx *ctx, const gbh_params *p, double dt, int64_t nsteps, i
     ctx->last_substeps = 1;
     if (n > 0 && (rc = ctx->state_holes ? run_split_steps(ctx, p, dt, nsteps) : run_steps(ctx, p, dt, nsteps)))
         return rc;
-    if ((rc = download_state(ctx, px, py, pz, vx, vy, vz, ax, ay, az))) return rc;
+    if (n > 0 && ctx->evused >= 3) {
+        // The positions are final once the last force evaluation starts (its first stage event):
+        // copy them back on the copy stream while that tree build and walk run.
+        size_t b = sizeof(double) * size_t(n);
+        CK(cudaStreamWaitEvent(ctx->copy_stream, ctx->evpool[ctx->evused - 3], 0));
+        double *dst[3] = {px, py, pz};
+        const double *src[3] = {ctx->px, ctx->py, ctx->pz};
+        for (int k = 0; k < 3; ++k) {
+            CK(cudaMemcpyAsync(dst[k], src[k], b, cudaMemcpyDeviceToHost, ctx->copy_stream));
+            ctx->d2h += int64_t(b);
+        }
+        cudaError_t e = cudaEventRecord(ctx->copy_done, ctx->copy_stream);
+        if (e == cudaSuccess) rc = download_state(ctx, nullptr, nullptr, nullptr, vx, vy, vz, ax, ay, az);
+        if (e == cudaSuccess && rc == GBH_OK) e = cudaStreamWaitEvent(ctx->stream, ctx->copy_done, 0);
+        if (e != cudaSuccess || rc != GBH_OK) {
+            cudaStreamSynchronize(ctx->copy_stream);  // no copy into the caller's arrays after return
+            return rc != GBH_OK ? rc : fail(ctx, GBH_ERR_CUDA, "position copy: %s", cudaGetErrorString(e));
+        }
+    } else if ((rc = download_state(ctx, px, py, pz, vx, vy, vz, ax, ay, az))) {
+        return rc;
+    }
     return finish(ctx, n > 0);
 }
 
