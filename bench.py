@@ -46,8 +46,8 @@ METRIC = "particle-steps/s @N=1M θ=0.5: mixed vs plain GPU walk at RMS force er
 N_DEFAULT = 1 << 20
 THETA, EPS, DT = 0.5, 0.02, 1e-3
 # DRAM bytes (read + write) of one k_walk_mixed2 launch on this workload by leaf size, from the
-# ncu captures summarised in profiles/walk_mixed2_merger_1M_theta0.5_leaf*.md.
-WALK_TRAFFIC_BYTES = {8: 79_383_296, 16: 63_032_576, 24: 58_338_304}
+# ncu capture summarised in profiles/walk_mixed2_merger_1M_theta0.5_leaf32.md.
+WALK_TRAFFIC_BYTES = {32: 72_727_552}
 TUNE_LEAVES = [8, 12, 16, 24, 32]
 RMS_BOUND = 2e-3
 REFERENCE_LEAF = 24  # bh.go:67-68, the reference solver's default leaf size
