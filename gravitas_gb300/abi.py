@@ -64,7 +64,8 @@ class BlockStats(ctypes.Structure):
 class Diagnostics(ctypes.Structure):
     _fields_ = [("kinetic", ctypes.c_double), ("potential", ctypes.c_double), ("total", ctypes.c_double),
                 ("momentum", ctypes.c_double * 3), ("angular_momentum", ctypes.c_double * 3),
-                ("center_of_mass", ctypes.c_double * 3), ("mass", ctypes.c_double)]
+                ("center_of_mass", ctypes.c_double * 3), ("mass", ctypes.c_double), ("quality", ctypes.c_int32),
+                ("reserved", ctypes.c_int32)]
 
     def as_dict(self):
         return {k: (list(getattr(self, k)) if k in ("momentum", "angular_momentum", "center_of_mass")

@@ -958,17 +958,24 @@ int gbh_state_diagnostics(gbh_ctx *ctx, const gbh_params *p, double c, gbh_diagn
     if (!holes.empty()) CK(cudaMemcpy(ctx->holes, holes.data(), holes.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
     int leaf = leaf_of(p);
     double theta = std::min(theta_of(p), 0.9);
-    // the build zeroes alive holes' accelerations: use the force scratch of the potential path
     const bool forest = ctx->nsys > 1;
-    CK(gbh::tree_alloc(ctx->tb, n, leaf, ctx->nsys));
+    // TotalEnergy (diag.go:31-40): the exact pair sum up to exactEnergyLimit bodies, else the tree
+    const bool exact = !forest && n <= gbh::kExactEnergyLimit;
     CK(grow(ctx->scratch3, ctx->scratch3_cap, 3 * n));
     double *sa = ctx->scratch3;
-    CK(gbh::tree_build(L, ctx->tb, n, ctx->px, ctx->py, ctx->pz, ctx->mass, kind, alive, sa, sa + n, sa + 2 * n, theta,
-                       leaf, p->dark_matter_off, true, true, forest ? ctx->sys_of : nullptr,
-                       forest ? ctx->sys_off : nullptr));
-    CK(gbh::potential_fp64(L, ctx->tb, n, ctx->px, ctx->py, ctx->pz, ctx->mass, kind, alive, ctx->holes,
-                           int32_t(holes.size()), p->softening * p->softening, c, p->dark_matter_off,
-                           !p->monopole_only, ctx->part, ctx->scalar));
+    if (exact) {
+        CK(gbh::potential_exact_fp64(L, n, ctx->px, ctx->py, ctx->pz, ctx->mass, kind, p->softening * p->softening,
+                                     c, p->dark_matter_off, sa, ctx->scalar));
+    } else {
+        // the build zeroes alive holes' accelerations: use the force scratch of the potential path
+        CK(gbh::tree_alloc(ctx->tb, n, leaf, ctx->nsys));
+        CK(gbh::tree_build(L, ctx->tb, n, ctx->px, ctx->py, ctx->pz, ctx->mass, kind, alive, sa, sa + n, sa + 2 * n,
+                           theta, leaf, p->dark_matter_off, true, true, forest ? ctx->sys_of : nullptr,
+                           forest ? ctx->sys_off : nullptr));
+        CK(gbh::potential_fp64(L, ctx->tb, n, ctx->px, ctx->py, ctx->pz, ctx->mass, kind, alive, ctx->holes,
+                               int32_t(holes.size()), p->softening * p->softening, c, p->dark_matter_off,
+                               !p->monopole_only, ctx->part, ctx->scalar));
+    }
     double u = 0;
     CK(cudaMemcpyAsync(&u, ctx->scalar, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
     CK(wait_stream(ctx));
@@ -976,11 +983,12 @@ int gbh_state_diagnostics(gbh_ctx *ctx, const gbh_params *p, double c, gbh_diagn
     CK(gbh::diagnostics(L, n, ctx->px, ctx->py, ctx->pz, ctx->vx, ctx->vy, ctx->vz, ctx->mass, kind, c,
                         p->dark_matter_off, ctx->part, ctx->scalar));
     CK(cudaMemcpyAsync(sums, ctx->scalar, sizeof sums, cudaMemcpyDeviceToHost, ctx->stream));
-    rc = finish(ctx, true);
+    rc = finish(ctx, !exact);
     if (rc) return rc;
     out->kinetic = sums[0];
     out->potential = u;
     out->total = sums[0] + u;
+    out->quality = exact ? 2 : 1;
     for (int k = 0; k < 3; ++k) {
         out->momentum[k] = sums[1 + k];
         out->angular_momentum[k] = sums[4 + k];

@@ -175,6 +175,12 @@ cudaError_t potential_fp64(const Launch &L, const TreeBufs &b, int64_t n, const 
                            const uint8_t *kind, const uint8_t *alive, const int32_t *holes,
                            int32_t nholes, double eps2, double c, int dm_off, int quad,
                            double *part, double *u_dev);
+// Exact pair potential of all bodies (PotentialEnergyParallel, diag.go:42-62): rows (n doubles of
+// scratch) in ascending i, each over j > i ascending; result in *u_dev.
+constexpr int64_t kExactEnergyLimit = 30000;  // exactEnergyLimit, diag.go:16-19
+cudaError_t potential_exact_fp64(const Launch &L, int64_t n, const double *px, const double *py, const double *pz,
+                                 const double *mass, const uint8_t *kind, double eps2, double c, int dm_off,
+                                 double *rows, double *u_dev);
 // Sums of diag.go: out[0] kinetic (bodies that gravitate), out[1..3] momentum, out[4..6]
 // angular momentum, out[7..9] sum m x, out[10] mass. part holds diag_parts() x 11 doubles.
 int diag_parts();

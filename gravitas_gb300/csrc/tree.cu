@@ -1025,6 +1025,56 @@ __device__ __forceinline__ double pair_potential(double mi, double mj, double r2
     return mi * mj * (-2 / rs + 4 / (rs * rs) * (re - 1.5 * rs));
 }
 
+// PotentialEnergyParallel (diag.go:42-62): row i of the exact pair sum, sum over j > i of the
+// pair model's potential in ascending j, kinds and liveness as the reference reads them (all
+// bodies). The rows are then added in ascending i (the reference adds its ParallelFor chunks
+// in completion order, so only round-off may differ).
+__global__ __launch_bounds__(kDirThreads) void k_pot_exact_rows(int64_t n, const double *__restrict__ px,
+                                                                const double *__restrict__ py,
+                                                                const double *__restrict__ pz,
+                                                                const double *__restrict__ mass,
+                                                                const uint8_t *__restrict__ kind, double eps2, double c,
+                                                                int dm_off, double *rows) {
+    __shared__ double s_x[kDirThreads], s_y[kDirThreads], s_z[kDirThreads], s_m[kDirThreads];
+    __shared__ uint8_t s_k[kDirThreads];
+    const int64_t i0 = int64_t(blockIdx.x) * kDirThreads;
+    const int64_t i = i0 + threadIdx.x;
+    const bool act = i < n;
+    const uint8_t ki = act && kind ? kind[i] : 0;
+    const double xi = act ? px[i] : 0, yi = act ? py[i] : 0, zi = act ? pz[i] : 0, mi = act ? mass[i] : 0;
+    const double smi = dm_off && ki == GBH_DARK_MATTER ? 0.0 : mi;
+    double part = 0;
+    for (int64_t j0 = i0 + 1; j0 < n; j0 += kDirThreads) {
+        int64_t j = j0 + threadIdx.x;
+        if (j < n) {
+            s_x[threadIdx.x] = px[j];
+            s_y[threadIdx.x] = py[j];
+            s_z[threadIdx.x] = pz[j];
+            s_m[threadIdx.x] = mass[j];
+            s_k[threadIdx.x] = kind ? kind[j] : 0;
+        }
+        __syncthreads();
+        int cnt = n - j0 < kDirThreads ? int(n - j0) : kDirThreads;
+        for (int t = 0; t < cnt; ++t) {
+            if (j0 + t <= i) continue;
+            double dx = s_x[t] - xi, dy = s_y[t] - yi, dz = s_z[t] - zi;
+            uint8_t kj = s_k[t];
+            double rs = pair_rs(ki, mi, kj, s_m[t], c);
+            double smj = dm_off && kj == GBH_DARK_MATTER ? 0.0 : s_m[t];
+            part += pair_potential(smi, smj, dx * dx + dy * dy + dz * dz, eps2, rs);
+        }
+        __syncthreads();
+    }
+    if (act) rows[i] = part;
+}
+
+__global__ void k_pot_exact_final(int64_t n, const double *__restrict__ rows, double *out) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    double sum = 0;
+    for (int64_t i = 0; i < n; ++i) sum += rows[i];
+    *out = sum;
+}
+
 // holePotential, potential.go:84-96.
 __device__ double hole_potential(int64_t i, const double *px, const double *py, const double *pz, const double *mass,
                                  const uint8_t *kind, const int32_t *holes, int32_t nholes, double eps2, double c,
@@ -1552,6 +1602,17 @@ cudaError_t direct_fp64(const Launch &L, int64_t n, const double *px, const doub
     if (ntargets == 0 || n == 0) return cudaSuccess;
     k_direct_fp64<<<blocks_for(ntargets, kDirThreads), kDirThreads, 0, L.stream>>>(n, px, py, pz, mass, kind, eps2,
                                                                                   dm_off, targets, ntargets, ax, ay, az);
+    GBH_LAUNCH_CHECK();
+    return cudaSuccess;
+}
+
+cudaError_t potential_exact_fp64(const Launch &L, int64_t n, const double *px, const double *py, const double *pz,
+                                 const double *mass, const uint8_t *kind, double eps2, double c, int dm_off,
+                                 double *rows, double *u_dev) {
+    k_pot_exact_rows<<<blocks_for(n, kDirThreads), kDirThreads, 0, L.stream>>>(n, px, py, pz, mass, kind, eps2, c,
+                                                                               dm_off, rows);
+    GBH_LAUNCH_CHECK();
+    k_pot_exact_final<<<1, 32, 0, L.stream>>>(n, rows, u_dev);
     GBH_LAUNCH_CHECK();
     return cudaSuccess;
 }

@@ -217,12 +217,16 @@ int gbh_state_accelerations(gbh_ctx *ctx, const gbh_params *p);
    GPU. */
 typedef struct {
     double kinetic;             /* sourceKinetic: sum of m u^2 / (gamma + 1) over bodies that gravitate (diag.go:80-88) */
-    double potential;           /* tree potential at min(theta, 0.9) (potential.go:12-42) */
+    double potential;           /* exact pair sum for up to 30,000 bodies (PotentialEnergyParallel,
+                                   diag.go:42-62), else the tree potential at min(theta, 0.9)
+                                   (potential.go:12-42); forests always use the tree */
     double total;               /* kinetic + potential (TotalEnergy without gas, diag.go:43-51) */
     double momentum[3];         /* Momentum, all bodies (diag.go:89-96) */
     double angular_momentum[3]; /* AngularMomentum about the origin (diag.go:98-105) */
     double center_of_mass[3];   /* CenterOfMass (diag.go:107-120) */
     double mass;                /* its total mass */
+    int32_t quality;            /* EnergyQuality (diag.go:21-27): 2 exact, 1 tree estimate */
+    int32_t reserved;
 } gbh_diagnostics;
 
 /* Diagnostics of the resident state; c is the speed of light of the pair model (0: Newtonian). */

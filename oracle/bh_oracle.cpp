@@ -1317,29 +1317,24 @@ void orc_adjoint_direct(int64_t n, const double *px, const double *py, const dou
 double orc_potential_exact(int64_t n, const double *px, const double *py, const double *pz,
                            const double *mass, const uint8_t *kind, double eps, double c, int dm_off,
                            int workers) {
-    // diag.go:44-64; parts summed in chunk order.
+    // diag.go:42-62: each row i summed over j > i ascending, the rows added in ascending i (the
+    // reference adds its ParallelFor chunks in completion order, so only round-off may differ).
     double eps2 = eps * eps;
-    int64_t chunk = 64;
-    int64_t nch = (n + chunk - 1) / chunk;
-    std::vector<double> parts(nch, 0.0);
-    parallel_for(nch, 1, workers, [&](int64_t lo, int64_t hi) {
-        for (int64_t ci = lo; ci < hi; ++ci) {
-            double part = 0;
-            for (int64_t i = ci * chunk; i < std::min(n, (ci + 1) * chunk); ++i) {
-                double xi = px[i], yi = py[i], zi = pz[i];
-                for (int64_t j = i + 1; j < n; ++j) {
-                    double dx = px[j] - xi, dy = py[j] - yi, dz = pz[j] - zi;
-                    double rs = pair_rs(kind[i], mass[i], kind[j], mass[j], c);
-                    part += pair_potential(source_mass(kind[i], mass[i], dm_off),
-                                           source_mass(kind[j], mass[j], dm_off), dx * dx + dy * dy + dz * dz,
-                                           eps2, rs);
-                }
+    std::vector<double> rows(size_t(std::max<int64_t>(n, 0)), 0.0);
+    parallel_for(n, 64, workers, [&](int64_t lo, int64_t hi) {
+        for (int64_t i = lo; i < hi; ++i) {
+            double xi = px[i], yi = py[i], zi = pz[i], part = 0;
+            for (int64_t j = i + 1; j < n; ++j) {
+                double dx = px[j] - xi, dy = py[j] - yi, dz = pz[j] - zi;
+                double rs = pair_rs(kind[i], mass[i], kind[j], mass[j], c);
+                part += pair_potential(source_mass(kind[i], mass[i], dm_off), source_mass(kind[j], mass[j], dm_off),
+                                       dx * dx + dy * dy + dz * dz, eps2, rs);
             }
-            parts[ci] = part;
+            rows[size_t(i)] = part;
         }
     });
     double sum = 0;
-    for (double p : parts) sum += p;
+    for (double r : rows) sum += r;
     return sum;
 }
 

@@ -52,6 +52,7 @@ def test_params_layout_matches_header():
     assert ctypes.sizeof(abi.Params) == 40
     assert ctypes.sizeof(abi.AdjointParams) == 48
     assert ctypes.sizeof(abi.TuneEntry) == 64
+    assert ctypes.sizeof(abi.Diagnostics) == 112
     assert ctypes.sizeof(abi.Config) == 32
     assert ctypes.sizeof(abi.Timings) == 80
     assert abi.NODE_DTYPE.itemsize == 104

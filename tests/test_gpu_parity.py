@@ -295,6 +295,8 @@ def test_graph_replay_matches_plain_launches(ctx, walk):
 
 
 def test_diagnostics_match_oracle_and_sums(ctx):  # diag.go:31-120, potential.go:12-42
+    """1,502 bodies (two holes, c = 10): TotalEnergy's exact pair sum (n <= 30,000), bit for
+    bit against the oracle's restatement; the other sums against numpy."""
     g = np.load(os.path.join(GOLDEN, "disk.npz"))
     s = {k: g[k].copy() for k in ("px", "py", "pz", "vx", "vy", "vz", "mass", "kind", "alive")}
     n = len(s["px"])
@@ -308,7 +310,10 @@ def test_diagnostics_match_oracle_and_sums(ctx):  # diag.go:31-120, potential.go
     u2 = (v * v).sum(1)
     kin = (m * u2 / (np.sqrt(1 + u2 / c ** 2) + 1)).sum()
     assert abs(d["kinetic"] - kin) <= 1e-12 * abs(kin)
-    assert abs((d["potential"] - float(g["potential"])) / float(g["potential"])) <= 1e-12
+    assert d["quality"] == 2
+    assert d["potential"] == O.potential_exact(s["px"], s["py"], s["pz"], m, s["kind"], eps=float(g["eps"]), c=c)
+    # the exact sum and the tree estimate agree to the tree's accuracy
+    assert abs((d["potential"] - float(g["potential"])) / float(g["potential"])) <= 1e-3
     assert abs(d["total"] - (d["kinetic"] + d["potential"])) <= 1e-15 * abs(d["total"]) + 1e-300
     assert np.allclose(d["momentum"], (m[:, None] * v).sum(0), rtol=1e-12, atol=1e-14)
     assert np.allclose(d["angular_momentum"], (m[:, None] * np.cross(x, v)).sum(0), rtol=1e-12, atol=1e-14)
@@ -498,3 +503,22 @@ def test_blocking_sync_frees_the_waiting_thread():
     assert cpu < 0.5 * wall, (cpu, wall)
     for k in st:
         assert np.array_equal(st[k], out[0][2][k]), k
+
+
+def test_diagnostics_switch_to_the_tree_above_30000_bodies(ctx):
+    """diag.go:16-40: exact up to exactEnergyLimit = 30,000 bodies, the tree potential above."""
+    for n, quality in ((30000, 2), (30001, 1)):
+        s = ics.plummer(n, seed=41)
+        s["kind"][::97] = O.DARK_MATTER
+        ctx.call("gbh_state_upload", n, *[P(s[k]) for k in ("px", "py", "pz", "vx", "vy", "vz")], None, None, None,
+                 P(s["mass"]), P(s["kind"]), P(s["alive"]))
+        par = abi.make_params(0.5, 0.01, 8, False, True, "fp64")
+        d = ctx.diagnostics(par)
+        assert d["quality"] == quality
+        exact = O.potential_exact(s["px"], s["py"], s["pz"], s["mass"], s["kind"], eps=0.01, dm_off=True)
+        if quality == 2:
+            assert d["potential"] == exact
+        else:
+            t = O.Tree(s["px"], s["py"], s["pz"], s["mass"], s["kind"], s["alive"], theta=0.5, leaf=8, dm_off=True)
+            assert abs(d["potential"] - t.potential(0.01)) <= 1e-12 * abs(exact)
+            assert abs(d["potential"] - exact) <= 1e-4 * abs(exact)
