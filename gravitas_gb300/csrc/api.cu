@@ -121,6 +121,22 @@ cudaError_t grow(T *&p, int64_t &cap, int64_t need) {
     return e;
 }
 
+// Grow-only target list and its 3-column output (tout holds 3 x targets_cap doubles).
+cudaError_t grow_targets(gbh_ctx *c, int64_t need) {
+    if (need <= c->targets_cap && c->targets && c->tout) return cudaSuccess;
+    int64_t cap = 0;
+    cudaError_t e = grow(c->targets, cap, need);
+    if (e != cudaSuccess) {
+        c->targets_cap = 0;
+        return e;
+    }
+    if (c->tout) cudaFree(c->tout);
+    c->tout = nullptr;
+    e = cudaMalloc(&c->tout, sizeof(double) * 3 * size_t(cap));
+    c->targets_cap = e == cudaSuccess ? cap : 0;
+    return e;
+}
+
 void free_state(gbh_ctx *c) {
     void *ptrs[] = {c->px, c->py, c->pz, c->vx, c->vy, c->vz, c->ax, c->ay, c->az, c->mass, c->kind, c->alive};
     for (void *p : ptrs)
@@ -809,10 +825,7 @@ int gbh_direct_accelerations(gbh_ctx *ctx, const gbh_params *p, int64_t n, const
         (rc = h2d(ctx, ctx->mass, mass, b)))
         return rc;
     if (kind && (rc = h2d(ctx, ctx->kind, kind, size_t(n)))) return rc;
-    CK(grow(ctx->targets, ctx->targets_cap, ntargets));
-    CK(cudaFree(ctx->tout));
-    ctx->tout = nullptr;
-    CK(cudaMalloc(&ctx->tout, sizeof(double) * 3 * size_t(ctx->targets_cap)));
+    CK(grow_targets(ctx, ntargets));
     if (targets && (rc = h2d(ctx, ctx->targets, targets, sizeof(int64_t) * size_t(ntargets)))) return rc;
     double *tx = ctx->tout, *ty = tx + ctx->targets_cap, *tz = ty + ctx->targets_cap;
     Launch L = launch_of(ctx);
@@ -1196,10 +1209,7 @@ int gbh_autotune(gbh_ctx *ctx, const gbh_params *base, const double *thetas, int
         off.resize(size_t(ctx->nsys) + 1);
         CK(cudaMemcpy(off.data(), ctx->sys_off, sizeof(int64_t) * off.size(), cudaMemcpyDeviceToHost));
     }
-    CK(grow(ctx->targets, ctx->targets_cap, 2 * ns));
-    CK(cudaFree(ctx->tout));
-    ctx->tout = nullptr;
-    CK(cudaMalloc(&ctx->tout, sizeof(double) * 3 * size_t(ctx->targets_cap)));
+    CK(grow_targets(ctx, 2 * ns));
     Launch L = launch_of(ctx);
     const double eps2 = base->softening * base->softening;
     std::vector<int64_t> rel(static_cast<size_t>(ns));

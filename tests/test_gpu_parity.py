@@ -522,3 +522,46 @@ def test_diagnostics_switch_to_the_tree_above_30000_bodies(ctx):
             t = O.Tree(s["px"], s["py"], s["pz"], s["mass"], s["kind"], s["alive"], theta=0.5, leaf=8, dm_off=True)
             assert abs(d["potential"] - t.potential(0.01)) <= 1e-12 * abs(exact)
             assert abs(d["potential"] - exact) <= 1e-4 * abs(exact)
+
+
+def test_no_device_allocation_after_warm_up():
+    """The context owns grow-only device buffers: once every entry point has run on a state,
+    repeating the calls on the same sizes allocates nothing (the device's free memory stays)."""
+    torch = pytest.importorskip("torch")
+    s = ics.test_disk(3000)
+    n = len(s["px"])
+    F = ("px", "py", "pz", "vx", "vy", "vz", "ax", "ay", "az")
+    tg = np.arange(0, n, 5, dtype=np.int64)
+    out = [np.zeros(len(tg)) for _ in range(3)]
+    c = abi.Context(0)
+    try:
+        def every_call():
+            par = abi.make_params(0.5, 0.06, 8, False, False, "mixed")
+            a = [np.zeros(n) for _ in range(3)]
+            c.call("gbh_accelerations", par, n, P(s["px"]), P(s["py"]), P(s["pz"]), P(s["mass"]), P(s["kind"]),
+                   P(s["alive"]), P(a[0]), P(a[1]), P(a[2]))
+            c.call("gbh_direct_accelerations", par, n, P(s["px"]), P(s["py"]), P(s["pz"]), P(s["mass"]), P(s["kind"]),
+                   P(tg), len(tg), P(out[0]), P(out[1]), P(out[2]))
+            st = {k: s[k].copy() for k in F}
+            c.call("gbh_step_kdk", par, 4e-3, 2, 0, n, *[P(st[k]) for k in F], P(s["mass"]), P(s["kind"]),
+                   P(s["alive"]))
+            c.call("gbh_state_upload", n, *[P(s[k]) for k in ("px", "py", "pz", "vx", "vy", "vz")], None, None, None,
+                   P(s["mass"]), P(s["kind"]), P(s["alive"]))
+            c.call("gbh_state_step", par, 4e-3, 2)
+            c.diagnostics(par, c=0.0)
+            c.call("gbh_state_accelerations", par)
+            c.autotune(par, thetas=[0.5], leaves=[8, 16], groups=[64], sample=256, reps=1)
+            x0 = np.stack([s["px"], s["py"], s["pz"]], 1)
+            v0 = np.stack([s["vx"], s["vy"], s["vz"]], 1)
+            xT, _ = c.fwd_save(x0, v0, s["mass"], 1e-3, 0.06, 4, 2)
+            c.bwd(xT, None)
+        every_call()
+        every_call()
+        torch.cuda.synchronize()
+        free0 = torch.cuda.mem_get_info(0)[0]
+        for _ in range(3):
+            every_call()
+        torch.cuda.synchronize()
+        assert torch.cuda.mem_get_info(0)[0] == free0
+    finally:
+        c.close()
