@@ -790,16 +790,27 @@ int gbh_potential_energy(gbh_ctx *ctx, const gbh_params *p, int64_t n, const dou
     Launch L = launch_of(ctx);
     int leaf = leaf_of(p);
     double theta = std::min(theta_of(p), 0.9);  // diagTheta, potential.go:12-14
+    // FP64 walk: the reference's sums bit for bit; other walks: the mixed walk's potential
+    const bool fp64 = p->walk == GBH_WALK_FP64;
     CK(gbh::tree_alloc(ctx->tb, n, leaf, 1));
+    ctx->tb.group = 64;
     CK(gbh::tree_build(L, ctx->tb, n, ctx->px, ctx->py, ctx->pz, ctx->mass, kind ? ctx->kind : nullptr,
-                       alive ? ctx->alive : nullptr, ctx->ax, ctx->ay, ctx->az, theta, leaf, p->dark_matter_off, true));
+                       alive ? ctx->alive : nullptr, ctx->ax, ctx->ay, ctx->az, theta, leaf, p->dark_matter_off, fp64,
+                       false));
     int64_t nparts = (ctx->tb.cap_n + 255) / 256;
     CK(grow(ctx->part, ctx->part_cap, nparts));
     if (!ctx->scalar) CK(cudaMalloc(&ctx->scalar, 256));
     double eps2 = p->softening * p->softening;
-    CK(gbh::potential_fp64(L, ctx->tb, n, ctx->px, ctx->py, ctx->pz, ctx->mass, kind ? ctx->kind : nullptr,
-                           alive ? ctx->alive : nullptr, ctx->holes, int32_t(holes.size()), eps2, c,
-                           p->dark_matter_off, !p->monopole_only, ctx->part, ctx->scalar));
+    if (fp64) {
+        CK(gbh::potential_fp64(L, ctx->tb, n, ctx->px, ctx->py, ctx->pz, ctx->mass, kind ? ctx->kind : nullptr,
+                               alive ? ctx->alive : nullptr, ctx->holes, int32_t(holes.size()), eps2, c,
+                               p->dark_matter_off, !p->monopole_only, ctx->part, ctx->scalar));
+    } else {
+        CK(grow(ctx->scratch3, ctx->scratch3_cap, 3 * ctx->tb.cap_n));
+        CK(gbh::potential_mixed(L, ctx->tb, n, ctx->px, ctx->py, ctx->pz, ctx->mass, kind ? ctx->kind : nullptr,
+                                alive ? ctx->alive : nullptr, ctx->holes, int32_t(holes.size()), eps2, c,
+                                p->dark_matter_off, !p->monopole_only, ctx->scratch3, ctx->part, ctx->scalar));
+    }
     if ((rc = d2h(ctx, u, ctx->scalar, sizeof(double)))) return rc;
     return finish(ctx, true);
 }
@@ -980,14 +991,25 @@ int gbh_state_diagnostics(gbh_ctx *ctx, const gbh_params *p, double c, gbh_diagn
         CK(gbh::potential_exact_fp64(L, n, ctx->px, ctx->py, ctx->pz, ctx->mass, kind, p->softening * p->softening,
                                      c, p->dark_matter_off, sa, ctx->scalar));
     } else {
-        // the build zeroes alive holes' accelerations: use the force scratch of the potential path
+        // the build zeroes alive holes' accelerations: use the force scratch of the potential path.
+        // FP64 walk: the reference's sums bit for bit; other walks: the mixed walk's potential.
+        const bool fp64 = p->walk == GBH_WALK_FP64;
         CK(gbh::tree_alloc(ctx->tb, n, leaf, ctx->nsys));
+        CK(grow(ctx->scratch3, ctx->scratch3_cap, 3 * ctx->tb.cap_n));
+        sa = ctx->scratch3;
+        ctx->tb.group = 64;
         CK(gbh::tree_build(L, ctx->tb, n, ctx->px, ctx->py, ctx->pz, ctx->mass, kind, alive, sa, sa + n, sa + 2 * n,
-                           theta, leaf, p->dark_matter_off, true, true, forest ? ctx->sys_of : nullptr,
+                           theta, leaf, p->dark_matter_off, fp64, fp64, forest ? ctx->sys_of : nullptr,
                            forest ? ctx->sys_off : nullptr));
-        CK(gbh::potential_fp64(L, ctx->tb, n, ctx->px, ctx->py, ctx->pz, ctx->mass, kind, alive, ctx->holes,
-                               int32_t(holes.size()), p->softening * p->softening, c, p->dark_matter_off,
-                               !p->monopole_only, ctx->part, ctx->scalar));
+        if (fp64) {
+            CK(gbh::potential_fp64(L, ctx->tb, n, ctx->px, ctx->py, ctx->pz, ctx->mass, kind, alive, ctx->holes,
+                                   int32_t(holes.size()), p->softening * p->softening, c, p->dark_matter_off,
+                                   !p->monopole_only, ctx->part, ctx->scalar));
+        } else {
+            CK(gbh::potential_mixed(L, ctx->tb, n, ctx->px, ctx->py, ctx->pz, ctx->mass, kind, alive, ctx->holes,
+                                    int32_t(holes.size()), p->softening * p->softening, c, p->dark_matter_off,
+                                    !p->monopole_only, sa, ctx->part, ctx->scalar));
+        }
     }
     double u = 0;
     CK(cudaMemcpyAsync(&u, ctx->scalar, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));

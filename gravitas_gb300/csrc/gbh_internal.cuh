@@ -175,6 +175,12 @@ cudaError_t potential_fp64(const Launch &L, const TreeBufs &b, int64_t n, const 
                            const uint8_t *kind, const uint8_t *alive, const int32_t *holes,
                            int32_t nholes, double eps2, double c, int dm_off, int quad,
                            double *part, double *u_dev);
+// Potential from the mixed walk (FP32 node terms, compensated per-star sums, FP64 reduction);
+// psi holds cap_n doubles of scratch. Used for every walk but GBH_WALK_FP64.
+cudaError_t potential_mixed(const Launch &L, const TreeBufs &b, int64_t n, const double *px, const double *py,
+                            const double *pz, const double *mass, const uint8_t *kind, const uint8_t *alive,
+                            const int32_t *holes, int32_t nholes, double eps2, double c, int dm_off, int quad,
+                            double *psi, double *part, double *u_dev);
 // Exact pair potential of all bodies (PotentialEnergyParallel, diag.go:42-62): rows (n doubles of
 // scratch) in ascending i, each over j > i ascending; result in *u_dev.
 constexpr int64_t kExactEnergyLimit = 30000;  // exactEnergyLimit, diag.go:16-19
@@ -267,6 +273,9 @@ cudaError_t walk_plain(const Launch &L, const TreeBufs &b, int64_t nstars_cap, f
                        double *ax, double *ay, double *az, bool targets = false);
 cudaError_t walk_mixed(const Launch &L, const TreeBufs &b, int64_t nstars_cap, float eps2,
                        int quad, double *ax, double *ay, double *az, bool targets = false);
+// psi[k] = sum m / r + (d.Q.d) / (2 r^5) of sorted star k (walkPotential with the mixed walk).
+cudaError_t walk_mixed_potential(const Launch &L, const TreeBufs &b, int64_t nstars_cap, float eps2, int quad,
+                                 double *psi);
 cudaError_t fp32_fma_probe(const Launch &L, int blocks, int iters, float *out);
 
 }  // namespace gbh

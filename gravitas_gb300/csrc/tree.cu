@@ -1606,6 +1606,62 @@ cudaError_t direct_fp64(const Launch &L, int64_t n, const double *px, const doub
     return cudaSuccess;
 }
 
+// Potential from the mixed walk's psi (sorted order): the block sums of m_k psi_k minus each
+// star's hole pairs, as k_potential_walk forms them from the FP64 walk.
+__global__ __launch_bounds__(kThreads) void k_potential_parts_psi(const DevInfo *info, const int32_t *__restrict__ order,
+                                                                  const double *__restrict__ psi, const double *px,
+                                                                  const double *py, const double *pz,
+                                                                  const double *mass, const uint8_t *kind,
+                                                                  const int32_t *holes, int32_t nholes, double eps2,
+                                                                  double c, int dm_off, double *part) {
+    int64_t k = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    double v = 0;
+    if (k < info->nstars) {
+        int32_t i = order[k];
+        double smi = (dm_off && kind && kind[i] == GBH_DARK_MATTER) ? 0.0 : mass[i];
+        v = smi * psi[k] - (nholes ? hole_potential(i, px, py, pz, mass, kind, holes, nholes, eps2, c, dm_off) : 0.0);
+    }
+    __shared__ double s[kThreads];
+    s[threadIdx.x] = v;
+    __syncthreads();
+    for (int o = kThreads / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) s[threadIdx.x] += s[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) part[blockIdx.x] = s[0];
+}
+
+// U = -(parts - hole pairs) / 2, the hole-star pairs taken over the alive non-hole bodies in
+// state order (k_potential_final takes them over the sorted copies).
+__global__ void k_potential_final_state(int64_t nparts, const double *part, int64_t n, const double *px,
+                                        const double *py, const double *pz, const double *mass, const uint8_t *kind,
+                                        const uint8_t *alive, const int32_t *holes, int32_t nholes, double eps2,
+                                        double c, int dm_off, double *u) {
+    __shared__ double s[kThreads];
+    double v = 0;
+    for (int64_t b = threadIdx.x; b < nparts; b += blockDim.x) v += part[b];
+    for (int32_t t = 0; t < nholes; ++t) {
+        int32_t i = holes[t];
+        double x = px[i], y = py[i], z = pz[i];
+        double rs = schwarzschild(mass[i], c);
+        for (int64_t j = threadIdx.x; j < n; j += blockDim.x) {
+            uint8_t kj = kind ? kind[j] : 0;
+            if (kj == GBH_BLACK_HOLE || (alive && !alive[j])) continue;
+            double smj = (dm_off && kj == GBH_DARK_MATTER) ? 0.0 : mass[j];
+            double dx = px[j] - x, dy = py[j] - y, dz = pz[j] - z;
+            v -= pair_potential(mass[i], smj, dx * dx + dy * dy + dz * dz, eps2, rs);
+        }
+        if (threadIdx.x == 0) v -= hole_potential(i, px, py, pz, mass, kind, holes, nholes, eps2, c, dm_off);
+    }
+    s[threadIdx.x] = v;
+    __syncthreads();
+    for (int o = kThreads / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) s[threadIdx.x] += s[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *u = -s[0] / 2;
+}
+
 cudaError_t potential_exact_fp64(const Launch &L, int64_t n, const double *px, const double *py, const double *pz,
                                  const double *mass, const uint8_t *kind, double eps2, double c, int dm_off,
                                  double *rows, double *u_dev) {
@@ -1613,6 +1669,22 @@ cudaError_t potential_exact_fp64(const Launch &L, int64_t n, const double *px, c
                                                                                dm_off, rows);
     GBH_LAUNCH_CHECK();
     k_pot_exact_final<<<1, 32, 0, L.stream>>>(n, rows, u_dev);
+    GBH_LAUNCH_CHECK();
+    return cudaSuccess;
+}
+
+cudaError_t potential_mixed(const Launch &L, const TreeBufs &b, int64_t n, const double *px, const double *py,
+                            const double *pz, const double *mass, const uint8_t *kind, const uint8_t *alive,
+                            const int32_t *holes, int32_t nholes, double eps2, double c, int dm_off, int quad,
+                            double *psi, double *part, double *u_dev) {
+    cudaError_t e = walk_mixed_potential(L, b, b.cap_n, float(eps2), quad, psi);
+    if (e != cudaSuccess) return e;
+    unsigned nb = blocks_for(b.cap_n, kThreads);
+    k_potential_parts_psi<<<nb, kThreads, 0, L.stream>>>(b.info, b.order, psi, px, py, pz, mass, kind, holes, nholes,
+                                                         eps2, c, dm_off, part);
+    GBH_LAUNCH_CHECK();
+    k_potential_final_state<<<1, kThreads, 0, L.stream>>>(nb, part, n, px, py, pz, mass, kind, alive, holes, nholes,
+                                                          eps2, c, dm_off, u_dev);
     GBH_LAUNCH_CHECK();
     return cudaSuccess;
 }

@@ -126,7 +126,9 @@ __device__ __forceinline__ void kahan_fold2(float2 &s, float2 &c, float2 &part) 
     kahan_fold(s.y, c.y, part.y);
 }
 
-template <bool kQuad, bool kSoft>
+// kPot: the same walk accumulating psi = sum m / r + (d.Q.d) / (2 r^5) (walkPotential,
+// potential.go:44-81) per star instead of the acceleration; psi goes to ax[sorted index].
+template <bool kQuad, bool kSoft, bool kPot>
 __global__ __launch_bounds__(kMixedThreads, 8) void k_walk_mixed2(const DevInfo *info, const MNode *__restrict__ nodes,
                                                                const int2 *__restrict__ ranges,
                                                                const float4 *__restrict__ st_hi,
@@ -188,7 +190,17 @@ __global__ __launch_bounds__(kMixedThreads, 8) void k_walk_mixed2(const DevInfo 
             const float2 ir = make_float2(rsqrtf(r2.x), rsqrtf(r2.y));
             const float2 ir2 = mul2(ir, ir);
             const float2 ir3 = mul2(ir, ir2);
-            if (kQuad) {
+            if constexpr (kPot) {
+                float2 t = mul2(f2(nd.b.w), ir);
+                if (kQuad) {
+                    const float2 qx = fma2(f2(nd.d.x), dz, fma2(f2(nd.c.w), dy, mul2(f2(nd.c.x), dx)));
+                    const float2 qy = fma2(f2(nd.d.y), dz, fma2(f2(nd.c.y), dy, mul2(f2(nd.c.w), dx)));
+                    const float2 qz = fma2(f2(nd.c.z), dz, fma2(f2(nd.d.y), dy, mul2(f2(nd.d.x), dx)));
+                    const float2 dqd = fma2(dz, qz, fma2(dy, qy, mul2(dx, qx)));
+                    t = fma2(mul2(f2(0.5f), dqd), mul2(ir3, ir2), t);
+                }
+                px = add2(px, t);
+            } else if (kQuad) {
                 const float2 qx = fma2(f2(nd.d.x), dz, fma2(f2(nd.c.w), dy, mul2(f2(nd.c.x), dx)));
                 const float2 qy = fma2(f2(nd.d.y), dz, fma2(f2(nd.c.y), dy, mul2(f2(nd.c.w), dx)));
                 const float2 qz = fma2(f2(nd.c.z), dz, fma2(f2(nd.d.y), dy, mul2(f2(nd.d.x), dx)));
@@ -232,10 +244,18 @@ __global__ __launch_bounds__(kMixedThreads, 8) void k_walk_mixed2(const DevInfo 
                 } else {
                     ir = make_float2(r2.x > 0.f ? rsqrtf(r2.x) : 0.f, r2.y > 0.f ? rsqrtf(r2.y) : 0.f);
                 }
-                const float2 f = mul2(mul2(f2(so.w), ir), mul2(ir, ir));
-                px = fma2(f, ex, px);
-                py = fma2(f, ey, py);
-                pz = fma2(f, ez, pz);
+                if constexpr (kPot) {
+                    // the self pair has zero separation but m / eps is not zero: skip j == self
+                    float2 t = mul2(f2(so.w), ir);
+                    t.x = j == k0 ? 0.f : t.x;
+                    t.y = j == k1 ? 0.f : t.y;
+                    px = add2(px, t);
+                } else {
+                    const float2 f = mul2(mul2(f2(so.w), ir), mul2(ir, ir));
+                    px = fma2(f, ex, px);
+                    py = fma2(f, ey, py);
+                    pz = fma2(f, ez, pz);
+                }
             }
             i = next;
         }
@@ -252,6 +272,11 @@ __global__ __launch_bounds__(kMixedThreads, 8) void k_walk_mixed2(const DevInfo 
     kahan_fold2(sx, cx, px);
     kahan_fold2(sy, cy, py);
     kahan_fold2(sz, cz, pz);
+    if constexpr (kPot) {
+        if (v0) ax[k0] = double(sx.x) - double(cx.x);
+        if (v1) ax[k1] = double(sx.y) - double(cx.y);
+        return;
+    }
     if (v0) {
         int32_t o = order[k0];
         ax[o] = double(sx.x) - double(cx.x);
@@ -299,14 +324,14 @@ cudaError_t walk_plain(const Launch &L, const TreeBufs &b, int64_t nstars_cap, f
     return cudaGetLastError();
 }
 
-template <bool kQuad, bool kSoft>
+template <bool kQuad, bool kSoft, bool kPot = false>
 static cudaError_t launch_mixed(const Launch &L, const TreeBufs &b, int64_t nstars_cap, float eps2, double *ax,
                                 double *ay, double *az, bool targets) {
     const bool forest = b.nsys > 1;
     const int gsize = b.group == 32 ? 32 : 64;
     int64_t groups = forest ? b.cap_groups : (nstars_cap + gsize - 1) / gsize;
     int64_t blocks = (groups + kMixedThreads / 32 - 1) / (kMixedThreads / 32);
-    k_walk_mixed2<kQuad, kSoft><<<unsigned(blocks < 1 ? 1 : blocks), kMixedThreads, 0, L.stream>>>(
+    k_walk_mixed2<kQuad, kSoft, kPot><<<unsigned(blocks < 1 ? 1 : blocks), kMixedThreads, 0, L.stream>>>(
         b.info, b.mnodes, b.mrange, b.st_hi, b.st_lo, b.st_off, b.order, eps2, ax, ay, az,
         targets ? b.targets : nullptr,
         forest ? b.groups : nullptr, gsize == 64 ? 1 : 0, b.info);
@@ -321,6 +346,15 @@ cudaError_t walk_mixed(const Launch &L, const TreeBufs &b, int64_t nstars_cap, f
     if (quad) return launch_mixed<true, false>(L, b, nstars_cap, eps2, ax, ay, az, targets);
     if (soft) return launch_mixed<false, true>(L, b, nstars_cap, eps2, ax, ay, az, targets);
     return launch_mixed<false, false>(L, b, nstars_cap, eps2, ax, ay, az, targets);
+}
+
+cudaError_t walk_mixed_potential(const Launch &L, const TreeBufs &b, int64_t nstars_cap, float eps2, int quad,
+                                 double *psi) {
+    bool soft = eps2 > 0.f;
+    if (quad && soft) return launch_mixed<true, true, true>(L, b, nstars_cap, eps2, psi, nullptr, nullptr, false);
+    if (quad) return launch_mixed<true, false, true>(L, b, nstars_cap, eps2, psi, nullptr, nullptr, false);
+    if (soft) return launch_mixed<false, true, true>(L, b, nstars_cap, eps2, psi, nullptr, nullptr, false);
+    return launch_mixed<false, false, true>(L, b, nstars_cap, eps2, psi, nullptr, nullptr, false);
 }
 
 cudaError_t fp32_fma_probe(const Launch &L, int blocks, int iters, float *out) {

@@ -243,6 +243,33 @@ def test_potential_matches_oracle(ctx):
     assert abs((u[0] - float(g["potential"])) / float(g["potential"])) <= 1e-12
 
 
+@pytest.mark.parametrize("dm_off", [False, True])
+def test_mixed_potential_matches_fp64_tree_potential(ctx, dm_off):
+    """The mixed walk's potential (FP32 node terms, compensated sums, 64-star groups that open a
+    node wherever any star would): against the exact pair sum at least as accurate as the
+    reference's per-star tree estimate (the FP64 walk, bit for bit the oracle's), holes and the
+    pair model included."""
+    s = ics.test_disk(40000)
+    s["kind"][3::11] = O.DARK_MATTER
+    n = len(s["px"])
+    u = {}
+    for walk in ("fp64", "mixed"):
+        out = np.zeros(1)
+        par = abi.make_params(0.5, 0.06, 16, False, dm_off, walk)
+        ctx.call("gbh_potential_energy", par, n, P(s["px"]), P(s["py"]), P(s["pz"]), P(s["mass"]), P(s["kind"]),
+                 P(s["alive"]), 10.0, P(out))
+        u[walk] = out[0]
+        ctx.call("gbh_state_upload", n, *[P(s[k]) for k in ("px", "py", "pz", "vx", "vy", "vz")], None, None, None,
+                 P(s["mass"]), P(s["kind"]), P(s["alive"]))
+        d = ctx.diagnostics(par, c=10.0)
+        assert d["quality"] == 1 and d["potential"] == out[0], walk
+    t = O.Tree(s["px"], s["py"], s["pz"], s["mass"], s["kind"], s["alive"], theta=0.5, leaf=16, dm_off=dm_off)
+    assert abs(u["fp64"] - t.potential(0.06, c=10.0)) <= 1e-12 * abs(u["fp64"])
+    exact = O.potential_exact(s["px"], s["py"], s["pz"], s["mass"], s["kind"], eps=0.06, c=10.0, dm_off=dm_off)
+    assert abs(u["mixed"] - exact) <= abs(u["fp64"] - exact) + 1e-7 * abs(exact), (u["mixed"], u["fp64"], exact)
+    assert abs(u["mixed"] - exact) <= 2e-5 * abs(exact)
+
+
 def test_kdk_fp64_bit_exact(ctx):
     g = np.load(os.path.join(GOLDEN, "kdk.npz"))
     st = {k: g[f"in_{k}"].copy() for k in ("px", "py", "pz", "vx", "vy", "vz", "mass")}
