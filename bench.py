@@ -365,7 +365,8 @@ def run_profile(args):
     evaluations with the chosen walk (tree build + walk each). --profile adjoint runs one
     forward + backward of the 32,768-body adjoint workload over 4 steps (checkpoints every 2);
     --profile forest two force evaluations of the 64-system forest at the autotuner's choice
-    (theta 0.7, leaf 16, group 64)."""
+    (theta 0.7, leaf 16, group 64); --profile build two force evaluations of a Plummer sphere of
+    --n bodies (leaf 32), for captures of the build kernels."""
     from gravitas_gb300 import abi
     P = abi.ptr
     if args.profile == "adjoint":
@@ -376,6 +377,21 @@ def run_profile(args):
         t = ctx.timings()
         print(json.dumps({"profile": "adjoint", "n": ADJ_N, "steps": 4, "loss": loss, "bwd_ms": t["total_ms"],
                           "pair_ms": t["walk_ms"], "launches": t["launches"]}))
+        ctx.close()
+        return 0
+    if args.profile == "build":
+        from gravitas_gb300 import ics
+        n = args.n
+        s = ics.plummer(n, seed=0)
+        ctx = abi.Context(0)
+        ctx.call("gbh_state_upload", n, *[P(s[k]) for k in ("px", "py", "pz", "vx", "vy", "vz")], None, None, None,
+                 P(s["mass"]), None, None)
+        par = abi.make_params(THETA, 0.01, args.leaf or 32, False, False, "mixed", group_size=64)
+        for _ in range(2):
+            ctx.call("gbh_state_accelerations", par)
+        t = ctx.timings()
+        print(json.dumps({"profile": "build", "n": n, "build_ms": t["build_ms"], "walk_ms": t["walk_ms"],
+                          "nnodes": t["nnodes"], "launches": t["launches"]}))
         ctx.close()
         return 0
     if args.profile == "forest":
@@ -639,7 +655,7 @@ def main():
     ap.add_argument("--n", type=int, default=N_DEFAULT)
     ap.add_argument("--leaf", type=int, default=0,
                     help="leaf size; 0 (default) lets the autotuner choose for each walk")
-    ap.add_argument("--profile", choices=["mixed", "plain", "fp64", "adjoint", "forest"], default=None,
+    ap.add_argument("--profile", choices=["mixed", "plain", "fp64", "adjoint", "forest", "build"], default=None,
                     help="run only two force evaluations with this walk (for ncu captures)")
     ap.add_argument("--workload", choices=["merger", "adjoint", "forest", "scaling"], default="merger",
                     help="adjoint: the differentiable workload (gbh_fwd_save / gbh_bwd); forest: 64 systems in "

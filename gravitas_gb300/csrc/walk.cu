@@ -229,6 +229,7 @@ __global__ __launch_bounds__(kMixedThreads, 8) void k_walk_mixed2(const DevInfo 
             }
             // Leaf stars: separation = (leaf com - star) + (leaf star - com), the first the visit's
             // double-float separation, the second the star's FP32 offset stored by the upsweep.
+#pragma unroll 4  // measured 2-3 % faster than no unrolling (independent source stars)
             for (int j = r.x; j < r.y; ++j) {
                 const float4 so = st_off[j];
                 const float2 ex = add2(dx, f2(so.x));
