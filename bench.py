@@ -481,6 +481,23 @@ def run_adjoint(args):
         fd = (vals[0] - vals[1]) / (2 * h)
         g = dv[i, c] if q % 2 == 0 else dm[i]
         errs.append(abs(g - fd) / max(abs(fd), 1e-3 * scale))
+    # the same gradient against central differences of the tree dynamics (theta 0.5, mixed walk,
+    # leaf 8): the opening-test discontinuities are far below the difference quotient at h = 1e-4
+    tree_errs = []
+    par = abi.make_params(THETA, ADJ_EPS, 8, False, False, "mixed")
+    F = ("px", "py", "pz", "vx", "vy", "vz", "ax", "ay", "az")
+    for q in range(args.fd_coords // 2):
+        i, c = int(rng.integers(n)), int(rng.integers(3))
+        vals = []
+        for sign in (1.0, -1.0):
+            st = {k: (s[k].copy() if k in s else np.zeros(n)) for k in F}
+            st[("vx", "vy", "vz")[c]][i] += sign * h
+            ctx.call("gbh_step_kdk", par, ADJ_DT, T, 0, n, *[abi.ptr(st[k]) for k in F], abi.ptr(s["mass"]), None,
+                     None)
+            x = np.stack([st["px"], st["py"], st["pz"]], 1)
+            vals.append(float(np.sum((x - targets) ** 2) / n))
+        fd = (vals[0] - vals[1]) / (2 * h)
+        tree_errs.append(abs(dv[i, c] - fd) / max(abs(fd), 1e-3 * scale))
     # CPU baseline: the oracle's FP64 adjoint on a bounded sample (all bodies, 4 steps)
     cpu = None
     if rank == 0:
@@ -507,6 +524,9 @@ def run_adjoint(args):
                      "peak_source": "FP32 FMA probe of this run"},
         "fd_check": {"coords": len(errs), "h": h, "max_rel": float(max(errs)) if errs else None,
                      "median_rel": float(np.median(errs)) if errs else None},
+        "fd_check_tree_dynamics": {"coords": len(tree_errs), "h": h, "theta": THETA, "walk": "mixed, leaf 8",
+                                   "max_rel": float(max(tree_errs)) if tree_errs else None,
+                                   "median_rel": float(np.median(tree_errs)) if tree_errs else None},
         "cpu_baseline": cpu, "clocks": clk.summary(),
     }
     if rank == 0:
