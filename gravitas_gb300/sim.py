@@ -127,7 +127,8 @@ class DirectSolver:
 
 
 class Simulation:
-    """Simulation.Step (sim.go:248-288) for states without alive black holes or hydro."""
+    """Simulation.Step (sim.go:248-288) without hydro: the KDK step, or with alive black holes
+    the hole-aware split step (c = 0)."""
 
     def __init__(self, state: State, solver: Solver, params: Params):
         self.state, self.solver, self.params = state, solver, params
@@ -143,6 +144,30 @@ class Simulation:
         self.acc_valid = True
         self.time += n * self.params.dt
         self.steps += n
+
+    def save(self, path: str) -> None:
+        """A .gravitas snapshot of the run (save.Capture + Write, save.go:69-148), with the last
+        forces when they are valid, so that a loaded run continues bit-identically."""
+        from . import snapshot
+        s = self.state
+        state = {"px": s.pos_x, "py": s.pos_y, "pz": s.pos_z, "vx": s.vel_x, "vy": s.vel_y, "vz": s.vel_z,
+                 "mass": s.mass, "kind": s.kind}
+        params = {"Dt": self.params.dt, "Softening": self.params.softening, "C": self.params.c,
+                  "DarkMatterOff": self.params.dark_matter_off}
+        forces = (s.acc_x, s.acc_y, s.acc_z) if self.acc_valid else None
+        snapshot.save(path, state, params, time=self.time, steps=self.steps, forces=forces)
+
+    @classmethod
+    def load(cls, path: str, solver: "Solver") -> "Simulation":
+        """A run restored from a snapshot (File.Restore, save.go:121-130)."""
+        from . import snapshot
+        st, params, meta = snapshot.load_state(path)
+        state = State(st["px"], st["py"], st["pz"], st["vx"], st["vy"], st["vz"], st["ax"], st["ay"], st["az"],
+                      st["mass"], st["kind"], st["alive"])
+        m = cls(state, solver, Params(dt=params.get("Dt", 0.0), softening=params.get("Softening", 0.0),
+                                      c=params.get("C", 0.0), dark_matter_off=bool(params.get("DarkMatterOff", False))))
+        m.time, m.steps, m.acc_valid = float(meta["Time"]), int(meta["Steps"]), bool(meta["forces"])
+        return m
 
 
 def trajectory_loss_gradient(state: dict, targets: np.ndarray, dt: float, softening: float, nsteps: int,
