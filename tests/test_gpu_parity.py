@@ -611,3 +611,20 @@ def test_snapshot_save_load_continues_bit_identically(tmp_path):
     c.step(3)
     for f in ("pos_x", "pos_y", "pos_z", "vel_x", "vel_y", "vel_z", "acc_x", "acc_y", "acc_z"):
         assert np.array_equal(getattr(a.state, f), getattr(c.state, f)), f
+
+
+def test_evolve_driver_continues_a_snapshot(tmp_path):
+    """The headless driver: evolve a scene to t, continue the written snapshot to 2t; the result
+    equals one run to 2t (steps are deterministic and the snapshot keeps the forces)."""
+    from gravitas_gb300 import evolve, snapshot
+    d = str(tmp_path)
+    a, b, c = (os.path.join(d, f) for f in ("a.gravitas", "b.gravitas", "c.gravitas"))
+    common = ["--scene", "plummer", "--n", "4096", "--dt", "1e-3", "--chunk", "7"]
+    assert evolve.main(common + ["-t", "0.02", "-o", a]) == 0
+    assert evolve.main(["--in", a, "-t", "0.04", "-o", b, "--chunk", "7"]) == 0
+    assert evolve.main(common + ["-t", "0.04", "-o", c]) == 0
+    sb, _, mb = snapshot.load_state(b)
+    sc, _, mc = snapshot.load_state(c)
+    assert mb["Steps"] == mc["Steps"] == 40
+    for k in ("px", "py", "pz", "vx", "vy", "vz", "ax", "ay", "az"):
+        assert np.array_equal(sb[k], sc[k]), k
