@@ -173,6 +173,7 @@ int check_params(gbh_ctx *ctx, const gbh_params *p) {
     if (p->walk < GBH_WALK_MIXED || p->walk > GBH_WALK_FP64) return fail(ctx, GBH_ERR_ARG, "walk %d", p->walk);
     if (p->group_size != 0 && p->group_size != 32 && p->group_size != 64)
         return fail(ctx, GBH_ERR_ARG, "group_size %d (0, 32 or 64)", p->group_size);
+    if (!(p->c >= 0 && std::isfinite(p->c))) return fail(ctx, GBH_ERR_ARG, "c %g must be finite and >= 0", p->c);
     return GBH_OK;
 }
 
@@ -325,7 +326,7 @@ void free_graph(StepGraph &g) {
 bool same_params(const gbh_params &a, const gbh_params &b) {
     return a.theta == b.theta && a.softening == b.softening && a.leaf_size == b.leaf_size &&
            a.monopole_only == b.monopole_only && a.dark_matter_off == b.dark_matter_off && a.walk == b.walk &&
-           (a.group_size == 32) == (b.group_size == 32);
+           (a.group_size == 32) == (b.group_size == 32) && a.c == b.c;
 }
 
 // out[q] = a[idx[q]] for the three arrays of a (n doubles apart in out).
@@ -351,7 +352,7 @@ int capture_step(gbh_ctx *ctx, const gbh_params *p, double dt, const uint8_t *ki
     CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
     ctx->capturing = true;
     int rc = GBH_OK;
-    cudaError_t e = gbh::kick_drift(L, n, h, dt, ctx->px, ctx->py, ctx->pz, ctx->vx, ctx->vy, ctx->vz, ctx->ax, ctx->ay,
+    cudaError_t e = gbh::kick_drift(L, n, h, dt, p->c, ctx->px, ctx->py, ctx->pz, ctx->vx, ctx->vy, ctx->vz, ctx->ax, ctx->ay,
                                     ctx->az);
     if (e == cudaSuccess)
         rc = forces(ctx, p, n, ctx->px, ctx->py, ctx->pz, ctx->mass, kind, alive, ctx->ax, ctx->ay, ctx->az,
@@ -398,9 +399,9 @@ int capture_step(gbh_ctx *ctx, const gbh_params *p, double dt, const uint8_t *ki
 }
 
 // Steps on the resident state (sim.go:252-288, no holes, no hydro).
-// The hole-aware step (split.go:161-204, stepSplit) with c = 0 and no gas: forces of pairs with a
-// hole summed directly, near stars and holes in power-of-two substeps, star-star forces from the
-// tree once per step. The substep count of the last step goes to ctx->last_substeps.
+// The hole-aware step (split.go:161-204, stepSplit) without gas, instant gravity and no spins:
+// forces of pairs with a hole summed directly (Paczynski-Wiita star-hole pairs for c > 0), near
+// stars and holes in power-of-two substeps, star-star forces from the tree once per step. The substep count of the last step goes to ctx->last_substeps.
 int run_split_steps(gbh_ctx *ctx, const gbh_params *p, double dt, int64_t nsteps) {
     Launch L = launch_of(ctx);
     const int64_t n = ctx->n;
@@ -408,6 +409,7 @@ int run_split_steps(gbh_ctx *ctx, const gbh_params *p, double dt, int64_t nsteps
     const uint8_t *alive = ctx->state_has_alive ? ctx->alive : nullptr;
     const double theta = theta_of(p), eps2 = p->softening * p->softening, h = 0.5 * dt;
     const int dm = p->dark_matter_off;
+    const double c = p->c;
     gbh::SplitBufs &sb = ctx->split;
     CK(gbh::split_reserve(sb, n, ctx->hole_list));
     CK(cudaMemcpyAsync(sb.holes, ctx->hole_list.data(), sizeof(int32_t) * ctx->hole_list.size(),
@@ -424,7 +426,7 @@ int run_split_steps(gbh_ctx *ctx, const gbh_params *p, double dt, int64_t nsteps
     unsigned long long sc[2];
     for (int64_t step = 0; step < nsteps; ++step) {
         // classify (split.go:41-81): the host needs the substep count
-        CK(gbh::split_classify(L, sb, n, px, py, pz, ctx->mass, kind, eps2, 20.0 * dt));
+        CK(gbh::split_classify(L, sb, n, px, py, pz, ctx->mass, kind, eps2, c, 20.0 * dt));
         CK(cudaMemcpyAsync(sc, sb.scalars, sizeof sc, cudaMemcpyDeviceToHost, ctx->stream));
         CK(wait_stream(ctx));
         double tau_min;
@@ -434,20 +436,20 @@ int run_split_steps(gbh_ctx *ctx, const gbh_params *p, double dt, int64_t nsteps
         if (!std::isinf(tau_min))
             while (double(k) * tau_min < 20.0 * dt && k < 256) k *= 2;
         ctx->last_substeps = k;
-        CK(gbh::split_outer(L, sb, n, px, py, pz, ctx->mass, kind, dm, eps2));
+        CK(gbh::split_outer(L, sb, n, px, py, pz, ctx->mass, kind, dm, eps2, c));
         CK(gbh::split_kick_outer(L, sb, n, h, vx, vy, vz, ctx->ax, ctx->ay, ctx->az));
         const double hs = dt / double(k);
-        CK(gbh::split_fast(L, sb, n, nnear, px, py, pz, ctx->mass, kind, dm, eps2));
+        CK(gbh::split_fast(L, sb, n, nnear, px, py, pz, ctx->mass, kind, dm, eps2, c));
         for (int64_t q = 0; q < k; ++q) {
-            CK(gbh::split_fast_update(L, sb, n, nnear, false, 0.5 * hs, px, py, pz, vx, vy, vz));
-            CK(gbh::split_fast_update(L, sb, n, nnear, true, hs, px, py, pz, vx, vy, vz));
-            CK(gbh::split_fast(L, sb, n, nnear, px, py, pz, ctx->mass, kind, dm, eps2));
-            CK(gbh::split_fast_update(L, sb, n, nnear, false, 0.5 * hs, px, py, pz, vx, vy, vz));
+            CK(gbh::split_fast_update(L, sb, n, nnear, false, 0.5 * hs, c, px, py, pz, vx, vy, vz));
+            CK(gbh::split_fast_update(L, sb, n, nnear, true, hs, c, px, py, pz, vx, vy, vz));
+            CK(gbh::split_fast(L, sb, n, nnear, px, py, pz, ctx->mass, kind, dm, eps2, c));
+            CK(gbh::split_fast_update(L, sb, n, nnear, false, 0.5 * hs, c, px, py, pz, vx, vy, vz));
         }
-        CK(gbh::split_drift_far(L, sb, n, dt, kind, px, py, pz, vx, vy, vz));
+        CK(gbh::split_drift_far(L, sb, n, dt, c, kind, px, py, pz, vx, vy, vz));
         int rc = slow();  // advanceGas without gas (blockstep.go:129-135)
         if (rc) return rc;
-        CK(gbh::split_outer(L, sb, n, px, py, pz, ctx->mass, kind, dm, eps2));
+        CK(gbh::split_outer(L, sb, n, px, py, pz, ctx->mass, kind, dm, eps2, c));
         CK(gbh::split_kick_outer(L, sb, n, h, vx, vy, vz, ctx->ax, ctx->ay, ctx->az));
     }
     return GBH_OK;
@@ -490,7 +492,7 @@ int run_steps(gbh_ctx *ctx, const gbh_params *p, double dt, int64_t nsteps) {
     double h = 0.5 * dt;
     for (int64_t s = 0; s < nsteps; ++s) {
         CK(throttle_before(ctx, s));
-        CK(gbh::kick_drift(L, n, h, dt, ctx->px, ctx->py, ctx->pz, ctx->vx, ctx->vy, ctx->vz, ctx->ax, ctx->ay,
+        CK(gbh::kick_drift(L, n, h, dt, p->c, ctx->px, ctx->py, ctx->pz, ctx->vx, ctx->vy, ctx->vz, ctx->ax, ctx->ay,
                            ctx->az));
         int rc = forces(ctx, p, n, ctx->px, ctx->py, ctx->pz, ctx->mass, kind, alive, ctx->ax, ctx->ay, ctx->az, theta,
                         true);
@@ -569,7 +571,7 @@ int run_block_steps(gbh_ctx *ctx, const gbh_params *p, double T, double eta, int
             int32_t tn = ctx->info_host.next_tick;
             if (tn <= t || tn > ticks) return fail(ctx, GBH_ERR_LIMIT, "block steps: next event %d after %d", tn, t);
             if (st && (st->min_substep_ticks == 0 || tn - t < st->min_substep_ticks)) st->min_substep_ticks = tn - t;
-            CK(gbh::block_drift(L, n, double(tn - t) * (T / double(ticks)), ctx->px, ctx->py, ctx->pz, ctx->vx,
+            CK(gbh::block_drift(L, n, double(tn - t) * (T / double(ticks)), p->c, ctx->px, ctx->py, ctx->pz, ctx->vx,
                                 ctx->vy, ctx->vz));
             t = tn;
             if ((rc = forces_active(ctx, p, kind, alive, ctx->end_tick, t))) return rc;

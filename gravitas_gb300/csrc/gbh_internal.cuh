@@ -145,7 +145,7 @@ cudaError_t tree_build(const Launch &L, TreeBufs &b, int64_t n, const double *px
 cudaError_t block_open(const Launch &L, const TreeBufs &b, int64_t n, double T, int levels, double eta, double eps,
                        const double *ax, const double *ay, const double *az, double *vx, double *vy, double *vz,
                        uint8_t *rung, int32_t *end);
-cudaError_t block_drift(const Launch &L, int64_t n, double dt, double *px, double *py, double *pz, const double *vx,
+cudaError_t block_drift(const Launch &L, int64_t n, double dt, double c, double *px, double *py, double *pz, const double *vx,
                         const double *vy, const double *vz);
 cudaError_t block_close(const Launch &L, const TreeBufs &b, int64_t n, int32_t tick, double T, int levels, double eta,
                         double eps, const double *ax, const double *ay, const double *az, double *vx, double *vy,
@@ -162,7 +162,7 @@ cudaError_t walk_fp64(const Launch &L, const TreeBufs &b, int64_t n, double eps2
 cudaError_t select_targets(const Launch &L, TreeBufs &b, const int32_t *end, int32_t tick);
 cudaError_t kick(const Launch &L, int64_t n, double h, double *vx, double *vy, double *vz,
                  const double *ax, const double *ay, const double *az);
-cudaError_t kick_drift(const Launch &L, int64_t n, double h, double dt, double *px, double *py,
+cudaError_t kick_drift(const Launch &L, int64_t n, double h, double dt, double c, double *px, double *py,
                        double *pz, double *vx, double *vy, double *vz, const double *ax,
                        const double *ay, const double *az);
 cudaError_t direct_fp64(const Launch &L, int64_t n, const double *px, const double *py,
@@ -224,20 +224,21 @@ cudaError_t split_reserve(SplitBufs &s, int64_t n, const std::vector<int32_t> &h
 void split_free(SplitBufs &s);
 // Near flags and list, minimum timescale (scalars) for the current positions.
 cudaError_t split_classify(const Launch &L, SplitBufs &s, int64_t n, const double *px, const double *py,
-                           const double *pz, const double *mass, const uint8_t *kind, double eps2, double limit);
+                           const double *pz, const double *mass, const uint8_t *kind, double eps2, double c,
+                           double limit);
 // far = hole pulls of the far stars and the far stars' pulls on the holes.
 cudaError_t split_outer(const Launch &L, SplitBufs &s, int64_t n, const double *px, const double *py,
-                        const double *pz, const double *mass, const uint8_t *kind, int dm_off, double eps2);
+                        const double *pz, const double *mass, const uint8_t *kind, int dm_off, double eps2, double c);
 cudaError_t split_kick_outer(const Launch &L, SplitBufs &s, int64_t n, double h, double *vx, double *vy, double *vz,
                              const double *ax, const double *ay, const double *az);
 // fast = hole pulls of the near stars, and the holes' pulls from the other holes and the near stars.
 cudaError_t split_fast(const Launch &L, SplitBufs &s, int64_t n, int32_t nnear, const double *px, const double *py,
-                       const double *pz, const double *mass, const uint8_t *kind, int dm_off, double eps2);
+                       const double *pz, const double *mass, const uint8_t *kind, int dm_off, double eps2, double c);
 // Near stars and holes: v += h fast (drift = false) or x += h v (drift = true).
 cudaError_t split_fast_update(const Launch &L, SplitBufs &s, int64_t n, int32_t nnear, bool drift, double h,
-                              double *px, double *py, double *pz, double *vx, double *vy, double *vz);
-cudaError_t split_drift_far(const Launch &L, SplitBufs &s, int64_t n, double dt, const uint8_t *kind, double *px,
-                            double *py, double *pz, const double *vx, const double *vy, const double *vz);
+                              double c, double *px, double *py, double *pz, double *vx, double *vy, double *vz);
+cudaError_t split_drift_far(const Launch &L, SplitBufs &s, int64_t n, double dt, double c, const uint8_t *kind,
+                            double *px, double *py, double *pz, const double *vx, const double *vy, const double *vz);
 
 // ---- adjoint.cu (gradient of the KDK leapfrog with the softened direct-sum force) ----
 struct AdjTape {

@@ -946,8 +946,10 @@ __global__ __launch_bounds__(kThreads) void k_kick(int64_t n, double h, double *
     vz[i] += h * az[i];
 }
 
-__global__ __launch_bounds__(kThreads) void k_kick_drift(int64_t n, double h, double dt, double *px, double *py,
-                                                         double *pz, double *vx, double *vy, double *vz,
+// kick (sim.go:305-313) then drift (sim.go:315-343): x += dt u for c <= 0 (inv_c2 == 0), else
+// x += dt u / sqrt(1 + u^2 / c^2) with the reference's 1 / c^2 factor inv_c2.
+__global__ __launch_bounds__(kThreads) void k_kick_drift(int64_t n, double h, double dt, double inv_c2, double *px,
+                                                         double *py, double *pz, double *vx, double *vy, double *vz,
                                                          const double *__restrict__ ax, const double *__restrict__ ay,
                                                          const double *__restrict__ az) {
     int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
@@ -956,9 +958,11 @@ __global__ __launch_bounds__(kThreads) void k_kick_drift(int64_t n, double h, do
     vx[i] = x;
     vy[i] = y;
     vz[i] = z;
-    px[i] += dt * x;
-    py[i] += dt * y;
-    pz[i] += dt * z;
+    double f = dt;
+    if (inv_c2 > 0) f = dt / sqrt(1 + (x * x + y * y + z * z) * inv_c2);
+    px[i] += f * x;
+    py[i] += f * y;
+    pz[i] += f * z;
 }
 
 // ---------------------------------------------------------------- direct sum (direct.go:18-48)
@@ -1588,10 +1592,12 @@ cudaError_t kick(const Launch &L, int64_t n, double h, double *vx, double *vy, d
     return cudaSuccess;
 }
 
-cudaError_t kick_drift(const Launch &L, int64_t n, double h, double dt, double *px, double *py, double *pz, double *vx,
-                       double *vy, double *vz, const double *ax, const double *ay, const double *az) {
+cudaError_t kick_drift(const Launch &L, int64_t n, double h, double dt, double c, double *px, double *py, double *pz,
+                       double *vx, double *vy, double *vz, const double *ax, const double *ay, const double *az) {
     if (n == 0) return cudaSuccess;
-    k_kick_drift<<<blocks_for(n, kThreads), kThreads, 0, L.stream>>>(n, h, dt, px, py, pz, vx, vy, vz, ax, ay, az);
+    const double inv_c2 = c > 0 ? 1 / (c * c) : 0.0;  // sim.go:335 (invC2)
+    k_kick_drift<<<blocks_for(n, kThreads), kThreads, 0, L.stream>>>(n, h, dt, inv_c2, px, py, pz, vx, vy, vz, ax, ay,
+                                                                     az);
     GBH_LAUNCH_CHECK();
     return cudaSuccess;
 }
@@ -1974,14 +1980,17 @@ __global__ __launch_bounds__(kThreads) void k_block_open(int64_t n, double T, in
     atomicMin(&info->next_tick, e);
 }
 
-__global__ __launch_bounds__(kThreads) void k_block_drift(int64_t n, double dt, double *px, double *py, double *pz,
-                                                          const double *__restrict__ vx, const double *__restrict__ vy,
-                                                          const double *__restrict__ vz) {
+// driftOne (sim.go:345-350): x += dt u / gamma(u, c), gamma = 1 for c <= 0 (relativity.go:15-20).
+__global__ __launch_bounds__(kThreads) void k_block_drift(int64_t n, double dt, double c, double *px, double *py,
+                                                          double *pz, const double *__restrict__ vx,
+                                                          const double *__restrict__ vy, const double *__restrict__ vz) {
     int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    px[i] += dt * vx[i];
-    py[i] += dt * vy[i];
-    pz[i] += dt * vz[i];
+    double ux = vx[i], uy = vy[i], uz = vz[i];
+    double f = dt / (c <= 0 ? 1.0 : sqrt(1 + (ux * ux + uy * uy + uz * uz) / (c * c)));
+    px[i] += f * ux;
+    py[i] += f * uy;
+    pz[i] += f * uz;
 }
 
 // Bodies whose step ends at tick: closing half kick with the new acceleration, then (before
@@ -2028,9 +2037,9 @@ cudaError_t block_open(const Launch &L, const TreeBufs &b, int64_t n, double T, 
     return cudaSuccess;
 }
 
-cudaError_t block_drift(const Launch &L, int64_t n, double dt, double *px, double *py, double *pz, const double *vx,
-                        const double *vy, const double *vz) {
-    k_block_drift<<<blocks_for(n, kThreads), kThreads, 0, L.stream>>>(n, dt, px, py, pz, vx, vy, vz);
+cudaError_t block_drift(const Launch &L, int64_t n, double dt, double c, double *px, double *py, double *pz,
+                        const double *vx, const double *vy, const double *vz) {
+    k_block_drift<<<blocks_for(n, kThreads), kThreads, 0, L.stream>>>(n, dt, c, px, py, pz, vx, vy, vz);
     GBH_LAUNCH_CHECK();
     return cudaSuccess;
 }

@@ -86,7 +86,7 @@ class Solver:
 
     def params(self, p: Params) -> abi.Params:
         return abi.make_params(self.theta, p.softening, self.leaf_size, self.monopole_only, p.dark_matter_off,
-                               self.walk)
+                               self.walk, c=p.c)
 
     def accelerations(self, s: State, p: Params) -> None:
         """Fills s.acc_* (bh.go:125-151): holes get 0, dead bodies keep their entries."""

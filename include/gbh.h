@@ -71,6 +71,9 @@ typedef struct {
     int32_t walk;            /* GBH_WALK_* */
     int32_t group_size;      /* stars per warp of GBH_WALK_MIXED: 64 (0 means 64) or 32 */
     int32_t reserved;        /* zero */
+    double c;                /* speed of light of the steps (Params.C): 0 Newtonian; > 0 drifts by
+                                u / gamma (sim.go:315-343) and uses Paczynski-Wiita star-hole
+                                pairs in the hole-aware step (pair.go:26-35) */
 } gbh_params;
 
 enum {

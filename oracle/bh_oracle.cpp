@@ -552,6 +552,19 @@ namespace {
 
 double schwarzschild(double m, double c) { return c <= 0 ? 0 : 2 * m / (c * c); }  // relativity.go:49-54
 
+double gamma_of(double ux, double uy, double uz, double c) {  // relativity.go:15-20
+    if (c <= 0) return 1;
+    return std::sqrt(1 + (ux * ux + uy * uy + uz * uz) / (c * c));
+}
+
+double pair_force(double m, double r2, double eps2, double rs) {  // pair.go:26-35
+    double re2 = r2 + eps2;
+    double re = std::sqrt(re2);
+    if (rs == 0) return m / (re2 * re);
+    double den = std::max(re - rs, rs / 2);
+    return m / (den * den * re);
+}
+
 double pair_rs(uint8_t ki, double mi, uint8_t kj, double mj, double c) {  // pair.go:14-23
     bool hi = ki == ORC_BLACK_HOLE, hj = kj == ORC_BLACK_HOLE;
     if (c <= 0 || hi == hj) return 0;
@@ -839,7 +852,7 @@ void orc_direct_targets(int64_t n, const double *px, const double *py, const dou
 void orc_kdk(int64_t n, double *px, double *py, double *pz, double *vx, double *vy, double *vz,
              double *ax, double *ay, double *az, const double *mass, const uint8_t *kind,
              const uint8_t *alive, double dt, double eps, double theta, int leaf_size, int monopole_only,
-             int dm_off, int acc_valid, int64_t nsteps, int workers) {
+             int dm_off, int acc_valid, int64_t nsteps, int workers, double c) {
     orc_tree t;
     t.theta = theta == 0 ? 0.9 : theta;
     t.leaf = leaf_size > 0 ? leaf_size : 24;
@@ -856,10 +869,21 @@ void orc_kdk(int64_t n, double *px, double *py, double *pz, double *vx, double *
             vy[i] += h * ay[i];
             vz[i] += h * az[i];
         }
-        for (int64_t i = 0; i < n; ++i) {  // drift sim.go:327-334 (c <= 0)
-            px[i] += dt * vx[i];
-            py[i] += dt * vy[i];
-            pz[i] += dt * vz[i];
+        if (c <= 0) {
+            for (int64_t i = 0; i < n; ++i) {  // drift sim.go:327-334
+                px[i] += dt * vx[i];
+                py[i] += dt * vy[i];
+                pz[i] += dt * vz[i];
+            }
+        } else {
+            const double inv_c2 = 1 / (c * c);
+            for (int64_t i = 0; i < n; ++i) {  // drift sim.go:335-343: the coordinate velocity u / gamma
+                double ux = vx[i], uy = vy[i], uz = vz[i];
+                double f = dt / std::sqrt(1 + (ux * ux + uy * uy + uz * uz) * inv_c2);
+                px[i] += f * ux;
+                py[i] += f * uy;
+                pz[i] += f * uz;
+            }
         }
         forces();  // advanceGas without gas: Solver.Accelerations (blockstep.go:129-135)
         for (int64_t i = 0; i < n; ++i) {
@@ -877,19 +901,13 @@ constexpr double kSubstepsPerTau = 20.0;  // split.go:20-21
 constexpr int kMaxSubsteps = 256;         // split.go:22-23
 constexpr int64_t kHoleChunk = 256;       // bodies per partial sum of a hole's far-star pull
 
-// pair.go:26-35 (PairForce) with rs = 0.
-inline double pair_force0(double m, double r2, double eps2) {
-    double re2 = r2 + eps2;
-    double re = std::sqrt(re2);
-    return m / (re2 * re);
-}
 
 }  // namespace
 
 void orc_split_kdk(int64_t n, double *px, double *py, double *pz, double *vx, double *vy, double *vz, double *ax,
                    double *ay, double *az, const double *mass, const uint8_t *kind, const uint8_t *alive, double dt,
                    double eps, double theta, int leaf_size, int monopole_only, int dm_off, int acc_valid,
-                   int64_t nsteps, int workers, int64_t *substeps, uint8_t *near_out) {
+                   int64_t nsteps, int workers, int64_t *substeps, uint8_t *near_out, double c) {
     orc_tree t;
     t.theta = theta == 0 ? 0.9 : theta;
     t.leaf = leaf_size > 0 ? leaf_size : 24;
@@ -905,11 +923,13 @@ void orc_split_kdk(int64_t n, double *px, double *py, double *pz, double *vx, do
     std::vector<int64_t> holes, near;
     std::vector<uint8_t> is_near(size_t(n), 0);
     std::vector<double> far(3 * size_t(n)), fast(3 * size_t(n));
+    auto kind_of = [&](int64_t i) -> uint8_t { return kind ? kind[i] : uint8_t(ORC_STAR); };
     // split.go:27-36
     auto timescale = [&](int64_t i, int64_t hh) {
         double dx = px[i] - px[hh], dy = py[i] - py[hh], dz = pz[i] - pz[hh];
         double r2 = dx * dx + dy * dy + dz * dz;
-        double a = pair_force0(mass[hh], r2, eps2) * std::sqrt(r2);
+        double rs = pair_rs(kind_of(i), mass[i], ORC_BLACK_HOLE, mass[hh], c);
+        double a = pair_force(mass[hh], r2, eps2, rs) * std::sqrt(r2);
         if (a == 0) return std::numeric_limits<double>::infinity();
         return std::sqrt(std::sqrt(r2 + eps2) / a);
     };
@@ -919,7 +939,8 @@ void orc_split_kdk(int64_t n, double *px, double *py, double *pz, double *vx, do
         for (int64_t hh : holes) {
             if (hh == i) continue;
             double dx = px[hh] - px[i], dy = py[hh] - py[i], dz = pz[hh] - pz[i];
-            double f = pair_force0(mass[hh], dx * dx + dy * dy + dz * dz, eps2);
+            double rs = pair_rs(kind_of(i), mass[i], ORC_BLACK_HOLE, mass[hh], c);
+            double f = pair_force(mass[hh], dx * dx + dy * dy + dz * dz, eps2, rs);
             fx += f * dx;
             fy += f * dy;
             fz += f * dz;
@@ -934,12 +955,13 @@ void orc_split_kdk(int64_t n, double *px, double *py, double *pz, double *vx, do
         });
         for (int64_t hh : holes) {
             double x = px[hh], y = py[hh], z = pz[hh];
+            double rs = schwarzschild(mass[hh], c);
             for (int64_t c0 = 0; c0 < n; c0 += kHoleChunk) {
                 double sx = 0, sy = 0, sz = 0;
                 for (int64_t i = c0; i < std::min(n, c0 + kHoleChunk); ++i) {
                     if (is_hole(i) || is_near[size_t(i)]) continue;
                     double dx = px[i] - x, dy = py[i] - y, dz = pz[i] - z;
-                    double f = pair_force0(src_mass(i), dx * dx + dy * dy + dz * dz, eps2);
+                    double f = pair_force(src_mass(i), dx * dx + dy * dy + dz * dz, eps2, rs);
                     sx += f * dx;
                     sy += f * dy;
                     sz += f * dz;
@@ -955,11 +977,12 @@ void orc_split_kdk(int64_t n, double *px, double *py, double *pz, double *vx, do
         for (int64_t i : near) hole_pull(i, fast[size_t(i)], fast[size_t(n + i)], fast[size_t(2 * n + i)]);
         for (int64_t hh : holes) {
             double x = px[hh], y = py[hh], z = pz[hh];
+            double rs = schwarzschild(mass[hh], c);
             double sx, sy, sz;
             hole_pull(hh, sx, sy, sz);
             for (int64_t i : near) {
                 double dx = px[i] - x, dy = py[i] - y, dz = pz[i] - z;
-                double f = pair_force0(src_mass(i), dx * dx + dy * dy + dz * dz, eps2);
+                double f = pair_force(src_mass(i), dx * dx + dy * dy + dz * dz, eps2, rs);
                 sx += f * dx;
                 sy += f * dy;
                 sz += f * dz;
@@ -984,9 +1007,9 @@ void orc_split_kdk(int64_t n, double *px, double *py, double *pz, double *vx, do
                 vz[i] += k * fast[size_t(2 * n + i)];
             }
     };
-    auto drift_idx = [&](const std::vector<int64_t> &idx, double d) {  // split.go:226-234, c = 0
+    auto drift_idx = [&](const std::vector<int64_t> &idx, double d) {  // split.go:226-234
         for (int64_t i : idx) {
-            double f = d / 1.0;
+            double f = d / gamma_of(vx[i], vy[i], vz[i], c);
             px[i] += f * vx[i];
             py[i] += f * vy[i];
             pz[i] += f * vz[i];
@@ -1004,10 +1027,13 @@ void orc_split_kdk(int64_t n, double *px, double *py, double *pz, double *vx, do
                 vy[i] += h * ay[i];
                 vz[i] += h * az[i];
             }
-            for (int64_t i = 0; i < n; ++i) {
-                px[i] += dt * vx[i];
-                py[i] += dt * vy[i];
-                pz[i] += dt * vz[i];
+            const double inv_c2 = c > 0 ? 1 / (c * c) : 0;
+            for (int64_t i = 0; i < n; ++i) {  // drift sim.go:315-343
+                double f = dt;
+                if (c > 0) f = dt / std::sqrt(1 + (vx[i] * vx[i] + vy[i] * vy[i] + vz[i] * vz[i]) * inv_c2);
+                px[i] += f * vx[i];
+                py[i] += f * vy[i];
+                pz[i] += f * vz[i];
             }
             forces();
             for (int64_t i = 0; i < n; ++i) {
@@ -1056,7 +1082,7 @@ void orc_split_kdk(int64_t n, double *px, double *py, double *pz, double *vx, do
         }
         for (int64_t i = 0; i < n; ++i) {  // driftFar
             if (is_hole(i) || is_near[size_t(i)]) continue;
-            double f = dt / 1.0;
+            double f = dt / gamma_of(vx[i], vy[i], vz[i], c);
             px[i] += f * vx[i];
             py[i] += f * vy[i];
             pz[i] += f * vz[i];
@@ -1073,7 +1099,7 @@ void orc_split_kdk(int64_t n, double *px, double *py, double *pz, double *vx, do
 void orc_block_kdk(int64_t n, double *px, double *py, double *pz, double *vx, double *vy, double *vz, double *ax,
                    double *ay, double *az, const double *mass, const uint8_t *kind, const uint8_t *alive, double T,
                    double eta, int levels, double eps, double theta, int leaf_size, int monopole_only, int dm_off,
-                   int acc_valid, int64_t nsteps, int workers, int64_t *substeps, int64_t *evals) {
+                   int acc_valid, int64_t nsteps, int workers, int64_t *substeps, int64_t *evals, double c) {
     orc_tree t;
     t.theta = theta == 0 ? 0.9 : theta;
     t.leaf = leaf_size > 0 ? leaf_size : 24;
@@ -1118,9 +1144,10 @@ void orc_block_kdk(int64_t n, double *px, double *py, double *pz, double *vx, do
             int32_t tn = next;
             double d = double(tn - tk) * (T / double(ticks));
             for (int64_t i = 0; i < n; ++i) {
-                px[i] += d * vx[i];
-                py[i] += d * vy[i];
-                pz[i] += d * vz[i];
+                double f = d / gamma_of(vx[i], vy[i], vz[i], c);  // driftOne, sim.go:345-350
+                px[i] += f * vx[i];
+                py[i] += f * vy[i];
+                pz[i] += f * vz[i];
             }
             tk = tn;
             t.build(n, px, py, pz, mass, kind, alive, dm_off);
@@ -1313,6 +1340,12 @@ void orc_adjoint_direct(int64_t n, const double *px, const double *py, const dou
     std::copy(lw.begin(), lw.end(), dvz);
     std::copy(lm.begin(), lm.end(), dm);
 }
+
+double orc_pair_force(double m, double r2, double eps2, double rs) { return pair_force(m, r2, eps2, rs); }
+double orc_pair_potential(double mi, double mj, double r2, double eps2, double rs) {
+    return pair_potential(mi, mj, r2, eps2, rs);
+}
+double orc_pair_rs(uint8_t ki, double mi, uint8_t kj, double mj, double c) { return pair_rs(ki, mi, kj, mj, c); }
 
 double orc_potential_exact(int64_t n, const double *px, const double *py, const double *pz,
                            const double *mass, const uint8_t *kind, double eps, double c, int dm_off,

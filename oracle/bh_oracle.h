@@ -113,7 +113,7 @@ void orc_direct_targets(int64_t n, const double *px, const double *py, const dou
 
 /*
  * sim.go:252-288 with no holes and no gas: nsteps KDK steps with the
- * Barnes-Hut solver (c = 0 drift, sim.go:327-334). Forces at entry are taken
+ * Barnes-Hut solver (drift sim.go:315-343: x += dt v for c <= 0, x += dt u / gamma for c > 0). Forces at entry are taken
  * from acc when acc_valid, else computed first (initForces, gas.go:14-17).
  * Arrays are updated in place.
  */
@@ -121,7 +121,7 @@ void orc_kdk(int64_t n, double *px, double *py, double *pz, double *vx, double *
              double *vz, double *ax, double *ay, double *az, const double *mass,
              const uint8_t *kind, const uint8_t *alive, double dt, double eps, double theta,
              int leaf_size, int monopole_only, int dark_matter_off, int acc_valid,
-             int64_t nsteps, int workers);
+             int64_t nsteps, int workers, double c);
 
 /*
  * Block time steps for gravity, on the scheme of the reference's gas block steps
@@ -135,12 +135,14 @@ void orc_block_kdk(int64_t n, double *px, double *py, double *pz, double *vx, do
                    double *vz, double *ax, double *ay, double *az, const double *mass,
                    const uint8_t *kind, const uint8_t *alive, double dt, double eta, int levels,
                    double eps, double theta, int leaf_size, int monopole_only, int dark_matter_off,
-                   int acc_valid, int64_t nsteps, int workers, int64_t *substeps, int64_t *evals);
+                   int acc_valid, int64_t nsteps, int workers, int64_t *substeps, int64_t *evals,
+                   double c);
 
 /*
- * The hole-aware step of internal/sim/split.go:1-259 (stepSplit) with c = 0 (Newtonian pairs,
- * pair.go:26-35 with rs = 0; no relativistic drift, frame dragging, retardation or accretion)
- * and no gas: star-star forces from the tree once per step; every force involving an alive
+ * The hole-aware step of internal/sim/split.go:1-259 (stepSplit) without gas, with the pair model
+ * of pair.go:26-35 (Paczynski-Wiita star-hole forces for c > 0) and the drift of u / gamma, but
+ * with instant gravity, no frame dragging (no spins) and no accretion or collapse (those follow
+ * the step in sim.go:260-287 and are not restated): star-star forces from the tree once per step; every force involving an alive
  * black hole summed directly; stars whose timescale at a hole is below 20 dt ("near") and the
  * holes take n power-of-two substeps (classify, split.go:41-81). Steps without holes are the
  * plain KDK of orc_kdk. A hole's pull from the far stars is summed in chunks of 256 bodies
@@ -152,7 +154,7 @@ void orc_split_kdk(int64_t n, double *px, double *py, double *pz, double *vx, do
                    double *vz, double *ax, double *ay, double *az, const double *mass,
                    const uint8_t *kind, const uint8_t *alive, double dt, double eps, double theta,
                    int leaf_size, int monopole_only, int dark_matter_off, int acc_valid,
-                   int64_t nsteps, int workers, int64_t *substeps, uint8_t *near);
+                   int64_t nsteps, int workers, int64_t *substeps, uint8_t *near, double c);
 
 /*
  * Adjoint of the KDK leapfrog (sim.go:302-343) with the softened direct-sum force
@@ -172,6 +174,11 @@ void orc_adjoint_direct(int64_t n, const double *px, const double *py, const dou
 void orc_kdk_direct(int64_t n, double *px, double *py, double *pz, double *vx, double *vy,
                     double *vz, const double *mass, double eps, double dt, int64_t nsteps,
                     int workers);
+
+/* The pair model (pair.go:14-47): PairForce, PairPotential, PairRS. */
+double orc_pair_force(double m, double r2, double eps2, double rs);
+double orc_pair_potential(double mi, double mj, double r2, double eps2, double rs);
+double orc_pair_rs(uint8_t ki, double mi, uint8_t kj, double mj, double c);
 
 /* diag.go:44-64 exact pair potential (no holes: plain softened Newtonian). */
 double orc_potential_exact(int64_t n, const double *px, const double *py, const double *pz,

@@ -64,13 +64,16 @@ def lib():
             "orc_tree_potential": (_D, [_P, _I64, _P, _P, _P, _P, _P, _P, _D, _D, _INT, _INT, _INT]),
             "orc_direct": (None, [_I64, _P, _P, _P, _P, _P, _D, _INT, _INT, _P, _P, _P]),
             "orc_direct_targets": (None, [_I64, _P, _P, _P, _P, _P, _D, _INT, _P, _I64, _INT, _P, _P, _P]),
-            "orc_kdk": (None, [_I64] + [_P] * 12 + [_D, _D, _D, _INT, _INT, _INT, _INT, _I64, _INT]),
+            "orc_kdk": (None, [_I64] + [_P] * 12 + [_D, _D, _D, _INT, _INT, _INT, _INT, _I64, _INT, _D]),
             "orc_potential_exact": (_D, [_I64, _P, _P, _P, _P, _P, _D, _D, _INT, _INT]),
-            "orc_split_kdk": (None, [_I64] + [_P] * 12 + [_D, _D, _D, _INT, _INT, _INT, _INT, _I64, _INT, _P, _P]),
+            "orc_split_kdk": (None, [_I64] + [_P] * 12 + [_D, _D, _D, _INT, _INT, _INT, _INT, _I64, _INT, _P, _P, _D]),
+            "orc_pair_force": (_D, [_D, _D, _D, _D]),
+            "orc_pair_potential": (_D, [_D, _D, _D, _D, _D]),
+            "orc_pair_rs": (_D, [ctypes.c_uint8, _D, ctypes.c_uint8, _D, _D]),
             "orc_adjoint_direct": (None, [_I64] + [_P] * 7 + [_D, _D, _I64, _I64] + [_P] * 13 + [_INT]),
             "orc_kdk_direct": (None, [_I64] + [_P] * 7 + [_D, _D, _I64, _INT]),
             "orc_block_kdk": (None, [_I64] + [_P] * 12 + [_D, _D, _INT, _D, _D, _INT, _INT, _INT, _INT, _I64, _INT,
-                                                         _P, _P]),
+                                                         _P, _P, _D]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -210,8 +213,9 @@ def potential_exact(px, py, pz, mass, kind=None, eps=0.0, c=0.0, dm_off=False, w
 
 
 def kdk(state: dict, dt, eps, theta, leaf, nsteps, monopole_only=False, dm_off=False,
-        acc_valid=False, workers=0):
-    """nsteps KDK steps (sim.go:252-288, no holes, no gas) on a dict of SoA arrays, in place."""
+        acc_valid=False, workers=0, c=0.0):
+    """nsteps KDK steps (sim.go:252-288, no holes, no gas; drift of u / gamma when c > 0) on a
+    dict of SoA arrays, in place."""
     s = state
     n = len(s["px"])
     for k in ("px", "py", "pz", "vx", "vy", "vz", "ax", "ay", "az", "mass"):
@@ -220,12 +224,12 @@ def kdk(state: dict, dt, eps, theta, leaf, nsteps, monopole_only=False, dm_off=F
     alive = _u8(s.get("alive", np.ones(n, np.uint8)))
     lib().orc_kdk(n, *[_ptr(s[k]) for k in ("px", "py", "pz", "vx", "vy", "vz", "ax", "ay", "az", "mass")],
                   _ptr(kind), _ptr(alive), dt, eps, theta, leaf, int(monopole_only), int(dm_off),
-                  int(acc_valid), nsteps, workers)
+                  int(acc_valid), nsteps, workers, float(c))
     return s
 
 
 def block_kdk(state: dict, dt, eta, levels, eps, theta, leaf, nsteps, monopole_only=False, dm_off=False,
-              acc_valid=False, workers=0):
+              acc_valid=False, workers=0, c=0.0):
     """Block-step KDK (the scheme of gbh_state_step_block) on a dict of SoA arrays, in place;
     returns (events, walked stars)."""
     s = state
@@ -235,7 +239,7 @@ def block_kdk(state: dict, dt, eta, levels, eps, theta, leaf, nsteps, monopole_o
     a, b = np.zeros(1, np.int64), np.zeros(1, np.int64)
     lib().orc_block_kdk(n, *[_ptr(s[k]) for k in ("px", "py", "pz", "vx", "vy", "vz", "ax", "ay", "az", "mass")],
                         _ptr(kind), _ptr(alive), dt, eta, levels, eps, theta, leaf, int(monopole_only), int(dm_off),
-                        int(acc_valid), nsteps, workers, _ptr(a), _ptr(b))
+                        int(acc_valid), nsteps, workers, _ptr(a), _ptr(b), float(c))
     return int(a[0]), int(b[0])
 
 
@@ -263,9 +267,9 @@ def adjoint_direct(state: dict, dt, eps, nsteps, every, gx, gv, workers=0):
 
 
 def split_kdk(state: dict, dt, eps, theta, leaf, nsteps, monopole_only=False, dm_off=False, acc_valid=False,
-              workers=0):
-    """The hole-aware step (split.go, c = 0, no gas) on a dict of SoA arrays, in place; returns
-    (substeps of the last step, near flags of the last step)."""
+              workers=0, c=0.0):
+    """The hole-aware step (split.go, no gas, instant gravity, no spins) on a dict of SoA arrays,
+    in place; returns (substeps of the last step, near flags of the last step)."""
     s = state
     n = len(s["px"])
     for k in ("px", "py", "pz", "vx", "vy", "vz", "ax", "ay", "az", "mass"):
@@ -276,5 +280,17 @@ def split_kdk(state: dict, dt, eps, theta, leaf, nsteps, monopole_only=False, dm
     near = np.zeros(n, np.uint8)
     lib().orc_split_kdk(n, *[_ptr(s[k]) for k in ("px", "py", "pz", "vx", "vy", "vz", "ax", "ay", "az", "mass")],
                         _ptr(kind), _ptr(alive), dt, eps, theta, leaf, int(monopole_only), int(dm_off),
-                        int(acc_valid), nsteps, workers, _ptr(sub), _ptr(near))
+                        int(acc_valid), nsteps, workers, _ptr(sub), _ptr(near), float(c))
     return int(sub[0]), near.astype(bool)
+
+
+def pair_force(m, r2, eps2, rs):
+    return lib().orc_pair_force(m, r2, eps2, rs)
+
+
+def pair_potential(mi, mj, r2, eps2, rs):
+    return lib().orc_pair_potential(mi, mj, r2, eps2, rs)
+
+
+def pair_rs(ki, mi, kj, mj, c):
+    return lib().orc_pair_rs(ki, mi, kj, mj, c)

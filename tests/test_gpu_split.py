@@ -108,3 +108,44 @@ def test_forest_with_holes_is_rejected(ctx):
     with pytest.raises(abi.GbhError) as ei:
         ctx.call("gbh_state_step", abi.make_params(0.5, 0.06, 8), 0.004, 1)
     assert ei.value.code == abi.ERR_UNSUPPORTED
+
+
+@pytest.mark.parametrize("c", [10.0, 3.0])
+def test_fp64_split_steps_with_speed_of_light_bit_exact(ctx, c):
+    """c > 0: Paczynski-Wiita star-hole pairs (pair.go:26-35) in the direct hole sums and the
+    timescales, and every drift by u / gamma (split.go:226-250)."""
+    s = disk_with_extras(3000, seed=3)
+    par = abi.make_params(0.5, 0.06, 8, False, False, "fp64", c=c)
+    got, sub = step_host(ctx, s, par, 0.004, 10)
+    ref = {k: s[k].copy() for k in (*F9, "mass", "kind", "alive")}
+    rsub, _ = O.split_kdk(ref, 0.004, 0.06, 0.5, 8, 10, c=c)
+    assert sub == rsub
+    for k in F9:
+        assert np.array_equal(got[k], ref[k]), k
+    newton, _ = step_host(ctx, s, abi.make_params(0.5, 0.06, 8, False, False, "fp64"), 0.004, 10)
+    assert not np.array_equal(newton["px"], got["px"])  # the speed of light changed the run
+
+
+def test_fp64_kdk_and_block_steps_with_speed_of_light_bit_exact(ctx):
+    """Without holes: the global KDK's drift u / sqrt(1 + u^2 / c^2) (sim.go:335-343) and the block
+    steps' driftOne (sim.go:345-350), against the oracle."""
+    s = ics.plummer(5000, seed=8)
+    for k in ("vx", "vy", "vz"):
+        s[k] = s[k] * 4.0  # fast enough that gamma matters at c = 3
+    n = len(s["px"])
+    par = abi.make_params(0.5, 0.01, 8, False, False, "fp64", c=3.0)
+    got, _ = step_host(ctx, s, par, 1e-3, 5)
+    ref = {k: s[k].copy() for k in (*F9, "mass")}
+    O.kdk(ref, dt=1e-3, eps=0.01, theta=0.5, leaf=8, nsteps=5, c=3.0)
+    for k in F9:
+        assert np.array_equal(got[k], ref[k]), k
+    ctx.call("gbh_state_upload", n, *[P(s[k]) for k in ("px", "py", "pz", "vx", "vy", "vz")], None, None, None,
+             P(s["mass"]), None, None)
+    st = ctx.step_block(par, 1e-2, 0.025, 6, 2)
+    blk = {k: np.zeros(n) for k in F9}
+    ctx.call("gbh_state_download", *[P(blk[k]) for k in F9])
+    ref = {k: s[k].copy() for k in (*F9, "mass")}
+    events, walked = O.block_kdk(ref, dt=1e-2, eta=0.025, levels=6, eps=0.01, theta=0.5, leaf=8, nsteps=2, c=3.0)
+    assert (st["substeps"], st["evaluations"]) == (events, walked)
+    for k in F9:
+        assert np.array_equal(blk[k], ref[k]), k

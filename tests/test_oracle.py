@@ -359,3 +359,38 @@ def test_split_without_holes_is_the_plain_step():
     assert sub == 1 and not near.any()
     for k in a:
         assert np.array_equal(a[k], b[k]), k
+
+
+# ---- the pair model (pair.go), behind the split step for c > 0 ----
+
+def test_pair_force_is_gradient_of_potential():  # pair_test.go:8-18
+    m, eps2, h = 0.7, 0.01 * 0.01, 1e-7
+    for rs in (0.0, 0.05):
+        for r in (0.06, 0.074, 0.08, 0.15, 0.4, 2.0):  # below and above 1.5 rs
+            du = (O.pair_potential(1, m, (r + h) ** 2, eps2, rs) - O.pair_potential(1, m, (r - h) ** 2, eps2, rs)) / (2 * h)
+            f = O.pair_force(m, r * r, eps2, rs) * r
+            assert abs(f - du) <= 1e-6 * abs(f), (rs, r, f, du)
+
+
+def test_pair_potential_limits():  # pair_test.go:20-31
+    assert O.pair_potential(2, 3, 4, 0, 0) == -3.0
+    assert abs(O.pair_potential(1, 1, 1, 0, 0.1) - (-1 / 0.9)) <= 1e-15
+    S, H, D = O.STAR, O.BLACK_HOLE, O.DARK_MATTER
+    assert O.pair_rs(S, 1, S, 1, 10) == 0 and O.pair_rs(H, 1, H, 1, 10) == 0 and O.pair_rs(S, 1, H, 5, 10) == 0.1
+
+
+def test_dark_matter_pairs_are_newtonian_except_with_holes():  # pair_test.go:33-41
+    S, H, D = O.STAR, O.BLACK_HOLE, O.DARK_MATTER
+    assert O.pair_rs(D, 1, S, 1, 10) == 0 and O.pair_rs(S, 1, D, 1, 10) == 0 and O.pair_rs(D, 1, D, 1, 10) == 0
+    assert O.pair_rs(D, 1, H, 5, 10) == 0.1
+
+
+def test_relativistic_drift_slows_fast_bodies():
+    """sim.go:315-343: with c > 0 a body moves by dt u / gamma; a body at u = c sqrt(3) drifts half
+    as far as with c = 0 (gamma = 2), and slow bodies agree with the Newtonian drift."""
+    z = np.zeros(2)
+    s = dict(px=np.array([0.0, 1e6]), py=z.copy(), pz=z.copy(), vx=np.array([10 * np.sqrt(3), 1e-3]), vy=z.copy(),
+             vz=z.copy(), ax=z.copy(), ay=z.copy(), az=z.copy(), mass=np.array([1e-12, 1e-12]))
+    O.kdk(s, dt=1e-2, eps=0.1, theta=0.5, leaf=8, nsteps=1, c=10.0, workers=1)
+    assert abs(s["px"][0] - 1e-2 * 10 * np.sqrt(3) / 2) <= 1e-12
+    assert abs(s["px"][1] - (1e6 + 1e-5)) <= 1e-9
