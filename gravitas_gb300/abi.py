@@ -37,6 +37,7 @@ class Params(ctypes.Structure):
 
 CFG_NO_GRAPHS = 1
 CFG_BLOCKING_SYNC = 2
+CFG_NO_LPT = 4
 
 
 class Config(ctypes.Structure):

@@ -78,6 +78,7 @@ struct gbh_ctx {
     gbh::SplitBufs split;             // buffers of the hole-aware step
     std::vector<int32_t> hole_list;   // alive holes of the resident state, ascending
     bool use_graphs = true;
+    bool use_lpt = true;  // longest-first group order of the mixed walk
     cudaEvent_t wait_ev = nullptr;  // GBH_CFG_BLOCKING_SYNC: host waits sleep on this event
     cudaEvent_t ahead[4] = {};      // GBH_CFG_BLOCKING_SYNC: ends of the last steps launched
     bool capturing = false;  // stage events become graph event-record nodes
@@ -258,6 +259,7 @@ int forces(gbh_ctx *ctx, const gbh_params *p, int64_t n, const double *px, const
     forest = forest && ctx->nsys > 1;
     CK(gbh::tree_alloc(ctx->tb, n, leaf, forest ? ctx->nsys : 1));
     ctx->tb.group = p->group_size == 32 ? 32 : 64;
+    ctx->tb.lpt = ctx->use_lpt;
     CK(stage_event(ctx));
     CK(gbh::tree_build(L, ctx->tb, n, px, py, pz, mass, kind, alive, ax, ay, az, theta, leaf, p->dark_matter_off,
                        p->walk == GBH_WALK_FP64, p->walk == GBH_WALK_PLAIN, forest ? ctx->sys_of : nullptr,
@@ -667,6 +669,7 @@ int gbh_create(const gbh_config *cfg, gbh_ctx **out, char *err, int errlen) {
     gbh_ctx *c = new gbh_ctx();
     c->device = dev;
     c->use_graphs = !(cfg && (cfg->flags & GBH_CFG_NO_GRAPHS));
+    c->use_lpt = !(cfg && (cfg->flags & GBH_CFG_NO_LPT));
     if (cfg && (cfg->flags & GBH_CFG_BLOCKING_SYNC)) {
         e = cudaEventCreateWithFlags(&c->wait_ev, cudaEventBlockingSync | cudaEventDisableTiming);
         for (auto &ev : c->ahead)

@@ -112,6 +112,12 @@ struct TreeBufs {
     int32_t *sid_sorted = nullptr;  // only when nsys > 1
     int4 *groups = nullptr;         // (first sorted star, count, root, 0); only when nsys > 1
     int64_t cap_groups = 0;
+    // Longest-first launch order of the single-system mixed walk: the walk records each group's
+    // cost, k_lpt_order turns the costs into the order of the next walk (gperm[cap_groups] = the
+    // group count it was made for; any other count means launch order).
+    uint32_t *gcost = nullptr;
+    int32_t *gperm = nullptr;
+    bool lpt = true;                // set per call by the caller
     bool moments_exact = false;     // the last build ran the bit-exact FP64 upsweep
     // scan temporaries
     uint32_t *scan_tmp = nullptr;

@@ -1368,7 +1368,7 @@ static cudaError_t scan_dyn(const Launch &L, const uint32_t *in, uint32_t *out, 
 
 void tree_free(TreeBufs &b) {
     void *ptrs[] = {b.flag, b.bbox_part, b.keys, b.keys_alt, b.order, b.order_alt, b.hist, b.sx, b.sy, b.sz, b.sm,
-                    b.st_hi, b.st_lo, b.st_off, b.chain_cnt, b.leaves, b.targets, b.geo, b.sid_sorted, b.groups, b.pre_parent, b.pre_info, b.pre_nchild, b.pre_mask, b.pre_ref, b.nodes,
+                    b.st_hi, b.st_lo, b.st_off, b.chain_cnt, b.leaves, b.targets, b.geo, b.sid_sorted, b.groups, b.gcost, b.gperm, b.pre_parent, b.pre_info, b.pre_nchild, b.pre_mask, b.pre_ref, b.nodes,
                     b.n_parent, b.n_info, b.n_arrive, b.pnodes, b.mnodes, b.mrange, b.scan_tmp, b.info};
     for (void *p : ptrs)
         if (p) cudaFree(p);
@@ -1426,6 +1426,8 @@ cudaError_t tree_alloc(TreeBufs &b, int64_t n, int leaf, int32_t nsys) {
     GBH_ALLOC(b.geo, csys);
     GBH_ALLOC(b.sid_sorted, cn);
     GBH_ALLOC(b.groups, cgroups);
+    GBH_ALLOC(b.gcost, cgroups);
+    GBH_ALLOC(b.gperm, cgroups + 1);
     GBH_ALLOC(b.pre_parent, cnodes);
     GBH_ALLOC(b.pre_info, cnodes);
     GBH_ALLOC(b.pre_nchild, cnodes);
@@ -1450,6 +1452,8 @@ cudaError_t tree_alloc(TreeBufs &b, int64_t n, int leaf, int32_t nsys) {
     b.cap_sys = csys;
     b.cap_groups = cgroups;
     b.nsys = nsys;
+    // no launch order yet: gperm[cap_groups] = -1 matches no group count
+    if ((e = cudaMemset(b.gperm, 0xff, sizeof(int32_t) * size_t(cgroups + 1))) != cudaSuccess) return e;
     return cudaMemset(b.info, 0, sizeof(DevInfo));
 }
 

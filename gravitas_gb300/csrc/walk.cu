@@ -138,7 +138,8 @@ __global__ __launch_bounds__(kMixedThreads, 8) void k_walk_mixed2(const DevInfo 
                                                                double *ax, double *ay, double *az,
                                                                const int32_t *__restrict__ targets,
                                                                const int4 *__restrict__ groups, int pair,
-                                                               DevInfo *err_info) {
+                                                               const int32_t *__restrict__ gperm, int32_t perm_cap,
+                                                               uint32_t *gcost, DevInfo *err_info) {
     // pair: 64-star groups, lane l walks stars 2l and 2l + 1; else 32-star groups, one star per
     // lane (the second FP32x2 slot then repeats the first and is not written)
     const int lane = threadIdx.x & 31;
@@ -153,9 +154,13 @@ __global__ __launch_bounds__(kMixedThreads, 8) void k_walk_mixed2(const DevInfo 
         nt = e.x + e.y;
         root = e.z;
     } else {
-        base = g * (pair ? 64 : 32);
+        const int gsize = pair ? 64 : 32;
         nt = targets ? int32_t(info->ntargets) : ns;
-        if (base >= nt) return;  // uniform over the warp
+        if (g * gsize >= nt) return;  // uniform over the warp
+        // longest first: walk the group the last walk's costs put at this position
+        int32_t gw = g;
+        if (gperm && gperm[perm_cap] == (nt + gsize - 1) / gsize) gw = gperm[g];
+        base = gw * gsize;
     }
     const int32_t t0 = base + (pair ? 2 * lane : lane), t1 = t0 + 1;
     const bool v0 = t0 < nt, v1 = pair && t1 < nt;
@@ -171,7 +176,7 @@ __global__ __launch_bounds__(kMixedThreads, 8) void k_walk_mixed2(const DevInfo 
 
     float2 sx = f2(0.f), sy = f2(0.f), sz = f2(0.f), cx = f2(0.f), cy = f2(0.f), cz = f2(0.f);
     float2 px = f2(0.f), py = f2(0.f), pz = f2(0.f);
-    uint32_t visits = 0;
+    uint32_t visits = 0, pairs = 0;
     int i = nn > 0 ? root : -1;
     while (i >= 0) {
         if (uint32_t(i) >= nn) {
@@ -227,6 +232,7 @@ __global__ __launch_bounds__(kMixedThreads, 8) void k_walk_mixed2(const DevInfo 
                 if (lane == 0) set_err(err_info, 5);
                 break;
             }
+            pairs += uint32_t(r.y - r.x);
             // Leaf stars: separation = (leaf com - star) + (leaf star - com), the first the visit's
             // double-float separation, the second the star's FP32 offset stored by the upsweep.
 #pragma unroll 4  // measured 2-3 % faster than no unrolling (independent source stars)
@@ -273,6 +279,7 @@ __global__ __launch_bounds__(kMixedThreads, 8) void k_walk_mixed2(const DevInfo 
     kahan_fold2(sx, cx, px);
     kahan_fold2(sy, cy, py);
     kahan_fold2(sz, cz, pz);
+    if (gcost && lane == 0) gcost[base / (pair ? 64 : 32)] = 2u * visits + pairs;  // the group's cost
     if constexpr (kPot) {
         if (v0) ax[k0] = double(sx.x) - double(cx.x);
         if (v1) ax[k1] = double(sx.y) - double(cx.y);
@@ -325,17 +332,71 @@ cudaError_t walk_plain(const Launch &L, const TreeBufs &b, int64_t nstars_cap, f
     return cudaGetLastError();
 }
 
+// Longest-first order for the next walk from this walk's group costs: groups bucketed by
+// floor(log2 cost), most expensive bucket first, ascending group index inside a bucket (so that
+// neighbouring warps keep walking neighbouring groups). One block of kLptThreads threads, each
+// owning a contiguous run of groups.
+constexpr int kLptThreads = 512, kLptBuckets = 16;  // 32 KB of shared counts
+__global__ __launch_bounds__(kLptThreads) void k_lpt_order(const DevInfo *info, int gsize, const uint32_t *gcost,
+                                                           int32_t *gperm, int32_t perm_cap) {
+    __shared__ uint32_t cnt[kLptBuckets][kLptThreads];
+    __shared__ uint32_t base[kLptBuckets];
+    const int t = threadIdx.x;
+    const int32_t ng = int32_t((info->nstars + gsize - 1) / gsize);
+    if (ng > perm_cap) return;  // no order: the walk keeps launch order
+    const int32_t per = (ng + kLptThreads - 1) / kLptThreads;
+    const int32_t g0 = t * per, g1 = g0 + per < ng ? g0 + per : ng;
+    auto bucket = [&](uint32_t c) {
+        int l = 31 - __clz(c | 1u);
+        return kLptBuckets - 1 - (l < kLptBuckets ? l : kLptBuckets - 1);
+    };
+    for (int k = 0; k < kLptBuckets; ++k) cnt[k][t] = 0;
+    for (int32_t g = g0; g < g1; ++g) ++cnt[bucket(gcost[g])][t];
+    __syncthreads();
+    if (t < kLptBuckets) {  // exclusive scan of each bucket's row over the threads
+        uint32_t run = 0;
+        for (int q = 0; q < kLptThreads; ++q) {
+            uint32_t c = cnt[t][q];
+            cnt[t][q] = run;
+            run += c;
+        }
+        base[t] = run;
+    }
+    __syncthreads();
+    if (t == 0) {  // bucket totals to bucket offsets
+        uint32_t run = 0;
+        for (int k = 0; k < kLptBuckets; ++k) {
+            uint32_t c = base[k];
+            base[k] = run;
+            run += c;
+        }
+    }
+    __syncthreads();
+    for (int32_t g = g0; g < g1; ++g) {
+        int k = bucket(gcost[g]);
+        gperm[base[k] + cnt[k][t]++] = g;
+    }
+    __syncthreads();
+    if (t == 0) gperm[perm_cap] = ng;
+}
+
 template <bool kQuad, bool kSoft, bool kPot = false>
 static cudaError_t launch_mixed(const Launch &L, const TreeBufs &b, int64_t nstars_cap, float eps2, double *ax,
                                 double *ay, double *az, bool targets) {
     const bool forest = b.nsys > 1;
     const int gsize = b.group == 32 ? 32 : 64;
     int64_t groups = forest ? b.cap_groups : (nstars_cap + gsize - 1) / gsize;
+    const bool lpt = b.lpt && !forest && !targets && !kPot;
     int64_t blocks = (groups + kMixedThreads / 32 - 1) / (kMixedThreads / 32);
     k_walk_mixed2<kQuad, kSoft, kPot><<<unsigned(blocks < 1 ? 1 : blocks), kMixedThreads, 0, L.stream>>>(
         b.info, b.mnodes, b.mrange, b.st_hi, b.st_lo, b.st_off, b.order, eps2, ax, ay, az,
         targets ? b.targets : nullptr,
-        forest ? b.groups : nullptr, gsize == 64 ? 1 : 0, b.info);
+        forest ? b.groups : nullptr, gsize == 64 ? 1 : 0, lpt ? b.gperm : nullptr, int32_t(b.cap_groups),
+        lpt ? b.gcost : nullptr, b.info);
+    ++*L.count;
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess || !lpt) return e;
+    k_lpt_order<<<1, kLptThreads, 0, L.stream>>>(b.info, gsize, b.gcost, b.gperm, int32_t(b.cap_groups));
     ++*L.count;
     return cudaGetLastError();
 }

@@ -82,7 +82,10 @@ enum {
     /* Host waits for the GPU sleep on a blocking-sync event instead of spinning, so a caller
        thread blocked in a call (a goroutine running Accelerations while Hydro.Forces runs on
        the other cores, gas.go:20-25) leaves its core free. */
-    GBH_CFG_BLOCKING_SYNC = 2
+    GBH_CFG_BLOCKING_SYNC = 2,
+    /* The mixed walk launches its groups in index order instead of longest first (the order
+       the previous walk's group costs give); results are identical either way. */
+    GBH_CFG_NO_LPT = 4
 };
 
 typedef struct {
