@@ -311,11 +311,14 @@ int finish(gbh_ctx *ctx, bool tree) {
     return GBH_OK;
 }
 
+// Alive holes among n bodies. memchr (vectorised in the C library) skips the runs of other kinds,
+// so a host call on a million bodies costs tens of microseconds, not a byte loop.
 int count_holes(const uint8_t *kind, const uint8_t *alive, int64_t n) {
-    if (!kind) return 0;
+    if (!kind || n <= 0) return 0;
     int64_t h = 0;
-    for (int64_t i = 0; i < n; ++i)
-        if ((alive ? alive[i] : 1) && kind[i] == GBH_BLACK_HOLE) ++h;
+    for (const uint8_t *q = kind, *end = kind + n;
+         (q = static_cast<const uint8_t *>(std::memchr(q, GBH_BLACK_HOLE, size_t(end - q)))) != nullptr; ++q)
+        if (!alive || alive[q - kind]) ++h;
     return int(std::min<int64_t>(h, 1 << 30));
 }
 
@@ -621,8 +624,9 @@ int upload_state(gbh_ctx *ctx, int64_t n, const double *px, const double *py, co
     ctx->state_holes = count_holes(kind, alive, n);
     ctx->hole_list.clear();
     if (ctx->state_holes)  // collectHoles, sim.go:294-302 (kinds and liveness do not change in a step)
-        for (int64_t i = 0; i < n; ++i)
-            if ((alive ? alive[i] : 1) && kind[i] == GBH_BLACK_HOLE) ctx->hole_list.push_back(int32_t(i));
+        for (const uint8_t *q = kind, *end = kind + n;
+             (q = static_cast<const uint8_t *>(std::memchr(q, GBH_BLACK_HOLE, size_t(end - q)))) != nullptr; ++q)
+            if (!alive || alive[q - kind]) ctx->hole_list.push_back(int32_t(q - kind));
     if (ctx->nsys != 1) {
         ctx->nsys = 1;
         ++ctx->sys_gen;
@@ -788,8 +792,9 @@ int gbh_potential_energy(gbh_ctx *ctx, const gbh_params *p, int64_t n, const dou
     // Holes in state order (collect, build.go:65-69).
     std::vector<int32_t> holes;
     if (kind)
-        for (int64_t i = 0; i < n; ++i)
-            if ((alive ? alive[i] : 1) && kind[i] == GBH_BLACK_HOLE) holes.push_back(int32_t(i));
+        for (const uint8_t *q = kind, *end = kind + n;
+             (q = static_cast<const uint8_t *>(std::memchr(q, GBH_BLACK_HOLE, size_t(end - q)))) != nullptr; ++q)
+            if (!alive || alive[q - kind]) holes.push_back(int32_t(q - kind));
     CK(grow(ctx->holes, ctx->holes_cap, int64_t(holes.size()) + 1));
     if (!holes.empty() && (rc = h2d(ctx, ctx->holes, holes.data(), holes.size() * sizeof(int32_t)))) return rc;
     Launch L = launch_of(ctx);
@@ -961,6 +966,7 @@ int gbh_state_accelerations(gbh_ctx *ctx, const gbh_params *p) {
 int gbh_state_diagnostics(gbh_ctx *ctx, const gbh_params *p, double c, gbh_diagnostics *out) {
     int rc = begin(ctx);
     if (rc || (rc = check_params(ctx, p))) return rc;
+    if (!ctx->have_state) return fail(ctx, GBH_ERR_STATE, "no resident state (gbh_state_upload first)");
     if (!out) return fail(ctx, GBH_ERR_ARG, "out is NULL");
     if (!ctx->have_state) return fail(ctx, GBH_ERR_STATE, "no resident state (gbh_state_upload first)");
     *out = gbh_diagnostics{};
@@ -973,16 +979,7 @@ int gbh_state_diagnostics(gbh_ctx *ctx, const gbh_params *p, double c, gbh_diagn
     CK(grow(ctx->part, ctx->part_cap, std::max<int64_t>((ctx->cap + 255) / 256, int64_t(gbh::diag_parts()) * 11)));
     if (!ctx->scalar) CK(cudaMalloc(&ctx->scalar, 256));
     // potential: the tree at min(theta, 0.9) with the FP64 walk (potential.go:12-42)
-    std::vector<uint8_t> hkind, halive;
-    std::vector<int32_t> holes;
-    if (ctx->state_holes) {  // hole list in state order
-        hkind.resize(size_t(n));
-        halive.assign(size_t(n), 1);
-        CK(cudaMemcpy(hkind.data(), ctx->kind, size_t(n), cudaMemcpyDeviceToHost));
-        if (alive) CK(cudaMemcpy(halive.data(), ctx->alive, size_t(n), cudaMemcpyDeviceToHost));
-        for (int64_t i = 0; i < n; ++i)
-            if (halive[size_t(i)] && hkind[size_t(i)] == GBH_BLACK_HOLE) holes.push_back(int32_t(i));
-    }
+    const std::vector<int32_t> &holes = ctx->hole_list;  // alive holes of the state, from its upload
     CK(grow(ctx->holes, ctx->holes_cap, int64_t(holes.size()) + 1));
     if (!holes.empty()) CK(cudaMemcpy(ctx->holes, holes.data(), holes.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
     int leaf = leaf_of(p);

@@ -628,3 +628,29 @@ def test_evolve_driver_continues_a_snapshot(tmp_path):
     assert mb["Steps"] == mc["Steps"] == 40
     for k in ("px", "py", "pz", "vx", "vy", "vz", "ax", "ay", "az"):
         assert np.array_equal(sb[k], sc[k]), k
+
+
+def test_resident_calls_need_a_state():
+    """Calls on the resident state fail with GBH_ERR_STATE before an upload, and after a call that
+    reused the state buffers for host arrays (gbh_accelerations)."""
+    c = abi.Context(0)
+    try:
+        par = abi.make_params(0.5, 0.01, 8)
+        for call in (lambda: c.diagnostics(par), lambda: c.call("gbh_state_step", par, 1e-3, 1),
+                     lambda: c.call("gbh_state_accelerations", par)):
+            with pytest.raises(abi.GbhError) as ei:
+                call()
+            assert ei.value.code == abi.ERR_STATE
+        s = ics.plummer(1000, seed=3)
+        n = len(s["px"])
+        c.call("gbh_state_upload", n, *[P(s[k]) for k in ("px", "py", "pz", "vx", "vy", "vz")], None, None, None,
+               P(s["mass"]), None, None)
+        c.diagnostics(par)
+        a = [np.zeros(n) for _ in range(3)]
+        c.call("gbh_accelerations", par, n, P(s["px"]), P(s["py"]), P(s["pz"]), P(s["mass"]), None, None,
+               P(a[0]), P(a[1]), P(a[2]))
+        with pytest.raises(abi.GbhError) as ei:
+            c.diagnostics(par)
+        assert ei.value.code == abi.ERR_STATE
+    finally:
+        c.close()
