@@ -134,20 +134,25 @@ def make_workload(n, seed=0):
     return ics.merger(n, seed=seed)
 
 
-def cpu_reference_steps(s, steps, leaf, workers=0, count=False):
+def cpu_reference_steps(s, steps, leaf, workers=0, count=False, initial=None):
     """Times full KDK steps of the CPU oracle (the reference's algorithm, FP64) on a copy of s;
-    optionally also returns the reference walk's interaction counts at the initial state."""
+    optionally also returns the reference walk's interaction counts at the initial state. The
+    initial forces are computed untimed, or taken from `initial` (a state whose accelerations
+    are s's forces: the oracle's forces do not depend on its thread count)."""
     from oracle import oracle as O
     counts = None
     if count:
         t = O.Tree(s["px"], s["py"], s["pz"], s["mass"], theta=THETA, leaf=leaf, workers=workers)
         counts = t.counts(EPS, workers=workers)
         del t
-    st = {k: np.array(s[k], copy=True) for k in (*FIELDS, "mass")}
-    O.kdk(st, dt=DT, eps=EPS, theta=THETA, leaf=leaf, nsteps=0, workers=workers)  # initial forces
+    src = s if initial is None else initial
+    st = {k: np.array(src[k], copy=True) for k in (*FIELDS, "mass")}
+    if initial is None:
+        O.kdk(st, dt=DT, eps=EPS, theta=THETA, leaf=leaf, nsteps=0, workers=workers)  # initial forces
+    first = {k: v.copy() for k, v in st.items()}
     t0 = time.perf_counter()
     O.kdk(st, dt=DT, eps=EPS, theta=THETA, leaf=leaf, nsteps=steps, acc_valid=True, workers=workers)
-    return time.perf_counter() - t0, counts
+    return time.perf_counter() - t0, counts, first
 
 
 def run_reference(args):
@@ -159,9 +164,9 @@ def run_reference(args):
     cores = os.cpu_count() or 1
     # one warm-up step, then at most as many timed steps as fit in about a minute
     leaf = args.leaf or REFERENCE_LEAF
-    warm, _ = cpu_reference_steps(s, max(1, min(args.warmup, 1)), leaf, workers=0)
+    warm, _, _ = cpu_reference_steps(s, max(1, min(args.warmup, 1)), leaf, workers=0)
     k = max(1, min(args.steps, int(60.0 / max(warm, 1e-3))))
-    el, _ = cpu_reference_steps(s, k, leaf, workers=0)
+    el, _, _ = cpu_reference_steps(s, k, leaf, workers=0)
     value = n * k / el
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": args.gpus,
@@ -314,8 +319,10 @@ def run(args):
         # CPU baseline leg: the oracle (reference algorithm) on the host cores, bounded sample,
         # plus the reference walk's interaction counts behind the algorithmic FLOP figure
         cpu_steps = 1
-        el, counts = cpu_reference_steps(s, cpu_steps, leaf, workers=0, count=True)
+        el, counts, first = cpu_reference_steps(s, cpu_steps, leaf, workers=0, count=True)
         cores = os.cpu_count() or 1
+        # the same step on one thread (initial forces reused from the run above)
+        el1, _, _ = cpu_reference_steps(s, 1, leaf, workers=1, initial=first)
         n_pn, n_pp, n_open = counts
         flop = 50 * n_pn + 18 * n_pp + 8 * n_open
         walk_s = w_mixed / args.steps * 1e-3
@@ -340,7 +347,9 @@ def run(args):
                          "walk_ms": w_mixed / args.steps, "build_ms": b_mixed / args.steps},
             "cpu_baseline": {"value": n * cpu_steps / el, "unit": "particle-steps/s", "cores": cores, "kind": "port",
                              "sample": f"{cpu_steps} full KDK step of the {n}-particle workload, C++ restatement "
-                                       f"of the reference CPU Barnes-Hut (FP64), {cores} threads"},
+                                       f"of the reference CPU Barnes-Hut (FP64), {cores} threads",
+                             "single_core": {"value": n / el1, "unit": "particle-steps/s", "cores": 1,
+                                             "sample": "the same full KDK step on one thread"}},
             "e2e": {"value": e2e_value, "unit": "particle-steps/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "api": "gbh_step_kdk on pinned host buffers, 1 step per call"},
             "gpu_launches": launches,
