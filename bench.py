@@ -47,7 +47,7 @@ N_DEFAULT = 1 << 20
 THETA, EPS, DT = 0.5, 0.02, 1e-3
 # DRAM bytes (read + write) of one k_walk_mixed2 launch on this workload by leaf size, from the
 # ncu capture summarised in profiles/walk_mixed2_merger_1M_theta0.5_leaf32.md.
-WALK_TRAFFIC_BYTES = {32: 72_727_552}
+WALK_TRAFFIC_BYTES = {32: 85_735_936}
 TUNE_LEAVES = [8, 12, 16, 24, 32]
 RMS_BOUND = 2e-3
 REFERENCE_LEAF = 24  # bh.go:67-68, the reference solver's default leaf size
@@ -87,15 +87,20 @@ class Clocks:
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
     def __init__(self, device: int):
-        self.device, self.rows, self.proc = device, [], None
+        self.device, self.rows, self.proc, self.first = device, [], None, 0
 
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.Q}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
+            # the timed region starts once the sampler is live (its first line), at most 3 s later
+            t0 = time.perf_counter()
+            while not self.rows and self.proc.poll() is None and time.perf_counter() - t0 < 3.0:
+                time.sleep(0.01)
+            self.first = len(self.rows)  # samples taken before the timed region are not counted
         except OSError:
             self.proc = None
         return self
@@ -115,7 +120,7 @@ class Clocks:
     def summary(self):
         sm, mx, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for r in self.rows:
+        for r in self.rows[self.first:] if len(self.rows) > self.first else self.rows:
             try:
                 sm.append(float(r[1]))
                 mx = float(r[2])
@@ -264,7 +269,9 @@ def run(args):
     l0, l1 = np.array(diag[0]["angular_momentum"]), np.array(diag[1]["angular_momentum"])
     drift = {"steps": args.warmup + args.steps, "dt": DT, "energy_rel": abs((e1 - e0) / e0),
              "angular_momentum_rel": float(np.linalg.norm(l1 - l0) / np.linalg.norm(l0)),
-             "energy_method": "FP64 tree potential at theta 0.5 + FP64 kinetic (gbh_state_diagnostics)"}
+             "energy_method": "tree potential at theta 0.5 from the mixed walk in potential mode (FP32 "
+                              "interactions, compensated per-star sums, FP64 total) + FP64 kinetic "
+                              "(gbh_state_diagnostics with the step's parameters)"}
     t_plain, w_plain, b_plain, _, _ = timed_steps("plain", args.steps, args.warmup)
 
     def maxr(x):
