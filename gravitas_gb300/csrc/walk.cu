@@ -148,10 +148,13 @@ __global__ __launch_bounds__(kMixedThreads, 8) void k_walk_mixed2(const DevInfo 
     const int32_t ns = int32_t(info->nstars);  // the C-ABI caps n at 2^30
     const uint32_t nn = uint32_t(info->nnodes);
     const int32_t g = int32_t((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
-    int32_t base, nt, root = 0;
+    // longest first: walk the group the last walk's costs put at this position (gperm holds a
+    // permutation of the groups, valid while its recorded group count matches)
+    int32_t base, nt, root = 0, gw = g;
     if (groups) {  // a forest: group g = up to 64 (32) stars of one system, walked from its root
         if (uint32_t(g) >= info->ngroups) return;
-        const int4 e = groups[g];
+        if (gperm && gperm[perm_cap] == int32_t(info->ngroups)) gw = gperm[g];
+        const int4 e = groups[gw];
         base = e.x;
         nt = e.x + e.y;
         root = e.z;
@@ -159,8 +162,6 @@ __global__ __launch_bounds__(kMixedThreads, 8) void k_walk_mixed2(const DevInfo 
         const int gsize = pair ? 64 : 32;
         nt = targets ? int32_t(info->ntargets) : ns;
         if (g * gsize >= nt) return;  // uniform over the warp
-        // longest first: walk the group the last walk's costs put at this position
-        int32_t gw = g;
         if (gperm && gperm[perm_cap] == (nt + gsize - 1) / gsize) gw = gperm[g];
         base = gw * gsize;
     }
@@ -313,7 +314,7 @@ __global__ __launch_bounds__(kMixedThreads, 8) void k_walk_mixed2(const DevInfo 
     kahan_fold2(sx, cx, px);
     kahan_fold2(sy, cy, py);
     kahan_fold2(sz, cz, pz);
-    if (gcost && lane == 0) gcost[base / (pair ? 64 : 32)] = 2u * visits + pairs;  // the group's cost
+    if (gcost && lane == 0) gcost[gw] = 2u * visits + pairs;  // the group's cost
     if constexpr (kPot) {
         if (v0) ax[k0] = double(sx.x) - double(cx.x);
         if (v1) ax[k1] = double(sx.y) - double(cx.y);
@@ -371,12 +372,12 @@ cudaError_t walk_plain(const Launch &L, const TreeBufs &b, int64_t nstars_cap, f
 // neighbouring warps keep walking neighbouring groups). One block of kLptThreads threads, each
 // owning a contiguous run of groups.
 constexpr int kLptThreads = 512, kLptBuckets = 16;  // 32 KB of shared counts
-__global__ __launch_bounds__(kLptThreads) void k_lpt_order(const DevInfo *info, int gsize, const uint32_t *gcost,
-                                                           int32_t *gperm, int32_t perm_cap) {
+__global__ __launch_bounds__(kLptThreads) void k_lpt_order(const DevInfo *info, int gsize, bool forest,
+                                                           const uint32_t *gcost, int32_t *gperm, int32_t perm_cap) {
     __shared__ uint32_t cnt[kLptBuckets][kLptThreads];
     __shared__ uint32_t base[kLptBuckets];
     const int t = threadIdx.x;
-    const int32_t ng = int32_t((info->nstars + gsize - 1) / gsize);
+    const int32_t ng = forest ? int32_t(info->ngroups) : int32_t((info->nstars + gsize - 1) / gsize);
     if (ng > perm_cap) return;  // no order: the walk keeps launch order
     const int32_t per = (ng + kLptThreads - 1) / kLptThreads;
     const int32_t g0 = t * per, g1 = g0 + per < ng ? g0 + per : ng;
@@ -420,7 +421,7 @@ static cudaError_t launch_mixed_t(const Launch &L, const TreeBufs &b, int64_t ns
     const bool forest = b.nsys > 1;
     const int gsize = b.group == 32 ? 32 : 64;
     int64_t groups = forest ? b.cap_groups : (nstars_cap + gsize - 1) / gsize;
-    const bool lpt = b.lpt && !forest && !targets && !kPot;
+    const bool lpt = b.lpt && !targets && !kPot;
     int64_t blocks = (groups + kMixedThreads / 32 - 1) / (kMixedThreads / 32);
     k_walk_mixed2<kQuad, kSoft, kPot, kShared><<<unsigned(blocks < 1 ? 1 : blocks), kMixedThreads, 0, L.stream>>>(
         b.info, b.mnodes, b.mrange, b.st_hi, b.st_lo, b.st_off, b.order, eps2, ax, ay, az,
@@ -430,7 +431,7 @@ static cudaError_t launch_mixed_t(const Launch &L, const TreeBufs &b, int64_t ns
     ++*L.count;
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess || !lpt) return e;
-    k_lpt_order<<<1, kLptThreads, 0, L.stream>>>(b.info, gsize, b.gcost, b.gperm, int32_t(b.cap_groups));
+    k_lpt_order<<<1, kLptThreads, 0, L.stream>>>(b.info, gsize, forest, b.gcost, b.gperm, int32_t(b.cap_groups));
     ++*L.count;
     return cudaGetLastError();
 }

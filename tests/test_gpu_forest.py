@@ -155,3 +155,32 @@ def test_autotune_on_a_forest_meets_the_bound(ctx):
                         eps=0.01, targets=t)
         e = np.linalg.norm(a[lo:hi][t] - want, axis=1) / np.linalg.norm(want, axis=1)
         assert np.sqrt(np.mean(e ** 2)) < 4e-3, q
+
+
+def test_longest_first_order_changes_no_bit(ctx):
+    """The mixed walk launches its groups in the order the previous walk's group costs give
+    (longest first) unless GBH_CFG_NO_LPT; every group sums only its own interactions, so the
+    order changes no result, for a forest and for a single system."""
+    s, off = ics.forest(nsys=6, seed=5, nmin=500, nmax=8000)
+    n = int(off[-1])
+    par = abi.make_params(0.5, 0.02, 16, False, False, "mixed")
+    other = abi.Context(0, abi.CFG_NO_LPT)
+    try:
+        got = []
+        for c in (ctx, other):
+            upload_forest(c, s, off)
+            c.call("gbh_state_step", par, 1e-3, 4)
+            got.append(download(c, n))
+        for k in F9:
+            assert np.array_equal(got[0][k], got[1][k]), k
+        m = ics.merger(60000, seed=2)
+        got = []
+        for c in (ctx, other):
+            c.call("gbh_state_upload", 60000, *[P(m[k]) for k in ("px", "py", "pz", "vx", "vy", "vz")], None, None,
+                   None, P(m["mass"]), None, None)
+            c.call("gbh_state_step", par, 1e-3, 4)
+            got.append(download(c, 60000))
+        for k in F9:
+            assert np.array_equal(got[0][k], got[1][k]), k
+    finally:
+        other.close()
