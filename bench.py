@@ -416,11 +416,12 @@ def run_profile(args):
         ctx = abi.Context(0)
         ctx.forest_upload(off, s["px"], s["py"], s["pz"], s["vx"], s["vy"], s["vz"], s["mass"], s["kind"],
                           s["alive"])
-        par = abi.make_params(0.7, EPS, 16, False, False, "mixed", group_size=64)
+        # the autotuner's pick for this forest (theta 0.7, leaf 32, 64-star groups); --leaf overrides
+        par = abi.make_params(0.7, EPS, args.leaf or 32, False, False, "mixed", group_size=64)
         for _ in range(2):
             ctx.call("gbh_state_accelerations", par)
         t = ctx.timings()
-        print(json.dumps({"profile": "forest", "n": int(off[-1]), "build_ms": t["build_ms"], "walk_ms": t["walk_ms"],
+        print(json.dumps({"profile": "forest", "leaf": par.leaf_size, "n": int(off[-1]), "build_ms": t["build_ms"], "walk_ms": t["walk_ms"],
                           "nnodes": t["nnodes"], "launches": t["launches"]}))
         ctx.close()
         return 0

@@ -546,16 +546,21 @@ __global__ __launch_bounds__(kThreads) void k_chain_count(const uint64_t *__rest
     int L0 = start_level(keys, i, R.lo);
     uint32_t c = 0;
     if (L0 <= kMaxLevel) {
+        // A level-L cell starting at i holds more than leaf stars exactly when the star leaf
+        // positions on is still inside it (cells are contiguous runs of the sorted keys).
+        const uint64_t ki = keys[i];
+        const bool ahead = i + leaf < R.hi;
+        const uint64_t ka = ahead ? keys[i + leaf] : 0;
         bool exists = true;
         if (i > R.lo) {  // the parent cell (level L0-1) contains i-1 and i; it splits iff it holds > leaf stars
             int Lp = L0 - 1;
-            exists = cell_end(keys, R.hi, i, Lp) - cell_start(keys, R.lo, i, Lp) > leaf;
+            exists = (ahead && prefix(ka, Lp) == prefix(ki, Lp)) ||
+                     cell_end(keys, R.hi, i, Lp) - cell_start(keys, R.lo, i, Lp) > leaf;
         }
         if (exists) {
             for (int L = L0;; ++L) {
-                int64_t e = cell_end(keys, R.hi, i, L);
                 ++c;
-                if (!(e - i > leaf && L < kMaxLevel)) break;
+                if (!(ahead && prefix(ka, L) == prefix(ki, L) && L < kMaxLevel)) break;
             }
         }
     }
