@@ -130,8 +130,11 @@ __device__ __forceinline__ void kahan_fold2(float2 &s, float2 &c, float2 &part) 
 // kPot: the same walk accumulating psi = sum m / r + (d.Q.d) / (2 r^5) (walkPotential,
 // potential.go:44-81) per star instead of the acceleration; psi goes to ax[sorted index].
 // kShared: no target list, so a lane's two stars share one origin (see the separations below).
+// Without a target list 9 blocks of 128 per SM (56 registers, a few spills) measured 1.8 % faster
+// than 8 (64 registers, no room for a ninth block); 10 (48 registers) was slower. The target-list
+// form needs more registers and keeps 8.
 template <bool kQuad, bool kSoft, bool kPot, bool kShared>
-__global__ __launch_bounds__(kMixedThreads, 8) void k_walk_mixed2(const DevInfo *info, const MNode *__restrict__ nodes,
+__global__ __launch_bounds__(kMixedThreads, kShared ? 9 : 8) void k_walk_mixed2(const DevInfo *info, const MNode *__restrict__ nodes,
                                                                const int2 *__restrict__ ranges,
                                                                const float4 *__restrict__ st_hi,
                                                                const float4 *__restrict__ st_lo,
