@@ -47,7 +47,7 @@ N_DEFAULT = 1 << 20
 THETA, EPS, DT = 0.5, 0.02, 1e-3
 # DRAM bytes (read + write) of one k_walk_mixed2 launch on this workload by leaf size, from the
 # ncu capture summarised in profiles/walk_mixed2_merger_1M_theta0.5_leaf32.md.
-WALK_TRAFFIC_BYTES = {32: 85_735_936}
+WALK_TRAFFIC_BYTES = {32: 86_668_288}
 TUNE_LEAVES = [8, 12, 16, 24, 32]
 RMS_BOUND = 2e-3
 REFERENCE_LEAF = 24  # bh.go:67-68, the reference solver's default leaf size
@@ -139,16 +139,17 @@ def make_workload(n, seed=0):
     return ics.merger(n, seed=seed)
 
 
-def cpu_reference_steps(s, steps, leaf, workers=0, count=False, initial=None):
+def cpu_reference_steps(s, steps, leaf, workers=0, count=False, initial=None, group=64):
     """Times full KDK steps of the CPU oracle (the reference's algorithm, FP64) on a copy of s;
-    optionally also returns the reference walk's interaction counts at the initial state. The
+    optionally also returns, at the initial state, the reference walk's interaction counts and
+    the counts of the group walk the mixed walk executes (groups of `group` sorted stars). The
     initial forces are computed untimed, or taken from `initial` (a state whose accelerations
     are s's forces: the oracle's forces do not depend on its thread count)."""
     from oracle import oracle as O
     counts = None
     if count:
         t = O.Tree(s["px"], s["py"], s["pz"], s["mass"], theta=THETA, leaf=leaf, workers=workers)
-        counts = t.counts(EPS, workers=workers)
+        counts = (t.counts(EPS, workers=workers), t.group_counts(group, workers=workers))
         del t
     src = s if initial is None else initial
     st = {k: np.array(src[k], copy=True) for k in (*FIELDS, "mass")}
@@ -326,12 +327,14 @@ def run(args):
         # CPU baseline leg: the oracle (reference algorithm) on the host cores, bounded sample,
         # plus the reference walk's interaction counts behind the algorithmic FLOP figure
         cpu_steps = 1
-        el, counts, first = cpu_reference_steps(s, cpu_steps, leaf, workers=0, count=True)
+        group = tuned["mixed"][0].group_size or 64
+        el, (counts, gcounts), first = cpu_reference_steps(s, cpu_steps, leaf, workers=0, count=True, group=group)
         cores = os.cpu_count() or 1
         # the same step on one thread (initial forces reused from the run above)
         el1, _, _ = cpu_reference_steps(s, 1, leaf, workers=1, initial=first)
         n_pn, n_pp, n_open = counts
         flop = 50 * n_pn + 18 * n_pp + 8 * n_open
+        flop_exec = 50 * gcounts[0] + 18 * gcounts[1] + 8 * gcounts[2]
         walk_s = w_mixed / args.steps * 1e-3
         achieved = flop / walk_s / 1e12
         line = {
@@ -351,7 +354,14 @@ def run(args):
                          "kernel": "k_walk_mixed2", "flop_per_launch": flop,
                          "peak_source": "FP32 FMA microbenchmark in this run (gbh_probe_fp32_peak); "
                                         "MEASURED_PEAKS.json has no FP32 figure",
-                         "walk_ms": w_mixed / args.steps, "build_ms": b_mixed / args.steps},
+                         "walk_ms": w_mixed / args.steps, "build_ms": b_mixed / args.steps,
+                         "executed": {"flop_per_launch": flop_exec, "over_credited": flop_exec / flop,
+                                      "achieved": flop_exec / walk_s / 1e12,
+                                      "frac": flop_exec / walk_s / 1e12 / peak,
+                                      "source": f"oracle group-walk counts (orc_tree_group_counts) for "
+                                                f"{group}-star groups at the same theta and leaf: every star "
+                                                f"of a group takes part in each of its group's visits, as in "
+                                                f"k_walk_mixed2; same FLOP weights"}},
             "cpu_baseline": {"value": n * cpu_steps / el, "unit": "particle-steps/s", "cores": cores, "kind": "port",
                              "sample": f"{cpu_steps} full KDK step of the {n}-particle workload, C++ restatement "
                                        f"of the reference CPU Barnes-Hut (FP64), {cores} threads",

@@ -685,6 +685,54 @@ void orc_tree_counts(const orc_tree *t, double eps, int monopole_only, int worke
     *n_open = c;
 }
 
+// Counts of the group walk the GPU's mixed walk executes: each group of `group` consecutive
+// sorted stars walks the tree together and opens a node when any of its stars would (d2 < crit2,
+// bh.go:165); every star of the group then takes part in each visit. Same definitions as
+// orc_tree_counts (accepted nodes, leaf pairs without the self pair, opened nodes including leaf
+// visits), summed over the stars, so group = 1 gives the per-star counts.
+void orc_tree_group_counts(const orc_tree *t, int group, int workers, int64_t *n_node, int64_t *n_pp,
+                           int64_t *n_open) {
+    const int64_t ns = int64_t(t->order.size());
+    const int64_t g = group < 1 ? 1 : group;
+    const int64_t ng = (ns + g - 1) / g;
+    std::atomic<int64_t> a{0}, b{0}, c{0};
+    if (!t->nodes.empty()) {
+        parallel_for(ng, 16, workers, [&](int64_t lo, int64_t hi) {
+            int64_t cnt[3] = {0, 0, 0};
+            for (int64_t q = lo; q < hi; ++q) {
+                const int64_t s0 = q * g, s1 = s0 + g < ns ? s0 + g : ns, gs = s1 - s0;
+                for (int32_t i = 0; i >= 0;) {
+                    const orc_node &nd = t->nodes[size_t(i)];
+                    bool open = false;
+                    for (int64_t k = s0; k < s1 && !open; ++k) {
+                        double dx = nd.x - t->sx[size_t(k)], dy = nd.y - t->sy[size_t(k)], dz = nd.z - t->sz[size_t(k)];
+                        open = dx * dx + dy * dy + dz * dz < nd.crit2;
+                    }
+                    if (!open) {
+                        cnt[0] += gs;
+                        i = nd.next;
+                        continue;
+                    }
+                    cnt[2] += gs;
+                    if (nd.first >= 0) {
+                        i = nd.first;
+                        continue;
+                    }
+                    const int64_t l0 = s0 > nd.lo ? s0 : int64_t(nd.lo), l1 = s1 < nd.hi ? s1 : int64_t(nd.hi);
+                    cnt[1] += gs * int64_t(nd.hi - nd.lo) - (l1 > l0 ? l1 - l0 : 0);  // no self pairs
+                    i = nd.next;
+                }
+            }
+            a += cnt[0];
+            b += cnt[1];
+            c += cnt[2];
+        });
+    }
+    *n_node = a;
+    *n_pp = b;
+    *n_open = c;
+}
+
 // gpu_darwin.go:84-117 with the float32 packing of :187-202, on the CPU.
 void orc_tree_walk_fp32(const orc_tree *t, double eps, int workers, float *acc3) {
     struct GNode {

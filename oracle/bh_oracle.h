@@ -86,6 +86,14 @@ void orc_tree_counts(const orc_tree *t, double eps, int monopole_only, int worke
                      const int32_t *targets, int64_t ntargets, int64_t *n_node,
                      int64_t *n_pp, int64_t *n_open);
 /*
+ * Counts of the group walk that the GPU mixed walk executes: groups of `group` consecutive
+ * sorted stars open a node when any of their stars would; every star takes part in each of its
+ * group's visits. Summed over stars with the definitions of orc_tree_counts (group = 1 gives
+ * the per-star counts).
+ */
+void orc_tree_group_counts(const orc_tree *t, int group, int workers, int64_t *n_node,
+                           int64_t *n_pp, int64_t *n_open);
+/*
  * The float32 Metal walk (internal/sim/bh/gpu_darwin.go:84-117, nodes packed as
  * :187-202) restated on the CPU. Output in sorted order, 3 floats per star.
  */

@@ -60,6 +60,7 @@ def lib():
             "orc_tree_walk_point": (None, [_P, _D, _D, _D, ctypes.c_int32, _D, _INT, _P]),
             "orc_tree_walk_potential_point": (_D, [_P, _D, _D, _D, ctypes.c_int32, _D, _INT]),
             "orc_tree_counts": (None, [_P, _D, _INT, _INT, _P, _I64, _P, _P, _P]),
+            "orc_tree_group_counts": (None, [_P, _INT, _INT, _P, _P, _P]),
             "orc_tree_walk_fp32": (None, [_P, _D, _INT, _P]),
             "orc_tree_potential": (_D, [_P, _I64, _P, _P, _P, _P, _P, _P, _D, _D, _INT, _INT, _INT]),
             "orc_direct": (None, [_I64, _P, _P, _P, _P, _P, _D, _INT, _INT, _P, _P, _P]),
@@ -174,6 +175,14 @@ class Tree:
         lib().orc_tree_counts(self._t, eps, int(monopole_only),
                               self.workers if workers is None else workers,
                               _ptr(t), 0 if t is None else len(t), _ptr(a), _ptr(b), _ptr(c))
+        return int(a[0]), int(b[0]), int(c[0])
+
+    def group_counts(self, group=64, workers=None):
+        """(accepted nodes, leaf pairs, opened nodes) summed over the stars of the group walk the
+        GPU's mixed walk executes (groups of `group` consecutive sorted stars, any-open)."""
+        a, b, c = (np.zeros(1, np.int64) for _ in range(3))
+        lib().orc_tree_group_counts(self._t, int(group), self.workers if workers is None else workers,
+                                    _ptr(a), _ptr(b), _ptr(c))
         return int(a[0]), int(b[0]), int(c[0])
 
     def walk_fp32(self, eps, workers=None):

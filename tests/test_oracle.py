@@ -394,3 +394,23 @@ def test_relativistic_drift_slows_fast_bodies():
     O.kdk(s, dt=1e-2, eps=0.1, theta=0.5, leaf=8, nsteps=1, c=10.0, workers=1)
     assert abs(s["px"][0] - 1e-2 * 10 * np.sqrt(3) / 2) <= 1e-12
     assert abs(s["px"][1] - (1e6 + 1e-5)) <= 1e-9
+
+
+def test_group_walk_counts():
+    """The group-walk counts behind the executed-work figure: a group of one star is the
+    per-star walk, and an aligned group of 64 is the union of two of 32 (of 32 single stars), so
+    it opens every node they open: openings, leaf pairs and the FLOP count can only grow."""
+    s = ics.galaxy(20000, seed=9)
+    t = O.Tree(s["px"], s["py"], s["pz"], s["mass"], s["kind"], theta=0.5, leaf=16)
+    per_star = t.counts(0.01)
+    assert t.group_counts(1) == per_star
+    assert t.group_counts(1, workers=1) == t.group_counts(1, workers=4)
+    prev = per_star
+    for g in (32, 64):
+        got = t.group_counts(g)
+        assert got[1] >= prev[1] and got[2] >= prev[2]  # more leaf pairs and openings
+        flops = [50 * c[0] + 18 * c[1] + 8 * c[2] for c in (prev, got)]
+        assert flops[1] >= flops[0]
+        prev = got
+    empty = O.Tree(np.zeros(0), np.zeros(0), np.zeros(0), np.zeros(0), theta=0.5, leaf=16)
+    assert empty.group_counts(64) == (0, 0, 0)
