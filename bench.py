@@ -47,7 +47,7 @@ N_DEFAULT = 1 << 20
 THETA, EPS, DT = 0.5, 0.02, 1e-3
 # DRAM bytes (read + write) of one k_walk_mixed2 launch on this workload by leaf size, from the
 # ncu capture summarised in profiles/walk_mixed2_merger_1M_theta0.5_leaf32.md.
-WALK_TRAFFIC_BYTES = {32: 86_668_288}
+WALK_TRAFFIC_BYTES = {24: 90_435_328, 32: 86_668_288}
 TUNE_LEAVES = [8, 12, 16, 24, 32]
 RMS_BOUND = 2e-3
 REFERENCE_LEAF = 24  # bh.go:67-68, the reference solver's default leaf size
