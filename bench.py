@@ -24,7 +24,9 @@ error <= 2e-3; --leaf fixes it instead.
 all host threads) on the same workload at the reference solver's default leaf size, 24.
 
 --workload adjoint and --workload forest print the lines of the differentiable and the batched
-workloads instead (see run_adjoint and run_forest).
+workloads instead (see run_adjoint and run_forest); --workload sweep runs the merger at theta
+0.3, 0.5 and 0.8 for 200 steps each (run_sweep), --workload scaling the Plummer sphere from 1M
+to 64M bodies (run_scaling).
 """
 from __future__ import annotations
 
@@ -377,7 +379,12 @@ def run(args):
             "force_error": errs["mixed"],
             "drift": drift,
             "interactions": {"accepted_nodes": n_pn, "leaf_pairs": n_pp, "opened_nodes": n_open,
-                             "per_star": (n_pn + n_pp) / n, "nodes": nnodes},
+                             "per_star": (n_pn + n_pp) / n, "nodes": nnodes,
+                             "per_s": (n_pn + n_pp) / walk_s,
+                             "per_s_of_step": (n_pn + n_pp) * args.steps / (t_mixed * 1e-3),
+                             "source": "the reference per-star walk's node and leaf-pair interactions "
+                                       "(oracle counts at the initial state) per second of walk time and "
+                                       "of full-step time"},
         }
         print(json.dumps(line), flush=True)
     ctx.close()
@@ -693,10 +700,69 @@ def run_scaling(args):
     return 0
 
 
+def run_sweep(args):
+    """The large-merger configuration's theta sweep: the 1M merger at theta 0.3, 0.5 and 0.8
+    (mixed walk, leaf 32, 64-star groups, eps 0.02), 200 global KDK steps of dt = 1e-3 each
+    (the default --steps of this workload), graph-replayed in one call. Per theta: particle-steps/s from CUDA events,
+    walk and build time, RMS / p99 force error of the initial forces against the FP64 direct sum
+    on 4,096 seeded stars, and the drift of energy and angular momentum over the run, all
+    measured with one estimator (the mixed-walk tree potential at theta 0.5). One line of JSON."""
+    import torch
+
+    from gravitas_gb300 import abi
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if rank != 0:
+        return 0
+    P = abi.ptr
+    n = args.n
+    s = make_workload(n)
+    steps = args.steps
+    ctx = abi.Context(local)
+    rng = np.random.default_rng(1234)
+    targets = np.sort(rng.choice(n, 4096, replace=False)).astype(np.int64)
+    want = np.zeros((3, 4096))
+    ctx.call("gbh_direct_accelerations", abi.make_params(0, EPS, 0, False, False, "fp64"), n, P(s["px"]),
+             P(s["py"]), P(s["pz"]), P(s["mass"]), None, P(targets), 4096, P(want[0]), P(want[1]), P(want[2]))
+    want = want.T
+    est = abi.make_params(0.5, EPS, 32, False, False, "mixed", group_size=64)  # the drift estimator
+    rows = []
+    with Clocks(local) as clk:
+        for theta in (0.3, 0.5, 0.8):
+            par = abi.make_params(theta, EPS, args.leaf or 32, False, False, "mixed", group_size=64)
+            ctx.call("gbh_state_upload", n, *[P(s[k]) for k in ("px", "py", "pz", "vx", "vy", "vz")], None, None,
+                     None, P(s["mass"]), None, None)
+            ctx.call("gbh_state_accelerations", par)
+            a = [np.zeros(n) for _ in range(3)]
+            ctx.call("gbh_state_download", None, None, None, None, None, None, P(a[0]), P(a[1]), P(a[2]))
+            err = rel_err_stats(np.stack(a, axis=1)[targets], want)
+            d0 = ctx.diagnostics(est)
+            ctx.call("gbh_state_step", par, DT, steps)
+            t = ctx.timings()
+            d1 = ctx.diagnostics(est)
+            l0, l1 = np.array(d0["angular_momentum"]), np.array(d1["angular_momentum"])
+            rows.append({"theta": theta, "ms_per_step": t["total_ms"] / steps, "walk_ms": t["walk_ms"] / steps,
+                         "build_ms": t["build_ms"] / steps,
+                         "particle_steps_per_s": n * steps / (t["total_ms"] * 1e-3), "force_error": err,
+                         "energy_drift": abs((d1["total"] - d0["total"]) / d0["total"]),
+                         "angular_momentum_drift": float(np.linalg.norm(l1 - l0) / np.linalg.norm(l0)),
+                         "nodes": t["nnodes"], "launches_per_step": t["launches"] / steps})
+            print(json.dumps({"sweep_row": rows[-1]}), flush=True)
+    ctx.close()
+    print(json.dumps({"metric": "merger theta sweep: particle-steps/s, force error and drift per theta",
+                      "unit": "particle-steps/s", "n_gpus": 1, "steps": steps, "data": "synthetic",
+                      "config": {"workload": workload_name(n, args.leaf or 32), "dt": DT, "group_size": 64,
+                                 "estimator": "energy and angular momentum from gbh_state_diagnostics with the "
+                                              "mixed walk at theta 0.5 for every row",
+                                 "l2": "not flushed: the steps run back to back in one graph-replayed call"},
+                      "rows": rows, "clocks": clk.summary()}), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=None, help="timed steps (default 10; 200 for --workload sweep)")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--n", type=int, default=N_DEFAULT)
@@ -704,19 +770,23 @@ def main():
                     help="leaf size; 0 (default) lets the autotuner choose for each walk")
     ap.add_argument("--profile", choices=["mixed", "plain", "fp64", "adjoint", "forest", "build"], default=None,
                     help="run only two force evaluations with this walk (for ncu captures)")
-    ap.add_argument("--workload", choices=["merger", "adjoint", "forest", "scaling"], default="merger",
+    ap.add_argument("--workload", choices=["merger", "adjoint", "forest", "scaling", "sweep"], default="merger",
                     help="adjoint: the differentiable workload (gbh_fwd_save / gbh_bwd); forest: 64 systems in "
                          "one state with the autotuner; each prints its own JSON line")
     ap.add_argument("--fd-coords", type=int, default=16, help="adjoint: coordinates checked by central differences")
     ap.add_argument("--sizes", type=int, nargs="+", default=[1 << 20, 1 << 22, 1 << 24, 1 << 26],
                     help="scaling: body counts")
     args = ap.parse_args()
+    if args.steps is None:
+        args.steps = 200 if args.workload == "sweep" else 10
     if args.workload == "adjoint":
         return run_adjoint(args)
     if args.workload == "forest":
         return run_forest(args)
     if args.workload == "scaling":
         return run_scaling(args)
+    if args.workload == "sweep":
+        return run_sweep(args)
     if args.profile:
         return run_profile(args)
     if args.warmup < 3 and args.impl == "ours":
