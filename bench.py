@@ -25,8 +25,9 @@ all host threads) on the same workload at the reference solver's default leaf si
 
 --workload adjoint and --workload forest print the lines of the differentiable and the batched
 workloads instead (see run_adjoint and run_forest); --workload sweep runs the merger at theta
-0.3, 0.5 and 0.8 for 200 steps each (run_sweep), --workload scaling the Plummer sphere from 1M
-to 64M bodies (run_scaling).
+0.3, 0.5 and 0.8 for 200 steps each (run_sweep), --workload galaxy the 131,072-body galaxy in
+500 six-level block steps (run_galaxy), --workload scaling the Plummer sphere from 1M to 64M
+bodies (run_scaling).
 """
 from __future__ import annotations
 
@@ -759,6 +760,90 @@ def run_sweep(args):
     return 0
 
 
+def run_galaxy(args):
+    """The galaxy configuration: the 131,072-body disk + bulge + NFW-halo galaxy (halo particles at
+    4x the disk particle mass), eps 0.02, theta 0.5, power-of-two block steps with 6 levels driven
+    by eta sqrt(eps / |a|), eta 0.025, 500 block steps of T = 1.6e-2 (--steps overrides), mixed
+    walk at the leaf the autotuner picks. Reported: block steps per second, particle-steps/s (each
+    block step advances every particle by T), the events and walked stars, and the energy and
+    angular-momentum drift; beside it the first 50 block steps' simulated time in global steps at
+    the finest rung (T / 32), timed and with its drift, for the scheme's saving. One line of JSON."""
+    import torch
+
+    from gravitas_gb300 import abi, ics
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if rank != 0:
+        return 0
+    P = abi.ptr
+    g = ics.galaxy(131072, seed=0)
+    n = len(g["px"])
+    T, levels, eta, eps = 1.6e-2, 6, 0.025, 0.02
+    steps = args.steps
+    ctx = abi.Context(local)
+
+    def upload():
+        ctx.call("gbh_state_upload", n, *[P(g[k]) for k in ("px", "py", "pz", "vx", "vy", "vz")], None, None, None,
+                 P(g["mass"]), P(g["kind"]), P(g["alive"]))
+
+    upload()
+    base = abi.make_params(THETA, eps, args.leaf or 16, False, False, "mixed")
+    if args.leaf:
+        par = base
+    else:
+        par, _ = ctx.autotune(base, thetas=[THETA], leaves=TUNE_LEAVES, groups=[64], rms_bound=RMS_BOUND,
+                              sample=4096, reps=3)
+
+    def run_block(nsteps):
+        upload()
+        ctx.step_block(par, T, eta, levels, 1)  # warm-up: buffers and captured graphs
+        upload()
+        d0 = ctx.diagnostics(par)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        st = ctx.step_block(par, T, eta, levels, nsteps)
+        torch.cuda.synchronize()
+        el = time.perf_counter() - t0
+        d1 = ctx.diagnostics(par)
+        return el, st, d0, d1
+
+    def drifts(d0, d1):
+        l0, l1 = np.array(d0["angular_momentum"]), np.array(d1["angular_momentum"])
+        return abs((d1["total"] - d0["total"]) / d0["total"]), float(np.linalg.norm(l1 - l0) / np.linalg.norm(l0))
+
+    with Clocks(local) as clk:
+        el, st, d0, d1 = run_block(steps)
+        de, dl = drifts(d0, d1)
+        short = min(steps, 50)
+        el_s, st_s, s0, s1 = run_block(short)
+        de_s, _ = drifts(s0, s1)
+        upload()
+        f0 = ctx.diagnostics(par)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ctx.call("gbh_state_step", par, T / 32, 32 * short)
+        torch.cuda.synchronize()
+        el_g = time.perf_counter() - t0
+        de_g, _ = drifts(f0, ctx.diagnostics(par))
+    ctx.close()
+    print(json.dumps({
+        "metric": "galaxy block steps: particle-steps/s (each block step advances all particles by T)",
+        "value": n * steps / el, "unit": "particle-steps/s", "n_gpus": 1, "steps": steps, "data": "synthetic",
+        "config": {"workload": f"galaxy N={n} (40 % exponential disk, 10 % Hernquist bulge, 50 % NFW halo at 4x "
+                               f"the disk particle mass), eps={eps}, theta={THETA}, {levels} levels, eta={eta}, T={T}",
+                   "leaf_size": par.leaf_size, "group_size": par.group_size or 64,
+                   "timing": "wall clock around one gbh_state_step_block call (host reads one event tick per event)"},
+        "block_steps_per_s": steps / el, "events": st["substeps"], "walked_stars": st["evaluations"],
+        "walked_fraction": st["evaluations"] / (n * st["substeps"]) if st["substeps"] else None,
+        "energy_drift": de, "angular_momentum_drift": dl,
+        "vs_finest_rung_global_steps": {
+            "block_steps": short, "block_seconds": el_s, "block_energy_drift": de_s,
+            "global_steps": 32 * short, "global_seconds": el_g, "global_energy_drift": de_g,
+            "speedup": el_g / el_s},
+        "clocks": clk.summary()}), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
@@ -770,15 +855,18 @@ def main():
                     help="leaf size; 0 (default) lets the autotuner choose for each walk")
     ap.add_argument("--profile", choices=["mixed", "plain", "fp64", "adjoint", "forest", "build"], default=None,
                     help="run only two force evaluations with this walk (for ncu captures)")
-    ap.add_argument("--workload", choices=["merger", "adjoint", "forest", "scaling", "sweep"], default="merger",
+    ap.add_argument("--workload", choices=["merger", "adjoint", "forest", "scaling", "sweep", "galaxy"],
+                    default="merger",
                     help="adjoint: the differentiable workload (gbh_fwd_save / gbh_bwd); forest: 64 systems in "
-                         "one state with the autotuner; each prints its own JSON line")
+                         "one state with the autotuner; sweep: the merger at theta 0.3 / 0.5 / 0.8; galaxy: the "
+                         "131,072-body galaxy in block steps; scaling: 1M to 64M bodies; each prints its own "
+                         "JSON line")
     ap.add_argument("--fd-coords", type=int, default=16, help="adjoint: coordinates checked by central differences")
     ap.add_argument("--sizes", type=int, nargs="+", default=[1 << 20, 1 << 22, 1 << 24, 1 << 26],
                     help="scaling: body counts")
     args = ap.parse_args()
     if args.steps is None:
-        args.steps = 200 if args.workload == "sweep" else 10
+        args.steps = {"sweep": 200, "galaxy": 500}.get(args.workload, 10)
     if args.workload == "adjoint":
         return run_adjoint(args)
     if args.workload == "forest":
@@ -787,6 +875,8 @@ def main():
         return run_scaling(args)
     if args.workload == "sweep":
         return run_sweep(args)
+    if args.workload == "galaxy":
+        return run_galaxy(args)
     if args.profile:
         return run_profile(args)
     if args.warmup < 3 and args.impl == "ours":
