@@ -38,6 +38,7 @@ class Params(ctypes.Structure):
 CFG_NO_GRAPHS = 1
 CFG_BLOCKING_SYNC = 2
 CFG_NO_LPT = 4
+CFG_NO_SPLIT = 8
 
 
 class Config(ctypes.Structure):

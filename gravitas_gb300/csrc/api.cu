@@ -79,6 +79,7 @@ struct gbh_ctx {
     std::vector<int32_t> hole_list;   // alive holes of the resident state, ascending
     bool use_graphs = true;
     bool use_lpt = true;  // longest-first group order of the mixed walk
+    bool use_split = true;  // split walks of few groups over several warps
     cudaEvent_t wait_ev = nullptr;  // GBH_CFG_BLOCKING_SYNC: host waits sleep on this event
     cudaEvent_t ahead[4] = {};      // GBH_CFG_BLOCKING_SYNC: ends of the last steps launched
     bool capturing = false;  // stage events become graph event-record nodes
@@ -260,6 +261,7 @@ int forces(gbh_ctx *ctx, const gbh_params *p, int64_t n, const double *px, const
     CK(gbh::tree_alloc(ctx->tb, n, leaf, forest ? ctx->nsys : 1));
     ctx->tb.group = p->group_size == 32 ? 32 : 64;
     ctx->tb.lpt = ctx->use_lpt;
+    ctx->tb.split = ctx->use_split;
     CK(stage_event(ctx));
     CK(gbh::tree_build(L, ctx->tb, n, px, py, pz, mass, kind, alive, ax, ay, az, theta, leaf, p->dark_matter_off,
                        p->walk == GBH_WALK_FP64, p->walk == GBH_WALK_PLAIN, forest ? ctx->sys_of : nullptr,
@@ -276,7 +278,8 @@ int forces(gbh_ctx *ctx, const gbh_params *p, int64_t n, const double *px, const
             CK(gbh::walk_plain(L, ctx->tb, ctx->tb.cap_n, float(eps2), ax, ay, az));
             break;
         default:
-            CK(gbh::walk_mixed(L, ctx->tb, ctx->tb.cap_n, float(eps2), quad, ax, ay, az));
+            // sized by the body count (not the capacity): a split walk's parts depend on n alone
+            CK(gbh::walk_mixed(L, ctx->tb, n, float(eps2), quad, ax, ay, az));
             break;
     }
     CK(stage_event(ctx));
@@ -516,6 +519,9 @@ int forces_active(gbh_ctx *ctx, const gbh_params *p, const uint8_t *kind, const 
     int leaf = leaf_of(p);
     int64_t n = ctx->n;
     CK(gbh::tree_alloc(ctx->tb, n, leaf));
+    ctx->tb.group = p->group_size == 32 ? 32 : 64;
+    ctx->tb.lpt = ctx->use_lpt;
+    ctx->tb.split = ctx->use_split;
     CK(stage_event(ctx));
     CK(gbh::tree_build(L, ctx->tb, n, ctx->px, ctx->py, ctx->pz, ctx->mass, kind, alive, ctx->ax, ctx->ay, ctx->az,
                        theta_of(p), leaf, p->dark_matter_off, p->walk == GBH_WALK_FP64, p->walk == GBH_WALK_PLAIN));
@@ -532,7 +538,7 @@ int forces_active(gbh_ctx *ctx, const gbh_params *p, const uint8_t *kind, const 
             CK(gbh::walk_plain(L, ctx->tb, ctx->tb.cap_n, float(eps2), ctx->ax, ctx->ay, ctx->az, true));
             break;
         default:
-            CK(gbh::walk_mixed(L, ctx->tb, ctx->tb.cap_n, float(eps2), quad, ctx->ax, ctx->ay, ctx->az, true));
+            CK(gbh::walk_mixed(L, ctx->tb, n, float(eps2), quad, ctx->ax, ctx->ay, ctx->az, true));
             break;
     }
     CK(stage_event(ctx));
@@ -674,6 +680,7 @@ int gbh_create(const gbh_config *cfg, gbh_ctx **out, char *err, int errlen) {
     c->device = dev;
     c->use_graphs = !(cfg && (cfg->flags & GBH_CFG_NO_GRAPHS));
     c->use_lpt = !(cfg && (cfg->flags & GBH_CFG_NO_LPT));
+    c->use_split = !(cfg && (cfg->flags & GBH_CFG_NO_SPLIT));
     if (cfg && (cfg->flags & GBH_CFG_BLOCKING_SYNC)) {
         e = cudaEventCreateWithFlags(&c->wait_ev, cudaEventBlockingSync | cudaEventDisableTiming);
         for (auto &ev : c->ahead)

@@ -118,6 +118,12 @@ struct TreeBufs {
     uint32_t *gcost = nullptr;
     int32_t *gperm = nullptr;
     bool lpt = true;                // set per call by the caller
+    // Split walks: when a single system has too few 64-star groups to fill the GPU, each group's
+    // walk is shared by several warps (parts), each owning a contiguous range of source stars;
+    // the parts' sums land in part_acc ([part][axis][cap_n]) and are added in part order.
+    double *part_acc = nullptr;
+    int64_t part_cap = 0;           // doubles
+    bool split = true;              // set per call by the caller
     bool moments_exact = false;     // the last build ran the bit-exact FP64 upsweep
     // scan temporaries
     uint32_t *scan_tmp = nullptr;
@@ -157,6 +163,15 @@ cudaError_t block_close(const Launch &L, const TreeBufs &b, int64_t n, int32_t t
                         double eps, const double *ax, const double *ay, const double *az, double *vx, double *vy,
                         double *vz, uint8_t *rung, int32_t *end);
 // ---- moments.cu ----
+// Parts per group of a split mixed walk over n stars in groups of gsize (1: no split, at most
+// 8), from the number of groups per SM.
+constexpr int kMaxWalkParts = 8;
+int walk_parts(int64_t n, int gsize);
+// Grows part_acc for a split walk over the n bodies of a call (no allocation when it already
+// fits). The parts depend on n alone, never on the buffers' capacity, so the same inputs give
+// the same bits in any context.
+cudaError_t split_reserve(TreeBufs &b, int64_t n);
+
 // FP32 upsweep; writes the walk records of the plain walk (PNode) and/or the mixed walk (MNode).
 cudaError_t upsweep_fast(const Launch &L, TreeBufs &b, bool plain_records);
 // Fills the FP64 moment fields of the node table from the MNode records (after an FP32 upsweep).

@@ -1374,7 +1374,7 @@ static cudaError_t scan_dyn(const Launch &L, const uint32_t *in, uint32_t *out, 
 void tree_free(TreeBufs &b) {
     void *ptrs[] = {b.flag, b.bbox_part, b.keys, b.keys_alt, b.order, b.order_alt, b.hist, b.sx, b.sy, b.sz, b.sm,
                     b.st_hi, b.st_lo, b.st_off, b.chain_cnt, b.leaves, b.targets, b.geo, b.sid_sorted, b.groups, b.gcost, b.gperm, b.pre_parent, b.pre_info, b.pre_nchild, b.pre_mask, b.pre_ref, b.nodes,
-                    b.n_parent, b.n_info, b.n_arrive, b.pnodes, b.mnodes, b.mrange, b.scan_tmp, b.info};
+                    b.n_parent, b.n_info, b.n_arrive, b.pnodes, b.mnodes, b.mrange, b.scan_tmp, b.info, b.part_acc};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     b = TreeBufs{};
@@ -1389,7 +1389,7 @@ cudaError_t tree_alloc(TreeBufs &b, int64_t n, int leaf, int32_t nsys) {
     if (nsys < 1) nsys = 1;
     if (n <= b.cap_n && need_nodes <= b.cap_nodes && nsys <= b.cap_sys && n / 32 + nsys + 1 <= b.cap_groups) {
         b.nsys = nsys;
-        return cudaSuccess;
+        return split_reserve(b, n);
     }
     if (nsys > b.cap_sys) b.cap_sys = 0;
     int64_t cn = n > b.cap_n ? n + n / 4 : b.cap_n;  // grow by 1.25x like gpuBuffers.ensure (gpu_darwin.go:164-177)
@@ -1459,7 +1459,8 @@ cudaError_t tree_alloc(TreeBufs &b, int64_t n, int leaf, int32_t nsys) {
     b.nsys = nsys;
     // no launch order yet: gperm[cap_groups] = -1 matches no group count
     if ((e = cudaMemset(b.gperm, 0xff, sizeof(int32_t) * size_t(cgroups + 1))) != cudaSuccess) return e;
-    return cudaMemset(b.info, 0, sizeof(DevInfo));
+    if ((e = cudaMemset(b.info, 0, sizeof(DevInfo))) != cudaSuccess) return e;
+    return split_reserve(b, n);
 }
 
 #define GBH_LAUNCH_CHECK()                         \

@@ -133,7 +133,12 @@ __device__ __forceinline__ void kahan_fold2(float2 &s, float2 &c, float2 &part) 
 // Without a target list 9 blocks of 128 per SM (56 registers, a few spills) measured 1.8 % faster
 // than 8 (64 registers, no room for a ninth block); 10 (48 registers) was slower. The target-list
 // form needs more registers and keeps 8.
-template <bool kQuad, bool kSoft, bool kPot, bool kShared>
+// kSplit: each group's walk is shared by nparts warps, part p owning the source stars
+// [p ns / nparts, (p + 1) ns / nparts): a node is owned by the part that holds its first star
+// (nodes are visited in pre-order, so first stars never decrease along the walk); every part
+// tests the nodes whose ranges reach into its own, with the group's vote, so all parts agree on
+// every node and each accepted node and opened leaf is added by exactly its owner.
+template <bool kQuad, bool kSoft, bool kPot, bool kShared, bool kSplit = false>
 __global__ __launch_bounds__(kMixedThreads, kShared ? 9 : 8) void k_walk_mixed2(const DevInfo *info, const MNode *__restrict__ nodes,
                                                                const int2 *__restrict__ ranges,
                                                                const float4 *__restrict__ st_hi,
@@ -144,13 +149,18 @@ __global__ __launch_bounds__(kMixedThreads, kShared ? 9 : 8) void k_walk_mixed2(
                                                                const int32_t *__restrict__ targets,
                                                                const int4 *__restrict__ groups, int pair,
                                                                const int32_t *__restrict__ gperm, int32_t perm_cap,
-                                                               uint32_t *gcost, DevInfo *err_info) {
+                                                               uint32_t *gcost, DevInfo *err_info, int nparts,
+                                                               double *part_acc, int64_t part_stride) {
     // pair: 64-star groups, lane l walks stars 2l and 2l + 1; else 32-star groups, one star per
     // lane (the second FP32x2 slot then repeats the first and is not written)
     const int lane = threadIdx.x & 31;
     const int32_t ns = int32_t(info->nstars);  // the C-ABI caps n at 2^30
     const uint32_t nn = uint32_t(info->nnodes);
-    const int32_t g = int32_t((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    const int32_t wid = int32_t((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    const int32_t g = kSplit ? wid / nparts : wid;
+    const int part = kSplit ? wid - g * nparts : 0;
+    const int32_t s_lo = kSplit ? int32_t(int64_t(ns) * part / nparts) : 0;
+    const int32_t s_hi = kSplit ? int32_t(int64_t(ns) * (part + 1) / nparts) : ns;
     // longest first: walk the group the last walk's costs put at this position (gperm holds a
     // permutation of the groups, valid while its recorded group count matches)
     int32_t base, nt, root = 0, gw = g;
@@ -201,6 +211,20 @@ __global__ __launch_bounds__(kMixedThreads, kShared ? 9 : 8) void k_walk_mixed2(
             break;
         }
         const MNode nd = nodes[i];
+        bool own = true;  // this warp adds the node's interactions (always, unless split)
+        if constexpr (kSplit) {
+            const int2 rg = ranges[i];
+            if (rg.x >= s_hi) break;  // this node and every later one start after the part
+            if (rg.y <= s_lo) {       // the whole subtree lies before the part
+                i = __float_as_int(nd.d.w);
+                if (++visits > nn + 32u) {
+                    if (lane == 0) set_err(err_info, 4);
+                    break;
+                }
+                continue;
+            }
+            own = rg.x >= s_lo;
+        }
         float2 dx, dy, dz;
         if constexpr (kShared) {  // 6 scalar adds + 3 packed: measured 2-3 % faster than 9 packed
             dx = add2(f2((nd.a.x + nox.x) + nd.b.x), nrx);
@@ -215,37 +239,39 @@ __global__ __launch_bounds__(kMixedThreads, kShared ? 9 : 8) void k_walk_mixed2(
         const bool open = __any_sync(kFull, (d2.x < nd.a.w) | (d2.y < nd.a.w));
         const int first = __float_as_int(nd.d.z), next = __float_as_int(nd.d.w);
         if (!open) {
-            const float2 r2 = add2(d2, e2);
-            const float2 ir = make_float2(rsqrtf(r2.x), rsqrtf(r2.y));
-            const float2 ir2 = mul2(ir, ir);
-            const float2 ir3 = mul2(ir, ir2);
-            if constexpr (kPot) {
-                float2 t = mul2(f2(nd.b.w), ir);
-                if (kQuad) {
+            if (own) {
+                const float2 r2 = add2(d2, e2);
+                const float2 ir = make_float2(rsqrtf(r2.x), rsqrtf(r2.y));
+                const float2 ir2 = mul2(ir, ir);
+                const float2 ir3 = mul2(ir, ir2);
+                if constexpr (kPot) {
+                    float2 t = mul2(f2(nd.b.w), ir);
+                    if (kQuad) {
+                        const float2 qx = fma2(f2(nd.d.x), dz, fma2(f2(nd.c.w), dy, mul2(f2(nd.c.x), dx)));
+                        const float2 qy = fma2(f2(nd.d.y), dz, fma2(f2(nd.c.y), dy, mul2(f2(nd.c.w), dx)));
+                        const float2 qz = fma2(f2(nd.c.z), dz, fma2(f2(nd.d.y), dy, mul2(f2(nd.d.x), dx)));
+                        const float2 dqd = fma2(dz, qz, fma2(dy, qy, mul2(dx, qx)));
+                        t = fma2(mul2(f2(0.5f), dqd), mul2(ir3, ir2), t);
+                    }
+                    px = add2(px, t);
+                } else if (kQuad) {
                     const float2 qx = fma2(f2(nd.d.x), dz, fma2(f2(nd.c.w), dy, mul2(f2(nd.c.x), dx)));
                     const float2 qy = fma2(f2(nd.d.y), dz, fma2(f2(nd.c.y), dy, mul2(f2(nd.c.w), dx)));
                     const float2 qz = fma2(f2(nd.c.z), dz, fma2(f2(nd.d.y), dy, mul2(f2(nd.d.x), dx)));
+                    const float2 ir5 = mul2(ir3, ir2);
                     const float2 dqd = fma2(dz, qz, fma2(dy, qy, mul2(dx, qx)));
-                    t = fma2(mul2(f2(0.5f), dqd), mul2(ir3, ir2), t);
+                    const float2 u = mul2(mul2(f2(2.5f), ir2), dqd);
+                    const float2 f = fma2(ir5, u, mul2(f2(nd.b.w), ir3));
+                    const float2 nir5 = mul2(f2(-1.f), ir5);
+                    px = fma2(nir5, qx, fma2(f, dx, px));
+                    py = fma2(nir5, qy, fma2(f, dy, py));
+                    pz = fma2(nir5, qz, fma2(f, dz, pz));
+                } else {
+                    const float2 f = mul2(f2(nd.b.w), ir3);
+                    px = fma2(f, dx, px);
+                    py = fma2(f, dy, py);
+                    pz = fma2(f, dz, pz);
                 }
-                px = add2(px, t);
-            } else if (kQuad) {
-                const float2 qx = fma2(f2(nd.d.x), dz, fma2(f2(nd.c.w), dy, mul2(f2(nd.c.x), dx)));
-                const float2 qy = fma2(f2(nd.d.y), dz, fma2(f2(nd.c.y), dy, mul2(f2(nd.c.w), dx)));
-                const float2 qz = fma2(f2(nd.c.z), dz, fma2(f2(nd.d.y), dy, mul2(f2(nd.d.x), dx)));
-                const float2 ir5 = mul2(ir3, ir2);
-                const float2 dqd = fma2(dz, qz, fma2(dy, qy, mul2(dx, qx)));
-                const float2 u = mul2(mul2(f2(2.5f), ir2), dqd);
-                const float2 f = fma2(ir5, u, mul2(f2(nd.b.w), ir3));
-                const float2 nir5 = mul2(f2(-1.f), ir5);
-                px = fma2(nir5, qx, fma2(f, dx, px));
-                py = fma2(nir5, qy, fma2(f, dy, py));
-                pz = fma2(nir5, qz, fma2(f, dz, pz));
-            } else {
-                const float2 f = mul2(f2(nd.b.w), ir3);
-                px = fma2(f, dx, px);
-                py = fma2(f, dy, py);
-                pz = fma2(f, dz, pz);
             }
             i = next;
         } else if (first >= 0) {
@@ -256,50 +282,52 @@ __global__ __launch_bounds__(kMixedThreads, kShared ? 9 : 8) void k_walk_mixed2(
                 if (lane == 0) set_err(err_info, 5);
                 break;
             }
-            pairs += uint32_t(r.y - r.x);
-            // Leaf stars: separation = (leaf com - star) + (leaf star - com), the first the visit's
-            // separation, the second the star's FP32 offset stored by the upsweep. In a star's own
-            // leaf the first term is replaced by the negative of the star's own stored offset, so
-            // that its self pair is exactly zero and its close pairs are differences of two offsets.
-            float2 lx = dx, ly = dy, lz = dz;
-            if (k0 >= r.x && k0 < r.y) {
-                const float4 o = st_off[k0];
-                lx.x = -o.x;
-                ly.x = -o.y;
-                lz.x = -o.z;
-            }
-            if (k1 >= r.x && k1 < r.y) {
-                const float4 o = st_off[k1];
-                lx.y = -o.x;
-                ly.y = -o.y;
-                lz.y = -o.z;
-            }
-#pragma unroll 4  // measured 2-3 % faster than no unrolling (independent source stars)
-            for (int j = r.x; j < r.y; ++j) {
-                const float4 so = st_off[j];
-                const float2 ex = add2(lx, f2(so.x));
-                const float2 ey = add2(ly, f2(so.y));
-                const float2 ez = add2(lz, f2(so.z));
-                const float2 r2 = fma2(ez, ez, fma2(ey, ey, fma2(ex, ex, e2)));
-                // A star paired with itself gives a separation of exactly 0: with eps2 > 0 that adds
-                // 0, as skipping j == self does (bh.go:191-193). Without softening r2 = 0 is masked.
-                float2 ir;
-                if (kSoft) {
-                    ir = make_float2(rsqrtf(r2.x), rsqrtf(r2.y));
-                } else {
-                    ir = make_float2(r2.x > 0.f ? rsqrtf(r2.x) : 0.f, r2.y > 0.f ? rsqrtf(r2.y) : 0.f);
+            if (own) {
+                pairs += uint32_t(r.y - r.x);
+                // Leaf stars: separation = (leaf com - star) + (leaf star - com), the first the visit's
+                // separation, the second the star's FP32 offset stored by the upsweep. In a star's own
+                // leaf the first term is replaced by the negative of the star's own stored offset, so
+                // that its self pair is exactly zero and its close pairs are differences of two offsets.
+                float2 lx = dx, ly = dy, lz = dz;
+                if (k0 >= r.x && k0 < r.y) {
+                    const float4 o = st_off[k0];
+                    lx.x = -o.x;
+                    ly.x = -o.y;
+                    lz.x = -o.z;
                 }
-                if constexpr (kPot) {
-                    // the self pair has zero separation but m / eps is not zero: skip j == self
-                    float2 t = mul2(f2(so.w), ir);
-                    t.x = j == k0 ? 0.f : t.x;
-                    t.y = j == k1 ? 0.f : t.y;
-                    px = add2(px, t);
-                } else {
-                    const float2 f = mul2(mul2(f2(so.w), ir), mul2(ir, ir));
-                    px = fma2(f, ex, px);
-                    py = fma2(f, ey, py);
-                    pz = fma2(f, ez, pz);
+                if (k1 >= r.x && k1 < r.y) {
+                    const float4 o = st_off[k1];
+                    lx.y = -o.x;
+                    ly.y = -o.y;
+                    lz.y = -o.z;
+                }
+    #pragma unroll 4  // measured 2-3 % faster than no unrolling (independent source stars)
+                for (int j = r.x; j < r.y; ++j) {
+                    const float4 so = st_off[j];
+                    const float2 ex = add2(lx, f2(so.x));
+                    const float2 ey = add2(ly, f2(so.y));
+                    const float2 ez = add2(lz, f2(so.z));
+                    const float2 r2 = fma2(ez, ez, fma2(ey, ey, fma2(ex, ex, e2)));
+                    // A star paired with itself gives a separation of exactly 0: with eps2 > 0 that adds
+                    // 0, as skipping j == self does (bh.go:191-193). Without softening r2 = 0 is masked.
+                    float2 ir;
+                    if (kSoft) {
+                        ir = make_float2(rsqrtf(r2.x), rsqrtf(r2.y));
+                    } else {
+                        ir = make_float2(r2.x > 0.f ? rsqrtf(r2.x) : 0.f, r2.y > 0.f ? rsqrtf(r2.y) : 0.f);
+                    }
+                    if constexpr (kPot) {
+                        // the self pair has zero separation but m / eps is not zero: skip j == self
+                        float2 t = mul2(f2(so.w), ir);
+                        t.x = j == k0 ? 0.f : t.x;
+                        t.y = j == k1 ? 0.f : t.y;
+                        px = add2(px, t);
+                    } else {
+                        const float2 f = mul2(mul2(f2(so.w), ir), mul2(ir, ir));
+                        px = fma2(f, ex, px);
+                        py = fma2(f, ey, py);
+                        pz = fma2(f, ez, pz);
+                    }
                 }
             }
             i = next;
@@ -317,6 +345,20 @@ __global__ __launch_bounds__(kMixedThreads, kShared ? 9 : 8) void k_walk_mixed2(
     kahan_fold2(sx, cx, px);
     kahan_fold2(sy, cy, py);
     kahan_fold2(sz, cz, pz);
+    if constexpr (kSplit) {  // the part's sums, by sorted index; k_split_combine adds the parts
+        double *q = part_acc + int64_t(part) * 3 * part_stride;
+        if (v0) {
+            q[k0] = double(sx.x) - double(cx.x);
+            q[part_stride + k0] = double(sy.x) - double(cy.x);
+            q[2 * part_stride + k0] = double(sz.x) - double(cz.x);
+        }
+        if (v1) {
+            q[k1] = double(sx.y) - double(cx.y);
+            q[part_stride + k1] = double(sy.y) - double(cy.y);
+            q[2 * part_stride + k1] = double(sz.y) - double(cz.y);
+        }
+        return;
+    }
     if (gcost && lane == 0) gcost[gw] = 2u * visits + pairs;  // the group's cost
     if constexpr (kPot) {
         if (v0) ax[k0] = double(sx.x) - double(cx.x);
@@ -418,19 +460,60 @@ __global__ __launch_bounds__(kLptThreads) void k_lpt_order(const DevInfo *info, 
     if (t == 0) gperm[perm_cap] = ng;
 }
 
+// Sum of a split walk's parts for every walked star, in part order, to state order.
+__global__ __launch_bounds__(256) void k_split_combine(const DevInfo *info, const int32_t *__restrict__ order,
+                                                       const int32_t *__restrict__ targets, int nparts,
+                                                       const double *__restrict__ part_acc, int64_t stride,
+                                                       double *ax, double *ay, double *az) {
+    const int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    const int64_t nt = targets ? int64_t(info->ntargets) : info->nstars;
+    if (t >= nt) return;
+    const int32_t k = targets ? targets[t] : int32_t(t);
+    double x = 0, y = 0, z = 0;
+    for (int p = 0; p < nparts; ++p) {
+        const double *q = part_acc + int64_t(p) * 3 * stride;
+        x += q[k];
+        y += q[stride + k];
+        z += q[2 * stride + k];
+    }
+    const int32_t o = order[k];
+    ax[o] = x;
+    ay[o] = y;
+    az[o] = z;
+}
+
 template <bool kQuad, bool kSoft, bool kPot, bool kShared>
 static cudaError_t launch_mixed_t(const Launch &L, const TreeBufs &b, int64_t nstars_cap, float eps2, double *ax,
                                 double *ay, double *az, bool targets) {
     const bool forest = b.nsys > 1;
     const int gsize = b.group == 32 ? 32 : 64;
     int64_t groups = forest ? b.cap_groups : (nstars_cap + gsize - 1) / gsize;
+    if constexpr (!kPot) {  // few groups: split each group's walk over several warps
+        const int parts = (!forest && b.split) ? walk_parts(nstars_cap, gsize) : 1;
+        if (parts > 1 && b.part_acc && int64_t(parts) * 3 * nstars_cap <= b.part_cap) {
+            const int64_t warps = groups * parts;
+            const int64_t wblocks = (warps + kMixedThreads / 32 - 1) / (kMixedThreads / 32);
+            k_walk_mixed2<kQuad, kSoft, false, kShared, true>
+                <<<unsigned(wblocks < 1 ? 1 : wblocks), kMixedThreads, 0, L.stream>>>(
+                    b.info, b.mnodes, b.mrange, b.st_hi, b.st_lo, b.st_off, b.order, eps2, ax, ay, az,
+                    targets ? b.targets : nullptr, nullptr, gsize == 64 ? 1 : 0, nullptr, int32_t(b.cap_groups),
+                    nullptr, b.info, parts, b.part_acc, nstars_cap);
+            ++*L.count;
+            cudaError_t e = cudaGetLastError();
+            if (e != cudaSuccess) return e;
+            k_split_combine<<<blocks_for(nstars_cap, 256), 256, 0, L.stream>>>(
+                b.info, b.order, targets ? b.targets : nullptr, parts, b.part_acc, nstars_cap, ax, ay, az);
+            ++*L.count;
+            return cudaGetLastError();
+        }
+    }
     const bool lpt = b.lpt && !targets && !kPot;
     int64_t blocks = (groups + kMixedThreads / 32 - 1) / (kMixedThreads / 32);
     k_walk_mixed2<kQuad, kSoft, kPot, kShared><<<unsigned(blocks < 1 ? 1 : blocks), kMixedThreads, 0, L.stream>>>(
         b.info, b.mnodes, b.mrange, b.st_hi, b.st_lo, b.st_off, b.order, eps2, ax, ay, az,
         targets ? b.targets : nullptr,
         forest ? b.groups : nullptr, gsize == 64 ? 1 : 0, lpt ? b.gperm : nullptr, int32_t(b.cap_groups),
-        lpt ? b.gcost : nullptr, b.info);
+        lpt ? b.gcost : nullptr, b.info, 1, nullptr, 0);
     ++*L.count;
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess || !lpt) return e;
@@ -464,6 +547,41 @@ cudaError_t walk_mixed_potential(const Launch &L, const TreeBufs &b, int64_t nst
     if (quad) return launch_mixed<true, false, true>(L, b, nstars_cap, eps2, psi, nullptr, nullptr, false);
     if (soft) return launch_mixed<false, true, true>(L, b, nstars_cap, eps2, psi, nullptr, nullptr, false);
     return launch_mixed<false, false, true>(L, b, nstars_cap, eps2, psi, nullptr, nullptr, false);
+}
+
+int walk_parts(int64_t n, int gsize) {
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms < 1)
+        sms = 152;
+    // Measured on the 1M-body galaxy model cut to 16k-512k bodies (leaf 32): each part re-tests
+    // the nodes above its range and skips the subtrees beside it, so splitting pays only while
+    // the unsplit walk leaves most of the GPU idle. Best part counts by groups per SM: up to 7
+    // -> 8 (3.4x at 16k bodies, 1.9x at 64k), up to 14 -> 4 (1.09x at 128k), up to 21 -> 2
+    // (1.15x at 192k), more -> no split (2 parts were 1.2x slower at 256k).
+    const int64_t groups = (n + gsize - 1) / gsize;
+    if (groups <= 7 * int64_t(sms)) return kMaxWalkParts;
+    if (groups <= 14 * int64_t(sms)) return 4;
+    if (groups <= 21 * int64_t(sms)) return 2;
+    return 1;
+}
+
+cudaError_t split_reserve(TreeBufs &b, int64_t n) {
+    const int parts = walk_parts(n, 64);  // 64-star groups split the most
+    if (parts <= 1) return cudaSuccess;
+    const int64_t need = int64_t(parts) * 3 * n;
+    if (need <= b.part_cap) return cudaSuccess;
+    if (b.part_acc) cudaFree(b.part_acc);
+    b.part_acc = nullptr;
+    b.part_cap = 0;
+    const int64_t cap = need + need / 4;
+    cudaError_t e = cudaMalloc(&b.part_acc, sizeof(double) * size_t(cap));
+    if (e != cudaSuccess) {
+        b.part_acc = nullptr;
+        return e;
+    }
+    b.part_cap = cap;
+    return cudaSuccess;
 }
 
 cudaError_t fp32_fma_probe(const Launch &L, int blocks, int iters, float *out) {

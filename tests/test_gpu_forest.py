@@ -85,8 +85,11 @@ def test_forest_trees_and_fp64_forces_equal_each_system_alone(ctx, theta, leaf):
 
 
 @pytest.mark.parametrize("walk,group", [("mixed", 64), ("mixed", 32), ("plain", 0), ("fp64", 0)])
-def test_forest_steps_equal_each_system_stepped_alone(ctx, walk, group):
-    """Bit-identical: the same per-system trees, the same 64- (32-) star groups, the same kernels."""
+def test_forest_steps_equal_each_system_stepped_alone(walk, group):
+    """Bit-identical: the same per-system trees, the same 64- (32-) star groups, the same kernels
+    (a forest never splits a group's walk over several warps; the small systems alone would, so
+    this comparison runs with GBH_CFG_NO_SPLIT)."""
+    ctx = abi.Context(0, abi.CFG_NO_SPLIT)
     s, off = ics.forest(nsys=6, seed=3, nmin=500, nmax=4000)
     nsys, n = len(off) - 1, int(off[-1])
     par = abi.make_params(0.5, 0.02, 8, False, False, walk, group_size=group)
@@ -102,6 +105,7 @@ def test_forest_steps_equal_each_system_stepped_alone(ctx, walk, group):
         alone = download(ctx, hi - lo)
         for k in F9:
             assert np.array_equal(forest[k][lo:hi], alone[k]), (q, k)
+    ctx.close()
 
 
 def test_forest_mixed_accuracy_per_system(ctx):
