@@ -132,9 +132,47 @@ __global__ __launch_bounds__(kScanThreads) void k_scan_apply(const uint32_t *in,
     }
 }
 
+// One block of kSingleThreads scanning up to kSingleThreads * kSingleItems entries in one launch
+// (each thread a run of consecutive entries): the small scans of a small build take one launch
+// instead of three.
+constexpr int kSingleThreads = 1024, kSingleItems = 8;
+__global__ __launch_bounds__(kSingleThreads) void k_scan_single(const uint32_t *in, uint32_t *out, int64_t n,
+                                                                const int64_t *ndyn) {
+    __shared__ uint32_t s_warp[kSingleThreads / 32];
+    const int64_t ne = dyn_len(n, ndyn);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int64_t base = int64_t(threadIdx.x) * kSingleItems;
+    uint32_t v[kSingleItems];
+    uint32_t sum = 0;
+#pragma unroll
+    for (int k = 0; k < kSingleItems; ++k) {
+        v[k] = base + k < ne ? in[base + k] : 0;
+        sum += v[k];
+    }
+    const uint32_t incl = warp_incl_scan(sum);
+    if (lane == 31) s_warp[warp] = incl;
+    __syncthreads();
+    if (warp == 0) {
+        const uint32_t w = s_warp[lane];  // kSingleThreads / 32 == 32 warp totals
+        s_warp[lane] = warp_incl_scan(w) - w;
+    }
+    __syncthreads();
+    uint32_t run = s_warp[warp] + incl - sum;
+#pragma unroll
+    for (int k = 0; k < kSingleItems; ++k) {
+        if (base + k < ne) out[base + k] = run;
+        run += v[k];
+    }
+}
+
 cudaError_t scan_rec(const Launch &L, const uint32_t *in, uint32_t *out, int64_t n, const int64_t *ndyn,
                      uint32_t *tmp, int64_t tmp_cap) {
     int64_t tiles = (n + kScanTile - 1) / kScanTile;
+    if (tiles > 1 && n <= int64_t(kSingleThreads) * kSingleItems) {
+        k_scan_single<<<1, kSingleThreads, 0, L.stream>>>(in, out, n, ndyn);
+        ++*L.count;
+        return cudaGetLastError();
+    }
     if (tiles <= 1) {
         k_scan_apply<<<1, kScanThreads, 0, L.stream>>>(in, out, n, ndyn, nullptr);
         ++*L.count;
