@@ -80,6 +80,7 @@ struct gbh_ctx {
     bool use_graphs = true;
     bool use_lpt = true;  // longest-first group order of the mixed walk
     bool use_split = true;  // split walks of few groups over several warps
+    int64_t active_hint = 0;  // block steps: the stars the last event walked
     cudaEvent_t wait_ev = nullptr;  // GBH_CFG_BLOCKING_SYNC: host waits sleep on this event
     cudaEvent_t ahead[4] = {};      // GBH_CFG_BLOCKING_SYNC: ends of the last steps launched
     bool capturing = false;  // stage events become graph event-record nodes
@@ -262,6 +263,7 @@ int forces(gbh_ctx *ctx, const gbh_params *p, int64_t n, const double *px, const
     ctx->tb.group = p->group_size == 32 ? 32 : 64;
     ctx->tb.lpt = ctx->use_lpt;
     ctx->tb.split = ctx->use_split;
+    ctx->tb.walk_hint = 0;
     CK(stage_event(ctx));
     CK(gbh::tree_build(L, ctx->tb, n, px, py, pz, mass, kind, alive, ax, ay, az, theta, leaf, p->dark_matter_off,
                        p->walk == GBH_WALK_FP64, p->walk == GBH_WALK_PLAIN, forest ? ctx->sys_of : nullptr,
@@ -522,6 +524,7 @@ int forces_active(gbh_ctx *ctx, const gbh_params *p, const uint8_t *kind, const 
     ctx->tb.group = p->group_size == 32 ? 32 : 64;
     ctx->tb.lpt = ctx->use_lpt;
     ctx->tb.split = ctx->use_split;
+    ctx->tb.walk_hint = ctx->active_hint;  // this event's list is not known on the host yet
     CK(stage_event(ctx));
     CK(gbh::tree_build(L, ctx->tb, n, ctx->px, ctx->py, ctx->pz, ctx->mass, kind, alive, ctx->ax, ctx->ay, ctx->az,
                        theta_of(p), leaf, p->dark_matter_off, p->walk == GBH_WALK_FP64, p->walk == GBH_WALK_PLAIN));
@@ -573,6 +576,7 @@ int run_block_steps(gbh_ctx *ctx, const gbh_params *p, double T, double eta, int
     }
     CK(gbh::tree_alloc(ctx->tb, n, leaf_of(p)));
     int rc;
+    ctx->active_hint = n;  // the first event is sized for all bodies
     for (int64_t s = 0; s < nsteps; ++s) {
         CK(gbh::block_open(L, ctx->tb, n, T, levels, eta, eps, ctx->ax, ctx->ay, ctx->az, ctx->vx, ctx->vy, ctx->vz,
                            ctx->rung, ctx->end_tick));
@@ -589,6 +593,7 @@ int run_block_steps(gbh_ctx *ctx, const gbh_params *p, double T, double eta, int
             CK(gbh::block_close(L, ctx->tb, n, t, T, levels, eta, eps, ctx->ax, ctx->ay, ctx->az, ctx->vx, ctx->vy,
                                 ctx->vz, ctx->rung, ctx->end_tick));
             if ((rc = read_info(ctx))) return rc;
+            if (ctx->info_host.ntargets > 0) ctx->active_hint = int64_t(ctx->info_host.ntargets);
             if (st) {
                 st->substeps += 1;
                 st->evaluations += ctx->info_host.ntargets;

@@ -124,6 +124,7 @@ struct TreeBufs {
     double *part_acc = nullptr;
     int64_t part_cap = 0;           // doubles
     bool split = true;              // set per call by the caller
+    int64_t walk_hint = 0;          // a target-list walk's expected list length (0: the body count)
     bool moments_exact = false;     // the last build ran the bit-exact FP64 upsweep
     // scan temporaries
     uint32_t *scan_tmp = nullptr;
@@ -164,8 +165,8 @@ cudaError_t block_close(const Launch &L, const TreeBufs &b, int64_t n, int32_t t
                         double *vz, uint8_t *rung, int32_t *end);
 // ---- moments.cu ----
 // Parts per group of a split mixed walk over n stars in groups of gsize (1: no split, at most
-// 8), from the number of groups per SM.
-constexpr int kMaxWalkParts = 8;
+// 16), from the number of groups per SM.
+constexpr int kMaxWalkParts = 16;
 int walk_parts(int64_t n, int gsize);
 // Grows part_acc for a split walk over the n bodies of a call (no allocation when it already
 // fits). The parts depend on n alone, never on the buffers' capacity, so the same inputs give
