@@ -501,7 +501,7 @@ cudaError_t adj_reserve(AdjTape &t, int64_t n, int64_t nsteps, int64_t every, do
         t.block = nullptr;
         t.bytes = 0;
         size_t want = bytes + bytes / 4;
-        cudaError_t e = cudaMalloc(&t.block, want);
+        cudaError_t e = dev_alloc(&t.block, want);
         if (e != cudaSuccess) return e;
         t.bytes = want;
     }

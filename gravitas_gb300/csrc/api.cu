@@ -7,6 +7,8 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <atomic>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -93,6 +95,29 @@ struct gbh_ctx {
     std::string err;
 };
 
+namespace gbh {
+
+// The allocation-failure test hook: -1 disarmed, k >= 0 fails the allocation after k more.
+static std::atomic<long long> g_alloc_fault{-1};
+
+void arm_alloc_fault(long long after) { g_alloc_fault.store(after < 0 ? -1 : after); }
+
+cudaError_t dev_alloc_bytes(void **p, size_t bytes) {
+    long long k = g_alloc_fault.load();
+    while (k >= 0) {
+        if (g_alloc_fault.compare_exchange_weak(k, k - 1)) {
+            if (k == 0) {  // fire once; the counter is now -1 (disarmed)
+                *p = nullptr;
+                return cudaErrorMemoryAllocation;
+            }
+            break;
+        }
+    }
+    return cudaMalloc(p, bytes);
+}
+
+}  // namespace gbh
+
 namespace {
 
 int fail(gbh_ctx *c, int code, const char *fmt, ...) {
@@ -119,7 +144,7 @@ cudaError_t grow(T *&p, int64_t &cap, int64_t need) {
     if (p) cudaFree(p);
     p = nullptr;
     int64_t c = std::max<int64_t>(need + need / 4, 16);
-    cudaError_t e = cudaMalloc(&p, sizeof(T) * size_t(c));
+    cudaError_t e = gbh::dev_alloc(&p, sizeof(T) * size_t(c));
     cap = e == cudaSuccess ? c : 0;
     return e;
 }
@@ -135,7 +160,7 @@ cudaError_t grow_targets(gbh_ctx *c, int64_t need) {
     }
     if (c->tout) cudaFree(c->tout);
     c->tout = nullptr;
-    e = cudaMalloc(&c->tout, sizeof(double) * 3 * size_t(cap));
+    e = gbh::dev_alloc(&c->tout, sizeof(double) * 3 * size_t(cap));
     c->targets_cap = e == cudaSuccess ? cap : 0;
     return e;
 }
@@ -156,9 +181,9 @@ cudaError_t ensure_state(gbh_ctx *c, int64_t n) {
     cudaError_t e = cudaSuccess;
     double **d[] = {&c->px, &c->py, &c->pz, &c->vx, &c->vy, &c->vz, &c->ax, &c->ay, &c->az, &c->mass};
     for (double **p : d)
-        if (e == cudaSuccess) e = cudaMalloc(p, sizeof(double) * size_t(cap));
-    if (e == cudaSuccess) e = cudaMalloc(&c->kind, size_t(cap));
-    if (e == cudaSuccess) e = cudaMalloc(&c->alive, size_t(cap));
+        if (e == cudaSuccess) e = gbh::dev_alloc(p, sizeof(double) * size_t(cap));
+    if (e == cudaSuccess) e = gbh::dev_alloc(&c->kind, size_t(cap));
+    if (e == cudaSuccess) e = gbh::dev_alloc(&c->alive, size_t(cap));
     if (e != cudaSuccess) {
         free_state(c);
         return e;
@@ -672,6 +697,10 @@ int gbh_create(const gbh_config *cfg, gbh_ctx **out, char *err, int errlen) {
     };
     if (!out) return report(GBH_ERR_ARG, "out is NULL");
     *out = nullptr;
+    {  // the allocation-failure test hook (see dev_alloc): armed by GBH_FAULT_ALLOC, else off
+        const char *f = std::getenv("GBH_FAULT_ALLOC");
+        gbh::arm_alloc_fault(f && *f ? std::atoll(f) : -1);
+    }
     int dev = cfg ? cfg->device : 0;
     int count = 0;
     cudaError_t e = cudaGetDeviceCount(&count);
@@ -821,7 +850,7 @@ int gbh_potential_energy(gbh_ctx *ctx, const gbh_params *p, int64_t n, const dou
                        false));
     int64_t nparts = (ctx->tb.cap_n + 255) / 256;
     CK(grow(ctx->part, ctx->part_cap, nparts));
-    if (!ctx->scalar) CK(cudaMalloc(&ctx->scalar, 256));
+    if (!ctx->scalar) CK(gbh::dev_alloc(&ctx->scalar, 256));
     double eps2 = p->softening * p->softening;
     if (fp64) {
         CK(gbh::potential_fp64(L, ctx->tb, n, ctx->px, ctx->py, ctx->pz, ctx->mass, kind ? ctx->kind : nullptr,
@@ -989,7 +1018,7 @@ int gbh_state_diagnostics(gbh_ctx *ctx, const gbh_params *p, double c, gbh_diagn
     const uint8_t *alive = ctx->state_has_alive ? ctx->alive : nullptr;
     Launch L = launch_of(ctx);
     CK(grow(ctx->part, ctx->part_cap, std::max<int64_t>((ctx->cap + 255) / 256, int64_t(gbh::diag_parts()) * 11)));
-    if (!ctx->scalar) CK(cudaMalloc(&ctx->scalar, 256));
+    if (!ctx->scalar) CK(gbh::dev_alloc(&ctx->scalar, 256));
     // potential: the tree at min(theta, 0.9) with the FP64 walk (potential.go:12-42)
     const std::vector<int32_t> &holes = ctx->hole_list;  // alive holes of the state, from its upload
     CK(grow(ctx->holes, ctx->holes_cap, int64_t(holes.size()) + 1));
@@ -1361,7 +1390,7 @@ int gbh_probe_fp32_peak(gbh_ctx *ctx, double ms, double *tflops) {
     int rc = begin(ctx);
     if (rc) return rc;
     if (!tflops) return fail(ctx, GBH_ERR_ARG, "tflops is NULL");
-    if (!ctx->probe) CK(cudaMalloc(&ctx->probe, sizeof(float) * 65536));
+    if (!ctx->probe) CK(gbh::dev_alloc(&ctx->probe, sizeof(float) * 65536));
     Launch L = launch_of(ctx);
     int blocks = ctx->num_sms * 8;  // 8 x 256 threads = 64 warps per SM
     int iters = 64;

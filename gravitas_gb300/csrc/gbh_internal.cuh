@@ -164,6 +164,17 @@ cudaError_t block_close(const Launch &L, const TreeBufs &b, int64_t n, int32_t t
                         double eps, const double *ax, const double *ay, const double *az, double *vx, double *vy,
                         double *vz, uint8_t *rung, int32_t *end);
 // ---- moments.cu ----
+// Every device allocation of the library goes through dev_alloc. A test hook: when a context is
+// created with GBH_FAULT_ALLOC=k in the environment, the allocation after the next k successful
+// ones fails once with cudaErrorMemoryAllocation (cudaMalloc is not called), so that tests can
+// drive the out-of-memory paths from the host; without the variable nothing fails.
+cudaError_t dev_alloc_bytes(void **p, size_t bytes);
+template <class T>
+inline cudaError_t dev_alloc(T **p, size_t bytes) {
+    return dev_alloc_bytes(reinterpret_cast<void **>(p), bytes);
+}
+void arm_alloc_fault(long long after);  // after < 0 disarms
+
 // Parts per group of a split mixed walk over n stars in groups of gsize (1: no split, at most
 // 16), from the number of groups per SM.
 constexpr int kMaxWalkParts = 16;

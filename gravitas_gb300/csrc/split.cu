@@ -314,12 +314,12 @@ cudaError_t split_reserve(SplitBufs &s, int64_t n, const std::vector<int32_t> &h
         s.cap_n = 0;
         int64_t cap = n + n / 4;
         s.scan_cap = scan_tmp_size(cap);
-        if (e == cudaSuccess) e = cudaMalloc(&s.near8, size_t(cap));
-        if (e == cudaSuccess) e = cudaMalloc(&s.near32, sizeof(uint32_t) * size_t(cap));
-        if (e == cudaSuccess) e = cudaMalloc(&s.near, sizeof(int32_t) * size_t(cap));
-        if (e == cudaSuccess) e = cudaMalloc(&s.scan_tmp, sizeof(uint32_t) * size_t(s.scan_cap));
-        if (e == cudaSuccess) e = cudaMalloc(&s.far, sizeof(double) * 3 * size_t(cap));
-        if (e == cudaSuccess) e = cudaMalloc(&s.fast, sizeof(double) * 3 * size_t(cap));
+        if (e == cudaSuccess) e = dev_alloc(&s.near8, size_t(cap));
+        if (e == cudaSuccess) e = dev_alloc(&s.near32, sizeof(uint32_t) * size_t(cap));
+        if (e == cudaSuccess) e = dev_alloc(&s.near, sizeof(int32_t) * size_t(cap));
+        if (e == cudaSuccess) e = dev_alloc(&s.scan_tmp, sizeof(uint32_t) * size_t(s.scan_cap));
+        if (e == cudaSuccess) e = dev_alloc(&s.far, sizeof(double) * 3 * size_t(cap));
+        if (e == cudaSuccess) e = dev_alloc(&s.fast, sizeof(double) * 3 * size_t(cap));
         if (e != cudaSuccess) return e;
         s.cap_n = cap;
     }
@@ -328,17 +328,17 @@ cudaError_t split_reserve(SplitBufs &s, int64_t n, const std::vector<int32_t> &h
         if (s.part) cudaFree(s.part);
         s.part = nullptr;
         s.cap_part = 0;
-        if ((e = cudaMalloc(&s.part, sizeof(double) * size_t(need_part + need_part / 4)))) return e;
+        if ((e = dev_alloc(&s.part, sizeof(double) * size_t(need_part + need_part / 4)))) return e;
         s.cap_part = need_part + need_part / 4;
     }
     if (nh > s.cap_holes) {
         if (s.holes) cudaFree(s.holes);
         s.holes = nullptr;
         s.cap_holes = 0;
-        if ((e = cudaMalloc(&s.holes, sizeof(int32_t) * size_t(nh)))) return e;
+        if ((e = dev_alloc(&s.holes, sizeof(int32_t) * size_t(nh)))) return e;
         s.cap_holes = nh;
     }
-    if (!s.scalars && (e = cudaMalloc(&s.scalars, 2 * sizeof(unsigned long long)))) return e;
+    if (!s.scalars && (e = dev_alloc(&s.scalars, 2 * sizeof(unsigned long long)))) return e;
     s.nholes = nh;
     return cudaSuccess;
 }

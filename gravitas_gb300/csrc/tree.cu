@@ -1445,7 +1445,7 @@ cudaError_t tree_alloc(TreeBufs &b, int64_t n, int leaf, int32_t nsys) {
     cudaError_t e = cudaSuccess;
 #define GBH_ALLOC(ptr, count)                                                     \
     do {                                                                          \
-        if (e == cudaSuccess) e = cudaMalloc(&(ptr), sizeof(*(ptr)) * size_t(count)); \
+        if (e == cudaSuccess) e = dev_alloc(&(ptr), sizeof(*(ptr)) * size_t(count)); \
     } while (0)
     GBH_ALLOC(b.flag, cn);
     GBH_ALLOC(b.bbox_part, kFlagBlocksMax * 6);

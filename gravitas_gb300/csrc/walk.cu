@@ -580,7 +580,7 @@ cudaError_t split_reserve(TreeBufs &b, int64_t n) {
     b.part_acc = nullptr;
     b.part_cap = 0;
     const int64_t cap = need + need / 4;
-    cudaError_t e = cudaMalloc(&b.part_acc, sizeof(double) * size_t(cap));
+    cudaError_t e = dev_alloc(&b.part_acc, sizeof(double) * size_t(cap));
     if (e != cudaSuccess) {
         b.part_acc = nullptr;
         return e;

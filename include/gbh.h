@@ -36,7 +36,9 @@ enum {
     GBH_OK = 0,
     GBH_ERR_ARG = 1,         /* invalid argument (null pointer, negative size, bad enum) */
     GBH_ERR_CUDA = 2,        /* a CUDA runtime call failed (message has the CUDA error) */
-    GBH_ERR_NOMEM = 3,       /* device allocation failed */
+    GBH_ERR_NOMEM = 3,       /* device allocation failed (test hook: with GBH_FAULT_ALLOC=k in the
+                                environment when a context is created, the allocation after k
+                                successful ones fails once, without touching the device) */
     GBH_ERR_LIMIT = 4,       /* a device-side walk exceeded its step bound (corrupt input?) */
     GBH_ERR_STATE = 5,       /* no resident state, or sizes do not match it */
     GBH_ERR_UNSUPPORTED = 6  /* input outside this path (e.g. alive black holes in a step) */
