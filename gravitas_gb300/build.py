@@ -77,7 +77,7 @@ def build(force: bool = False, verbose: bool = False, extra: list[str] | None = 
     with ThreadPoolExecutor(max_workers=len(UNITS)) as ex:
         objs = list(ex.map(compile_unit, UNITS.items()))
     tmp = LIB_PATH + ".tmp"
-    cmd = [cc, *ARCH, "-shared", "-o", tmp, *objs]
+    cmd = [cc, *ARCH, "-shared", "-o", tmp, *objs, "-ldl"]  # NVTX3 loads a profiler's hooks with dlopen
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"nvcc link failed:\n{r.stdout}\n{r.stderr}")

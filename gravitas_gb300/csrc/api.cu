@@ -2,6 +2,7 @@
 // of the force and step path (bh.Solver.Accelerations, Simulation.Step) over the kernels of
 // tree.cu and walk.cu.
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <algorithm>
 #include <cmath>
@@ -96,6 +97,15 @@ struct gbh_ctx {
 };
 
 namespace gbh {
+
+// NVTX range for profilers (Nsight Systems shows every C-ABI call and its build and walk stages
+// on the CPU timeline); without a profiler attached a push or pop is a no-op call.
+struct NvtxRange {
+    explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange &) = delete;
+    NvtxRange &operator=(const NvtxRange &) = delete;
+};
 
 // The allocation-failure test hook: -1 disarmed, k >= 0 fails the allocation after k more.
 static std::atomic<long long> g_alloc_fault{-1};
@@ -290,10 +300,14 @@ int forces(gbh_ctx *ctx, const gbh_params *p, int64_t n, const double *px, const
     ctx->tb.split = ctx->use_split;
     ctx->tb.walk_hint = 0;
     CK(stage_event(ctx));
-    CK(gbh::tree_build(L, ctx->tb, n, px, py, pz, mass, kind, alive, ax, ay, az, theta, leaf, p->dark_matter_off,
-                       p->walk == GBH_WALK_FP64, p->walk == GBH_WALK_PLAIN, forest ? ctx->sys_of : nullptr,
-                       forest ? ctx->sys_off : nullptr));
+    {
+        gbh::NvtxRange r("tree build");
+        CK(gbh::tree_build(L, ctx->tb, n, px, py, pz, mass, kind, alive, ax, ay, az, theta, leaf,
+                           p->dark_matter_off, p->walk == GBH_WALK_FP64, p->walk == GBH_WALK_PLAIN,
+                           forest ? ctx->sys_of : nullptr, forest ? ctx->sys_off : nullptr));
+    }
     CK(stage_event(ctx));
+    gbh::NvtxRange walk_range("walk");
     double eps2 = p->softening * p->softening;
     int quad = !p->monopole_only;
     switch (p->walk) {
@@ -788,6 +802,7 @@ int gbh_device_name(gbh_ctx *ctx, char *out, int len) {
 int gbh_accelerations(gbh_ctx *ctx, const gbh_params *p, int64_t n, const double *px, const double *py,
                       const double *pz, const double *mass, const uint8_t *kind, const uint8_t *alive, double *ax,
                       double *ay, double *az) {
+    gbh::NvtxRange nvtx_range_(__func__);
     int rc = begin(ctx);
     if (rc || (rc = check_params(ctx, p))) return rc;
     if (n < 0 || n > (int64_t(1) << 30)) return fail(ctx, GBH_ERR_ARG, "n = %lld out of range", (long long)n);
@@ -814,6 +829,7 @@ int gbh_accelerations(gbh_ctx *ctx, const gbh_params *p, int64_t n, const double
 int gbh_potential_energy(gbh_ctx *ctx, const gbh_params *p, int64_t n, const double *px, const double *py,
                          const double *pz, const double *mass, const uint8_t *kind, const uint8_t *alive, double c,
                          double *u) {
+    gbh::NvtxRange nvtx_range_(__func__);
     int rc = begin(ctx);
     if (rc || (rc = check_params(ctx, p))) return rc;
     if (!u) return fail(ctx, GBH_ERR_ARG, "u is NULL");
@@ -869,6 +885,7 @@ int gbh_potential_energy(gbh_ctx *ctx, const gbh_params *p, int64_t n, const dou
 int gbh_direct_accelerations(gbh_ctx *ctx, const gbh_params *p, int64_t n, const double *px, const double *py,
                              const double *pz, const double *mass, const uint8_t *kind, const int64_t *targets,
                              int64_t ntargets, double *ax, double *ay, double *az) {
+    gbh::NvtxRange nvtx_range_(__func__);
     int rc = begin(ctx);
     if (rc || (rc = check_params(ctx, p))) return rc;
     if (n < 0 || n > (int64_t(1) << 30)) return fail(ctx, GBH_ERR_ARG, "n out of range");
@@ -902,6 +919,7 @@ int gbh_direct_accelerations(gbh_ctx *ctx, const gbh_params *p, int64_t n, const
 int gbh_step_kdk(gbh_ctx *ctx, const gbh_params *p, double dt, int64_t nsteps, int32_t acc_valid, int64_t n,
                  double *px, double *py, double *pz, double *vx, double *vy, double *vz, double *ax, double *ay,
                  double *az, const double *mass, const uint8_t *kind, const uint8_t *alive) {
+    gbh::NvtxRange nvtx_range_(__func__);
     int rc = begin(ctx);
     if (rc || (rc = check_params(ctx, p))) return rc;
     if (nsteps < 0) return fail(ctx, GBH_ERR_ARG, "nsteps < 0");
@@ -940,6 +958,7 @@ int gbh_step_kdk(gbh_ctx *ctx, const gbh_params *p, double dt, int64_t nsteps, i
 int gbh_state_upload(gbh_ctx *ctx, int64_t n, const double *px, const double *py, const double *pz, const double *vx,
                      const double *vy, const double *vz, const double *ax, const double *ay, const double *az,
                      const double *mass, const uint8_t *kind, const uint8_t *alive) {
+    gbh::NvtxRange nvtx_range_(__func__);
     int rc = begin(ctx);
     if (rc) return rc;
     CK(cudaEventRecord(ctx->ev[0], ctx->stream));
@@ -949,6 +968,7 @@ int gbh_state_upload(gbh_ctx *ctx, int64_t n, const double *px, const double *py
 
 int gbh_state_download(gbh_ctx *ctx, double *px, double *py, double *pz, double *vx, double *vy, double *vz, double *ax,
                        double *ay, double *az) {
+    gbh::NvtxRange nvtx_range_(__func__);
     int rc = begin(ctx);
     if (rc) return rc;
     if (!ctx->have_state) return fail(ctx, GBH_ERR_STATE, "no resident state");
@@ -958,6 +978,7 @@ int gbh_state_download(gbh_ctx *ctx, double *px, double *py, double *pz, double 
 }
 
 int gbh_state_step(gbh_ctx *ctx, const gbh_params *p, double dt, int64_t nsteps) {
+    gbh::NvtxRange nvtx_range_(__func__);
     int rc = begin(ctx);
     if (rc || (rc = check_params(ctx, p))) return rc;
     if (!ctx->have_state) return fail(ctx, GBH_ERR_STATE, "no resident state (gbh_state_upload first)");
@@ -974,6 +995,7 @@ int gbh_state_step(gbh_ctx *ctx, const gbh_params *p, double dt, int64_t nsteps)
 
 int gbh_state_step_block(gbh_ctx *ctx, const gbh_params *p, double dt, double eta, int32_t levels, int64_t nsteps,
                          gbh_blockstats *stats) {
+    gbh::NvtxRange nvtx_range_(__func__);
     int rc = begin(ctx);
     if (rc || (rc = check_params(ctx, p))) return rc;
     if (!ctx->have_state) return fail(ctx, GBH_ERR_STATE, "no resident state (gbh_state_upload first)");
@@ -992,6 +1014,7 @@ int gbh_state_step_block(gbh_ctx *ctx, const gbh_params *p, double dt, double et
 }
 
 int gbh_state_accelerations(gbh_ctx *ctx, const gbh_params *p) {
+    gbh::NvtxRange nvtx_range_(__func__);
     int rc = begin(ctx);
     if (rc || (rc = check_params(ctx, p))) return rc;
     if (!ctx->have_state) return fail(ctx, GBH_ERR_STATE, "no resident state (gbh_state_upload first)");
@@ -1005,6 +1028,7 @@ int gbh_state_accelerations(gbh_ctx *ctx, const gbh_params *p) {
 }
 
 int gbh_state_diagnostics(gbh_ctx *ctx, const gbh_params *p, double c, gbh_diagnostics *out) {
+    gbh::NvtxRange nvtx_range_(__func__);
     int rc = begin(ctx);
     if (rc || (rc = check_params(ctx, p))) return rc;
     if (!ctx->have_state) return fail(ctx, GBH_ERR_STATE, "no resident state (gbh_state_upload first)");
@@ -1080,6 +1104,7 @@ int gbh_forest_upload(gbh_ctx *ctx, int32_t nsys, const int64_t *offsets, const 
                       const double *pz, const double *vx, const double *vy, const double *vz, const double *ax,
                       const double *ay, const double *az, const double *mass, const uint8_t *kind,
                       const uint8_t *alive) {
+    gbh::NvtxRange nvtx_range_(__func__);
     int rc = begin(ctx);
     if (rc) return rc;
     if (nsys < 1 || nsys > 65535) return fail(ctx, GBH_ERR_ARG, "nsys %d outside [1, 65535]", nsys);
@@ -1146,6 +1171,7 @@ int gbh_tree_size(gbh_ctx *ctx, int64_t *nstars, int64_t *nnodes) {
 }
 
 int gbh_tree_export(gbh_ctx *ctx, uint64_t *keys, int32_t *order, gbh_node *nodes, int64_t node_cap) {
+    gbh::NvtxRange nvtx_range_(__func__);
     int rc = begin(ctx);
     if (rc) return rc;
     if (!ctx->tb.info) return fail(ctx, GBH_ERR_STATE, "no tree built yet");
@@ -1168,6 +1194,7 @@ int gbh_tree_export(gbh_ctx *ctx, uint64_t *keys, int32_t *order, gbh_node *node
 int gbh_fwd_save(gbh_ctx *ctx, const gbh_adjoint_params *ap, int64_t n, const double *px, const double *py,
                  const double *pz, const double *vx, const double *vy, const double *vz, const double *mass,
                  double *out_px, double *out_py, double *out_pz, double *out_vx, double *out_vy, double *out_vz) {
+    gbh::NvtxRange nvtx_range_(__func__);
     int rc = begin(ctx);
     if (rc) return rc;
     ctx->adj.valid = false;
@@ -1202,6 +1229,7 @@ int gbh_fwd_save(gbh_ctx *ctx, const gbh_adjoint_params *ap, int64_t n, const do
 
 int gbh_bwd(gbh_ctx *ctx, const double *gx, const double *gy, const double *gz, const double *gvx, const double *gvy,
             const double *gvz, double *dx, double *dy, double *dz, double *dvx, double *dvy, double *dvz, double *dm) {
+    gbh::NvtxRange nvtx_range_(__func__);
     int rc = begin(ctx);
     if (rc) return rc;
     gbh::AdjTape &t = ctx->adj;
@@ -1228,6 +1256,7 @@ int gbh_bwd(gbh_ctx *ctx, const double *gx, const double *gy, const double *gz, 
 int gbh_autotune(gbh_ctx *ctx, const gbh_params *base, const double *thetas, int32_t nthetas, const int32_t *leaves,
                  int32_t nleaves, const int32_t *groups, int32_t ngroups, double rms_bound, int32_t sample,
                  int32_t reps, gbh_params *best, gbh_tune_entry *table, int32_t table_cap, int32_t *ntable) {
+    gbh::NvtxRange nvtx_range_(__func__);
     int rc = begin(ctx);
     if (rc || (rc = check_params(ctx, base))) return rc;
     if (!best) return fail(ctx, GBH_ERR_ARG, "best is NULL");
@@ -1387,6 +1416,7 @@ int gbh_last_timings(gbh_ctx *ctx, gbh_timings *t) {
 }
 
 int gbh_probe_fp32_peak(gbh_ctx *ctx, double ms, double *tflops) {
+    gbh::NvtxRange nvtx_range_(__func__);
     int rc = begin(ctx);
     if (rc) return rc;
     if (!tflops) return fail(ctx, GBH_ERR_ARG, "tflops is NULL");
