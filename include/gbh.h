@@ -170,13 +170,15 @@ int gbh_direct_accelerations(gbh_ctx *ctx, const gbh_params *p, int64_t n, const
                              double *ax, double *ay, double *az);
 
 /*
- * sim.Simulation.Step (sim.go:248-288) repeated nsteps times, with c = 0 and no gas
- * hydro. Without alive black holes: kick(dt/2), drift(dt) (sim.go:327-334),
+ * sim.Simulation.Step (sim.go:248-288) repeated nsteps times, without gas hydro, with
+ * the speed of light p->c (0: Newtonian). Without alive black holes: kick(dt/2),
+ * drift(dt) (sim.go:327-343: x += dt v, or dt u / gamma for c > 0),
  * Solver.Accelerations, kick(dt/2); each step replays one CUDA graph (captured on
  * first use for the sizes and parameters given, re-captured when they change) unless
  * the context was created with GBH_CFG_NO_GRAPHS; results are identical either way.
  * With alive black holes: the hole-aware split step (split.go:161-204, stepSplit):
- * forces of pairs with a hole summed directly (pair.go:26-35, Newtonian for c = 0),
+ * forces of pairs with a hole summed directly with the pair model (pair.go:14-47:
+ * Newtonian for c = 0, Paczynski-Wiita star-hole forces for c > 0),
  * stars whose timescale at a hole is below 20 dt and the holes advanced in 2^k
  * substeps (classify, split.go:41-81; k of the last step in gbh_timings.substeps),
  * star-star forces from the tree once per step; no graph (the substep count is read
