@@ -417,6 +417,7 @@ cudaError_t walk_plain(const Launch &L, const TreeBufs &b, int64_t nstars_cap, f
 // neighbouring warps keep walking neighbouring groups). One block of kLptThreads threads, each
 // owning a contiguous run of groups.
 constexpr int kLptThreads = 512, kLptBuckets = 16;  // 32 KB of shared counts
+static_assert(kLptThreads / 32 == kLptBuckets, "the warp totals reuse the bucket array");
 __global__ __launch_bounds__(kLptThreads) void k_lpt_order(const DevInfo *info, int gsize, bool forest,
                                                            const uint32_t *gcost, int32_t *gperm, int32_t perm_cap) {
     __shared__ uint32_t cnt[kLptBuckets][kLptThreads];
@@ -433,28 +434,46 @@ __global__ __launch_bounds__(kLptThreads) void k_lpt_order(const DevInfo *info, 
     for (int k = 0; k < kLptBuckets; ++k) cnt[k][t] = 0;
     for (int32_t g = g0; g < g1; ++g) ++cnt[bucket(gcost[g])][t];
     __syncthreads();
-    if (t < kLptBuckets) {  // exclusive scan of each bucket's row over the threads
-        uint32_t run = 0;
-        for (int q = 0; q < kLptThreads; ++q) {
-            uint32_t c = cnt[t][q];
-            cnt[t][q] = run;
-            run += c;
+    // Exclusive scan of the counts in bucket-major order, kItems consecutive entries per thread:
+    // entry (k, q) becomes the position of thread q's first group of bucket k in the order.
+    constexpr int kItems = kLptBuckets * kLptThreads / kLptThreads;
+    uint32_t *flat = &cnt[0][0];
+    uint32_t v[kItems], sum = 0;
+#pragma unroll
+    for (int i = 0; i < kItems; ++i) {
+        v[i] = flat[t * kItems + i];
+        sum += v[i];
+    }
+    const int lane = t & 31, warp = t >> 5;
+    uint32_t incl = sum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(kFull, incl, o);
+        if (lane >= o) incl += y;
+    }
+    if (lane == 31) base[warp] = incl;  // warp totals (kLptThreads / 32 == kLptBuckets of them)
+    __syncthreads();
+    if (warp == 0) {
+        const uint32_t w = lane < kLptThreads / 32 ? base[lane] : 0;
+        uint32_t wi = w;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(kFull, wi, o);
+            if (lane >= o) wi += y;
         }
-        base[t] = run;
+        if (lane < kLptThreads / 32) base[lane] = wi - w;
     }
     __syncthreads();
-    if (t == 0) {  // bucket totals to bucket offsets
-        uint32_t run = 0;
-        for (int k = 0; k < kLptBuckets; ++k) {
-            uint32_t c = base[k];
-            base[k] = run;
-            run += c;
-        }
+    uint32_t run = base[warp] + incl - sum;
+#pragma unroll
+    for (int i = 0; i < kItems; ++i) {
+        flat[t * kItems + i] = run;
+        run += v[i];
     }
     __syncthreads();
     for (int32_t g = g0; g < g1; ++g) {
         int k = bucket(gcost[g]);
-        gperm[base[k] + cnt[k][t]++] = g;
+        gperm[cnt[k][t]++] = g;
     }
     __syncthreads();
     if (t == 0) gperm[perm_cap] = ng;
