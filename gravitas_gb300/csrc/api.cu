@@ -232,7 +232,7 @@ int begin(gbh_ctx *ctx) {
 
 Launch launch_of(gbh_ctx *ctx) { return Launch{ctx->stream, &ctx->launches, ctx->num_sms}; }
 
-// Waits for the context's stream: a spin in the driver by default, a sleep on a blocking-sync
+// Waits for the context's stream: a spin in the CUDA driver by default, a sleep on a blocking-sync
 // event with GBH_CFG_BLOCKING_SYNC (the waiting thread then leaves its core to other work).
 cudaError_t wait_stream(gbh_ctx *ctx) {
     if (!ctx->wait_ev) return cudaStreamSynchronize(ctx->stream);
@@ -241,7 +241,7 @@ cudaError_t wait_stream(gbh_ctx *ctx) {
 }
 
 // Before launching step s: with GBH_CFG_BLOCKING_SYNC, sleep until step s - 4 has finished, so
-// that the driver's launch queue never fills (a full queue makes the launching thread spin).
+// that the CUDA driver's launch queue never fills (a full queue makes the launching thread spin).
 cudaError_t throttle_before(gbh_ctx *ctx, int64_t s) {
     if (!ctx->wait_ev || s < 4) return cudaSuccess;
     return cudaEventSynchronize(ctx->ahead[s % 4]);
