@@ -33,7 +33,7 @@ constexpr int kEwThreads = 256;
 
 inline unsigned ew_blocks(int64_t n) { return unsigned(std::max<int64_t>(1, (n + kEwThreads - 1) / kEwThreads)); }
 
-// ---- FP64 pair kernels (the checker's loops, j ascending) ----
+// ---- FP64 pair kernels (the oracle's loop order, j ascending) ----
 
 __global__ void __launch_bounds__(kPairThreads) k_force64(int64_t n, const double *__restrict__ px,
                                                           const double *__restrict__ py,

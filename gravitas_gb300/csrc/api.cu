@@ -251,7 +251,7 @@ cudaError_t throttle_after(gbh_ctx *ctx, int64_t s) {
     return ctx->wait_ev ? cudaEventRecord(ctx->ahead[s % 4], ctx->stream) : cudaSuccess;
 }
 
-// Takes the next stage event of the call from the pool (creating it if needed).
+// Takes the next stage event of the call from the context's event pool (creating it if needed).
 cudaError_t next_stage_event(gbh_ctx *ctx, cudaEvent_t *ev) {
     if (ctx->evused == ctx->evpool.size()) {
         cudaEvent_t e;

@@ -170,7 +170,7 @@ void orc_split_kdk(int64_t n, double *px, double *py, double *pz, double *vx, do
  * positions, velocities and masses, given its gradient (gx.., gv..) with respect to the final
  * positions and velocities after nsteps steps of dt from the state (x0, v0). FP64. The forward
  * trajectory is replayed from checkpoints every `every` steps. No counterpart in the
- * reference: the checker of gbh_adjoint_*.
+ * reference: the oracle of gbh_fwd_save / gbh_bwd.
  */
 void orc_adjoint_direct(int64_t n, const double *px, const double *py, const double *pz,
                         const double *vx, const double *vy, const double *vz, const double *mass,

@@ -1,7 +1,7 @@
-"""GPU parity tests at the sizes of the reference workloads the benchmark configurations name:
-C1 (Plummer 16,384, 100 KDK steps), C2 (disk + bulge + NFW-halo galaxy of 131,072 bodies with
-6-rung block steps), C5 (the 1,048,576-body merger at theta 0.3, 0.5 and 0.8). C3 (forest) and
-C4 (adjoint) have their own files."""
+"""GPU parity tests at the sizes of the measured workloads: the Plummer sphere of 16,384 bodies
+(100 KDK steps), the disk + bulge + NFW-halo galaxy of 131,072 bodies (6-rung block steps) and
+the 1,048,576-body merger (theta 0.3, 0.5 and 0.8). The forest and the adjoint workloads have
+their own files."""
 import numpy as np
 import pytest
 
@@ -45,8 +45,8 @@ def accelerations(ctx, s, par):
     return np.stack(a, 1)
 
 
-def test_c1_plummer_100_steps_fp64_bit_exact(ctx):
-    """Config 1: equal-mass Plummer N = 16,384 (float32 positions and velocities), eps 0.01,
+def test_plummer_16k_100_steps_fp64_bit_exact(ctx):
+    """The equal-mass Plummer N = 16,384 (float32 positions and velocities), eps 0.01,
     theta 0.5, leaf 8, 100 KDK steps of 1e-3: the FP64 walk's trajectory equals the oracle's."""
     s = ics.plummer(16384, seed=0)
     n = len(s["px"])
@@ -59,8 +59,8 @@ def test_c1_plummer_100_steps_fp64_bit_exact(ctx):
         assert np.array_equal(got[k], ref[k]), k
 
 
-def test_c1_fp32_walks_against_reference_tree_and_direct_sum(ctx):
-    """Config 1 forces: the plain walk against the reference CPU tree (gpu_test.go:8-21
+def test_plummer_16k_fp32_walks_against_reference_tree_and_direct_sum(ctx):
+    """Forces of the 16,384-body Plummer sphere: the plain walk against the reference CPU tree (gpu_test.go:8-21
     tolerances), the mixed walk against the FP64 direct sum at equal or better RMS and p99
     error than the reference per-star walk."""
     s = ics.plummer(16384, seed=0)
@@ -76,8 +76,8 @@ def test_c1_fp32_walks_against_reference_tree_and_direct_sum(ctx):
     assert r_mix <= 1.001 * r_tree and p_mix <= 1.001 * p_tree and r_mix <= 2e-3
 
 
-def test_c2_galaxy_block_steps(ctx):
-    """Config 2: the 131,072-body galaxy (40 % disk, 10 % bulge, 50 % NFW dark halo at 4x the
+def test_galaxy_131k_block_steps(ctx):
+    """The 131,072-body galaxy (40 % disk, 10 % bulge, 50 % NFW dark halo at 4x the
     disk particle mass), eps 0.02, theta 0.5, 6 rungs, eta 0.025. Block steps conserve energy
     as well as global steps at the finest rung, with far fewer star walks."""
     g = ics.galaxy(131072, seed=0)
@@ -96,7 +96,7 @@ def test_c2_galaxy_block_steps(ctx):
     assert d_block <= max(5 * d_fine, 2e-5), (d_block, d_fine)
 
 
-def test_c2_galaxy_block_steps_fp64_bit_exact_with_oracle(ctx):
+def test_galaxy_block_steps_fp64_bit_exact_with_oracle(ctx):
     """The same scheme on a smaller galaxy (dark matter included) through the FP64 walk equals
     the oracle's restatement: trajectories, event count and walked stars."""
     g = ics.galaxy(8192, seed=1)
@@ -111,8 +111,8 @@ def test_c2_galaxy_block_steps_fp64_bit_exact_with_oracle(ctx):
         assert np.array_equal(got[k], ref[k]), k
 
 
-def test_c5_merger_1m_theta_sweep(ctx):
-    """Config 5: the 1,048,576-body merger at theta 0.3, 0.5 and 0.8. On 4,096 seeded stars the
+def test_merger_1m_theta_sweep(ctx):
+    """The 1,048,576-body merger at theta 0.3, 0.5 and 0.8. On 4,096 seeded stars the
     mixed walk's RMS force error against the FP64 direct sum is at most the plain per-star
     walk's, and within 2e-3 up to theta 0.5; one 6-rung block step keeps energy to 1e-5."""
     s = ics.merger(1 << 20, seed=0)

@@ -1,4 +1,4 @@
-"""CPU tests pinning the oracle (the checker) to the reference's own tests.
+"""CPU tests pinning the oracle to the reference's own tests.
 
 The reference (Go) cannot run here and stores no golden vectors for this path; its tests are a
 known-answer test and relations. Each test below restates one of them against the C++ oracle
