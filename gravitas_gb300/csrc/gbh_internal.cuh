@@ -176,9 +176,11 @@ inline cudaError_t dev_alloc(T **p, size_t bytes) {
 void arm_alloc_fault(long long after);  // after < 0 disarms
 
 // Parts per group of a split mixed walk over n stars in groups of gsize (1: no split, at most
-// 16), from the number of groups per SM.
-constexpr int kMaxWalkParts = 16;
+// 32), from the number of groups per SM.
+constexpr int kMaxWalkParts = 32;
 int walk_parts(int64_t n, int gsize);
+// The most parts a walk sized for n bodies may take (its part_acc budget; 1: never split).
+int walk_parts_budget(int64_t n);
 // Grows part_acc for a split walk over the n bodies of a call (no allocation when it already
 // fits). The parts depend on n alone, never on the buffers' capacity, so the same inputs give
 // the same bits in any context.

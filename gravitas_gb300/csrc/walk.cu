@@ -510,7 +510,9 @@ static cudaError_t launch_mixed_t(const Launch &L, const TreeBufs &b, int64_t ns
     if constexpr (!kPot) {  // few groups: split each group's walk over several warps
         // a target list walks about walk_hint stars (the previous event's count): part by that
         const int64_t walked = targets && b.walk_hint > 0 && b.walk_hint < nstars_cap ? b.walk_hint : nstars_cap;
-        const int parts = (!forest && b.split) ? walk_parts(walked, gsize) : 1;
+        int parts = (!forest && b.split) ? walk_parts(walked, gsize) : 1;
+        const int budget = walk_parts_budget(nstars_cap);  // a function of n alone, never of capacity
+        if (parts > budget) parts = budget;
         if (parts > 1 && b.part_acc && int64_t(parts) * 3 * nstars_cap <= b.part_cap) {
             const int64_t warps = groups * parts;
             const int64_t wblocks = (warps + kMixedThreads / 32 - 1) / (kMixedThreads / 32);
@@ -575,12 +577,14 @@ int walk_parts(int64_t n, int gsize) {
     if (cudaGetDevice(&dev) != cudaSuccess ||
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms < 1)
         sms = 152;
-    // Measured on the galaxy model at 16k-512k bodies (leaf 32): each part re-tests the nodes
+    // Measured on the galaxy model at 8k-512k bodies (leaf 32): each part re-tests the nodes
     // above its range and skips the subtrees beside it, so splitting pays only while the unsplit
-    // walk leaves most of the GPU idle. Best part counts by groups per SM: up to 5 -> 16 (5.4x at
-    // 16k bodies), up to 7 -> 8 (1.9x at 64k), up to 14 -> 4 (1.09x at 128k), up to 21 -> 2
-    // (1.15x at 192k), more -> no split (2 parts were 1.2x slower at 256k).
+    // walk leaves most of the GPU idle. Best part counts by groups per SM: up to 2.5 -> 32 (1.2x
+    // over 16 parts at 16k bodies), up to 5 -> 16 (5x over no split at 16k), up to 7 -> 8 (1.9x
+    // at 64k), up to 14 -> 4 (1.09x at 128k), up to 21 -> 2 (1.15x at 192k), more -> no split
+    // (2 parts were 1.2x slower at 256k).
     const int64_t groups = (n + gsize - 1) / gsize;
+    if (2 * groups <= 5 * int64_t(sms)) return 32;
     if (groups <= 5 * int64_t(sms)) return 16;
     if (groups <= 7 * int64_t(sms)) return 8;
     if (groups <= 14 * int64_t(sms)) return 4;
@@ -588,11 +592,16 @@ int walk_parts(int64_t n, int gsize) {
     return 1;
 }
 
+int walk_parts_budget(int64_t n) {
+    // whenever a walk over these n bodies may split: 16 parts (a target list may walk few enough
+    // groups for more parts than all n would take), or 32 where n itself takes 32
+    const int np = walk_parts(n, 64);
+    return np <= 1 ? 1 : (np > 16 ? np : 16);
+}
+
 cudaError_t split_reserve(TreeBufs &b, int64_t n) {
-    // room for the most parts whenever a walk over these n bodies may split (a target list may
-    // walk few enough groups for the most parts even where all n would take fewer)
-    if (walk_parts(n, 64) <= 1) return cudaSuccess;
-    const int parts = kMaxWalkParts;
+    const int parts = walk_parts_budget(n);
+    if (parts <= 1) return cudaSuccess;
     const int64_t need = int64_t(parts) * 3 * n;
     if (need <= b.part_cap) return cudaSuccess;
     if (b.part_acc) cudaFree(b.part_acc);

@@ -90,7 +90,7 @@ enum {
     GBH_CFG_NO_LPT = 4,
     /* The mixed walk of a single system never splits a group's walk over several warps. With few
        groups (up to 21 per SM: below about 200,000 stars on a GB300) each group's walk is
-       otherwise shared by 2 to 16 warps, each adding the interactions of its own range of source
+       otherwise shared by 2 to 32 warps, each adding the interactions of its own range of source
        stars, and the parts are summed in order: the same interactions, a different order of
        summation. */
     GBH_CFG_NO_SPLIT = 8
