@@ -697,3 +697,30 @@ def test_resident_calls_need_a_state():
         assert ei.value.code == abi.ERR_STATE
     finally:
         c.close()
+
+
+def test_results_do_not_depend_on_a_contexts_history():
+    """Buffers only grow, so a context that held a larger state keeps larger buffers; the walk's
+    launch shape (split parts, group order) is a function of the inputs alone, so block steps and
+    forces of the same state are bit-identical in a fresh context and in one that held 200,000
+    bodies before."""
+    small = ics.galaxy(60000, seed=6)
+    big = ics.galaxy(200000, seed=7)
+    par = abi.make_params(0.5, 0.02, 16, False, False, "mixed")
+    out = []
+    for history in (None, big):
+        c = abi.Context(0)
+        try:
+            if history is not None:
+                upload_state(c, history)
+                c.step_block(par, 1.6e-2, 0.025, 6, 1)
+            upload_state(c, small)
+            c.step_block(par, 1.6e-2, 0.025, 6, 2)
+            st = download_state(c, len(small["px"]))
+            c.call("gbh_state_accelerations", par)
+            st["forces"] = download_state(c, len(small["px"]))["ax"]
+            out.append(st)
+        finally:
+            c.close()
+    for k in out[0]:
+        assert np.array_equal(out[0][k], out[1][k]), k
