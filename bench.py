@@ -53,7 +53,7 @@ THETA, EPS, DT = 0.5, 0.02, 1e-3
 WALK_TRAFFIC_BYTES = {24: 90_435_328, 32: 86_668_288}
 TUNE_LEAVES = [8, 12, 16, 24, 32]
 RMS_BOUND = 2e-3
-REFERENCE_LEAF = 24  # bh.go:67-68, the reference solver's default leaf size
+REFERENCE_LEAF = 24  # bh.go:17-19, the reference solver's default leaf size
 FIELDS = ("px", "py", "pz", "vx", "vy", "vz", "ax", "ay", "az")
 
 
@@ -182,7 +182,7 @@ def run_reference(args):
         "steps": k, "warmup": 1, "ms_per_step": el / k * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": workload_name(n, leaf), "requested_steps": args.steps,
-                   "leaf_size": leaf, "tuning": "the reference solver's default leaf size (bh.go:67-68)"},
+                   "leaf_size": leaf, "tuning": "the reference solver's default leaf size (bh.go:17-19)"},
         "cpu_baseline": {"value": value, "unit": "particle-steps/s", "cores": cores, "kind": "port",
                          "sample": f"{k} full KDK steps of the {n}-particle workload (C++ restatement of the "
                                    f"reference CPU Barnes-Hut, FP64, {cores} threads; Go is not available)"},

@@ -215,8 +215,8 @@ int check_params(gbh_ctx *ctx, const gbh_params *p) {
     return GBH_OK;
 }
 
-double theta_of(const gbh_params *p) { return p->theta == 0 ? 0.9 : p->theta; }  // bh.go:118-123
-int leaf_of(const gbh_params *p) { return p->leaf_size > 0 ? p->leaf_size : 24; }  // bh.go:67-68
+double theta_of(const gbh_params *p) { return p->theta == 0 ? 0.9 : p->theta; }  // bh.go:69-74
+int leaf_of(const gbh_params *p) { return p->leaf_size > 0 ? p->leaf_size : 24; }  // bh.go:17-19
 
 int begin(gbh_ctx *ctx) {
     if (!ctx) return GBH_ERR_ARG;
@@ -448,7 +448,7 @@ int capture_step(gbh_ctx *ctx, const gbh_params *p, double dt, const uint8_t *ki
 }
 
 // Steps on the resident state (sim.go:252-288, no holes, no hydro).
-// The hole-aware step (split.go:161-204, stepSplit) without gas, instant gravity and no spins:
+// The hole-aware step (split.go:162-200, stepSplit) without gas, instant gravity and no spins:
 // forces of pairs with a hole summed directly (Paczynski-Wiita star-hole pairs for c > 0), near
 // stars and holes in power-of-two substeps, star-star forces from the tree once per step. The substep count of the last step goes to ctx->last_substeps.
 int run_split_steps(gbh_ctx *ctx, const gbh_params *p, double dt, int64_t nsteps) {
@@ -474,7 +474,7 @@ int run_split_steps(gbh_ctx *ctx, const gbh_params *p, double dt, int64_t nsteps
     }
     unsigned long long sc[2];
     for (int64_t step = 0; step < nsteps; ++step) {
-        // classify (split.go:41-81): the host needs the substep count
+        // classify (split.go:39-85): the host needs the substep count
         CK(gbh::split_classify(L, sb, n, px, py, pz, ctx->mass, kind, eps2, c, 20.0 * dt));
         CK(cudaMemcpyAsync(sc, sb.scalars, sizeof sc, cudaMemcpyDeviceToHost, ctx->stream));
         CK(wait_stream(ctx));
@@ -815,7 +815,7 @@ int gbh_accelerations(gbh_ctx *ctx, const gbh_params *p, int64_t n, const double
     if ((rc = h2d(ctx, ctx->px, px, b)) || (rc = h2d(ctx, ctx->py, py, b)) || (rc = h2d(ctx, ctx->pz, pz, b)) ||
         (rc = h2d(ctx, ctx->mass, mass, b)))
         return rc;
-    // Dead bodies keep their entries (bh.go:141-150 writes only stars and holes).
+    // Dead bodies keep their entries (bh.go:92-101 writes only stars and holes).
     if ((rc = h2d(ctx, ctx->ax, ax, b)) || (rc = h2d(ctx, ctx->ay, ay, b)) || (rc = h2d(ctx, ctx->az, az, b))) return rc;
     if (kind && (rc = h2d(ctx, ctx->kind, kind, size_t(n)))) return rc;
     if (alive && (rc = h2d(ctx, ctx->alive, alive, size_t(n)))) return rc;

@@ -216,7 +216,7 @@ cudaError_t potential_mixed(const Launch &L, const TreeBufs &b, int64_t n, const
                             const double *pz, const double *mass, const uint8_t *kind, const uint8_t *alive,
                             const int32_t *holes, int32_t nholes, double eps2, double c, int dm_off, int quad,
                             double *psi, double *part, double *u_dev);
-// Exact pair potential of all bodies (PotentialEnergyParallel, diag.go:42-62): rows (n doubles of
+// Exact pair potential of all bodies (PotentialEnergyParallel, diag.go:42-64): rows (n doubles of
 // scratch) in ascending i, each over j > i ascending; result in *u_dev.
 constexpr int64_t kExactEnergyLimit = 30000;  // exactEnergyLimit, diag.go:16-19
 cudaError_t potential_exact_fp64(const Launch &L, int64_t n, const double *px, const double *py, const double *pz,

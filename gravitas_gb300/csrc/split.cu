@@ -81,7 +81,7 @@ __device__ __forceinline__ double source_mass(int64_t i, const double *mass, con
     return dm_off && kind[i] == GBH_DARK_MATTER ? 0.0 : mass[i];  // Params.SourceMass, sim.go:93-98
 }
 
-// classify (split.go:41-81): near flags (byte and u32 for the scan) and the minimum timescale
+// classify (split.go:39-85): near flags (byte and u32 for the scan) and the minimum timescale
 // (as the bits of a positive double, ordered like the value) over near stars and hole pairs.
 __global__ void k_classify(int64_t n, const double *__restrict__ px, const double *__restrict__ py,
                            const double *__restrict__ pz, const double *__restrict__ mass,

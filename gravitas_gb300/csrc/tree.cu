@@ -226,7 +226,7 @@ __device__ __forceinline__ void block_minmax(long long mn[3], long long mx[3], d
     }
 }
 
-// Star flags, per-block bbox partials; alive holes get zero acceleration (bh.go:148-150).
+// Star flags, per-block bbox partials; alive holes get zero acceleration (bh.go:99-101).
 __global__ __launch_bounds__(kThreads) void k_flags_bbox(int64_t n, const double *__restrict__ px,
                                                          const double *__restrict__ py, const double *__restrict__ pz,
                                                          const uint8_t *__restrict__ kind,
@@ -688,7 +688,7 @@ __global__ __launch_bounds__(kThreads) void k_ref_index(const DevInfo *info, con
     }
 }
 
-// Links and ranges of every node in the reference layout (bh.go:108-116).
+// Links and ranges of every node in the reference layout (bh.go:59-67).
 __global__ __launch_bounds__(kThreads) void k_emit_nodes(const uint64_t *__restrict__ keys, DevInfo *info,
                                                          const uint32_t *__restrict__ cnt,
                                                          const uint32_t *__restrict__ base,
@@ -905,7 +905,7 @@ __global__ __launch_bounds__(kThreads) void k_upsweep(const uint64_t *__restrict
     }
 }
 
-// ---------------------------------------------------------------- FP64 walk (bh.go:155-204)
+// ---------------------------------------------------------------- FP64 walk (bh.go:106-155)
 
 __global__ __launch_bounds__(kThreads) void k_walk_fp64(const DevInfo *info, const gbh_node *__restrict__ nodes,
                                                         const double *__restrict__ sx, const double *__restrict__ sy,
@@ -1072,7 +1072,7 @@ __device__ __forceinline__ double pair_potential(double mi, double mj, double r2
     return mi * mj * (-2 / rs + 4 / (rs * rs) * (re - 1.5 * rs));
 }
 
-// PotentialEnergyParallel (diag.go:42-62): row i of the exact pair sum, sum over j > i of the
+// PotentialEnergyParallel (diag.go:42-64): row i of the exact pair sum, sum over j > i of the
 // pair model's potential in ascending j, kinds and liveness as the reference reads them (all
 // bodies). The rows are then added in ascending i (the reference adds its ParallelFor chunks
 // in completion order, so only round-off may differ).
@@ -1872,7 +1872,7 @@ namespace {
 constexpr int kDiagSums = 11;  // kinetic, p(3), L(3), m x (3), m
 
 // Per-block sums over bodies i (all bodies, as Momentum/AngularMomentum/CenterOfMass iterate
-// s.Len(); kinetic over the bodies that gravitate, sourceKinetic diag.go:80-88).
+// s.Len(); kinetic over the bodies that gravitate, sourceKinetic diag.go:66-76).
 __global__ __launch_bounds__(kThreads) void k_diag_partial(int64_t n, const double *__restrict__ px,
                                                            const double *__restrict__ py, const double *__restrict__ pz,
                                                            const double *__restrict__ vx, const double *__restrict__ vy,

@@ -4,7 +4,7 @@
 //   internal/sim/bh/gpu_darwin.go:76-118 (all FP32, uncompensated, per-star opening).
 // walk_mixed: one warp per group of 64 consecutive Morton-sorted stars (two per lane, packed
 //   FP32x2 arithmetic) walking the skip-pointer tree in lockstep. A node is opened when any star of the group would open it under the
-//   reference criterion d2 < crit2 (bh.go:165), so every star sees each accepted node exactly
+//   reference criterion d2 < crit2 (bh.go:116), so every star sees each accepted node exactly
 //   where the reference would accept it or deeper. Positions are FP64 split into hi + lo FP32
 //   parts; a separation is formed from hi differences, exact for nearby points (Sterbenz) and
 //   relatively small for distant ones, plus the lo parts, so separations stay accurate however
@@ -309,7 +309,7 @@ __global__ __launch_bounds__(kMixedThreads, kShared ? 9 : 8) void k_walk_mixed2(
                     const float2 ez = add2(lz, f2(so.z));
                     const float2 r2 = fma2(ez, ez, fma2(ey, ey, fma2(ex, ex, e2)));
                     // A star paired with itself gives a separation of exactly 0: with eps2 > 0 that adds
-                    // 0, as skipping j == self does (bh.go:191-193). Without softening r2 = 0 is masked.
+                    // 0, as skipping j == self does (bh.go:142-144). Without softening r2 = 0 is masked.
                     float2 ir;
                     if (kSoft) {
                         ir = make_float2(rsqrtf(r2.x), rsqrtf(r2.y));

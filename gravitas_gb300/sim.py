@@ -2,7 +2,7 @@
 
 Names follow the reference: State is sim.State (internal/sim/state.go:33-52) as SoA numpy
 arrays, Params the fields of sim.Params the path reads (sim.go:9-23), Solver is bh.Solver
-(internal/sim/bh/bh.go:77-151, potential.go:12-42), DirectSolver is direct.Solver
+(internal/sim/bh/bh.go:28-102, potential.go:12-42), DirectSolver is direct.Solver
 (internal/sim/direct/direct.go:14-48) and Simulation.step is Simulation.Step (sim.go:248-288)
 for states without black holes or hydro. Every computation runs in libgbh.so on the GPU.
 """
@@ -14,9 +14,9 @@ import numpy as np
 
 from . import abi
 
-DEFAULT_THETA = 0.9   # bh.go:63-66
-LEAF_SIZE = 24        # bh.go:67-68
-DIAG_THETA = 0.9      # bh.go:69-72
+DEFAULT_THETA = 0.9   # bh.go:14-16
+LEAF_SIZE = 24        # bh.go:17-19
+DIAG_THETA = 0.9      # bh.go:20-23
 
 _F = ("pos_x", "pos_y", "pos_z", "vel_x", "vel_y", "vel_z", "acc_x", "acc_y", "acc_z", "mass")
 
@@ -89,7 +89,7 @@ class Solver:
                                self.walk, c=p.c)
 
     def accelerations(self, s: State, p: Params) -> None:
-        """Fills s.acc_* (bh.go:125-151): holes get 0, dead bodies keep their entries."""
+        """Fills s.acc_* (bh.go:76-102): holes get 0, dead bodies keep their entries."""
         P = abi.ptr
         self.ctx.call("gbh_accelerations", self.params(p), len(s), P(s.pos_x), P(s.pos_y), P(s.pos_z), P(s.mass),
                       P(s.kind), P(s.alive), P(s.acc_x), P(s.acc_y), P(s.acc_z))

@@ -5,7 +5,7 @@
  * reference binds its force solver through the Go interface
  *     type Solver interface { Accelerations(s *State, p Params) }
  * (internal/sim/sim.go:100-105), implemented by bh.Solver
- * (internal/sim/bh/bh.go:77-151), and reaches native code through cgo static C
+ * (internal/sim/bh/bh.go:28-102), and reaches native code through cgo static C
  * functions (internal/sim/bh/gpu_darwin.go:18-62: gpu_init / gpu_buffer /
  * gpu_walk, synchronous, 0-or-error-code returns with a message buffer). The
  * entry points below replace those; each cites the reference interface it
@@ -58,17 +58,17 @@ enum {
        kernel internal/sim/bh/gpu_darwin.go:76-118. */
     GBH_WALK_PLAIN = 1,
     /* One thread per star in FP64 with the reference's operation order: bit
-       identical to bh.Solver.walk (internal/sim/bh/bh.go:155-204). */
+       identical to bh.Solver.walk (internal/sim/bh/bh.go:106-155). */
     GBH_WALK_FP64 = 2
 };
 
-/* Solver knobs: bh.Solver{Theta, MonopoleOnly} (bh.go:77-87) and the
+/* Solver knobs: bh.Solver{Theta, MonopoleOnly} (bh.go:29-38) and the
    sim.Params fields the force path reads (sim.go:9-23). */
 typedef struct {
-    double theta;            /* opening angle; 0 means 0.9 (bh.go:63-66, 118-123) */
+    double theta;            /* opening angle; 0 means 0.9 (bh.go:14-16, 69-74) */
     double softening;        /* Plummer softening length eps (Params.Softening) */
-    int32_t leaf_size;       /* max stars per leaf; 0 means 24 (bh.go:67-68) */
-    int32_t monopole_only;   /* drop quadrupoles of accepted nodes (bh.go:82-83) */
+    int32_t leaf_size;       /* max stars per leaf; 0 means 24 (bh.go:17-19) */
+    int32_t monopole_only;   /* drop quadrupoles of accepted nodes (bh.go:34-35) */
     int32_t dark_matter_off; /* dark matter pulls nothing (Params.DarkMatterOff, sim.go:92-98) */
     int32_t walk;            /* GBH_WALK_* */
     int32_t group_size;      /* stars per warp of GBH_WALK_MIXED: 64 (0 means 64) or 32 */
@@ -102,7 +102,7 @@ typedef struct {
     int32_t reserved[6];     /* zero */
 } gbh_config;
 
-/* One tree node, field for field internal/sim/bh/bh.go:108-116 (104 bytes). */
+/* One tree node, field for field internal/sim/bh/bh.go:59-67 (104 bytes). */
 typedef struct {
     double x, y, z, m;
     double qxx, qyy, qzz, qxy, qxz, qyz;
@@ -122,7 +122,7 @@ typedef struct {
     int64_t launches;  /* kernels launched by the last call */
     int64_t h2d_bytes; /* host-to-device bytes copied by the last call */
     int64_t d2h_bytes; /* device-to-host bytes copied by the last call */
-    int64_t substeps;  /* hole substeps of the last step (Simulation.Substeps, split.go:168); 1 without holes */
+    int64_t substeps;  /* hole substeps of the last step (Simulation.Substeps, split.go:174); 1 without holes */
 } gbh_timings;
 
 typedef struct gbh_ctx gbh_ctx;
@@ -139,7 +139,7 @@ const char *gbh_last_error(const gbh_ctx *ctx);
 int gbh_device_name(gbh_ctx *ctx, char *out, int len);
 
 /*
- * bh.Solver.Accelerations (bh.go:125-151) on host arrays of one sim.State
+ * bh.Solver.Accelerations (bh.go:76-102) on host arrays of one sim.State
  * (state.go:33-52): fills ax/ay/az for every alive non-hole body from the
  * star–star forces, sets alive black holes to 0 and leaves dead bodies'
  * entries untouched. kind and alive may be NULL (all stars, all alive).
@@ -176,11 +176,11 @@ int gbh_direct_accelerations(gbh_ctx *ctx, const gbh_params *p, int64_t n, const
  * Solver.Accelerations, kick(dt/2); each step replays one CUDA graph (captured on
  * first use for the sizes and parameters given, re-captured when they change) unless
  * the context was created with GBH_CFG_NO_GRAPHS; results are identical either way.
- * With alive black holes: the hole-aware split step (split.go:161-204, stepSplit):
+ * With alive black holes: the hole-aware split step (split.go:162-200, stepSplit):
  * forces of pairs with a hole summed directly with the pair model (pair.go:14-47:
  * Newtonian for c = 0, Paczynski-Wiita star-hole forces for c > 0),
  * stars whose timescale at a hole is below 20 dt and the holes advanced in 2^k
- * substeps (classify, split.go:41-81; k of the last step in gbh_timings.substeps),
+ * substeps (classify, split.go:39-85; k of the last step in gbh_timings.substeps),
  * star-star forces from the tree once per step; no graph (the substep count is read
  * back every step). If acc_valid is 0 the forces are computed first (initForces,
  * gas.go:14-17). Arrays are read and written in place; the state stays on the device
@@ -229,17 +229,17 @@ int gbh_state_step_block(gbh_ctx *ctx, const gbh_params *p, double dt, double et
 /* Accelerations of the resident state (as gbh_accelerations, no copies). */
 int gbh_state_accelerations(gbh_ctx *ctx, const gbh_params *p);
 
-/* Conserved quantities of the resident state (internal/sim/diag.go:31-120), FP64 on the
+/* Conserved quantities of the resident state (internal/sim/diag.go:31-135), FP64 on the
    GPU. */
 typedef struct {
-    double kinetic;             /* sourceKinetic: sum of m u^2 / (gamma + 1) over bodies that gravitate (diag.go:80-88) */
+    double kinetic;             /* sourceKinetic: sum of m u^2 / (gamma + 1) over bodies that gravitate (diag.go:66-76) */
     double potential;           /* exact pair sum for up to 30,000 bodies (PotentialEnergyParallel,
-                                   diag.go:42-62), else the tree potential at min(theta, 0.9)
+                                   diag.go:42-64), else the tree potential at min(theta, 0.9)
                                    (potential.go:12-42); forests always use the tree */
-    double total;               /* kinetic + potential (TotalEnergy without gas, diag.go:43-51) */
-    double momentum[3];         /* Momentum, all bodies (diag.go:89-96) */
-    double angular_momentum[3]; /* AngularMomentum about the origin (diag.go:98-105) */
-    double center_of_mass[3];   /* CenterOfMass (diag.go:107-120) */
+    double total;               /* kinetic + potential (TotalEnergy without gas, diag.go:31-40) */
+    double momentum[3];         /* Momentum, all bodies (diag.go:102-110) */
+    double angular_momentum[3]; /* AngularMomentum about the origin (diag.go:112-120) */
+    double center_of_mass[3];   /* CenterOfMass (diag.go:122-135) */
     double mass;                /* its total mass */
     int32_t quality;            /* EnergyQuality (diag.go:21-27): 2 exact, 1 tree estimate */
     int32_t reserved;

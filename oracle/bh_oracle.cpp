@@ -456,7 +456,7 @@ struct orc_tree {
         build_node(nodes, 0, 0, int32_t(ns), 0, mnX + half, mnY + half, mnZ + half, half, -1);
     }
 
-    // walk bh.go:155-204 (FP64), with optional interaction counts.
+    // walk bh.go:106-155 (FP64), with optional interaction counts.
     template <bool kCount>
     void walk(double x, double y, double z, int32_t self, double eps2, bool quad, double &oax,
               double &oay, double &oaz, int64_t *cnt) const {
@@ -607,7 +607,7 @@ void orc_tree_free(orc_tree *t) { delete t; }
 int64_t orc_tree_build(orc_tree *t, int64_t n, const double *px, const double *py, const double *pz,
                        const double *mass, const uint8_t *kind, const uint8_t *alive, double theta,
                        int leaf_size, int dark_matter_off, int workers) {
-    t->theta = theta == 0 ? 0.9 : theta;  // bh.go:118-123 (DefaultTheta)
+    t->theta = theta == 0 ? 0.9 : theta;  // bh.go:69-74 (DefaultTheta)
     t->leaf = leaf_size > 0 ? leaf_size : 24;
     t->workers = workers;
     t->build(n, px, py, pz, mass, kind, alive, dark_matter_off);
@@ -649,7 +649,7 @@ void orc_tree_accelerations(const orc_tree *t, int64_t n, double eps, int monopo
             t->walk<false>(t->sx[k], t->sy[k], t->sz[k], int32_t(k), eps2, quad, ax[i], ay[i], az[i], nullptr);
         }
     });
-    for (int32_t i : t->holes) ax[i] = ay[i] = az[i] = 0;  // bh.go:148-150
+    for (int32_t i : t->holes) ax[i] = ay[i] = az[i] = 0;  // bh.go:99-101
 }
 
 void orc_tree_walk_point(const orc_tree *t, double x, double y, double z, int32_t self, double eps2,
@@ -687,7 +687,7 @@ void orc_tree_counts(const orc_tree *t, double eps, int monopole_only, int worke
 
 // Counts of the group walk the GPU's mixed walk executes: each group of `group` consecutive
 // sorted stars walks the tree together and opens a node when any of its stars would (d2 < crit2,
-// bh.go:165); every star of the group then takes part in each visit. Same definitions as
+// bh.go:116); every star of the group then takes part in each visit. Same definitions as
 // orc_tree_counts (accepted nodes, leaf pairs without the self pair, opened nodes including leaf
 // visits), summed over the stars, so group = 1 gives the per-star counts.
 void orc_tree_group_counts(const orc_tree *t, int group, int workers, int64_t *n_node, int64_t *n_pp,
@@ -1092,7 +1092,7 @@ void orc_split_kdk(int64_t n, double *px, double *py, double *pz, double *vx, do
             last = 1;
             continue;
         }
-        // classify, split.go:41-81
+        // classify, split.go:39-85
         const double limit = kNearSteps * dt;
         double tau_min = std::numeric_limits<double>::infinity();
         for (int64_t i = 0; i < n; ++i) {
@@ -1116,7 +1116,7 @@ void orc_split_kdk(int64_t n, double *px, double *py, double *pz, double *vx, do
         if (!std::isinf(tau_min))
             while (double(k) * tau_min < kSubstepsPerTau * dt && k < kMaxSubsteps) k *= 2;
         last = k;
-        // stepSplit, split.go:161-204 (c = 0, no gas, no spin)
+        // stepSplit, split.go:162-200 (c = 0, no gas, no spin)
         outer();
         kick_outer(h);
         const double hs = dt / double(k);
@@ -1398,7 +1398,7 @@ double orc_pair_rs(uint8_t ki, double mi, uint8_t kj, double mj, double c) { ret
 double orc_potential_exact(int64_t n, const double *px, const double *py, const double *pz,
                            const double *mass, const uint8_t *kind, double eps, double c, int dm_off,
                            int workers) {
-    // diag.go:42-62: each row i summed over j > i ascending, the rows added in ascending i (the
+    // diag.go:42-64: each row i summed over j > i ascending, the rows added in ascending i (the
     // reference adds its ParallelFor chunks in completion order, so only round-off may differ).
     double eps2 = eps * eps;
     std::vector<double> rows(size_t(std::max<int64_t>(n, 0)), 0.0);

@@ -23,7 +23,7 @@
 extern "C" {
 #endif
 
-/* Mirrors internal/sim/bh/bh.go:108-116 (type node). */
+/* Mirrors internal/sim/bh/bh.go:59-67 (type node). */
 typedef struct {
     double x, y, z, m;
     double qxx, qyy, qzz, qxy, qxz, qyz;
@@ -66,12 +66,12 @@ void orc_tree_export(const orc_tree *t, uint64_t *keys, int32_t *order, orc_node
                      double *sx, double *sy, double *sz, double *sm, int32_t *holes);
 
 /*
- * bh.go:125-151 + walk bh.go:155-204: accelerations in state order (n =
+ * bh.go:76-102 + walk bh.go:106-155: accelerations in state order (n =
  * the state length passed to build), holes and dead bodies get 0.
  */
 void orc_tree_accelerations(const orc_tree *t, int64_t n, double eps, int monopole_only,
                             int workers, double *ax, double *ay, double *az);
-/* walk bh.go:155-204 for one point; self = sorted index to skip or -1. */
+/* walk bh.go:106-155 for one point; self = sorted index to skip or -1. */
 void orc_tree_walk_point(const orc_tree *t, double x, double y, double z, int32_t self,
                          double eps2, int monopole_only, double *a3);
 /* walkPotential potential.go:45-81 for one point. */
@@ -152,7 +152,7 @@ void orc_block_kdk(int64_t n, double *px, double *py, double *pz, double *vx, do
  * with instant gravity, no frame dragging (no spins) and no accretion or collapse (those follow
  * the step in sim.go:260-287 and are not restated): star-star forces from the tree once per step; every force involving an alive
  * black hole summed directly; stars whose timescale at a hole is below 20 dt ("near") and the
- * holes take n power-of-two substeps (classify, split.go:41-81). Steps without holes are the
+ * holes take n power-of-two substeps (classify, split.go:39-85). Steps without holes are the
  * plain KDK of orc_kdk. A hole's pull from the far stars is summed in chunks of 256 bodies
  * (sequential inside a chunk, chunks in index order); the reference sums its ParallelFor chunks
  * in completion order, so its last bits vary from run to run there. *substeps gets n of the

@@ -364,7 +364,7 @@ def test_graph_replay_matches_plain_launches(ctx, walk):
         assert np.array_equal(out[0][k], out[1][k]), k
 
 
-def test_diagnostics_match_oracle_and_sums(ctx):  # diag.go:31-120, potential.go:12-42
+def test_diagnostics_match_oracle_and_sums(ctx):  # diag.go:31-135, potential.go:12-42
     """1,502 bodies (two holes, c = 10): TotalEnergy's exact pair sum (n <= 30,000), bit for
     bit against the oracle's restatement; the other sums against numpy."""
     g = np.load(os.path.join(GOLDEN, "disk.npz"))

@@ -379,7 +379,7 @@ def test_pair_potential_limits():  # pair_test.go:20-31
     assert O.pair_rs(S, 1, S, 1, 10) == 0 and O.pair_rs(H, 1, H, 1, 10) == 0 and O.pair_rs(S, 1, H, 5, 10) == 0.1
 
 
-def test_dark_matter_pairs_are_newtonian_except_with_holes():  # pair_test.go:33-41
+def test_dark_matter_pairs_are_newtonian_except_with_holes():  # pair_test.go:32-39
     S, H, D = O.STAR, O.BLACK_HOLE, O.DARK_MATTER
     assert O.pair_rs(D, 1, S, 1, 10) == 0 and O.pair_rs(S, 1, D, 1, 10) == 0 and O.pair_rs(D, 1, D, 1, 10) == 0
     assert O.pair_rs(D, 1, H, 5, 10) == 0.1
