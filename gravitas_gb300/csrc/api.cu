@@ -87,6 +87,11 @@ struct gbh_ctx {
     cudaEvent_t wait_ev = nullptr;  // GBH_CFG_BLOCKING_SYNC: host waits sleep on this event
     cudaEvent_t ahead[4] = {};      // GBH_CFG_BLOCKING_SYNC: ends of the last steps launched
     bool capturing = false;  // stage events become graph event-record nodes
+    // The corrupt-link test hook: with GBH_FAULT_LINK set (non-empty) when the context is created,
+    // the next tree built outside graph capture gets a cycle (the last leaf's skip link points back
+    // at node 0) before its walk, so the walk runs into its step bound and the call returns
+    // GBH_ERR_LIMIT naming the walk kernel. It fires once.
+    bool fault_link = false;
     // bookkeeping
     int64_t launches = 0;
     int64_t h2d = 0, d2h = 0;
@@ -306,6 +311,10 @@ int forces(gbh_ctx *ctx, const gbh_params *p, int64_t n, const double *px, const
                            p->dark_matter_off, p->walk == GBH_WALK_FP64, p->walk == GBH_WALK_PLAIN,
                            forest ? ctx->sys_of : nullptr, forest ? ctx->sys_off : nullptr));
     }
+    if (ctx->fault_link && !ctx->capturing) {
+        ctx->fault_link = false;
+        CK(gbh::fault_link(L, ctx->tb));
+    }
     CK(stage_event(ctx));
     gbh::NvtxRange walk_range("walk");
     double eps2 = p->softening * p->softening;
@@ -325,6 +334,15 @@ int forces(gbh_ctx *ctx, const gbh_params *p, int64_t n, const double *px, const
     }
     CK(stage_event(ctx));
     return GBH_OK;
+}
+
+// The status of a device-side check recorded in the DevInfo the host has read back.
+int info_status(gbh_ctx *ctx) {
+    const DevInfo &i = ctx->info_host;
+    if (!i.err) return GBH_OK;
+    if (i.err_where == gbh::kErrNonFinite)
+        return fail(ctx, GBH_ERR_ARG, "an alive star has a non-finite position or mass (outputs are undefined)");
+    return fail(ctx, GBH_ERR_LIMIT, "device walk exceeded its step bound (kernel %d)", i.err_where);
 }
 
 // Waits for the stream, reads the device scalars and fills the timings of the call.
@@ -349,8 +367,7 @@ int finish(gbh_ctx *ctx, bool tree) {
     if (tree) {
         t.nstars = ctx->info_host.nstars;
         t.nnodes = ctx->info_host.nnodes;
-        if (ctx->info_host.err)
-            return fail(ctx, GBH_ERR_LIMIT, "device walk exceeded its step bound (kernel %d)", ctx->info_host.err_where);
+        return info_status(ctx);
     }
     return GBH_OK;
 }
@@ -591,9 +608,7 @@ int forces_active(gbh_ctx *ctx, const gbh_params *p, const uint8_t *kind, const 
 int read_info(gbh_ctx *ctx) {
     CK(cudaMemcpyAsync(&ctx->info_host, ctx->tb.info, sizeof(DevInfo), cudaMemcpyDeviceToHost, ctx->stream));
     CK(wait_stream(ctx));
-    if (ctx->info_host.err)
-        return fail(ctx, GBH_ERR_LIMIT, "device walk exceeded its step bound (kernel %d)", ctx->info_host.err_where);
-    return GBH_OK;
+    return info_status(ctx);
 }
 
 // Block-step KDK on the resident state (see block_open in tree.cu for the scheme).
@@ -729,6 +744,10 @@ int gbh_create(const gbh_config *cfg, gbh_ctx **out, char *err, int errlen) {
     c->use_graphs = !(cfg && (cfg->flags & GBH_CFG_NO_GRAPHS));
     c->use_lpt = !(cfg && (cfg->flags & GBH_CFG_NO_LPT));
     c->use_split = !(cfg && (cfg->flags & GBH_CFG_NO_SPLIT));
+    {
+        const char *f = std::getenv("GBH_FAULT_LINK");
+        c->fault_link = f && *f;
+    }
     if (cfg && (cfg->flags & GBH_CFG_BLOCKING_SYNC)) {
         e = cudaEventCreateWithFlags(&c->wait_ev, cudaEventBlockingSync | cudaEventDisableTiming);
         for (auto &ev : c->ahead)

@@ -20,6 +20,11 @@ constexpr int kMortonBits = 21;           // morton.go:4
 constexpr int kMaxLevel = kMortonBits;    // buildNode splits only below level 21 (build.go:136)
 constexpr int kNoCell = 22;               // "starts no cell": duplicate of the previous key
 
+// DevInfo.err_where of a build whose alive stars include a non-finite position or mass (the
+// caller gets GBH_ERR_ARG); every other value names the kernel whose bound or check failed
+// (GBH_ERR_LIMIT).
+constexpr int kErrNonFinite = 20;
+
 // Per-build scalars kept on the device, so a step needs no host round trip.
 struct DevInfo {
     double minx, miny, minz;  // bbox min of the stars (build.go:12)
@@ -188,6 +193,10 @@ cudaError_t split_reserve(TreeBufs &b, int64_t n);
 
 // FP32 upsweep; writes the walk records of the plain walk (PNode) and/or the mixed walk (MNode).
 cudaError_t upsweep_fast(const Launch &L, TreeBufs &b, bool plain_records);
+// Test hook (GBH_FAULT_LINK): points the skip link of every leaf that ends its system's walk
+// (next == -1) back at node 0 in the node table and in both FP32 walk records, so that every walk
+// that reaches that leaf cycles until its step bound stops it. Indices stay in range.
+cudaError_t fault_link(const Launch &L, TreeBufs &b);
 // Fills the FP64 moment fields of the node table from the MNode records (after an FP32 upsweep).
 cudaError_t export_fast_moments(const Launch &L, TreeBufs &b);
 // Walks: every star, or (targets = true) the stars listed in b.targets (count in DevInfo.ntargets).

@@ -15,7 +15,12 @@
 //
 // The host cannot use the name g_scratch as a device address (in host code it names a
 // host-side stand-in), so the device address is looked up once per device, with that device
-// current, by cudaGetSymbolAddress, and passed to the kernels.
+// current, by cudaGetSymbolAddress, and passed to the kernels. The looked-up address belongs to
+// the device's context of that moment: a cudaDeviceReset destroys it, and the entry point must
+// not be called on that device again in the same process.
+//
+// Each call waits for its stream before it returns (it reads the number of sorted bodies back to
+// the host).
 #include <cuda_runtime.h>
 
 #include <cstdio>
@@ -74,8 +79,9 @@ extern "C" int gbh_morton_order_noalloc(int32_t device, void *stream, int64_t n,
         // Set-up, once per device with that device current: the device address of g_scratch.
         std::lock_guard<std::mutex> lock(g_setup_mu);
         if (!g_scratch_addr[device]) {
-            if (gbh::morton_sort_scratch_bytes(kNoAllocMaxBodies) > kScratchBytes)
-                return report(err, errlen, GBH_ERR_CUDA, "static scratch array smaller than its stated capacity");
+            if (gbh::morton_sort_scratch_bytes(kNoAllocMaxBodies) > kScratchBytes)  // a build inconsistency
+                return report(err, errlen, GBH_ERR_STATE,
+                              "internal error: the static scratch array is smaller than its stated capacity");
             void *ptr = nullptr;
             e = cudaGetSymbolAddress(&ptr, g_scratch);
             if (e != cudaSuccess) return report_cuda(err, errlen, "cudaGetSymbolAddress", e);
@@ -95,6 +101,8 @@ extern "C" int gbh_morton_order_noalloc(int32_t device, void *stream, int64_t n,
     e = cudaMemcpyAsync(&h, info, sizeof h, cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) return report_cuda(err, errlen, "Morton ordering", e);
+    if (h.err && h.err_where == gbh::kErrNonFinite)
+        return report(err, errlen, GBH_ERR_ARG, "an alive star has a non-finite position (outputs are undefined)");
     if (h.err) return report(err, errlen, GBH_ERR_LIMIT, "device-side consistency check failed in the radix sort");
     *nstars = n > 0 ? h.nstars : 0;
     return GBH_OK;

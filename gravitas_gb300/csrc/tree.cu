@@ -227,8 +227,13 @@ __device__ __forceinline__ void block_minmax(long long mn[3], long long mx[3], d
 }
 
 // Star flags, per-block bbox partials; alive holes get zero acceleration (bh.go:99-101).
+// A non-finite coordinate of a star makes the bbox non-finite by itself (NaN and infinities map to
+// keys beyond every finite one); a non-finite mass is folded in as the key of a NaN, so that
+// k_bbox_final can reject the input before keys are formed (collect, build.go:62-113, would
+// carry a NaN into the root cube and every key).
 __global__ __launch_bounds__(kThreads) void k_flags_bbox(int64_t n, const double *__restrict__ px,
                                                          const double *__restrict__ py, const double *__restrict__ pz,
+                                                         const double *__restrict__ mass,
                                                          const uint8_t *__restrict__ kind,
                                                          const uint8_t *__restrict__ alive, uint32_t *__restrict__ flag,
                                                          double *__restrict__ part, double *ax, double *ay, double *az) {
@@ -240,7 +245,7 @@ __global__ __launch_bounds__(kThreads) void k_flags_bbox(int64_t n, const double
         if (st) {
             long long x = ord_key(px[i]), y = ord_key(py[i]), z = ord_key(pz[i]);
             mn[0] = min(mn[0], x);
-            mx[0] = max(mx[0], x);
+            mx[0] = max(mx[0], mass && !isfinite(mass[i]) ? LLONG_MAX : x);
             mn[1] = min(mn[1], y);
             mx[1] = max(mx[1], y);
             mn[2] = min(mn[2], z);
@@ -307,6 +312,11 @@ __global__ __launch_bounds__(kFinalThreads) void k_bbox_final(int nparts, const 
     info->err_where = 0;
     info->work = 0;
     info->nleaves = 0;
+    if (ns > 0 && !(isfinite(mn[0]) && isfinite(mn[1]) && isfinite(mn[2]) && isfinite(mx[0]) && isfinite(mx[1]) &&
+                    isfinite(mx[2]))) {
+        info->err = 1;  // reported to the caller as GBH_ERR_ARG
+        info->err_where = kErrNonFinite;
+    }
     for (int c = 0; c < 3; ++c) {
         float h = __double2float_rn(mn[c]);
         info->min_hi[c] = h;
@@ -1236,8 +1246,12 @@ constexpr int kFlagBlocksMax = 1024;
 
 namespace {
 
-__global__ void k_sys_init(int32_t nsys, SysGeo *geo) {
+__global__ void k_sys_init(int32_t nsys, SysGeo *geo, DevInfo *info) {
     int32_t s = int32_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (s == 0) {  // cleared before k_sys_final may report a non-finite system
+        info->err = 0;
+        info->err_where = 0;
+    }
     if (s >= nsys) return;
     for (int c = 0; c < 3; ++c) {
         geo[s].kmin[c] = LLONG_MAX;
@@ -1249,6 +1263,7 @@ __global__ void k_sys_init(int32_t nsys, SysGeo *geo) {
 // warp-wide atomic per quantity when the warp's stars share a system).
 __global__ __launch_bounds__(kThreads) void k_flags_sys(int64_t n, const double *__restrict__ px,
                                                         const double *__restrict__ py, const double *__restrict__ pz,
+                                                        const double *__restrict__ mass,
                                                         const uint8_t *__restrict__ kind,
                                                         const uint8_t *__restrict__ alive,
                                                         const uint16_t *__restrict__ sys_of, uint32_t *__restrict__ flag,
@@ -1263,7 +1278,7 @@ __global__ __launch_bounds__(kThreads) void k_flags_sys(int64_t n, const double 
         flag[i] = st;
         if (st) {
             s = sys_of[i];
-            k[0] = ord_key(px[i]);
+            k[0] = mass && !isfinite(mass[i]) ? LLONG_MAX : ord_key(px[i]);  // as in k_flags_bbox
             k[1] = ord_key(py[i]);
             k[2] = ord_key(pz[i]);
         } else if (al && kd == GBH_BLACK_HOLE) {
@@ -1308,8 +1323,6 @@ __global__ void k_sys_final(int32_t nsys, int64_t n, const int64_t *__restrict__
         info->theta = theta;
         info->nstars = total;
         info->nnodes = 0;
-        info->err = 0;
-        info->err_where = 0;
         info->work = 0;
         info->nleaves = 0;
     }
@@ -1320,6 +1333,7 @@ __global__ void k_sys_final(int32_t nsys, int64_t n, const int64_t *__restrict__
         mn[c] = ord_val(g.kmin[c]);
         mx[c] = ord_val(g.kmax[c]);
     }
+
     double side = fmax(mx[0] - mn[0], fmax(mx[1] - mn[1], mx[2] - mn[2]));
     side = fmax(side * (1 + 1e-9), 1e-12);
     g.minx = mn[0];
@@ -1340,6 +1354,10 @@ __global__ void k_sys_final(int32_t nsys, int64_t n, const int64_t *__restrict__
     int64_t a = sys_off[s], b = sys_off[s + 1];
     g.star_lo = int32_t(a < n ? int64_t(scan[a]) : total);
     g.star_hi = int32_t(b < n ? int64_t(scan[b]) : total);
+    // an empty system keeps its initial keys (a NaN box); a system with stars must be finite
+    if (g.star_hi > g.star_lo && !(isfinite(mn[0]) && isfinite(mn[1]) && isfinite(mn[2]) && isfinite(mx[0]) &&
+                                   isfinite(mx[1]) && isfinite(mx[2])))
+        dev_error(info, kErrNonFinite);
 }
 
 // Each star's Morton key in its own system's cube (build.go:19-31).
@@ -1521,7 +1539,7 @@ cudaError_t tree_build(const Launch &L, TreeBufs &b, int64_t n, const double *px
         // collect + bbox (build.go:62-113)
         unsigned fb = blocks_for(n, kThreads);
         if (fb > unsigned(kFlagBlocksMax)) fb = kFlagBlocksMax;
-        k_flags_bbox<<<fb, kThreads, 0, s>>>(n, px, py, pz, kind, alive, b.flag, b.bbox_part, ax, ay, az);
+        k_flags_bbox<<<fb, kThreads, 0, s>>>(n, px, py, pz, mass, kind, alive, b.flag, b.bbox_part, ax, ay, az);
         GBH_LAUNCH_CHECK();
         e = scan_u32(L, b.flag, b.flag, n, b.scan_tmp, b.scan_tmp_cap);
         if (e != cudaSuccess) return e;
@@ -1533,10 +1551,10 @@ cudaError_t tree_build(const Launch &L, TreeBufs &b, int64_t n, const double *px
     } else {
         // collect per system: each system gets its own root cube and keys (build.go:11-31)
         const unsigned sb = blocks_for(b.nsys, 128);
-        k_sys_init<<<sb, 128, 0, s>>>(b.nsys, b.geo);
+        k_sys_init<<<sb, 128, 0, s>>>(b.nsys, b.geo, b.info);
         GBH_LAUNCH_CHECK();
-        k_flags_sys<<<blocks_for(n, kThreads), kThreads, 0, s>>>(n, px, py, pz, kind, alive, sys_of, b.flag, b.geo, ax,
-                                                                 ay, az);
+        k_flags_sys<<<blocks_for(n, kThreads), kThreads, 0, s>>>(n, px, py, pz, mass, kind, alive, sys_of, b.flag,
+                                                                 b.geo, ax, ay, az);
         GBH_LAUNCH_CHECK();
         e = scan_u32(L, b.flag, b.flag, n, b.scan_tmp, b.scan_tmp_cap);
         if (e != cudaSuccess) return e;
@@ -1618,6 +1636,25 @@ cudaError_t tree_build(const Launch &L, TreeBufs &b, int64_t n, const double *px
     k_upsweep<<<nb, kThreads, 0, s>>>(b.keys, b.info, cnt, base, b.pre_ref, b.sx, b.sy, b.sz, b.sm, b.nodes,
                                       b.n_parent, b.n_info, b.n_arrive, b.pnodes, b.mnodes, b.mrange, sid, b.geo,
                                       b.info);
+    GBH_LAUNCH_CHECK();
+    return cudaSuccess;
+}
+
+namespace {
+__global__ __launch_bounds__(kThreads) void k_fault_link(const DevInfo *info, gbh_node *nodes, PNode *pnodes,
+                                                         MNode *mnodes, int64_t cap) {
+    const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= info->nnodes || i >= cap) return;
+    if (nodes[i].next != -1 || nodes[i].first != -1) return;
+    nodes[i].next = 0;
+    pnodes[i].links.y = 0;
+    mnodes[i].d.w = __int_as_float(0);
+}
+}  // namespace
+
+cudaError_t fault_link(const Launch &L, TreeBufs &b) {
+    k_fault_link<<<blocks_for(b.cap_nodes, kThreads), kThreads, 0, L.stream>>>(b.info, b.nodes, b.pnodes, b.mnodes,
+                                                                               b.cap_nodes);
     GBH_LAUNCH_CHECK();
     return cudaSuccess;
 }

@@ -1,7 +1,8 @@
-"""Headless evolution to a save file, the gravity-only counterpart of tools/evolve (main.go:21-120):
+"""Headless evolution to a save file, the gravity-only counterpart of tools/evolve (main.go:22-100):
 build a scene (or continue from a .gravitas snapshot), step it with the GPU solver until the
-simulated time reaches -t, report progress, stop at the first body with a non-finite position,
-velocity or acceleration (firstBad), and write the state as a snapshot.
+simulated time reaches -t, report progress, stop with exit status 1 at the first body whose state
+is NaN or beyond 1e6 in magnitude (the watchdog firstBad, main.go:63-74 and 185-194), and write
+the state as a snapshot.
 
     python -m gravitas_gb300.evolve --scene merger --n 1048576 -t 0.05 -o evolved.gravitas
     python -m gravitas_gb300.evolve --in evolved.gravitas -t 0.1 -o later.gravitas
@@ -17,7 +18,7 @@ import time
 
 import numpy as np
 
-from . import ics
+from . import abi, ics
 from .sim import Params, Simulation, Solver, State
 
 SCENES = {
@@ -29,12 +30,28 @@ SCENES = {
 
 
 def first_bad(s: State) -> int:
-    """The first body with a non-finite position, velocity or acceleration, or -1 (main.go:129-140)."""
+    """firstBad (tools/evolve/main.go:185-194): the first body whose x position, x velocity or x
+    acceleration is NaN or larger than 1e6 in magnitude (infinities included), or -1. The
+    reference also tests the gas fields U and H, which this library does not hold."""
     bad = np.zeros(len(s), bool)
-    for a in (s.pos_x, s.pos_y, s.pos_z, s.vel_x, s.vel_y, s.vel_z, s.acc_x, s.acc_y, s.acc_z):
-        bad |= ~np.isfinite(a)
+    for a in (s.pos_x, s.vel_x, s.acc_x):
+        bad |= np.isnan(a) | (np.abs(a) > 1e6)
     idx = np.flatnonzero(bad)
     return int(idx[0]) if len(idx) else -1
+
+
+def report_bad(m: Simulation, i: int, out=None) -> None:
+    """The watchdog's report (main.go:64-72): the bad body, then every black hole's mass, distance
+    and speed (to standard output, as the reference prints it)."""
+    out = out or sys.stdout
+    s = m.state
+    print(f"step {m.steps} t={m.time:.5f}: body {i} kind {s.kind[i]} pos ({s.pos_x[i]:g} {s.pos_y[i]:g} "
+          f"{s.pos_z[i]:g}) vel ({s.vel_x[i]:g} {s.vel_y[i]:g} {s.vel_z[i]:g}) acc ({s.acc_x[i]:g} {s.acc_y[i]:g} "
+          f"{s.acc_z[i]:g}) m {s.mass[i]:g}", file=out)
+    for h in np.flatnonzero(s.kind == abi.BLACK_HOLE):
+        d = np.sqrt((s.pos_x[h] - s.pos_x[i]) ** 2 + (s.pos_y[h] - s.pos_y[i]) ** 2 + (s.pos_z[h] - s.pos_z[i]) ** 2)
+        v = np.sqrt(s.vel_x[h] ** 2 + s.vel_y[h] ** 2 + s.vel_z[h] ** 2)
+        print(f"  hole {h} m {s.mass[h]:g} at distance {d:g}, speed {v:g}", file=out)
 
 
 def main(argv=None) -> int:
@@ -50,7 +67,9 @@ def main(argv=None) -> int:
     ap.add_argument("--every", type=float, default=0.0, help="also report progress every this much simulation time")
     ap.add_argument("--in", dest="inp", default="", help="continue from this save file instead of building the scene")
     ap.add_argument("-o", default="evolved.gravitas", help="save file to write")
-    ap.add_argument("--chunk", type=int, default=50, help="steps per library call")
+    ap.add_argument("--chunk", type=int, default=1,
+                    help="steps per library call; the watchdog looks at the state after every call (1: after "
+                         "every step, as the reference does)")
     a = ap.parse_args(argv)
 
     solver = Solver(theta=a.theta, leaf_size=a.leaf)
@@ -68,9 +87,7 @@ def main(argv=None) -> int:
         steps += k
         i = first_bad(m.state)
         if i >= 0:
-            s = m.state
-            print(f"step {m.steps} t={m.time:.5f}: body {i} kind {s.kind[i]} pos ({s.pos_x[i]} {s.pos_y[i]} "
-                  f"{s.pos_z[i]}) vel ({s.vel_x[i]} {s.vel_y[i]} {s.vel_z[i]})", file=sys.stderr)
+            report_bad(m, i)
             return 1
         if a.every > 0 and m.time >= nxt:
             nxt += a.every

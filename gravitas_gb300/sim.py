@@ -146,20 +146,28 @@ class Simulation:
         self.steps += n
 
     def save(self, path: str) -> None:
-        """A .gravitas snapshot of the run (save.Capture + Write, save.go:69-148), with the last
-        forces when they are valid, so that a loaded run continues bit-identically."""
+        """A .gravitas snapshot of the run (save.Capture + Write, save.go:66-146), with the last
+        forces when they are valid, so that a loaded run continues bit-identically.
+
+        The file format has no alive flags: File.State (save.go:84-111) makes every saved body
+        alive. The reference never holds dead bodies when it saves, because accretion and
+        collapse remove them at once (State.Compact, state.go:99-122). So the snapshot holds the
+        alive bodies only, in state order, as Compact leaves them; the Simulation itself is not
+        changed."""
         from . import snapshot
         s = self.state
-        state = {"px": s.pos_x, "py": s.pos_y, "pz": s.pos_z, "vx": s.vel_x, "vy": s.vel_y, "vz": s.vel_z,
-                 "mass": s.mass, "kind": s.kind}
+        keep = s.alive.astype(bool) if len(s.alive) == len(s) else np.ones(len(s), bool)
+        sel = (lambda a: a) if keep.all() else (lambda a: np.ascontiguousarray(a[keep]))
+        state = {"px": sel(s.pos_x), "py": sel(s.pos_y), "pz": sel(s.pos_z), "vx": sel(s.vel_x),
+                 "vy": sel(s.vel_y), "vz": sel(s.vel_z), "mass": sel(s.mass), "kind": sel(s.kind)}
         params = {"Dt": self.params.dt, "Softening": self.params.softening, "C": self.params.c,
                   "DarkMatterOff": self.params.dark_matter_off}
-        forces = (s.acc_x, s.acc_y, s.acc_z) if self.acc_valid else None
+        forces = (sel(s.acc_x), sel(s.acc_y), sel(s.acc_z)) if self.acc_valid else None
         snapshot.save(path, state, params, time=self.time, steps=self.steps, forces=forces)
 
     @classmethod
     def load(cls, path: str, solver: "Solver") -> "Simulation":
-        """A run restored from a snapshot (File.Restore, save.go:121-130)."""
+        """A run restored from a snapshot (File.Restore, save.go:113-121)."""
         from . import snapshot
         st, params, meta = snapshot.load_state(path)
         state = State(st["px"], st["py"], st["pz"], st["vx"], st["vy"], st["vz"], st["ax"], st["ay"], st["az"],

@@ -434,7 +434,9 @@ def decode(data: bytes):
 
 _PARAMS = Struct("Params", [("Dt", FLOAT), ("Softening", FLOAT), ("C", FLOAT), ("DarkMatterOff", BOOL)])
 _FLOATS = Slice(FLOAT)
-_FORCES = Struct("Forces", [("AccX", _FLOATS), ("AccY", _FLOATS), ("AccZ", _FLOATS)])
+# sim.Forces (sim.go:187-191): RestoreForces (sim.go:208-212) installs a saved evaluation only when
+# AccX and Rho both hold one entry per body, so Rho is written too (zeros: no gas density here).
+_FORCES = Struct("Forces", [("AccX", _FLOATS), ("AccY", _FLOATS), ("AccZ", _FLOATS), ("Rho", _FLOATS)])
 _FILE = Struct("File", [
     ("Format", INT), ("Params", _PARAMS), ("Time", FLOAT), ("Steps", INT),
     ("PosX", _FLOATS), ("PosY", _FLOATS), ("PosZ", _FLOATS), ("VelX", _FLOATS), ("VelY", _FLOATS),
@@ -444,21 +446,22 @@ _FILE = Struct("File", [
 def save(path: str, state: dict, params: dict, time: float = 0.0, steps: int = 0, forces=None) -> None:
     """Writes a snapshot: state holds px..vz, mass and kind (numpy arrays in state order);
     params Dt, Softening, C, DarkMatterOff; forces (ax, ay, az) of the last force evaluation or
-    None (save.go:69-86 captures the same, plus fields this library does not own)."""
+    None (save.go:66-82 captures the same, plus fields this library does not own)."""
     f = {"Format": FORMAT, "Time": time, "Steps": steps,
          "Params": {k: params.get(k, 0) for k in ("Dt", "Softening", "C", "DarkMatterOff")},
          "PosX": state["px"], "PosY": state["py"], "PosZ": state["pz"],
          "VelX": state["vx"], "VelY": state["vy"], "VelZ": state["vz"], "Mass": state["mass"],
          "Kind": np.asarray(state.get("kind", np.zeros(len(state["mass"]), np.uint8)), np.uint8).tobytes()}
     if forces is not None:
-        f["Forces"] = {"AccX": forces[0], "AccY": forces[1], "AccZ": forces[2]}
+        f["Forces"] = {"AccX": forces[0], "AccY": forces[1], "AccZ": forces[2],
+                       "Rho": np.zeros(len(state["mass"]))}
     data = Encoder().encode(_FILE, f).getvalue()
     with gzip.open(path, "wb") as g:
         g.write(data)
 
 
 def read(path: str) -> dict:
-    """The decoded save.File of a snapshot, every field the stream holds (save.go:150-175)."""
+    """The decoded save.File of a snapshot, every field the stream holds (save.go:148-170)."""
     with open(path, "rb") as fh:
         raw = fh.read()
     try:

@@ -34,12 +34,17 @@ extern "C" {
 
 enum {
     GBH_OK = 0,
-    GBH_ERR_ARG = 1,         /* invalid argument (null pointer, negative size, bad enum) */
+    GBH_ERR_ARG = 1,         /* invalid argument (null pointer, negative size, bad enum), or an
+                                alive star with a non-finite position or mass: found on the device
+                                by the tree build's bounding-box reduction, before keys are formed
+                                (the call's outputs are then undefined) */
     GBH_ERR_CUDA = 2,        /* a CUDA runtime call failed (message has the CUDA error) */
     GBH_ERR_NOMEM = 3,       /* device allocation failed (test hook: with GBH_FAULT_ALLOC=k in the
                                 environment when a context is created, the allocation after k
                                 successful ones fails once, without touching the device) */
-    GBH_ERR_LIMIT = 4,       /* a device-side walk exceeded its step bound (corrupt input?) */
+    GBH_ERR_LIMIT = 4,       /* a device-side walk exceeded its step bound (a corrupt tree); the
+                                message names the kernel (test hook: with GBH_FAULT_LINK set when a
+                                context is created, its next tree gets a cycle in its skip links) */
     GBH_ERR_STATE = 5,       /* no resident state, or sizes do not match it */
     GBH_ERR_UNSUPPORTED = 6  /* input outside this path (e.g. alive black holes in a step) */
 };
@@ -374,9 +379,13 @@ int gbh_probe_fp32_peak(gbh_ctx *ctx, double ms, double *tflops);
  * It allocates nothing: its temporaries live in one static device array of 4.5 MiB that
  * every GPU which loads the library holds until the process exits, enough for at most
  * 262,144 bodies; larger n returns GBH_ERR_ARG. The first call on a device looks up that
- * array's device address, so make it before any stream capture. All calls share the array:
- * calls that overlap on the GPU (for instance on two streams of one device) race and must
- * be serialised by the caller. Errors are returned as a code with a message in err.
+ * array's device address, so make it before any stream capture. The address is kept for the
+ * life of the process: after a cudaDeviceReset of that device, do not call this entry point on
+ * it again. All calls share the array: calls that overlap on the GPU (for instance on two
+ * streams of one device) race and must be serialised by the caller. Every call waits for its
+ * stream to finish before returning (it reads the number of sorted bodies back to the host).
+ * An alive star with a non-finite position gives GBH_ERR_ARG. Errors are returned as a code
+ * with a message in err.
  */
 int gbh_morton_order_noalloc(int32_t device, void *stream, int64_t n, const double *px,
                              const double *py, const double *pz, const uint8_t *kind,

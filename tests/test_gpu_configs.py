@@ -135,3 +135,64 @@ def test_merger_1m_theta_sweep(ctx):
     ctx.step_block(par, 4e-3, 0.025, 6, 1)
     e1 = ctx.diagnostics(par)["total"]
     assert abs((e1 - e0) / e0) < 1e-5
+
+
+@pytest.fixture(scope="module")
+def merger_1m():
+    """The headline workload's inputs: the 1,048,576-body merger, the bench's 4,096 seeded
+    targets and their FP64 direct-sum accelerations (eps 0.02)."""
+    s = ics.merger(1 << 20, seed=0)
+    n = len(s["px"])
+    rng = np.random.default_rng(1234)
+    tg = np.sort(rng.choice(n, 4096, replace=False)).astype(np.int64)
+    c = abi.Context(0)
+    want = np.zeros((3, len(tg)))
+    c.call("gbh_direct_accelerations", abi.make_params(0, 0.02, 0, False, False, "fp64"), n, P(s["px"]),
+           P(s["py"]), P(s["pz"]), P(s["mass"]), P(s["kind"]), P(tg), len(tg), P(want[0]), P(want[1]), P(want[2]))
+    c.close()
+    return s, tg, want.T
+
+
+def reference_tree_at(s, tg, leaf):
+    """The reference per-star walk (bh.go:106-155, FP64) at theta 0.5 for the targets, and the
+    oracle tree itself."""
+    tree = O.Tree(s["px"], s["py"], s["pz"], s["mass"], s["kind"], s["alive"], theta=0.5, leaf=leaf)
+    order = tree.export()["order"]
+    sorted_of = np.empty(len(s["px"]), np.int64)
+    sorted_of[order] = np.arange(len(order))
+    ref = np.array([tree.walk_point(s["px"][i], s["py"][i], s["pz"][i], 0.02 ** 2, int(sorted_of[i])) for i in tg])
+    return tree, ref, sorted_of
+
+
+@pytest.mark.parametrize("leaf,group", [(24, 64), (32, 64), (24, 32), (32, 32)])
+def test_merger_1m_mixed_walk_per_star_against_the_reference_tree(ctx, merger_1m, leaf, group):
+    """The headline configuration (1M merger, theta 0.5, eps 0.02, the leaf sizes the autotuner
+    picks between, both group sizes), star by star on the bench's 4,096 seeded targets against the
+    reference per-star tree walk at the same theta and leaf. The mixed walk opens every node the
+    reference opens for a star (and some it accepts, for the star's group), so it differs from
+    the reference tree by part of the tree's own error, plus FP32 rounding. Bound, per star:
+    |a_mixed - a_tree| / |a_tree| <= 2 x (that star's tree error |a_tree - a_direct| / |a_direct|)
+    + 1e-5; over the targets the median of the same ratio <= 2e-4."""
+    s, tg, direct = merger_1m
+    _, ref, _ = reference_tree_at(s, tg, leaf)
+    got = accelerations(ctx, s, abi.make_params(0.5, 0.02, leaf, False, False, "mixed", group_size=group))[tg]
+    d = np.linalg.norm(got - ref, axis=1) / np.linalg.norm(ref, axis=1)
+    e_tree = np.linalg.norm(ref - direct, axis=1) / np.linalg.norm(direct, axis=1)
+    worst = int(np.argmax(d - 2 * e_tree))
+    assert np.all(d <= 2 * e_tree + 1e-5), (tg[worst], d[worst], e_tree[worst])
+    assert np.median(d) <= 2e-4, np.median(d)
+
+
+def test_merger_1m_plain_walk_per_star_against_the_reference_fp32_walk(ctx, merger_1m):
+    """The plain walk at leaf 32 (the Metal kernel's CUDA twin) against the oracle's FP32
+    restatement of the Metal walk (gpu_darwin.go:84-117) on the same tree, and against the FP64
+    reference tree with the bounds of gpu_test.go:8-21 (median 1e-5, max 1e-3), on the bench's
+    4,096 targets."""
+    s, tg, _ = merger_1m
+    tree, ref, sorted_of = reference_tree_at(s, tg, 32)
+    fp32 = tree.walk_fp32(0.02).astype(np.float64)[sorted_of[tg]]
+    got = accelerations(ctx, s, abi.make_params(0.5, 0.02, 32, False, False, "plain"))[tg]
+    d32 = np.linalg.norm(got - fp32, axis=1) / np.linalg.norm(fp32, axis=1)
+    assert np.median(d32) <= 1e-6 and d32.max() <= 1e-4, (np.median(d32), d32.max())
+    d64 = np.linalg.norm(got - ref, axis=1) / np.linalg.norm(ref, axis=1)
+    assert np.median(d64) <= 1e-5 and d64.max() <= 1e-3, (np.median(d64), d64.max())

@@ -112,3 +112,62 @@ def test_garbage_is_rejected(tmp_path):  # save_test.go:89-100
             f.write(blob)
         with pytest.raises(S.GobError):
             S.read(p)
+
+
+def test_saved_forces_satisfy_the_reference_restore_condition(tmp_path):
+    """RestoreForces (sim.go:208-212) installs saved forces only when AccX and Rho both hold one
+    entry per body; the writer therefore sends Rho (zeros) beside the accelerations."""
+    s = ics.plummer(500, seed=6)
+    n = len(s["px"])
+    p = os.path.join(tmp_path, "f.gravitas")
+    S.save(p, s, {"Dt": 1e-3, "Softening": 0.01}, forces=(s["ax"] + 1, s["ay"], s["az"]))
+    f = S.read(p)["Forces"]
+    assert len(f["AccX"]) == n and len(f["Rho"]) == n and not np.any(f["Rho"])
+
+
+def test_simulation_save_keeps_only_alive_bodies(tmp_path):
+    """The file format has no alive flags (File.State makes every body alive), and the reference
+    never saves dead bodies because it compacts them away at once (State.Compact,
+    state.go:99-122). Simulation.save writes the alive bodies in state order, with their forces,
+    and leaves the in-memory state as it was."""
+    from gravitas_gb300.sim import Params, Simulation, State
+
+    d = ics.plummer(400, seed=7)
+    st = State.from_dict(d)
+    rng = np.random.default_rng(1)
+    st.acc_x[:] = rng.normal(size=len(st))
+    st.alive[[3, 150, 399]] = 0
+    m = Simulation(st, solver=None, params=Params(dt=1e-3, softening=0.01))
+    m.acc_valid = True
+    p = os.path.join(tmp_path, "dead.gravitas")
+    m.save(p)
+    got, _, meta = S.load_state(p)
+    keep = st.alive.astype(bool)
+    assert len(got["px"]) == keep.sum() == 397 and meta["forces"]
+    assert np.array_equal(got["px"], st.pos_x[keep]) and np.array_equal(got["ax"], st.acc_x[keep])
+    assert np.array_equal(got["kind"], st.kind[keep]) and got["alive"].all()
+    assert len(st) == 400 and st.alive.sum() == 397
+
+
+def test_evolve_watchdog_restates_first_bad(capsys):
+    """firstBad (tools/evolve/main.go:185-194): NaN or |v| > 1e6 in the x position, x velocity or x
+    acceleration marks a body (infinities included; the y and z components are not looked at, as
+    in the reference); the report names the body and every black hole's distance and speed."""
+    from gravitas_gb300 import evolve
+    from gravitas_gb300.sim import Params, Simulation, State
+
+    st = State.from_dict(ics.plummer(50, seed=2))
+    assert evolve.first_bad(st) == -1
+    st.pos_y[5] = np.nan  # not a component firstBad reads
+    st.vel_z[6] = 1e9
+    assert evolve.first_bad(st) == -1
+    for arr, v, i in ((st.acc_x, np.nan, 30), (st.vel_x, -2e6, 20), (st.pos_x, np.inf, 9)):
+        arr[i] = v
+        assert evolve.first_bad(st) == i
+    st.pos_x[9] = 1e6  # the bound itself is allowed
+    assert evolve.first_bad(st) == 20
+    st.kind[40] = 1
+    m = Simulation(st, solver=None, params=Params(dt=1e-3))
+    evolve.report_bad(m, 20)
+    out = capsys.readouterr().out
+    assert "body 20" in out and "hole 40" in out
