@@ -32,7 +32,7 @@ class GbhError(RuntimeError):
 class Params(ctypes.Structure):
     _fields_ = [("theta", ctypes.c_double), ("softening", ctypes.c_double), ("leaf_size", ctypes.c_int32),
                 ("monopole_only", ctypes.c_int32), ("dark_matter_off", ctypes.c_int32), ("walk", ctypes.c_int32),
-                ("group_size", ctypes.c_int32), ("reserved", ctypes.c_int32), ("c", ctypes.c_double)]
+                ("group_size", ctypes.c_int32), ("list_depth", ctypes.c_int32), ("c", ctypes.c_double)]
 
 
 CFG_NO_GRAPHS = 1
@@ -87,10 +87,10 @@ class TuneEntry(ctypes.Structure):
     _fields_ = [("theta", ctypes.c_double), ("leaf_size", ctypes.c_int32), ("group_size", ctypes.c_int32),
                 ("ms", ctypes.c_double), ("build_ms", ctypes.c_double), ("walk_ms", ctypes.c_double),
                 ("rms_err", ctypes.c_double), ("p99_err", ctypes.c_double), ("meets", ctypes.c_int32),
-                ("reserved", ctypes.c_int32)]
+                ("list_depth", ctypes.c_int32)]
 
     def as_dict(self):
-        return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}
+        return {k: getattr(self, k) for k, _ in self._fields_}
 
 NODE_DTYPE = np.dtype(
     [("x", "f8"), ("y", "f8"), ("z", "f8"), ("m", "f8"),
@@ -177,10 +177,10 @@ def ptr(a):
 
 
 def make_params(theta=0.0, softening=0.0, leaf_size=0, monopole_only=False, dark_matter_off=False,
-                walk="mixed", group_size=0, c=0.0) -> Params:
+                walk="mixed", group_size=0, c=0.0, list_depth=0) -> Params:
     w = WALKS[walk] if isinstance(walk, str) else int(walk)
     return Params(float(theta), float(softening), int(leaf_size), int(bool(monopole_only)),
-                  int(bool(dark_matter_off)), w, int(group_size), 0, float(c))
+                  int(bool(dark_matter_off)), w, int(group_size), int(list_depth), float(c))
 
 
 class Context:

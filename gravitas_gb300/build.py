@@ -4,6 +4,7 @@ Each translation unit gets its own floating-point flags:
   tree.cu  -fmad=false   FP64 keys, moments, FP64 walk, direct sum and kick/drift keep the
                          reference's rounded multiply-then-add order (bit-exact parity);
   walk.cu  fast FP32     FMA contraction on, approximate FP32 division and square root;
+  walk_lists.cu          the list walk, with the flags of walk.cu;
   moments.cu             FP32 node moments for the FP32 walks (FMA on, IEEE FP32 division);
   api.cu                 host code;
   noalloc.cu             the entry point whose temporaries live in a static device array;
@@ -29,6 +30,7 @@ COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler",
 UNITS = {
     "tree.cu": ["-fmad=false"],
     "walk.cu": ["-prec-div=false", "-prec-sqrt=false", "-ftz=true"],
+    "walk_lists.cu": ["-prec-div=false", "-prec-sqrt=false", "-ftz=true"],
     "moments.cu": [],
     "api.cu": [],
     "noalloc.cu": [],

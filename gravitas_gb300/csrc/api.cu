@@ -216,11 +216,22 @@ int check_params(gbh_ctx *ctx, const gbh_params *p) {
     if (p->walk < GBH_WALK_MIXED || p->walk > GBH_WALK_FP64) return fail(ctx, GBH_ERR_ARG, "walk %d", p->walk);
     if (p->group_size != 0 && p->group_size != 32 && p->group_size != 64)
         return fail(ctx, GBH_ERR_ARG, "group_size %d (0, 32 or 64)", p->group_size);
+    if (p->list_depth != 0 && (p->list_depth < 2 || p->list_depth > gbh::list_depth_max(false)))
+        return fail(ctx, GBH_ERR_ARG, "list_depth %d (0, or 2 to %d)", p->list_depth, gbh::list_depth_max(false));
     if (!(p->c >= 0 && std::isfinite(p->c))) return fail(ctx, GBH_ERR_ARG, "c %g must be finite and >= 0", p->c);
     return GBH_OK;
 }
 
 double theta_of(const gbh_params *p) { return p->theta == 0 ? 0.9 : p->theta; }  // bh.go:69-74
+
+// Stars per group of the mixed walk: 32 (the list walk) or 64 (the paired walk). By default the
+// list walk, except for a single system with so few groups per SM that the paired walk shares
+// each group among several warps (with GBH_CFG_NO_SPLIT it then walks them unshared).
+int group_of(const gbh_params *p, int64_t n, bool forest) {
+    if (p->group_size == 32 || p->group_size == 64) return p->group_size;
+    if (forest) return 32;
+    return gbh::walk_parts(n, 64) > 1 ? 64 : 32;
+}
 int leaf_of(const gbh_params *p) { return p->leaf_size > 0 ? p->leaf_size : 24; }  // bh.go:17-19
 
 int begin(gbh_ctx *ctx) {
@@ -300,7 +311,8 @@ int forces(gbh_ctx *ctx, const gbh_params *p, int64_t n, const double *px, const
     int leaf = leaf_of(p);
     forest = forest && ctx->nsys > 1;
     CK(gbh::tree_alloc(ctx->tb, n, leaf, forest ? ctx->nsys : 1));
-    ctx->tb.group = p->group_size == 32 ? 32 : 64;
+    ctx->tb.group = group_of(p, n, forest);
+    ctx->tb.list_depth = p->list_depth;
     ctx->tb.lpt = ctx->use_lpt;
     ctx->tb.split = ctx->use_split;
     ctx->tb.walk_hint = 0;
@@ -392,7 +404,7 @@ void free_graph(StepGraph &g) {
 bool same_params(const gbh_params &a, const gbh_params &b) {
     return a.theta == b.theta && a.softening == b.softening && a.leaf_size == b.leaf_size &&
            a.monopole_only == b.monopole_only && a.dark_matter_off == b.dark_matter_off && a.walk == b.walk &&
-           (a.group_size == 32) == (b.group_size == 32) && a.c == b.c;
+           a.group_size == b.group_size && a.list_depth == b.list_depth && a.c == b.c;
 }
 
 // out[q] = a[idx[q]] for the three arrays of a (n doubles apart in out).
@@ -577,7 +589,8 @@ int forces_active(gbh_ctx *ctx, const gbh_params *p, const uint8_t *kind, const 
     int leaf = leaf_of(p);
     int64_t n = ctx->n;
     CK(gbh::tree_alloc(ctx->tb, n, leaf));
-    ctx->tb.group = p->group_size == 32 ? 32 : 64;
+    ctx->tb.group = group_of(p, n, false);  // as the global step, so that one level is that step
+    ctx->tb.list_depth = p->list_depth;
     ctx->tb.lpt = ctx->use_lpt;
     ctx->tb.split = ctx->use_split;
     ctx->tb.walk_hint = ctx->active_hint;  // this event's list is not known on the host yet
@@ -1358,15 +1371,21 @@ int gbh_autotune(gbh_ctx *ctx, const gbh_params *base, const double *thetas, int
     gbh_tune_entry cur_best = {}, any_best = {};
     for (int32_t a = 0; a < nthetas; ++a)
         for (int32_t b = 0; b < nleaves; ++b)
-            for (int32_t c = 0; c < ngroups; ++c) {
+            for (int32_t c = 0; c < ngroups * 2; ++c) {
+                // the list walk (32-star groups) also sweeps its list depth unless the caller set one
+                const bool lists = base->walk == GBH_WALK_MIXED && groups[c / 2] == 32;
+                static const int32_t kDepths[2] = {24, 48};
+                if ((c & 1) && !(lists && base->list_depth == 0)) continue;
                 gbh_params p = *base;
                 p.theta = thetas[a];
                 p.leaf_size = leaves[b];
-                p.group_size = groups[c];
+                p.group_size = groups[c / 2];
+                p.list_depth = lists ? (base->list_depth ? base->list_depth : kDepths[c & 1]) : 0;
                 gbh_tune_entry e = {};
                 e.theta = p.theta;
                 e.leaf_size = p.leaf_size;
                 e.group_size = base->walk == GBH_WALK_MIXED ? (p.group_size == 32 ? 32 : 64) : 0;
+                e.list_depth = p.list_depth;
                 std::vector<double> tot, bld, wlk;
                 for (int32_t r = -1; r < reps; ++r) {  // r = -1: untimed warm-up (allocation)
                     ctx->evused = 0;
@@ -1420,6 +1439,7 @@ int gbh_autotune(gbh_ctx *ctx, const gbh_params *base, const double *thetas, int
     best->theta = w.theta;
     best->leaf_size = w.leaf_size;
     best->group_size = w.group_size;
+    best->list_depth = w.list_depth;
     if (ntable) *ntable = count;
     ctx->evused = 0;
     CK(cudaEventRecord(ctx->ev[0], ctx->stream));

@@ -80,7 +80,8 @@ struct TreeBufs {
     int64_t cap_n = 0;      // bodies
     int64_t cap_nodes = 0;  // nodes
     int64_t generation = 0; // incremented whenever the buffers are reallocated
-    int32_t group = 64;     // stars per mixed-walk group (32 or 64), set before tree_build
+    int32_t group = 64;     // stars per mixed-walk group (32: the list walk, or 64), set before tree_build
+    int32_t list_depth = 0; // the list walk's node-list depth (0: kDefaultListDepth), set per call
     // compaction / bbox
     uint32_t *flag = nullptr;     // star flags, then their exclusive scan
     double *bbox_part = nullptr;  // per-block partial min/max (6 per block)
@@ -108,6 +109,8 @@ struct TreeBufs {
     PNode *pnodes = nullptr;
     MNode *mnodes = nullptr;
     int2 *mrange = nullptr;
+    int2 *tlink = nullptr;          // list walk: (first, children) of inner nodes, (~lo, hi) of leaves
+    uint32_t *walk_ctr = nullptr;   // list walk: next group to take (persistent warps)
     int32_t *leaves = nullptr;      // sorted position of every leaf's first star
     int32_t *targets = nullptr;     // sorted positions of the stars a restricted walk evaluates
     // forest: systems, their geometry, the system of every sorted star, mixed-walk groups
@@ -194,8 +197,9 @@ cudaError_t split_reserve(TreeBufs &b, int64_t n);
 // FP32 upsweep; writes the walk records of the plain walk (PNode) and/or the mixed walk (MNode).
 cudaError_t upsweep_fast(const Launch &L, TreeBufs &b, bool plain_records);
 // Test hook (GBH_FAULT_LINK): points the skip link of every leaf that ends its system's walk
-// (next == -1) back at node 0 in the node table and in both FP32 walk records, so that every walk
-// that reaches that leaf cycles until its step bound stops it. Indices stay in range.
+// (next == -1) back at node 0 in the node table and in both FP32 walk records, and makes node 0
+// that leaf's child for the list walk, so that every walk that reaches that leaf cycles until its
+// step bound stops it. Indices stay in range.
 cudaError_t fault_link(const Launch &L, TreeBufs &b);
 // Fills the FP64 moment fields of the node table from the MNode records (after an FP32 upsweep).
 cudaError_t export_fast_moments(const Launch &L, TreeBufs &b);
@@ -322,5 +326,16 @@ cudaError_t walk_mixed(const Launch &L, const TreeBufs &b, int64_t nstars_cap, f
 cudaError_t walk_mixed_potential(const Launch &L, const TreeBufs &b, int64_t nstars_cap, float eps2, int quad,
                                  double *psi);
 cudaError_t fp32_fma_probe(const Launch &L, int blocks, int iters, float *out);
+// Longest-first order of the next walk's groups of gsize stars, from this walk's group costs.
+cudaError_t lpt_order(const Launch &L, const TreeBufs &b, int gsize);
+
+// ---- walk_lists.cu (the list walk: decoupled traversal and evaluation, 32-star groups) ----
+constexpr int kDefaultListDepth = 48;
+// The largest node-list depth (entries evaluated per flush) of the list walk.
+int list_depth_max(bool exact);
+// Every star, or (targets = true) the stars listed in b.targets; b.group must have been 32 for the
+// build of a forest. Persistent warps; needs b.cap_nodes < 2^29.
+cudaError_t walk_lists(const Launch &L, const TreeBufs &b, float eps2, int quad, double *ax, double *ay, double *az,
+                       int list_depth, bool targets);
 
 }  // namespace gbh

@@ -82,9 +82,10 @@ __device__ __forceinline__ void quad_add(FMom &q, float m, float ex, float ey, f
 // Finishes node r: centre of mass from the reference point and mean offset (or the geometric
 // centre for zero mass), crit2, and the walk records.
 __device__ __forceinline__ void finish_fast(const SysGeo &inf, FMom &q, float rhx, float rhy, float rhz, float rlx,
-                                            float rly, float rlz, float ox, float oy, float oz, uint64_t key, int L,
-                                            const gbh_node *nodes, int32_t r, PNode *pn, MNode *mn, int2 *mr,
-                                            bool plain_records) {
+                                            float rly, float rlz, float ox, float oy, float oz, uint64_t key,
+                                            uint32_t ninfo, const gbh_node *nodes, int32_t r, PNode *pn, MNode *mn,
+                                            int2 *mr, int2 *tl, bool plain_records) {
+    const int L = int(ninfo & 0xffu);
     int sh = 3 * (kMaxLevel - L);
     uint64_t pre = L == 0 ? 0 : key >> sh;
     float cx = ref_minus_centre(rhx, rlx, inf.min_hi[0], inf.min_lo[0], inf.side_hi, inf.side_lo, compact3(pre >> 2), L);
@@ -117,6 +118,8 @@ __device__ __forceinline__ void finish_fast(const SysGeo &inf, FMom &q, float rh
     m.d = make_float4(q.qxz, q.qyz, __int_as_float(first), __int_as_float(next));
     mn[r] = m;
     mr[r] = make_int2(lo, hi);
+    // links of the list walk: (first child, children) of an inner node, (~first star, end) of a leaf
+    tl[r] = first >= 0 ? make_int2(first, int((ninfo >> 8) & 0xffu)) : make_int2(~lo, hi);
 }
 
 __global__ __launch_bounds__(kThreads) void k_upsweep_fast(const uint64_t *__restrict__ keys, const DevInfo *info,
@@ -129,7 +132,8 @@ __global__ __launch_bounds__(kThreads) void k_upsweep_fast(const uint64_t *__res
                                                            float4 *__restrict__ st_off, const gbh_node *nodes,
                                                            const int32_t *__restrict__ n_parent,
                                                            const uint32_t *__restrict__ n_info, int32_t *n_arrive,
-                                                           PNode *pn, MNode *mn, int2 *mr, bool plain_records,
+                                                           PNode *pn, MNode *mn, int2 *mr, int2 *tl,
+                                                           bool plain_records,
                                                            const int32_t *__restrict__ sid_sorted,
                                                            const SysGeo *__restrict__ geo, DevInfo *err_info) {
     int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
@@ -178,7 +182,7 @@ __global__ __launch_bounds__(kThreads) void k_upsweep_fast(const uint64_t *__res
             }
         }
         finish_fast(geo[sid_sorted ? sid_sorted[lo] : 0], q, rh.x, rh.y, rh.z, rl.x, rl.y, rl.z, ox, oy, oz, keys[lo],
-                    int(n_info[r] & 0xffu), nodes, r, pn, mn, mr, plain_records);
+                    n_info[r], nodes, r, pn, mn, mr, tl, plain_records);
         // Each star's offset from the leaf's centre of mass, formed with the operations of the
         // mixed walk's separation (com_hi - star_hi) + (com_lo - star_lo), negated: a star paired
         // with itself then gets a separation of exactly 0 (IEEE addition is sign-symmetric).
@@ -236,7 +240,7 @@ __global__ __launch_bounds__(kThreads) void k_upsweep_fast(const uint64_t *__res
         }
         const int32_t plo = nodes[par].lo;
         finish_fast(geo[sid_sorted ? sid_sorted[plo] : 0], q, ra.x, ra.y, ra.z, rb.x, rb.y, rb.z, ox, oy, oz, keys[plo],
-                    int(n_info[par] & 0xffu), nodes, par, pn, mn, mr, plain_records);
+                    n_info[par], nodes, par, pn, mn, mr, tl, plain_records);
         cur = par;
     }
 }
@@ -269,7 +273,7 @@ cudaError_t upsweep_fast(const Launch &L, TreeBufs &b, bool plain_records) {
     k_upsweep_fast<<<unsigned(nb < 1 ? 1 : nb), kThreads, 0, L.stream>>>(
         b.keys, b.info, b.leaves, cnt, base, b.pre_ref, b.st_hi, b.st_lo, b.st_off, b.nodes, b.n_parent, b.n_info,
         b.n_arrive,
-        b.pnodes, b.mnodes, b.mrange, plain_records, b.nsys > 1 ? b.sid_sorted : nullptr, b.geo, b.info);
+        b.pnodes, b.mnodes, b.mrange, b.tlink, plain_records, b.nsys > 1 ? b.sid_sorted : nullptr, b.geo, b.info);
     ++*L.count;
     return cudaGetLastError();
 }

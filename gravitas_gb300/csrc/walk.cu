@@ -554,8 +554,17 @@ static cudaError_t launch_mixed(const Launch &L, const TreeBufs &b, int64_t nsta
     return launch_mixed_t<kQuad, kSoft, kPot, true>(L, b, nstars_cap, eps2, ax, ay, az, false);
 }
 
+cudaError_t lpt_order(const Launch &L, const TreeBufs &b, int gsize) {
+    k_lpt_order<<<1, kLptThreads, 0, L.stream>>>(b.info, gsize, b.nsys > 1, b.gcost, b.gperm, int32_t(b.cap_groups));
+    ++*L.count;
+    return cudaGetLastError();
+}
+
 cudaError_t walk_mixed(const Launch &L, const TreeBufs &b, int64_t nstars_cap, float eps2, int quad, double *ax,
                        double *ay, double *az, bool targets) {
+    // 32-star groups: the list walk (walk_lists.cu); 64-star groups: the paired walk above
+    if (b.group == 32 && b.cap_nodes < (int64_t(1) << 29))
+        return walk_lists(L, b, eps2, quad, ax, ay, az, b.list_depth, targets);
     bool soft = eps2 > 0.f;
     if (quad && soft) return launch_mixed<true, true>(L, b, nstars_cap, eps2, ax, ay, az, targets);
     if (quad) return launch_mixed<true, false>(L, b, nstars_cap, eps2, ax, ay, az, targets);

@@ -1,0 +1,596 @@
+// walk_lists.cu — the list walk: the mixed-precision FP32 walk with decoupled traversal and
+// evaluation (compiled like walk.cu: FMA contraction on, fast FP32 division and square root).
+//
+// One warp owns a group of up to 32 consecutive Morton-sorted stars, one per lane, and builds the
+// group's interaction lists cooperatively before evaluating them:
+//
+// * Traversal is node-parallel. The warp keeps a stack of sibling ranges (an opened inner node's
+//   children are contiguous in the reference's serial layout, build.go:142-152) in shared memory
+//   and tests up to 32 nodes per step, one per lane, with the opening criterion of the reference
+//   walk (bh.go:116: open when d2 < crit2) taken over every star of the group: a node is accepted
+//   only when no star of the group would open it. The test is the group's bounding box first; a
+//   node the box cannot accept is refined against each star. Both tests add a margin that covers
+//   their FP32 rounding, so every star sees each accepted node exactly where the reference would
+//   accept it, or deeper.
+// * Accepted nodes and the stars of opened leaves are appended (ballot + popc offsets) to two
+//   lists in shared memory, staged as FP32 records relative to the group's origin. When a list
+//   reaches its depth (a knob of gbh_params.list_depth) the warp evaluates it: every lane takes
+//   two list entries at once in packed FP32x2 arithmetic (__ffma2_rn and friends) against its own
+//   star, the records read as broadcasts from shared memory, with no branch and no dependence
+//   between entries.
+// * Persistent warps (one launch of num_SMs x resident blocks) take groups from a counter, longest
+//   first in the order the previous walk's group costs give (k_lpt_order). A walk restricted to a
+//   target list (block steps) takes groups of 32 consecutive list entries; a full list walks
+//   exactly as no list.
+//
+// Precision: positions are FP64 split into hi + lo FP32 parts. The group's origin O is its first
+// star's hi part; a star's or node's offset from O is (hi - O) + lo in FP32, exact for nearby
+// points and relatively accurate for distant ones, and a separation is the difference of two
+// offsets. That is accurate to FP32 rounding of the group's extent; a group whose extent is large
+// against its stars' spacing and the softening (one that straddles a jump of the Morton curve)
+// forms every separation as (hi_j - hi_i) + (lo_j - lo_i) instead, accurate to FP32 rounding of
+// the separation itself. Each star sums each list in FP32 and folds the sum into a Kahan sum.
+#include <cuda_runtime.h>
+
+#include "gbh_internal.cuh"
+
+namespace gbh {
+
+namespace {
+
+constexpr unsigned kFull = 0xffffffffu;
+constexpr int kLwWarps = 2;              // warps per block (shared memory ~10 KB per warp)
+constexpr int kLwThreads = 32 * kLwWarps;
+// Sibling ranges of one depth on the stack were all pushed by one step (ranges are popped only
+// from the deepest level, and a step pushes the children of the nodes it tests, one level deeper),
+// so at most 32 per depth, and depths run from 1 to kMaxLevel.
+constexpr int kStackCap = 32 * (kMaxLevel + 1);
+constexpr int kLevels = kMaxLevel + 3;
+constexpr int kNodeF4 = 224;  // node list buffer, float4 slots (3,584 B)
+constexpr int kSrcF4 = 192;   // source list buffer, float4 slots (3,072 B)
+
+// Record layouts. A pair of list entries (A, B) is stored field by field as (A, B) float pairs,
+// so that one packed FP32x2 operand is one 8-byte half of a float4 read.
+//   node, compact: (x, y | z, m | qxx, qyy | qzz, qxy | qxz, qyz) — 5 float4 per pair
+//   node, exact:   the same with x, y, z the hi parts, then (xlo, ylo | zlo, 0) — 7 float4
+//   source, compact: (x, y | z, m) — 2 float4;  exact: (xhi, yhi | zhi, m | xlo, ylo | zlo, 0) — 4
+// Quadrupole components are stored negated (the term -Q.d / r^5 becomes a fused add).
+template <bool kExact>
+struct Layout {
+    static constexpr int kNodePair = kExact ? 7 : 5;
+    static constexpr int kSrcPair = kExact ? 4 : 2;
+    static constexpr int kNodeCap = 2 * (kNodeF4 / kNodePair);  // entries: 88 compact, 64 exact
+    static constexpr int kSrcCap = 2 * (kSrcF4 / kSrcPair);     // entries: 192 compact, 96 exact
+};
+
+struct __align__(16) WarpMem {
+    float4 nbuf[kNodeF4];
+    float4 sbuf[kSrcF4];
+    float4 tgt[32];              // the group's stars relative to its origin (refined opening tests)
+    uint32_t stack[kStackCap];   // sibling ranges: first | (count - 1) << 29
+    int32_t lvl[kLevels];        // first stack slot of each depth
+    int32_t batch[32];           // the nodes of the current step
+    int32_t owner[32];           // source staging: the lane whose leaf starts at each slot
+};
+
+__device__ __forceinline__ void set_err(DevInfo *info, int where) {
+    atomicExch(&info->err, 1);
+    info->err_where = where;
+}
+
+__device__ __forceinline__ float2 f2(float v) { return make_float2(v, v); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 lo2(float4 v) { return make_float2(v.x, v.y); }
+__device__ __forceinline__ float2 hi2(float4 v) { return make_float2(v.z, v.w); }
+
+// Kahan fold of a list's FP32 sum into the running sum (s, c): true sum = s - c.
+__device__ __forceinline__ void kahan_fold(float &s, float &c, float part) {
+    float y = part - c;
+    float t = s + y;
+    c = (t - s) - y;
+    s = t;
+}
+
+// The group's star, as its lane holds it.
+struct Target {
+    float tx, ty, tz;     // offset from the group origin (compact separations)
+    float hx, hy, hz;     // hi parts (exact separations)
+    float lx, ly, lz;     // lo parts
+};
+
+struct Acc {
+    float2 px, py, pz;    // the current list's sums (entry A, entry B halves)
+    float sx, sy, sz, cx, cy, cz;  // Kahan sums
+    __device__ __forceinline__ void fold() {
+        kahan_fold(sx, cx, px.x + px.y);
+        kahan_fold(sy, cy, py.x + py.y);
+        kahan_fold(sz, cz, pz.x + pz.y);
+        px = py = pz = f2(0.f);
+    }
+};
+
+// Separation (entry - star) along one axis for a pair of entries.
+template <bool kExact>
+__device__ __forceinline__ float2 sep(float2 h, float2 l, float nt, float nh, float nl) {
+    if constexpr (kExact) return add2(add2(h, f2(nh)), add2(l, f2(nl)));
+    else return add2(h, f2(nt));
+}
+
+// Evaluates the node list (count entries, padded to pairs) for the lane's star.
+template <bool kExact, bool kQuad, bool kSoft>
+__device__ __forceinline__ void eval_nodes(const WarpMem &W, int count, const Target &t, float eps2, Acc &a) {
+    using Lay = Layout<kExact>;
+    const float2 e2 = f2(eps2);
+    const int np = (count + 1) >> 1;
+#pragma unroll 2
+    for (int p = 0; p < np; ++p) {
+        const float4 *r = &W.nbuf[p * Lay::kNodePair];
+        const float4 r0 = r[0], r1 = r[1];
+        float2 lx = f2(0.f), ly = f2(0.f), lz = f2(0.f);
+        if constexpr (kExact) {
+            const float4 r5 = r[5], r6 = r[6];
+            lx = lo2(r5);
+            ly = hi2(r5);
+            lz = lo2(r6);
+        }
+        const float2 dx = sep<kExact>(lo2(r0), lx, -t.tx, -t.hx, -t.lx);
+        const float2 dy = sep<kExact>(hi2(r0), ly, -t.ty, -t.hy, -t.ly);
+        const float2 dz = sep<kExact>(lo2(r1), lz, -t.tz, -t.hz, -t.lz);
+        const float2 r2 = fma2(dz, dz, fma2(dy, dy, fma2(dx, dx, e2)));
+        float2 ir;
+        if constexpr (kSoft) {
+            ir = make_float2(rsqrtf(r2.x), rsqrtf(r2.y));
+        } else {  // an accepted node never sits on a star (d2 >= crit2 > 0); kept for safety
+            ir = make_float2(r2.x > 0.f ? rsqrtf(r2.x) : 0.f, r2.y > 0.f ? rsqrtf(r2.y) : 0.f);
+        }
+        const float2 ir2 = mul2(ir, ir);
+        const float2 ir3 = mul2(ir2, ir);
+        const float2 mir3 = mul2(hi2(r1), ir3);
+        if constexpr (kQuad) {
+            const float4 r2a = r[2], r3 = r[3], r4 = r[4];
+            // q = -Q.d (the record holds -Q): qx = -(qxx dx + qxy dy + qxz dz), ...
+            const float2 qx = fma2(lo2(r4), dz, fma2(hi2(r3), dy, mul2(lo2(r2a), dx)));
+            const float2 qy = fma2(hi2(r4), dz, fma2(hi2(r2a), dy, mul2(hi2(r3), dx)));
+            const float2 qz = fma2(lo2(r3), dz, fma2(hi2(r4), dy, mul2(lo2(r4), dx)));
+            const float2 dqd = fma2(dz, qz, fma2(dy, qy, mul2(dx, qx)));  // -(d.Q.d)
+            const float2 ir5 = mul2(ir3, ir2);
+            // f = m / r^3 + 5/2 (d.Q.d) / r^7;  a += f d - Q.d / r^5 (bh.go:117-133)
+            const float2 f = fma2(mul2(dqd, mul2(ir5, ir2)), f2(-2.5f), mir3);
+            a.px = fma2(ir5, qx, fma2(f, dx, a.px));
+            a.py = fma2(ir5, qy, fma2(f, dy, a.py));
+            a.pz = fma2(ir5, qz, fma2(f, dz, a.pz));
+        } else {
+            a.px = fma2(mir3, dx, a.px);
+            a.py = fma2(mir3, dy, a.py);
+            a.pz = fma2(mir3, dz, a.pz);
+        }
+    }
+    a.fold();
+}
+
+// Evaluates the source list (leaf stars, count entries padded to pairs): m / (r^2 + eps^2)^(3/2).
+// A star paired with itself has a separation of exactly 0 (its record and its target are formed by
+// the same operations), which adds 0 with softening, as skipping j == self does (bh.go:142-144);
+// without softening r2 = 0 is masked.
+template <bool kExact, bool kSoft>
+__device__ __forceinline__ void eval_sources(const WarpMem &W, int count, const Target &t, float eps2, Acc &a) {
+    using Lay = Layout<kExact>;
+    const float2 e2 = f2(eps2);
+    const int np = (count + 1) >> 1;
+#pragma unroll 4
+    for (int p = 0; p < np; ++p) {
+        const float4 *r = &W.sbuf[p * Lay::kSrcPair];
+        const float4 r0 = r[0], r1 = r[1];
+        float2 lx = f2(0.f), ly = f2(0.f), lz = f2(0.f);
+        if constexpr (kExact) {
+            const float4 r2a = r[2], r3 = r[3];
+            lx = lo2(r2a);
+            ly = hi2(r2a);
+            lz = lo2(r3);
+        }
+        const float2 dx = sep<kExact>(lo2(r0), lx, -t.tx, -t.hx, -t.lx);
+        const float2 dy = sep<kExact>(hi2(r0), ly, -t.ty, -t.hy, -t.ly);
+        const float2 dz = sep<kExact>(lo2(r1), lz, -t.tz, -t.hz, -t.lz);
+        const float2 r2 = fma2(dz, dz, fma2(dy, dy, fma2(dx, dx, e2)));
+        float2 ir;
+        if constexpr (kSoft) {
+            ir = make_float2(rsqrtf(r2.x), rsqrtf(r2.y));
+        } else {
+            ir = make_float2(r2.x > 0.f ? rsqrtf(r2.x) : 0.f, r2.y > 0.f ? rsqrtf(r2.y) : 0.f);
+        }
+        const float2 f = mul2(mul2(hi2(r1), ir), mul2(ir, ir));
+        a.px = fma2(f, dx, a.px);
+        a.py = fma2(f, dy, a.py);
+        a.pz = fma2(f, dz, a.pz);
+    }
+    a.fold();
+}
+
+// Writes field f of list entry e into a pair-interleaved record buffer.
+__device__ __forceinline__ void put(float4 *buf, int pair_f4, int e, int f, float v) {
+    reinterpret_cast<float *>(buf + (e >> 1) * pair_f4)[2 * f + (e & 1)] = v;
+}
+
+// Odd counts: entry B of the last pair becomes a copy of A with zero mass and quadrupole (its
+// separation is A's, so its terms are exactly zero).
+template <int kPairF4, int kFields>
+__device__ __forceinline__ void pad_pair(float4 *buf, int count, int lane, int mass_field, int q_first, int q_last) {
+    if (!(count & 1)) return;
+    if (lane < kFields) {
+        float *r = reinterpret_cast<float *>(buf + (count >> 1) * kPairF4);
+        const bool zero = lane == mass_field || (lane >= q_first && lane <= q_last);
+        r[2 * lane + 1] = zero ? 0.f : r[2 * lane];
+    }
+    __syncwarp();
+}
+
+struct GroupOut {
+    uint32_t cost;
+    bool ok;
+};
+
+// Walks one group with the given separation form; a is zeroed by the caller.
+template <bool kExact, bool kQuad, bool kSoft>
+__device__ __forceinline__ GroupOut walk_group(WarpMem &W, int lane, int cnt, int32_t root, const Target &t, float Ox,
+                                            float Oy, float Oz, float bx0, float by0, float bz0, float bx1,
+                                            float by1, float bz1, float ext, float eps2, int node_depth,
+                                            int src_depth, const MNode *__restrict__ nodes,
+                                            const int2 *__restrict__ tlink, const float4 *__restrict__ st_hi,
+                                            const float4 *__restrict__ st_lo, int32_t nn, int32_t ns,
+                                            DevInfo *err_info, Acc &a) {
+    using Lay = Layout<kExact>;
+    constexpr int kNodeFields = kExact ? 13 : 10;
+    constexpr int kSrcFields = kExact ? 7 : 4;
+    const unsigned lt = (1u << lane) - 1u;
+    // one step appends at most 32 entries to a list below its depth
+    if (node_depth > Lay::kNodeCap - 32) node_depth = Lay::kNodeCap - 32;
+    if (src_depth > Lay::kSrcCap - 32) src_depth = Lay::kSrcCap - 32;
+    int ncount = 0, scount = 0, sp = 1, dtop = 0;
+    uint32_t tested = 0, acc_nodes = 0, pairs = 0;
+    if (lane == 0) {
+        W.stack[0] = uint32_t(root);  // the root alone (count 1)
+        W.lvl[0] = 0;
+    }
+    __syncwarp();
+    auto flush_nodes = [&]() {
+        pad_pair<Lay::kNodePair, kNodeFields>(W.nbuf, ncount, lane, 3, 4, 9);
+        eval_nodes<kExact, kQuad, kSoft>(W, ncount, t, eps2, a);
+        __syncwarp();
+        ncount = 0;
+    };
+    auto flush_sources = [&]() {
+        pad_pair<Lay::kSrcPair, kSrcFields>(W.sbuf, scount, lane, 3, 32, 32);
+        eval_sources<kExact, kSoft>(W, scount, t, eps2, a);
+        __syncwarp();
+        scount = 0;
+    };
+    while (sp > 0) {
+        // ---- pop the sibling ranges of the deepest level, at most 32 nodes
+        const int avail = sp - W.lvl[dtop];
+        const int nr = avail < 32 ? avail : 32;
+        uint32_t e = 0;
+        int c = 0;
+        if (lane < nr) {
+            e = W.stack[sp - 1 - lane];
+            c = int(e >> 29) + 1;
+        }
+        int incl = c;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(kFull, incl, o);
+            if (lane >= o) incl += y;
+        }
+        const int r = __popc(__ballot_sync(kFull, lane < nr && incl <= 32));
+        const int total = __shfl_sync(kFull, incl, r - 1);
+        if (lane < r) {
+            const int32_t first = int32_t(e & 0x1fffffffu);
+            for (int i = 0; i < c; ++i) W.batch[incl - c + i] = first + i;
+        }
+        __syncwarp();
+        sp -= r;
+        const int depth = dtop;
+        const int32_t node = lane < total ? W.batch[lane] : -1;
+        tested += uint32_t(total);
+        // ---- test
+        bool acc = false, open_in = false, open_leaf = false, bad = false;
+        int2 tl = make_int2(0, 0);
+        float4 na = make_float4(0.f, 0.f, 0.f, 0.f), nb = na;
+        float cx = 0.f, cy = 0.f, cz = 0.f;
+        if (node >= 0) {
+            if (node >= nn) {
+                bad = true;
+            } else {
+                na = nodes[node].a;
+                nb = nodes[node].b;
+                tl = tlink[node];
+                cx = (na.x - Ox) + nb.x;
+                cy = (na.y - Oy) + nb.y;
+                cz = (na.z - Oz) + nb.z;
+                // Margin for FP32 rounding: every offset (node or star, from O) carries an error
+                // below 2^-23 of its size, so accept only when the computed distance exceeds crit
+                // by sqrt(3) 2^-22 (|c| + extent) and the squared distance its bound by 2^-21; crit
+                // itself (from the FP32 moments) gets 2^-20 against the FP64 moments' value.
+                const float crit = sqrtf(na.w) * (1.f + 9.6e-7f);
+                const float slack = (fmaxf(fabsf(cx), fmaxf(fabsf(cy), fabsf(cz))) + ext) * 4.2e-7f;
+                const float lim = (crit + slack) * (crit + slack) * (1.f + 4.8e-7f);
+                const float qx = fmaxf(0.f, fmaxf(bx0 - cx, cx - bx1));
+                const float qy = fmaxf(0.f, fmaxf(by0 - cy, cy - by1));
+                const float qz = fmaxf(0.f, fmaxf(bz0 - cz, cz - bz1));
+                acc = qx * qx + qy * qy + qz * qz >= lim;
+                if (!acc) {  // refine against every star of the group
+                    bool far = true;
+                    for (int j = 0; j < cnt && far; ++j) {
+                        const float4 s = W.tgt[j];
+                        const float ex = cx - s.x, ey = cy - s.y, ez = cz - s.z;
+                        far = ex * ex + ey * ey + ez * ez >= lim;
+                    }
+                    acc = far;
+                }
+                if (!acc) {
+                    if (tl.x >= 0) {
+                        open_in = true;
+                        bad = tl.y < 1 || tl.y > 8 || tl.x + tl.y > nn;
+                    } else {
+                        open_leaf = true;
+                        bad = ~tl.x < 0 || tl.y > ns || ~tl.x >= tl.y;
+                    }
+                }
+            }
+        }
+        const unsigned mi = __ballot_sync(kFull, open_in);
+        const int npush = __popc(mi);
+        if (__any_sync(kFull, bad) || tested > uint32_t(nn) + 32u || sp + npush > kStackCap ||
+            (npush && depth + 1 >= kLevels)) {
+            if (lane == 0) set_err(err_info, 8);  // a corrupt tree: stop this group
+            return GroupOut{0, false};
+        }
+        // ---- push the children of opened inner nodes (one level deeper)
+        if (npush) {
+            if (open_in) W.stack[sp + __popc(mi & lt)] = uint32_t(tl.x) | uint32_t(tl.y - 1) << 29;
+            if (lane == 0) W.lvl[depth + 1] = sp;
+            sp += npush;
+            dtop = depth + 1;
+        }
+        __syncwarp();
+        if (!npush) {
+            while (dtop > 0 && W.lvl[dtop] >= sp) --dtop;
+        }
+        // ---- append accepted nodes to the node list
+        const unsigned ma = __ballot_sync(kFull, acc);
+        if (ma) {
+            if (acc) {
+                const int en = ncount + __popc(ma & lt);
+                const float4 qc = nodes[node].c, qd = nodes[node].d;
+                constexpr int P = Lay::kNodePair;
+                if constexpr (kExact) {
+                    put(W.nbuf, P, en, 0, na.x);
+                    put(W.nbuf, P, en, 1, na.y);
+                    put(W.nbuf, P, en, 2, na.z);
+                    put(W.nbuf, P, en, 10, nb.x);
+                    put(W.nbuf, P, en, 11, nb.y);
+                    put(W.nbuf, P, en, 12, nb.z);
+                } else {
+                    put(W.nbuf, P, en, 0, cx);
+                    put(W.nbuf, P, en, 1, cy);
+                    put(W.nbuf, P, en, 2, cz);
+                }
+                put(W.nbuf, P, en, 3, nb.w);
+                put(W.nbuf, P, en, 4, -qc.x);  // qxx
+                put(W.nbuf, P, en, 5, -qc.y);  // qyy
+                put(W.nbuf, P, en, 6, -qc.z);  // qzz
+                put(W.nbuf, P, en, 7, -qc.w);  // qxy
+                put(W.nbuf, P, en, 8, -qd.x);  // qxz
+                put(W.nbuf, P, en, 9, -qd.y);  // qyz
+            }
+            const int nacc = __popc(ma);
+            ncount += nacc;
+            acc_nodes += uint32_t(nacc);
+            __syncwarp();
+            if (ncount >= node_depth) flush_nodes();
+        }
+        // ---- stage the stars of opened leaves into the source list, 32 at a time
+        const unsigned ml = __ballot_sync(kFull, open_leaf);
+        if (ml) {
+            const int lo = open_leaf ? ~tl.x : 0;
+            const int lc = open_leaf ? tl.y - lo : 0;
+            int inc = lc;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int y = __shfl_up_sync(kFull, inc, o);
+                if (lane >= o) inc += y;
+            }
+            const int excl = inc - lc;
+            const int T = __shfl_sync(kFull, inc, 31);
+            pairs += uint32_t(T);
+            for (int cs = 0; cs < T; cs += 32) {
+                const bool mine = open_leaf && excl < cs + 32 && excl + lc > cs;
+                const int p0 = mine ? (excl > cs ? excl - cs : 0) : 0;
+                if (mine) W.owner[p0] = lane;
+                const unsigned starts = __reduce_or_sync(kFull, mine ? 1u << p0 : 0u);
+                __syncwarp();
+                const int j = cs + lane;
+                const int pos = 31 - __clz(starts & (kFull >> (31 - lane)));
+                const int ow = j < T ? W.owner[pos] : 0;
+                const int olo = __shfl_sync(kFull, lo, ow), oex = __shfl_sync(kFull, excl, ow);
+                if (j < T) {
+                    const int32_t star = olo + (j - oex);
+                    const float4 h = st_hi[star], l = st_lo[star];
+                    const int en = scount + lane;
+                    constexpr int P = Lay::kSrcPair;
+                    if constexpr (kExact) {
+                        put(W.sbuf, P, en, 0, h.x);
+                        put(W.sbuf, P, en, 1, h.y);
+                        put(W.sbuf, P, en, 2, h.z);
+                        put(W.sbuf, P, en, 4, l.x);
+                        put(W.sbuf, P, en, 5, l.y);
+                        put(W.sbuf, P, en, 6, l.z);
+                    } else {
+                        put(W.sbuf, P, en, 0, (h.x - Ox) + l.x);
+                        put(W.sbuf, P, en, 1, (h.y - Oy) + l.y);
+                        put(W.sbuf, P, en, 2, (h.z - Oz) + l.z);
+                    }
+                    put(W.sbuf, P, en, 3, h.w);
+                }
+                scount += T - cs < 32 ? T - cs : 32;
+                __syncwarp();
+                if (scount >= src_depth) flush_sources();
+            }
+        }
+    }
+    if (ncount) flush_nodes();
+    if (scount) flush_sources();
+    return GroupOut{(31u * acc_nodes + 12u * pairs) / 16u + tested, true};
+}
+
+template <bool kQuad, bool kSoft>
+__global__ __launch_bounds__(kLwThreads) void k_walk_lists(const DevInfo *info, const MNode *__restrict__ nodes,
+                                                           const int2 *__restrict__ tlink,
+                                                           const float4 *__restrict__ st_hi,
+                                                           const float4 *__restrict__ st_lo,
+                                                           const int32_t *__restrict__ order, float eps, float eps2,
+                                                           double *ax, double *ay, double *az,
+                                                           const int4 *__restrict__ groups,
+                                                           const int32_t *__restrict__ targets,
+                                                           const int32_t *__restrict__ gperm, int32_t perm_cap,
+                                                           uint32_t *gcost, uint32_t *work_ctr, DevInfo *err_info,
+                                                           int node_depth, int src_depth) {
+    __shared__ WarpMem smem[kLwWarps];
+    WarpMem &W = smem[threadIdx.x >> 5];
+    const int lane = threadIdx.x & 31;
+    const int32_t ns = int32_t(info->nstars);
+    const int32_t nn = int32_t(info->nnodes);
+    const bool forest = groups != nullptr;
+    // a target list (block steps): groups of 32 consecutive entries; else every star
+    const int32_t nt = targets ? int32_t(info->ntargets) : ns;
+    const int32_t ng = nn > 0 ? (forest ? int32_t(info->ngroups) : (nt + 31) / 32) : 0;
+    const bool lpt = gperm && gperm[perm_cap] == ng;
+    for (;;) {
+        int32_t idx = 0;
+        if (lane == 0) idx = int32_t(atomicAdd(work_ctr, 1u));
+        idx = __shfl_sync(kFull, idx, 0);
+        if (idx >= ng) break;
+        const int32_t g = lpt ? gperm[idx] : idx;
+        int32_t base, cnt, root = 0;
+        if (forest) {
+            const int4 ge = groups[g];
+            base = ge.x;
+            cnt = ge.y;
+            root = ge.z;
+        } else {
+            base = g * 32;
+            cnt = nt - base < 32 ? nt - base : 32;
+        }
+        if (cnt <= 0) continue;
+        if (cnt > 32) cnt = 32;
+        const bool valid = lane < cnt;
+        const int32_t k = targets ? targets[base + (valid ? lane : 0)] : base + (valid ? lane : 0);
+        const float4 h = st_hi[k], l = st_lo[k];
+        const float Ox = __shfl_sync(kFull, h.x, 0), Oy = __shfl_sync(kFull, h.y, 0), Oz = __shfl_sync(kFull, h.z, 0);
+        Target t;
+        t.tx = (h.x - Ox) + l.x;
+        t.ty = (h.y - Oy) + l.y;
+        t.tz = (h.z - Oz) + l.z;
+        t.hx = h.x;
+        t.hy = h.y;
+        t.hz = h.z;
+        t.lx = l.x;
+        t.ly = l.y;
+        t.lz = l.z;
+        W.tgt[lane] = make_float4(t.tx, t.ty, t.tz, 0.f);
+        // the group's box, its extent from the origin and the spacing of consecutive stars
+        float bx0 = t.tx, by0 = t.ty, bz0 = t.tz, bx1 = t.tx, by1 = t.ty, bz1 = t.tz;
+        const float nx = __shfl_down_sync(kFull, t.tx, 1), ny = __shfl_down_sync(kFull, t.ty, 1),
+                    nz = __shfl_down_sync(kFull, t.tz, 1);
+        float gap = lane + 1 < cnt ? fmaxf(fabsf(nx - t.tx), fmaxf(fabsf(ny - t.ty), fabsf(nz - t.tz))) : 3.0e38f;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            bx0 = fminf(bx0, __shfl_xor_sync(kFull, bx0, o));
+            by0 = fminf(by0, __shfl_xor_sync(kFull, by0, o));
+            bz0 = fminf(bz0, __shfl_xor_sync(kFull, bz0, o));
+            bx1 = fmaxf(bx1, __shfl_xor_sync(kFull, bx1, o));
+            by1 = fmaxf(by1, __shfl_xor_sync(kFull, by1, o));
+            bz1 = fmaxf(bz1, __shfl_xor_sync(kFull, bz1, o));
+            gap = fminf(gap, __shfl_xor_sync(kFull, gap, o));
+        }
+        const float ext = fmaxf(fmaxf(fmaxf(-bx0, bx1), fmaxf(-by0, by1)), fmaxf(-bz0, bz1));
+        __syncwarp();
+        // Offsets from O carry rounding errors of 2^-24 of the group's extent; separations formed
+        // from them stay accurate while the extent is within 2^12 of the softening or of the
+        // closest consecutive stars. Beyond that (a group across a jump of the Morton curve) the
+        // separations take the hi and lo parts apart.
+        const bool exact = ext > 4096.f * fmaxf(eps, gap);
+        Acc a;
+        a.px = a.py = a.pz = f2(0.f);
+        a.sx = a.sy = a.sz = a.cx = a.cy = a.cz = 0.f;
+        GroupOut r;
+        if (exact)
+            r = walk_group<true, kQuad, kSoft>(W, lane, cnt, root, t, Ox, Oy, Oz, bx0, by0, bz0, bx1, by1, bz1, ext,
+                                                eps2, node_depth, src_depth, nodes, tlink, st_hi, st_lo, nn, ns,
+                                                err_info, a);
+        else
+            r = walk_group<false, kQuad, kSoft>(W, lane, cnt, root, t, Ox, Oy, Oz, bx0, by0, bz0, bx1, by1, bz1, ext,
+                                                 eps2, node_depth, src_depth, nodes, tlink, st_hi, st_lo, nn, ns,
+                                                 err_info, a);
+        __syncwarp();
+        if (!r.ok) break;  // the error flag is set; the host reports GBH_ERR_LIMIT
+        if (gcost && lane == 0) gcost[g] = r.cost;
+        if (valid) {
+            const int32_t o = order[k];
+            ax[o] = double(a.sx) - double(a.cx);
+            ay[o] = double(a.sy) - double(a.cy);
+            az[o] = double(a.sz) - double(a.cz);
+        }
+    }
+}
+
+template <bool kQuad, bool kSoft>
+cudaError_t launch_lists(const Launch &L, const TreeBufs &b, float eps2, double *ax, double *ay, double *az,
+                         int node_depth, int src_depth, bool lpt, bool targets) {
+    static int blocks_per_sm = 0;  // per instantiation; the same on every device of this architecture
+    if (!blocks_per_sm) {
+        cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_walk_lists<kQuad, kSoft>,
+                                                                      kLwThreads, 0);
+        if (e != cudaSuccess) return e;
+        if (blocks_per_sm < 1) blocks_per_sm = 1;
+    }
+    const bool forest = b.nsys > 1;
+    cudaError_t e = cudaMemsetAsync(b.walk_ctr, 0, sizeof(uint32_t), L.stream);
+    if (e != cudaSuccess) return e;
+    const int sms = L.num_sms > 0 ? L.num_sms : 152;
+    k_walk_lists<kQuad, kSoft><<<unsigned(sms * blocks_per_sm), kLwThreads, 0, L.stream>>>(
+        b.info, b.mnodes, b.tlink, b.st_hi, b.st_lo, b.order, sqrtf(eps2), eps2, ax, ay, az,
+        forest ? b.groups : nullptr, targets ? b.targets : nullptr, lpt ? b.gperm : nullptr, int32_t(b.cap_groups),
+        lpt ? b.gcost : nullptr,
+        b.walk_ctr, b.info, node_depth, src_depth);
+    ++*L.count;
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+int list_depth_max(bool exact) { return exact ? Layout<true>::kNodeCap - 32 : Layout<false>::kNodeCap - 32; }
+
+cudaError_t walk_lists(const Launch &L, const TreeBufs &b, float eps2, int quad, double *ax, double *ay, double *az,
+                       int list_depth, bool targets) {
+    // The list depth is the node list's flush threshold (entries per lane and evaluation); the
+    // source list flushes at twice it. Both are capped so that one step's appends always fit; an
+    // exact-separation group uses the smaller of its own cap and the depth.
+    int nd = list_depth > 0 ? list_depth : kDefaultListDepth;
+    if (nd < 2) nd = 2;
+    if (nd > Layout<false>::kNodeCap - 32) nd = Layout<false>::kNodeCap - 32;
+    int sd = 2 * nd;
+    if (sd > Layout<false>::kSrcCap - 32) sd = Layout<false>::kSrcCap - 32;
+    const bool lpt = b.lpt && !targets;  // a target list changes from event to event
+    const bool soft = eps2 > 0.f;
+    cudaError_t e;
+    if (quad && soft) e = launch_lists<true, true>(L, b, eps2, ax, ay, az, nd, sd, lpt, targets);
+    else if (quad) e = launch_lists<true, false>(L, b, eps2, ax, ay, az, nd, sd, lpt, targets);
+    else if (soft) e = launch_lists<false, true>(L, b, eps2, ax, ay, az, nd, sd, lpt, targets);
+    else e = launch_lists<false, false>(L, b, eps2, ax, ay, az, nd, sd, lpt, targets);
+    if (e != cudaSuccess || !lpt) return e;
+    return lpt_order(L, b, 32);
+}
+
+}  // namespace gbh

@@ -54,10 +54,15 @@ enum { GBH_STAR = 0, GBH_BLACK_HOLE = 1, GBH_DARK_MATTER = 2, GBH_GAS = 3 };
 
 /* Tree walk variants. */
 enum {
-    /* Warp-cooperative walk: one warp per group of 64 (or 32, see group_size)
-       Morton-consecutive stars, two per lane in packed FP32x2 arithmetic, FP32
-       separations formed from hi + lo splits of the FP64 positions, compensated
-       per-star accumulation. The default. */
+    /* Warp-cooperative FP32 walk with compensated per-star accumulation and
+       separations formed from hi + lo splits of the FP64 positions; every star
+       sees each accepted node exactly where the reference walk accepts it, or
+       deeper. Two kernels (see group_size): the list walk, one warp per 32
+       Morton-consecutive stars that builds the group's interaction lists with
+       node-parallel opening tests and evaluates them from shared memory two
+       entries at a time in packed FP32x2 arithmetic; and the paired walk, one
+       warp per 64 stars (two per lane) walking the skip links in lockstep. The
+       default. */
     GBH_WALK_MIXED = 0,
     /* One thread per star, all FP32, uncompensated: the CUDA twin of the Metal
        kernel internal/sim/bh/gpu_darwin.go:76-118. */
@@ -76,8 +81,12 @@ typedef struct {
     int32_t monopole_only;   /* drop quadrupoles of accepted nodes (bh.go:34-35) */
     int32_t dark_matter_off; /* dark matter pulls nothing (Params.DarkMatterOff, sim.go:92-98) */
     int32_t walk;            /* GBH_WALK_* */
-    int32_t group_size;      /* stars per warp of GBH_WALK_MIXED: 64 (0 means 64) or 32 */
-    int32_t reserved;        /* zero */
+    int32_t group_size;      /* GBH_WALK_MIXED: 32 the list walk, 64 the paired walk, 0 the list walk
+                                except for a single system of up to 21 64-star groups per SM
+                                (below about 200,000 stars on a GB300), where the paired walk
+                                shares each group's walk among several warps (GBH_CFG_NO_SPLIT) */
+    int32_t list_depth;      /* list walk: node-list entries evaluated per pass, 2 to 56 (0 means 48;
+                                source lists take twice as many, up to 160) */
     double c;                /* speed of light of the steps (Params.C): 0 Newtonian; > 0 drifts by
                                 u / gamma (sim.go:315-343) and uses Paczynski-Wiita star-hole
                                 pairs in the hole-aware step (pair.go:26-35) */
@@ -319,7 +328,7 @@ typedef struct {
     double rms_err;     /* RMS of the per-body relative force error on the sample */
     double p99_err;     /* 99th percentile of the same */
     int32_t meets;      /* rms_err <= rms_bound */
-    int32_t reserved;
+    int32_t list_depth; /* list walk (group 32): its node-list depth; 0 for the other walks */
 } gbh_tune_entry;
 
 /*
@@ -329,7 +338,8 @@ typedef struct {
  * the shortest median force evaluation (reps timed runs, CUDA events) among those whose RMS
  * relative force error, on `sample` evenly spaced alive stars against the FP64 direct sum
  * over each star's own system, is at most rms_bound. NULL or empty lists take the defaults
- * theta {0.4, 0.5, 0.7}, leaf {4, 8, 16, 32}, group {64, 32}; sample <= 0 means 1024 and
+ * theta {0.4, 0.5, 0.7}, leaf {4, 8, 16, 32}, group {64, 32}, and for group 32 the list
+ * depths {24, 48} unless base->list_depth is set; sample <= 0 means 1024 and
  * reps <= 0 means 3. Every candidate is written to table (up to table_cap) and counted in
  * *ntable. If none meets the bound, *best is the most accurate one and the call returns
  * GBH_ERR_LIMIT. The resident accelerations are left stale (the next step recomputes them).

@@ -175,16 +175,16 @@ def test_non_finite_inputs_of_a_forest_system_are_rejected():
         assert ei.value.code == abi.ERR_ARG
 
 
-@pytest.mark.parametrize("walk,kernel,flags", [("mixed", 4, 0), ("mixed", 4, abi.CFG_NO_SPLIT), ("plain", 3, 0),
-                                               ("fp64", 1, 0)])
-def test_walk_step_bound_stops_a_walk_on_a_corrupt_tree(walk, kernel, flags):
+@pytest.mark.parametrize("walk,group,kernel,flags", [("mixed", 64, 4, 0), ("mixed", 64, 4, abi.CFG_NO_SPLIT),
+                                                     ("mixed", 32, 8, 0), ("plain", 0, 3, 0), ("fp64", 0, 1, 0)])
+def test_walk_step_bound_stops_a_walk_on_a_corrupt_tree(walk, group, kernel, flags):
     """With the corrupt-link hook armed (GBH_FAULT_LINK when the context is created), the next
     tree's last leaf links back to node 0: every walk then cycles until its device-side step bound
     stops it, sets the error flag and the call returns GBH_ERR_LIMIT naming the walk kernel. The
     hook fires once, and the next call on the same context gives exactly the results of a fresh
     context. Indices stay in range, so the cycle is bounded work, not a fault."""
     s = ics.plummer(4096, seed=5)
-    par = abi.make_params(0.5, 0.01, 8, False, False, walk)
+    par = abi.make_params(0.5, 0.01, 8, False, False, walk, group_size=group)
     with abi.Context(0, flags) as c0:
         want = forces(c0, s, par)
     os.environ["GBH_FAULT_LINK"] = "1"

@@ -142,11 +142,11 @@ def test_autotune_on_a_forest_meets_the_bound(ctx):
     base = abi.make_params(0.5, 0.01, 8, False, False, "mixed")
     best, table = ctx.autotune(base, thetas=[0.4, 0.7], leaves=[8, 16], groups=[64, 32], rms_bound=2e-3,
                                sample=512, reps=2, strict=True)
-    assert len(table) == 8
+    assert len(table) == 12  # group 64, and group 32 (the list walk) at two list depths
     meets = [e for e in table if e["meets"]]
     assert meets and min(e["ms"] for e in meets) == min(
-        e["ms"] for e in meets if (e["theta"], e["leaf_size"], e["group_size"]) ==
-        (best.theta, best.leaf_size, best.group_size))
+        e["ms"] for e in meets if (e["theta"], e["leaf_size"], e["group_size"], e["list_depth"]) ==
+        (best.theta, best.leaf_size, best.group_size, best.list_depth))
     # the chosen parameters step the forest, and its forces meet the bound per system
     ctx.call("gbh_state_step", best, 1e-3, 1)
     ctx.call("gbh_state_accelerations", best)

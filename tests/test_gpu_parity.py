@@ -214,10 +214,11 @@ def test_walks_are_deterministic(ctx, walk):
     assert np.array_equal(a, b)
 
 
-@pytest.mark.parametrize("n,group,scene", [(20000, 64, "galaxy"), (100000, 64, "galaxy"), (100000, 32, "galaxy"),
-                                           (700, 64, "galaxy"), (20000, 64, "disk")])
+@pytest.mark.parametrize("n,group,scene", [(20000, 64, "galaxy"), (100000, 64, "galaxy"), (700, 64, "galaxy"),
+                                           (20000, 64, "disk")])
 def test_split_walk_adds_the_same_interactions(ctx, n, group, scene):
-    """With few groups each group's walk is split over several warps by source-star range. The
+    """With few groups each group's walk of the paired walk (64-star groups) is split over several
+    warps by source-star range (the list walk never splits). The
     parts together add exactly the unsplit walk's interactions, in another order: the split
     forces equal the unsplit ones to FP32 summation rounding (global relative norm <= 1e-6,
     every star <= 1e-4), are as accurate against the FP64 direct sum, and repeat bit for bit."""
@@ -519,13 +520,13 @@ def test_autotune_single_system(ctx):
              P(s["mass"]), None, None)
     base = abi.make_params(0.5, 0.01, 8, False, False, "mixed")
     best, table = ctx.autotune(base, rms_bound=2e-3, sample=1024, reps=2, strict=True)
-    assert len(table) == 3 * 4 * 2
-    assert {(e["theta"], e["leaf_size"], e["group_size"]) for e in table} == {
-        (t, l, g) for t in (0.4, 0.5, 0.7) for l in (4, 8, 16, 32) for g in (32, 64)}
+    assert len(table) == 3 * 4 * 3  # group 64, and group 32 (the list walk) at list depths 24 and 48
+    assert {(e["theta"], e["leaf_size"], e["group_size"], e["list_depth"]) for e in table} == {
+        (t, l, g, d) for t in (0.4, 0.5, 0.7) for l in (4, 8, 16, 32) for g, d in ((64, 0), (32, 24), (32, 48))}
     for e in table:  # the error estimate does not depend on the timing
         assert 0 < e["rms_err"] < 2e-2 and e["ms"] > 0 and e["build_ms"] > 0 and e["walk_ms"] > 0
-    chosen = [e for e in table if (e["theta"], e["leaf_size"], e["group_size"]) ==
-              (best.theta, best.leaf_size, best.group_size)][0]
+    chosen = [e for e in table if (e["theta"], e["leaf_size"], e["group_size"], e["list_depth"]) ==
+              (best.theta, best.leaf_size, best.group_size, best.list_depth)][0]
     assert chosen["meets"] and chosen["ms"] == min(e["ms"] for e in table if e["meets"])
     # an unreachable bound: the most accurate candidate and GBH_ERR_LIMIT
     best2, table2 = ctx.autotune(base, thetas=[0.7], leaves=[16], groups=[64], rms_bound=1e-9, sample=64, reps=1)
