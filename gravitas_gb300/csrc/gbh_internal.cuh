@@ -75,6 +75,15 @@ struct __align__(16) MNode {
     float4 a, b, c, d;
 };
 
+// List-walk node: a = (com_hi.xyz, crit), b = (com_lo.xyz, link), c = -(qxx, qyy, qzz, qxy),
+// d = (-qxz, -qyz, m, leaf end). crit = 2 half / theta + |com - centre| (the square root of
+// MNode's crit2), negated for a leaf. link (as bits) = first | (children - 1) << 29 for an inner
+// node (its children are [first, first + children) in the reference layout), lo for a leaf of
+// stars [lo, end).
+struct __align__(16) LNode {
+    float4 a, b, c, d;
+};
+
 // Device buffers of the tree path (all owned by the context).
 struct TreeBufs {
     int64_t cap_n = 0;      // bodies
@@ -109,7 +118,7 @@ struct TreeBufs {
     PNode *pnodes = nullptr;
     MNode *mnodes = nullptr;
     int2 *mrange = nullptr;
-    int2 *tlink = nullptr;          // list walk: (first, children) of inner nodes, (~lo, hi) of leaves
+    LNode *lnode = nullptr;         // list-walk records
     uint32_t *walk_ctr = nullptr;   // list walk: next group to take (persistent warps)
     int32_t *leaves = nullptr;      // sorted position of every leaf's first star
     int32_t *targets = nullptr;     // sorted positions of the stars a restricted walk evaluates

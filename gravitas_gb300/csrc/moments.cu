@@ -84,7 +84,7 @@ __device__ __forceinline__ void quad_add(FMom &q, float m, float ex, float ey, f
 __device__ __forceinline__ void finish_fast(const SysGeo &inf, FMom &q, float rhx, float rhy, float rhz, float rlx,
                                             float rly, float rlz, float ox, float oy, float oz, uint64_t key,
                                             uint32_t ninfo, const gbh_node *nodes, int32_t r, PNode *pn, MNode *mn,
-                                            int2 *mr, int2 *tl, bool plain_records) {
+                                            int2 *mr, LNode *ln, bool plain_records) {
     const int L = int(ninfo & 0xffu);
     int sh = 3 * (kMaxLevel - L);
     uint64_t pre = L == 0 ? 0 : key >> sh;
@@ -118,8 +118,14 @@ __device__ __forceinline__ void finish_fast(const SysGeo &inf, FMom &q, float rh
     m.d = make_float4(q.qxz, q.qyz, __int_as_float(first), __int_as_float(next));
     mn[r] = m;
     mr[r] = make_int2(lo, hi);
-    // links of the list walk: (first child, children) of an inner node, (~first star, end) of a leaf
-    tl[r] = first >= 0 ? make_int2(first, int((ninfo >> 8) & 0xffu)) : make_int2(~lo, hi);
+    // the list walk's record (the link packs the children's range; the caller keeps nodes < 2^29)
+    const uint32_t link = first >= 0 ? uint32_t(first) | ((((ninfo >> 8) & 0xffu) - 1u) & 7u) << 29 : uint32_t(lo);
+    LNode l;
+    l.a = make_float4(q.hx, q.hy, q.hz, first >= 0 ? crit : -crit);  // the sign marks a leaf
+    l.b = make_float4(q.lx, q.ly, q.lz, __uint_as_float(link));
+    l.c = make_float4(-q.qxx, -q.qyy, -q.qzz, -q.qxy);
+    l.d = make_float4(-q.qxz, -q.qyz, q.m, __int_as_float(hi));
+    ln[r] = l;
 }
 
 __global__ __launch_bounds__(kThreads) void k_upsweep_fast(const uint64_t *__restrict__ keys, const DevInfo *info,
@@ -132,7 +138,7 @@ __global__ __launch_bounds__(kThreads) void k_upsweep_fast(const uint64_t *__res
                                                            float4 *__restrict__ st_off, const gbh_node *nodes,
                                                            const int32_t *__restrict__ n_parent,
                                                            const uint32_t *__restrict__ n_info, int32_t *n_arrive,
-                                                           PNode *pn, MNode *mn, int2 *mr, int2 *tl,
+                                                           PNode *pn, MNode *mn, int2 *mr, LNode *ln,
                                                            bool plain_records,
                                                            const int32_t *__restrict__ sid_sorted,
                                                            const SysGeo *__restrict__ geo, DevInfo *err_info) {
@@ -182,7 +188,7 @@ __global__ __launch_bounds__(kThreads) void k_upsweep_fast(const uint64_t *__res
             }
         }
         finish_fast(geo[sid_sorted ? sid_sorted[lo] : 0], q, rh.x, rh.y, rh.z, rl.x, rl.y, rl.z, ox, oy, oz, keys[lo],
-                    n_info[r], nodes, r, pn, mn, mr, tl, plain_records);
+                    n_info[r], nodes, r, pn, mn, mr, ln, plain_records);
         // Each star's offset from the leaf's centre of mass, formed with the operations of the
         // mixed walk's separation (com_hi - star_hi) + (com_lo - star_lo), negated: a star paired
         // with itself then gets a separation of exactly 0 (IEEE addition is sign-symmetric).
@@ -240,7 +246,7 @@ __global__ __launch_bounds__(kThreads) void k_upsweep_fast(const uint64_t *__res
         }
         const int32_t plo = nodes[par].lo;
         finish_fast(geo[sid_sorted ? sid_sorted[plo] : 0], q, ra.x, ra.y, ra.z, rb.x, rb.y, rb.z, ox, oy, oz, keys[plo],
-                    n_info[par], nodes, par, pn, mn, mr, tl, plain_records);
+                    n_info[par], nodes, par, pn, mn, mr, ln, plain_records);
         cur = par;
     }
 }
@@ -273,7 +279,7 @@ cudaError_t upsweep_fast(const Launch &L, TreeBufs &b, bool plain_records) {
     k_upsweep_fast<<<unsigned(nb < 1 ? 1 : nb), kThreads, 0, L.stream>>>(
         b.keys, b.info, b.leaves, cnt, base, b.pre_ref, b.st_hi, b.st_lo, b.st_off, b.nodes, b.n_parent, b.n_info,
         b.n_arrive,
-        b.pnodes, b.mnodes, b.mrange, b.tlink, plain_records, b.nsys > 1 ? b.sid_sorted : nullptr, b.geo, b.info);
+        b.pnodes, b.mnodes, b.mrange, b.lnode, plain_records, b.nsys > 1 ? b.sid_sorted : nullptr, b.geo, b.info);
     ++*L.count;
     return cudaGetLastError();
 }

@@ -1430,7 +1430,7 @@ static cudaError_t scan_dyn(const Launch &L, const uint32_t *in, uint32_t *out, 
 void tree_free(TreeBufs &b) {
     void *ptrs[] = {b.flag, b.bbox_part, b.keys, b.keys_alt, b.order, b.order_alt, b.hist, b.sx, b.sy, b.sz, b.sm,
                     b.st_hi, b.st_lo, b.st_off, b.chain_cnt, b.leaves, b.targets, b.geo, b.sid_sorted, b.groups, b.gcost, b.gperm, b.pre_parent, b.pre_info, b.pre_nchild, b.pre_mask, b.pre_ref, b.nodes,
-                    b.n_parent, b.n_info, b.n_arrive, b.pnodes, b.mnodes, b.mrange, b.tlink, b.walk_ctr, b.scan_tmp, b.info, b.part_acc};
+                    b.n_parent, b.n_info, b.n_arrive, b.pnodes, b.mnodes, b.mrange, b.lnode, b.walk_ctr, b.scan_tmp, b.info, b.part_acc};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     b = TreeBufs{};
@@ -1501,7 +1501,7 @@ cudaError_t tree_alloc(TreeBufs &b, int64_t n, int leaf, int32_t nsys) {
     GBH_ALLOC(b.pnodes, cnodes);
     GBH_ALLOC(b.mnodes, cnodes);
     GBH_ALLOC(b.mrange, cnodes);
-    GBH_ALLOC(b.tlink, cnodes);
+    GBH_ALLOC(b.lnode, cnodes);
     GBH_ALLOC(b.walk_ctr, 16);
     GBH_ALLOC(b.scan_tmp, scan_cap);
     GBH_ALLOC(b.info, 1);
@@ -1644,20 +1644,21 @@ cudaError_t tree_build(const Launch &L, TreeBufs &b, int64_t n, const double *px
 
 namespace {
 __global__ __launch_bounds__(kThreads) void k_fault_link(const DevInfo *info, gbh_node *nodes, PNode *pnodes,
-                                                         MNode *mnodes, int2 *tlink, int64_t cap) {
+                                                         MNode *mnodes, LNode *lnode, int64_t cap) {
     const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= info->nnodes || i >= cap) return;
     if (nodes[i].next != -1 || nodes[i].first != -1) return;
     nodes[i].next = 0;
     pnodes[i].links.y = 0;
     mnodes[i].d.w = __int_as_float(0);
-    tlink[i] = make_int2(0, 1);  // the list walk: the leaf becomes an inner node whose child is node 0
+    lnode[i].a.w = fabsf(lnode[i].a.w);  // the list walk: the leaf becomes an inner node whose child is node 0
+    lnode[i].b.w = __int_as_float(0);
 }
 }  // namespace
 
 cudaError_t fault_link(const Launch &L, TreeBufs &b) {
     k_fault_link<<<blocks_for(b.cap_nodes, kThreads), kThreads, 0, L.stream>>>(b.info, b.nodes, b.pnodes, b.mnodes,
-                                                                               b.tlink, b.cap_nodes);
+                                                                               b.lnode, b.cap_nodes);
     GBH_LAUNCH_CHECK();
     return cudaSuccess;
 }

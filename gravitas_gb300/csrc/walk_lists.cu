@@ -66,11 +66,10 @@ struct Layout {
 struct __align__(16) WarpMem {
     float4 nbuf[kNodeF4];
     float4 sbuf[kSrcF4];
-    float4 tgt[32];              // the group's stars relative to its origin (refined opening tests)
     uint32_t stack[kStackCap];   // sibling ranges: first | (count - 1) << 29
     int32_t lvl[kLevels];        // first stack slot of each depth
-    int32_t batch[32];           // the nodes of the current step
-    int32_t owner[32];           // source staging: the lane whose leaf starts at each slot
+    float4 rq[32];               // the nodes of a step that the box test keeps, pair-interleaved
+    int32_t owner[32];           // source staging: the lane whose leaf run starts at each slot
 };
 
 __device__ __forceinline__ void set_err(DevInfo *info, int where) {
@@ -233,27 +232,27 @@ struct GroupOut {
 
 // Walks one group with the given separation form; a is zeroed by the caller.
 template <bool kExact, bool kQuad, bool kSoft>
-__device__ __forceinline__ GroupOut walk_group(WarpMem &W, int lane, int cnt, int32_t root, const Target &t, float Ox,
-                                            float Oy, float Oz, float bx0, float by0, float bz0, float bx1,
-                                            float by1, float bz1, float ext, float eps2, int node_depth,
-                                            int src_depth, const MNode *__restrict__ nodes,
-                                            const int2 *__restrict__ tlink, const float4 *__restrict__ st_hi,
-                                            const float4 *__restrict__ st_lo, int32_t nn, int32_t ns,
-                                            DevInfo *err_info, Acc &a) {
+__device__ __forceinline__ GroupOut walk_group(WarpMem &W, int lane, int32_t root, const Target &t, float Ox,
+                                               float Oy, float Oz, float bx0, float by0, float bz0, float bx1,
+                                               float by1, float bz1, float ext, float eps2, int node_depth,
+                                               int src_depth, const LNode *__restrict__ nodes,
+                                               const float4 *__restrict__ st_hi, const float4 *__restrict__ st_lo,
+                                               int32_t nn, int32_t ns, DevInfo *err_info, Acc &a) {
     using Lay = Layout<kExact>;
     constexpr int kNodeFields = kExact ? 13 : 10;
     constexpr int kSrcFields = kExact ? 7 : 4;
-    const unsigned lt = (1u << lane) - 1u;
+    const unsigned lt = (1u << lane) - 1u, upto = kFull >> (31 - lane);
     // one step appends at most 32 entries to a list below its depth
     if (node_depth > Lay::kNodeCap - 32) node_depth = Lay::kNodeCap - 32;
     if (src_depth > Lay::kSrcCap - 32) src_depth = Lay::kSrcCap - 32;
     int ncount = 0, scount = 0, sp = 1, dtop = 0;
     uint32_t tested = 0, acc_nodes = 0, pairs = 0;
     if (lane == 0) {
-        W.stack[0] = uint32_t(root);  // the root alone (count 1)
+        W.stack[0] = uint32_t(root);  // the root alone (a range of one)
         W.lvl[0] = 0;
     }
     __syncwarp();
+    const float2 ntx = f2(-t.tx), nty = f2(-t.ty), ntz = f2(-t.tz);
     auto flush_nodes = [&]() {
         pad_pair<Lay::kNodePair, kNodeFields>(W.nbuf, ncount, lane, 3, 4, 9);
         eval_nodes<kExact, kQuad, kSoft>(W, ncount, t, eps2, a);
@@ -267,78 +266,89 @@ __device__ __forceinline__ GroupOut walk_group(WarpMem &W, int lane, int cnt, in
         scount = 0;
     };
     while (sp > 0) {
-        // ---- pop the sibling ranges of the deepest level, at most 32 nodes
+        // ---- pop the sibling ranges of the deepest level, at most 32 nodes; lane j takes node j
+        // of their concatenation (the range holding it is the last one starting at or before j)
         const int avail = sp - W.lvl[dtop];
         const int nr = avail < 32 ? avail : 32;
-        uint32_t e = 0;
-        int c = 0;
-        if (lane < nr) {
-            e = W.stack[sp - 1 - lane];
-            c = int(e >> 29) + 1;
-        }
+        const uint32_t e = lane < nr ? W.stack[sp - 1 - lane] : 0u;
+        const int c = lane < nr ? int(e >> 29) + 1 : 0;
         int incl = c;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
             const int y = __shfl_up_sync(kFull, incl, o);
             if (lane >= o) incl += y;
         }
-        const int r = __popc(__ballot_sync(kFull, lane < nr && incl <= 32));
+        const bool taken = lane < nr && incl <= 32;
+        const int r = __popc(__ballot_sync(kFull, taken));
         const int total = __shfl_sync(kFull, incl, r - 1);
-        if (lane < r) {
-            const int32_t first = int32_t(e & 0x1fffffffu);
-            for (int i = 0; i < c; ++i) W.batch[incl - c + i] = first + i;
-        }
-        __syncwarp();
+        const unsigned starts = __reduce_or_sync(kFull, taken ? 1u << (incl - c) : 0u);
+        const int q = __popc(starts & upto) - 1;
+        const int32_t qfirst = __shfl_sync(kFull, int32_t(e & 0x1fffffffu), q);
+        const int qexcl = __shfl_sync(kFull, incl - c, q);
         sp -= r;
         const int depth = dtop;
-        const int32_t node = lane < total ? W.batch[lane] : -1;
+        const int32_t node = lane < total ? qfirst + (lane - qexcl) : -1;
         tested += uint32_t(total);
-        // ---- test
-        bool acc = false, open_in = false, open_leaf = false, bad = false;
-        int2 tl = make_int2(0, 0);
+        // ---- test: the group's box, then (all lanes at once) every star for what the box keeps
+        bool acc = false, bad = node >= nn;
         float4 na = make_float4(0.f, 0.f, 0.f, 0.f), nb = na;
-        float cx = 0.f, cy = 0.f, cz = 0.f;
-        if (node >= 0) {
-            if (node >= nn) {
-                bad = true;
-            } else {
-                na = nodes[node].a;
-                nb = nodes[node].b;
-                tl = tlink[node];
-                cx = (na.x - Ox) + nb.x;
-                cy = (na.y - Oy) + nb.y;
-                cz = (na.z - Oz) + nb.z;
-                // Margin for FP32 rounding: every offset (node or star, from O) carries an error
-                // below 2^-23 of its size, so accept only when the computed distance exceeds crit
-                // by sqrt(3) 2^-22 (|c| + extent) and the squared distance its bound by 2^-21; crit
-                // itself (from the FP32 moments) gets 2^-20 against the FP64 moments' value.
-                const float crit = sqrtf(na.w) * (1.f + 9.6e-7f);
-                const float slack = (fmaxf(fabsf(cx), fmaxf(fabsf(cy), fabsf(cz))) + ext) * 4.2e-7f;
-                const float lim = (crit + slack) * (crit + slack) * (1.f + 4.8e-7f);
-                const float qx = fmaxf(0.f, fmaxf(bx0 - cx, cx - bx1));
-                const float qy = fmaxf(0.f, fmaxf(by0 - cy, cy - by1));
-                const float qz = fmaxf(0.f, fmaxf(bz0 - cz, cz - bz1));
-                acc = qx * qx + qy * qy + qz * qz >= lim;
-                if (!acc) {  // refine against every star of the group
-                    bool far = true;
-                    for (int j = 0; j < cnt && far; ++j) {
-                        const float4 s = W.tgt[j];
-                        const float ex = cx - s.x, ey = cy - s.y, ez = cz - s.z;
-                        far = ex * ex + ey * ey + ez * ez >= lim;
-                    }
-                    acc = far;
-                }
-                if (!acc) {
-                    if (tl.x >= 0) {
-                        open_in = true;
-                        bad = tl.y < 1 || tl.y > 8 || tl.x + tl.y > nn;
-                    } else {
-                        open_leaf = true;
-                        bad = ~tl.x < 0 || tl.y > ns || ~tl.x >= tl.y;
-                    }
-                }
-            }
+        float cx = 0.f, cy = 0.f, cz = 0.f, lim = 0.f;
+        if (node >= 0 && !bad) {
+            na = nodes[node].a;
+            nb = nodes[node].b;
+            cx = (na.x - Ox) + nb.x;
+            cy = (na.y - Oy) + nb.y;
+            cz = (na.z - Oz) + nb.z;
+            // Margin for FP32 rounding: every offset (node or star, from O) carries an error below
+            // 2^-23 of its size, so accept only when the computed distance exceeds crit by sqrt(3)
+            // 2^-22 (|c| + extent) and the squared distance its bound by 2^-21; crit itself (from
+            // the FP32 moments) gets 2^-20 against the FP64 moments' value.
+            const float slack = (fmaxf(fabsf(cx), fmaxf(fabsf(cy), fabsf(cz))) + ext) * 4.2e-7f;
+            const float crit = fabsf(na.w);
+            const float cr = fmaf(crit, 9.6e-7f, crit) + slack;
+            lim = cr * cr * (1.f + 4.8e-7f);
+            const float qx = fmaxf(0.f, fmaxf(bx0 - cx, cx - bx1));
+            const float qy = fmaxf(0.f, fmaxf(by0 - cy, cy - by1));
+            const float qz = fmaxf(0.f, fmaxf(bz0 - cz, cz - bz1));
+            acc = qx * qx + qy * qy + qz * qz >= lim;
         }
+        const unsigned mref = __ballot_sync(kFull, node >= 0 && !bad && !acc);
+        if (mref) {
+            // the box keeps these nodes: each lane tests its own star against two of them at once
+            // (packed FP32x2); lanes beyond the group repeat the first star
+            const int slot = __popc(mref & lt), nref = __popc(mref);
+            if ((mref >> lane) & 1u) {
+                float *rq = reinterpret_cast<float *>(&W.rq[0]) + (slot >> 1) * 8 + (slot & 1);
+                rq[0] = cx;
+                rq[2] = cy;
+                rq[4] = cz;
+                rq[6] = lim;
+            }
+            if ((nref & 1) && lane == 0) {  // pad the last pair with a copy of its first entry
+                float *rq = reinterpret_cast<float *>(&W.rq[0]) + (nref >> 1) * 8;
+                rq[1] = rq[0];
+                rq[3] = rq[2];
+                rq[5] = rq[4];
+                rq[7] = rq[6];
+            }
+            __syncwarp();
+            unsigned near = 0;
+            for (int p = 0; p < nref; p += 2) {
+                const float4 r0 = reinterpret_cast<const float4 *>(&W.rq[0])[p >> 1 << 1];
+                const float4 r1 = reinterpret_cast<const float4 *>(&W.rq[0])[(p >> 1 << 1) + 1];
+                const float2 ex = add2(lo2(r0), ntx), ey = add2(hi2(r0), nty), ez = add2(lo2(r1), ntz);
+                const float2 d2 = fma2(ez, ez, fma2(ey, ey, mul2(ex, ex)));
+                const float2 ql = hi2(r1);
+                near |= (__any_sync(kFull, d2.x < ql.x) ? 1u : 0u) << p;
+                near |= (__any_sync(kFull, d2.y < ql.y) ? 1u : 0u) << (p + 1);
+            }
+            __syncwarp();
+            if ((mref >> lane) & 1u) acc = !((near >> slot) & 1u);
+        }
+        const uint32_t link = __float_as_uint(nb.w);
+        const bool open_in = node >= 0 && !bad && !acc && !(na.w < 0.f);
+        const bool open_leaf = node >= 0 && !bad && !acc && na.w < 0.f;
+        if (open_in) bad = int64_t(link & 0x1fffffffu) + int64_t(link >> 29) + 1 > nn;
         const unsigned mi = __ballot_sync(kFull, open_in);
         const int npush = __popc(mi);
         if (__any_sync(kFull, bad) || tested > uint32_t(nn) + 32u || sp + npush > kStackCap ||
@@ -346,9 +356,9 @@ __device__ __forceinline__ GroupOut walk_group(WarpMem &W, int lane, int cnt, in
             if (lane == 0) set_err(err_info, 8);  // a corrupt tree: stop this group
             return GroupOut{0, false};
         }
-        // ---- push the children of opened inner nodes (one level deeper)
+        // ---- push the children of opened inner nodes (one level deeper); the link is the range
         if (npush) {
-            if (open_in) W.stack[sp + __popc(mi & lt)] = uint32_t(tl.x) | uint32_t(tl.y - 1) << 29;
+            if (open_in) W.stack[sp + __popc(mi & lt)] = uint32_t(link);
             if (lane == 0) W.lvl[depth + 1] = sp;
             sp += npush;
             dtop = depth + 1;
@@ -376,13 +386,13 @@ __device__ __forceinline__ GroupOut walk_group(WarpMem &W, int lane, int cnt, in
                     put(W.nbuf, P, en, 1, cy);
                     put(W.nbuf, P, en, 2, cz);
                 }
-                put(W.nbuf, P, en, 3, nb.w);
-                put(W.nbuf, P, en, 4, -qc.x);  // qxx
-                put(W.nbuf, P, en, 5, -qc.y);  // qyy
-                put(W.nbuf, P, en, 6, -qc.z);  // qzz
-                put(W.nbuf, P, en, 7, -qc.w);  // qxy
-                put(W.nbuf, P, en, 8, -qd.x);  // qxz
-                put(W.nbuf, P, en, 9, -qd.y);  // qyz
+                put(W.nbuf, P, en, 3, qd.z);  // m
+                put(W.nbuf, P, en, 4, qc.x);  // -qxx
+                put(W.nbuf, P, en, 5, qc.y);  // -qyy
+                put(W.nbuf, P, en, 6, qc.z);  // -qzz
+                put(W.nbuf, P, en, 7, qc.w);  // -qxy
+                put(W.nbuf, P, en, 8, qd.x);  // -qxz
+                put(W.nbuf, P, en, 9, qd.y);  // -qyz
             }
             const int nacc = __popc(ma);
             ncount += nacc;
@@ -393,8 +403,13 @@ __device__ __forceinline__ GroupOut walk_group(WarpMem &W, int lane, int cnt, in
         // ---- stage the stars of opened leaves into the source list, 32 at a time
         const unsigned ml = __ballot_sync(kFull, open_leaf);
         if (ml) {
-            const int lo = open_leaf ? ~tl.x : 0;
-            const int lc = open_leaf ? tl.y - lo : 0;
+            const int lo = open_leaf ? int(link) : 0;
+            const int hi = open_leaf ? __float_as_int(nodes[node].d.w) : 0;
+            if (__any_sync(kFull, open_leaf && (lo < 0 || hi > ns || lo >= hi))) {
+                if (lane == 0) set_err(err_info, 8);
+                return GroupOut{0, false};
+            }
+            const int lc = hi - lo;
             int inc = lc;
 #pragma unroll
             for (int o = 1; o < 32; o <<= 1) {
@@ -405,14 +420,14 @@ __device__ __forceinline__ GroupOut walk_group(WarpMem &W, int lane, int cnt, in
             const int T = __shfl_sync(kFull, inc, 31);
             pairs += uint32_t(T);
             for (int cs = 0; cs < T; cs += 32) {
+                // slot cs + j belongs to the last leaf whose (clipped) run starts at or before it
                 const bool mine = open_leaf && excl < cs + 32 && excl + lc > cs;
-                const int p0 = mine ? (excl > cs ? excl - cs : 0) : 0;
+                const int p0 = excl > cs ? excl - cs : 0;
                 if (mine) W.owner[p0] = lane;
-                const unsigned starts = __reduce_or_sync(kFull, mine ? 1u << p0 : 0u);
+                const unsigned st = __reduce_or_sync(kFull, mine ? 1u << p0 : 0u);
                 __syncwarp();
                 const int j = cs + lane;
-                const int pos = 31 - __clz(starts & (kFull >> (31 - lane)));
-                const int ow = j < T ? W.owner[pos] : 0;
+                const int ow = j < T ? W.owner[31 - __clz(st & upto)] : 0;
                 const int olo = __shfl_sync(kFull, lo, ow), oex = __shfl_sync(kFull, excl, ow);
                 if (j < T) {
                     const int32_t star = olo + (j - oex);
@@ -445,8 +460,7 @@ __device__ __forceinline__ GroupOut walk_group(WarpMem &W, int lane, int cnt, in
 }
 
 template <bool kQuad, bool kSoft>
-__global__ __launch_bounds__(kLwThreads) void k_walk_lists(const DevInfo *info, const MNode *__restrict__ nodes,
-                                                           const int2 *__restrict__ tlink,
+__global__ __launch_bounds__(kLwThreads) void k_walk_lists(const DevInfo *info, const LNode *__restrict__ nodes,
                                                            const float4 *__restrict__ st_hi,
                                                            const float4 *__restrict__ st_lo,
                                                            const int32_t *__restrict__ order, float eps, float eps2,
@@ -498,7 +512,6 @@ __global__ __launch_bounds__(kLwThreads) void k_walk_lists(const DevInfo *info, 
         t.lx = l.x;
         t.ly = l.y;
         t.lz = l.z;
-        W.tgt[lane] = make_float4(t.tx, t.ty, t.tz, 0.f);
         // the group's box, its extent from the origin and the spacing of consecutive stars
         float bx0 = t.tx, by0 = t.ty, bz0 = t.tz, bx1 = t.tx, by1 = t.ty, bz1 = t.tz;
         const float nx = __shfl_down_sync(kFull, t.tx, 1), ny = __shfl_down_sync(kFull, t.ty, 1),
@@ -526,12 +539,12 @@ __global__ __launch_bounds__(kLwThreads) void k_walk_lists(const DevInfo *info, 
         a.sx = a.sy = a.sz = a.cx = a.cy = a.cz = 0.f;
         GroupOut r;
         if (exact)
-            r = walk_group<true, kQuad, kSoft>(W, lane, cnt, root, t, Ox, Oy, Oz, bx0, by0, bz0, bx1, by1, bz1, ext,
-                                                eps2, node_depth, src_depth, nodes, tlink, st_hi, st_lo, nn, ns,
+            r = walk_group<true, kQuad, kSoft>(W, lane, root, t, Ox, Oy, Oz, bx0, by0, bz0, bx1, by1, bz1, ext,
+                                                eps2, node_depth, src_depth, nodes, st_hi, st_lo, nn, ns,
                                                 err_info, a);
         else
-            r = walk_group<false, kQuad, kSoft>(W, lane, cnt, root, t, Ox, Oy, Oz, bx0, by0, bz0, bx1, by1, bz1, ext,
-                                                 eps2, node_depth, src_depth, nodes, tlink, st_hi, st_lo, nn, ns,
+            r = walk_group<false, kQuad, kSoft>(W, lane, root, t, Ox, Oy, Oz, bx0, by0, bz0, bx1, by1, bz1, ext,
+                                                 eps2, node_depth, src_depth, nodes, st_hi, st_lo, nn, ns,
                                                  err_info, a);
         __syncwarp();
         if (!r.ok) break;  // the error flag is set; the host reports GBH_ERR_LIMIT
@@ -560,7 +573,7 @@ cudaError_t launch_lists(const Launch &L, const TreeBufs &b, float eps2, double 
     if (e != cudaSuccess) return e;
     const int sms = L.num_sms > 0 ? L.num_sms : 152;
     k_walk_lists<kQuad, kSoft><<<unsigned(sms * blocks_per_sm), kLwThreads, 0, L.stream>>>(
-        b.info, b.mnodes, b.tlink, b.st_hi, b.st_lo, b.order, sqrtf(eps2), eps2, ax, ay, az,
+        b.info, b.lnode, b.st_hi, b.st_lo, b.order, sqrtf(eps2), eps2, ax, ay, az,
         forest ? b.groups : nullptr, targets ? b.targets : nullptr, lpt ? b.gperm : nullptr, int32_t(b.cap_groups),
         lpt ? b.gcost : nullptr,
         b.walk_ctr, b.info, node_depth, src_depth);
