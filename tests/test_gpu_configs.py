@@ -169,18 +169,27 @@ def test_merger_1m_mixed_walk_per_star_against_the_reference_tree(ctx, merger_1m
     """The headline configuration (1M merger, theta 0.5, eps 0.02, the leaf sizes the autotuner
     picks between, both group sizes), star by star on the bench's 4,096 seeded targets against the
     reference per-star tree walk at the same theta and leaf. The mixed walk opens every node the
-    reference opens for a star (and some it accepts, for the star's group), so it differs from
-    the reference tree by part of the tree's own error, plus FP32 rounding. Bound, per star:
-    |a_mixed - a_tree| / |a_tree| <= 2 x (that star's tree error |a_tree - a_direct| / |a_direct|)
-    + 1e-5; over the targets the median of the same ratio <= 2e-4."""
+    reference opens for a star (and some it accepts, for the star's group), so its own error
+    against the direct sum is a theta-0.5 tree error no larger than the reference's, and by the
+    triangle inequality |a_mixed - a_tree| <= |a_mixed - a_direct| + |a_tree - a_direct|. A star
+    whose reference error happens to be small (terms that cancel) still carries a mixed-walk error
+    of the tree's typical size, so the bound adds the reference's RMS error. Bound, per star:
+    |a_mixed - a_tree| / |a_tree| <= 2 x (e_tree + RMS(e_tree)), e_tree = |a_tree - a_direct| /
+    |a_direct| (measured: at most 1.2 x (e_tree + RMS)); over the targets the median of the same
+    ratio <= 2e-4; against the direct sum the mixed walk's RMS and 99th percentile are at most the
+    reference tree's."""
     s, tg, direct = merger_1m
     _, ref, _ = reference_tree_at(s, tg, leaf)
     got = accelerations(ctx, s, abi.make_params(0.5, 0.02, leaf, False, False, "mixed", group_size=group))[tg]
     d = np.linalg.norm(got - ref, axis=1) / np.linalg.norm(ref, axis=1)
     e_tree = np.linalg.norm(ref - direct, axis=1) / np.linalg.norm(direct, axis=1)
-    worst = int(np.argmax(d - 2 * e_tree))
-    assert np.all(d <= 2 * e_tree + 1e-5), (tg[worst], d[worst], e_tree[worst])
+    rms_tree = float(np.sqrt(np.mean(e_tree ** 2)))
+    bound = 2 * (e_tree + rms_tree)
+    worst = int(np.argmax(d / bound))
+    assert np.all(d <= bound), (tg[worst], d[worst], e_tree[worst], rms_tree)
     assert np.median(d) <= 2e-4, np.median(d)
+    e = np.linalg.norm(got - direct, axis=1) / np.linalg.norm(direct, axis=1)
+    assert np.sqrt(np.mean(e ** 2)) <= rms_tree and np.percentile(e, 99) <= np.percentile(e_tree, 99)
 
 
 def test_merger_1m_plain_walk_per_star_against_the_reference_fp32_walk(ctx, merger_1m):

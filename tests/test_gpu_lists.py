@@ -97,12 +97,20 @@ def test_list_walk_coincident_stars_and_tiny_systems(ctx):
     a = forces(ctx, s, lists(0.0, 0.01, 0))
     want = forces(ctx, s, abi.make_params(0.0, 0.01, 0, False, False, "fp64"))
     assert np.isfinite(a).all() and np.allclose(a, want, rtol=1e-5, atol=1e-6)
+    # One or two stars: nothing to approximate, so the FP64 walk's forces to FP32 rounding. 31 and
+    # 33 stars: one group covers (nearly) the whole system, so the list walk opens nodes that the
+    # per-star walk accepts for some stars; against the FP64 direct sum it is at least as accurate.
     for m in (1, 2, 31, 33):
         t = ics.plummer(max(m, 2), seed=m)
         t = {k: v[:m] for k, v in t.items()}
         got = forces(ctx, t, lists(0.5, 0.01, 4))
         ref = forces(ctx, t, abi.make_params(0.5, 0.01, 4, False, False, "fp64"))
-        assert np.allclose(got, ref, rtol=1e-5, atol=1e-7), m
+        assert np.isfinite(got).all(), m
+        if m <= 2:
+            assert np.allclose(got, ref, rtol=1e-5, atol=1e-7), m
+        else:
+            want = O.direct(t["px"], t["py"], t["pz"], t["mass"], eps=0.01)
+            assert rms(rel(got, want)) <= 1.001 * rms(rel(ref, want)) + 1e-6, m
 
 
 def test_list_walk_kinds_dead_holes_and_dark_matter_off(ctx):
