@@ -19,9 +19,14 @@ error <= 2e-3; --leaf fixes it instead.
               in the same run
   errors      RMS and p99 relative force error of both walks against the FP64 direct sum on
               4,096 seeded targets
+  cpu_baseline  the CPU restatement of the reference step at the mixed walk's leaf size, best of
+              5 single steps on every host thread (and one step on one thread)
+  configs     the batched forest (5 steps after the autotuner's sweep) and the galaxy (50
+              six-level block steps), run short (--no-configs leaves them out)
 
 --impl reference times the CPU restatement of the reference's Barnes-Hut step (oracle/, FP64,
-all host threads) on the same workload at the reference solver's default leaf size, 24.
+all host threads) on the same workload at the reference solver's default leaf size, 24, and at
+leaf 32 (the leaf sizes the autotuner picks between here), and reports the faster.
 
 --workload adjoint and --workload forest print the lines of the differentiable and the batched
 workloads instead (see run_adjoint and run_forest); --workload sweep runs the merger at theta
@@ -48,18 +53,25 @@ sys.path.insert(0, ROOT)
 METRIC = "particle-steps/s @N=1M θ=0.5: mixed vs plain GPU walk at RMS force err ≤2e-3"
 N_DEFAULT = 1 << 20
 THETA, EPS, DT = 0.5, 0.02, 1e-3
-# DRAM bytes (read + write) of one k_walk_mixed2 launch on this workload by leaf size, from the
-# ncu capture summarised in profiles/walk_mixed2_merger_1M_theta0.5_leaf32.md.
-WALK_TRAFFIC_BYTES = {24: 90_435_328, 32: 86_668_288}
+# DRAM bytes (read + write) of one walk launch on this workload (a force evaluation of
+# `bench.py --profile mixed --leaf L`), by kernel and leaf size, from ncu captures of
+# dram__bytes_read.sum + dram__bytes_write.sum. Stored figures,
+# not measured in the bench's own run (a counter capture cannot run inside a timed region).
+WALK_TRAFFIC_BYTES = {(32, 24): 55_931_904, (32, 32): 61_613_568,  # (stars per group, leaf size)
+                      (64, 24): 58_973_952, (64, 32): 67_039_232}
 TUNE_LEAVES = [8, 12, 16, 24, 32]
 RMS_BOUND = 2e-3
 REFERENCE_LEAF = 24  # bh.go:17-19, the reference solver's default leaf size
+# leaf sizes the reference arm times: its own default and the leaves the autotuner picks between
+# for the mixed walk on this workload; the arm reports the fastest
+REFERENCE_LEAVES = (24, 32)
+CPU_BEST_OF = 5
 FIELDS = ("px", "py", "pz", "vx", "vy", "vz", "ax", "ay", "az")
 
 
-def workload_name(n, leaf):
+def workload_name(n):
     return (f"merger N={n} (2 x {n // 2} disk+bulge+NFW-halo galaxies, pericentre 5, separation 40), "
-            f"theta={THETA}, leaf={leaf}, eps={EPS}, dt={DT}, global KDK steps")
+            f"theta={THETA}, eps={EPS}, dt={DT}, global KDK steps")
 
 
 def max_over_ranks(x: float, world: int, device: str) -> float:
@@ -165,27 +177,38 @@ def cpu_reference_steps(s, steps, leaf, workers=0, count=False, initial=None, gr
 
 
 def run_reference(args):
+    """The reference arm: the CPU restatement of the reference's Barnes-Hut step (oracle/, FP64,
+    every host thread) on the headline workload, at each leaf size of REFERENCE_LEAVES (one
+    warm-up step, then up to --steps timed steps, at most about 30 s per leaf); the line reports
+    the fastest leaf."""
     rank, world, _ = dist_env()
     if rank != 0:
         return 0
     n = args.n
     s = make_workload(n)
     cores = os.cpu_count() or 1
-    # one warm-up step, then at most as many timed steps as fit in about a minute
-    leaf = args.leaf or REFERENCE_LEAF
-    warm, _, _ = cpu_reference_steps(s, max(1, min(args.warmup, 1)), leaf, workers=0)
-    k = max(1, min(args.steps, int(60.0 / max(warm, 1e-3))))
-    el, _, _ = cpu_reference_steps(s, k, leaf, workers=0)
-    value = n * k / el
+    leaves = (args.leaf,) if args.leaf else REFERENCE_LEAVES
+    per_leaf = {}
+    first = None
+    for leaf in leaves:
+        warm, _, first_l = cpu_reference_steps(s, 1, leaf, workers=0)
+        k = max(1, min(args.steps, int(30.0 / max(warm, 1e-3))))
+        el, _, _ = cpu_reference_steps(s, k, leaf, workers=0, initial=first_l)
+        per_leaf[leaf] = {"value": n * k / el, "steps": k, "ms_per_step": el / k * 1e3}
+    leaf = max(per_leaf, key=lambda L: per_leaf[L]["value"])
+    value, k = per_leaf[leaf]["value"], per_leaf[leaf]["steps"]
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": args.gpus,
-        "steps": k, "warmup": 1, "ms_per_step": el / k * 1e3, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": workload_name(n, leaf), "requested_steps": args.steps,
-                   "leaf_size": leaf, "tuning": "the reference solver's default leaf size (bh.go:17-19)"},
+        "steps": k, "warmup": 1, "ms_per_step": per_leaf[leaf]["ms_per_step"], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": workload_name(n), "requested_steps": args.steps, "leaf_size": leaf,
+                   "tuning": f"fastest of leaf sizes {list(leaves)} (the reference solver's default, bh.go:17-19, "
+                             f"and the leaf sizes the GPU autotuner picks between on this workload)"},
+        "per_leaf": {str(L): v for L, v in per_leaf.items()},
         "cpu_baseline": {"value": value, "unit": "particle-steps/s", "cores": cores, "kind": "port",
-                         "sample": f"{k} full KDK steps of the {n}-particle workload (C++ restatement of the "
-                                   f"reference CPU Barnes-Hut, FP64, {cores} threads; Go is not available)"},
+                         "sample": f"{k} full KDK steps of the {n}-particle workload at leaf {leaf} after one warm-up "
+                                   f"step (C++ restatement of the reference CPU Barnes-Hut, FP64, {cores} threads; "
+                                   f"Go is not available)"},
         "e2e": {"value": value, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -325,13 +348,23 @@ def run(args):
                  P(s["py"]), P(s["pz"]), P(s["mass"]), None, None, P(a[0]), P(a[1]), P(a[2]))
         errs[walk] = rel_err_stats(np.stack(a, axis=1)[targets], want)
 
+    # the batched and the galaxy configurations, run short beside the headline (their own
+    # workloads print full lines: --workload forest, --workload galaxy)
+    configs = None
+    if rank == 0 and not args.no_configs:
+        configs = {"forest": forest_summary(local, 5, 2, table=False),
+                   "galaxy": galaxy_summary(local, 50, compare=False)}
+
     line = None
     if rank == 0:
-        # CPU baseline leg: the oracle (reference algorithm) on the host cores, bounded sample,
-        # plus the reference walk's interaction counts behind the algorithmic FLOP figure
-        cpu_steps = 1
+        # CPU baseline leg: the oracle (reference algorithm) on the host cores at the GPU arm's leaf
+        # size, best of CPU_BEST_OF single steps after one warm-up step (a bounded sample), plus the
+        # reference walk's interaction counts behind the algorithmic FLOP figure
         group = tuned["mixed"][0].group_size or 64
-        el, (counts, gcounts), first = cpu_reference_steps(s, cpu_steps, leaf, workers=0, count=True, group=group)
+        kernel = f"k_walk_lists ({group}-star groups, {group // 32} star(s) a lane)"
+        _, (counts, gcounts), first = cpu_reference_steps(s, 1, leaf, workers=0, count=True, group=group)
+        cpu_times = [cpu_reference_steps(s, 1, leaf, workers=0, initial=first)[0] for _ in range(CPU_BEST_OF)]
+        el = min(cpu_times)
         cores = os.cpu_count() or 1
         # the same step on one thread (initial forces reused from the run above)
         el1, _, _ = cpu_reference_steps(s, 1, leaf, workers=1, initial=first)
@@ -344,17 +377,18 @@ def run(args):
             "metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_mixed / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32 walk, f64 state", "data": "synthetic",
-            "config": {"workload": workload_name(n, leaf), "parallelism": "replicas" if world > 1 else "1 gpu",
+            "config": {"workload": workload_name(n), "parallelism": "replicas" if world > 1 else "1 gpu",
                        "l2": "flushed (256 MiB write) between timed steps; events cover each step only",
-                       "leaf_size": leaf, "group_size": tuned["mixed"][0].group_size or 64,
+                       "leaf_size": leaf, "group_size": group, "list_depth": tuned["mixed"][0].list_depth,
                        "plain_leaf_size": tuned["plain"][0].leaf_size,
                        "tuning": "gbh_autotune at theta 0.5, RMS force error <= 2e-3 on 4096 stars" if not args.leaf
                        else "fixed by --leaf"},
             "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                         "frac": achieved / peak, "traffic": WALK_TRAFFIC_BYTES.get(leaf),
-                         "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch at "
-                                           "this leaf size (null: not captured at this leaf size)",
-                         "kernel": "k_walk_mixed2", "flop_per_launch": flop,
+                         "frac": achieved / peak, "traffic": WALK_TRAFFIC_BYTES.get((group, leaf)),
+                         "traffic_source": "stored, not measured in this run: ncu dram__bytes_read.sum + "
+                                           "dram__bytes_write.sum of one launch of this kernel at this leaf size "
+                                           "on this workload (null: not captured for this kernel and leaf size)",
+                         "kernel": kernel, "flop_per_launch": flop,
                          "peak_source": "FP32 FMA microbenchmark in this run (gbh_probe_fp32_peak); "
                                         "MEASURED_PEAKS.json has no FP32 figure",
                          "walk_ms": w_mixed / args.steps, "build_ms": b_mixed / args.steps,
@@ -364,10 +398,12 @@ def run(args):
                                       "source": f"oracle group-walk counts (orc_tree_group_counts) for "
                                                 f"{group}-star groups at the same theta and leaf: every star "
                                                 f"of a group takes part in each of its group's visits, as in "
-                                                f"k_walk_mixed2; same FLOP weights"}},
-            "cpu_baseline": {"value": n * cpu_steps / el, "unit": "particle-steps/s", "cores": cores, "kind": "port",
-                             "sample": f"{cpu_steps} full KDK step of the {n}-particle workload, C++ restatement "
-                                       f"of the reference CPU Barnes-Hut (FP64), {cores} threads",
+                                                f"{kernel}; same FLOP weights"}},
+            "cpu_baseline": {"value": n / el, "unit": "particle-steps/s", "cores": cores, "kind": "port",
+                             "sample": f"best of {CPU_BEST_OF} full KDK steps of the {n}-particle workload at leaf "
+                                       f"{leaf} after one warm-up step, C++ restatement of the reference CPU "
+                                       f"Barnes-Hut (FP64), {cores} threads",
+                             "step_seconds": cpu_times,
                              "single_core": {"value": n / el1, "unit": "particle-steps/s", "cores": 1,
                                              "sample": "the same full KDK step on one thread"}},
             "e2e": {"value": e2e_value, "unit": "particle-steps/s", "h2d_bytes_per_step": h2d,
@@ -387,6 +423,8 @@ def run(args):
                                        "(oracle counts at the initial state) per second of walk time and "
                                        "of full-step time"},
         }
+        if configs:
+            line["configs"] = configs
         print(json.dumps(line), flush=True)
     ctx.close()
     if world > 1:
@@ -449,11 +487,11 @@ def run_profile(args):
     ctx.call("gbh_state_upload", n, *[P(s[k]) for k in ("px", "py", "pz", "vx", "vy", "vz")], None, None, None,
              P(s["mass"]), None, None)
     leaf = args.leaf or REFERENCE_LEAF
-    par = abi.make_params(THETA, EPS, leaf, False, False, args.profile)
+    par = abi.make_params(THETA, EPS, leaf, False, False, args.profile, group_size=args.group)
     for _ in range(2):
         ctx.call("gbh_state_accelerations", par)
     t = ctx.timings()
-    print(json.dumps({"profile": args.profile, "n": n, "leaf": leaf, "build_ms": t["build_ms"],
+    print(json.dumps({"profile": args.profile, "n": n, "leaf": leaf, "group": args.group, "build_ms": t["build_ms"],
                       "walk_ms": t["walk_ms"], "nnodes": t["nnodes"], "launches": t["launches"]}))
     ctx.close()
     return 0
@@ -502,6 +540,7 @@ def run_adjoint(args):
     # central differences of the same forward on random velocity and mass coordinates
     rng = np.random.default_rng(5)
     h, errs, scale = 1e-4, [], float(np.abs(np.concatenate([dv.ravel(), dm])).max())
+    pure, small = [], 0  # |g - fd| / |fd| without the floor; coordinates whose |fd| is below the floor
     for q in range(args.fd_coords):
         i, c = int(rng.integers(n)), int(rng.integers(3))
         vals = []
@@ -516,6 +555,8 @@ def run_adjoint(args):
         fd = (vals[0] - vals[1]) / (2 * h)
         g = dv[i, c] if q % 2 == 0 else dm[i]
         errs.append(abs(g - fd) / max(abs(fd), 1e-3 * scale))
+        pure.append(abs(g - fd) / abs(fd) if fd != 0 else float("inf"))
+        small += abs(fd) < 1e-3 * scale
     # the same gradient against central differences of the tree dynamics (theta 0.5, mixed walk,
     # leaf 8): the opening-test discontinuities are far below the difference quotient at h = 1e-4
     tree_errs = []
@@ -558,7 +599,12 @@ def run_adjoint(args):
                      "unit": "TFLOP/s", "frac": achieved / peak, "flop_per_pair": [ADJ_FLOP_FORCE, ADJ_FLOP_VJP],
                      "peak_source": "FP32 FMA probe of this run"},
         "fd_check": {"coords": len(errs), "h": h, "max_rel": float(max(errs)) if errs else None,
-                     "median_rel": float(np.median(errs)) if errs else None},
+                     "median_rel": float(np.median(errs)) if errs else None,
+                     "error": "|g - fd| / max(|fd|, 1e-3 max|g|)",
+                     "pure": {"error": "|g - fd| / |fd|", "max_rel": float(max(pure)) if pure else None,
+                              "median_rel": float(np.median(pure)) if pure else None,
+                              "p90_rel": float(np.percentile(pure, 90)) if pure else None,
+                              "coords_below_floor": int(small)}},
         "fd_check_tree_dynamics": {"coords": len(tree_errs), "h": h, "theta": THETA, "walk": "mixed, leaf 8",
                                    "max_rel": float(max(tree_errs)) if tree_errs else None,
                                    "median_rel": float(np.median(tree_errs)) if tree_errs else None},
@@ -570,18 +616,17 @@ def run_adjoint(args):
     return 0
 
 
-def run_forest(args):
+def forest_summary(local, steps, warmup, table=True):
     """The batched workload: 64 independent Plummer or disk+bulge+halo systems of log-uniform
     N in [2048, 65536] and scale radius in [0.5, 2], one state (gbh_forest_upload). The autotuner
     (gbh_autotune) sweeps theta {0.4, 0.5, 0.7} x leaf {4, 8, 16, 32} x group {32, 64} for the
-    fastest force evaluation with RMS error <= 2e-3; then K graph-captured KDK steps run with the
-    chosen parameters (one build and one walk launch per step for all systems), and every system
-    is checked against its own FP64 direct sum on sampled stars. One line of JSON."""
+    fastest force evaluation with RMS error <= 2e-3; then `steps` KDK steps run with the chosen
+    parameters (one build and one walk launch per step for all systems; device time from CUDA
+    events, L2 flushed between steps), and every system is checked against its own FP64 direct
+    sum on sampled stars. Returns a dict (the forest line's fields)."""
     import torch
 
     from gravitas_gb300 import abi, ics
-    rank, world, local = dist_env()
-    torch.cuda.set_device(local)
     P = abi.ptr
     s, off = ics.forest(nsys=64, seed=0)
     n, nsys = int(off[-1]), len(off) - 1
@@ -595,17 +640,17 @@ def run_forest(args):
     upload()
     base = abi.make_params(0.5, EPS, 8, False, False, "mixed")
     t0 = time.perf_counter()
-    best, table = ctx.autotune(base, rms_bound=2e-3, sample=2048, reps=3)
+    best, tab = ctx.autotune(base, rms_bound=2e-3, sample=2048, reps=3)
     tune_s = time.perf_counter() - t0
-    default = [e for e in table if (e["theta"], e["leaf_size"], e["group_size"]) == (0.5, 8, 64)][0]
+    default = [e for e in tab if (e["theta"], e["leaf_size"], e["group_size"]) == (0.5, 8, 64)][0]
     upload()
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         ctx.call("gbh_state_step", best, DT, 1)
     torch.cuda.synchronize()
     tot = walk_ms = build_ms = 0.0
     launches = 0
     with Clocks(local) as clk:
-        for _ in range(args.steps):
+        for _ in range(steps):
             flush.fill_(1)
             torch.cuda.synchronize()
             ctx.call("gbh_state_step", best, DT, 1)
@@ -633,28 +678,45 @@ def run_forest(args):
         e = np.linalg.norm(a[lo:hi][tg] - want.T, axis=1) / np.linalg.norm(want.T, axis=1)
         rms.append(float(np.sqrt(np.mean(e ** 2))))
         p99.append(float(np.percentile(e, 99)))
-    value = n * args.steps / (tot * 1e-3)
-    line = {
-        "metric": f"forest particle-steps/s: {nsys} systems, N={n}, autotuned at RMS force err <= 2e-3",
-        "value": value, "unit": "particle-steps/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": tot / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32 walk, f64 state", "data": "synthetic",
-        "config": {"workload": f"forest of {nsys} Plummer or disk+bulge+halo systems, N_i log-uniform in "
-                               f"[2048, 65536], scale U[0.5, 2], eps={EPS}, dt={DT}, global KDK steps",
-                   "l2": "flushed (256 MiB write) between timed steps"},
-        "chosen": {"theta": best.theta, "leaf_size": best.leaf_size, "group_size": best.group_size},
-        "autotune": {"seconds": tune_s, "candidates": len(table),
-                     "chosen_force_ms": min(e["ms"] for e in table if e["meets"]) if any(e["meets"] for e in table)
-                     else None, "default_force_ms": default["ms"], "default_rms_err": default["rms_err"],
-                     "table": [{k: (round(v, 6) if isinstance(v, float) else v) for k, v in e.items()} for e in table]},
-        "walk_ms": walk_ms / args.steps, "build_ms": build_ms / args.steps, "gpu_launches": launches,
-        "launches_per_step": launches / args.steps,
+    ctx.close()
+    out = {
+        "value": n * steps / (tot * 1e-3), "unit": "particle-steps/s", "steps": steps, "warmup": warmup,
+        "ms_per_step": tot / steps, "n": n, "systems": nsys,
+        "workload": f"forest of {nsys} Plummer or disk+bulge+halo systems, N_i log-uniform in [2048, 65536], "
+                    f"scale U[0.5, 2], eps={EPS}, dt={DT}, global KDK steps",
+        "chosen": {"theta": best.theta, "leaf_size": best.leaf_size, "group_size": best.group_size,
+                   "list_depth": best.list_depth},
+        "autotune": {"seconds": tune_s, "candidates": len(tab),
+                     "chosen_force_ms": min(e["ms"] for e in tab if e["meets"]) if any(e["meets"] for e in tab)
+                     else None, "default_force_ms": default["ms"], "default_rms_err": default["rms_err"]},
+        "walk_ms": walk_ms / steps, "build_ms": build_ms / steps, "gpu_launches": launches,
+        "launches_per_step": launches / steps,
         "force_error_per_system": {"max_rms": max(rms), "median_rms": float(np.median(rms)), "max_p99": max(p99)},
         "clocks": clk.summary(),
     }
+    if table:
+        out["autotune"]["table"] = [{k: (round(v, 6) if isinstance(v, float) else v) for k, v in e.items()}
+                                    for e in tab]
+    return out
+
+
+def run_forest(args):
+    """The batched workload's own line (forest_summary with --steps and --warmup)."""
+    import torch
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    f = forest_summary(local, args.steps, args.warmup)
+    line = {
+        "metric": f"forest particle-steps/s: {f['systems']} systems, N={f['n']}, autotuned at RMS force err <= 2e-3",
+        "value": f["value"], "unit": f["unit"], "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": f["ms_per_step"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 walk, f64 state", "data": "synthetic",
+        "config": {"workload": f["workload"], "l2": "flushed (256 MiB write) between timed steps"},
+        **{k: f[k] for k in ("chosen", "autotune", "walk_ms", "build_ms", "gpu_launches", "launches_per_step",
+                             "force_error_per_system", "clocks")},
+    }
     if rank == 0:
         print(json.dumps(line), flush=True)
-    ctx.close()
     return 0
 
 
@@ -752,7 +814,7 @@ def run_sweep(args):
     ctx.close()
     print(json.dumps({"metric": "merger theta sweep: particle-steps/s, force error and drift per theta",
                       "unit": "particle-steps/s", "n_gpus": 1, "steps": steps, "data": "synthetic",
-                      "config": {"workload": workload_name(n, args.leaf or 32), "dt": DT, "group_size": 64,
+                      "config": {"workload": workload_name(n), "leaf_size": args.leaf or 32, "dt": DT, "group_size": 64,
                                  "estimator": "energy and angular momentum from gbh_state_diagnostics with the "
                                               "mixed walk at theta 0.5 for every row",
                                  "l2": "not flushed: the steps run back to back in one graph-replayed call"},
@@ -760,26 +822,21 @@ def run_sweep(args):
     return 0
 
 
-def run_galaxy(args):
+def galaxy_summary(local, steps, leaf=0, compare=True):
     """The galaxy configuration: the 131,072-body disk + bulge + NFW-halo galaxy (halo particles at
     4x the disk particle mass), eps 0.02, theta 0.5, power-of-two block steps with 6 levels driven
-    by eta sqrt(eps / |a|), eta 0.025, 500 block steps of T = 1.6e-2 (--steps overrides), mixed
-    walk at the leaf the autotuner picks. Reported: block steps per second, particle-steps/s (each
-    block step advances every particle by T), the events and walked stars, and the energy and
-    angular-momentum drift; beside it the first 50 block steps' simulated time in global steps at
-    the finest rung (T / 32), timed and with its drift, for the scheme's saving. One line of JSON."""
+    by eta sqrt(eps / |a|), eta 0.025, `steps` block steps of T = 1.6e-2, mixed walk at the leaf
+    the autotuner picks (or `leaf`). Returns block steps per second, particle-steps/s (each block
+    step advances every particle by T), the events and walked stars, and the energy and
+    angular-momentum drift; with `compare`, also the first 50 block steps' simulated time in
+    global steps at the finest rung (T / 32), timed and with its drift, for the scheme's saving."""
     import torch
 
     from gravitas_gb300 import abi, ics
-    rank, world, local = dist_env()
-    torch.cuda.set_device(local)
-    if rank != 0:
-        return 0
     P = abi.ptr
     g = ics.galaxy(131072, seed=0)
     n = len(g["px"])
     T, levels, eta, eps = 1.6e-2, 6, 0.025, 0.02
-    steps = args.steps
     ctx = abi.Context(local)
 
     def upload():
@@ -787,11 +844,11 @@ def run_galaxy(args):
                  P(g["mass"]), P(g["kind"]), P(g["alive"]))
 
     upload()
-    base = abi.make_params(THETA, eps, args.leaf or 16, False, False, "mixed")
-    if args.leaf:
+    base = abi.make_params(THETA, eps, leaf or 16, False, False, "mixed")
+    if leaf:
         par = base
     else:
-        par, _ = ctx.autotune(base, thetas=[THETA], leaves=TUNE_LEAVES, groups=[64], rms_bound=RMS_BOUND,
+        par, _ = ctx.autotune(base, thetas=[THETA], leaves=TUNE_LEAVES, groups=[64, 32], rms_bound=RMS_BOUND,
                               sample=4096, reps=3)
 
     def run_block(nsteps):
@@ -814,33 +871,50 @@ def run_galaxy(args):
     with Clocks(local) as clk:
         el, st, d0, d1 = run_block(steps)
         de, dl = drifts(d0, d1)
-        short = min(steps, 50)
-        el_s, st_s, s0, s1 = run_block(short)
-        de_s, _ = drifts(s0, s1)
-        upload()
-        f0 = ctx.diagnostics(par)
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        ctx.call("gbh_state_step", par, T / 32, 32 * short)
-        torch.cuda.synchronize()
-        el_g = time.perf_counter() - t0
-        de_g, _ = drifts(f0, ctx.diagnostics(par))
+        cmp = None
+        if compare:
+            short = min(steps, 50)
+            el_s, st_s, s0, s1 = run_block(short)
+            de_s, _ = drifts(s0, s1)
+            upload()
+            f0 = ctx.diagnostics(par)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            ctx.call("gbh_state_step", par, T / 32, 32 * short)
+            torch.cuda.synchronize()
+            el_g = time.perf_counter() - t0
+            de_g, _ = drifts(f0, ctx.diagnostics(par))
+            cmp = {"block_steps": short, "block_seconds": el_s, "block_energy_drift": de_s,
+                   "global_steps": 32 * short, "global_seconds": el_g, "global_energy_drift": de_g,
+                   "speedup": el_g / el_s}
     ctx.close()
-    print(json.dumps({
-        "metric": "galaxy block steps: particle-steps/s (each block step advances all particles by T)",
-        "value": n * steps / el, "unit": "particle-steps/s", "n_gpus": 1, "steps": steps, "data": "synthetic",
-        "config": {"workload": f"galaxy N={n} (40 % exponential disk, 10 % Hernquist bulge, 50 % NFW halo at 4x "
-                               f"the disk particle mass), eps={eps}, theta={THETA}, {levels} levels, eta={eta}, T={T}",
-                   "leaf_size": par.leaf_size, "group_size": par.group_size or 64,
-                   "timing": "wall clock around one gbh_state_step_block call (host reads one event tick per event)"},
+    out = {
+        "value": n * steps / el, "unit": "particle-steps/s", "steps": steps,
+        "workload": f"galaxy N={n} (40 % exponential disk, 10 % Hernquist bulge, 50 % NFW halo at 4x the disk "
+                    f"particle mass), eps={eps}, theta={THETA}, {levels} levels, eta={eta}, T={T}",
+        "leaf_size": par.leaf_size, "group_size": par.group_size or 64, "list_depth": par.list_depth,
+        "timing": "wall clock around one gbh_state_step_block call (host reads one event tick per event)",
         "block_steps_per_s": steps / el, "events": st["substeps"], "walked_stars": st["evaluations"],
         "walked_fraction": st["evaluations"] / (n * st["substeps"]) if st["substeps"] else None,
-        "energy_drift": de, "angular_momentum_drift": dl,
-        "vs_finest_rung_global_steps": {
-            "block_steps": short, "block_seconds": el_s, "block_energy_drift": de_s,
-            "global_steps": 32 * short, "global_seconds": el_g, "global_energy_drift": de_g,
-            "speedup": el_g / el_s},
-        "clocks": clk.summary()}), flush=True)
+        "energy_drift": de, "angular_momentum_drift": dl, "clocks": clk.summary()}
+    if cmp:
+        out["vs_finest_rung_global_steps"] = cmp
+    return out
+
+
+def run_galaxy(args):
+    """The galaxy configuration's own line (galaxy_summary with --steps, default 500)."""
+    import torch
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if rank != 0:
+        return 0
+    gsum = galaxy_summary(local, args.steps, args.leaf)
+    line = {"metric": "galaxy block steps: particle-steps/s (each block step advances all particles by T)",
+            "value": gsum["value"], "unit": gsum["unit"], "n_gpus": 1, "steps": args.steps, "data": "synthetic",
+            "config": {k: gsum[k] for k in ("workload", "leaf_size", "group_size", "list_depth", "timing")}}
+    line.update({k: v for k, v in gsum.items() if k not in line["config"] and k not in ("value", "unit", "steps")})
+    print(json.dumps(line), flush=True)
     return 0
 
 
@@ -861,6 +935,10 @@ def main():
                          "one state with the autotuner; sweep: the merger at theta 0.3 / 0.5 / 0.8; galaxy: the "
                          "131,072-body galaxy in block steps; scaling: 1M to 64M bodies; each prints its own "
                          "JSON line")
+    ap.add_argument("--group", type=int, default=0, choices=[0, 32, 64],
+                    help="--profile mixed: the mixed walk's group size (0: the library's default)")
+    ap.add_argument("--no-configs", action="store_true",
+                    help="headline: leave out the short forest and galaxy runs reported beside it")
     ap.add_argument("--fd-coords", type=int, default=16, help="adjoint: coordinates checked by central differences")
     ap.add_argument("--sizes", type=int, nargs="+", default=[1 << 20, 1 << 22, 1 << 24, 1 << 26],
                     help="scaling: body counts")

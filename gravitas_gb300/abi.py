@@ -39,6 +39,7 @@ CFG_NO_GRAPHS = 1
 CFG_BLOCKING_SYNC = 2
 CFG_NO_LPT = 4
 CFG_NO_SPLIT = 8
+CFG_PAIRED = 16
 
 
 class Config(ctypes.Structure):

@@ -24,6 +24,9 @@ constexpr int kNoCell = 22;               // "starts no cell": duplicate of the 
 // caller gets GBH_ERR_ARG); every other value names the kernel whose bound or check failed
 // (GBH_ERR_LIMIT).
 constexpr int kErrNonFinite = 20;
+// A one-sweep sort pass or a single-pass scan whose look-back wait ran past its bound.
+constexpr int kErrSortWait = 30;
+constexpr int kErrScanWait = 31;
 
 // Per-build scalars kept on the device, so a step needs no host round trip.
 struct DevInfo {
@@ -98,6 +101,10 @@ struct TreeBufs {
     uint64_t *keys = nullptr, *keys_alt = nullptr;
     int32_t *order = nullptr, *order_alt = nullptr;
     uint32_t *hist = nullptr;     // radix digit table
+    // one-sweep sort and single-pass scans: digit histograms, tile counters and look-back words
+    // (cleared at the start of every build)
+    uint32_t *os_state = nullptr;
+    int64_t os_words = 0;
     // sorted stars
     double *sx = nullptr, *sy = nullptr, *sz = nullptr, *sm = nullptr;
     float4 *st_hi = nullptr, *st_lo = nullptr;
@@ -141,6 +148,7 @@ struct TreeBufs {
     double *part_acc = nullptr;
     int64_t part_cap = 0;           // doubles
     bool split = true;              // set per call by the caller
+    bool paired = false;            // 64-star groups take the paired walk (set per call)
     int64_t walk_hint = 0;          // a target-list walk's expected list length (0: the body count)
     bool moments_exact = false;     // the last build ran the bit-exact FP64 upsweep
     // scan temporaries
@@ -338,13 +346,14 @@ cudaError_t fp32_fma_probe(const Launch &L, int blocks, int iters, float *out);
 // Longest-first order of the next walk's groups of gsize stars, from this walk's group costs.
 cudaError_t lpt_order(const Launch &L, const TreeBufs &b, int gsize);
 
-// ---- walk_lists.cu (the list walk: decoupled traversal and evaluation, 32-star groups) ----
+// ---- walk_lists.cu (the list walk: decoupled traversal and evaluation, 32- or 64-star groups) ----
 constexpr int kDefaultListDepth = 48;
 // The largest node-list depth (entries evaluated per flush) of the list walk.
 int list_depth_max(bool exact);
-// Every star, or (targets = true) the stars listed in b.targets; b.group must have been 32 for the
-// build of a forest. Persistent warps; needs b.cap_nodes < 2^29.
+// Every star, or (targets = true) the stars listed in b.targets, in groups of 32 x stars_per_lane
+// (1 or 2) stars; a forest's build must have made groups of that size (b.group). Persistent
+// warps; needs b.cap_nodes < 2^29.
 cudaError_t walk_lists(const Launch &L, const TreeBufs &b, float eps2, int quad, double *ax, double *ay, double *az,
-                       int list_depth, bool targets);
+                       int list_depth, bool targets, int stars_per_lane);
 
 }  // namespace gbh

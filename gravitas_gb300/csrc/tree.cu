@@ -188,6 +188,100 @@ cudaError_t scan_rec(const Launch &L, const uint32_t *in, uint32_t *out, int64_t
     return cudaGetLastError();
 }
 
+// Polls of a look-back wait (the one-sweep sort's and the single-pass scan's) before the block
+// gives up and records an error: far beyond any wait of a running predecessor.
+constexpr int kOsSpinLimit = 1 << 22;
+
+// Look-back words are read and written whole (count and flag in one word); nothing else is
+// passed through them, so volatile (uncached, untorn) accesses suffice.
+__device__ __forceinline__ uint32_t ld_volatile(const uint32_t *p) { return *reinterpret_cast<const volatile uint32_t *>(p); }
+__device__ __forceinline__ void st_volatile(uint32_t *p, uint32_t v) { *reinterpret_cast<volatile uint32_t *>(p) = v; }
+__device__ __forceinline__ unsigned long long ld_volatile64(const unsigned long long *p) {
+    return *reinterpret_cast<const volatile unsigned long long *>(p);
+}
+__device__ __forceinline__ void st_volatile64(unsigned long long *p, unsigned long long v) {
+    *reinterpret_cast<volatile unsigned long long *>(p) = v;
+}
+
+// Single-pass exclusive scan with decoupled look-back (one launch): a block takes the next tile
+// from *ctr, publishes its sum, adds its predecessors' (their inclusive prefix, or their sums
+// back to one that has published a prefix) and publishes its own inclusive prefix. Waits are
+// bounded as in the one-sweep sort. status: one 64-bit word per tile (flag in the top 2 bits).
+__global__ __launch_bounds__(kScanThreads) void k_scan_lb(const uint32_t *in, uint32_t *out, int64_t n,
+                                                          const int64_t *ndyn, uint32_t *ctr,
+                                                          unsigned long long *status, DevInfo *info) {
+    __shared__ uint32_t s_warp[kScanThreads / 32 + 1];
+    __shared__ uint32_t s_tile;
+    __shared__ unsigned long long s_prefix;
+    if (threadIdx.x == 0) s_tile = atomicAdd(ctr, 1u);
+    __syncthreads();
+    const uint32_t tile = s_tile;
+    const int64_t ne = dyn_len(n, ndyn);
+    if (int64_t(tile) * kScanTile >= ne) return;  // uniform
+    const int64_t base = int64_t(tile) * kScanTile + int64_t(threadIdx.x) * kScanItems;
+    uint32_t v[kScanItems];
+    uint32_t sum = 0;
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+        v[k] = base + k < ne ? in[base + k] : 0;
+        sum += v[k];
+    }
+    uint32_t total;
+    uint32_t run = block_excl_scan(sum, s_warp, total);
+    if (threadIdx.x < 32) {
+        // warp 0 publishes the tile's sum, then reads its predecessors' words 32 at a time (lane j
+        // the (j+1)-th tile back) and adds them down to the nearest published prefix
+        constexpr unsigned long long kAgg = 1ull << 62, kPre = 2ull << 62, kVal = (1ull << 62) - 1;
+        const int lane = threadIdx.x;
+        unsigned long long excl = 0;
+        if (tile == 0) {
+            if (lane == 0) st_volatile64(status, kPre | total);
+        } else {
+            if (lane == 0) st_volatile64(status + tile, kAgg | total);
+            int64_t t = int64_t(tile) - 1;
+            int spins = 0;
+            bool bad = false;
+            for (;;) {
+                const int64_t idx = t - lane;
+                unsigned long long w = idx >= 0 ? ld_volatile64(status + idx) : kPre;  // before tile 0: prefix 0
+                // every word up to the nearest prefix must be published; wait for the others
+                for (;;) {
+                    const unsigned pre = __ballot_sync(0xffffffffu, (w >> 62) == 2);
+                    const unsigned upto = pre ? (pre & (0u - pre)) * 2u - 1u : 0xffffffffu;  // lanes to the first prefix
+                    const unsigned wait = __ballot_sync(0xffffffffu, !(w >> 62)) & upto;
+                    if (!wait) break;
+                    if (++spins > kOsSpinLimit) {
+                        bad = true;
+                        break;
+                    }
+                    if ((wait >> lane) & 1u) w = ld_volatile64(status + idx);
+                }
+                if (bad) break;
+                const unsigned pre = __ballot_sync(0xffffffffu, (w >> 62) == 2);
+                const unsigned upto = pre ? (pre & (0u - pre)) * 2u - 1u : 0xffffffffu;
+                unsigned long long v = ((upto >> lane) & 1u) ? (w & kVal) : 0ull;
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+                excl += v;
+                if (pre) break;
+                t -= 32;
+            }
+            if (lane == 0) {
+                if (bad) dev_error(info, kErrScanWait);
+                st_volatile64(status + tile, kPre | ((excl + total) & kVal));
+            }
+        }
+        if (lane == 0) s_prefix = excl;
+    }
+    __syncthreads();
+    run += uint32_t(s_prefix);
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+        if (base + k < ne) out[base + k] = run;
+        run += v[k];
+    }
+}
+
 // ---------------------------------------------------------------- collect + bbox + keys
 
 __device__ __forceinline__ bool is_star(uint8_t alive, uint8_t kind) { return alive && kind != GBH_BLACK_HOLE; }
@@ -236,7 +330,12 @@ __global__ __launch_bounds__(kThreads) void k_flags_bbox(int64_t n, const double
                                                          const double *__restrict__ mass,
                                                          const uint8_t *__restrict__ kind,
                                                          const uint8_t *__restrict__ alive, uint32_t *__restrict__ flag,
-                                                         double *__restrict__ part, double *ax, double *ay, double *az) {
+                                                         double *__restrict__ part, double *ax, double *ay, double *az,
+                                                         DevInfo *info) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) {  // the build's first kernel clears the error record
+        info->err = 0;
+        info->err_where = 0;
+    }
     long long mn[3] = {LLONG_MAX, LLONG_MAX, LLONG_MAX}, mx[3] = {LLONG_MIN, LLONG_MIN, LLONG_MIN};
     for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
         uint8_t al = alive ? alive[i] : 1, kd = kind ? kind[i] : 0;
@@ -308,8 +407,6 @@ __global__ __launch_bounds__(kFinalThreads) void k_bbox_final(int nparts, const 
     info->theta = theta;
     info->nstars = ns;
     info->nnodes = 0;
-    info->err = 0;
-    info->err_where = 0;
     info->work = 0;
     info->nleaves = 0;
     if (ns > 0 && !(isfinite(mn[0]) && isfinite(mn[1]) && isfinite(mn[2]) && isfinite(mx[0]) && isfinite(mx[1]) &&
@@ -469,6 +566,192 @@ __global__ __launch_bounds__(kRsThreads) void k_rs_scatter(const uint64_t *__res
         __syncthreads();
         if (valid) {
             uint32_t pos = s_goff[d] + s_w[buf][warp][d] + rank;
+            if (pos < n) {
+                kout[pos] = k[it];
+                vout[pos] = v[it];
+            } else {
+                dev_error(info, 10);
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------- one-sweep radix sort
+//
+// The same stable LSD sort in one launch per pass after a single histogram launch. k_os_hist
+// reads the keys once and counts every pass's digits (and, for a forest, the two system-id
+// digits); a pass block takes the next tile from a counter, ranks its keys exactly as
+// k_rs_scatter does, publishes its per-digit counts and then looks back over its predecessors'
+// published counts (decoupled look-back: a predecessor's word holds either its own count or its
+// inclusive prefix) to find where each of its digits starts. Tiles are taken in counter order, so
+// every tile a block waits for belongs to a block that is already running. Each wait is bounded:
+// past kOsSpinLimit polls the block records an error (reported as GBH_ERR_LIMIT), publishes what
+// it has so that its successors are not held, and its output is not used.
+
+constexpr int kOsPassesMax = 10;  // 8 key digits, then 2 system-id digits (forest)
+constexpr uint32_t kOsAgg = 1u << 30, kOsPre = 2u << 30, kOsCount = (1u << 30) - 1u;
+// States of up to kOsMaxN bodies (capacity) build with the one-sweep sort and single-pass scans;
+// larger ones with the three-launch passes. Measured on the merger (CUDA events, whole build,
+// one-sweep against three-launch): 16k bodies 0.29 / 0.36 ms, 64k 0.32 / 0.45, 131k 0.36 / 0.46,
+// 262k 0.41 / 0.50, 1M 0.72 / 0.69. With every tile of a large pass resident at once, each
+// tile's look-back walks back to the nearest published prefix while all of them are still
+// aggregates, a chain of L2 round trips that outgrows the launches it saves.
+constexpr int64_t kOsMaxN = int64_t(3) << 18;
+static_assert(kOsMaxN * 8 < int64_t(kOsCount), "one-sweep counts are 30-bit");
+constexpr int kOsHistBlocksPerSm = 2;
+constexpr int kOsWindow = 8;  // predecessors' look-back words read per round trip
+
+// Word offsets inside TreeBufs::os_state.
+constexpr int64_t kOsHistWords = int64_t(kOsPassesMax) * kRsBins;  // [pass][digit]
+constexpr int64_t kOsCtrWords = 32;                                 // tile counters: passes, then scans
+constexpr int kOsScanCtr = kOsPassesMax;                            // first scan counter
+constexpr int kOsScans = 3;                                         // flags, chain counts, child counts
+__host__ __device__ inline int64_t os_scan_tiles(int64_t n) { return (n + kScanTile - 1) / kScanTile; }
+__host__ __device__ inline int64_t os_sort_tiles(int64_t n) { return (n + kRsTile - 1) / kRsTile; }
+
+template <bool kSid>
+__device__ __forceinline__ uint32_t os_digit(uint64_t k, int32_t v, const uint16_t *__restrict__ sys_of, int shift) {
+    return (kSid ? uint32_t(sys_of[v] >> shift) : uint32_t(k >> shift)) & (kRsBins - 1);
+}
+
+// Every pass's digit histogram in one read of the keys (warp-aggregated shared counters, then one
+// global add per non-zero bin and block).
+template <bool kSid>
+__global__ __launch_bounds__(kRsThreads) void k_os_hist(const uint64_t *__restrict__ keys,
+                                                        const int32_t *__restrict__ vals,
+                                                        const uint16_t *__restrict__ sys_of, const DevInfo *info,
+                                                        uint32_t *__restrict__ ghist) {
+    constexpr int kPasses = kSid ? kOsPassesMax : 8;
+    __shared__ uint32_t h[kPasses * kRsBins];
+    for (int i = threadIdx.x; i < kPasses * kRsBins; i += blockDim.x) h[i] = 0;
+    __syncthreads();
+    const int64_t n = info->nstars;
+    const int lane = threadIdx.x & 31;
+    const int64_t stride = int64_t(gridDim.x) * blockDim.x;
+    // whole warps iterate together (the match below needs every lane)
+    for (int64_t i0 = int64_t(blockIdx.x) * blockDim.x + (threadIdx.x & ~31); i0 < n; i0 += stride) {
+        const int64_t i = i0 + lane;
+        const bool valid = i < n;
+        const uint64_t k = valid ? keys[i] : 0;
+        const uint32_t sd = kSid && valid ? uint32_t(sys_of[vals[i]]) : 0u;
+#pragma unroll
+        for (int p = 0; p < kPasses; ++p) {
+            const uint32_t d = p < 8 ? uint32_t(k >> (8 * p)) & 255u : (sd >> (8 * (p - 8))) & 255u;
+            const uint32_t peers = __match_any_sync(0xffffffffu, valid ? d : 256u + lane);
+            if (valid && (peers & ((1u << lane) - 1u)) == 0) atomicAdd(&h[p * kRsBins + d], __popc(peers));
+        }
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < kPasses * kRsBins; i += blockDim.x)
+        if (h[i]) atomicAdd(&ghist[i], h[i]);
+}
+
+// One stable pass over the tile the block takes. status: [tile][digit] words of this pass.
+template <bool kSid>
+__global__ __launch_bounds__(kRsThreads) void k_os_pass(const uint64_t *__restrict__ kin,
+                                                        const int32_t *__restrict__ vin, uint64_t *__restrict__ kout,
+                                                        int32_t *__restrict__ vout, const uint16_t *__restrict__ sys_of,
+                                                        DevInfo *info, int shift, const uint32_t *__restrict__ ghist,
+                                                        uint32_t *ctr, uint32_t *status) {
+    __shared__ uint32_t s_run[kRsBins];
+    __shared__ uint32_t s_goff[kRsBins];
+    __shared__ uint32_t s_w[2][kRsWarps][kRsBins];
+    __shared__ uint32_t s_warp[kScanThreads / 32 + 1];
+    __shared__ uint32_t s_tile;
+    static_assert(kRsThreads == kScanThreads && kRsThreads == kRsBins, "one thread per digit");
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    if (tid == 0) s_tile = atomicAdd(ctr, 1u);
+    s_run[tid] = 0;
+#pragma unroll
+    for (int w = 0; w < kRsWarps; ++w) {
+        s_w[0][w][tid] = 0;
+        s_w[1][w][tid] = 0;
+    }
+    // where each digit starts in the output: exclusive scan of the pass's histogram
+    uint32_t total;
+    const uint32_t gstart = block_excl_scan(ghist[tid], s_warp, total);  // its barriers publish s_tile too
+    const uint32_t tile = s_tile;
+    const int64_t n = info->nstars;
+    const int64_t base = int64_t(tile) * kRsTile;
+    if (base >= n) return;  // uniform over the block
+    uint64_t k[kRsItems];
+    int32_t v[kRsItems];
+    uint32_t loc[kRsItems];
+#pragma unroll
+    for (int it = 0; it < kRsItems; ++it) {
+        const int64_t idx = base + it * kRsThreads + tid;
+        if (idx < n) {
+            k[it] = kin[idx];
+            v[it] = vin[idx];
+        }
+    }
+    // rank within the tile in (item round, warp, lane) order, as k_rs_scatter
+    const uint32_t lt = (1u << lane) - 1u;
+#pragma unroll
+    for (int it = 0; it < kRsItems; ++it) {
+        const int buf = it & 1;
+        const bool valid = base + it * kRsThreads + tid < n;
+        const uint32_t d = valid ? os_digit<kSid>(k[it], v[it], sys_of, shift) : 0u;
+        const uint32_t peers = __match_any_sync(0xffffffffu, valid ? d : uint32_t(kRsBins + lane));
+        const uint32_t rank = __popc(peers & lt);
+        if (valid && rank == 0) s_w[buf][warp][d] = __popc(peers);
+        __syncthreads();
+        uint32_t run = s_run[tid];
+#pragma unroll
+        for (int w = 0; w < kRsWarps; ++w) {
+            const uint32_t c = s_w[buf][w][tid];
+            s_w[buf][w][tid] = run;
+            run += c;
+            s_w[buf ^ 1][w][tid] = 0;
+        }
+        s_run[tid] = run;
+        __syncthreads();
+        loc[it] = valid ? s_w[buf][warp][d] + rank : 0u;
+    }
+    // look-back for digit tid: this tile's count is s_run[tid]. Predecessors' words are read
+    // kOsWindow at a time (independent loads), then taken in order back to the first prefix.
+    const uint32_t agg = s_run[tid];
+    uint32_t *mine = status + size_t(tile) * kRsBins + tid;
+    uint32_t excl = 0;
+    if (tile == 0) {
+        st_volatile(mine, kOsPre | agg);
+    } else {
+        st_volatile(mine, kOsAgg | agg);
+        int64_t t = int64_t(tile) - 1;
+        int spins = 0;
+        bool done = false, bad = false;
+        while (!done && !bad) {
+            uint32_t w[kOsWindow];
+#pragma unroll
+            for (int j = 0; j < kOsWindow; ++j)  // before tile 0: a prefix of 0
+                w[j] = t - j >= 0 ? ld_volatile(status + size_t(t - j) * kRsBins + tid) : kOsPre;
+#pragma unroll
+            for (int j = 0; j < kOsWindow; ++j) {
+                if (done || bad) continue;
+                while (!(w[j] >> 30)) {  // not published yet: wait for this word
+                    if (++spins > kOsSpinLimit) {
+                        bad = true;
+                        break;
+                    }
+                    w[j] = ld_volatile(status + size_t(t - j) * kRsBins + tid);
+                }
+                if (bad) continue;
+                excl += w[j] & kOsCount;
+                done = (w[j] >> 30) == (kOsPre >> 30);
+            }
+            t -= kOsWindow;
+        }
+        if (bad) dev_error(info, kErrSortWait);
+        st_volatile(mine, kOsPre | ((excl + agg) & kOsCount));
+    }
+    s_goff[tid] = gstart + excl;
+    __syncthreads();
+#pragma unroll
+    for (int it = 0; it < kRsItems; ++it) {
+        const int64_t idx = base + it * kRsThreads + tid;
+        if (idx < n) {
+            const uint32_t d = os_digit<kSid>(k[it], v[it], sys_of, shift);
+            const uint32_t pos = s_goff[d] + loc[it];
             if (pos < n) {
                 kout[pos] = k[it];
                 vout[pos] = v[it];
@@ -1428,7 +1711,7 @@ static cudaError_t scan_dyn(const Launch &L, const uint32_t *in, uint32_t *out, 
 }
 
 void tree_free(TreeBufs &b) {
-    void *ptrs[] = {b.flag, b.bbox_part, b.keys, b.keys_alt, b.order, b.order_alt, b.hist, b.sx, b.sy, b.sz, b.sm,
+    void *ptrs[] = {b.flag, b.bbox_part, b.keys, b.keys_alt, b.order, b.order_alt, b.hist, b.os_state, b.sx, b.sy, b.sz, b.sm,
                     b.st_hi, b.st_lo, b.st_off, b.chain_cnt, b.leaves, b.targets, b.geo, b.sid_sorted, b.groups, b.gcost, b.gperm, b.pre_parent, b.pre_info, b.pre_nchild, b.pre_mask, b.pre_ref, b.nodes,
                     b.n_parent, b.n_info, b.n_arrive, b.pnodes, b.mnodes, b.mrange, b.lnode, b.walk_ctr, b.scan_tmp, b.info, b.part_acc};
     for (void *p : ptrs)
@@ -1504,6 +1787,12 @@ cudaError_t tree_alloc(TreeBufs &b, int64_t n, int leaf, int32_t nsys) {
     GBH_ALLOC(b.lnode, cnodes);
     GBH_ALLOC(b.walk_ctr, 16);
     GBH_ALLOC(b.scan_tmp, scan_cap);
+    int64_t os_words = 0;
+    if (cn <= kOsMaxN) {  // node capacity stays below 2^30 too (at most 12 nodes a body)
+        const int64_t stiles = os_scan_tiles(cn > cnodes ? cn : cnodes);
+        os_words = kOsHistWords + kOsCtrWords + 2 * kOsScans * stiles + kOsPassesMax * os_sort_tiles(cn) * kRsBins;
+        GBH_ALLOC(b.os_state, os_words);
+    }
     GBH_ALLOC(b.info, 1);
 #undef GBH_ALLOC
     if (e != cudaSuccess) {
@@ -1512,6 +1801,7 @@ cudaError_t tree_alloc(TreeBufs &b, int64_t n, int leaf, int32_t nsys) {
     }
     b.cap_n = cn;
     b.cap_nodes = cnodes;
+    b.os_words = os_words;
     b.cap_sys = csys;
     b.cap_groups = cgroups;
     b.nsys = nsys;
@@ -1528,6 +1818,24 @@ cudaError_t tree_alloc(TreeBufs &b, int64_t n, int leaf, int32_t nsys) {
         if (e_ != cudaSuccess) return e_;          \
     } while (0)
 
+// Word offset of the sort's look-back words in os_state (after the histograms, the counters and
+// the scans' 64-bit words).
+static int64_t os_scan_cap(const TreeBufs &b) { return os_scan_tiles(b.cap_n > b.cap_nodes ? b.cap_n : b.cap_nodes); }
+static int64_t os_sort_base(const TreeBufs &b) { return kOsHistWords + kOsCtrWords + 2 * kOsScans * os_scan_cap(b); }
+
+// Single-pass exclusive scan `which` (0 flags, 1 chain counts, 2 child counts) of a build.
+static cudaError_t scan_lb(const Launch &L, TreeBufs &b, int which, const uint32_t *in, uint32_t *out, int64_t n,
+                           const int64_t *ndyn) {
+    const int64_t tiles = os_scan_tiles(n);
+    if (tiles < 1) return cudaSuccess;
+    uint32_t *ctr = b.os_state + kOsHistWords + kOsScanCtr + which;
+    unsigned long long *st =
+        reinterpret_cast<unsigned long long *>(b.os_state + kOsHistWords + kOsCtrWords) + which * os_scan_cap(b);
+    k_scan_lb<<<unsigned(tiles), kScanThreads, 0, L.stream>>>(in, out, n, ndyn, ctr, st, b.info);
+    ++*L.count;
+    return cudaGetLastError();
+}
+
 cudaError_t tree_build(const Launch &L, TreeBufs &b, int64_t n, const double *px, const double *py, const double *pz,
                        const double *mass, const uint8_t *kind, const uint8_t *alive, double *ax, double *ay,
                        double *az, double theta, int leaf, int dm_off, bool exact, bool plain_records,
@@ -1537,13 +1845,22 @@ cudaError_t tree_build(const Launch &L, TreeBufs &b, int64_t n, const double *px
     const bool forest = b.nsys > 1;
     if (forest && (!sys_of || !sys_off)) return cudaErrorInvalidValue;
     cudaError_t e;
+    // one-sweep sort and single-pass scans (capacity up to kOsMaxN bodies): histograms, tile
+    // counters and the look-back words of the passes this build runs start at zero
+    const bool os = b.os_state != nullptr;
+    const int npass = forest ? kOsPassesMax : 8;
+    if (os) {
+        const int64_t words = os_sort_base(b) + int64_t(npass) * os_sort_tiles(cap) * kRsBins;
+        if ((e = cudaMemsetAsync(b.os_state, 0, sizeof(uint32_t) * size_t(words), s)) != cudaSuccess) return e;
+    }
     if (!forest) {
         // collect + bbox (build.go:62-113)
         unsigned fb = blocks_for(n, kThreads);
         if (fb > unsigned(kFlagBlocksMax)) fb = kFlagBlocksMax;
-        k_flags_bbox<<<fb, kThreads, 0, s>>>(n, px, py, pz, mass, kind, alive, b.flag, b.bbox_part, ax, ay, az);
+        k_flags_bbox<<<fb, kThreads, 0, s>>>(n, px, py, pz, mass, kind, alive, b.flag, b.bbox_part, ax, ay, az,
+                                             b.info);
         GBH_LAUNCH_CHECK();
-        e = scan_u32(L, b.flag, b.flag, n, b.scan_tmp, b.scan_tmp_cap);
+        e = os ? scan_lb(L, b, 0, b.flag, b.flag, n, nullptr) : scan_u32(L, b.flag, b.flag, n, b.scan_tmp, b.scan_tmp_cap);
         if (e != cudaSuccess) return e;
         k_bbox_final<<<1, kFinalThreads, 0, s>>>(int(fb), b.bbox_part, n, b.flag, kind, alive, theta, b.info, b.geo);
         GBH_LAUNCH_CHECK();
@@ -1558,7 +1875,7 @@ cudaError_t tree_build(const Launch &L, TreeBufs &b, int64_t n, const double *px
         k_flags_sys<<<blocks_for(n, kThreads), kThreads, 0, s>>>(n, px, py, pz, mass, kind, alive, sys_of, b.flag,
                                                                  b.geo, ax, ay, az);
         GBH_LAUNCH_CHECK();
-        e = scan_u32(L, b.flag, b.flag, n, b.scan_tmp, b.scan_tmp_cap);
+        e = os ? scan_lb(L, b, 0, b.flag, b.flag, n, nullptr) : scan_u32(L, b.flag, b.flag, n, b.scan_tmp, b.scan_tmp_cap);
         if (e != cudaSuccess) return e;
         k_sys_final<<<sb, 128, 0, s>>>(b.nsys, n, sys_off, b.flag, kind, alive, theta, b.geo, b.info);
         GBH_LAUNCH_CHECK();
@@ -1570,7 +1887,32 @@ cudaError_t tree_build(const Launch &L, TreeBufs &b, int64_t n, const double *px
     const uint32_t ntiles = uint32_t((cap + kRsTile - 1) / kRsTile);
     uint64_t *kin = b.keys, *kout = b.keys_alt;
     int32_t *vin = b.order, *vout = b.order_alt;
-    for (int shift = 0; shift < 64; shift += 8) {
+    if (os) {
+        // forest: then stably by system, (system, key) order, each system's stars contiguous
+        uint32_t *ghist = b.os_state, *ctr = b.os_state + kOsHistWords;
+        unsigned hb = unsigned(L.num_sms > 0 ? L.num_sms : 152) * kOsHistBlocksPerSm;
+        if (int64_t(hb) * kRsThreads > cap) hb = blocks_for(cap, kRsThreads);
+        if (forest) k_os_hist<true><<<hb, kRsThreads, 0, s>>>(kin, vin, sys_of, b.info, ghist);
+        else k_os_hist<false><<<hb, kRsThreads, 0, s>>>(kin, vin, nullptr, b.info, ghist);
+        GBH_LAUNCH_CHECK();
+        for (int p = 0; p < npass; ++p) {
+            uint32_t *st = b.os_state + os_sort_base(b) + int64_t(p) * ntiles * kRsBins;
+            if (p < 8)
+                k_os_pass<false><<<ntiles, kRsThreads, 0, s>>>(kin, vin, kout, vout, nullptr, b.info, 8 * p,
+                                                               ghist + p * kRsBins, ctr + p, st);
+            else
+                k_os_pass<true><<<ntiles, kRsThreads, 0, s>>>(kin, vin, kout, vout, sys_of, b.info, 8 * (p - 8),
+                                                              ghist + p * kRsBins, ctr + p, st);
+            GBH_LAUNCH_CHECK();
+            uint64_t *tk = kin;
+            kin = kout;
+            kout = tk;
+            int32_t *tv = vin;
+            vin = vout;
+            vout = tv;
+        }
+    }
+    for (int shift = 0; shift < 64 && !os; shift += 8) {
         k_rs_hist<false><<<ntiles, kRsThreads, 0, s>>>(kin, vin, nullptr, b.info, shift, ntiles, b.hist);
         GBH_LAUNCH_CHECK();
         e = scan_u32(L, b.hist, b.hist, int64_t(ntiles) * kRsBins, b.scan_tmp, b.scan_tmp_cap);
@@ -1584,7 +1926,7 @@ cudaError_t tree_build(const Launch &L, TreeBufs &b, int64_t n, const double *px
         vin = vout;
         vout = tv;
     }
-    if (forest) {  // then stably by system: (system, key) order, each system's stars contiguous
+    if (forest && !os) {  // then stably by system: (system, key) order, each system's stars contiguous
         for (int shift = 0; shift < 16; shift += 8) {
             k_rs_hist<true><<<ntiles, kRsThreads, 0, s>>>(kin, vin, sys_of, b.info, shift, ntiles, b.hist);
             GBH_LAUNCH_CHECK();
@@ -1611,7 +1953,8 @@ cudaError_t tree_build(const Launch &L, TreeBufs &b, int64_t n, const double *px
     const int32_t *sid = forest ? b.sid_sorted : nullptr;
     k_chain_count<<<nb, kThreads, 0, s>>>(b.keys, b.info, sid, b.geo, leaf, cnt);
     GBH_LAUNCH_CHECK();
-    e = scan_dyn(L, cnt, base, cap, &b.info->nstars, b.scan_tmp, b.scan_tmp_cap);
+    e = os ? scan_lb(L, b, 1, cnt, base, cap, &b.info->nstars)
+           : scan_dyn(L, cnt, base, cap, &b.info->nstars, b.scan_tmp, b.scan_tmp_cap);
     if (e != cudaSuccess) return e;
     e = cudaMemsetAsync(b.pre_mask, 0, sizeof(uint32_t) * size_t(b.cap_nodes), s);
     if (e == cudaSuccess) e = cudaMemsetAsync(b.pre_nchild, 0, sizeof(uint32_t) * size_t(b.cap_nodes), s);
@@ -1619,7 +1962,8 @@ cudaError_t tree_build(const Launch &L, TreeBufs &b, int64_t n, const double *px
     k_chain_emit<<<nb, kThreads, 0, s>>>(b.keys, b.info, cnt, base, b.pre_parent, b.pre_info, b.pre_nchild, b.pre_mask,
                                          b.leaves, sid, b.geo);
     GBH_LAUNCH_CHECK();
-    e = scan_dyn(L, b.pre_nchild, b.pre_nchild, b.cap_nodes, &b.info->nnodes, b.scan_tmp, b.scan_tmp_cap);
+    e = os ? scan_lb(L, b, 2, b.pre_nchild, b.pre_nchild, b.cap_nodes, &b.info->nnodes)
+           : scan_dyn(L, b.pre_nchild, b.pre_nchild, b.cap_nodes, &b.info->nnodes, b.scan_tmp, b.scan_tmp_cap);
     if (e != cudaSuccess) return e;
     k_ref_index<<<nb, kThreads, 0, s>>>(b.info, cnt, base, b.pre_parent, b.pre_info, b.pre_mask, b.pre_nchild,
                                         b.pre_ref, sid, b.geo);

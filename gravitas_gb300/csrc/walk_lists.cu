@@ -117,9 +117,11 @@ __device__ __forceinline__ float2 sep(float2 h, float2 l, float nt, float nh, fl
     else return add2(h, f2(nt));
 }
 
-// Evaluates the node list (count entries, padded to pairs) for the lane's star.
-template <bool kExact, bool kQuad, bool kSoft>
-__device__ __forceinline__ void eval_nodes(const WarpMem &W, int count, const Target &t, float eps2, Acc &a) {
+// Evaluates the node list (count entries, padded to pairs) for the lane's kS stars: each pair of
+// records is read once and evaluated for every star of the lane.
+template <bool kExact, bool kQuad, bool kSoft, int kS>
+__device__ __forceinline__ void eval_nodes(const WarpMem &W, int count, const Target (&t)[kS], float eps2,
+                                           Acc (&a)[kS]) {
     using Lay = Layout<kExact>;
     const float2 e2 = f2(eps2);
     const int np = (count + 1) >> 1;
@@ -134,51 +136,61 @@ __device__ __forceinline__ void eval_nodes(const WarpMem &W, int count, const Ta
             ly = hi2(r5);
             lz = lo2(r6);
         }
-        const float2 dx = sep<kExact>(lo2(r0), lx, -t.tx, -t.hx, -t.lx);
-        const float2 dy = sep<kExact>(hi2(r0), ly, -t.ty, -t.hy, -t.ly);
-        const float2 dz = sep<kExact>(lo2(r1), lz, -t.tz, -t.hz, -t.lz);
-        const float2 r2 = fma2(dz, dz, fma2(dy, dy, fma2(dx, dx, e2)));
-        float2 ir;
-        if constexpr (kSoft) {
-            ir = make_float2(rsqrtf(r2.x), rsqrtf(r2.y));
-        } else {  // an accepted node never sits on a star (d2 >= crit2 > 0); kept for safety
-            ir = make_float2(r2.x > 0.f ? rsqrtf(r2.x) : 0.f, r2.y > 0.f ? rsqrtf(r2.y) : 0.f);
-        }
-        const float2 ir2 = mul2(ir, ir);
-        const float2 ir3 = mul2(ir2, ir);
-        const float2 mir3 = mul2(hi2(r1), ir3);
+        float4 r2a, r3, r4;
         if constexpr (kQuad) {
-            const float4 r2a = r[2], r3 = r[3], r4 = r[4];
-            // q = -Q.d (the record holds -Q): qx = -(qxx dx + qxy dy + qxz dz), ...
-            const float2 qx = fma2(lo2(r4), dz, fma2(hi2(r3), dy, mul2(lo2(r2a), dx)));
-            const float2 qy = fma2(hi2(r4), dz, fma2(hi2(r2a), dy, mul2(hi2(r3), dx)));
-            const float2 qz = fma2(lo2(r3), dz, fma2(hi2(r4), dy, mul2(lo2(r4), dx)));
-            const float2 dqd = fma2(dz, qz, fma2(dy, qy, mul2(dx, qx)));  // -(d.Q.d)
-            const float2 ir5 = mul2(ir3, ir2);
-            // f = m / r^3 + 5/2 (d.Q.d) / r^7;  a += f d - Q.d / r^5 (bh.go:117-133)
-            const float2 f = fma2(mul2(dqd, mul2(ir5, ir2)), f2(-2.5f), mir3);
-            a.px = fma2(ir5, qx, fma2(f, dx, a.px));
-            a.py = fma2(ir5, qy, fma2(f, dy, a.py));
-            a.pz = fma2(ir5, qz, fma2(f, dz, a.pz));
-        } else {
-            a.px = fma2(mir3, dx, a.px);
-            a.py = fma2(mir3, dy, a.py);
-            a.pz = fma2(mir3, dz, a.pz);
+            r2a = r[2];
+            r3 = r[3];
+            r4 = r[4];
+        }
+#pragma unroll
+        for (int q = 0; q < kS; ++q) {
+            const float2 dx = sep<kExact>(lo2(r0), lx, -t[q].tx, -t[q].hx, -t[q].lx);
+            const float2 dy = sep<kExact>(hi2(r0), ly, -t[q].ty, -t[q].hy, -t[q].ly);
+            const float2 dz = sep<kExact>(lo2(r1), lz, -t[q].tz, -t[q].hz, -t[q].lz);
+            const float2 r2 = fma2(dz, dz, fma2(dy, dy, fma2(dx, dx, e2)));
+            float2 ir;
+            if constexpr (kSoft) {
+                ir = make_float2(rsqrtf(r2.x), rsqrtf(r2.y));
+            } else {  // an accepted node never sits on a star (d2 >= crit2 > 0); kept for safety
+                ir = make_float2(r2.x > 0.f ? rsqrtf(r2.x) : 0.f, r2.y > 0.f ? rsqrtf(r2.y) : 0.f);
+            }
+            const float2 ir2 = mul2(ir, ir);
+            const float2 ir3 = mul2(ir2, ir);
+            const float2 mir3 = mul2(hi2(r1), ir3);
+            if constexpr (kQuad) {
+                // q = -Q.d (the record holds -Q): qx = -(qxx dx + qxy dy + qxz dz), ...
+                const float2 qx = fma2(lo2(r4), dz, fma2(hi2(r3), dy, mul2(lo2(r2a), dx)));
+                const float2 qy = fma2(hi2(r4), dz, fma2(hi2(r2a), dy, mul2(hi2(r3), dx)));
+                const float2 qz = fma2(lo2(r3), dz, fma2(hi2(r4), dy, mul2(lo2(r4), dx)));
+                const float2 dqd = fma2(dz, qz, fma2(dy, qy, mul2(dx, qx)));  // -(d.Q.d)
+                const float2 ir5 = mul2(ir3, ir2);
+                // f = m / r^3 + 5/2 (d.Q.d) / r^7;  a += f d - Q.d / r^5 (bh.go:117-133)
+                const float2 f = fma2(mul2(dqd, mul2(ir5, ir2)), f2(-2.5f), mir3);
+                a[q].px = fma2(ir5, qx, fma2(f, dx, a[q].px));
+                a[q].py = fma2(ir5, qy, fma2(f, dy, a[q].py));
+                a[q].pz = fma2(ir5, qz, fma2(f, dz, a[q].pz));
+            } else {
+                a[q].px = fma2(mir3, dx, a[q].px);
+                a[q].py = fma2(mir3, dy, a[q].py);
+                a[q].pz = fma2(mir3, dz, a[q].pz);
+            }
         }
     }
-    a.fold();
+#pragma unroll
+    for (int q = 0; q < kS; ++q) a[q].fold();
 }
 
 // Evaluates the source list (leaf stars, count entries padded to pairs): m / (r^2 + eps^2)^(3/2).
 // A star paired with itself has a separation of exactly 0 (its record and its target are formed by
 // the same operations), which adds 0 with softening, as skipping j == self does (bh.go:142-144);
 // without softening r2 = 0 is masked.
-template <bool kExact, bool kSoft>
-__device__ __forceinline__ void eval_sources(const WarpMem &W, int count, const Target &t, float eps2, Acc &a) {
+template <bool kExact, bool kSoft, int kS>
+__device__ __forceinline__ void eval_sources(const WarpMem &W, int count, const Target (&t)[kS], float eps2,
+                                             Acc (&a)[kS]) {
     using Lay = Layout<kExact>;
     const float2 e2 = f2(eps2);
     const int np = (count + 1) >> 1;
-#pragma unroll 4
+#pragma unroll(kS == 1 ? 4 : 2)
     for (int p = 0; p < np; ++p) {
         const float4 *r = &W.sbuf[p * Lay::kSrcPair];
         const float4 r0 = r[0], r1 = r[1];
@@ -189,22 +201,26 @@ __device__ __forceinline__ void eval_sources(const WarpMem &W, int count, const 
             ly = hi2(r2a);
             lz = lo2(r3);
         }
-        const float2 dx = sep<kExact>(lo2(r0), lx, -t.tx, -t.hx, -t.lx);
-        const float2 dy = sep<kExact>(hi2(r0), ly, -t.ty, -t.hy, -t.ly);
-        const float2 dz = sep<kExact>(lo2(r1), lz, -t.tz, -t.hz, -t.lz);
-        const float2 r2 = fma2(dz, dz, fma2(dy, dy, fma2(dx, dx, e2)));
-        float2 ir;
-        if constexpr (kSoft) {
-            ir = make_float2(rsqrtf(r2.x), rsqrtf(r2.y));
-        } else {
-            ir = make_float2(r2.x > 0.f ? rsqrtf(r2.x) : 0.f, r2.y > 0.f ? rsqrtf(r2.y) : 0.f);
+#pragma unroll
+        for (int q = 0; q < kS; ++q) {
+            const float2 dx = sep<kExact>(lo2(r0), lx, -t[q].tx, -t[q].hx, -t[q].lx);
+            const float2 dy = sep<kExact>(hi2(r0), ly, -t[q].ty, -t[q].hy, -t[q].ly);
+            const float2 dz = sep<kExact>(lo2(r1), lz, -t[q].tz, -t[q].hz, -t[q].lz);
+            const float2 r2 = fma2(dz, dz, fma2(dy, dy, fma2(dx, dx, e2)));
+            float2 ir;
+            if constexpr (kSoft) {
+                ir = make_float2(rsqrtf(r2.x), rsqrtf(r2.y));
+            } else {
+                ir = make_float2(r2.x > 0.f ? rsqrtf(r2.x) : 0.f, r2.y > 0.f ? rsqrtf(r2.y) : 0.f);
+            }
+            const float2 f = mul2(mul2(hi2(r1), ir), mul2(ir, ir));
+            a[q].px = fma2(f, dx, a[q].px);
+            a[q].py = fma2(f, dy, a[q].py);
+            a[q].pz = fma2(f, dz, a[q].pz);
         }
-        const float2 f = mul2(mul2(hi2(r1), ir), mul2(ir, ir));
-        a.px = fma2(f, dx, a.px);
-        a.py = fma2(f, dy, a.py);
-        a.pz = fma2(f, dz, a.pz);
     }
-    a.fold();
+#pragma unroll
+    for (int q = 0; q < kS; ++q) a[q].fold();
 }
 
 // Writes field f of list entry e into a pair-interleaved record buffer.
@@ -231,13 +247,13 @@ struct GroupOut {
 };
 
 // Walks one group with the given separation form; a is zeroed by the caller.
-template <bool kExact, bool kQuad, bool kSoft>
-__device__ __forceinline__ GroupOut walk_group(WarpMem &W, int lane, int32_t root, const Target &t, float Ox,
+template <bool kExact, bool kQuad, bool kSoft, int kS>
+__device__ __forceinline__ GroupOut walk_group(WarpMem &W, int lane, int32_t root, const Target (&t)[kS], float Ox,
                                                float Oy, float Oz, float bx0, float by0, float bz0, float bx1,
                                                float by1, float bz1, float ext, float eps2, int node_depth,
                                                int src_depth, const LNode *__restrict__ nodes,
                                                const float4 *__restrict__ st_hi, const float4 *__restrict__ st_lo,
-                                               int32_t nn, int32_t ns, DevInfo *err_info, Acc &a) {
+                                               int32_t nn, int32_t ns, DevInfo *err_info, Acc (&a)[kS]) {
     using Lay = Layout<kExact>;
     constexpr int kNodeFields = kExact ? 13 : 10;
     constexpr int kSrcFields = kExact ? 7 : 4;
@@ -252,16 +268,22 @@ __device__ __forceinline__ GroupOut walk_group(WarpMem &W, int lane, int32_t roo
         W.lvl[0] = 0;
     }
     __syncwarp();
-    const float2 ntx = f2(-t.tx), nty = f2(-t.ty), ntz = f2(-t.tz);
+    float2 ntx[kS], nty[kS], ntz[kS];
+#pragma unroll
+    for (int q = 0; q < kS; ++q) {
+        ntx[q] = f2(-t[q].tx);
+        nty[q] = f2(-t[q].ty);
+        ntz[q] = f2(-t[q].tz);
+    }
     auto flush_nodes = [&]() {
         pad_pair<Lay::kNodePair, kNodeFields>(W.nbuf, ncount, lane, 3, 4, 9);
-        eval_nodes<kExact, kQuad, kSoft>(W, ncount, t, eps2, a);
+        eval_nodes<kExact, kQuad, kSoft, kS>(W, ncount, t, eps2, a);
         __syncwarp();
         ncount = 0;
     };
     auto flush_sources = [&]() {
         pad_pair<Lay::kSrcPair, kSrcFields>(W.sbuf, scount, lane, 3, 32, 32);
-        eval_sources<kExact, kSoft>(W, scount, t, eps2, a);
+        eval_sources<kExact, kSoft, kS>(W, scount, t, eps2, a);
         __syncwarp();
         scount = 0;
     };
@@ -291,11 +313,15 @@ __device__ __forceinline__ GroupOut walk_group(WarpMem &W, int lane, int32_t roo
         tested += uint32_t(total);
         // ---- test: the group's box, then (all lanes at once) every star for what the box keeps
         bool acc = false, bad = node >= nn;
-        float4 na = make_float4(0.f, 0.f, 0.f, 0.f), nb = na;
+        float4 na = make_float4(0.f, 0.f, 0.f, 0.f), nb = na, nc = na, nd = na;
         float cx = 0.f, cy = 0.f, cz = 0.f, lim = 0.f;
         if (node >= 0 && !bad) {
             na = nodes[node].a;
             nb = nodes[node].b;
+            if constexpr (kS == 2) {  // the whole record at once (measured faster with two stars a lane)
+                nc = nodes[node].c;
+                nd = nodes[node].d;
+            }
             cx = (na.x - Ox) + nb.x;
             cy = (na.y - Oy) + nb.y;
             cz = (na.z - Oz) + nb.z;
@@ -314,8 +340,8 @@ __device__ __forceinline__ GroupOut walk_group(WarpMem &W, int lane, int32_t roo
         }
         const unsigned mref = __ballot_sync(kFull, node >= 0 && !bad && !acc);
         if (mref) {
-            // the box keeps these nodes: each lane tests its own star against two of them at once
-            // (packed FP32x2); lanes beyond the group repeat the first star
+            // the box keeps these nodes: each lane tests its own stars against two of them at once
+            // (packed FP32x2); stars beyond the group repeat the group's first star
             const int slot = __popc(mref & lt), nref = __popc(mref);
             if ((mref >> lane) & 1u) {
                 float *rq = reinterpret_cast<float *>(&W.rq[0]) + (slot >> 1) * 8 + (slot & 1);
@@ -336,11 +362,17 @@ __device__ __forceinline__ GroupOut walk_group(WarpMem &W, int lane, int32_t roo
             for (int p = 0; p < nref; p += 2) {
                 const float4 r0 = reinterpret_cast<const float4 *>(&W.rq[0])[p >> 1 << 1];
                 const float4 r1 = reinterpret_cast<const float4 *>(&W.rq[0])[(p >> 1 << 1) + 1];
-                const float2 ex = add2(lo2(r0), ntx), ey = add2(hi2(r0), nty), ez = add2(lo2(r1), ntz);
-                const float2 d2 = fma2(ez, ez, fma2(ey, ey, mul2(ex, ex)));
                 const float2 ql = hi2(r1);
-                near |= (__any_sync(kFull, d2.x < ql.x) ? 1u : 0u) << p;
-                near |= (__any_sync(kFull, d2.y < ql.y) ? 1u : 0u) << (p + 1);
+                bool nx = false, ny = false;
+#pragma unroll
+                for (int q = 0; q < kS; ++q) {
+                    const float2 ex = add2(lo2(r0), ntx[q]), ey = add2(hi2(r0), nty[q]), ez = add2(lo2(r1), ntz[q]);
+                    const float2 d2 = fma2(ez, ez, fma2(ey, ey, mul2(ex, ex)));
+                    nx |= d2.x < ql.x;
+                    ny |= d2.y < ql.y;
+                }
+                near |= (__any_sync(kFull, nx) ? 1u : 0u) << p;
+                near |= (__any_sync(kFull, ny) ? 1u : 0u) << (p + 1);
             }
             __syncwarp();
             if ((mref >> lane) & 1u) acc = !((near >> slot) & 1u);
@@ -372,7 +404,7 @@ __device__ __forceinline__ GroupOut walk_group(WarpMem &W, int lane, int32_t roo
         if (ma) {
             if (acc) {
                 const int en = ncount + __popc(ma & lt);
-                const float4 qc = nodes[node].c, qd = nodes[node].d;
+                const float4 qc = kS == 2 ? nc : nodes[node].c, qd = kS == 2 ? nd : nodes[node].d;
                 constexpr int P = Lay::kNodePair;
                 if constexpr (kExact) {
                     put(W.nbuf, P, en, 0, na.x);
@@ -404,7 +436,7 @@ __device__ __forceinline__ GroupOut walk_group(WarpMem &W, int lane, int32_t roo
         const unsigned ml = __ballot_sync(kFull, open_leaf);
         if (ml) {
             const int lo = open_leaf ? int(link) : 0;
-            const int hi = open_leaf ? __float_as_int(nodes[node].d.w) : 0;
+            const int hi = open_leaf ? __float_as_int(kS == 2 ? nd.w : nodes[node].d.w) : 0;
             if (__any_sync(kFull, open_leaf && (lo < 0 || hi > ns || lo >= hi))) {
                 if (lane == 0) set_err(err_info, 8);
                 return GroupOut{0, false};
@@ -456,10 +488,10 @@ __device__ __forceinline__ GroupOut walk_group(WarpMem &W, int lane, int32_t roo
     }
     if (ncount) flush_nodes();
     if (scount) flush_sources();
-    return GroupOut{(31u * acc_nodes + 12u * pairs) / 16u + tested, true};
+    return GroupOut{(31u * acc_nodes + 12u * pairs) * uint32_t(kS) / 16u + tested, true};
 }
 
-template <bool kQuad, bool kSoft>
+template <bool kQuad, bool kSoft, int kS>
 __global__ __launch_bounds__(kLwThreads) void k_walk_lists(const DevInfo *info, const LNode *__restrict__ nodes,
                                                            const float4 *__restrict__ st_hi,
                                                            const float4 *__restrict__ st_lo,
@@ -470,15 +502,16 @@ __global__ __launch_bounds__(kLwThreads) void k_walk_lists(const DevInfo *info, 
                                                            const int32_t *__restrict__ gperm, int32_t perm_cap,
                                                            uint32_t *gcost, uint32_t *work_ctr, DevInfo *err_info,
                                                            int node_depth, int src_depth) {
+    constexpr int kG = 32 * kS;  // stars per group: lane l holds stars l, 32 + l, ...
     __shared__ WarpMem smem[kLwWarps];
     WarpMem &W = smem[threadIdx.x >> 5];
     const int lane = threadIdx.x & 31;
     const int32_t ns = int32_t(info->nstars);
     const int32_t nn = int32_t(info->nnodes);
     const bool forest = groups != nullptr;
-    // a target list (block steps): groups of 32 consecutive entries; else every star
+    // a target list (block steps): groups of kG consecutive entries; else every star
     const int32_t nt = targets ? int32_t(info->ntargets) : ns;
-    const int32_t ng = nn > 0 ? (forest ? int32_t(info->ngroups) : (nt + 31) / 32) : 0;
+    const int32_t ng = nn > 0 ? (forest ? int32_t(info->ngroups) : (nt + kG - 1) / kG) : 0;
     const bool lpt = gperm && gperm[perm_cap] == ng;
     for (;;) {
         int32_t idx = 0;
@@ -493,30 +526,65 @@ __global__ __launch_bounds__(kLwThreads) void k_walk_lists(const DevInfo *info, 
             cnt = ge.y;
             root = ge.z;
         } else {
-            base = g * 32;
-            cnt = nt - base < 32 ? nt - base : 32;
+            base = g * kG;
+            cnt = nt - base < kG ? nt - base : kG;
         }
         if (cnt <= 0) continue;
-        if (cnt > 32) cnt = 32;
-        const bool valid = lane < cnt;
-        const int32_t k = targets ? targets[base + (valid ? lane : 0)] : base + (valid ? lane : 0);
-        const float4 h = st_hi[k], l = st_lo[k];
-        const float Ox = __shfl_sync(kFull, h.x, 0), Oy = __shfl_sync(kFull, h.y, 0), Oz = __shfl_sync(kFull, h.z, 0);
-        Target t;
-        t.tx = (h.x - Ox) + l.x;
-        t.ty = (h.y - Oy) + l.y;
-        t.tz = (h.z - Oz) + l.z;
-        t.hx = h.x;
-        t.hy = h.y;
-        t.hz = h.z;
-        t.lx = l.x;
-        t.ly = l.y;
-        t.lz = l.z;
-        // the group's box, its extent from the origin and the spacing of consecutive stars
-        float bx0 = t.tx, by0 = t.ty, bz0 = t.tz, bx1 = t.tx, by1 = t.ty, bz1 = t.tz;
-        const float nx = __shfl_down_sync(kFull, t.tx, 1), ny = __shfl_down_sync(kFull, t.ty, 1),
-                    nz = __shfl_down_sync(kFull, t.tz, 1);
-        float gap = lane + 1 < cnt ? fmaxf(fabsf(nx - t.tx), fmaxf(fabsf(ny - t.ty), fabsf(nz - t.tz))) : 3.0e38f;
+        if (cnt > kG) cnt = kG;
+        // the lane's stars; a star beyond the group repeats the group's first star
+        bool valid[kS];
+        int32_t k[kS];
+        float4 h[kS], l[kS];
+#pragma unroll
+        for (int q = 0; q < kS; ++q) {
+            valid[q] = 32 * q + lane < cnt;
+            const int32_t e = base + (valid[q] ? 32 * q + lane : 0);
+            k[q] = targets ? targets[e] : e;
+            h[q] = st_hi[k[q]];
+            l[q] = st_lo[k[q]];
+        }
+        const float Ox = __shfl_sync(kFull, h[0].x, 0), Oy = __shfl_sync(kFull, h[0].y, 0),
+                    Oz = __shfl_sync(kFull, h[0].z, 0);
+        Target t[kS];
+#pragma unroll
+        for (int q = 0; q < kS; ++q) {
+            t[q].tx = (h[q].x - Ox) + l[q].x;
+            t[q].ty = (h[q].y - Oy) + l[q].y;
+            t[q].tz = (h[q].z - Oz) + l[q].z;
+            t[q].hx = h[q].x;
+            t[q].hy = h[q].y;
+            t[q].hz = h[q].z;
+            t[q].lx = l[q].x;
+            t[q].ly = l[q].y;
+            t[q].lz = l[q].z;
+        }
+        // the group's box, its extent from the origin and the spacing of consecutive stars (star
+        // 32 q + lane is followed by 32 q + lane + 1: the next lane's, or lane 0's next star)
+        float bx0 = t[0].tx, by0 = t[0].ty, bz0 = t[0].tz, bx1 = bx0, by1 = by0, bz1 = bz0;
+        float gap = 3.0e38f;
+#pragma unroll
+        for (int q = 0; q < kS; ++q) {
+            bx0 = fminf(bx0, t[q].tx);
+            by0 = fminf(by0, t[q].ty);
+            bz0 = fminf(bz0, t[q].tz);
+            bx1 = fmaxf(bx1, t[q].tx);
+            by1 = fmaxf(by1, t[q].ty);
+            bz1 = fmaxf(bz1, t[q].tz);
+            float nx = __shfl_down_sync(kFull, t[q].tx, 1), ny = __shfl_down_sync(kFull, t[q].ty, 1),
+                  nz = __shfl_down_sync(kFull, t[q].tz, 1);
+            if (q + 1 < kS) {
+                const float wx = __shfl_sync(kFull, t[q + 1 < kS ? q + 1 : q].tx, 0);
+                const float wy = __shfl_sync(kFull, t[q + 1 < kS ? q + 1 : q].ty, 0);
+                const float wz = __shfl_sync(kFull, t[q + 1 < kS ? q + 1 : q].tz, 0);
+                if (lane == 31) {
+                    nx = wx;
+                    ny = wy;
+                    nz = wz;
+                }
+            }
+            if (32 * q + lane + 1 < cnt)
+                gap = fminf(gap, fmaxf(fabsf(nx - t[q].tx), fmaxf(fabsf(ny - t[q].ty), fabsf(nz - t[q].tz))));
+        }
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
             bx0 = fminf(bx0, __shfl_xor_sync(kFull, bx0, o));
@@ -534,36 +602,42 @@ __global__ __launch_bounds__(kLwThreads) void k_walk_lists(const DevInfo *info, 
         // closest consecutive stars. Beyond that (a group across a jump of the Morton curve) the
         // separations take the hi and lo parts apart.
         const bool exact = ext > 4096.f * fmaxf(eps, gap);
-        Acc a;
-        a.px = a.py = a.pz = f2(0.f);
-        a.sx = a.sy = a.sz = a.cx = a.cy = a.cz = 0.f;
+        Acc a[kS];
+#pragma unroll
+        for (int q = 0; q < kS; ++q) {
+            a[q].px = a[q].py = a[q].pz = f2(0.f);
+            a[q].sx = a[q].sy = a[q].sz = a[q].cx = a[q].cy = a[q].cz = 0.f;
+        }
         GroupOut r;
         if (exact)
-            r = walk_group<true, kQuad, kSoft>(W, lane, root, t, Ox, Oy, Oz, bx0, by0, bz0, bx1, by1, bz1, ext,
-                                                eps2, node_depth, src_depth, nodes, st_hi, st_lo, nn, ns,
-                                                err_info, a);
+            r = walk_group<true, kQuad, kSoft, kS>(W, lane, root, t, Ox, Oy, Oz, bx0, by0, bz0, bx1, by1, bz1, ext,
+                                                    eps2, node_depth, src_depth, nodes, st_hi, st_lo, nn, ns,
+                                                    err_info, a);
         else
-            r = walk_group<false, kQuad, kSoft>(W, lane, root, t, Ox, Oy, Oz, bx0, by0, bz0, bx1, by1, bz1, ext,
-                                                 eps2, node_depth, src_depth, nodes, st_hi, st_lo, nn, ns,
-                                                 err_info, a);
+            r = walk_group<false, kQuad, kSoft, kS>(W, lane, root, t, Ox, Oy, Oz, bx0, by0, bz0, bx1, by1, bz1, ext,
+                                                     eps2, node_depth, src_depth, nodes, st_hi, st_lo, nn, ns,
+                                                     err_info, a);
         __syncwarp();
         if (!r.ok) break;  // the error flag is set; the host reports GBH_ERR_LIMIT
         if (gcost && lane == 0) gcost[g] = r.cost;
-        if (valid) {
-            const int32_t o = order[k];
-            ax[o] = double(a.sx) - double(a.cx);
-            ay[o] = double(a.sy) - double(a.cy);
-            az[o] = double(a.sz) - double(a.cz);
+#pragma unroll
+        for (int q = 0; q < kS; ++q) {
+            if (valid[q]) {
+                const int32_t o = order[k[q]];
+                ax[o] = double(a[q].sx) - double(a[q].cx);
+                ay[o] = double(a[q].sy) - double(a[q].cy);
+                az[o] = double(a[q].sz) - double(a[q].cz);
+            }
         }
     }
 }
 
-template <bool kQuad, bool kSoft>
+template <bool kQuad, bool kSoft, int kS>
 cudaError_t launch_lists(const Launch &L, const TreeBufs &b, float eps2, double *ax, double *ay, double *az,
                          int node_depth, int src_depth, bool lpt, bool targets) {
     static int blocks_per_sm = 0;  // per instantiation; the same on every device of this architecture
     if (!blocks_per_sm) {
-        cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_walk_lists<kQuad, kSoft>,
+        cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_walk_lists<kQuad, kSoft, kS>,
                                                                       kLwThreads, 0);
         if (e != cudaSuccess) return e;
         if (blocks_per_sm < 1) blocks_per_sm = 1;
@@ -572,7 +646,7 @@ cudaError_t launch_lists(const Launch &L, const TreeBufs &b, float eps2, double 
     cudaError_t e = cudaMemsetAsync(b.walk_ctr, 0, sizeof(uint32_t), L.stream);
     if (e != cudaSuccess) return e;
     const int sms = L.num_sms > 0 ? L.num_sms : 152;
-    k_walk_lists<kQuad, kSoft><<<unsigned(sms * blocks_per_sm), kLwThreads, 0, L.stream>>>(
+    k_walk_lists<kQuad, kSoft, kS><<<unsigned(sms * blocks_per_sm), kLwThreads, 0, L.stream>>>(
         b.info, b.lnode, b.st_hi, b.st_lo, b.order, sqrtf(eps2), eps2, ax, ay, az,
         forest ? b.groups : nullptr, targets ? b.targets : nullptr, lpt ? b.gperm : nullptr, int32_t(b.cap_groups),
         lpt ? b.gcost : nullptr,
@@ -581,12 +655,25 @@ cudaError_t launch_lists(const Launch &L, const TreeBufs &b, float eps2, double 
     return cudaGetLastError();
 }
 
+template <int kS>
+cudaError_t walk_lists_s(const Launch &L, const TreeBufs &b, float eps2, int quad, double *ax, double *ay,
+                         double *az, int nd, int sd, bool lpt, bool targets) {
+    const bool soft = eps2 > 0.f;
+    cudaError_t e;
+    if (quad && soft) e = launch_lists<true, true, kS>(L, b, eps2, ax, ay, az, nd, sd, lpt, targets);
+    else if (quad) e = launch_lists<true, false, kS>(L, b, eps2, ax, ay, az, nd, sd, lpt, targets);
+    else if (soft) e = launch_lists<false, true, kS>(L, b, eps2, ax, ay, az, nd, sd, lpt, targets);
+    else e = launch_lists<false, false, kS>(L, b, eps2, ax, ay, az, nd, sd, lpt, targets);
+    if (e != cudaSuccess || !lpt) return e;
+    return lpt_order(L, b, 32 * kS);
+}
+
 }  // namespace
 
 int list_depth_max(bool exact) { return exact ? Layout<true>::kNodeCap - 32 : Layout<false>::kNodeCap - 32; }
 
 cudaError_t walk_lists(const Launch &L, const TreeBufs &b, float eps2, int quad, double *ax, double *ay, double *az,
-                       int list_depth, bool targets) {
+                       int list_depth, bool targets, int stars_per_lane) {
     // The list depth is the node list's flush threshold (entries per lane and evaluation); the
     // source list flushes at twice it. Both are capped so that one step's appends always fit; an
     // exact-separation group uses the smaller of its own cap and the depth.
@@ -596,14 +683,8 @@ cudaError_t walk_lists(const Launch &L, const TreeBufs &b, float eps2, int quad,
     int sd = 2 * nd;
     if (sd > Layout<false>::kSrcCap - 32) sd = Layout<false>::kSrcCap - 32;
     const bool lpt = b.lpt && !targets;  // a target list changes from event to event
-    const bool soft = eps2 > 0.f;
-    cudaError_t e;
-    if (quad && soft) e = launch_lists<true, true>(L, b, eps2, ax, ay, az, nd, sd, lpt, targets);
-    else if (quad) e = launch_lists<true, false>(L, b, eps2, ax, ay, az, nd, sd, lpt, targets);
-    else if (soft) e = launch_lists<false, true>(L, b, eps2, ax, ay, az, nd, sd, lpt, targets);
-    else e = launch_lists<false, false>(L, b, eps2, ax, ay, az, nd, sd, lpt, targets);
-    if (e != cudaSuccess || !lpt) return e;
-    return lpt_order(L, b, 32);
+    if (stars_per_lane == 2) return walk_lists_s<2>(L, b, eps2, quad, ax, ay, az, nd, sd, lpt, targets);
+    return walk_lists_s<1>(L, b, eps2, quad, ax, ay, az, nd, sd, lpt, targets);
 }
 
 }  // namespace gbh

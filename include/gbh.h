@@ -57,12 +57,13 @@ enum {
     /* Warp-cooperative FP32 walk with compensated per-star accumulation and
        separations formed from hi + lo splits of the FP64 positions; every star
        sees each accepted node exactly where the reference walk accepts it, or
-       deeper. Two kernels (see group_size): the list walk, one warp per 32
-       Morton-consecutive stars that builds the group's interaction lists with
-       node-parallel opening tests and evaluates them from shared memory two
-       entries at a time in packed FP32x2 arithmetic; and the paired walk, one
-       warp per 64 stars (two per lane) walking the skip links in lockstep. The
-       default. */
+       deeper. Two kernels (see group_size): the list walk, one warp per 32 or
+       64 Morton-consecutive stars (one or two a lane) that builds the group's
+       interaction lists with node-parallel opening tests and evaluates them
+       from shared memory two entries at a time in packed FP32x2 arithmetic;
+       and the paired walk, one warp per 64 stars walking the skip links in
+       lockstep, whose split mode shares a group among several warps for small
+       systems. The default. */
     GBH_WALK_MIXED = 0,
     /* One thread per star, all FP32, uncompensated: the CUDA twin of the Metal
        kernel internal/sim/bh/gpu_darwin.go:76-118. */
@@ -81,10 +82,12 @@ typedef struct {
     int32_t monopole_only;   /* drop quadrupoles of accepted nodes (bh.go:34-35) */
     int32_t dark_matter_off; /* dark matter pulls nothing (Params.DarkMatterOff, sim.go:92-98) */
     int32_t walk;            /* GBH_WALK_* */
-    int32_t group_size;      /* GBH_WALK_MIXED: 32 the list walk, 64 the paired walk, 0 the list walk
-                                except for a single system of up to 21 64-star groups per SM
-                                (below about 200,000 stars on a GB300), where the paired walk
-                                shares each group's walk among several warps (GBH_CFG_NO_SPLIT) */
+    int32_t group_size;      /* GBH_WALK_MIXED: 32 the list walk with one star a lane; 64 the list
+                                walk with two, except for a single system of up to 21 64-star
+                                groups per SM (below about 200,000 stars on a GB300), where the
+                                paired walk shares each group's walk among several warps (unless
+                                GBH_CFG_NO_SPLIT); 0: 64 for a single system of at least 524,288
+                                stars or of up to 21 groups per SM, else 32 */
     int32_t list_depth;      /* list walk: node-list entries evaluated per pass, 2 to 56 (0 means 48;
                                 source lists take twice as many, up to 160) */
     double c;                /* speed of light of the steps (Params.C): 0 Newtonian; > 0 drifts by
@@ -104,10 +107,14 @@ enum {
     GBH_CFG_NO_LPT = 4,
     /* The mixed walk of a single system never splits a group's walk over several warps. With few
        groups (up to 21 per SM: below about 200,000 stars on a GB300) each group's walk is
-       otherwise shared by 2 to 32 warps, each adding the interactions of its own range of source
-       stars, and the parts are summed in order: the same interactions, a different order of
-       summation. */
-    GBH_CFG_NO_SPLIT = 8
+       otherwise shared by 2 to 32 warps (the paired walk's split mode), each adding the
+       interactions of its own range of source stars, and the parts are summed in order: the
+       same interactions, a different order of summation. Without splitting, 64-star groups take
+       the list walk (or the paired walk, with GBH_CFG_PAIRED). */
+    GBH_CFG_NO_SPLIT = 8,
+    /* 64-star groups of the mixed walk always take the paired walk (split or not), never the
+       list walk. */
+    GBH_CFG_PAIRED = 16
 };
 
 typedef struct {
@@ -328,7 +335,7 @@ typedef struct {
     double rms_err;     /* RMS of the per-body relative force error on the sample */
     double p99_err;     /* 99th percentile of the same */
     int32_t meets;      /* rms_err <= rms_bound */
-    int32_t list_depth; /* list walk (group 32): its node-list depth; 0 for the other walks */
+    int32_t list_depth; /* mixed walk: its list walk's node-list depth; 0 for the other walks */
 } gbh_tune_entry;
 
 /*
@@ -338,7 +345,7 @@ typedef struct {
  * the shortest median force evaluation (reps timed runs, CUDA events) among those whose RMS
  * relative force error, on `sample` evenly spaced alive stars against the FP64 direct sum
  * over each star's own system, is at most rms_bound. NULL or empty lists take the defaults
- * theta {0.4, 0.5, 0.7}, leaf {4, 8, 16, 32}, group {64, 32}, and for group 32 the list
+ * theta {0.4, 0.5, 0.7}, leaf {4, 8, 16, 32}, group {64, 32}, and for the mixed walk the list
  * depths {24, 48} unless base->list_depth is set; sample <= 0 means 1024 and
  * reps <= 0 means 3. Every candidate is written to table (up to table_cap) and counted in
  * *ntable. If none meets the bound, *best is the most accurate one and the call returns

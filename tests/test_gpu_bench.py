@@ -42,6 +42,9 @@ def test_headline_line_keeps_the_contract():
     assert d["gpu_launches"] > 0
     assert set(d["clocks"]) >= {"sm_mhz", "sm_max_mhz", "reasons"}
     assert d["interactions"]["per_s"] > 0
+    cfg = d["configs"]
+    assert cfg["forest"]["value"] > 0 and cfg["forest"]["force_error_per_system"]["max_rms"] <= 2e-3
+    assert cfg["galaxy"]["value"] > 0 and cfg["galaxy"]["events"] > 0
 
 
 def test_reference_arm_line():
@@ -49,6 +52,7 @@ def test_reference_arm_line():
     assert d["impl"] == "reference" and d["value"] > 0 and d["higher_is_better"] is True
     assert d["cpu_baseline"]["value"] == d["value"] and d["cpu_baseline"]["cores"] >= 1
     assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+    assert set(d["per_leaf"]) == {"24", "32"} and d["config"]["leaf_size"] in (24, 32)
 
 
 @pytest.mark.parametrize("args,keys", [

@@ -142,7 +142,7 @@ def test_autotune_on_a_forest_meets_the_bound(ctx):
     base = abi.make_params(0.5, 0.01, 8, False, False, "mixed")
     best, table = ctx.autotune(base, thetas=[0.4, 0.7], leaves=[8, 16], groups=[64, 32], rms_bound=2e-3,
                                sample=512, reps=2, strict=True)
-    assert len(table) == 12  # group 64, and group 32 (the list walk) at two list depths
+    assert len(table) == 16  # groups 64 and 32 (the list walk), each at two list depths
     meets = [e for e in table if e["meets"]]
     assert meets and min(e["ms"] for e in meets) == min(
         e["ms"] for e in meets if (e["theta"], e["leaf_size"], e["group_size"], e["list_depth"]) ==

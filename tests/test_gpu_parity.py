@@ -230,7 +230,7 @@ def test_split_walk_adds_the_same_interactions(ctx, n, group, scene):
         s["alive"][7::97] = 0
     n = len(s["px"])
     dm_off = scene == "disk"
-    whole = abi.Context(0, abi.CFG_NO_SPLIT)
+    whole = abi.Context(0, abi.CFG_NO_SPLIT | abi.CFG_PAIRED)  # the paired walk, unsplit
     try:
         par = abi.make_params(0.5, 0.02, 16, False, dm_off, "mixed", group_size=group)
         got = []
@@ -520,9 +520,9 @@ def test_autotune_single_system(ctx):
              P(s["mass"]), None, None)
     base = abi.make_params(0.5, 0.01, 8, False, False, "mixed")
     best, table = ctx.autotune(base, rms_bound=2e-3, sample=1024, reps=2, strict=True)
-    assert len(table) == 3 * 4 * 3  # group 64, and group 32 (the list walk) at list depths 24 and 48
+    assert len(table) == 3 * 4 * 4  # groups 64 and 32, each at list depths 24 and 48
     assert {(e["theta"], e["leaf_size"], e["group_size"], e["list_depth"]) for e in table} == {
-        (t, l, g, d) for t in (0.4, 0.5, 0.7) for l in (4, 8, 16, 32) for g, d in ((64, 0), (32, 24), (32, 48))}
+        (t, l, g, d) for t in (0.4, 0.5, 0.7) for l in (4, 8, 16, 32) for g in (64, 32) for d in (24, 48)}
     for e in table:  # the error estimate does not depend on the timing
         assert 0 < e["rms_err"] < 2e-2 and e["ms"] > 0 and e["build_ms"] > 0 and e["walk_ms"] > 0
     chosen = [e for e in table if (e["theta"], e["leaf_size"], e["group_size"], e["list_depth"]) ==
@@ -530,7 +530,7 @@ def test_autotune_single_system(ctx):
     assert chosen["meets"] and chosen["ms"] == min(e["ms"] for e in table if e["meets"])
     # an unreachable bound: the most accurate candidate and GBH_ERR_LIMIT
     best2, table2 = ctx.autotune(base, thetas=[0.7], leaves=[16], groups=[64], rms_bound=1e-9, sample=64, reps=1)
-    assert len(table2) == 1 and not table2[0]["meets"] and best2.theta == 0.7
+    assert len(table2) == 2 and not any(e["meets"] for e in table2) and best2.theta == 0.7
     with pytest.raises(abi.GbhError) as ei:
         ctx.autotune(base, thetas=[0.7], leaves=[16], groups=[64], rms_bound=1e-9, sample=64, reps=1, strict=True)
     assert ei.value.code == abi.ERR_LIMIT
