@@ -227,11 +227,12 @@ double theta_of(const gbh_params *p) { return p->theta == 0 ? 0.9 : p->theta; } 
 
 // Stars per group of the mixed walk: 32 (the list walk, one star a lane) or 64 (the list walk with
 // two, or for a single system with so few groups per SM that the paired walk shares each group
-// among several warps, that walk). By default 64 for large single systems (two stars a lane:
-// 0.93x the walk time of one on the 1M merger) and small ones (split walks), else 32.
+// among several warps, that walk). By default 64 for forests and large single systems (two stars
+// a lane: 0.93x the walk time of one on the 1M merger, and the autotuner's pick on the 64-system
+// forest) and for small ones (split walks), else 32.
 int group_of(const gbh_params *p, int64_t n, bool forest) {
     if (p->group_size == 32 || p->group_size == 64) return p->group_size;
-    if (forest) return 32;
+    if (forest) return 64;
     return gbh::walk_parts(n, 64) > 1 || n >= (int64_t(1) << 19) ? 64 : 32;
 }
 int leaf_of(const gbh_params *p) { return p->leaf_size > 0 ? p->leaf_size : 24; }  // bh.go:17-19

@@ -86,8 +86,8 @@ typedef struct {
                                 walk with two, except for a single system of up to 21 64-star
                                 groups per SM (below about 200,000 stars on a GB300), where the
                                 paired walk shares each group's walk among several warps (unless
-                                GBH_CFG_NO_SPLIT); 0: 64 for a single system of at least 524,288
-                                stars or of up to 21 groups per SM, else 32 */
+                                GBH_CFG_NO_SPLIT); 0: 64 for a forest and for a single system of
+                                at least 524,288 stars or of up to 21 groups per SM, else 32 */
     int32_t list_depth;      /* list walk: node-list entries evaluated per pass, 2 to 56 (0 means 48;
                                 source lists take twice as many, up to 160) */
     double c;                /* speed of light of the steps (Params.C): 0 Newtonian; > 0 drifts by
