@@ -96,6 +96,7 @@ struct TreeBufs {
     int32_t list_depth = 0; // the list walk's node-list depth (0: kDefaultListDepth), set per call
     // compaction / bbox
     uint32_t *flag = nullptr;     // star flags, then their exclusive scan
+    double4 *pos4 = nullptr;      // (x, y, z, m) of every star in state order, one 32-byte record
     double *bbox_part = nullptr;  // per-block partial min/max (6 per block)
     // sort
     uint64_t *keys = nullptr, *keys_alt = nullptr;

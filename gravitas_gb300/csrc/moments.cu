@@ -13,6 +13,8 @@
 // to FP32 rounding; the FP64 walk uses the bit-exact upsweep of tree.cu instead.
 #include <cuda_runtime.h>
 
+#include <cuda/atomic>
+
 #include "gbh_internal.cuh"
 
 namespace gbh {
@@ -203,10 +205,11 @@ __global__ __launch_bounds__(kThreads) void k_upsweep_fast(const uint64_t *__res
         int32_t par = n_parent[cur];
         if (par < 0) break;
         uint32_t nch = (n_info[par] >> 8) & 0xffu;
-        __threadfence();
-        int old = atomicAdd(&n_arrive[par], 1);
+        // arrival counter with acquire-release ordering: this child's records are visible to the
+        // last child to arrive, which reads every child's records after its own increment
+        cuda::atomic_ref<int, cuda::thread_scope_device> arrive(n_arrive[par]);
+        const int old = arrive.fetch_add(1, cuda::memory_order_acq_rel);
         if (old != int(nch) - 1) break;
-        __threadfence();
         int32_t first = nodes[par].first;
         if (first < 0 || int64_t(first) + nch > nn) {
             set_err(err_info, 22);

@@ -331,7 +331,7 @@ __global__ __launch_bounds__(kThreads) void k_flags_bbox(int64_t n, const double
                                                          const uint8_t *__restrict__ kind,
                                                          const uint8_t *__restrict__ alive, uint32_t *__restrict__ flag,
                                                          double *__restrict__ part, double *ax, double *ay, double *az,
-                                                         DevInfo *info) {
+                                                         DevInfo *info, double4 *__restrict__ pos4) {
     if (blockIdx.x == 0 && threadIdx.x == 0) {  // the build's first kernel clears the error record
         info->err = 0;
         info->err_where = 0;
@@ -342,9 +342,11 @@ __global__ __launch_bounds__(kThreads) void k_flags_bbox(int64_t n, const double
         bool st = is_star(al, kd);
         flag[i] = st;
         if (st) {
-            long long x = ord_key(px[i]), y = ord_key(py[i]), z = ord_key(pz[i]);
+            const double vx = px[i], vy = py[i], vz = pz[i], m = mass ? mass[i] : 0.0;
+            pos4[i] = make_double4(vx, vy, vz, m);  // one record for k_gather's reads through the sort order
+            long long x = ord_key(vx), y = ord_key(vy), z = ord_key(vz);
             mn[0] = min(mn[0], x);
-            mx[0] = max(mx[0], mass && !isfinite(mass[i]) ? LLONG_MAX : x);
+            mx[0] = max(mx[0], mass && !isfinite(m) ? LLONG_MAX : x);
             mn[1] = min(mn[1], y);
             mx[1] = max(mx[1], y);
             mn[2] = min(mn[2], z);
@@ -384,21 +386,31 @@ __global__ __launch_bounds__(kFinalThreads) void k_bbox_final(int nparts, const 
         }
     }
     __syncthreads();
-    if (threadIdx.x != 0) return;
-    for (int w = 1; w < int(blockDim.x / 32); ++w)
-        for (int c = 0; c < 3; ++c) {
-            s[c][0] = min(s[c][0], s[c][w]);
-            s[3 + c][0] = max(s[3 + c][0], s[3 + c][w]);
-        }
+    // warp 0 reduces the warps' values (lane w holds warp w's)
+    if (warp != 0) return;
+    static_assert(kFinalThreads / 32 == 32, "one value per lane");
     double mn[3], mx[3];
     for (int c = 0; c < 3; ++c) {
-        mn[c] = ord_val(s[c][0]);
-        mx[c] = ord_val(s[3 + c][0]);
+        long long a = s[c][lane], b = s[3 + c][lane];
+        for (int o = 16; o > 0; o >>= 1) {
+            a = min(a, __shfl_xor_sync(0xffffffffu, a, o));
+            b = max(b, __shfl_xor_sync(0xffffffffu, b, o));
+        }
+        mn[c] = ord_val(a);
+        mx[c] = ord_val(b);
     }
-    int64_t ns = 0;
-    if (n > 0) ns = int64_t(scan[n - 1]) + (is_star(alive ? alive[n - 1] : 1, kind ? kind[n - 1] : 0) ? 1 : 0);
     double side = fmax(mx[0] - mn[0], fmax(mx[1] - mn[1], mx[2] - mn[2]));
     side = fmax(side * (1 + 1e-9), 1e-12);
+    // opening bases 2 half_L / theta, half_L = side / 2^(L+1): halving is exact, so lane L forms its
+    // own level's half with one exact scaling instead of L successive halvings
+    if (lane <= kMaxLevel) {
+        const double half = ldexp(side, -(lane + 1));
+        info->crit_base[lane] = __double2float_rn(2 * half / theta);
+        if (geo) geo[0].crit_base[lane] = info->crit_base[lane];
+    }
+    if (lane != 0) return;
+    int64_t ns = 0;
+    if (n > 0) ns = int64_t(scan[n - 1]) + (is_star(alive ? alive[n - 1] : 1, kind ? kind[n - 1] : 0) ? 1 : 0);
     info->minx = mn[0];
     info->miny = mn[1];
     info->minz = mn[2];
@@ -422,8 +434,6 @@ __global__ __launch_bounds__(kFinalThreads) void k_bbox_final(int nparts, const 
     float sh = __double2float_rn(side);
     info->side_hi = sh;
     info->side_lo = __double2float_rn(side - double(sh));
-    double half = side / 2;
-    for (int L = 0; L <= kMaxLevel; ++L, half = half / 2) info->crit_base[L] = __double2float_rn(2 * half / theta);
     if (geo) {  // the single system of a plain state
         SysGeo &g = geo[0];
         g.minx = info->minx;
@@ -437,7 +447,6 @@ __global__ __launch_bounds__(kFinalThreads) void k_bbox_final(int nparts, const 
         }
         g.side_hi = info->side_hi;
         g.side_lo = info->side_lo;
-        for (int L = 0; L <= kMaxLevel; ++L) g.crit_base[L] = info->crit_base[L];
         g.star_lo = 0;
         g.star_hi = int32_t(ns);
         g.root = 0;
@@ -764,10 +773,11 @@ __global__ __launch_bounds__(kRsThreads) void k_os_pass(const uint64_t *__restri
 
 // ---------------------------------------------------------------- sorted copies
 
-// build.go:34-41 with SourceMass (sim.go:93-98); FP32 hi/lo split for the walks.
+// build.go:34-41 with SourceMass (sim.go:93-98); FP32 hi/lo split for the walks. Each star's
+// position and mass come from its 32-byte record written by the collect kernel: one sector read
+// through the sort order instead of one sector per array.
 __global__ __launch_bounds__(kThreads) void k_gather(const DevInfo *info, const int32_t *__restrict__ order,
-                                                     const double *__restrict__ px, const double *__restrict__ py,
-                                                     const double *__restrict__ pz, const double *__restrict__ mass,
+                                                     const double4 *__restrict__ pos4,
                                                      const uint8_t *__restrict__ kind, int dm_off, int fp64_copies,
                                                      double *__restrict__ sx, double *__restrict__ sy,
                                                      double *__restrict__ sz, double *__restrict__ sm,
@@ -778,8 +788,9 @@ __global__ __launch_bounds__(kThreads) void k_gather(const DevInfo *info, const 
     if (k >= info->nstars) return;
     int32_t i = order[k];
     if (sys_of) sid_sorted[k] = sys_of[i];
-    double x = px[i], y = py[i], z = pz[i];
-    double m = mass[i];
+    const double4 p = pos4[i];
+    const double x = p.x, y = p.y, z = p.z;
+    double m = p.w;
     if (dm_off && kind && kind[i] == GBH_DARK_MATTER) m = 0;
     if (fp64_copies) {  // read by the FP64 upsweep, walk and potential only
         sx[k] = x;
@@ -1550,7 +1561,8 @@ __global__ __launch_bounds__(kThreads) void k_flags_sys(int64_t n, const double 
                                                         const uint8_t *__restrict__ kind,
                                                         const uint8_t *__restrict__ alive,
                                                         const uint16_t *__restrict__ sys_of, uint32_t *__restrict__ flag,
-                                                        SysGeo *geo, double *ax, double *ay, double *az) {
+                                                        SysGeo *geo, double *ax, double *ay, double *az,
+                                                        double4 *__restrict__ pos4) {
     int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     bool st = false;
     int s = -1;
@@ -1561,9 +1573,11 @@ __global__ __launch_bounds__(kThreads) void k_flags_sys(int64_t n, const double 
         flag[i] = st;
         if (st) {
             s = sys_of[i];
-            k[0] = mass && !isfinite(mass[i]) ? LLONG_MAX : ord_key(px[i]);  // as in k_flags_bbox
-            k[1] = ord_key(py[i]);
-            k[2] = ord_key(pz[i]);
+            const double vx = px[i], vy = py[i], vz = pz[i], m = mass ? mass[i] : 0.0;
+            pos4[i] = make_double4(vx, vy, vz, m);
+            k[0] = mass && !isfinite(m) ? LLONG_MAX : ord_key(vx);  // as in k_flags_bbox
+            k[1] = ord_key(vy);
+            k[2] = ord_key(vz);
         } else if (al && kd == GBH_BLACK_HOLE) {
             ax[i] = 0;
             ay[i] = 0;
@@ -1711,7 +1725,7 @@ static cudaError_t scan_dyn(const Launch &L, const uint32_t *in, uint32_t *out, 
 }
 
 void tree_free(TreeBufs &b) {
-    void *ptrs[] = {b.flag, b.bbox_part, b.keys, b.keys_alt, b.order, b.order_alt, b.hist, b.os_state, b.sx, b.sy, b.sz, b.sm,
+    void *ptrs[] = {b.flag, b.pos4, b.bbox_part, b.keys, b.keys_alt, b.order, b.order_alt, b.hist, b.os_state, b.sx, b.sy, b.sz, b.sm,
                     b.st_hi, b.st_lo, b.st_off, b.chain_cnt, b.leaves, b.targets, b.geo, b.sid_sorted, b.groups, b.gcost, b.gperm, b.pre_parent, b.pre_info, b.pre_nchild, b.pre_mask, b.pre_ref, b.nodes,
                     b.n_parent, b.n_info, b.n_arrive, b.pnodes, b.mnodes, b.mrange, b.lnode, b.walk_ctr, b.scan_tmp, b.info, b.part_acc};
     for (void *p : ptrs)
@@ -1749,6 +1763,7 @@ cudaError_t tree_alloc(TreeBufs &b, int64_t n, int leaf, int32_t nsys) {
         if (e == cudaSuccess) e = dev_alloc(&(ptr), sizeof(*(ptr)) * size_t(count)); \
     } while (0)
     GBH_ALLOC(b.flag, cn);
+    GBH_ALLOC(b.pos4, cn);
     GBH_ALLOC(b.bbox_part, kFlagBlocksMax * 6);
     GBH_ALLOC(b.keys, cn);
     GBH_ALLOC(b.keys_alt, cn);
@@ -1858,7 +1873,7 @@ cudaError_t tree_build(const Launch &L, TreeBufs &b, int64_t n, const double *px
         unsigned fb = blocks_for(n, kThreads);
         if (fb > unsigned(kFlagBlocksMax)) fb = kFlagBlocksMax;
         k_flags_bbox<<<fb, kThreads, 0, s>>>(n, px, py, pz, mass, kind, alive, b.flag, b.bbox_part, ax, ay, az,
-                                             b.info);
+                                             b.info, b.pos4);
         GBH_LAUNCH_CHECK();
         e = os ? scan_lb(L, b, 0, b.flag, b.flag, n, nullptr) : scan_u32(L, b.flag, b.flag, n, b.scan_tmp, b.scan_tmp_cap);
         if (e != cudaSuccess) return e;
@@ -1873,7 +1888,7 @@ cudaError_t tree_build(const Launch &L, TreeBufs &b, int64_t n, const double *px
         k_sys_init<<<sb, 128, 0, s>>>(b.nsys, b.geo, b.info);
         GBH_LAUNCH_CHECK();
         k_flags_sys<<<blocks_for(n, kThreads), kThreads, 0, s>>>(n, px, py, pz, mass, kind, alive, sys_of, b.flag,
-                                                                 b.geo, ax, ay, az);
+                                                                 b.geo, ax, ay, az, b.pos4);
         GBH_LAUNCH_CHECK();
         e = os ? scan_lb(L, b, 0, b.flag, b.flag, n, nullptr) : scan_u32(L, b.flag, b.flag, n, b.scan_tmp, b.scan_tmp_cap);
         if (e != cudaSuccess) return e;
@@ -1945,7 +1960,7 @@ cudaError_t tree_build(const Launch &L, TreeBufs &b, int64_t n, const double *px
     }
     // sorted copies (build.go:34-41)
     const unsigned nb = blocks_for(cap, kThreads);
-    k_gather<<<nb, kThreads, 0, s>>>(b.info, b.order, px, py, pz, mass, kind, dm_off, exact ? 1 : 0, b.sx, b.sy, b.sz,
+    k_gather<<<nb, kThreads, 0, s>>>(b.info, b.order, b.pos4, kind, dm_off, exact ? 1 : 0, b.sx, b.sy, b.sz,
                                      b.sm, b.st_hi, b.st_lo, forest ? sys_of : nullptr, b.sid_sorted);
     GBH_LAUNCH_CHECK();
     // node set
