@@ -87,6 +87,11 @@ struct __align__(16) LNode {
     float4 a, b, c, d;
 };
 
+// A star's FP64 position and mass in one 32-byte record (one sector per read).
+struct __align__(32) Pos4 {
+    double x, y, z, m;
+};
+
 // Device buffers of the tree path (all owned by the context).
 struct TreeBufs {
     int64_t cap_n = 0;      // bodies
@@ -96,7 +101,7 @@ struct TreeBufs {
     int32_t list_depth = 0; // the list walk's node-list depth (0: kDefaultListDepth), set per call
     // compaction / bbox
     uint32_t *flag = nullptr;     // star flags, then their exclusive scan
-    double4 *pos4 = nullptr;      // (x, y, z, m) of every star in state order, one 32-byte record
+    Pos4 *pos4 = nullptr;         // (x, y, z, m) of every star in state order, one 32-byte record
     double *bbox_part = nullptr;  // per-block partial min/max (6 per block)
     // sort
     uint64_t *keys = nullptr, *keys_alt = nullptr;

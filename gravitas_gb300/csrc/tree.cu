@@ -331,7 +331,7 @@ __global__ __launch_bounds__(kThreads) void k_flags_bbox(int64_t n, const double
                                                          const uint8_t *__restrict__ kind,
                                                          const uint8_t *__restrict__ alive, uint32_t *__restrict__ flag,
                                                          double *__restrict__ part, double *ax, double *ay, double *az,
-                                                         DevInfo *info, double4 *__restrict__ pos4) {
+                                                         DevInfo *info, Pos4 *__restrict__ pos4) {
     if (blockIdx.x == 0 && threadIdx.x == 0) {  // the build's first kernel clears the error record
         info->err = 0;
         info->err_where = 0;
@@ -343,7 +343,7 @@ __global__ __launch_bounds__(kThreads) void k_flags_bbox(int64_t n, const double
         flag[i] = st;
         if (st) {
             const double vx = px[i], vy = py[i], vz = pz[i], m = mass ? mass[i] : 0.0;
-            pos4[i] = make_double4(vx, vy, vz, m);  // one record for k_gather's reads through the sort order
+            pos4[i] = Pos4{vx, vy, vz, m};  // one record for k_gather's reads through the sort order
             long long x = ord_key(vx), y = ord_key(vy), z = ord_key(vz);
             mn[0] = min(mn[0], x);
             mx[0] = max(mx[0], mass && !isfinite(m) ? LLONG_MAX : x);
@@ -777,7 +777,7 @@ __global__ __launch_bounds__(kRsThreads) void k_os_pass(const uint64_t *__restri
 // position and mass come from its 32-byte record written by the collect kernel: one sector read
 // through the sort order instead of one sector per array.
 __global__ __launch_bounds__(kThreads) void k_gather(const DevInfo *info, const int32_t *__restrict__ order,
-                                                     const double4 *__restrict__ pos4,
+                                                     const Pos4 *__restrict__ pos4,
                                                      const uint8_t *__restrict__ kind, int dm_off, int fp64_copies,
                                                      double *__restrict__ sx, double *__restrict__ sy,
                                                      double *__restrict__ sz, double *__restrict__ sm,
@@ -788,9 +788,9 @@ __global__ __launch_bounds__(kThreads) void k_gather(const DevInfo *info, const 
     if (k >= info->nstars) return;
     int32_t i = order[k];
     if (sys_of) sid_sorted[k] = sys_of[i];
-    const double4 p = pos4[i];
+    const Pos4 p = pos4[i];
     const double x = p.x, y = p.y, z = p.z;
-    double m = p.w;
+    double m = p.m;
     if (dm_off && kind && kind[i] == GBH_DARK_MATTER) m = 0;
     if (fp64_copies) {  // read by the FP64 upsweep, walk and potential only
         sx[k] = x;
@@ -1562,7 +1562,7 @@ __global__ __launch_bounds__(kThreads) void k_flags_sys(int64_t n, const double 
                                                         const uint8_t *__restrict__ alive,
                                                         const uint16_t *__restrict__ sys_of, uint32_t *__restrict__ flag,
                                                         SysGeo *geo, double *ax, double *ay, double *az,
-                                                        double4 *__restrict__ pos4) {
+                                                        Pos4 *__restrict__ pos4) {
     int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     bool st = false;
     int s = -1;
@@ -1574,7 +1574,7 @@ __global__ __launch_bounds__(kThreads) void k_flags_sys(int64_t n, const double 
         if (st) {
             s = sys_of[i];
             const double vx = px[i], vy = py[i], vz = pz[i], m = mass ? mass[i] : 0.0;
-            pos4[i] = make_double4(vx, vy, vz, m);
+            pos4[i] = Pos4{vx, vy, vz, m};
             k[0] = mass && !isfinite(m) ? LLONG_MAX : ord_key(vx);  // as in k_flags_bbox
             k[1] = ord_key(vy);
             k[2] = ord_key(vz);

@@ -63,13 +63,18 @@ struct Layout {
     static constexpr int kSrcCap = 2 * (kSrcF4 / kSrcPair);     // entries: 192 compact, 96 exact
 };
 
-struct __align__(16) WarpMem {
-    float4 nbuf[kNodeF4];
-    float4 sbuf[kSrcF4];
+// The traversal's own shared memory.
+struct __align__(16) TravMem {
     uint32_t stack[kStackCap];   // sibling ranges: first | (count - 1) << 29
     int32_t lvl[kLevels];        // first stack slot of each depth
     float4 rq[32];               // the nodes of a step that the box test keeps, pair-interleaved
     int32_t owner[32];           // source staging: the lane whose leaf run starts at each slot
+};
+
+struct __align__(16) WarpMem {
+    float4 nbuf[kNodeF4];
+    float4 sbuf[kSrcF4];
+    TravMem tm;
 };
 
 __device__ __forceinline__ void set_err(DevInfo *info, int where) {
@@ -120,14 +125,14 @@ __device__ __forceinline__ float2 sep(float2 h, float2 l, float nt, float nh, fl
 // Evaluates the node list (count entries, padded to pairs) for the lane's kS stars: each pair of
 // records is read once and evaluated for every star of the lane.
 template <bool kExact, bool kQuad, bool kSoft, int kS>
-__device__ __forceinline__ void eval_nodes(const WarpMem &W, int count, const Target (&t)[kS], float eps2,
+__device__ __forceinline__ void eval_nodes(const float4 *nbuf, int count, const Target (&t)[kS], float eps2,
                                            Acc (&a)[kS]) {
     using Lay = Layout<kExact>;
     const float2 e2 = f2(eps2);
     const int np = (count + 1) >> 1;
 #pragma unroll 2
     for (int p = 0; p < np; ++p) {
-        const float4 *r = &W.nbuf[p * Lay::kNodePair];
+        const float4 *r = &nbuf[p * Lay::kNodePair];
         const float4 r0 = r[0], r1 = r[1];
         float2 lx = f2(0.f), ly = f2(0.f), lz = f2(0.f);
         if constexpr (kExact) {
@@ -185,14 +190,14 @@ __device__ __forceinline__ void eval_nodes(const WarpMem &W, int count, const Ta
 // the same operations), which adds 0 with softening, as skipping j == self does (bh.go:142-144);
 // without softening r2 = 0 is masked.
 template <bool kExact, bool kSoft, int kS>
-__device__ __forceinline__ void eval_sources(const WarpMem &W, int count, const Target (&t)[kS], float eps2,
+__device__ __forceinline__ void eval_sources(const float4 *sbuf, int count, const Target (&t)[kS], float eps2,
                                              Acc (&a)[kS]) {
     using Lay = Layout<kExact>;
     const float2 e2 = f2(eps2);
     const int np = (count + 1) >> 1;
 #pragma unroll(kS == 1 ? 4 : 2)
     for (int p = 0; p < np; ++p) {
-        const float4 *r = &W.sbuf[p * Lay::kSrcPair];
+        const float4 *r = &sbuf[p * Lay::kSrcPair];
         const float4 r0 = r[0], r1 = r[1];
         float2 lx = f2(0.f), ly = f2(0.f), lz = f2(0.f);
         if constexpr (kExact) {
@@ -246,9 +251,14 @@ struct GroupOut {
     bool ok;
 };
 
+// The warp's list buffers (evaluated by the walking warp itself whenever one is full).
+struct InPlace {
+    float4 *nbuf, *sbuf;
+};
+
 // Walks one group with the given separation form; a is zeroed by the caller.
-template <bool kExact, bool kQuad, bool kSoft, int kS>
-__device__ __forceinline__ GroupOut walk_group(WarpMem &W, int lane, int32_t root, const Target (&t)[kS], float Ox,
+template <bool kExact, bool kQuad, bool kSoft, int kS, class Sink>
+__device__ __forceinline__ GroupOut walk_group(TravMem &W, Sink &sink, int lane, int32_t root, const Target (&t)[kS], float Ox,
                                                float Oy, float Oz, float bx0, float by0, float bz0, float bx1,
                                                float by1, float bz1, float ext, float eps2, int node_depth,
                                                int src_depth, const LNode *__restrict__ nodes,
@@ -276,14 +286,14 @@ __device__ __forceinline__ GroupOut walk_group(WarpMem &W, int lane, int32_t roo
         ntz[q] = f2(-t[q].tz);
     }
     auto flush_nodes = [&]() {
-        pad_pair<Lay::kNodePair, kNodeFields>(W.nbuf, ncount, lane, 3, 4, 9);
-        eval_nodes<kExact, kQuad, kSoft, kS>(W, ncount, t, eps2, a);
+        pad_pair<Lay::kNodePair, kNodeFields>(sink.nbuf, ncount, lane, 3, 4, 9);
+        eval_nodes<kExact, kQuad, kSoft, kS>(sink.nbuf, ncount, t, eps2, a);
         __syncwarp();
         ncount = 0;
     };
     auto flush_sources = [&]() {
-        pad_pair<Lay::kSrcPair, kSrcFields>(W.sbuf, scount, lane, 3, 32, 32);
-        eval_sources<kExact, kSoft, kS>(W, scount, t, eps2, a);
+        pad_pair<Lay::kSrcPair, kSrcFields>(sink.sbuf, scount, lane, 3, 32, 32);
+        eval_sources<kExact, kSoft, kS>(sink.sbuf, scount, t, eps2, a);
         __syncwarp();
         scount = 0;
     };
@@ -407,24 +417,24 @@ __device__ __forceinline__ GroupOut walk_group(WarpMem &W, int lane, int32_t roo
                 const float4 qc = kS == 2 ? nc : nodes[node].c, qd = kS == 2 ? nd : nodes[node].d;
                 constexpr int P = Lay::kNodePair;
                 if constexpr (kExact) {
-                    put(W.nbuf, P, en, 0, na.x);
-                    put(W.nbuf, P, en, 1, na.y);
-                    put(W.nbuf, P, en, 2, na.z);
-                    put(W.nbuf, P, en, 10, nb.x);
-                    put(W.nbuf, P, en, 11, nb.y);
-                    put(W.nbuf, P, en, 12, nb.z);
+                    put(sink.nbuf, P, en, 0, na.x);
+                    put(sink.nbuf, P, en, 1, na.y);
+                    put(sink.nbuf, P, en, 2, na.z);
+                    put(sink.nbuf, P, en, 10, nb.x);
+                    put(sink.nbuf, P, en, 11, nb.y);
+                    put(sink.nbuf, P, en, 12, nb.z);
                 } else {
-                    put(W.nbuf, P, en, 0, cx);
-                    put(W.nbuf, P, en, 1, cy);
-                    put(W.nbuf, P, en, 2, cz);
+                    put(sink.nbuf, P, en, 0, cx);
+                    put(sink.nbuf, P, en, 1, cy);
+                    put(sink.nbuf, P, en, 2, cz);
                 }
-                put(W.nbuf, P, en, 3, qd.z);  // m
-                put(W.nbuf, P, en, 4, qc.x);  // -qxx
-                put(W.nbuf, P, en, 5, qc.y);  // -qyy
-                put(W.nbuf, P, en, 6, qc.z);  // -qzz
-                put(W.nbuf, P, en, 7, qc.w);  // -qxy
-                put(W.nbuf, P, en, 8, qd.x);  // -qxz
-                put(W.nbuf, P, en, 9, qd.y);  // -qyz
+                put(sink.nbuf, P, en, 3, qd.z);  // m
+                put(sink.nbuf, P, en, 4, qc.x);  // -qxx
+                put(sink.nbuf, P, en, 5, qc.y);  // -qyy
+                put(sink.nbuf, P, en, 6, qc.z);  // -qzz
+                put(sink.nbuf, P, en, 7, qc.w);  // -qxy
+                put(sink.nbuf, P, en, 8, qd.x);  // -qxz
+                put(sink.nbuf, P, en, 9, qd.y);  // -qyz
             }
             const int nacc = __popc(ma);
             ncount += nacc;
@@ -467,18 +477,18 @@ __device__ __forceinline__ GroupOut walk_group(WarpMem &W, int lane, int32_t roo
                     const int en = scount + lane;
                     constexpr int P = Lay::kSrcPair;
                     if constexpr (kExact) {
-                        put(W.sbuf, P, en, 0, h.x);
-                        put(W.sbuf, P, en, 1, h.y);
-                        put(W.sbuf, P, en, 2, h.z);
-                        put(W.sbuf, P, en, 4, l.x);
-                        put(W.sbuf, P, en, 5, l.y);
-                        put(W.sbuf, P, en, 6, l.z);
+                        put(sink.sbuf, P, en, 0, h.x);
+                        put(sink.sbuf, P, en, 1, h.y);
+                        put(sink.sbuf, P, en, 2, h.z);
+                        put(sink.sbuf, P, en, 4, l.x);
+                        put(sink.sbuf, P, en, 5, l.y);
+                        put(sink.sbuf, P, en, 6, l.z);
                     } else {
-                        put(W.sbuf, P, en, 0, (h.x - Ox) + l.x);
-                        put(W.sbuf, P, en, 1, (h.y - Oy) + l.y);
-                        put(W.sbuf, P, en, 2, (h.z - Oz) + l.z);
+                        put(sink.sbuf, P, en, 0, (h.x - Ox) + l.x);
+                        put(sink.sbuf, P, en, 1, (h.y - Oy) + l.y);
+                        put(sink.sbuf, P, en, 2, (h.z - Oz) + l.z);
                     }
-                    put(W.sbuf, P, en, 3, h.w);
+                    put(sink.sbuf, P, en, 3, h.w);
                 }
                 scount += T - cs < 32 ? T - cs : 32;
                 __syncwarp();
@@ -489,6 +499,143 @@ __device__ __forceinline__ GroupOut walk_group(WarpMem &W, int lane, int32_t roo
     if (ncount) flush_nodes();
     if (scount) flush_sources();
     return GroupOut{(31u * acc_nodes + 12u * pairs) * uint32_t(kS) / 16u + tested, true};
+}
+
+// A group's range of list entries or stars (forest: its table entry; else groups of kG).
+struct GroupRange {
+    int32_t base, cnt, root;
+};
+template <int kG>
+__device__ __forceinline__ GroupRange group_range(int32_t g, const int4 *__restrict__ groups, int32_t nt) {
+    GroupRange r;
+    if (groups) {
+        const int4 ge = groups[g];
+        r.base = ge.x;
+        r.cnt = ge.y;
+        r.root = ge.z;
+    } else {
+        r.base = g * kG;
+        r.cnt = nt - r.base < kG ? nt - r.base : kG;
+        r.root = 0;
+    }
+    if (r.cnt > kG) r.cnt = kG;
+    return r;
+}
+
+// The lane's stars of a group (star 32 q + lane; one beyond the group repeats the group's first
+// star), their offsets from the group origin O (the first star's hi part) and hi/lo parts.
+template <int kS>
+struct GroupStars {
+    bool valid[kS];
+    int32_t k[kS];
+    Target t[kS];
+    float Ox, Oy, Oz;
+};
+template <int kS>
+__device__ __forceinline__ void group_stars(int lane, const GroupRange &R, const int32_t *__restrict__ targets,
+                                            const float4 *__restrict__ st_hi, const float4 *__restrict__ st_lo,
+                                            GroupStars<kS> &G) {
+    float4 h[kS], l[kS];
+#pragma unroll
+    for (int q = 0; q < kS; ++q) {
+        G.valid[q] = 32 * q + lane < R.cnt;
+        const int32_t e = R.base + (G.valid[q] ? 32 * q + lane : 0);
+        G.k[q] = targets ? targets[e] : e;
+        h[q] = st_hi[G.k[q]];
+        l[q] = st_lo[G.k[q]];
+    }
+    G.Ox = __shfl_sync(kFull, h[0].x, 0);
+    G.Oy = __shfl_sync(kFull, h[0].y, 0);
+    G.Oz = __shfl_sync(kFull, h[0].z, 0);
+#pragma unroll
+    for (int q = 0; q < kS; ++q) {
+        G.t[q].tx = (h[q].x - G.Ox) + l[q].x;
+        G.t[q].ty = (h[q].y - G.Oy) + l[q].y;
+        G.t[q].tz = (h[q].z - G.Oz) + l[q].z;
+        G.t[q].hx = h[q].x;
+        G.t[q].hy = h[q].y;
+        G.t[q].hz = h[q].z;
+        G.t[q].lx = l[q].x;
+        G.t[q].ly = l[q].y;
+        G.t[q].lz = l[q].z;
+    }
+}
+
+// The group's box, its extent from the origin, and whether its separations take hi and lo parts
+// apart: offsets from O carry rounding errors of 2^-24 of the group's extent, so separations
+// formed from them stay accurate while the extent is within 2^12 of the softening or of the
+// closest consecutive stars (star 32 q + lane is followed by the next lane's, or lane 0's next
+// star); beyond that (a group across a jump of the Morton curve) they take hi and lo apart.
+struct GroupBox {
+    float bx0, by0, bz0, bx1, by1, bz1, ext;
+    bool exact;
+};
+template <int kS>
+__device__ __forceinline__ GroupBox group_box(int lane, int32_t cnt, const Target (&t)[kS], float eps) {
+    GroupBox B;
+    B.bx0 = B.bx1 = t[0].tx;
+    B.by0 = B.by1 = t[0].ty;
+    B.bz0 = B.bz1 = t[0].tz;
+    float gap = 3.0e38f;
+#pragma unroll
+    for (int q = 0; q < kS; ++q) {
+        B.bx0 = fminf(B.bx0, t[q].tx);
+        B.by0 = fminf(B.by0, t[q].ty);
+        B.bz0 = fminf(B.bz0, t[q].tz);
+        B.bx1 = fmaxf(B.bx1, t[q].tx);
+        B.by1 = fmaxf(B.by1, t[q].ty);
+        B.bz1 = fmaxf(B.bz1, t[q].tz);
+        float nx = __shfl_down_sync(kFull, t[q].tx, 1), ny = __shfl_down_sync(kFull, t[q].ty, 1),
+              nz = __shfl_down_sync(kFull, t[q].tz, 1);
+        if (q + 1 < kS) {
+            const float wx = __shfl_sync(kFull, t[q + 1 < kS ? q + 1 : q].tx, 0);
+            const float wy = __shfl_sync(kFull, t[q + 1 < kS ? q + 1 : q].ty, 0);
+            const float wz = __shfl_sync(kFull, t[q + 1 < kS ? q + 1 : q].tz, 0);
+            if (lane == 31) {
+                nx = wx;
+                ny = wy;
+                nz = wz;
+            }
+        }
+        if (32 * q + lane + 1 < cnt)
+            gap = fminf(gap, fmaxf(fabsf(nx - t[q].tx), fmaxf(fabsf(ny - t[q].ty), fabsf(nz - t[q].tz))));
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        B.bx0 = fminf(B.bx0, __shfl_xor_sync(kFull, B.bx0, o));
+        B.by0 = fminf(B.by0, __shfl_xor_sync(kFull, B.by0, o));
+        B.bz0 = fminf(B.bz0, __shfl_xor_sync(kFull, B.bz0, o));
+        B.bx1 = fmaxf(B.bx1, __shfl_xor_sync(kFull, B.bx1, o));
+        B.by1 = fmaxf(B.by1, __shfl_xor_sync(kFull, B.by1, o));
+        B.bz1 = fmaxf(B.bz1, __shfl_xor_sync(kFull, B.bz1, o));
+        gap = fminf(gap, __shfl_xor_sync(kFull, gap, o));
+    }
+    B.ext = fmaxf(fmaxf(fmaxf(-B.bx0, B.bx1), fmaxf(-B.by0, B.by1)), fmaxf(-B.bz0, B.bz1));
+    B.exact = B.ext > 4096.f * fmaxf(eps, gap);
+    return B;
+}
+
+template <int kS>
+__device__ __forceinline__ void zero_acc(Acc (&a)[kS]) {
+#pragma unroll
+    for (int q = 0; q < kS; ++q) {
+        a[q].px = a[q].py = a[q].pz = f2(0.f);
+        a[q].sx = a[q].sy = a[q].sz = a[q].cx = a[q].cy = a[q].cz = 0.f;
+    }
+}
+
+template <int kS>
+__device__ __forceinline__ void store_acc(const GroupStars<kS> &G, const Acc (&a)[kS], const int32_t *__restrict__ order,
+                                          double *ax, double *ay, double *az) {
+#pragma unroll
+    for (int q = 0; q < kS; ++q) {
+        if (G.valid[q]) {
+            const int32_t o = order[G.k[q]];
+            ax[o] = double(a[q].sx) - double(a[q].cx);
+            ay[o] = double(a[q].sy) - double(a[q].cy);
+            az[o] = double(a[q].sz) - double(a[q].cz);
+        }
+    }
 }
 
 template <bool kQuad, bool kSoft, int kS>
@@ -508,10 +655,9 @@ __global__ __launch_bounds__(kLwThreads) void k_walk_lists(const DevInfo *info, 
     const int lane = threadIdx.x & 31;
     const int32_t ns = int32_t(info->nstars);
     const int32_t nn = int32_t(info->nnodes);
-    const bool forest = groups != nullptr;
     // a target list (block steps): groups of kG consecutive entries; else every star
     const int32_t nt = targets ? int32_t(info->ntargets) : ns;
-    const int32_t ng = nn > 0 ? (forest ? int32_t(info->ngroups) : (nt + kG - 1) / kG) : 0;
+    const int32_t ng = nn > 0 ? (groups ? int32_t(info->ngroups) : (nt + kG - 1) / kG) : 0;
     const bool lpt = gperm && gperm[perm_cap] == ng;
     for (;;) {
         int32_t idx = 0;
@@ -519,116 +665,28 @@ __global__ __launch_bounds__(kLwThreads) void k_walk_lists(const DevInfo *info, 
         idx = __shfl_sync(kFull, idx, 0);
         if (idx >= ng) break;
         const int32_t g = lpt ? gperm[idx] : idx;
-        int32_t base, cnt, root = 0;
-        if (forest) {
-            const int4 ge = groups[g];
-            base = ge.x;
-            cnt = ge.y;
-            root = ge.z;
-        } else {
-            base = g * kG;
-            cnt = nt - base < kG ? nt - base : kG;
-        }
-        if (cnt <= 0) continue;
-        if (cnt > kG) cnt = kG;
-        // the lane's stars; a star beyond the group repeats the group's first star
-        bool valid[kS];
-        int32_t k[kS];
-        float4 h[kS], l[kS];
-#pragma unroll
-        for (int q = 0; q < kS; ++q) {
-            valid[q] = 32 * q + lane < cnt;
-            const int32_t e = base + (valid[q] ? 32 * q + lane : 0);
-            k[q] = targets ? targets[e] : e;
-            h[q] = st_hi[k[q]];
-            l[q] = st_lo[k[q]];
-        }
-        const float Ox = __shfl_sync(kFull, h[0].x, 0), Oy = __shfl_sync(kFull, h[0].y, 0),
-                    Oz = __shfl_sync(kFull, h[0].z, 0);
-        Target t[kS];
-#pragma unroll
-        for (int q = 0; q < kS; ++q) {
-            t[q].tx = (h[q].x - Ox) + l[q].x;
-            t[q].ty = (h[q].y - Oy) + l[q].y;
-            t[q].tz = (h[q].z - Oz) + l[q].z;
-            t[q].hx = h[q].x;
-            t[q].hy = h[q].y;
-            t[q].hz = h[q].z;
-            t[q].lx = l[q].x;
-            t[q].ly = l[q].y;
-            t[q].lz = l[q].z;
-        }
-        // the group's box, its extent from the origin and the spacing of consecutive stars (star
-        // 32 q + lane is followed by 32 q + lane + 1: the next lane's, or lane 0's next star)
-        float bx0 = t[0].tx, by0 = t[0].ty, bz0 = t[0].tz, bx1 = bx0, by1 = by0, bz1 = bz0;
-        float gap = 3.0e38f;
-#pragma unroll
-        for (int q = 0; q < kS; ++q) {
-            bx0 = fminf(bx0, t[q].tx);
-            by0 = fminf(by0, t[q].ty);
-            bz0 = fminf(bz0, t[q].tz);
-            bx1 = fmaxf(bx1, t[q].tx);
-            by1 = fmaxf(by1, t[q].ty);
-            bz1 = fmaxf(bz1, t[q].tz);
-            float nx = __shfl_down_sync(kFull, t[q].tx, 1), ny = __shfl_down_sync(kFull, t[q].ty, 1),
-                  nz = __shfl_down_sync(kFull, t[q].tz, 1);
-            if (q + 1 < kS) {
-                const float wx = __shfl_sync(kFull, t[q + 1 < kS ? q + 1 : q].tx, 0);
-                const float wy = __shfl_sync(kFull, t[q + 1 < kS ? q + 1 : q].ty, 0);
-                const float wz = __shfl_sync(kFull, t[q + 1 < kS ? q + 1 : q].tz, 0);
-                if (lane == 31) {
-                    nx = wx;
-                    ny = wy;
-                    nz = wz;
-                }
-            }
-            if (32 * q + lane + 1 < cnt)
-                gap = fminf(gap, fmaxf(fabsf(nx - t[q].tx), fmaxf(fabsf(ny - t[q].ty), fabsf(nz - t[q].tz))));
-        }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            bx0 = fminf(bx0, __shfl_xor_sync(kFull, bx0, o));
-            by0 = fminf(by0, __shfl_xor_sync(kFull, by0, o));
-            bz0 = fminf(bz0, __shfl_xor_sync(kFull, bz0, o));
-            bx1 = fmaxf(bx1, __shfl_xor_sync(kFull, bx1, o));
-            by1 = fmaxf(by1, __shfl_xor_sync(kFull, by1, o));
-            bz1 = fmaxf(bz1, __shfl_xor_sync(kFull, bz1, o));
-            gap = fminf(gap, __shfl_xor_sync(kFull, gap, o));
-        }
-        const float ext = fmaxf(fmaxf(fmaxf(-bx0, bx1), fmaxf(-by0, by1)), fmaxf(-bz0, bz1));
+        const GroupRange R = group_range<kG>(g, groups, nt);
+        if (R.cnt <= 0) continue;
+        GroupStars<kS> G;
+        group_stars<kS>(lane, R, targets, st_hi, st_lo, G);
+        const GroupBox B = group_box<kS>(lane, R.cnt, G.t, eps);
         __syncwarp();
-        // Offsets from O carry rounding errors of 2^-24 of the group's extent; separations formed
-        // from them stay accurate while the extent is within 2^12 of the softening or of the
-        // closest consecutive stars. Beyond that (a group across a jump of the Morton curve) the
-        // separations take the hi and lo parts apart.
-        const bool exact = ext > 4096.f * fmaxf(eps, gap);
         Acc a[kS];
-#pragma unroll
-        for (int q = 0; q < kS; ++q) {
-            a[q].px = a[q].py = a[q].pz = f2(0.f);
-            a[q].sx = a[q].sy = a[q].sz = a[q].cx = a[q].cy = a[q].cz = 0.f;
-        }
+        zero_acc<kS>(a);
         GroupOut r;
-        if (exact)
-            r = walk_group<true, kQuad, kSoft, kS>(W, lane, root, t, Ox, Oy, Oz, bx0, by0, bz0, bx1, by1, bz1, ext,
-                                                    eps2, node_depth, src_depth, nodes, st_hi, st_lo, nn, ns,
-                                                    err_info, a);
+        InPlace sink{W.nbuf, W.sbuf};
+        if (B.exact)
+            r = walk_group<true, kQuad, kSoft, kS>(W.tm, sink, lane, R.root, G.t, G.Ox, G.Oy, G.Oz, B.bx0, B.by0,
+                                                    B.bz0, B.bx1, B.by1, B.bz1, B.ext, eps2, node_depth, src_depth,
+                                                    nodes, st_hi, st_lo, nn, ns, err_info, a);
         else
-            r = walk_group<false, kQuad, kSoft, kS>(W, lane, root, t, Ox, Oy, Oz, bx0, by0, bz0, bx1, by1, bz1, ext,
-                                                     eps2, node_depth, src_depth, nodes, st_hi, st_lo, nn, ns,
-                                                     err_info, a);
+            r = walk_group<false, kQuad, kSoft, kS>(W.tm, sink, lane, R.root, G.t, G.Ox, G.Oy, G.Oz, B.bx0, B.by0,
+                                                     B.bz0, B.bx1, B.by1, B.bz1, B.ext, eps2, node_depth, src_depth,
+                                                     nodes, st_hi, st_lo, nn, ns, err_info, a);
         __syncwarp();
         if (!r.ok) break;  // the error flag is set; the host reports GBH_ERR_LIMIT
         if (gcost && lane == 0) gcost[g] = r.cost;
-#pragma unroll
-        for (int q = 0; q < kS; ++q) {
-            if (valid[q]) {
-                const int32_t o = order[k[q]];
-                ax[o] = double(a[q].sx) - double(a[q].cx);
-                ay[o] = double(a[q].sy) - double(a[q].cy);
-                az[o] = double(a[q].sz) - double(a[q].cz);
-            }
-        }
+        store_acc<kS>(G, a, order, ax, ay, az);
     }
 }
 
