@@ -498,6 +498,7 @@ def run_profile(args):
 
 
 ADJ_N, ADJ_STEPS, ADJ_EVERY, ADJ_EPS, ADJ_DT = 32768, 1000, 50, 0.01, 1e-3
+ADJ_TREE_LEAF = 16
 ADJ_FLOP_FORCE, ADJ_FLOP_VJP = 18, 51  # algorithmic FLOP per ordered pair (force; kick adjoint)
 
 
@@ -506,7 +507,10 @@ def run_adjoint(args):
     initial positions, velocities and masses through gbh_fwd_save / gbh_bwd, on a Plummer
     sphere of 32,768 lognormal-mass bodies, 1,000 KDK steps of 1e-3, softening 0.01, checkpoints
     every 50 steps, FP32 pair kernels. Checked against central differences (h = 1e-4) of the
-    same forward on --fd-coords coordinates. One line of JSON; not the headline workload."""
+    same forward on --fd-coords coordinates. Beside it (tree_force) the gradient through the
+    Barnes-Hut force at theta 0.5 (the tree adjoint, lists frozen per step), timed and checked on
+    --tree-coords coordinates against differences of the same tree forward. One line of JSON; not
+    the headline workload."""
     from gravitas_gb300 import abi, ics, sim
     from oracle import oracle as O
     rank, world, local = dist_env()
@@ -604,6 +608,44 @@ def run_adjoint(args):
             vals.append(float(np.sum((x - targets) ** 2) / n))
         fd = (vals[0] - vals[1]) / (2 * h)
         tree_errs.append(abs(dv[i, c] - fd) / max(abs(fd), 1e-3 * scale))
+    # The tree force (config 4's theta 0.5): the adjoint of the list walk with each step's lists
+    # frozen, timed like the direct-sum gradient and checked against central differences of the
+    # same tree forward (velocities at h, masses at 1e-2 of their value)
+    tree = None
+    if args.tree_coords > 0:
+        tl = lambda: sim.trajectory_loss_gradient(s, targets, ADJ_DT, ADJ_EPS, T, K, abi.ADJ_FP32, ctx,
+                                                  abi.ADJ_TREE, THETA, ADJ_TREE_LEAF)
+        tl()
+        twalls = []
+        for _ in range(max(1, args.steps)):
+            t0 = time.perf_counter()
+            _, tdx, tdv, tdm = tl()
+            twalls.append(time.perf_counter() - t0)
+        tscale_v, tscale_m = float(np.abs(tdv).max()), float(np.abs(tdm).max())
+        terrs = []
+        for q in range(args.tree_coords):
+            i, c = int(rng.integers(n)), int(rng.integers(3))
+            hh = h if q % 2 == 0 else 1e-2 * float(s["mass"][i])
+            vals = []
+            for sign in (1.0, -1.0):
+                v, m = v0.copy(), s["mass"].copy()
+                if q % 2 == 0:
+                    v[i, c] += sign * hh
+                else:
+                    m[i] += sign * hh
+                xT, _ = ctx.fwd_save(x0, v, m, ADJ_DT, ADJ_EPS, T, T, abi.ADJ_FP32, abi.ADJ_TREE, THETA, ADJ_TREE_LEAF)
+                vals.append(float(np.sum((xT - targets) ** 2) / n))
+            fd = (vals[0] - vals[1]) / (2 * hh)
+            g = tdv[i, c] if q % 2 == 0 else tdm[i]
+            terrs.append(abs(g - fd) / max(abs(fd), 1e-3 * (tscale_v if q % 2 == 0 else tscale_m)))
+        tree = {"theta": THETA, "leaf": ADJ_TREE_LEAF, "walk": "list walk, 32-star groups, quadrupoles",
+                "ms_per_gradient": statistics.median(twalls) * 1e3,
+                "value": n * T / statistics.median(twalls), "unit": "particle-steps/s",
+                "fd_check": {"coords": len(terrs), "h_v": h, "h_m": "1e-2 m_i",
+                             "max_rel": float(max(terrs)) if terrs else None,
+                             "median_rel": float(np.median(terrs)) if terrs else None,
+                             "p90_rel": float(np.percentile(terrs, 90)) if terrs else None,
+                             "error": "|g - fd| / max(|fd|, 1e-3 max|g|), fd of the same tree forward"}}
     # CPU baseline: the oracle's FP64 adjoint on a bounded sample (all bodies, 4 steps)
     cpu = None
     if rank == 0:
@@ -644,6 +686,8 @@ def run_adjoint(args):
                                    "median_rel": float(np.median(tree_errs)) if tree_errs else None},
         "cpu_baseline": cpu, "clocks": clk.summary(),
     }
+    if tree:
+        line["tree_force"] = tree
     if rank == 0:
         print(json.dumps(line), flush=True)
     ctx.close()
@@ -974,6 +1018,9 @@ def main():
     ap.add_argument("--no-configs", action="store_true",
                     help="headline: leave out the short forest and galaxy runs reported beside it")
     ap.add_argument("--fd-coords", type=int, default=16, help="adjoint: coordinates checked by central differences")
+    ap.add_argument("--tree-coords", type=int, default=8,
+                    help="adjoint: coordinates of the tree-force gradient checked by central differences (0: no "
+                         "tree-force gradient)")
     ap.add_argument("--sizes", type=int, nargs="+", default=[1 << 20, 1 << 22, 1 << 24, 1 << 26],
                     help="scaling: body counts")
     args = ap.parse_args()

@@ -77,11 +77,14 @@ class Diagnostics(ctypes.Structure):
 
 class AdjointParams(ctypes.Structure):
     _fields_ = [("dt", ctypes.c_double), ("softening", ctypes.c_double), ("nsteps", ctypes.c_int64),
-                ("every", ctypes.c_int64), ("precision", ctypes.c_int32), ("reserved", ctypes.c_int32 * 3)]
+                ("every", ctypes.c_int64), ("precision", ctypes.c_int32), ("force", ctypes.c_int32),
+                ("leaf_size", ctypes.c_int32), ("reserved", ctypes.c_int32), ("theta", ctypes.c_double)]
 
 
 ADJ_FP32 = 0
 ADJ_FP64 = 1
+ADJ_DIRECT = 0
+ADJ_TREE = 1
 
 
 class TuneEntry(ctypes.Structure):
@@ -269,14 +272,17 @@ class Context:
         return d.as_dict()
 
     def fwd_save(self, x0: np.ndarray, v0: np.ndarray, mass: np.ndarray, dt: float, softening: float,
-                 nsteps: int, every: int, precision: int = ADJ_FP32):
-        """Forward half of the adjoint pair: (x_T, v_T), each n x 3, with the tape kept on the device."""
+                 nsteps: int, every: int, precision: int = ADJ_FP32, force: int = ADJ_DIRECT, theta: float = 0.0,
+                 leaf: int = 0):
+        """Forward half of the adjoint pair: (x_T, v_T), each n x 3, with the tape kept on the device.
+        force=ADJ_TREE steps with the Barnes-Hut force at theta and leaf size leaf."""
         x0 = np.ascontiguousarray(np.asarray(x0, np.float64).T)
         v0 = np.ascontiguousarray(np.asarray(v0, np.float64).T)
         m = np.ascontiguousarray(mass, np.float64)
         n = m.shape[0]
         out = np.empty((6, n))
-        ap = AdjointParams(float(dt), float(softening), int(nsteps), int(every), int(precision))
+        ap = AdjointParams(float(dt), float(softening), int(nsteps), int(every), int(precision), int(force),
+                           int(leaf), 0, float(theta))
         self.call("gbh_fwd_save", ctypes.byref(ap), n, *[ptr(x0[k]) for k in range(3)],
                   *[ptr(v0[k]) for k in range(3)], ptr(m), *[ptr(out[k]) for k in range(6)])
         return out[0:3].T.copy(), out[3:6].T.copy()

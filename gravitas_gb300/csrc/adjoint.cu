@@ -405,11 +405,29 @@ __global__ void k_vjp_reduce(int64_t n, int nsplit, const double *__restrict__ p
 
 inline cudaError_t mark(AdjTape &t) { return t.mark ? t.mark(t.mark_arg) : cudaSuccess; }
 
-// Accelerations at (x, y, z): FP64 straight into (ax, ay, az); FP32 into t.part (summed by k_update).
+// The tree at (x, y, z) for the tree force: FP32 moments, 32-star groups of the list walk.
+cudaError_t tree_at(const Launch &L, AdjTape &t, const double *x, const double *y, const double *z, double *ax,
+                    double *ay, double *az) {
+    TreeBufs &b = *t.tb;
+    b.group = 32;
+    b.list_depth = 0;
+    b.lpt = true;
+    return tree_build(L, b, t.n, x, y, z, t.m, nullptr, nullptr, ax, ay, az, t.theta, t.leaf, 0, false, false,
+                      nullptr, nullptr);
+}
+
+// Accelerations at (x, y, z): FP64 and the tree force straight into (ax, ay, az); FP32 pairs
+// into t.part (summed by k_update).
 cudaError_t force(const Launch &L, AdjTape &t, const double *x, const double *y, const double *z, double *ax,
                   double *ay, double *az) {
     cudaError_t e;
     if ((e = mark(t))) return e;
+    if (t.tree) {
+        if ((e = tree_at(L, t, x, y, z, ax, ay, az))) return e;
+        if ((e = mark(t))) return e;
+        if ((e = walk_lists(L, *t.tb, float(t.eps2), 1, ax, ay, az, 0, false, 1))) return e;
+        return mark(t);
+    }
     if (!t.fp32) {
         if ((e = mark(t))) return e;
         k_force64<<<unsigned((t.n + kPairThreads - 1) / kPairThreads), kPairThreads, 0, L.stream>>>(
@@ -430,7 +448,7 @@ cudaError_t force(const Launch &L, AdjTape &t, const double *x, const double *y,
 cudaError_t update(const Launch &L, AdjTape &t, int flags, const double *xin, double *xout, double *v, double *a,
                    double *ck) {
     int64_t n = t.n;
-    if (!t.fp32) flags &= ~kReduce;
+    if (!t.fp32 || t.tree) flags &= ~kReduce;
     k_update<<<ew_blocks(n), kEwThreads, 0, L.stream>>>(n, t.nsplit, t.part, flags, 0.5 * t.dt, t.dt, a, a + n,
                                                         a + 2 * n, xin, xin + n, xin + 2 * n, xout, xout + n,
                                                         xout + 2 * n, v, v + n, v + 2 * n, ck);
@@ -445,6 +463,17 @@ cudaError_t vjp(const Launch &L, AdjTape &t, const double *x, double c, bool dri
     double *lam = t.lam;
     cudaError_t e;
     if ((e = mark(t))) return e;
+    if (t.tree) {  // the tree at x again (the forward's lists), then its transposed Jacobian
+        if ((e = tree_at(L, t, x, x + n, x + 2 * n, t.ra, t.ra + n, t.ra + 2 * n))) return e;
+        if ((e = mark(t))) return e;
+        if ((e = walk_lists_adjoint(L, *t.tb, float(t.eps2), x, x + n, x + 2 * n, t.m, lam + 3 * n, lam + 4 * n,
+                                    lam + 5 * n, n, t.tbs, t.part)))
+            return e;
+        if ((e = mark(t))) return e;
+        k_vjp_reduce<<<ew_blocks(n), kEwThreads, 0, L.stream>>>(n, 1, t.part, c, drift ? 1 : 0, t.dt, lam);
+        ADJ_LAUNCH_CHECK();
+        return cudaSuccess;
+    }
     if (!t.fp32) {
         if ((e = mark(t))) return e;
         k_vjp64<<<unsigned((n + kPairThreads - 1) / kPairThreads), kPairThreads, 0, L.stream>>>(
@@ -476,6 +505,7 @@ cudaError_t vjp(const Launch &L, AdjTape &t, const double *x, double c, bool dri
 
 void adj_free(AdjTape &t) {
     if (t.block) cudaFree(t.block);
+    adj_tree_free(t.tbs);
     t = AdjTape{};
 }
 

@@ -1242,12 +1242,25 @@ int gbh_fwd_save(gbh_ctx *ctx, const gbh_adjoint_params *ap, int64_t n, const do
     if (ap->nsteps < 1 || ap->every < 1) return fail(ctx, GBH_ERR_ARG, "nsteps and every must be >= 1");
     if (ap->precision != GBH_ADJ_FP32 && ap->precision != GBH_ADJ_FP64)
         return fail(ctx, GBH_ERR_ARG, "precision %d", ap->precision);
+    if (ap->force != GBH_ADJ_DIRECT && ap->force != GBH_ADJ_TREE) return fail(ctx, GBH_ERR_ARG, "force %d", ap->force);
+    const bool tree = ap->force == GBH_ADJ_TREE;
+    if (tree && ap->precision != GBH_ADJ_FP32) return fail(ctx, GBH_ERR_ARG, "the tree force runs in FP32 only");
+    if (tree && !(ap->theta >= 0 && ap->theta <= 1)) return fail(ctx, GBH_ERR_ARG, "theta %g outside [0, 1]", ap->theta);
+    if (tree && ap->leaf_size < 0) return fail(ctx, GBH_ERR_ARG, "leaf_size %d < 0", ap->leaf_size);
     if (n < 1 || n > (int64_t(1) << 26)) return fail(ctx, GBH_ERR_ARG, "n = %lld out of range", (long long)n);
     if (!px || !py || !pz || !vx || !vy || !vz || !mass) return fail(ctx, GBH_ERR_ARG, "array argument is NULL");
     gbh::AdjTape &t = ctx->adj;
     CK(cudaEventRecord(ctx->ev[0], ctx->stream));
     CK(gbh::adj_reserve(t, n, ap->nsteps, ap->every, ap->dt, ap->softening, ap->precision == GBH_ADJ_FP32,
                         ctx->num_sms));
+    t.tree = tree;
+    if (tree) {  // the context's tree buffers, sized for this state
+        t.theta = ap->theta == 0 ? 0.9 : ap->theta;  // bh.go:69-74
+        t.leaf = ap->leaf_size > 0 ? ap->leaf_size : 24;
+        t.tb = &ctx->tb;
+        CK(gbh::tree_alloc(ctx->tb, n, t.leaf, 1));
+        CK(gbh::adj_tree_reserve(t.tbs, ctx->tb));
+    }
     size_t b = sizeof(double) * size_t(n);
     if ((rc = h2d(ctx, t.x, px, b)) || (rc = h2d(ctx, t.x + n, py, b)) || (rc = h2d(ctx, t.x + 2 * n, pz, b)) ||
         (rc = h2d(ctx, t.v, vx, b)) || (rc = h2d(ctx, t.v + n, vy, b)) || (rc = h2d(ctx, t.v + 2 * n, vz, b)) ||
@@ -1275,6 +1288,10 @@ int gbh_bwd(gbh_ctx *ctx, const double *gx, const double *gy, const double *gz, 
     const int64_t n = t.n;
     size_t b = sizeof(double) * size_t(n);
     CK(cudaEventRecord(ctx->ev[0], ctx->stream));
+    if (t.tree) {  // other calls since the forward may have resized the context's tree buffers
+        CK(gbh::tree_alloc(ctx->tb, n, t.leaf, 1));
+        CK(gbh::adj_tree_reserve(t.tbs, ctx->tb));
+    }
     const double *gin[6] = {gx, gy, gz, gvx, gvy, gvz};
     for (int k = 0; k < 6; ++k) {
         if (gin[k]) {

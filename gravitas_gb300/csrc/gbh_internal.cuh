@@ -312,6 +312,14 @@ cudaError_t split_drift_far(const Launch &L, SplitBufs &s, int64_t n, double dt,
                             double *px, double *py, double *pz, const double *vx, const double *vy, const double *vz);
 
 // ---- adjoint.cu (gradient of the KDK leapfrog with the softened direct-sum force) ----
+// Scratch of the tree adjoint (walk_lists.cu): node-moment and source-star accumulators, each
+// sorted star's own terms and its leaf.
+struct AdjTreeBufs {
+    double *nadj = nullptr, *sadj = nullptr, *tgt = nullptr;
+    int32_t *star_leaf = nullptr;
+    int64_t cap_nodes = 0, cap_n = 0;
+};
+
 struct AdjTape {
     void *block = nullptr;  // one grow-only allocation holding every array below
     size_t bytes = 0;
@@ -327,6 +335,13 @@ struct AdjTape {
     double *rv = nullptr, *ra = nullptr;              // 3n each: velocities and accelerations of the replay
     double *part = nullptr;                           // nsplit x 4n: FP32 pair sums per source split
     float4 *hi = nullptr, *lo = nullptr, *w = nullptr;  // n each: FP32 positions + mass, remainders, weights
+    // Tree force (gbh_adjoint_params.force = GBH_ADJ_TREE): the list walk in 32-star groups at
+    // theta and leaf size leaf, on the context's tree buffers, and the adjoint's own scratch.
+    bool tree = false;
+    double theta = 0.9;
+    int leaf = 24;
+    TreeBufs *tb = nullptr;
+    AdjTreeBufs tbs;
     // Optional stage marks around each pair-kernel launch: (prep start, pair start, pair end).
     cudaError_t (*mark)(void *) = nullptr;
     void *mark_arg = nullptr;
@@ -361,5 +376,14 @@ int list_depth_max(bool exact);
 // warps; needs b.cap_nodes < 2^29.
 cudaError_t walk_lists(const Launch &L, const TreeBufs &b, float eps2, int quad, double *ax, double *ay, double *az,
                        int list_depth, bool targets, int stars_per_lane);
+// The transposed Jacobian of the list walk's force (32-star groups, quadrupoles, softening > 0)
+// with the lists of the tree in b frozen: for weights w (state order) writes, in state order,
+// (J^T w)_i and (da/dm)^T w_i into out (x, y, z and m terms, n apart). px .. mass: the state the
+// tree was built from.
+cudaError_t walk_lists_adjoint(const Launch &L, const TreeBufs &b, float eps2, const double *px, const double *py,
+                               const double *pz, const double *mass, const double *wx, const double *wy,
+                               const double *wz, int64_t n, AdjTreeBufs &s, double *out);
+cudaError_t adj_tree_reserve(AdjTreeBufs &s, const TreeBufs &b);
+void adj_tree_free(AdjTreeBufs &s);
 
 }  // namespace gbh

@@ -251,19 +251,30 @@ struct GroupOut {
     bool ok;
 };
 
-// The warp's list buffers (evaluated by the walking warp itself whenever one is full).
+// The warp's list buffers and what a full list is handed to: InPlace evaluates the forces of
+// the lane's stars (the list walk); the adjoint sink below evaluates the transposed Jacobian.
 struct InPlace {
+    static constexpr bool kIndices = false;  // no node or star index per entry
     float4 *nbuf, *sbuf;
+    int32_t *nidx, *sidx;
+    template <bool kExact, bool kQuad, bool kSoft, int kS>
+    __device__ __forceinline__ void nodes(int count, const Target (&t)[kS], float eps2, Acc (&a)[kS], int) {
+        eval_nodes<kExact, kQuad, kSoft, kS>(nbuf, count, t, eps2, a);
+    }
+    template <bool kExact, bool kSoft, int kS>
+    __device__ __forceinline__ void sources(int count, const Target (&t)[kS], float eps2, Acc (&a)[kS], int) {
+        eval_sources<kExact, kSoft, kS>(sbuf, count, t, eps2, a);
+    }
 };
 
 // Walks one group with the given separation form; a is zeroed by the caller.
-template <bool kExact, bool kQuad, bool kSoft, int kS, class Sink>
+template <bool kExact, bool kQuad, bool kSoft, int kS, class Sink, class AccT>
 __device__ __forceinline__ GroupOut walk_group(TravMem &W, Sink &sink, int lane, int32_t root, const Target (&t)[kS], float Ox,
                                                float Oy, float Oz, float bx0, float by0, float bz0, float bx1,
                                                float by1, float bz1, float ext, float eps2, int node_depth,
                                                int src_depth, const LNode *__restrict__ nodes,
                                                const float4 *__restrict__ st_hi, const float4 *__restrict__ st_lo,
-                                               int32_t nn, int32_t ns, DevInfo *err_info, Acc (&a)[kS]) {
+                                               int32_t nn, int32_t ns, DevInfo *err_info, AccT (&a)[kS]) {
     using Lay = Layout<kExact>;
     constexpr int kNodeFields = kExact ? 13 : 10;
     constexpr int kSrcFields = kExact ? 7 : 4;
@@ -287,13 +298,13 @@ __device__ __forceinline__ GroupOut walk_group(TravMem &W, Sink &sink, int lane,
     }
     auto flush_nodes = [&]() {
         pad_pair<Lay::kNodePair, kNodeFields>(sink.nbuf, ncount, lane, 3, 4, 9);
-        eval_nodes<kExact, kQuad, kSoft, kS>(sink.nbuf, ncount, t, eps2, a);
+        sink.template nodes<kExact, kQuad, kSoft, kS>(ncount, t, eps2, a, lane);
         __syncwarp();
         ncount = 0;
     };
     auto flush_sources = [&]() {
         pad_pair<Lay::kSrcPair, kSrcFields>(sink.sbuf, scount, lane, 3, 32, 32);
-        eval_sources<kExact, kSoft, kS>(sink.sbuf, scount, t, eps2, a);
+        sink.template sources<kExact, kSoft, kS>(scount, t, eps2, a, lane);
         __syncwarp();
         scount = 0;
     };
@@ -428,6 +439,7 @@ __device__ __forceinline__ GroupOut walk_group(TravMem &W, Sink &sink, int lane,
                     put(sink.nbuf, P, en, 1, cy);
                     put(sink.nbuf, P, en, 2, cz);
                 }
+                if constexpr (Sink::kIndices) sink.nidx[en] = node;
                 put(sink.nbuf, P, en, 3, qd.z);  // m
                 put(sink.nbuf, P, en, 4, qc.x);  // -qxx
                 put(sink.nbuf, P, en, 5, qc.y);  // -qyy
@@ -489,6 +501,7 @@ __device__ __forceinline__ GroupOut walk_group(TravMem &W, Sink &sink, int lane,
                         put(sink.sbuf, P, en, 2, (h.z - Oz) + l.z);
                     }
                     put(sink.sbuf, P, en, 3, h.w);
+                    if constexpr (Sink::kIndices) sink.sidx[en] = star;
                 }
                 scount += T - cs < 32 ? T - cs : 32;
                 __syncwarp();
@@ -674,7 +687,7 @@ __global__ __launch_bounds__(kLwThreads) void k_walk_lists(const DevInfo *info, 
         Acc a[kS];
         zero_acc<kS>(a);
         GroupOut r;
-        InPlace sink{W.nbuf, W.sbuf};
+        InPlace sink{W.nbuf, W.sbuf, nullptr, nullptr};
         if (B.exact)
             r = walk_group<true, kQuad, kSoft, kS>(W.tm, sink, lane, R.root, G.t, G.Ox, G.Oy, G.Oz, B.bx0, B.by0,
                                                     B.bz0, B.bx1, B.by1, B.bz1, B.ext, eps2, node_depth, src_depth,
@@ -726,6 +739,329 @@ cudaError_t walk_lists_s(const Launch &L, const TreeBufs &b, float eps2, int qua
     return lpt_order(L, b, 32 * kS);
 }
 
+// ---------------------------------------------------------------- adjoint of the list walk
+//
+// The transposed Jacobian of the list walk's force with its interaction lists frozen (the lists
+// the forward walk builds at the same positions: the same traversal runs again). Target star i
+// with weight w_i (the adjoint of its velocity) and separation d = source - x_i, r^2 = |d|^2 + eps^2:
+//   accepted node n (quadrupole, bh.go:117-133): a = f d - Q d / r^5, f = m / r^3 + 5/2 (d.Q.d) / r^7,
+//     J = da/dd = f I + d (grad f)^T - Q / r^5 + 5 (Q d) d^T / r^7 (symmetric),
+//     grad f = -3 m d / r^5 + 5 Q d / r^7 - 35/2 (d.Q.d) d / r^9;
+//     star i gets -J w_i; the node's centre of mass +J w_i, its mass (d.w_i) / r^3, and each stored
+//     quadrupole component its derivative of w_i.a;
+//   leaf star j (softened pair, bh.go:145-150): K = I / r^3 - 3 d d^T / r^5, star i gets -m_j K w_i,
+//     star j gets +m_j K w_i and (d.w_i) / r^3 on its mass; a star paired with itself adds nothing.
+// Each warp sums a list entry's source terms over its 32 stars (a reduce-scatter: lane l ends
+// with term l) and adds them to the node's or star's FP64 accumulators with atomics.
+
+constexpr int kAdjNodeTerms = 10;  // centre of mass (3), mass, Q xx yy zz xy xz yz
+constexpr int kAdjStarTerms = 4;   // position (3), mass
+
+struct AdjAcc {
+    float wx, wy, wz;     // the lane's star's weight
+    int32_t k;            // its sorted index (a star's pair with itself is skipped)
+    double gx, gy, gz;    // its own terms, summed over the flushed lists
+};
+
+// Sums v[0..31] over the warp; afterwards lane l holds the sum of term l in v[0].
+__device__ __forceinline__ void reduce_scatter32(float (&v)[32], int lane) {
+#pragma unroll
+    for (int sft = 16; sft >= 1; sft >>= 1) {
+        const bool up = (lane & sft) != 0;
+#pragma unroll
+        for (int i = 0; i < sft; ++i) {
+            const float send = up ? v[i] : v[i + sft];
+            const float keep = up ? v[i + sft] : v[i];
+            v[i] = keep + __shfl_xor_sync(kFull, send, sft);
+        }
+    }
+}
+// The same for 8 terms: full sums over the two upper lane bits, then a scatter over the lower
+// three (lane l < 8 ends with term l).
+__device__ __forceinline__ void reduce_scatter8(float (&v)[8], int lane) {
+#pragma unroll
+    for (int sft = 16; sft >= 8; sft >>= 1)
+#pragma unroll
+        for (int i = 0; i < 8; ++i) v[i] += __shfl_xor_sync(kFull, v[i], sft);
+#pragma unroll
+    for (int sft = 4; sft >= 1; sft >>= 1) {
+        const bool up = (lane & sft) != 0;
+#pragma unroll
+        for (int i = 0; i < sft; ++i) {
+            const float send = up ? v[i] : v[i + sft];
+            const float keep = up ? v[i + sft] : v[i];
+            v[i] = keep + __shfl_xor_sync(kFull, send, sft);
+        }
+    }
+}
+
+struct AdjSink {
+    static constexpr bool kIndices = true;
+    float4 *nbuf, *sbuf;
+    int32_t *nidx, *sidx;
+    double *nadj;  // [node][kAdjNodeTerms]
+    double *sadj;  // [sorted star][kAdjStarTerms]
+
+    template <bool kExact, bool kQuad, bool kSoft, int kS>
+    __device__ __forceinline__ void nodes(int count, const Target (&tt)[kS], float eps2, AdjAcc (&aa)[kS],
+                                          int lane) {
+        static_assert(kS == 1 && kQuad && kSoft, "the adjoint walk: one star a lane, quadrupoles, softening");
+        using Lay = Layout<kExact>;
+        const Target &t = tt[0];
+        AdjAcc &a = aa[0];
+        const float2 e2 = f2(eps2), wx = f2(a.wx), wy = f2(a.wy), wz = f2(a.wz);
+        float2 gx = f2(0.f), gy = f2(0.f), gz = f2(0.f);
+        const int np = (count + 1) >> 1;
+        for (int p = 0; p < np; ++p) {
+            const float4 *r = &nbuf[p * Lay::kNodePair];
+            const float4 r0 = r[0], r1 = r[1], r2a = r[2], r3 = r[3], r4 = r[4];
+            float2 lx = f2(0.f), ly = f2(0.f), lz = f2(0.f);
+            if constexpr (kExact) {
+                const float4 r5 = r[5], r6 = r[6];
+                lx = lo2(r5);
+                ly = hi2(r5);
+                lz = lo2(r6);
+            }
+            const float2 dx = sep<kExact>(lo2(r0), lx, -t.tx, -t.hx, -t.lx);
+            const float2 dy = sep<kExact>(hi2(r0), ly, -t.ty, -t.hy, -t.ly);
+            const float2 dz = sep<kExact>(lo2(r1), lz, -t.tz, -t.hz, -t.lz);
+            const float2 rr = fma2(dz, dz, fma2(dy, dy, fma2(dx, dx, e2)));
+            const float2 ir = make_float2(rsqrtf(rr.x), rsqrtf(rr.y));
+            const float2 ir2 = mul2(ir, ir), ir3 = mul2(ir2, ir), ir5 = mul2(ir3, ir2), ir7 = mul2(ir5, ir2),
+                         ir9 = mul2(ir7, ir2);
+            const float2 m = hi2(r1);
+            // the record holds -Q: n = -Q
+            const float2 nxx = lo2(r2a), nyy = hi2(r2a), nzz = lo2(r3), nxy = hi2(r3), nxz = lo2(r4), nyz = hi2(r4);
+            const float2 qx = fma2(nxz, dz, fma2(nxy, dy, mul2(nxx, dx)));  // -(Q d)
+            const float2 qy = fma2(nyz, dz, fma2(nyy, dy, mul2(nxy, dx)));
+            const float2 qz = fma2(nzz, dz, fma2(nyz, dy, mul2(nxz, dx)));
+            const float2 dqd = fma2(dz, qz, fma2(dy, qy, mul2(dx, qx)));      // -(d.Q.d)
+            const float2 dw = fma2(dz, wz, fma2(dy, wy, mul2(dx, wx)));
+            const float2 qw = fma2(qz, wz, fma2(qy, wy, mul2(qx, wx)));       // -(Q d . w)
+            const float2 nwx = fma2(nxz, wz, fma2(nxy, wy, mul2(nxx, wx)));   // -(Q w)
+            const float2 nwy = fma2(nyz, wz, fma2(nyy, wy, mul2(nxy, wx)));
+            const float2 nwz = fma2(nzz, wz, fma2(nyz, wy, mul2(nxz, wx)));
+            const float2 f = fma2(mul2(dqd, ir7), f2(-2.5f), mul2(m, ir3));
+            // grad f . w = -3 m dw / r^5 - 5 (-(Qd.w)) / r^7 + 17.5 (-(dQd)) dw / r^9
+            const float2 gw = fma2(mul2(mul2(dqd, ir9), dw), f2(17.5f),
+                                   fma2(mul2(qw, ir7), f2(-5.f), mul2(mul2(m, ir5), mul2(dw, f2(-3.f)))));
+            const float2 c5 = mul2(mul2(ir7, dw), f2(-5.f));  // -5 dw / r^7, times -(Q d)
+            const float2 jx = fma2(c5, qx, fma2(ir5, nwx, fma2(dx, gw, mul2(f, wx))));
+            const float2 jy = fma2(c5, qy, fma2(ir5, nwy, fma2(dy, gw, mul2(f, wy))));
+            const float2 jz = fma2(c5, qz, fma2(ir5, nwz, fma2(dz, gw, mul2(f, wz))));
+            gx = add2(gx, jx);
+            gy = add2(gy, jy);
+            gz = add2(gz, jz);
+            // d(w.a)/dQ: xx: 5/2 dw dx^2 / r^7 - wx dx / r^5; xy: 5 dw dx dy / r^7 - (wx dy + wy dx) / r^5
+            const float2 qa = mul2(mul2(ir7, dw), f2(2.5f));
+            const float2 Gxx = fma2(mul2(qa, dx), dx, mul2(mul2(ir5, wx), mul2(dx, f2(-1.f))));
+            const float2 Gyy = fma2(mul2(qa, dy), dy, mul2(mul2(ir5, wy), mul2(dy, f2(-1.f))));
+            const float2 Gzz = fma2(mul2(qa, dz), dz, mul2(mul2(ir5, wz), mul2(dz, f2(-1.f))));
+            const float2 qa2 = add2(qa, qa);
+            const float2 Gxy = fma2(mul2(qa2, dx), dy, mul2(ir5, mul2(fma2(wx, dy, mul2(wy, dx)), f2(-1.f))));
+            const float2 Gxz = fma2(mul2(qa2, dx), dz, mul2(ir5, mul2(fma2(wx, dz, mul2(wz, dx)), f2(-1.f))));
+            const float2 Gyz = fma2(mul2(qa2, dy), dz, mul2(ir5, mul2(fma2(wy, dz, mul2(wz, dy)), f2(-1.f))));
+            const float2 am = mul2(dw, ir3);
+            const bool hasB = 2 * p + 1 < count;  // the padded last entry is no node
+            float v[32] = {jx.x,  jy.x,  jz.x,  am.x,  Gxx.x, Gyy.x, Gzz.x, Gxy.x, Gxz.x, Gyz.x, jx.y,
+                           jy.y,  jz.y,  am.y,  Gxx.y, Gyy.y, Gzz.y, Gxy.y, Gxz.y, Gyz.y, 0.f,  0.f,
+                           0.f,   0.f,   0.f,   0.f,   0.f,   0.f,   0.f,   0.f,   0.f,   0.f};
+            reduce_scatter32(v, lane);
+            if (lane < kAdjNodeTerms || (hasB && lane < 2 * kAdjNodeTerms)) {
+                const int e = 2 * p + (lane >= kAdjNodeTerms ? 1 : 0);
+                const int term = lane >= kAdjNodeTerms ? lane - kAdjNodeTerms : lane;
+                atomicAdd(&nadj[int64_t(nidx[e]) * kAdjNodeTerms + term], double(v[0]));
+            }
+        }
+        a.gx -= double(gx.x) + double(gx.y);
+        a.gy -= double(gy.x) + double(gy.y);
+        a.gz -= double(gz.x) + double(gz.y);
+    }
+
+    template <bool kExact, bool kSoft, int kS>
+    __device__ __forceinline__ void sources(int count, const Target (&tt)[kS], float eps2, AdjAcc (&aa)[kS],
+                                            int lane) {
+        static_assert(kS == 1 && kSoft, "the adjoint walk: one star a lane, softening");
+        using Lay = Layout<kExact>;
+        const Target &t = tt[0];
+        AdjAcc &a = aa[0];
+        const float2 e2 = f2(eps2), wx = f2(a.wx), wy = f2(a.wy), wz = f2(a.wz);
+        float2 gx = f2(0.f), gy = f2(0.f), gz = f2(0.f);
+        const int np = (count + 1) >> 1;
+        for (int p = 0; p < np; ++p) {
+            const float4 *r = &sbuf[p * Lay::kSrcPair];
+            const float4 r0 = r[0], r1 = r[1];
+            float2 lx = f2(0.f), ly = f2(0.f), lz = f2(0.f);
+            if constexpr (kExact) {
+                const float4 r2a = r[2], r3 = r[3];
+                lx = lo2(r2a);
+                ly = hi2(r2a);
+                lz = lo2(r3);
+            }
+            const float2 dx = sep<kExact>(lo2(r0), lx, -t.tx, -t.hx, -t.lx);
+            const float2 dy = sep<kExact>(hi2(r0), ly, -t.ty, -t.hy, -t.ly);
+            const float2 dz = sep<kExact>(lo2(r1), lz, -t.tz, -t.hz, -t.lz);
+            const float2 rr = fma2(dz, dz, fma2(dy, dy, fma2(dx, dx, e2)));
+            const float2 ir = make_float2(rsqrtf(rr.x), rsqrtf(rr.y));
+            const float2 ir2 = mul2(ir, ir), ir3 = mul2(ir2, ir), ir5 = mul2(ir3, ir2);
+            const bool hasB = 2 * p + 1 < count;
+            // a star and its own pair, and the padded last entry, contribute nothing
+            const float keepA = sidx[2 * p] == a.k ? 0.f : 1.f;
+            const float keepB = hasB && sidx[2 * p + 1] != a.k ? 1.f : 0.f;
+            const float2 m = mul2(hi2(r1), make_float2(keepA, keepB));
+            const float2 dw = fma2(dz, wz, fma2(dy, wy, mul2(dx, wx)));
+            // m K w = m (w / r^3 - 3 d dw / r^5)
+            const float2 c3 = mul2(mul2(ir5, dw), f2(-3.f));
+            const float2 kx = mul2(m, fma2(c3, dx, mul2(ir3, wx)));
+            const float2 ky = mul2(m, fma2(c3, dy, mul2(ir3, wy)));
+            const float2 kz = mul2(m, fma2(c3, dz, mul2(ir3, wz)));
+            gx = add2(gx, kx);
+            gy = add2(gy, ky);
+            gz = add2(gz, kz);
+            const float2 am = mul2(mul2(dw, ir3), make_float2(keepA, keepB));
+            float v[8] = {kx.x, ky.x, kz.x, am.x, kx.y, ky.y, kz.y, am.y};
+            reduce_scatter8(v, lane);
+            if (lane < kAdjStarTerms || (hasB && lane < 2 * kAdjStarTerms)) {
+                const int e = 2 * p + (lane >= kAdjStarTerms ? 1 : 0);
+                const int term = lane >= kAdjStarTerms ? lane - kAdjStarTerms : lane;
+                atomicAdd(&sadj[int64_t(sidx[e]) * kAdjStarTerms + term], double(v[0]));
+            }
+        }
+        a.gx -= double(gx.x) + double(gx.y);
+        a.gy -= double(gy.x) + double(gy.y);
+        a.gz -= double(gz.x) + double(gz.y);
+    }
+};
+
+struct __align__(16) AdjWarpMem {
+    float4 nbuf[kNodeF4];
+    float4 sbuf[kSrcF4];
+    int32_t nidx[Layout<false>::kNodeCap];
+    int32_t sidx[Layout<false>::kSrcCap];
+    TravMem tm;
+};
+
+// The adjoint walk over 32-star groups (the forward's group size in adjoint mode): the same
+// traversal as k_walk_lists<quad, soft, 1>, with the adjoint sink. w: the weights in state order
+// (three arrays); tgt: each sorted star's own terms (3 doubles).
+__global__ __launch_bounds__(kLwThreads) void k_walk_lists_adj(const DevInfo *info, const LNode *__restrict__ nodes,
+                                                               const float4 *__restrict__ st_hi,
+                                                               const float4 *__restrict__ st_lo,
+                                                               const int32_t *__restrict__ order, float eps,
+                                                               float eps2, const double *__restrict__ wx,
+                                                               const double *__restrict__ wy,
+                                                               const double *__restrict__ wz, double *tgt,
+                                                               double *nadj, double *sadj, uint32_t *work_ctr,
+                                                               DevInfo *err_info, int node_depth, int src_depth) {
+    constexpr int kS = 1, kG = 32;
+    __shared__ AdjWarpMem smem[kLwWarps];
+    AdjWarpMem &W = smem[threadIdx.x >> 5];
+    const int lane = threadIdx.x & 31;
+    const int32_t ns = int32_t(info->nstars);
+    const int32_t nn = int32_t(info->nnodes);
+    const int32_t ng = nn > 0 ? (ns + kG - 1) / kG : 0;
+    for (;;) {
+        int32_t idx = 0;
+        if (lane == 0) idx = int32_t(atomicAdd(work_ctr, 1u));
+        idx = __shfl_sync(kFull, idx, 0);
+        if (idx >= ng) break;
+        const GroupRange R = group_range<kG>(idx, nullptr, ns);
+        if (R.cnt <= 0) continue;
+        GroupStars<kS> G;
+        group_stars<kS>(lane, R, nullptr, st_hi, st_lo, G);
+        const GroupBox B = group_box<kS>(lane, R.cnt, G.t, eps);
+        __syncwarp();
+        AdjAcc a[1];
+        const int32_t o = order[G.k[0]];
+        // a lane beyond the group (a copy of the first star) weighs nothing: no source terms
+        a[0].wx = G.valid[0] ? float(wx[o]) : 0.f;
+        a[0].wy = G.valid[0] ? float(wy[o]) : 0.f;
+        a[0].wz = G.valid[0] ? float(wz[o]) : 0.f;
+        a[0].k = G.k[0];
+        a[0].gx = a[0].gy = a[0].gz = 0.0;
+        AdjSink sink{W.nbuf, W.sbuf, W.nidx, W.sidx, nadj, sadj};
+        GroupOut r;
+        if (B.exact)
+            r = walk_group<true, true, true, kS>(W.tm, sink, lane, R.root, G.t, G.Ox, G.Oy, G.Oz, B.bx0, B.by0, B.bz0,
+                                                 B.bx1, B.by1, B.bz1, B.ext, eps2, node_depth, src_depth, nodes, st_hi,
+                                                 st_lo, nn, ns, err_info, a);
+        else
+            r = walk_group<false, true, true, kS>(W.tm, sink, lane, R.root, G.t, G.Ox, G.Oy, G.Oz, B.bx0, B.by0,
+                                                  B.bz0, B.bx1, B.by1, B.bz1, B.ext, eps2, node_depth, src_depth,
+                                                  nodes, st_hi, st_lo, nn, ns, err_info, a);
+        __syncwarp();
+        if (!r.ok) break;
+        if (G.valid[0]) {
+            tgt[3 * int64_t(G.k[0])] = a[0].gx;
+            tgt[3 * int64_t(G.k[0]) + 1] = a[0].gy;
+            tgt[3 * int64_t(G.k[0]) + 2] = a[0].gz;
+        }
+    }
+}
+
+// The leaf of every sorted star (from the leaves' star ranges in their list records).
+__global__ void k_star_leaf(const DevInfo *info, const LNode *__restrict__ nodes, int32_t *star_leaf) {
+    const int64_t r = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (r >= info->nnodes) return;
+    const LNode nd = nodes[r];
+    if (!(nd.a.w < 0.f)) return;  // inner node
+    const int32_t lo = int32_t(__float_as_uint(nd.b.w)), hi = __float_as_int(nd.d.w);
+    const int32_t ns = int32_t(info->nstars);
+    for (int32_t j = lo < 0 ? 0 : lo; j < hi && j < ns; ++j) star_leaf[j] = int32_t(r);
+}
+
+// Per sorted star k: its own terms and its pair terms as a source, plus the chain rule through
+// the moments of every node that holds it (its leaf and the leaf's ancestors):
+//   com = sum m x / M:  x_k gets (m_k / M) A_c, m_k gets (x_k - com).A_c / M;  M: m_k gets A_m;
+//   Q = sum m (3 e e^T - |e|^2 I), e = x - com (the com's own dependence drops out, sum m e = 0):
+//   x_k gets m_k (dQ/de)^T G and m_k gets the Q of e_k contracted with G.
+// Written in state order into out (x, y, z, m terms, n apart).
+__global__ void k_adj_downsweep(const DevInfo *info, const LNode *__restrict__ nodes, const int32_t *__restrict__ parent,
+                                const int32_t *__restrict__ star_leaf, const int32_t *__restrict__ order,
+                                const double *__restrict__ px, const double *__restrict__ py,
+                                const double *__restrict__ pz, const double *__restrict__ mass,
+                                const double *__restrict__ tgt, const double *__restrict__ nadj,
+                                const double *__restrict__ sadj, int64_t n, double *out, DevInfo *err_info) {
+    const int64_t k = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    const int64_t ns = info->nstars;
+    if (k >= ns) return;
+    const int32_t i = order[k];
+    const double x = px[i], y = py[i], z = pz[i], mk = mass[i];
+    double gx = tgt[3 * k] + sadj[4 * k], gy = tgt[3 * k + 1] + sadj[4 * k + 1], gz = tgt[3 * k + 2] + sadj[4 * k + 2];
+    double gm = sadj[4 * k + 3];
+    int32_t r = star_leaf[k];
+    const int32_t nn = int32_t(info->nnodes);
+    for (int guard = 0; r >= 0 && guard <= kMaxLevel + 1; ++guard) {
+        if (r >= nn) {
+            atomicExch(&err_info->err, 1);
+            err_info->err_where = 24;
+            break;
+        }
+        const LNode nd = nodes[r];
+        const double M = double(nd.d.z);
+        const double *A = nadj + int64_t(r) * kAdjNodeTerms;
+        if (M > 0) {
+            const double ex = x - (double(nd.a.x) + double(nd.b.x)), ey = y - (double(nd.a.y) + double(nd.b.y)),
+                         ez = z - (double(nd.a.z) + double(nd.b.z));
+            const double Gxx = A[4], Gyy = A[5], Gzz = A[6], Gxy = A[7], Gxz = A[8], Gyz = A[9];
+            const double s = mk / M;
+            gx += s * A[0] + mk * ((4 * Gxx - 2 * Gyy - 2 * Gzz) * ex + 3 * Gxy * ey + 3 * Gxz * ez);
+            gy += s * A[1] + mk * ((4 * Gyy - 2 * Gxx - 2 * Gzz) * ey + 3 * Gxy * ex + 3 * Gyz * ez);
+            gz += s * A[2] + mk * ((4 * Gzz - 2 * Gxx - 2 * Gyy) * ez + 3 * Gxz * ex + 3 * Gyz * ey);
+            const double e2 = ex * ex + ey * ey + ez * ez;
+            gm += A[3] + (ex * A[0] + ey * A[1] + ez * A[2]) / M + Gxx * (3 * ex * ex - e2) +
+                  Gyy * (3 * ey * ey - e2) + Gzz * (3 * ez * ez - e2) + 3 * (Gxy * ex * ey + Gxz * ex * ez + Gyz * ey * ez);
+        } else {
+            gm += A[3];
+        }
+        r = parent[r];
+    }
+    out[i] = gx;
+    out[n + i] = gy;
+    out[2 * n + i] = gz;
+    out[3 * n + i] = gm;
+}
+
 }  // namespace
 
 int list_depth_max(bool exact) { return exact ? Layout<true>::kNodeCap - 32 : Layout<false>::kNodeCap - 32; }
@@ -743,6 +1079,60 @@ cudaError_t walk_lists(const Launch &L, const TreeBufs &b, float eps2, int quad,
     const bool lpt = b.lpt && !targets;  // a target list changes from event to event
     if (stars_per_lane == 2) return walk_lists_s<2>(L, b, eps2, quad, ax, ay, az, nd, sd, lpt, targets);
     return walk_lists_s<1>(L, b, eps2, quad, ax, ay, az, nd, sd, lpt, targets);
+}
+
+cudaError_t walk_lists_adjoint(const Launch &L, const TreeBufs &b, float eps2, const double *px, const double *py,
+                               const double *pz, const double *mass, const double *wx, const double *wy,
+                               const double *wz, int64_t n, AdjTreeBufs &s, double *out) {
+    cudaError_t e;
+    if ((e = cudaMemsetAsync(s.nadj, 0, sizeof(double) * kAdjNodeTerms * size_t(b.cap_nodes), L.stream))) return e;
+    if ((e = cudaMemsetAsync(s.sadj, 0, sizeof(double) * kAdjStarTerms * size_t(b.cap_n), L.stream))) return e;
+    if ((e = cudaMemsetAsync(s.star_leaf, 0xff, sizeof(int32_t) * size_t(b.cap_n), L.stream))) return e;
+    if ((e = cudaMemsetAsync(b.walk_ctr, 0, sizeof(uint32_t), L.stream))) return e;
+    static int blocks_per_sm = 0;
+    if (!blocks_per_sm) {
+        if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_walk_lists_adj, kLwThreads, 0)))
+            return e;
+        if (blocks_per_sm < 1) blocks_per_sm = 1;
+    }
+    const int sms = L.num_sms > 0 ? L.num_sms : 152;
+    const int nd = kDefaultListDepth, sd = 2 * kDefaultListDepth;
+    k_walk_lists_adj<<<unsigned(sms * blocks_per_sm), kLwThreads, 0, L.stream>>>(
+        b.info, b.lnode, b.st_hi, b.st_lo, b.order, sqrtf(eps2), eps2, wx, wy, wz, s.tgt, s.nadj, s.sadj, b.walk_ctr,
+        b.info, nd, sd);
+    ++*L.count;
+    if ((e = cudaGetLastError())) return e;
+    const unsigned nbn = unsigned((b.cap_nodes + 255) / 256), nbs = unsigned((b.cap_n + 255) / 256);
+    k_star_leaf<<<nbn < 1 ? 1 : nbn, 256, 0, L.stream>>>(b.info, b.lnode, s.star_leaf);
+    ++*L.count;
+    if ((e = cudaGetLastError())) return e;
+    k_adj_downsweep<<<nbs < 1 ? 1 : nbs, 256, 0, L.stream>>>(b.info, b.lnode, b.n_parent, s.star_leaf, b.order, px, py,
+                                                            pz, mass, s.tgt, s.nadj, s.sadj, n, out, b.info);
+    ++*L.count;
+    return cudaGetLastError();
+}
+
+cudaError_t adj_tree_reserve(AdjTreeBufs &s, const TreeBufs &b) {
+    if (s.cap_nodes >= b.cap_nodes && s.cap_n >= b.cap_n) return cudaSuccess;
+    adj_tree_free(s);
+    cudaError_t e = dev_alloc(&s.nadj, sizeof(double) * kAdjNodeTerms * size_t(b.cap_nodes));
+    if (e == cudaSuccess) e = dev_alloc(&s.sadj, sizeof(double) * kAdjStarTerms * size_t(b.cap_n));
+    if (e == cudaSuccess) e = dev_alloc(&s.tgt, sizeof(double) * 3 * size_t(b.cap_n));
+    if (e == cudaSuccess) e = dev_alloc(&s.star_leaf, sizeof(int32_t) * size_t(b.cap_n));
+    if (e != cudaSuccess) {
+        adj_tree_free(s);
+        return e;
+    }
+    s.cap_nodes = b.cap_nodes;
+    s.cap_n = b.cap_n;
+    return cudaSuccess;
+}
+
+void adj_tree_free(AdjTreeBufs &s) {
+    void *ptrs[] = {s.nadj, s.sadj, s.tgt, s.star_leaf};
+    for (void *p : ptrs)
+        if (p) cudaFree(p);
+    s = AdjTreeBufs{};
 }
 
 }  // namespace gbh

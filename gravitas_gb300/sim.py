@@ -179,15 +179,17 @@ class Simulation:
 
 
 def trajectory_loss_gradient(state: dict, targets: np.ndarray, dt: float, softening: float, nsteps: int,
-                             every: int = 50, precision: int = abi.ADJ_FP32, ctx: abi.Context | None = None):
+                             every: int = 50, precision: int = abi.ADJ_FP32, ctx: abi.Context | None = None,
+                             force: int = abi.ADJ_DIRECT, theta: float = 0.0, leaf: int = 0):
     """Loss L = mean_i |x_i(T) - target_i|^2 after nsteps KDK steps of the softened direct-sum
-    dynamics, and its gradient with respect to the initial positions, velocities (n x 3 each)
-    and masses, through the adjoint pair gbh_fwd_save / gbh_bwd (checkpoints every `every`
+    dynamics (force=abi.ADJ_TREE: the Barnes-Hut force at theta and leaf size leaf, its lists
+    frozen per step), and its gradient with respect to the initial positions, velocities (n x 3
+    each) and masses, through the adjoint pair gbh_fwd_save / gbh_bwd (checkpoints every `every`
     steps, recomputation in between). Returns (loss, dx0, dv0, dm)."""
     ctx = ctx or default_context()
     x0 = np.stack([state["px"], state["py"], state["pz"]], 1)
     v0 = np.stack([state["vx"], state["vy"], state["vz"]], 1)
-    xT, _ = ctx.fwd_save(x0, v0, state["mass"], dt, softening, nsteps, every, precision)
+    xT, _ = ctx.fwd_save(x0, v0, state["mass"], dt, softening, nsteps, every, precision, force, theta, leaf)
     r = xT - targets
     n = len(r)
     loss = float(np.sum(r * r) / n)

@@ -298,6 +298,7 @@ int gbh_forest_layout(gbh_ctx *ctx, int32_t nsys, int64_t *star_range, int64_t *
  * because the tree force jumps where a node's opening test or a star's cell changes.
  */
 enum { GBH_ADJ_FP32 = 0, GBH_ADJ_FP64 = 1 };
+enum { GBH_ADJ_DIRECT = 0, GBH_ADJ_TREE = 1 };
 typedef struct {
     double dt;         /* step length */
     double softening;  /* Plummer epsilon; must be > 0 */
@@ -305,7 +306,14 @@ typedef struct {
     int64_t every;     /* checkpoint interval K >= 1: (x, v, a) saved every K steps */
     int32_t precision; /* GBH_ADJ_FP64: pair sums bit-identical to the FP64 checker;
                           GBH_ADJ_FP32: FP32 pairs, double-float separations, compensated sums */
-    int32_t reserved[3];
+    int32_t force;     /* GBH_ADJ_DIRECT: the softened direct sum (direct.go:18-48), every body a
+                          source; GBH_ADJ_TREE (GBH_ADJ_FP32 only): the Barnes-Hut force of the
+                          mixed walk (quadrupoles, 32-star groups of the list walk, FP32 moments),
+                          differentiated with each step's interaction lists and tree topology
+                          frozen (the lists the forward builds at the same positions) */
+    int32_t leaf_size; /* GBH_ADJ_TREE: max stars per leaf; 0 means 24 */
+    int32_t reserved;
+    double theta;      /* GBH_ADJ_TREE: opening angle; 0 means 0.9 */
 } gbh_adjoint_params;
 
 /* Forward half: runs the steps from (x0, v0) with masses m, keeping checkpoints on the

@@ -50,7 +50,7 @@ def test_null_context_is_rejected():
 
 def test_params_layout_matches_header():
     assert ctypes.sizeof(abi.Params) == 48
-    assert ctypes.sizeof(abi.AdjointParams) == 48
+    assert ctypes.sizeof(abi.AdjointParams) == 56
     assert ctypes.sizeof(abi.TuneEntry) == 64
     assert ctypes.sizeof(abi.Diagnostics) == 112
     assert ctypes.sizeof(abi.Config) == 32

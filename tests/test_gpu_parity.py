@@ -100,6 +100,20 @@ def test_tree_bit_exact_random(ctx, n, leaf, seed, theta):
     assert np.array_equal(a, t.accelerations(0.01))
 
 
+@pytest.mark.parametrize("n,leaf,seed", [(700_000, 16, 12), (1_000_000, 32, 13)])
+def test_tree_bit_exact_both_sort_paths(ctx, n, leaf, seed):
+    """Keys, order and the node table against the oracle at sizes on both sides of the switch
+    between the one-sweep radix passes (capacity up to 786,432 bodies: 700k) and the three-launch
+    passes (1M), in a fresh context so that the capacity is the state's own."""
+    s = random_state(n, seed, kinds=True, dead=True)
+    c = abi.Context(0)
+    try:
+        gpu_acc(c, s, 0.5, leaf, 0.01, "fp64")
+        assert_tree_equal(c, s, 0.5, leaf)
+    finally:
+        c.close()
+
+
 def test_tree_bit_exact_kinds_dead_dm_off(ctx):
     s = random_state(20_000, 11, kinds=True, dead=True)
     s["kind"][::97] = O.BLACK_HOLE
