@@ -408,7 +408,8 @@ int gbh_probe_fp32_peak(gbh_ctx *ctx, double ms, double *tflops);
  * life of the process: after a cudaDeviceReset of that device, do not call this entry point on
  * it again. All calls share the array: calls that overlap on the GPU (for instance on two
  * streams of one device) race and must be serialised by the caller. Every call waits for its
- * stream to finish before returning (it reads the number of sorted bodies back to the host).
+ * stream to finish before returning (it reads the number of sorted bodies back to the host), so
+ * it cannot be called while that stream is being captured into a CUDA graph.
  * An alive star with a non-finite position gives GBH_ERR_ARG. Errors are returned as a code
  * with a message in err.
  */
