@@ -111,6 +111,10 @@ struct TreeBufs {
     // (cleared at the start of every build)
     uint32_t *os_state = nullptr;
     int64_t os_words = 0;
+    // larger states: single-pass scans of the three-launch passes' digit tables (a counter and
+    // the look-back words of each pass), cleared at each build
+    uint32_t *hs_state = nullptr;
+    int64_t hs_words = 0;
     // sorted stars
     double *sx = nullptr, *sy = nullptr, *sz = nullptr, *sm = nullptr;
     float4 *st_hi = nullptr, *st_lo = nullptr;

@@ -203,7 +203,8 @@ __device__ __forceinline__ void st_volatile64(unsigned long long *p, unsigned lo
     *reinterpret_cast<volatile unsigned long long *>(p) = v;
 }
 
-// Single-pass exclusive scan with decoupled look-back (one launch): a block takes the next tile
+// Single-pass exclusive scan with decoupled look-back (one launch; every scan of tree_build, in
+// place of a reduce, a scan of the tile sums and an apply): a block takes the next tile
 // from *ctr, publishes its sum, adds its predecessors' (their inclusive prefix, or their sums
 // back to one that has published a prefix) and publishes its own inclusive prefix. Waits are
 // bounded as in the one-sweep sort. status: one 64-bit word per tile (flag in the top 2 bits).
@@ -1725,7 +1726,7 @@ static cudaError_t scan_dyn(const Launch &L, const uint32_t *in, uint32_t *out, 
 }
 
 void tree_free(TreeBufs &b) {
-    void *ptrs[] = {b.flag, b.pos4, b.bbox_part, b.keys, b.keys_alt, b.order, b.order_alt, b.hist, b.os_state, b.sx, b.sy, b.sz, b.sm,
+    void *ptrs[] = {b.flag, b.pos4, b.bbox_part, b.keys, b.keys_alt, b.order, b.order_alt, b.hist, b.os_state, b.hs_state, b.sx, b.sy, b.sz, b.sm,
                     b.st_hi, b.st_lo, b.st_off, b.chain_cnt, b.leaves, b.targets, b.geo, b.sid_sorted, b.groups, b.gcost, b.gperm, b.pre_parent, b.pre_info, b.pre_nchild, b.pre_mask, b.pre_ref, b.nodes,
                     b.n_parent, b.n_info, b.n_arrive, b.pnodes, b.mnodes, b.mrange, b.lnode, b.walk_ctr, b.scan_tmp, b.info, b.part_acc};
     for (void *p : ptrs)
@@ -1802,6 +1803,12 @@ cudaError_t tree_alloc(TreeBufs &b, int64_t n, int leaf, int32_t nsys) {
     GBH_ALLOC(b.lnode, cnodes);
     GBH_ALLOC(b.walk_ctr, 16);
     GBH_ALLOC(b.scan_tmp, scan_cap);
+    // single-pass scans of larger states: the digit tables of the three-launch passes (10 with a
+    // forest's system digits) and the build's three other scans, each 2 words of counter and the
+    // 64-bit look-back words of its tiles
+    const int64_t hs_words = kOsPassesMax * (2 + 2 * os_scan_tiles(rs_tiles * kRsBins)) +
+                             kOsScans * (2 + 2 * os_scan_tiles(cn > cnodes ? cn : cnodes));
+    GBH_ALLOC(b.hs_state, hs_words);
     int64_t os_words = 0;
     if (cn <= kOsMaxN) {  // node capacity stays below 2^30 too (at most 12 nodes a body)
         const int64_t stiles = os_scan_tiles(cn > cnodes ? cn : cnodes);
@@ -1817,6 +1824,7 @@ cudaError_t tree_alloc(TreeBufs &b, int64_t n, int leaf, int32_t nsys) {
     b.cap_n = cn;
     b.cap_nodes = cnodes;
     b.os_words = os_words;
+    b.hs_words = hs_words;
     b.cap_sys = csys;
     b.cap_groups = cgroups;
     b.nsys = nsys;
@@ -1851,6 +1859,30 @@ static cudaError_t scan_lb(const Launch &L, TreeBufs &b, int which, const uint32
     return cudaGetLastError();
 }
 
+// Single-pass scans of larger states (hs_state), in place of the three-launch scans: pass p's
+// digit table (rs_tiles x 256 entries: at 1M bodies 81 tiles, a look-back of three round trips),
+// and scan `which` (0 flags, 1 chain counts, 2 child counts) of n entries.
+static cudaError_t scan_hs(const Launch &L, TreeBufs &b, uint32_t *base, const uint32_t *in, uint32_t *out, int64_t n,
+                           const int64_t *ndyn) {
+    const int64_t tiles = os_scan_tiles(n);
+    if (tiles < 1) return cudaSuccess;
+    k_scan_lb<<<unsigned(tiles), kScanThreads, 0, L.stream>>>(in, out, n, ndyn, base,
+                                                              reinterpret_cast<unsigned long long *>(base + 2), b.info);
+    ++*L.count;
+    return cudaGetLastError();
+}
+static int64_t hs_pass_words(const TreeBufs &b) { return 2 + 2 * os_scan_tiles(os_sort_tiles(b.cap_n) * kRsBins); }
+static cudaError_t scan_hist(const Launch &L, TreeBufs &b, int p, uint32_t ntiles) {
+    return scan_hs(L, b, b.hs_state + int64_t(p) * hs_pass_words(b), b.hist, b.hist, int64_t(ntiles) * kRsBins,
+                   nullptr);
+}
+static cudaError_t scan_big(const Launch &L, TreeBufs &b, int which, const uint32_t *in, uint32_t *out, int64_t n,
+                            const int64_t *ndyn) {
+    const int64_t stiles = os_scan_tiles(b.cap_n > b.cap_nodes ? b.cap_n : b.cap_nodes);
+    uint32_t *base = b.hs_state + kOsPassesMax * hs_pass_words(b) + int64_t(which) * (2 + 2 * stiles);
+    return scan_hs(L, b, base, in, out, n, ndyn);
+}
+
 cudaError_t tree_build(const Launch &L, TreeBufs &b, int64_t n, const double *px, const double *py, const double *pz,
                        const double *mass, const uint8_t *kind, const uint8_t *alive, double *ax, double *ay,
                        double *az, double theta, int leaf, int dm_off, bool exact, bool plain_records,
@@ -1867,6 +1899,8 @@ cudaError_t tree_build(const Launch &L, TreeBufs &b, int64_t n, const double *px
     if (os) {
         const int64_t words = os_sort_base(b) + int64_t(npass) * os_sort_tiles(cap) * kRsBins;
         if ((e = cudaMemsetAsync(b.os_state, 0, sizeof(uint32_t) * size_t(words), s)) != cudaSuccess) return e;
+    } else if ((e = cudaMemsetAsync(b.hs_state, 0, sizeof(uint32_t) * size_t(b.hs_words), s)) != cudaSuccess) {
+        return e;
     }
     if (!forest) {
         // collect + bbox (build.go:62-113)
@@ -1875,7 +1909,7 @@ cudaError_t tree_build(const Launch &L, TreeBufs &b, int64_t n, const double *px
         k_flags_bbox<<<fb, kThreads, 0, s>>>(n, px, py, pz, mass, kind, alive, b.flag, b.bbox_part, ax, ay, az,
                                              b.info, b.pos4);
         GBH_LAUNCH_CHECK();
-        e = os ? scan_lb(L, b, 0, b.flag, b.flag, n, nullptr) : scan_u32(L, b.flag, b.flag, n, b.scan_tmp, b.scan_tmp_cap);
+        e = os ? scan_lb(L, b, 0, b.flag, b.flag, n, nullptr) : scan_big(L, b, 0, b.flag, b.flag, n, nullptr);
         if (e != cudaSuccess) return e;
         k_bbox_final<<<1, kFinalThreads, 0, s>>>(int(fb), b.bbox_part, n, b.flag, kind, alive, theta, b.info, b.geo);
         GBH_LAUNCH_CHECK();
@@ -1890,7 +1924,7 @@ cudaError_t tree_build(const Launch &L, TreeBufs &b, int64_t n, const double *px
         k_flags_sys<<<blocks_for(n, kThreads), kThreads, 0, s>>>(n, px, py, pz, mass, kind, alive, sys_of, b.flag,
                                                                  b.geo, ax, ay, az, b.pos4);
         GBH_LAUNCH_CHECK();
-        e = os ? scan_lb(L, b, 0, b.flag, b.flag, n, nullptr) : scan_u32(L, b.flag, b.flag, n, b.scan_tmp, b.scan_tmp_cap);
+        e = os ? scan_lb(L, b, 0, b.flag, b.flag, n, nullptr) : scan_big(L, b, 0, b.flag, b.flag, n, nullptr);
         if (e != cudaSuccess) return e;
         k_sys_final<<<sb, 128, 0, s>>>(b.nsys, n, sys_off, b.flag, kind, alive, theta, b.geo, b.info);
         GBH_LAUNCH_CHECK();
@@ -1930,8 +1964,7 @@ cudaError_t tree_build(const Launch &L, TreeBufs &b, int64_t n, const double *px
     for (int shift = 0; shift < 64 && !os; shift += 8) {
         k_rs_hist<false><<<ntiles, kRsThreads, 0, s>>>(kin, vin, nullptr, b.info, shift, ntiles, b.hist);
         GBH_LAUNCH_CHECK();
-        e = scan_u32(L, b.hist, b.hist, int64_t(ntiles) * kRsBins, b.scan_tmp, b.scan_tmp_cap);
-        if (e != cudaSuccess) return e;
+        if ((e = scan_hist(L, b, shift / 8, ntiles)) != cudaSuccess) return e;
         k_rs_scatter<false><<<ntiles, kRsThreads, 0, s>>>(kin, vin, kout, vout, nullptr, b.info, shift, ntiles, b.hist);
         GBH_LAUNCH_CHECK();
         uint64_t *tk = kin;
@@ -1945,8 +1978,7 @@ cudaError_t tree_build(const Launch &L, TreeBufs &b, int64_t n, const double *px
         for (int shift = 0; shift < 16; shift += 8) {
             k_rs_hist<true><<<ntiles, kRsThreads, 0, s>>>(kin, vin, sys_of, b.info, shift, ntiles, b.hist);
             GBH_LAUNCH_CHECK();
-            e = scan_u32(L, b.hist, b.hist, int64_t(ntiles) * kRsBins, b.scan_tmp, b.scan_tmp_cap);
-            if (e != cudaSuccess) return e;
+            if ((e = scan_hist(L, b, 8 + shift / 8, ntiles)) != cudaSuccess) return e;
             k_rs_scatter<true><<<ntiles, kRsThreads, 0, s>>>(kin, vin, kout, vout, sys_of, b.info, shift, ntiles,
                                                              b.hist);
             GBH_LAUNCH_CHECK();
@@ -1968,8 +2000,7 @@ cudaError_t tree_build(const Launch &L, TreeBufs &b, int64_t n, const double *px
     const int32_t *sid = forest ? b.sid_sorted : nullptr;
     k_chain_count<<<nb, kThreads, 0, s>>>(b.keys, b.info, sid, b.geo, leaf, cnt);
     GBH_LAUNCH_CHECK();
-    e = os ? scan_lb(L, b, 1, cnt, base, cap, &b.info->nstars)
-           : scan_dyn(L, cnt, base, cap, &b.info->nstars, b.scan_tmp, b.scan_tmp_cap);
+    e = os ? scan_lb(L, b, 1, cnt, base, cap, &b.info->nstars) : scan_big(L, b, 1, cnt, base, cap, &b.info->nstars);
     if (e != cudaSuccess) return e;
     e = cudaMemsetAsync(b.pre_mask, 0, sizeof(uint32_t) * size_t(b.cap_nodes), s);
     if (e == cudaSuccess) e = cudaMemsetAsync(b.pre_nchild, 0, sizeof(uint32_t) * size_t(b.cap_nodes), s);
@@ -1978,7 +2009,7 @@ cudaError_t tree_build(const Launch &L, TreeBufs &b, int64_t n, const double *px
                                          b.leaves, sid, b.geo);
     GBH_LAUNCH_CHECK();
     e = os ? scan_lb(L, b, 2, b.pre_nchild, b.pre_nchild, b.cap_nodes, &b.info->nnodes)
-           : scan_dyn(L, b.pre_nchild, b.pre_nchild, b.cap_nodes, &b.info->nnodes, b.scan_tmp, b.scan_tmp_cap);
+           : scan_big(L, b, 2, b.pre_nchild, b.pre_nchild, b.cap_nodes, &b.info->nnodes);
     if (e != cudaSuccess) return e;
     k_ref_index<<<nb, kThreads, 0, s>>>(b.info, cnt, base, b.pre_parent, b.pre_info, b.pre_mask, b.pre_nchild,
                                         b.pre_ref, sid, b.geo);
