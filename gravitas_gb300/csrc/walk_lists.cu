@@ -1,8 +1,9 @@
 // walk_lists.cu — the list walk: the mixed-precision FP32 walk with decoupled traversal and
 // evaluation (compiled like walk.cu: FMA contraction on, fast FP32 division and square root).
 //
-// One warp owns a group of up to 32 consecutive Morton-sorted stars, one per lane, and builds the
-// group's interaction lists cooperatively before evaluating them:
+// One warp owns a group of up to 32 or 64 consecutive Morton-sorted stars, one or two per lane
+// (lane l holds stars l and 32 + l), and builds the group's interaction lists cooperatively before
+// evaluating them:
 //
 // * Traversal is node-parallel. The warp keeps a stack of sibling ranges (an opened inner node's
 //   children are contiguous in the reference's serial layout, build.go:142-152) in shared memory
@@ -15,13 +16,15 @@
 // * Accepted nodes and the stars of opened leaves are appended (ballot + popc offsets) to two
 //   lists in shared memory, staged as FP32 records relative to the group's origin. When a list
 //   reaches its depth (a knob of gbh_params.list_depth) the warp evaluates it: every lane takes
-//   two list entries at once in packed FP32x2 arithmetic (__ffma2_rn and friends) against its own
-//   star, the records read as broadcasts from shared memory, with no branch and no dependence
-//   between entries.
+//   two list entries at once in packed FP32x2 arithmetic (__ffma2_rn and friends) against each of
+//   its stars, the records read as broadcasts from shared memory (once for both stars of a lane),
+//   with no branch and no dependence between entries.
 // * Persistent warps (one launch of num_SMs x resident blocks) take groups from a counter, longest
 //   first in the order the previous walk's group costs give (k_lpt_order). A walk restricted to a
-//   target list (block steps) takes groups of 32 consecutive list entries; a full list walks
-//   exactly as no list.
+//   target list (block steps) takes groups of 32 or 64 consecutive list entries; a full list
+//   walks exactly as no list.
+// * The adjoint sink (at the end of the file) hands the same lists to the transposed Jacobian of
+//   the walk's force instead: the tree adjoint of the adjoint pair.
 //
 // Precision: positions are FP64 split into hi + lo FP32 parts. The group's origin O is its first
 // star's hi part; a star's or node's offset from O is (hi - O) + lo in FP32, exact for nearby
