@@ -1397,7 +1397,7 @@ int gbh_autotune(gbh_ctx *ctx, const gbh_params *base, const double *thetas, int
             for (int32_t c = 0; c < ngroups * 2; ++c) {
                 // the list walk also sweeps its list depth unless the caller set one
                 const bool lists = base->walk == GBH_WALK_MIXED;
-                static const int32_t kDepths[2] = {24, 48};
+                static const int32_t kDepths[2] = {24, 56};
                 if ((c & 1) && !(lists && base->list_depth == 0)) continue;
                 gbh_params p = *base;
                 p.theta = thetas[a];

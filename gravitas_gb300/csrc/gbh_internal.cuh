@@ -372,7 +372,7 @@ cudaError_t fp32_fma_probe(const Launch &L, int blocks, int iters, float *out);
 cudaError_t lpt_order(const Launch &L, const TreeBufs &b, int gsize);
 
 // ---- walk_lists.cu (the list walk: decoupled traversal and evaluation, 32- or 64-star groups) ----
-constexpr int kDefaultListDepth = 48;
+constexpr int kDefaultListDepth = 56;
 // The largest node-list depth (entries evaluated per flush) of the list walk.
 int list_depth_max(bool exact);
 // Every star, or (targets = true) the stars listed in b.targets, in groups of 32 x stars_per_lane

@@ -88,7 +88,7 @@ typedef struct {
                                 paired walk shares each group's walk among several warps (unless
                                 GBH_CFG_NO_SPLIT); 0: 64 for a forest and for a single system of
                                 at least 524,288 stars or of up to 21 groups per SM, else 32 */
-    int32_t list_depth;      /* list walk: node-list entries evaluated per pass, 2 to 56 (0 means 48;
+    int32_t list_depth;      /* list walk: node-list entries evaluated per pass, 2 to 56 (0 means 56;
                                 source lists take twice as many, up to 160) */
     double c;                /* speed of light of the steps (Params.C): 0 Newtonian; > 0 drifts by
                                 u / gamma (sim.go:315-343) and uses Paczynski-Wiita star-hole
@@ -354,7 +354,7 @@ typedef struct {
  * relative force error, on `sample` evenly spaced alive stars against the FP64 direct sum
  * over each star's own system, is at most rms_bound. NULL or empty lists take the defaults
  * theta {0.4, 0.5, 0.7}, leaf {4, 8, 16, 32}, group {64, 32}, and for the mixed walk the list
- * depths {24, 48} unless base->list_depth is set; sample <= 0 means 1024 and
+ * depths {24, 56} unless base->list_depth is set; sample <= 0 means 1024 and
  * reps <= 0 means 3. Every candidate is written to table (up to table_cap) and counted in
  * *ntable. If none meets the bound, *best is the most accurate one and the call returns
  * GBH_ERR_LIMIT. The resident accelerations are left stale (the next step recomputes them).

@@ -534,9 +534,9 @@ def test_autotune_single_system(ctx):
              P(s["mass"]), None, None)
     base = abi.make_params(0.5, 0.01, 8, False, False, "mixed")
     best, table = ctx.autotune(base, rms_bound=2e-3, sample=1024, reps=2, strict=True)
-    assert len(table) == 3 * 4 * 4  # groups 64 and 32, each at list depths 24 and 48
+    assert len(table) == 3 * 4 * 4  # groups 64 and 32, each at list depths 24 and 56
     assert {(e["theta"], e["leaf_size"], e["group_size"], e["list_depth"]) for e in table} == {
-        (t, l, g, d) for t in (0.4, 0.5, 0.7) for l in (4, 8, 16, 32) for g in (64, 32) for d in (24, 48)}
+        (t, l, g, d) for t in (0.4, 0.5, 0.7) for l in (4, 8, 16, 32) for g in (64, 32) for d in (24, 56)}
     for e in table:  # the error estimate does not depend on the timing
         assert 0 < e["rms_err"] < 2e-2 and e["ms"] > 0 and e["build_ms"] > 0 and e["walk_ms"] > 0
     chosen = [e for e in table if (e["theta"], e["leaf_size"], e["group_size"], e["list_depth"]) ==
