@@ -127,6 +127,7 @@ struct TreeBufs {
     uint32_t *pre_mask = nullptr;   // occupied child octants (bit per octant)
     uint32_t *pre_nchild = nullptr; // child count, then its exclusive scan
     int32_t *pre_ref = nullptr;     // reference index of pre-order node p
+    int32_t *pre_star = nullptr;    // sorted position whose chain holds pre-order node p
     // reference-layout node arrays (index r)
     gbh_node *nodes = nullptr;
     int32_t *n_parent = nullptr;

@@ -919,6 +919,7 @@ __global__ __launch_bounds__(kThreads) void k_chain_emit(const uint64_t *__restr
                                                          uint32_t *__restrict__ pre_info,
                                                          uint32_t *__restrict__ pre_nchild,
                                                          uint32_t *__restrict__ pre_mask,
+                                                         int32_t *__restrict__ pre_star,
                                                          int32_t *__restrict__ leaves,
                                                          const int32_t *__restrict__ sid_sorted,
                                                          const SysGeo *__restrict__ geo) {
@@ -954,6 +955,7 @@ __global__ __launch_bounds__(kThreads) void k_chain_emit(const uint64_t *__restr
         int32_t par = t == 0 ? parent_pre : int32_t(p) - 1;
         pre_parent[p] = par;
         pre_info[p] = uint32_t(L) | oct << 8;
+        pre_star[p] = int32_t(i);
         if (par >= 0) {  // every node marks its octant in its parent's child mask (both zeroed first)
             atomicOr(&pre_mask[par], 1u << oct);
             atomicAdd(&pre_nchild[par], 1u);
@@ -961,42 +963,53 @@ __global__ __launch_bounds__(kThreads) void k_chain_emit(const uint64_t *__restr
     }
 }
 
+// Grid of the per-node kernels below: they loop over the nodes, whose count only the device knows.
+inline unsigned node_blocks(int64_t cap_nodes) {
+    const unsigned nb = blocks_for(cap_nodes, kThreads);
+    return nb < 4096u ? nb : 4096u;
+}
+
 // Reference index of every node: 1 + (children allocated before its parent's block) + rank
-// among the parent's non-empty octants. child_base = exclusive scan of child counts.
-__global__ __launch_bounds__(kThreads) void k_ref_index(const DevInfo *info, const uint32_t *__restrict__ cnt,
-                                                        const uint32_t *__restrict__ base,
+// among the parent's non-empty octants. child_base = exclusive scan of child counts. One thread
+// per node (pre-order index p).
+__global__ __launch_bounds__(kThreads) void k_ref_index(DevInfo *info, const uint32_t *__restrict__ base,
+                                                        const int32_t *__restrict__ pre_star,
                                                         const int32_t *__restrict__ pre_parent,
                                                         const uint32_t *__restrict__ pre_info,
                                                         const uint32_t *__restrict__ pre_mask,
                                                         const uint32_t *__restrict__ child_base,
                                                         int32_t *__restrict__ pre_ref,
                                                         const int32_t *__restrict__ sid_sorted,
-                                                        const SysGeo *__restrict__ geo) {
-    int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-    int64_t n = info->nstars;
-    if (i >= n) return;
-    uint32_t c = cnt[i];
-    if (c == 0) return;
-    // a system's nodes are the pre-order block starting at its root (pre-order index of its
-    // first star's chain); its reference layout fills the same block
-    const uint32_t root = base[sys_range(sid_sorted, geo, i, n).lo];
-    uint32_t p = base[i];
-    for (uint32_t t = 0; t < c; ++t, ++p) {
-        int32_t pp = pre_parent[p];
+                                                        const SysGeo *__restrict__ geo, int64_t cap_nodes) {
+    const int64_t n = info->nstars, nn = info->nnodes < cap_nodes ? info->nnodes : cap_nodes;
+    if (blockIdx.x == 0 && threadIdx.x == 0 && info->nnodes > cap_nodes) dev_error(info, 11);
+    for (int64_t p = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; p < nn; p += int64_t(gridDim.x) * blockDim.x) {
+        const int64_t i = pre_star[p];
+        if (i < 0 || i >= n) {
+            dev_error(info, 11);
+            continue;
+        }
+        // a system's nodes are the pre-order block starting at its root (pre-order index of its
+        // first star's chain); its reference layout fills the same block
+        const uint32_t root = base[sys_range(sid_sorted, geo, i, n).lo];
+        const int32_t pp = pre_parent[p];
         if (pp < 0) {
             pre_ref[p] = int32_t(root);
             continue;
         }
-        uint32_t oct = (pre_info[p] >> 8) & 0xffu;
-        uint32_t pmask = pre_mask[pp];
+        const uint32_t oct = (pre_info[p] >> 8) & 0xffu;
+        const uint32_t pmask = pre_mask[pp];
         pre_ref[p] = int32_t(root + 1 + (child_base[pp] - child_base[root]) + __popc(pmask & ((1u << oct) - 1u)));
     }
 }
 
-// Links and ranges of every node in the reference layout (bh.go:59-67).
+// Links and ranges of every node in the reference layout (bh.go:59-67). One thread per node: the
+// search for the end of its cell runs beside the other nodes' searches, not after those of the
+// shallower nodes of its chain.
 __global__ __launch_bounds__(kThreads) void k_emit_nodes(const uint64_t *__restrict__ keys, DevInfo *info,
                                                          const uint32_t *__restrict__ cnt,
                                                          const uint32_t *__restrict__ base,
+                                                         const int32_t *__restrict__ pre_star,
                                                          const int32_t *__restrict__ pre_parent,
                                                          const uint32_t *__restrict__ pre_info,
                                                          const uint32_t *__restrict__ pre_mask,
@@ -1005,26 +1018,21 @@ __global__ __launch_bounds__(kThreads) void k_emit_nodes(const uint64_t *__restr
                                                          int32_t *__restrict__ n_parent, uint32_t *__restrict__ n_info,
                                                          int32_t *__restrict__ n_arrive,
                                                          const int32_t *__restrict__ sid_sorted,
-                                                         const SysGeo *__restrict__ geo) {
-    int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-    int64_t n = info->nstars;
-    if (i >= n) return;
-    const int64_t nn = info->nnodes;
-    uint32_t c = cnt[i];
-    if (c == 0) return;
-    const SysRange R = sys_range(sid_sorted, geo, i, n);
-    const uint32_t root = base[R.lo];
-    uint32_t p = base[i];
-    for (uint32_t t = 0; t < c; ++t, ++p) {
-        uint32_t inf = pre_info[p];
-        int L = int(inf & 0xffu);
-        uint32_t mask = pre_mask[p];
-        int64_t hi = cell_end(keys, R.hi, i, L);
-        int32_t r = pre_ref[p];
-        if (r < 0 || r >= nn) {
+                                                         const SysGeo *__restrict__ geo, int64_t cap_nodes) {
+    const int64_t n = info->nstars, nn = info->nnodes < cap_nodes ? info->nnodes : cap_nodes;
+    for (int64_t p = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; p < nn; p += int64_t(gridDim.x) * blockDim.x) {
+        const int64_t i = pre_star[p];
+        const int32_t r = pre_ref[p];
+        if (i < 0 || i >= n || r < 0 || r >= nn) {
             dev_error(info, 11);
             continue;
         }
+        const SysRange R = sys_range(sid_sorted, geo, i, n);
+        const uint32_t root = base[R.lo];
+        const uint32_t inf = pre_info[p];
+        const int L = int(inf & 0xffu);
+        const uint32_t mask = pre_mask[p];
+        const int64_t hi = cell_end(keys, R.hi, i, L);
         gbh_node &nd = nodes[r];
         nd.first = mask ? int32_t(root + 1 + (child_base[p] - child_base[root])) : -1;
         int32_t nx = hi == R.hi ? -1 : pre_ref[base[hi]];  // a system's walk ends at its own last node
@@ -1035,7 +1043,7 @@ __global__ __launch_bounds__(kThreads) void k_emit_nodes(const uint64_t *__restr
         nd.next = nx;
         nd.lo = int32_t(i);
         nd.hi = int32_t(hi);
-        int32_t pp = pre_parent[p];
+        const int32_t pp = pre_parent[p];
         n_parent[r] = pp < 0 ? -1 : pre_ref[pp];
         n_info[r] = uint32_t(L) | uint32_t(__popc(mask)) << 8;
         n_arrive[r] = 0;
@@ -1727,7 +1735,7 @@ static cudaError_t scan_dyn(const Launch &L, const uint32_t *in, uint32_t *out, 
 
 void tree_free(TreeBufs &b) {
     void *ptrs[] = {b.flag, b.pos4, b.bbox_part, b.keys, b.keys_alt, b.order, b.order_alt, b.hist, b.os_state, b.hs_state, b.sx, b.sy, b.sz, b.sm,
-                    b.st_hi, b.st_lo, b.st_off, b.chain_cnt, b.leaves, b.targets, b.geo, b.sid_sorted, b.groups, b.gcost, b.gperm, b.pre_parent, b.pre_info, b.pre_nchild, b.pre_mask, b.pre_ref, b.nodes,
+                    b.st_hi, b.st_lo, b.st_off, b.chain_cnt, b.leaves, b.targets, b.geo, b.sid_sorted, b.groups, b.gcost, b.gperm, b.pre_parent, b.pre_info, b.pre_nchild, b.pre_mask, b.pre_ref, b.pre_star, b.nodes,
                     b.n_parent, b.n_info, b.n_arrive, b.pnodes, b.mnodes, b.mrange, b.lnode, b.walk_ctr, b.scan_tmp, b.info, b.part_acc};
     for (void *p : ptrs)
         if (p) cudaFree(p);
@@ -1793,6 +1801,7 @@ cudaError_t tree_alloc(TreeBufs &b, int64_t n, int leaf, int32_t nsys) {
     GBH_ALLOC(b.pre_nchild, cnodes);
     GBH_ALLOC(b.pre_mask, cnodes);
     GBH_ALLOC(b.pre_ref, cnodes);
+    GBH_ALLOC(b.pre_star, cnodes);
     GBH_ALLOC(b.nodes, cnodes);
     GBH_ALLOC(b.n_parent, cnodes);
     GBH_ALLOC(b.n_info, cnodes);
@@ -2006,16 +2015,18 @@ cudaError_t tree_build(const Launch &L, TreeBufs &b, int64_t n, const double *px
     if (e == cudaSuccess) e = cudaMemsetAsync(b.pre_nchild, 0, sizeof(uint32_t) * size_t(b.cap_nodes), s);
     if (e != cudaSuccess) return e;
     k_chain_emit<<<nb, kThreads, 0, s>>>(b.keys, b.info, cnt, base, b.pre_parent, b.pre_info, b.pre_nchild, b.pre_mask,
-                                         b.leaves, sid, b.geo);
+                                         b.pre_star, b.leaves, sid, b.geo);
     GBH_LAUNCH_CHECK();
     e = os ? scan_lb(L, b, 2, b.pre_nchild, b.pre_nchild, b.cap_nodes, &b.info->nnodes)
            : scan_big(L, b, 2, b.pre_nchild, b.pre_nchild, b.cap_nodes, &b.info->nnodes);
     if (e != cudaSuccess) return e;
-    k_ref_index<<<nb, kThreads, 0, s>>>(b.info, cnt, base, b.pre_parent, b.pre_info, b.pre_mask, b.pre_nchild,
-                                        b.pre_ref, sid, b.geo);
+    const unsigned nbn = node_blocks(b.cap_nodes);
+    k_ref_index<<<nbn, kThreads, 0, s>>>(b.info, base, b.pre_star, b.pre_parent, b.pre_info, b.pre_mask, b.pre_nchild,
+                                         b.pre_ref, sid, b.geo, b.cap_nodes);
     GBH_LAUNCH_CHECK();
-    k_emit_nodes<<<nb, kThreads, 0, s>>>(b.keys, b.info, cnt, base, b.pre_parent, b.pre_info, b.pre_mask, b.pre_nchild,
-                                         b.pre_ref, b.nodes, b.n_parent, b.n_info, b.n_arrive, sid, b.geo);
+    k_emit_nodes<<<nbn, kThreads, 0, s>>>(b.keys, b.info, cnt, base, b.pre_star, b.pre_parent, b.pre_info, b.pre_mask,
+                                          b.pre_nchild, b.pre_ref, b.nodes, b.n_parent, b.n_info, b.n_arrive, sid,
+                                          b.geo, b.cap_nodes);
     GBH_LAUNCH_CHECK();
     if (forest) {
         k_sys_layout<<<1, 32, 0, s>>>(b.nsys, b.group == 32 ? 32 : 64, base, b.geo, b.info);
