@@ -619,11 +619,6 @@ constexpr int kOsScans = 3;                                         // flags, ch
 __host__ __device__ inline int64_t os_scan_tiles(int64_t n) { return (n + kScanTile - 1) / kScanTile; }
 __host__ __device__ inline int64_t os_sort_tiles(int64_t n) { return (n + kRsTile - 1) / kRsTile; }
 
-template <bool kSid>
-__device__ __forceinline__ uint32_t os_digit(uint64_t k, int32_t v, const uint16_t *__restrict__ sys_of, int shift) {
-    return (kSid ? uint32_t(sys_of[v] >> shift) : uint32_t(k >> shift)) & (kRsBins - 1);
-}
-
 // Every pass's digit histogram in one read of the keys (warp-aggregated shared counters, then one
 // global add per non-zero bin and block).
 template <bool kSid>
@@ -656,6 +651,52 @@ __global__ __launch_bounds__(kRsThreads) void k_os_hist(const uint64_t *__restri
         if (h[i]) atomicAdd(&ghist[i], h[i]);
 }
 
+// Ranks a tile's keys by digit, stably, for the one-sweep pass. Warp w holds the tile's keys
+// [w, w + 1) x kRsItems x 32 (item it of lane l: position w kRsItems 32 + it 32 + l), so the
+// order (warp, item, lane) is the input order. Each warp counts its own keys per digit in
+// s_w[w][digit] (the lowest lane of each group of equal digits reads and advances the counter;
+// no block barrier inside the loop), so a key's rank among its warp's earlier keys of the same
+// digit is the counter before its group plus its place in the group. On return s_w holds the
+// warp counts (the caller turns them into offsets after a barrier). Measured against the
+// round-barrier ranking of k_rs_scatter: the one-sweep builds 2-4 % faster (16k-262k bodies);
+// in k_rs_scatter it made the 1M and 4M builds 3-5 % slower, so that kernel keeps its own.
+template <bool kSid>
+__device__ __forceinline__ void rank_tile(const uint64_t *__restrict__ kin, const int32_t *__restrict__ vin,
+                                          const uint16_t *__restrict__ sys_of, int shift, int64_t base, int64_t n,
+                                          uint32_t (&s_w)[kRsWarps][kRsBins], uint64_t (&k)[kRsItems],
+                                          int32_t (&v)[kRsItems], uint32_t (&dig)[kRsItems],
+                                          uint32_t (&rk)[kRsItems]) {
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+#pragma unroll
+    for (int w = 0; w < kRsWarps; ++w) s_w[w][tid] = 0;
+    const int64_t wbase = base + int64_t(warp) * (kRsItems * 32);
+#pragma unroll
+    for (int it = 0; it < kRsItems; ++it) {
+        const int64_t idx = wbase + it * 32 + lane;
+        if (idx < n) {
+            k[it] = kin[idx];
+            v[it] = vin[idx];
+        }
+    }
+    __syncthreads();  // counters cleared
+    const uint32_t lt = (1u << lane) - 1u;
+#pragma unroll
+    for (int it = 0; it < kRsItems; ++it) {
+        const bool valid = wbase + it * 32 + lane < n;
+        uint32_t d = 0u;
+        if (valid) d = (kSid ? uint32_t(sys_of[v[it]] >> shift) : uint32_t(k[it] >> shift)) & (kRsBins - 1);
+        const uint32_t peers = __match_any_sync(0xffffffffu, valid ? d : uint32_t(kRsBins + lane));
+        const int leader = __ffs(peers) - 1;
+        uint32_t old = 0;
+        if (valid && lane == leader) old = s_w[warp][d];
+        old = __shfl_sync(0xffffffffu, old, leader);
+        rk[it] = old + __popc(peers & lt);
+        dig[it] = d;
+        if (valid && lane == leader) s_w[warp][d] = old + __popc(peers);
+        __syncwarp();
+    }
+}
+
 // One stable pass over the tile the block takes. status: [tile][digit] words of this pass.
 template <bool kSid>
 __global__ __launch_bounds__(kRsThreads) void k_os_pass(const uint64_t *__restrict__ kin,
@@ -663,20 +704,13 @@ __global__ __launch_bounds__(kRsThreads) void k_os_pass(const uint64_t *__restri
                                                         int32_t *__restrict__ vout, const uint16_t *__restrict__ sys_of,
                                                         DevInfo *info, int shift, const uint32_t *__restrict__ ghist,
                                                         uint32_t *ctr, uint32_t *status) {
-    __shared__ uint32_t s_run[kRsBins];
     __shared__ uint32_t s_goff[kRsBins];
-    __shared__ uint32_t s_w[2][kRsWarps][kRsBins];
+    __shared__ uint32_t s_w[kRsWarps][kRsBins];
     __shared__ uint32_t s_warp[kScanThreads / 32 + 1];
     __shared__ uint32_t s_tile;
     static_assert(kRsThreads == kScanThreads && kRsThreads == kRsBins, "one thread per digit");
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     if (tid == 0) s_tile = atomicAdd(ctr, 1u);
-    s_run[tid] = 0;
-#pragma unroll
-    for (int w = 0; w < kRsWarps; ++w) {
-        s_w[0][w][tid] = 0;
-        s_w[1][w][tid] = 0;
-    }
     // where each digit starts in the output: exclusive scan of the pass's histogram
     uint32_t total;
     const uint32_t gstart = block_excl_scan(ghist[tid], s_warp, total);  // its barriers publish s_tile too
@@ -686,41 +720,20 @@ __global__ __launch_bounds__(kRsThreads) void k_os_pass(const uint64_t *__restri
     if (base >= n) return;  // uniform over the block
     uint64_t k[kRsItems];
     int32_t v[kRsItems];
-    uint32_t loc[kRsItems];
+    uint32_t dig[kRsItems], rk[kRsItems];
+    rank_tile<kSid>(kin, vin, sys_of, shift, base, n, s_w, k, v, dig, rk);
+    __syncthreads();
+    // digit tid: each warp's start inside the tile, and the tile's count
+    uint32_t run = 0;
 #pragma unroll
-    for (int it = 0; it < kRsItems; ++it) {
-        const int64_t idx = base + it * kRsThreads + tid;
-        if (idx < n) {
-            k[it] = kin[idx];
-            v[it] = vin[idx];
-        }
+    for (int w = 0; w < kRsWarps; ++w) {
+        const uint32_t c = s_w[w][tid];
+        s_w[w][tid] = run;
+        run += c;
     }
-    // rank within the tile in (item round, warp, lane) order, as k_rs_scatter
-    const uint32_t lt = (1u << lane) - 1u;
-#pragma unroll
-    for (int it = 0; it < kRsItems; ++it) {
-        const int buf = it & 1;
-        const bool valid = base + it * kRsThreads + tid < n;
-        const uint32_t d = valid ? os_digit<kSid>(k[it], v[it], sys_of, shift) : 0u;
-        const uint32_t peers = __match_any_sync(0xffffffffu, valid ? d : uint32_t(kRsBins + lane));
-        const uint32_t rank = __popc(peers & lt);
-        if (valid && rank == 0) s_w[buf][warp][d] = __popc(peers);
-        __syncthreads();
-        uint32_t run = s_run[tid];
-#pragma unroll
-        for (int w = 0; w < kRsWarps; ++w) {
-            const uint32_t c = s_w[buf][w][tid];
-            s_w[buf][w][tid] = run;
-            run += c;
-            s_w[buf ^ 1][w][tid] = 0;
-        }
-        s_run[tid] = run;
-        __syncthreads();
-        loc[it] = valid ? s_w[buf][warp][d] + rank : 0u;
-    }
-    // look-back for digit tid: this tile's count is s_run[tid]. Predecessors' words are read
-    // kOsWindow at a time (independent loads), then taken in order back to the first prefix.
-    const uint32_t agg = s_run[tid];
+    // look-back for digit tid: this tile's count is run. Predecessors' words are read kOsWindow
+    // at a time (independent loads), then taken in order back to the first prefix.
+    const uint32_t agg = run;
     uint32_t *mine = status + size_t(tile) * kRsBins + tid;
     uint32_t excl = 0;
     if (tile == 0) {
@@ -756,12 +769,11 @@ __global__ __launch_bounds__(kRsThreads) void k_os_pass(const uint64_t *__restri
     }
     s_goff[tid] = gstart + excl;
     __syncthreads();
+    const int64_t wbase = base + int64_t(warp) * (kRsItems * 32);
 #pragma unroll
     for (int it = 0; it < kRsItems; ++it) {
-        const int64_t idx = base + it * kRsThreads + tid;
-        if (idx < n) {
-            const uint32_t d = os_digit<kSid>(k[it], v[it], sys_of, shift);
-            const uint32_t pos = s_goff[d] + loc[it];
+        if (wbase + it * 32 + lane < n) {
+            const uint32_t pos = s_goff[dig[it]] + s_w[warp][dig[it]] + rk[it];
             if (pos < n) {
                 kout[pos] = k[it];
                 vout[pos] = v[it];
