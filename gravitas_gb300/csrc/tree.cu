@@ -617,7 +617,16 @@ constexpr int64_t kOsCtrWords = 32;                                 // tile coun
 constexpr int kOsScanCtr = kOsPassesMax;                            // first scan counter
 constexpr int kOsScans = 3;                                         // flags, chain counts, child counts
 __host__ __device__ inline int64_t os_scan_tiles(int64_t n) { return (n + kScanTile - 1) / kScanTile; }
-__host__ __device__ inline int64_t os_sort_tiles(int64_t n) { return (n + kRsTile - 1) / kRsTile; }
+// Keys a thread of a one-sweep pass ranks: the fewest of 4, 8, 12 that keep a state of `cap`
+// bodies within 96 tiles (measured: more tiles spread a small sort over more SMs, fewer tiles
+// shorten the look-back; against 8 keys a thread, 4 made the 16k build 6 % faster and 12 the
+// 262k build 4 % faster).
+inline int os_items(int64_t cap) { return cap <= 96 * 4 * kRsThreads ? 4 : cap <= 96 * 8 * kRsThreads ? 8 : 12; }
+inline int64_t os_sort_tiles(int64_t n, int items) {
+    const int64_t tile = int64_t(items) * kRsThreads;
+    return (n + tile - 1) / tile;
+}
+inline int64_t rs_sort_tiles(int64_t n) { return (n + kRsTile - 1) / kRsTile; }
 
 // Every pass's digit histogram in one read of the keys (warp-aggregated shared counters, then one
 // global add per non-zero bin and block).
@@ -652,7 +661,7 @@ __global__ __launch_bounds__(kRsThreads) void k_os_hist(const uint64_t *__restri
 }
 
 // Ranks a tile's keys by digit, stably, for the one-sweep pass. Warp w holds the tile's keys
-// [w, w + 1) x kRsItems x 32 (item it of lane l: position w kRsItems 32 + it 32 + l), so the
+// [w, w + 1) x kItems x 32 (item it of lane l: position w kItems 32 + it 32 + l), so the
 // order (warp, item, lane) is the input order. Each warp counts its own keys per digit in
 // s_w[w][digit] (the lowest lane of each group of equal digits reads and advances the counter;
 // no block barrier inside the loop), so a key's rank among its warp's earlier keys of the same
@@ -660,18 +669,17 @@ __global__ __launch_bounds__(kRsThreads) void k_os_hist(const uint64_t *__restri
 // warp counts (the caller turns them into offsets after a barrier). Measured against the
 // round-barrier ranking of k_rs_scatter: the one-sweep builds 2-4 % faster (16k-262k bodies);
 // in k_rs_scatter it made the 1M and 4M builds 3-5 % slower, so that kernel keeps its own.
-template <bool kSid>
+template <bool kSid, int kItems>
 __device__ __forceinline__ void rank_tile(const uint64_t *__restrict__ kin, const int32_t *__restrict__ vin,
                                           const uint16_t *__restrict__ sys_of, int shift, int64_t base, int64_t n,
-                                          uint32_t (&s_w)[kRsWarps][kRsBins], uint64_t (&k)[kRsItems],
-                                          int32_t (&v)[kRsItems], uint32_t (&dig)[kRsItems],
-                                          uint32_t (&rk)[kRsItems]) {
+                                          uint32_t (&s_w)[kRsWarps][kRsBins], uint64_t (&k)[kItems],
+                                          int32_t (&v)[kItems], uint32_t (&dig)[kItems], uint32_t (&rk)[kItems]) {
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
 #pragma unroll
     for (int w = 0; w < kRsWarps; ++w) s_w[w][tid] = 0;
-    const int64_t wbase = base + int64_t(warp) * (kRsItems * 32);
+    const int64_t wbase = base + int64_t(warp) * (kItems * 32);
 #pragma unroll
-    for (int it = 0; it < kRsItems; ++it) {
+    for (int it = 0; it < kItems; ++it) {
         const int64_t idx = wbase + it * 32 + lane;
         if (idx < n) {
             k[it] = kin[idx];
@@ -681,7 +689,7 @@ __device__ __forceinline__ void rank_tile(const uint64_t *__restrict__ kin, cons
     __syncthreads();  // counters cleared
     const uint32_t lt = (1u << lane) - 1u;
 #pragma unroll
-    for (int it = 0; it < kRsItems; ++it) {
+    for (int it = 0; it < kItems; ++it) {
         const bool valid = wbase + it * 32 + lane < n;
         uint32_t d = 0u;
         if (valid) d = (kSid ? uint32_t(sys_of[v[it]] >> shift) : uint32_t(k[it] >> shift)) & (kRsBins - 1);
@@ -698,7 +706,7 @@ __device__ __forceinline__ void rank_tile(const uint64_t *__restrict__ kin, cons
 }
 
 // One stable pass over the tile the block takes. status: [tile][digit] words of this pass.
-template <bool kSid>
+template <bool kSid, int kItems>
 __global__ __launch_bounds__(kRsThreads) void k_os_pass(const uint64_t *__restrict__ kin,
                                                         const int32_t *__restrict__ vin, uint64_t *__restrict__ kout,
                                                         int32_t *__restrict__ vout, const uint16_t *__restrict__ sys_of,
@@ -716,12 +724,12 @@ __global__ __launch_bounds__(kRsThreads) void k_os_pass(const uint64_t *__restri
     const uint32_t gstart = block_excl_scan(ghist[tid], s_warp, total);  // its barriers publish s_tile too
     const uint32_t tile = s_tile;
     const int64_t n = info->nstars;
-    const int64_t base = int64_t(tile) * kRsTile;
+    const int64_t base = int64_t(tile) * (kItems * kRsThreads);
     if (base >= n) return;  // uniform over the block
-    uint64_t k[kRsItems];
-    int32_t v[kRsItems];
-    uint32_t dig[kRsItems], rk[kRsItems];
-    rank_tile<kSid>(kin, vin, sys_of, shift, base, n, s_w, k, v, dig, rk);
+    uint64_t k[kItems];
+    int32_t v[kItems];
+    uint32_t dig[kItems], rk[kItems];
+    rank_tile<kSid, kItems>(kin, vin, sys_of, shift, base, n, s_w, k, v, dig, rk);
     __syncthreads();
     // digit tid: each warp's start inside the tile, and the tile's count
     uint32_t run = 0;
@@ -769,9 +777,9 @@ __global__ __launch_bounds__(kRsThreads) void k_os_pass(const uint64_t *__restri
     }
     s_goff[tid] = gstart + excl;
     __syncthreads();
-    const int64_t wbase = base + int64_t(warp) * (kRsItems * 32);
+    const int64_t wbase = base + int64_t(warp) * (kItems * 32);
 #pragma unroll
-    for (int it = 0; it < kRsItems; ++it) {
+    for (int it = 0; it < kItems; ++it) {
         if (wbase + it * 32 + lane < n) {
             const uint32_t pos = s_goff[dig[it]] + s_w[warp][dig[it]] + rk[it];
             if (pos < n) {
@@ -1833,7 +1841,8 @@ cudaError_t tree_alloc(TreeBufs &b, int64_t n, int leaf, int32_t nsys) {
     int64_t os_words = 0;
     if (cn <= kOsMaxN) {  // node capacity stays below 2^30 too (at most 12 nodes a body)
         const int64_t stiles = os_scan_tiles(cn > cnodes ? cn : cnodes);
-        os_words = kOsHistWords + kOsCtrWords + 2 * kOsScans * stiles + kOsPassesMax * os_sort_tiles(cn) * kRsBins;
+        os_words = kOsHistWords + kOsCtrWords + 2 * kOsScans * stiles +
+                   kOsPassesMax * os_sort_tiles(cn, os_items(cn)) * kRsBins;
         GBH_ALLOC(b.os_state, os_words);
     }
     GBH_ALLOC(b.info, 1);
@@ -1892,7 +1901,7 @@ static cudaError_t scan_hs(const Launch &L, TreeBufs &b, uint32_t *base, const u
     ++*L.count;
     return cudaGetLastError();
 }
-static int64_t hs_pass_words(const TreeBufs &b) { return 2 + 2 * os_scan_tiles(os_sort_tiles(b.cap_n) * kRsBins); }
+static int64_t hs_pass_words(const TreeBufs &b) { return 2 + 2 * os_scan_tiles(rs_sort_tiles(b.cap_n) * kRsBins); }
 static cudaError_t scan_hist(const Launch &L, TreeBufs &b, int p, uint32_t ntiles) {
     return scan_hs(L, b, b.hs_state + int64_t(p) * hs_pass_words(b), b.hist, b.hist, int64_t(ntiles) * kRsBins,
                    nullptr);
@@ -1917,8 +1926,10 @@ cudaError_t tree_build(const Launch &L, TreeBufs &b, int64_t n, const double *px
     // counters and the look-back words of the passes this build runs start at zero
     const bool os = b.os_state != nullptr;
     const int npass = forest ? kOsPassesMax : 8;
+    const int os_k = os_items(cap);  // keys a thread of a one-sweep pass ranks
+    const int64_t os_tiles = os_sort_tiles(cap, os_k);
     if (os) {
-        const int64_t words = os_sort_base(b) + int64_t(npass) * os_sort_tiles(cap) * kRsBins;
+        const int64_t words = os_sort_base(b) + int64_t(npass) * os_tiles * kRsBins;
         if ((e = cudaMemsetAsync(b.os_state, 0, sizeof(uint32_t) * size_t(words), s)) != cudaSuccess) return e;
     } else if ((e = cudaMemsetAsync(b.hs_state, 0, sizeof(uint32_t) * size_t(b.hs_words), s)) != cudaSuccess) {
         return e;
@@ -1966,13 +1977,20 @@ cudaError_t tree_build(const Launch &L, TreeBufs &b, int64_t n, const double *px
         else k_os_hist<false><<<hb, kRsThreads, 0, s>>>(kin, vin, nullptr, b.info, ghist);
         GBH_LAUNCH_CHECK();
         for (int p = 0; p < npass; ++p) {
-            uint32_t *st = b.os_state + os_sort_base(b) + int64_t(p) * ntiles * kRsBins;
-            if (p < 8)
-                k_os_pass<false><<<ntiles, kRsThreads, 0, s>>>(kin, vin, kout, vout, nullptr, b.info, 8 * p,
-                                                               ghist + p * kRsBins, ctr + p, st);
-            else
-                k_os_pass<true><<<ntiles, kRsThreads, 0, s>>>(kin, vin, kout, vout, sys_of, b.info, 8 * (p - 8),
-                                                              ghist + p * kRsBins, ctr + p, st);
+            uint32_t *st = b.os_state + os_sort_base(b) + int64_t(p) * os_tiles * kRsBins;
+            const uint16_t *so = p < 8 ? nullptr : sys_of;
+            const int shift = p < 8 ? 8 * p : 8 * (p - 8);
+            const unsigned g = unsigned(os_tiles);
+            const uint32_t *gh = ghist + p * kRsBins;
+            if (p < 8) {
+                if (os_k == 4) k_os_pass<false, 4><<<g, kRsThreads, 0, s>>>(kin, vin, kout, vout, so, b.info, shift, gh, ctr + p, st);
+                else if (os_k == 8) k_os_pass<false, 8><<<g, kRsThreads, 0, s>>>(kin, vin, kout, vout, so, b.info, shift, gh, ctr + p, st);
+                else k_os_pass<false, 12><<<g, kRsThreads, 0, s>>>(kin, vin, kout, vout, so, b.info, shift, gh, ctr + p, st);
+            } else {
+                if (os_k == 4) k_os_pass<true, 4><<<g, kRsThreads, 0, s>>>(kin, vin, kout, vout, so, b.info, shift, gh, ctr + p, st);
+                else if (os_k == 8) k_os_pass<true, 8><<<g, kRsThreads, 0, s>>>(kin, vin, kout, vout, so, b.info, shift, gh, ctr + p, st);
+                else k_os_pass<true, 12><<<g, kRsThreads, 0, s>>>(kin, vin, kout, vout, so, b.info, shift, gh, ctr + p, st);
+            }
             GBH_LAUNCH_CHECK();
             uint64_t *tk = kin;
             kin = kout;
