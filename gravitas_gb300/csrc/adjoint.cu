@@ -412,6 +412,7 @@ cudaError_t tree_at(const Launch &L, AdjTape &t, const double *x, const double *
     b.group = 32;
     b.list_depth = 0;
     b.lpt = true;
+    b.split = true;  // few groups: the forward walk shares each among several warps (the same lists)
     return tree_build(L, b, t.n, x, y, z, t.m, nullptr, nullptr, ax, ay, az, t.theta, t.leaf, 0, false, false,
                       nullptr, nullptr);
 }
@@ -425,7 +426,7 @@ cudaError_t force(const Launch &L, AdjTape &t, const double *x, const double *y,
     if (t.tree) {
         if ((e = tree_at(L, t, x, y, z, ax, ay, az))) return e;
         if ((e = mark(t))) return e;
-        if ((e = walk_lists(L, *t.tb, float(t.eps2), 1, ax, ay, az, 0, false, 1))) return e;
+        if ((e = walk_lists(L, *t.tb, t.n, float(t.eps2), 1, ax, ay, az, 0, false, 1))) return e;
         return mark(t);
     }
     if (!t.fp32) {

@@ -217,6 +217,10 @@ constexpr int kMaxWalkParts = 32;
 int walk_parts(int64_t n, int gsize);
 // The most parts a walk sized for n bodies may take (its part_acc budget; 1: never split).
 int walk_parts_budget(int64_t n);
+// Parts of a split walk (1: none) and the sum of its parts to state order (walk.cu).
+int split_parts(const TreeBufs &b, int64_t nstars_cap, bool targets, int gsize);
+cudaError_t split_combine(const Launch &L, const TreeBufs &b, int nparts, int64_t stride, bool targets, double *ax,
+                          double *ay, double *az);
 // Grows part_acc for a split walk over the n bodies of a call (no allocation when it already
 // fits). The parts depend on n alone, never on the buffers' capacity, so the same inputs give
 // the same bits in any context.
@@ -378,9 +382,11 @@ constexpr int kDefaultListDepth = 56;
 int list_depth_max(bool exact);
 // Every star, or (targets = true) the stars listed in b.targets, in groups of 32 x stars_per_lane
 // (1 or 2) stars; a forest's build must have made groups of that size (b.group). Persistent
-// warps; needs b.cap_nodes < 2^29.
-cudaError_t walk_lists(const Launch &L, const TreeBufs &b, float eps2, int quad, double *ax, double *ay, double *az,
-                       int list_depth, bool targets, int stars_per_lane);
+// warps; needs b.cap_nodes < 2^29. With few groups for the GPU (b.split, split_parts) each group's
+// walk is shared among several warps; nstars_cap (>= the body count) is then the stride of the
+// part accumulators.
+cudaError_t walk_lists(const Launch &L, const TreeBufs &b, int64_t nstars_cap, float eps2, int quad, double *ax,
+                       double *ay, double *az, int list_depth, bool targets, int stars_per_lane);
 // The transposed Jacobian of the list walk's force (32-star groups, quadrupoles, softening > 0)
 // with the lists of the tree in b frozen: for weights w (state order) writes, in state order,
 // (J^T w)_i and (da/dm)^T w_i into out (x, y, z and m terms, n apart). px .. mass: the state the

@@ -560,15 +560,29 @@ cudaError_t lpt_order(const Launch &L, const TreeBufs &b, int gsize) {
     return cudaGetLastError();
 }
 
-// Whether a walk of 64-star groups shares each group among several warps (the paired walk's split
-// mode, for single systems with few groups per SM): the same decision as launch_mixed_t's.
-static bool paired_split(const TreeBufs &b, int64_t nstars_cap, bool targets) {
-    if (b.nsys > 1 || !b.split || !b.part_acc) return false;
+// Parts of a split walk of groups of gsize stars (1: no split), for single systems with few groups
+// per SM: by the stars the walk takes (a target list: the previous event's count), within the
+// budget of nstars_cap bodies and the part accumulators. The same decision as launch_mixed_t's.
+int split_parts(const TreeBufs &b, int64_t nstars_cap, bool targets, int gsize) {
+    if (b.nsys > 1 || !b.split || !b.part_acc) return 1;
     const int64_t walked = targets && b.walk_hint > 0 && b.walk_hint < nstars_cap ? b.walk_hint : nstars_cap;
-    int parts = walk_parts(walked, 64);
+    int parts = walk_parts(walked, gsize);
     const int budget = walk_parts_budget(nstars_cap);
     if (parts > budget) parts = budget;
-    return parts > 1 && int64_t(parts) * 3 * nstars_cap <= b.part_cap;
+    return parts > 1 && int64_t(parts) * 3 * nstars_cap <= b.part_cap ? parts : 1;
+}
+
+cudaError_t split_combine(const Launch &L, const TreeBufs &b, int nparts, int64_t stride, bool targets, double *ax,
+                          double *ay, double *az) {
+    k_split_combine<<<blocks_for(stride, 256), 256, 0, L.stream>>>(b.info, b.order, targets ? b.targets : nullptr,
+                                                                    nparts, b.part_acc, stride, ax, ay, az);
+    ++*L.count;
+    return cudaGetLastError();
+}
+
+// Whether a walk of 64-star groups takes the paired walk's split mode.
+static bool paired_split(const TreeBufs &b, int64_t nstars_cap, bool targets) {
+    return split_parts(b, nstars_cap, targets, 64) > 1;
 }
 
 cudaError_t walk_mixed(const Launch &L, const TreeBufs &b, int64_t nstars_cap, float eps2, int quad, double *ax,
@@ -576,9 +590,9 @@ cudaError_t walk_mixed(const Launch &L, const TreeBufs &b, int64_t nstars_cap, f
     // The list walk (walk_lists.cu) in groups of 32 (one star a lane) or 64 (two); the paired walk
     // above for 64-star groups of a system small enough for its split mode (or with b.paired)
     if (b.cap_nodes < (int64_t(1) << 29)) {
-        if (b.group == 32) return walk_lists(L, b, eps2, quad, ax, ay, az, b.list_depth, targets, 1);
+        if (b.group == 32) return walk_lists(L, b, nstars_cap, eps2, quad, ax, ay, az, b.list_depth, targets, 1);
         if (!b.paired && !paired_split(b, nstars_cap, targets))
-            return walk_lists(L, b, eps2, quad, ax, ay, az, b.list_depth, targets, 2);
+            return walk_lists(L, b, nstars_cap, eps2, quad, ax, ay, az, b.list_depth, targets, 2);
     }
     bool soft = eps2 > 0.f;
     if (quad && soft) return launch_mixed<true, true>(L, b, nstars_cap, eps2, ax, ay, az, targets);

@@ -270,14 +270,20 @@ struct InPlace {
     }
 };
 
-// Walks one group with the given separation form; a is zeroed by the caller.
-template <bool kExact, bool kQuad, bool kSoft, int kS, class Sink, class AccT>
+// Walks one group with the given separation form; a is zeroed by the caller. kSplit: this warp is
+// one part of the group's walk, owning the source stars [s_lo, s_hi) (ranges: each node's star
+// range): it skips nodes with no star in its range, tests every other node as the whole walk
+// would (so all parts agree on every node), adds an accepted node only when the node's first star
+// is its own, and an opened leaf's stars only within its range.
+template <bool kExact, bool kQuad, bool kSoft, int kS, bool kSplit = false, class Sink, class AccT>
 __device__ __forceinline__ GroupOut walk_group(TravMem &W, Sink &sink, int lane, int32_t root, const Target (&t)[kS], float Ox,
                                                float Oy, float Oz, float bx0, float by0, float bz0, float bx1,
                                                float by1, float bz1, float ext, float eps2, int node_depth,
                                                int src_depth, const LNode *__restrict__ nodes,
                                                const float4 *__restrict__ st_hi, const float4 *__restrict__ st_lo,
-                                               int32_t nn, int32_t ns, DevInfo *err_info, AccT (&a)[kS]) {
+                                               int32_t nn, int32_t ns, DevInfo *err_info, AccT (&a)[kS],
+                                               const int2 *__restrict__ ranges = nullptr, int32_t s_lo = 0,
+                                               int32_t s_hi = 0) {
     using Lay = Layout<kExact>;
     constexpr int kNodeFields = kExact ? 13 : 10;
     constexpr int kSrcFields = kExact ? 7 : 4;
@@ -333,10 +339,17 @@ __device__ __forceinline__ GroupOut walk_group(TravMem &W, Sink &sink, int lane,
         const int qexcl = __shfl_sync(kFull, incl - c, q);
         sp -= r;
         const int depth = dtop;
-        const int32_t node = lane < total ? qfirst + (lane - qexcl) : -1;
+        int32_t node = lane < total ? qfirst + (lane - qexcl) : -1;
         tested += uint32_t(total);
         // ---- test: the group's box, then (all lanes at once) every star for what the box keeps
-        bool acc = false, bad = node >= nn;
+        bool acc = false, bad = node >= nn, own = true;
+        if constexpr (kSplit) {
+            if (node >= 0 && !bad) {
+                const int2 rg = ranges[node];
+                if (rg.x >= s_hi || rg.y <= s_lo) node = -1;  // no star of this part below it
+                else own = rg.x >= s_lo;
+            }
+        }
         float4 na = make_float4(0.f, 0.f, 0.f, 0.f), nb = na, nc = na, nd = na;
         float cx = 0.f, cy = 0.f, cz = 0.f, lim = 0.f;
         if (node >= 0 && !bad) {
@@ -423,10 +436,11 @@ __device__ __forceinline__ GroupOut walk_group(TravMem &W, Sink &sink, int lane,
         if (!npush) {
             while (dtop > 0 && W.lvl[dtop] >= sp) --dtop;
         }
-        // ---- append accepted nodes to the node list
-        const unsigned ma = __ballot_sync(kFull, acc);
+        // ---- append accepted nodes to the node list (a part: the nodes whose first star is its own)
+        const bool add = kSplit ? acc && own : acc;
+        const unsigned ma = __ballot_sync(kFull, add);
         if (ma) {
-            if (acc) {
+            if (add) {
                 const int en = ncount + __popc(ma & lt);
                 const float4 qc = kS == 2 ? nc : nodes[node].c, qd = kS == 2 ? nd : nodes[node].d;
                 constexpr int P = Lay::kNodePair;
@@ -460,11 +474,17 @@ __device__ __forceinline__ GroupOut walk_group(TravMem &W, Sink &sink, int lane,
         // ---- stage the stars of opened leaves into the source list, 32 at a time
         const unsigned ml = __ballot_sync(kFull, open_leaf);
         if (ml) {
-            const int lo = open_leaf ? int(link) : 0;
-            const int hi = open_leaf ? __float_as_int(kS == 2 ? nd.w : nodes[node].d.w) : 0;
+            int lo = open_leaf ? int(link) : 0;
+            int hi = open_leaf ? __float_as_int(kS == 2 ? nd.w : nodes[node].d.w) : 0;
             if (__any_sync(kFull, open_leaf && (lo < 0 || hi > ns || lo >= hi))) {
                 if (lane == 0) set_err(err_info, 8);
                 return GroupOut{0, false};
+            }
+            if constexpr (kSplit) {  // the part's own stars of the leaf (at least one: it reaches in)
+                if (open_leaf) {
+                    lo = lo > s_lo ? lo : s_lo;
+                    hi = hi < s_hi ? hi : s_hi;
+                }
             }
             const int lc = hi - lo;
             int inc = lc;
@@ -654,7 +674,9 @@ __device__ __forceinline__ void store_acc(const GroupStars<kS> &G, const Acc (&a
     }
 }
 
-template <bool kQuad, bool kSoft, int kS>
+// kSplit: work item i walks part i % nparts of group i / nparts (walk_group's split mode) and
+// writes its sums by sorted index to part_acc[part][axis][star]; k_split_combine adds the parts.
+template <bool kQuad, bool kSoft, int kS, bool kSplit = false>
 __global__ __launch_bounds__(kLwThreads) void k_walk_lists(const DevInfo *info, const LNode *__restrict__ nodes,
                                                            const float4 *__restrict__ st_hi,
                                                            const float4 *__restrict__ st_lo,
@@ -664,7 +686,9 @@ __global__ __launch_bounds__(kLwThreads) void k_walk_lists(const DevInfo *info, 
                                                            const int32_t *__restrict__ targets,
                                                            const int32_t *__restrict__ gperm, int32_t perm_cap,
                                                            uint32_t *gcost, uint32_t *work_ctr, DevInfo *err_info,
-                                                           int node_depth, int src_depth) {
+                                                           int node_depth, int src_depth, int nparts = 1,
+                                                           double *part_acc = nullptr, int64_t part_stride = 0,
+                                                           const int2 *__restrict__ ranges = nullptr) {
     constexpr int kG = 32 * kS;  // stars per group: lane l holds stars l, 32 + l, ...
     __shared__ WarpMem smem[kLwWarps];
     WarpMem &W = smem[threadIdx.x >> 5];
@@ -674,13 +698,18 @@ __global__ __launch_bounds__(kLwThreads) void k_walk_lists(const DevInfo *info, 
     // a target list (block steps): groups of kG consecutive entries; else every star
     const int32_t nt = targets ? int32_t(info->ntargets) : ns;
     const int32_t ng = nn > 0 ? (groups ? int32_t(info->ngroups) : (nt + kG - 1) / kG) : 0;
-    const bool lpt = gperm && gperm[perm_cap] == ng;
+    const bool lpt = !kSplit && gperm && gperm[perm_cap] == ng;
+    const int32_t items = kSplit ? ng * nparts : ng;
     for (;;) {
         int32_t idx = 0;
         if (lane == 0) idx = int32_t(atomicAdd(work_ctr, 1u));
         idx = __shfl_sync(kFull, idx, 0);
-        if (idx >= ng) break;
+        if (idx >= items) break;
+        const int part = kSplit ? idx % nparts : 0;
+        if constexpr (kSplit) idx /= nparts;
         const int32_t g = lpt ? gperm[idx] : idx;
+        const int32_t s_lo = kSplit ? int32_t(int64_t(ns) * part / nparts) : 0;
+        const int32_t s_hi = kSplit ? int32_t(int64_t(ns) * (part + 1) / nparts) : ns;
         const GroupRange R = group_range<kG>(g, groups, nt);
         if (R.cnt <= 0) continue;
         GroupStars<kS> G;
@@ -692,35 +721,73 @@ __global__ __launch_bounds__(kLwThreads) void k_walk_lists(const DevInfo *info, 
         GroupOut r;
         InPlace sink{W.nbuf, W.sbuf, nullptr, nullptr};
         if (B.exact)
-            r = walk_group<true, kQuad, kSoft, kS>(W.tm, sink, lane, R.root, G.t, G.Ox, G.Oy, G.Oz, B.bx0, B.by0,
-                                                    B.bz0, B.bx1, B.by1, B.bz1, B.ext, eps2, node_depth, src_depth,
-                                                    nodes, st_hi, st_lo, nn, ns, err_info, a);
+            r = walk_group<true, kQuad, kSoft, kS, kSplit>(W.tm, sink, lane, R.root, G.t, G.Ox, G.Oy, G.Oz, B.bx0,
+                                                            B.by0, B.bz0, B.bx1, B.by1, B.bz1, B.ext, eps2, node_depth,
+                                                            src_depth, nodes, st_hi, st_lo, nn, ns, err_info, a,
+                                                            ranges, s_lo, s_hi);
         else
-            r = walk_group<false, kQuad, kSoft, kS>(W.tm, sink, lane, R.root, G.t, G.Ox, G.Oy, G.Oz, B.bx0, B.by0,
-                                                     B.bz0, B.bx1, B.by1, B.bz1, B.ext, eps2, node_depth, src_depth,
-                                                     nodes, st_hi, st_lo, nn, ns, err_info, a);
+            r = walk_group<false, kQuad, kSoft, kS, kSplit>(W.tm, sink, lane, R.root, G.t, G.Ox, G.Oy, G.Oz, B.bx0,
+                                                             B.by0, B.bz0, B.bx1, B.by1, B.bz1, B.ext, eps2, node_depth,
+                                                             src_depth, nodes, st_hi, st_lo, nn, ns, err_info, a,
+                                                             ranges, s_lo, s_hi);
         __syncwarp();
         if (!r.ok) break;  // the error flag is set; the host reports GBH_ERR_LIMIT
+        if constexpr (kSplit) {  // the part's sums by sorted index
+            double *q = part_acc + int64_t(part) * 3 * part_stride;
+#pragma unroll
+            for (int u = 0; u < kS; ++u)
+                if (G.valid[u]) {
+                    q[G.k[u]] = double(a[u].sx) - double(a[u].cx);
+                    q[part_stride + G.k[u]] = double(a[u].sy) - double(a[u].cy);
+                    q[2 * part_stride + G.k[u]] = double(a[u].sz) - double(a[u].cz);
+                }
+            continue;
+        }
         if (gcost && lane == 0) gcost[g] = r.cost;
         store_acc<kS>(G, a, order, ax, ay, az);
     }
 }
 
-template <bool kQuad, bool kSoft, int kS>
-cudaError_t launch_lists(const Launch &L, const TreeBufs &b, float eps2, double *ax, double *ay, double *az,
-                         int node_depth, int src_depth, bool lpt, bool targets) {
+template <bool kQuad, bool kSoft, int kS, bool kSplit>
+static int lists_blocks_per_sm() {
     static int blocks_per_sm = 0;  // per instantiation; the same on every device of this architecture
     if (!blocks_per_sm) {
-        cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_walk_lists<kQuad, kSoft, kS>,
-                                                                      kLwThreads, 0);
-        if (e != cudaSuccess) return e;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_walk_lists<kQuad, kSoft, kS, kSplit>,
+                                                          kLwThreads, 0) != cudaSuccess)
+            return 0;
         if (blocks_per_sm < 1) blocks_per_sm = 1;
     }
+    return blocks_per_sm;
+}
+
+template <bool kQuad, bool kSoft, int kS>
+cudaError_t launch_lists(const Launch &L, const TreeBufs &b, int64_t nstars_cap, float eps2, double *ax, double *ay,
+                         double *az, int node_depth, int src_depth, bool lpt, bool targets, bool &split) {
     const bool forest = b.nsys > 1;
     cudaError_t e = cudaMemsetAsync(b.walk_ctr, 0, sizeof(uint32_t), L.stream);
     if (e != cudaSuccess) return e;
     const int sms = L.num_sms > 0 ? L.num_sms : 152;
-    k_walk_lists<kQuad, kSoft, kS><<<unsigned(sms * blocks_per_sm), kLwThreads, 0, L.stream>>>(
+    if constexpr (kQuad && kSoft && kS == 1) {
+        // few groups: each group's walk shared among several warps (the same part count rule as
+        // the paired walk's split mode, by the stars the walk takes); 64-star groups of so few
+        // stars take the paired walk's split mode instead (walk_mixed)
+        const int parts = split_parts(b, nstars_cap, targets, 32 * kS);
+        split = parts > 1;
+        if (split) {
+            const int bps = lists_blocks_per_sm<kQuad, kSoft, kS, true>();
+            if (!bps) return cudaErrorUnknown;
+            k_walk_lists<kQuad, kSoft, kS, true><<<unsigned(sms * bps), kLwThreads, 0, L.stream>>>(
+                b.info, b.lnode, b.st_hi, b.st_lo, b.order, sqrtf(eps2), eps2, ax, ay, az, nullptr,
+                targets ? b.targets : nullptr, nullptr, int32_t(b.cap_groups), nullptr, b.walk_ctr, b.info,
+                node_depth, src_depth, parts, b.part_acc, nstars_cap, b.mrange);
+            ++*L.count;
+            if ((e = cudaGetLastError()) != cudaSuccess) return e;
+            return split_combine(L, b, parts, nstars_cap, targets, ax, ay, az);
+        }
+    }
+    const int bps = lists_blocks_per_sm<kQuad, kSoft, kS, false>();
+    if (!bps) return cudaErrorUnknown;
+    k_walk_lists<kQuad, kSoft, kS><<<unsigned(sms * bps), kLwThreads, 0, L.stream>>>(
         b.info, b.lnode, b.st_hi, b.st_lo, b.order, sqrtf(eps2), eps2, ax, ay, az,
         forest ? b.groups : nullptr, targets ? b.targets : nullptr, lpt ? b.gperm : nullptr, int32_t(b.cap_groups),
         lpt ? b.gcost : nullptr,
@@ -730,15 +797,16 @@ cudaError_t launch_lists(const Launch &L, const TreeBufs &b, float eps2, double 
 }
 
 template <int kS>
-cudaError_t walk_lists_s(const Launch &L, const TreeBufs &b, float eps2, int quad, double *ax, double *ay,
-                         double *az, int nd, int sd, bool lpt, bool targets) {
+cudaError_t walk_lists_s(const Launch &L, const TreeBufs &b, int64_t nstars_cap, float eps2, int quad, double *ax,
+                         double *ay, double *az, int nd, int sd, bool lpt, bool targets) {
     const bool soft = eps2 > 0.f;
     cudaError_t e;
-    if (quad && soft) e = launch_lists<true, true, kS>(L, b, eps2, ax, ay, az, nd, sd, lpt, targets);
-    else if (quad) e = launch_lists<true, false, kS>(L, b, eps2, ax, ay, az, nd, sd, lpt, targets);
-    else if (soft) e = launch_lists<false, true, kS>(L, b, eps2, ax, ay, az, nd, sd, lpt, targets);
-    else e = launch_lists<false, false, kS>(L, b, eps2, ax, ay, az, nd, sd, lpt, targets);
-    if (e != cudaSuccess || !lpt) return e;
+    bool split = false;
+    if (quad && soft) e = launch_lists<true, true, kS>(L, b, nstars_cap, eps2, ax, ay, az, nd, sd, lpt, targets, split);
+    else if (quad) e = launch_lists<true, false, kS>(L, b, nstars_cap, eps2, ax, ay, az, nd, sd, lpt, targets, split);
+    else if (soft) e = launch_lists<false, true, kS>(L, b, nstars_cap, eps2, ax, ay, az, nd, sd, lpt, targets, split);
+    else e = launch_lists<false, false, kS>(L, b, nstars_cap, eps2, ax, ay, az, nd, sd, lpt, targets, split);
+    if (e != cudaSuccess || !lpt || split) return e;  // a split walk records no group costs
     return lpt_order(L, b, 32 * kS);
 }
 
@@ -947,6 +1015,7 @@ struct __align__(16) AdjWarpMem {
 // The adjoint walk over 32-star groups (the forward's group size in adjoint mode): the same
 // traversal as k_walk_lists<quad, soft, 1>, with the adjoint sink. w: the weights in state order
 // (three arrays); tgt: each sorted star's own terms (3 doubles).
+template <bool kSplit>
 __global__ __launch_bounds__(kLwThreads) void k_walk_lists_adj(const DevInfo *info, const LNode *__restrict__ nodes,
                                                                const float4 *__restrict__ st_hi,
                                                                const float4 *__restrict__ st_lo,
@@ -955,7 +1024,9 @@ __global__ __launch_bounds__(kLwThreads) void k_walk_lists_adj(const DevInfo *in
                                                                const double *__restrict__ wy,
                                                                const double *__restrict__ wz, double *tgt,
                                                                double *nadj, double *sadj, uint32_t *work_ctr,
-                                                               DevInfo *err_info, int node_depth, int src_depth) {
+                                                               DevInfo *err_info, int node_depth, int src_depth,
+                                                               int nparts, double *part_tgt, int64_t part_stride,
+                                                               const int2 *__restrict__ ranges) {
     constexpr int kS = 1, kG = 32;
     __shared__ AdjWarpMem smem[kLwWarps];
     AdjWarpMem &W = smem[threadIdx.x >> 5];
@@ -963,11 +1034,16 @@ __global__ __launch_bounds__(kLwThreads) void k_walk_lists_adj(const DevInfo *in
     const int32_t ns = int32_t(info->nstars);
     const int32_t nn = int32_t(info->nnodes);
     const int32_t ng = nn > 0 ? (ns + kG - 1) / kG : 0;
+    const int32_t items = kSplit ? ng * nparts : ng;
     for (;;) {
         int32_t idx = 0;
         if (lane == 0) idx = int32_t(atomicAdd(work_ctr, 1u));
         idx = __shfl_sync(kFull, idx, 0);
-        if (idx >= ng) break;
+        if (idx >= items) break;
+        const int part = kSplit ? idx % nparts : 0;
+        if constexpr (kSplit) idx /= nparts;
+        const int32_t s_lo = kSplit ? int32_t(int64_t(ns) * part / nparts) : 0;
+        const int32_t s_hi = kSplit ? int32_t(int64_t(ns) * (part + 1) / nparts) : ns;
         const GroupRange R = group_range<kG>(idx, nullptr, ns);
         if (R.cnt <= 0) continue;
         GroupStars<kS> G;
@@ -985,21 +1061,48 @@ __global__ __launch_bounds__(kLwThreads) void k_walk_lists_adj(const DevInfo *in
         AdjSink sink{W.nbuf, W.sbuf, W.nidx, W.sidx, nadj, sadj};
         GroupOut r;
         if (B.exact)
-            r = walk_group<true, true, true, kS>(W.tm, sink, lane, R.root, G.t, G.Ox, G.Oy, G.Oz, B.bx0, B.by0, B.bz0,
-                                                 B.bx1, B.by1, B.bz1, B.ext, eps2, node_depth, src_depth, nodes, st_hi,
-                                                 st_lo, nn, ns, err_info, a);
+            r = walk_group<true, true, true, kS, kSplit>(W.tm, sink, lane, R.root, G.t, G.Ox, G.Oy, G.Oz, B.bx0, B.by0,
+                                                         B.bz0, B.bx1, B.by1, B.bz1, B.ext, eps2, node_depth,
+                                                         src_depth, nodes, st_hi, st_lo, nn, ns, err_info, a, ranges,
+                                                         s_lo, s_hi);
         else
-            r = walk_group<false, true, true, kS>(W.tm, sink, lane, R.root, G.t, G.Ox, G.Oy, G.Oz, B.bx0, B.by0,
-                                                  B.bz0, B.bx1, B.by1, B.bz1, B.ext, eps2, node_depth, src_depth,
-                                                  nodes, st_hi, st_lo, nn, ns, err_info, a);
+            r = walk_group<false, true, true, kS, kSplit>(W.tm, sink, lane, R.root, G.t, G.Ox, G.Oy, G.Oz, B.bx0,
+                                                          B.by0, B.bz0, B.bx1, B.by1, B.bz1, B.ext, eps2, node_depth,
+                                                          src_depth, nodes, st_hi, st_lo, nn, ns, err_info, a, ranges,
+                                                          s_lo, s_hi);
         __syncwarp();
         if (!r.ok) break;
         if (G.valid[0]) {
-            tgt[3 * int64_t(G.k[0])] = a[0].gx;
-            tgt[3 * int64_t(G.k[0]) + 1] = a[0].gy;
-            tgt[3 * int64_t(G.k[0]) + 2] = a[0].gz;
+            if constexpr (kSplit) {  // the part's own terms by sorted index; k_adj_part_combine adds them
+                double *q = part_tgt + int64_t(part) * 3 * part_stride;
+                q[G.k[0]] = a[0].gx;
+                q[part_stride + G.k[0]] = a[0].gy;
+                q[2 * part_stride + G.k[0]] = a[0].gz;
+            } else {
+                tgt[3 * int64_t(G.k[0])] = a[0].gx;
+                tgt[3 * int64_t(G.k[0]) + 1] = a[0].gy;
+                tgt[3 * int64_t(G.k[0]) + 2] = a[0].gz;
+            }
         }
     }
+}
+
+// A split adjoint walk's own terms of every star: the parts' sums in part order.
+__global__ __launch_bounds__(256) void k_adj_part_combine(const DevInfo *info, int nparts,
+                                                          const double *__restrict__ part_tgt, int64_t stride,
+                                                          double *tgt) {
+    const int64_t k = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (k >= info->nstars) return;
+    double x = 0, y = 0, z = 0;
+    for (int p = 0; p < nparts; ++p) {
+        const double *q = part_tgt + int64_t(p) * 3 * stride;
+        x += q[k];
+        y += q[stride + k];
+        z += q[2 * stride + k];
+    }
+    tgt[3 * k] = x;
+    tgt[3 * k + 1] = y;
+    tgt[3 * k + 2] = z;
 }
 
 // The leaf of every sorted star (from the leaves' star ranges in their list records).
@@ -1069,8 +1172,8 @@ __global__ void k_adj_downsweep(const DevInfo *info, const LNode *__restrict__ n
 
 int list_depth_max(bool exact) { return exact ? Layout<true>::kNodeCap - 32 : Layout<false>::kNodeCap - 32; }
 
-cudaError_t walk_lists(const Launch &L, const TreeBufs &b, float eps2, int quad, double *ax, double *ay, double *az,
-                       int list_depth, bool targets, int stars_per_lane) {
+cudaError_t walk_lists(const Launch &L, const TreeBufs &b, int64_t nstars_cap, float eps2, int quad, double *ax,
+                       double *ay, double *az, int list_depth, bool targets, int stars_per_lane) {
     // The list depth is the node list's flush threshold (entries per lane and evaluation); the
     // source list flushes at twice it. Both are capped so that one step's appends always fit; an
     // exact-separation group uses the smaller of its own cap and the depth.
@@ -1080,8 +1183,8 @@ cudaError_t walk_lists(const Launch &L, const TreeBufs &b, float eps2, int quad,
     int sd = 2 * nd;
     if (sd > Layout<false>::kSrcCap - 32) sd = Layout<false>::kSrcCap - 32;
     const bool lpt = b.lpt && !targets;  // a target list changes from event to event
-    if (stars_per_lane == 2) return walk_lists_s<2>(L, b, eps2, quad, ax, ay, az, nd, sd, lpt, targets);
-    return walk_lists_s<1>(L, b, eps2, quad, ax, ay, az, nd, sd, lpt, targets);
+    if (stars_per_lane == 2) return walk_lists_s<2>(L, b, nstars_cap, eps2, quad, ax, ay, az, nd, sd, lpt, targets);
+    return walk_lists_s<1>(L, b, nstars_cap, eps2, quad, ax, ay, az, nd, sd, lpt, targets);
 }
 
 cudaError_t walk_lists_adjoint(const Launch &L, const TreeBufs &b, float eps2, const double *px, const double *py,
@@ -1092,19 +1195,39 @@ cudaError_t walk_lists_adjoint(const Launch &L, const TreeBufs &b, float eps2, c
     if ((e = cudaMemsetAsync(s.sadj, 0, sizeof(double) * kAdjStarTerms * size_t(b.cap_n), L.stream))) return e;
     if ((e = cudaMemsetAsync(s.star_leaf, 0xff, sizeof(int32_t) * size_t(b.cap_n), L.stream))) return e;
     if ((e = cudaMemsetAsync(b.walk_ctr, 0, sizeof(uint32_t), L.stream))) return e;
-    static int blocks_per_sm = 0;
-    if (!blocks_per_sm) {
-        if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_walk_lists_adj, kLwThreads, 0)))
-            return e;
-        if (blocks_per_sm < 1) blocks_per_sm = 1;
-    }
+    // few groups: each group's walk shared among several warps, as the forward's (walk_lists)
+    const int parts = split_parts(b, n, false, 32);
     const int sms = L.num_sms > 0 ? L.num_sms : 152;
     const int nd = kDefaultListDepth, sd = 2 * kDefaultListDepth;
-    k_walk_lists_adj<<<unsigned(sms * blocks_per_sm), kLwThreads, 0, L.stream>>>(
-        b.info, b.lnode, b.st_hi, b.st_lo, b.order, sqrtf(eps2), eps2, wx, wy, wz, s.tgt, s.nadj, s.sadj, b.walk_ctr,
-        b.info, nd, sd);
-    ++*L.count;
-    if ((e = cudaGetLastError())) return e;
+    if (parts > 1) {
+        static int bps_split = 0;
+        if (!bps_split) {
+            if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps_split, k_walk_lists_adj<true>, kLwThreads, 0)))
+                return e;
+            if (bps_split < 1) bps_split = 1;
+        }
+        k_walk_lists_adj<true><<<unsigned(sms * bps_split), kLwThreads, 0, L.stream>>>(
+            b.info, b.lnode, b.st_hi, b.st_lo, b.order, sqrtf(eps2), eps2, wx, wy, wz, s.tgt, s.nadj, s.sadj,
+            b.walk_ctr, b.info, nd, sd, parts, b.part_acc, n, b.mrange);
+        ++*L.count;
+        if ((e = cudaGetLastError())) return e;
+        k_adj_part_combine<<<unsigned((n + 255) / 256), 256, 0, L.stream>>>(b.info, parts, b.part_acc, n, s.tgt);
+        ++*L.count;
+        if ((e = cudaGetLastError())) return e;
+    } else {
+        static int blocks_per_sm = 0;
+        if (!blocks_per_sm) {
+            if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_walk_lists_adj<false>, kLwThreads,
+                                                                   0)))
+                return e;
+            if (blocks_per_sm < 1) blocks_per_sm = 1;
+        }
+        k_walk_lists_adj<false><<<unsigned(sms * blocks_per_sm), kLwThreads, 0, L.stream>>>(
+            b.info, b.lnode, b.st_hi, b.st_lo, b.order, sqrtf(eps2), eps2, wx, wy, wz, s.tgt, s.nadj, s.sadj,
+            b.walk_ctr, b.info, nd, sd, 1, nullptr, 0, nullptr);
+        ++*L.count;
+        if ((e = cudaGetLastError())) return e;
+    }
     const unsigned nbn = unsigned((b.cap_nodes + 255) / 256), nbs = unsigned((b.cap_n + 255) / 256);
     k_star_leaf<<<nbn < 1 ? 1 : nbn, 256, 0, L.stream>>>(b.info, b.lnode, s.star_leaf);
     ++*L.count;

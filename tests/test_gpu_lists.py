@@ -202,3 +202,30 @@ def test_block_steps_one_level_is_the_global_step_with_the_list_walk(ctx, group)
     st = ctx.step_block(par, 8e-3, 0.025, 4, 2)
     e1 = ctx.diagnostics(par)["total"]
     assert st["evaluations"] < 2 * 8 * n and abs((e1 - e0) / e0) < 1e-4
+
+
+@pytest.mark.parametrize("scene,theta,leaf,eps", [("plummer", 0.5, 8, 0.01), ("galaxy", 0.6, 24, 0.02)])
+def test_split_list_walk_sums_the_same_interactions(scene, theta, leaf, eps):
+    """Few 32-star groups for the GPU: each group's walk is shared among several warps, each
+    owning a range of source stars (a node counts where its first star is, a leaf's stars where
+    they are). The parts add up to the same interactions as one warp's walk: the forces differ
+    only by the order of the FP32 sums (global relative norm <= 1e-6), and the split walk meets
+    the same accuracy bound against the FP64 direct sum."""
+    s = {"plummer": lambda: ics.plummer(16384, seed=11), "galaxy": lambda: ics.galaxy(20000, seed=12)}[scene]()
+    par = lists(theta, eps, leaf, group=32)
+    split, whole = abi.Context(0), abi.Context(0, abi.CFG_NO_SPLIT)
+    try:
+        a = forces(split, s, par)
+        b = forces(whole, s, par)
+        assert np.array_equal(a, forces(split, s, par))  # deterministic
+    finally:
+        split.close()
+        whole.close()
+    assert not np.array_equal(a, b)  # the parts' sums are grouped differently: the split walk ran
+    assert np.linalg.norm(a - b) <= 1e-6 * np.linalg.norm(b)
+    kind = s.get("kind")
+    want = O.direct(s["px"], s["py"], s["pz"], s["mass"], kind, eps=eps)
+    ref = O.Tree(s["px"], s["py"], s["pz"], s["mass"], kind, s.get("alive"), theta=theta, leaf=leaf).accelerations(eps)
+    live = np.linalg.norm(want, axis=1) > 0
+    e, e_ref = rel(a[live], want[live]), rel(ref[live], want[live])
+    assert rms(e) <= 1.001 * rms(e_ref) + 1e-7
