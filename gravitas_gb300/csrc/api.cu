@@ -233,7 +233,11 @@ double theta_of(const gbh_params *p) { return p->theta == 0 ? 0.9 : p->theta; } 
 int group_of(const gbh_params *p, int64_t n, bool forest) {
     if (p->group_size == 32 || p->group_size == 64) return p->group_size;
     if (forest) return 64;
-    return gbh::walk_parts(n, 64) > 1 || n >= (int64_t(1) << 19) ? 64 : 32;
+    // 32-star groups below 2^19 bodies: the list walk, shared among warps when the groups are few
+    // (measured on Plummer spheres and galaxies of 16k-131k bodies, walk time against 64-star
+    // groups in the paired walk's split mode: 0.11 / 0.17 ms at 16k, 0.38 / 0.76 at 65k, 0.69 /
+    // 1.54 at 131k; even at 262k); above, 64-star groups (two stars a lane)
+    return n >= (int64_t(1) << 19) ? 64 : 32;
 }
 int leaf_of(const gbh_params *p) { return p->leaf_size > 0 ? p->leaf_size : 24; }  // bh.go:17-19
 

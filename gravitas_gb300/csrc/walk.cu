@@ -580,19 +580,16 @@ cudaError_t split_combine(const Launch &L, const TreeBufs &b, int nparts, int64_
     return cudaGetLastError();
 }
 
-// Whether a walk of 64-star groups takes the paired walk's split mode.
-static bool paired_split(const TreeBufs &b, int64_t nstars_cap, bool targets) {
-    return split_parts(b, nstars_cap, targets, 64) > 1;
-}
 
 cudaError_t walk_mixed(const Launch &L, const TreeBufs &b, int64_t nstars_cap, float eps2, int quad, double *ax,
                        double *ay, double *az, bool targets) {
-    // The list walk (walk_lists.cu) in groups of 32 (one star a lane) or 64 (two); the paired walk
-    // above for 64-star groups of a system small enough for its split mode (or with b.paired)
+    // The list walk (walk_lists.cu) in groups of 32 (one star a lane) or 64 (two), split among
+    // warps when the groups are few; the paired walk above with b.paired (GBH_CFG_PAIRED). Measured
+    // against the paired walk's split mode on 16k-131k bodies: the split list walk takes half the
+    // time or less (0.11 / 0.17 ms at 16k, 0.37 / 0.76 at 65k, 0.78 / 1.54 at 131k, 64-star groups).
     if (b.cap_nodes < (int64_t(1) << 29)) {
         if (b.group == 32) return walk_lists(L, b, nstars_cap, eps2, quad, ax, ay, az, b.list_depth, targets, 1);
-        if (!b.paired && !paired_split(b, nstars_cap, targets))
-            return walk_lists(L, b, nstars_cap, eps2, quad, ax, ay, az, b.list_depth, targets, 2);
+        if (!b.paired) return walk_lists(L, b, nstars_cap, eps2, quad, ax, ay, az, b.list_depth, targets, 2);
     }
     bool soft = eps2 > 0.f;
     if (quad && soft) return launch_mixed<true, true>(L, b, nstars_cap, eps2, ax, ay, az, targets);

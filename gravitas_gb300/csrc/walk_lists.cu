@@ -767,10 +767,9 @@ cudaError_t launch_lists(const Launch &L, const TreeBufs &b, int64_t nstars_cap,
     cudaError_t e = cudaMemsetAsync(b.walk_ctr, 0, sizeof(uint32_t), L.stream);
     if (e != cudaSuccess) return e;
     const int sms = L.num_sms > 0 ? L.num_sms : 152;
-    if constexpr (kQuad && kSoft && kS == 1) {
+    if constexpr (kQuad && kSoft) {
         // few groups: each group's walk shared among several warps (the same part count rule as
-        // the paired walk's split mode, by the stars the walk takes); 64-star groups of so few
-        // stars take the paired walk's split mode instead (walk_mixed)
+        // the paired walk's split mode, by the stars the walk takes)
         const int parts = split_parts(b, nstars_cap, targets, 32 * kS);
         split = parts > 1;
         if (split) {

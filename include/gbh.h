@@ -57,13 +57,13 @@ enum {
     /* Warp-cooperative FP32 walk with compensated per-star accumulation and
        separations formed from hi + lo splits of the FP64 positions; every star
        sees each accepted node exactly where the reference walk accepts it, or
-       deeper. Two kernels (see group_size): the list walk, one warp per 32 or
-       64 Morton-consecutive stars (one or two a lane) that builds the group's
-       interaction lists with node-parallel opening tests and evaluates them
-       from shared memory two entries at a time in packed FP32x2 arithmetic;
-       and the paired walk, one warp per 64 stars walking the skip links in
-       lockstep, whose split mode shares a group among several warps for small
-       systems. The default. */
+       deeper. Two kernels: the list walk, one warp per 32 or 64
+       Morton-consecutive stars (one or two a lane; see group_size) that builds
+       the group's interaction lists with node-parallel opening tests and
+       evaluates them from shared memory two entries at a time in packed FP32x2
+       arithmetic, its split mode sharing a group among several warps for small
+       systems; and the paired walk (GBH_CFG_PAIRED), one warp per 64 stars
+       walking the skip links in lockstep. The default. */
     GBH_WALK_MIXED = 0,
     /* One thread per star, all FP32, uncompensated: the CUDA twin of the Metal
        kernel internal/sim/bh/gpu_darwin.go:76-118. */
@@ -82,12 +82,9 @@ typedef struct {
     int32_t monopole_only;   /* drop quadrupoles of accepted nodes (bh.go:34-35) */
     int32_t dark_matter_off; /* dark matter pulls nothing (Params.DarkMatterOff, sim.go:92-98) */
     int32_t walk;            /* GBH_WALK_* */
-    int32_t group_size;      /* GBH_WALK_MIXED: 32 the list walk with one star a lane; 64 the list
-                                walk with two, except for a single system of up to 21 64-star
-                                groups per SM (below about 200,000 stars on a GB300), where the
-                                paired walk shares each group's walk among several warps (unless
-                                GBH_CFG_NO_SPLIT); 0: 64 for a forest and for a single system of
-                                at least 524,288 stars or of up to 21 groups per SM, else 32 */
+    int32_t group_size;      /* GBH_WALK_MIXED: 32 the list walk with one star a lane; 64 with two
+                                (the paired walk with GBH_CFG_PAIRED); 0: 64 for a forest and for
+                                a single system of at least 524,288 stars, else 32 */
     int32_t list_depth;      /* list walk: node-list entries evaluated per pass, 2 to 56 (0 means 56;
                                 source lists take twice as many, up to 160) */
     double c;                /* speed of light of the steps (Params.C): 0 Newtonian; > 0 drifts by
@@ -106,14 +103,14 @@ enum {
        the previous walk's group costs give); results are identical either way. */
     GBH_CFG_NO_LPT = 4,
     /* The mixed walk of a single system never splits a group's walk over several warps. With few
-       groups (up to 21 per SM: below about 200,000 stars on a GB300) each group's walk is
-       otherwise shared by 2 to 32 warps (the paired walk's split mode), each adding the
-       interactions of its own range of source stars, and the parts are summed in order: the
-       same interactions, a different order of summation. Without splitting, 64-star groups take
-       the list walk (or the paired walk, with GBH_CFG_PAIRED). */
+       groups (up to 21 per SM: below about 100,000 stars in 32-star groups, 200,000 in 64-star
+       groups on a GB300, or as few stars in a block-step event's list) each group's walk is
+       otherwise shared by 2 to 32 warps (the split mode of the list walk, or of the paired walk),
+       each adding the interactions of its own range of source stars, and the parts are summed
+       in order: the same interactions, a different order of summation. */
     GBH_CFG_NO_SPLIT = 8,
-    /* 64-star groups of the mixed walk always take the paired walk (split or not), never the
-       list walk. */
+    /* 64-star groups of the mixed walk take the paired walk (split or not) instead of the list
+       walk. */
     GBH_CFG_PAIRED = 16
 };
 

@@ -175,7 +175,8 @@ def test_non_finite_inputs_of_a_forest_system_are_rejected():
         assert ei.value.code == abi.ERR_ARG
 
 
-@pytest.mark.parametrize("walk,group,kernel,flags", [("mixed", 64, 4, 0), ("mixed", 64, 4, abi.CFG_NO_SPLIT | abi.CFG_PAIRED),
+@pytest.mark.parametrize("walk,group,kernel,flags", [("mixed", 64, 8, 0), ("mixed", 64, 4, abi.CFG_PAIRED),
+                                                     ("mixed", 64, 4, abi.CFG_NO_SPLIT | abi.CFG_PAIRED),
                                                      ("mixed", 64, 8, abi.CFG_NO_SPLIT), ("mixed", 32, 8, 0),
                                                      ("plain", 0, 3, 0), ("fp64", 0, 1, 0)])
 def test_walk_step_bound_stops_a_walk_on_a_corrupt_tree(walk, group, kernel, flags):

@@ -1,7 +1,7 @@
 """GPU tests of the list walk (GBH_WALK_MIXED with 32-star groups, or 64-star groups of two stars a
 lane, walk_lists.cu): a warp builds its group's interaction lists with node-parallel opening tests
 and evaluates them from shared memory two entries at a time. The context is made with
-GBH_CFG_NO_SPLIT, so that 64-star groups of small systems take the list walk too. Its opening
+GBH_CFG_NO_SPLIT, so that one warp walks each group (the split mode is tested at the end). Its opening
 test takes the reference criterion (bh.go:116) over every star of the group, with a margin for
 FP32 rounding, so every star sees each accepted node where the reference accepts it or deeper:
 against the FP64 direct sum it is at least as accurate as the reference's per-star walk, and
@@ -204,15 +204,16 @@ def test_block_steps_one_level_is_the_global_step_with_the_list_walk(ctx, group)
     assert st["evaluations"] < 2 * 8 * n and abs((e1 - e0) / e0) < 1e-4
 
 
+@pytest.mark.parametrize("group", [32, 64])
 @pytest.mark.parametrize("scene,theta,leaf,eps", [("plummer", 0.5, 8, 0.01), ("galaxy", 0.6, 24, 0.02)])
-def test_split_list_walk_sums_the_same_interactions(scene, theta, leaf, eps):
-    """Few 32-star groups for the GPU: each group's walk is shared among several warps, each
+def test_split_list_walk_sums_the_same_interactions(scene, theta, leaf, eps, group):
+    """Few groups for the GPU: each group's walk is shared among several warps, each
     owning a range of source stars (a node counts where its first star is, a leaf's stars where
     they are). The parts add up to the same interactions as one warp's walk: the forces differ
     only by the order of the FP32 sums (global relative norm <= 1e-6), and the split walk meets
     the same accuracy bound against the FP64 direct sum."""
     s = {"plummer": lambda: ics.plummer(16384, seed=11), "galaxy": lambda: ics.galaxy(20000, seed=12)}[scene]()
-    par = lists(theta, eps, leaf, group=32)
+    par = lists(theta, eps, leaf, group=group)
     split, whole = abi.Context(0), abi.Context(0, abi.CFG_NO_SPLIT)
     try:
         a = forces(split, s, par)

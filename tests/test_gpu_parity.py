@@ -228,14 +228,18 @@ def test_walks_are_deterministic(ctx, walk):
     assert np.array_equal(a, b)
 
 
+@pytest.mark.parametrize("paired", [False, True])
 @pytest.mark.parametrize("n,group,scene", [(20000, 64, "galaxy"), (100000, 64, "galaxy"), (700, 64, "galaxy"),
-                                           (20000, 64, "disk")])
-def test_split_walk_adds_the_same_interactions(ctx, n, group, scene):
-    """With few groups each group's walk of the paired walk (64-star groups) is split over several
-    warps by source-star range (the list walk never splits). The
-    parts together add exactly the unsplit walk's interactions, in another order: the split
-    forces equal the unsplit ones to FP32 summation rounding (global relative norm <= 1e-6,
-    every star <= 1e-4), are as accurate against the FP64 direct sum, and repeat bit for bit."""
+                                           (20000, 64, "disk"), (20000, 32, "galaxy")])
+def test_split_walk_adds_the_same_interactions(n, group, scene, paired):
+    """With few groups each group's walk is split over several warps by source-star range (the
+    list walk's split mode; the paired walk's with GBH_CFG_PAIRED, 64-star groups). The parts
+    together add exactly the unsplit walk's interactions, in another order: the split forces
+    equal the unsplit ones to FP32 summation rounding (global relative norm <= 1e-6, every star
+    <= 1e-4), are as accurate against the FP64 direct sum, and repeat bit for bit."""
+    if paired and group != 64:
+        pytest.skip("the paired walk takes 64-star groups")
+    ctx = abi.Context(0, abi.CFG_PAIRED if paired else 0)
     if scene == "galaxy":
         s = ics.galaxy(n, seed=3)
     else:  # two black holes, dead bodies, dark matter that pulls nothing
@@ -244,7 +248,7 @@ def test_split_walk_adds_the_same_interactions(ctx, n, group, scene):
         s["alive"][7::97] = 0
     n = len(s["px"])
     dm_off = scene == "disk"
-    whole = abi.Context(0, abi.CFG_NO_SPLIT | abi.CFG_PAIRED)  # the paired walk, unsplit
+    whole = abi.Context(0, abi.CFG_NO_SPLIT | (abi.CFG_PAIRED if paired else 0))  # the same walk, unsplit
     try:
         par = abi.make_params(0.5, 0.02, 16, False, dm_off, "mixed", group_size=group)
         got = []
@@ -270,6 +274,7 @@ def test_split_walk_adds_the_same_interactions(ctx, n, group, scene):
         assert np.array_equal(again, first)
     finally:
         whole.close()
+        ctx.close()
 
 
 # ---------------------------------------------------------------- direct, potential, KDK
