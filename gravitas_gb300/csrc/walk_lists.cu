@@ -484,6 +484,7 @@ __device__ __forceinline__ GroupOut walk_group(TravMem &W, Sink &sink, int lane,
                 if (open_leaf) {
                     lo = lo > s_lo ? lo : s_lo;
                     hi = hi < s_hi ? hi : s_hi;
+                    if (hi < lo) hi = lo;  // only a record that disagrees with its range: no stars
                 }
             }
             const int lc = hi - lo;
