@@ -1925,7 +1925,14 @@ cudaError_t tree_build(const Launch &L, TreeBufs &b, int64_t n, const double *px
     // one-sweep sort and single-pass scans (capacity up to kOsMaxN bodies): histograms, tile
     // counters and the look-back words of the passes this build runs start at zero
     const bool os = b.os_state != nullptr;
-    const int npass = forest ? kOsPassesMax : 8;
+    // a forest then sorts stably by system id, one pass per byte: up to 256 systems the high
+    // byte is 0 everywhere, and that pass (a stable pass over equal digits) is left out
+    const int sid_passes = forest ? (b.nsys > 256 ? 2 : 1) : 0;
+    const int npass = 8 + sid_passes;
+    // the passes ping-pong between the two buffers and end in keys / order: with an odd count
+    // the keys are formed in the other pair
+    uint64_t *const keys0 = (npass & 1) ? b.keys_alt : b.keys;
+    int32_t *const order0 = (npass & 1) ? b.order_alt : b.order;
     const int os_k = os_items(cap);  // keys a thread of a one-sweep pass ranks
     const int64_t os_tiles = os_sort_tiles(cap, os_k);
     if (os) {
@@ -1945,8 +1952,8 @@ cudaError_t tree_build(const Launch &L, TreeBufs &b, int64_t n, const double *px
         if (e != cudaSuccess) return e;
         k_bbox_final<<<1, kFinalThreads, 0, s>>>(int(fb), b.bbox_part, n, b.flag, kind, alive, theta, b.info, b.geo);
         GBH_LAUNCH_CHECK();
-        k_compact_keys<<<blocks_for(n, kThreads), kThreads, 0, s>>>(n, px, py, pz, kind, alive, b.flag, b.info, b.keys,
-                                                                    b.order);
+        k_compact_keys<<<blocks_for(n, kThreads), kThreads, 0, s>>>(n, px, py, pz, kind, alive, b.flag, b.info, keys0,
+                                                                    order0);
         GBH_LAUNCH_CHECK();
     } else {
         // collect per system: each system gets its own root cube and keys (build.go:11-31)
@@ -1961,13 +1968,13 @@ cudaError_t tree_build(const Launch &L, TreeBufs &b, int64_t n, const double *px
         k_sys_final<<<sb, 128, 0, s>>>(b.nsys, n, sys_off, b.flag, kind, alive, theta, b.geo, b.info);
         GBH_LAUNCH_CHECK();
         k_compact_keys_sys<<<blocks_for(n, kThreads), kThreads, 0, s>>>(n, px, py, pz, kind, alive, sys_of, b.flag,
-                                                                        b.geo, b.keys, b.order);
+                                                                        b.geo, keys0, order0);
         GBH_LAUNCH_CHECK();
     }
     // radix sort (morton.go:25-49): 8 stable passes, ping-pong, result back in keys/order
     const uint32_t ntiles = uint32_t((cap + kRsTile - 1) / kRsTile);
-    uint64_t *kin = b.keys, *kout = b.keys_alt;
-    int32_t *vin = b.order, *vout = b.order_alt;
+    uint64_t *kin = keys0, *kout = keys0 == b.keys ? b.keys_alt : b.keys;
+    int32_t *vin = order0, *vout = order0 == b.order ? b.order_alt : b.order;
     if (os) {
         // forest: then stably by system, (system, key) order, each system's stars contiguous
         uint32_t *ghist = b.os_state, *ctr = b.os_state + kOsHistWords;
@@ -2014,7 +2021,7 @@ cudaError_t tree_build(const Launch &L, TreeBufs &b, int64_t n, const double *px
         vout = tv;
     }
     if (forest && !os) {  // then stably by system: (system, key) order, each system's stars contiguous
-        for (int shift = 0; shift < 16; shift += 8) {
+        for (int shift = 0; shift < 8 * sid_passes; shift += 8) {
             k_rs_hist<true><<<ntiles, kRsThreads, 0, s>>>(kin, vin, sys_of, b.info, shift, ntiles, b.hist);
             GBH_LAUNCH_CHECK();
             if ((e = scan_hist(L, b, 8 + shift / 8, ntiles)) != cudaSuccess) return e;
