@@ -601,6 +601,9 @@ cudaError_t walk_mixed(const Launch &L, const TreeBufs &b, int64_t nstars_cap, f
 cudaError_t walk_mixed_potential(const Launch &L, const TreeBufs &b, int64_t nstars_cap, float eps2, int quad,
                                  double *psi) {
     bool soft = eps2 > 0.f;
+    // the list walk's potential sink (64-star groups); the paired walk's potential mode otherwise
+    if (soft && b.group == 64 && !b.paired && b.cap_nodes < (int64_t(1) << 29))
+        return walk_lists_potential(L, b, eps2, quad, psi);
     if (quad && soft) return launch_mixed<true, true, true>(L, b, nstars_cap, eps2, psi, nullptr, nullptr, false);
     if (quad) return launch_mixed<true, false, true>(L, b, nstars_cap, eps2, psi, nullptr, nullptr, false);
     if (soft) return launch_mixed<false, true, true>(L, b, nstars_cap, eps2, psi, nullptr, nullptr, false);

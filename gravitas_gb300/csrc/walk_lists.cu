@@ -1105,6 +1105,165 @@ __global__ __launch_bounds__(256) void k_adj_part_combine(const DevInfo *info, i
     tgt[3 * k + 2] = z;
 }
 
+// ---- the tree potential with the list walk: psi_i = sum m / r + (d.Q.d) / (2 r^5) over the
+// accepted nodes and the opened leaves' stars (walkPotential, potential.go:44-81), a star's pair
+// with itself skipped by index (a coincident other star still counts, as in the reference)
+
+struct PotAcc {
+    float2 p;      // the current list's sums (entry A, entry B halves)
+    float s, c;    // Kahan sum
+    int32_t k;     // the star's sorted index
+    __device__ __forceinline__ void fold() {
+        kahan_fold(s, c, p.x + p.y);
+        p = f2(0.f);
+    }
+};
+
+struct PotSink {
+    static constexpr bool kIndices = true;
+    float4 *nbuf, *sbuf;
+    int32_t *nidx, *sidx;
+
+    template <bool kExact, bool kQuad, bool kSoft, int kS>
+    __device__ __forceinline__ void nodes(int count, const Target (&t)[kS], float eps2, PotAcc (&a)[kS], int) {
+        using Lay = Layout<kExact>;
+        const float2 e2 = f2(eps2);
+        const int np = (count + 1) >> 1;
+        for (int p = 0; p < np; ++p) {
+            const float4 *r = &nbuf[p * Lay::kNodePair];
+            const float4 r0 = r[0], r1 = r[1];
+            float2 lx = f2(0.f), ly = f2(0.f), lz = f2(0.f);
+            if constexpr (kExact) {
+                const float4 r5 = r[5], r6 = r[6];
+                lx = lo2(r5);
+                ly = hi2(r5);
+                lz = lo2(r6);
+            }
+            float4 r2a, r3, r4;
+            if constexpr (kQuad) {
+                r2a = r[2];
+                r3 = r[3];
+                r4 = r[4];
+            }
+#pragma unroll
+            for (int q = 0; q < kS; ++q) {
+                const float2 dx = sep<kExact>(lo2(r0), lx, -t[q].tx, -t[q].hx, -t[q].lx);
+                const float2 dy = sep<kExact>(hi2(r0), ly, -t[q].ty, -t[q].hy, -t[q].ly);
+                const float2 dz = sep<kExact>(lo2(r1), lz, -t[q].tz, -t[q].hz, -t[q].lz);
+                const float2 rr = fma2(dz, dz, fma2(dy, dy, fma2(dx, dx, e2)));
+                float2 ir;
+                if constexpr (kSoft) {
+                    ir = make_float2(rsqrtf(rr.x), rsqrtf(rr.y));
+                } else {
+                    ir = make_float2(rr.x > 0.f ? rsqrtf(rr.x) : 0.f, rr.y > 0.f ? rsqrtf(rr.y) : 0.f);
+                }
+                float2 v = mul2(hi2(r1), ir);
+                if constexpr (kQuad) {  // the record holds -Q: dqd = -(d.Q.d)
+                    const float2 qx = fma2(lo2(r4), dz, fma2(hi2(r3), dy, mul2(lo2(r2a), dx)));
+                    const float2 qy = fma2(hi2(r4), dz, fma2(hi2(r2a), dy, mul2(hi2(r3), dx)));
+                    const float2 qz = fma2(lo2(r3), dz, fma2(hi2(r4), dy, mul2(lo2(r4), dx)));
+                    const float2 dqd = fma2(dz, qz, fma2(dy, qy, mul2(dx, qx)));
+                    const float2 ir2 = mul2(ir, ir);
+                    v = fma2(mul2(f2(-0.5f), dqd), mul2(mul2(ir2, ir), ir2), v);
+                }
+                a[q].p = add2(a[q].p, v);
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < kS; ++q) a[q].fold();
+    }
+
+    template <bool kExact, bool kSoft, int kS>
+    __device__ __forceinline__ void sources(int count, const Target (&t)[kS], float eps2, PotAcc (&a)[kS], int) {
+        using Lay = Layout<kExact>;
+        const float2 e2 = f2(eps2);
+        const int np = (count + 1) >> 1;
+        for (int p = 0; p < np; ++p) {
+            const float4 *r = &sbuf[p * Lay::kSrcPair];
+            const float4 r0 = r[0], r1 = r[1];
+            float2 lx = f2(0.f), ly = f2(0.f), lz = f2(0.f);
+            if constexpr (kExact) {
+                const float4 r2a = r[2], r3 = r[3];
+                lx = lo2(r2a);
+                ly = hi2(r2a);
+                lz = lo2(r3);
+            }
+            const int32_t sA = sidx[2 * p], sB = 2 * p + 1 < count ? sidx[2 * p + 1] : -1;  // B: a zero-mass pad
+#pragma unroll
+            for (int q = 0; q < kS; ++q) {
+                const float2 dx = sep<kExact>(lo2(r0), lx, -t[q].tx, -t[q].hx, -t[q].lx);
+                const float2 dy = sep<kExact>(hi2(r0), ly, -t[q].ty, -t[q].hy, -t[q].ly);
+                const float2 dz = sep<kExact>(lo2(r1), lz, -t[q].tz, -t[q].hz, -t[q].lz);
+                const float2 rr = fma2(dz, dz, fma2(dy, dy, fma2(dx, dx, e2)));
+                float2 ir;
+                if constexpr (kSoft) {
+                    ir = make_float2(rsqrtf(rr.x), rsqrtf(rr.y));
+                } else {
+                    ir = make_float2(rr.x > 0.f ? rsqrtf(rr.x) : 0.f, rr.y > 0.f ? rsqrtf(rr.y) : 0.f);
+                }
+                float2 v = mul2(hi2(r1), ir);
+                v.x = sA == a[q].k ? 0.f : v.x;
+                v.y = sB == a[q].k ? 0.f : v.y;
+                a[q].p = add2(a[q].p, v);
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < kS; ++q) a[q].fold();
+    }
+};
+
+// psi of every star of a single system or forest (groups of 32 kS; forest groups from the build),
+// by sorted index: the list walk's traversal with the potential sink.
+template <bool kQuad, bool kSoft, int kS>
+__global__ __launch_bounds__(kLwThreads) void k_walk_lists_pot(const DevInfo *info, const LNode *__restrict__ nodes,
+                                                               const float4 *__restrict__ st_hi,
+                                                               const float4 *__restrict__ st_lo, float eps, float eps2,
+                                                               double *psi, const int4 *__restrict__ groups,
+                                                               uint32_t *work_ctr, DevInfo *err_info, int node_depth,
+                                                               int src_depth) {
+    constexpr int kG = 32 * kS;
+    __shared__ AdjWarpMem smem[kLwWarps];
+    AdjWarpMem &W = smem[threadIdx.x >> 5];
+    const int lane = threadIdx.x & 31;
+    const int32_t ns = int32_t(info->nstars);
+    const int32_t nn = int32_t(info->nnodes);
+    const int32_t ng = nn > 0 ? (groups ? int32_t(info->ngroups) : (ns + kG - 1) / kG) : 0;
+    for (;;) {
+        int32_t idx = 0;
+        if (lane == 0) idx = int32_t(atomicAdd(work_ctr, 1u));
+        idx = __shfl_sync(kFull, idx, 0);
+        if (idx >= ng) break;
+        const GroupRange R = group_range<kG>(idx, groups, ns);
+        if (R.cnt <= 0) continue;
+        GroupStars<kS> G;
+        group_stars<kS>(lane, R, nullptr, st_hi, st_lo, G);
+        const GroupBox B = group_box<kS>(lane, R.cnt, G.t, eps);
+        __syncwarp();
+        PotAcc a[kS];
+#pragma unroll
+        for (int q = 0; q < kS; ++q) {
+            a[q].p = f2(0.f);
+            a[q].s = a[q].c = 0.f;
+            a[q].k = G.k[q];
+        }
+        PotSink sink{W.nbuf, W.sbuf, W.nidx, W.sidx};
+        GroupOut r;
+        if (B.exact)
+            r = walk_group<true, kQuad, kSoft, kS>(W.tm, sink, lane, R.root, G.t, G.Ox, G.Oy, G.Oz, B.bx0, B.by0,
+                                                    B.bz0, B.bx1, B.by1, B.bz1, B.ext, eps2, node_depth, src_depth,
+                                                    nodes, st_hi, st_lo, nn, ns, err_info, a);
+        else
+            r = walk_group<false, kQuad, kSoft, kS>(W.tm, sink, lane, R.root, G.t, G.Ox, G.Oy, G.Oz, B.bx0, B.by0,
+                                                     B.bz0, B.bx1, B.by1, B.bz1, B.ext, eps2, node_depth, src_depth,
+                                                     nodes, st_hi, st_lo, nn, ns, err_info, a);
+        __syncwarp();
+        if (!r.ok) break;
+#pragma unroll
+        for (int q = 0; q < kS; ++q)
+            if (G.valid[q]) psi[G.k[q]] = double(a[q].s) - double(a[q].c);
+    }
+}
+
 // The leaf of every sorted star (from the leaves' star ranges in their list records).
 __global__ void k_star_leaf(const DevInfo *info, const LNode *__restrict__ nodes, int32_t *star_leaf) {
     const int64_t r = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
@@ -1185,6 +1344,29 @@ cudaError_t walk_lists(const Launch &L, const TreeBufs &b, int64_t nstars_cap, f
     const bool lpt = b.lpt && !targets;  // a target list changes from event to event
     if (stars_per_lane == 2) return walk_lists_s<2>(L, b, nstars_cap, eps2, quad, ax, ay, az, nd, sd, lpt, targets);
     return walk_lists_s<1>(L, b, nstars_cap, eps2, quad, ax, ay, az, nd, sd, lpt, targets);
+}
+
+template <bool kQuad>
+static cudaError_t launch_pot(const Launch &L, const TreeBufs &b, float eps2, double *psi) {
+    static int blocks_per_sm = 0;  // per instantiation
+    cudaError_t e;
+    if (!blocks_per_sm) {
+        if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_walk_lists_pot<kQuad, true, 2>,
+                                                               kLwThreads, 0)))
+            return e;
+        if (blocks_per_sm < 1) blocks_per_sm = 1;
+    }
+    if ((e = cudaMemsetAsync(b.walk_ctr, 0, sizeof(uint32_t), L.stream))) return e;
+    const int sms = L.num_sms > 0 ? L.num_sms : 152;
+    k_walk_lists_pot<kQuad, true, 2><<<unsigned(sms * blocks_per_sm), kLwThreads, 0, L.stream>>>(
+        b.info, b.lnode, b.st_hi, b.st_lo, sqrtf(eps2), eps2, psi, b.nsys > 1 ? b.groups : nullptr, b.walk_ctr,
+        b.info, kDefaultListDepth, 2 * kDefaultListDepth);
+    ++*L.count;
+    return cudaGetLastError();
+}
+
+cudaError_t walk_lists_potential(const Launch &L, const TreeBufs &b, float eps2, int quad, double *psi) {
+    return quad ? launch_pot<true>(L, b, eps2, psi) : launch_pot<false>(L, b, eps2, psi);
 }
 
 cudaError_t walk_lists_adjoint(const Launch &L, const TreeBufs &b, float eps2, const double *px, const double *py,
