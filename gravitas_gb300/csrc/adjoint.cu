@@ -403,13 +403,19 @@ __global__ void k_vjp_reduce(int64_t n, int nsplit, const double *__restrict__ p
 
 // ---- host helpers ----
 
+// Stars per group of the tree force's list walk: 64 (two a lane; each lane then adds its two
+// stars' terms before the adjoint walk's reduce-scatter).
+constexpr int kAdjGroup = 64;
+
 inline cudaError_t mark(AdjTape &t) { return t.mark ? t.mark(t.mark_arg) : cudaSuccess; }
 
-// The tree at (x, y, z) for the tree force: FP32 moments, 32-star groups of the list walk.
+// The tree at (x, y, z) for the tree force: FP32 moments, kAdjGroup-star groups of the list walk
+// (the forward and the adjoint walk take the same groups, and both split among warps when the
+// groups are few).
 cudaError_t tree_at(const Launch &L, AdjTape &t, const double *x, const double *y, const double *z, double *ax,
                     double *ay, double *az) {
     TreeBufs &b = *t.tb;
-    b.group = 32;
+    b.group = kAdjGroup;
     b.list_depth = 0;
     b.lpt = true;
     b.split = true;  // few groups: the forward walk shares each among several warps (the same lists)
@@ -426,7 +432,7 @@ cudaError_t force(const Launch &L, AdjTape &t, const double *x, const double *y,
     if (t.tree) {
         if ((e = tree_at(L, t, x, y, z, ax, ay, az))) return e;
         if ((e = mark(t))) return e;
-        if ((e = walk_lists(L, *t.tb, t.n, float(t.eps2), 1, ax, ay, az, 0, false, 1))) return e;
+        if ((e = walk_lists(L, *t.tb, t.n, float(t.eps2), 1, ax, ay, az, 0, false, kAdjGroup / 32))) return e;
         return mark(t);
     }
     if (!t.fp32) {

@@ -390,7 +390,7 @@ cudaError_t walk_lists(const Launch &L, const TreeBufs &b, int64_t nstars_cap, f
 // psi of every star by sorted index (the tree potential of potential.go:44-81) with the list walk:
 // 64-star groups of the build (b.group == 64), softening > 0, b.cap_nodes < 2^29.
 cudaError_t walk_lists_potential(const Launch &L, const TreeBufs &b, float eps2, int quad, double *psi);
-// The transposed Jacobian of the list walk's force (32-star groups, quadrupoles, softening > 0)
+// The transposed Jacobian of the list walk's force (the groups of b.group, quadrupoles, softening > 0)
 // with the lists of the tree in b frozen: for weights w (state order) writes, in state order,
 // (J^T w)_i and (da/dm)^T w_i into out (x, y, z and m terms, n apart). px .. mass: the state the
 // tree was built from.

@@ -873,15 +873,17 @@ struct AdjSink {
     double *nadj;  // [node][kAdjNodeTerms]
     double *sadj;  // [sorted star][kAdjStarTerms]
 
+    // With kS stars a lane, each lane adds its stars' source terms before the reduce-scatter, so
+    // its shuffles serve 32 kS stars (with one star the sums are the terms themselves, bit for bit).
     template <bool kExact, bool kQuad, bool kSoft, int kS>
     __device__ __forceinline__ void nodes(int count, const Target (&tt)[kS], float eps2, AdjAcc (&aa)[kS],
                                           int lane) {
-        static_assert(kS == 1 && kQuad && kSoft, "the adjoint walk: one star a lane, quadrupoles, softening");
+        static_assert(kQuad && kSoft, "the adjoint walk: quadrupoles, softening");
         using Lay = Layout<kExact>;
-        const Target &t = tt[0];
-        AdjAcc &a = aa[0];
-        const float2 e2 = f2(eps2), wx = f2(a.wx), wy = f2(a.wy), wz = f2(a.wz);
-        float2 gx = f2(0.f), gy = f2(0.f), gz = f2(0.f);
+        const float2 e2 = f2(eps2);
+        float2 gx[kS], gy[kS], gz[kS];
+#pragma unroll
+        for (int q = 0; q < kS; ++q) gx[q] = gy[q] = gz[q] = f2(0.f);
         const int np = (count + 1) >> 1;
         for (int p = 0; p < np; ++p) {
             const float4 *r = &nbuf[p * Lay::kNodePair];
@@ -893,50 +895,61 @@ struct AdjSink {
                 ly = hi2(r5);
                 lz = lo2(r6);
             }
-            const float2 dx = sep<kExact>(lo2(r0), lx, -t.tx, -t.hx, -t.lx);
-            const float2 dy = sep<kExact>(hi2(r0), ly, -t.ty, -t.hy, -t.ly);
-            const float2 dz = sep<kExact>(lo2(r1), lz, -t.tz, -t.hz, -t.lz);
-            const float2 rr = fma2(dz, dz, fma2(dy, dy, fma2(dx, dx, e2)));
-            const float2 ir = make_float2(rsqrtf(rr.x), rsqrtf(rr.y));
-            const float2 ir2 = mul2(ir, ir), ir3 = mul2(ir2, ir), ir5 = mul2(ir3, ir2), ir7 = mul2(ir5, ir2),
-                         ir9 = mul2(ir7, ir2);
             const float2 m = hi2(r1);
             // the record holds -Q: n = -Q
             const float2 nxx = lo2(r2a), nyy = hi2(r2a), nzz = lo2(r3), nxy = hi2(r3), nxz = lo2(r4), nyz = hi2(r4);
-            const float2 qx = fma2(nxz, dz, fma2(nxy, dy, mul2(nxx, dx)));  // -(Q d)
-            const float2 qy = fma2(nyz, dz, fma2(nyy, dy, mul2(nxy, dx)));
-            const float2 qz = fma2(nzz, dz, fma2(nyz, dy, mul2(nxz, dx)));
-            const float2 dqd = fma2(dz, qz, fma2(dy, qy, mul2(dx, qx)));      // -(d.Q.d)
-            const float2 dw = fma2(dz, wz, fma2(dy, wy, mul2(dx, wx)));
-            const float2 qw = fma2(qz, wz, fma2(qy, wy, mul2(qx, wx)));       // -(Q d . w)
-            const float2 nwx = fma2(nxz, wz, fma2(nxy, wy, mul2(nxx, wx)));   // -(Q w)
-            const float2 nwy = fma2(nyz, wz, fma2(nyy, wy, mul2(nxy, wx)));
-            const float2 nwz = fma2(nzz, wz, fma2(nyz, wy, mul2(nxz, wx)));
-            const float2 f = fma2(mul2(dqd, ir7), f2(-2.5f), mul2(m, ir3));
-            // grad f . w = -3 m dw / r^5 - 5 (-(Qd.w)) / r^7 + 17.5 (-(dQd)) dw / r^9
-            const float2 gw = fma2(mul2(mul2(dqd, ir9), dw), f2(17.5f),
-                                   fma2(mul2(qw, ir7), f2(-5.f), mul2(mul2(m, ir5), mul2(dw, f2(-3.f)))));
-            const float2 c5 = mul2(mul2(ir7, dw), f2(-5.f));  // -5 dw / r^7, times -(Q d)
-            const float2 jx = fma2(c5, qx, fma2(ir5, nwx, fma2(dx, gw, mul2(f, wx))));
-            const float2 jy = fma2(c5, qy, fma2(ir5, nwy, fma2(dy, gw, mul2(f, wy))));
-            const float2 jz = fma2(c5, qz, fma2(ir5, nwz, fma2(dz, gw, mul2(f, wz))));
-            gx = add2(gx, jx);
-            gy = add2(gy, jy);
-            gz = add2(gz, jz);
-            // d(w.a)/dQ: xx: 5/2 dw dx^2 / r^7 - wx dx / r^5; xy: 5 dw dx dy / r^7 - (wx dy + wy dx) / r^5
-            const float2 qa = mul2(mul2(ir7, dw), f2(2.5f));
-            const float2 Gxx = fma2(mul2(qa, dx), dx, mul2(mul2(ir5, wx), mul2(dx, f2(-1.f))));
-            const float2 Gyy = fma2(mul2(qa, dy), dy, mul2(mul2(ir5, wy), mul2(dy, f2(-1.f))));
-            const float2 Gzz = fma2(mul2(qa, dz), dz, mul2(mul2(ir5, wz), mul2(dz, f2(-1.f))));
-            const float2 qa2 = add2(qa, qa);
-            const float2 Gxy = fma2(mul2(qa2, dx), dy, mul2(ir5, mul2(fma2(wx, dy, mul2(wy, dx)), f2(-1.f))));
-            const float2 Gxz = fma2(mul2(qa2, dx), dz, mul2(ir5, mul2(fma2(wx, dz, mul2(wz, dx)), f2(-1.f))));
-            const float2 Gyz = fma2(mul2(qa2, dy), dz, mul2(ir5, mul2(fma2(wy, dz, mul2(wz, dy)), f2(-1.f))));
-            const float2 am = mul2(dw, ir3);
+            float v[32];
+#pragma unroll
+            for (int i = 0; i < 32; ++i) v[i] = 0.f;
+#pragma unroll
+            for (int q = 0; q < kS; ++q) {
+                const Target &t = tt[q];
+                const float2 wx = f2(aa[q].wx), wy = f2(aa[q].wy), wz = f2(aa[q].wz);
+                const float2 dx = sep<kExact>(lo2(r0), lx, -t.tx, -t.hx, -t.lx);
+                const float2 dy = sep<kExact>(hi2(r0), ly, -t.ty, -t.hy, -t.ly);
+                const float2 dz = sep<kExact>(lo2(r1), lz, -t.tz, -t.hz, -t.lz);
+                const float2 rr = fma2(dz, dz, fma2(dy, dy, fma2(dx, dx, e2)));
+                const float2 ir = make_float2(rsqrtf(rr.x), rsqrtf(rr.y));
+                const float2 ir2 = mul2(ir, ir), ir3 = mul2(ir2, ir), ir5 = mul2(ir3, ir2), ir7 = mul2(ir5, ir2),
+                             ir9 = mul2(ir7, ir2);
+                const float2 qx = fma2(nxz, dz, fma2(nxy, dy, mul2(nxx, dx)));  // -(Q d)
+                const float2 qy = fma2(nyz, dz, fma2(nyy, dy, mul2(nxy, dx)));
+                const float2 qz = fma2(nzz, dz, fma2(nyz, dy, mul2(nxz, dx)));
+                const float2 dqd = fma2(dz, qz, fma2(dy, qy, mul2(dx, qx)));      // -(d.Q.d)
+                const float2 dw = fma2(dz, wz, fma2(dy, wy, mul2(dx, wx)));
+                const float2 qw = fma2(qz, wz, fma2(qy, wy, mul2(qx, wx)));       // -(Q d . w)
+                const float2 nwx = fma2(nxz, wz, fma2(nxy, wy, mul2(nxx, wx)));   // -(Q w)
+                const float2 nwy = fma2(nyz, wz, fma2(nyy, wy, mul2(nxy, wx)));
+                const float2 nwz = fma2(nzz, wz, fma2(nyz, wy, mul2(nxz, wx)));
+                const float2 f = fma2(mul2(dqd, ir7), f2(-2.5f), mul2(m, ir3));
+                // grad f . w = -3 m dw / r^5 - 5 (-(Qd.w)) / r^7 + 17.5 (-(dQd)) dw / r^9
+                const float2 gw = fma2(mul2(mul2(dqd, ir9), dw), f2(17.5f),
+                                       fma2(mul2(qw, ir7), f2(-5.f), mul2(mul2(m, ir5), mul2(dw, f2(-3.f)))));
+                const float2 c5 = mul2(mul2(ir7, dw), f2(-5.f));  // -5 dw / r^7, times -(Q d)
+                const float2 jx = fma2(c5, qx, fma2(ir5, nwx, fma2(dx, gw, mul2(f, wx))));
+                const float2 jy = fma2(c5, qy, fma2(ir5, nwy, fma2(dy, gw, mul2(f, wy))));
+                const float2 jz = fma2(c5, qz, fma2(ir5, nwz, fma2(dz, gw, mul2(f, wz))));
+                gx[q] = add2(gx[q], jx);
+                gy[q] = add2(gy[q], jy);
+                gz[q] = add2(gz[q], jz);
+                // d(w.a)/dQ: xx: 5/2 dw dx^2 / r^7 - wx dx / r^5; xy: 5 dw dx dy / r^7 - (wx dy + wy dx) / r^5
+                const float2 qa = mul2(mul2(ir7, dw), f2(2.5f));
+                const float2 Gxx = fma2(mul2(qa, dx), dx, mul2(mul2(ir5, wx), mul2(dx, f2(-1.f))));
+                const float2 Gyy = fma2(mul2(qa, dy), dy, mul2(mul2(ir5, wy), mul2(dy, f2(-1.f))));
+                const float2 Gzz = fma2(mul2(qa, dz), dz, mul2(mul2(ir5, wz), mul2(dz, f2(-1.f))));
+                const float2 qa2 = add2(qa, qa);
+                const float2 Gxy = fma2(mul2(qa2, dx), dy, mul2(ir5, mul2(fma2(wx, dy, mul2(wy, dx)), f2(-1.f))));
+                const float2 Gxz = fma2(mul2(qa2, dx), dz, mul2(ir5, mul2(fma2(wx, dz, mul2(wz, dx)), f2(-1.f))));
+                const float2 Gyz = fma2(mul2(qa2, dy), dz, mul2(ir5, mul2(fma2(wy, dz, mul2(wz, dy)), f2(-1.f))));
+                const float2 am = mul2(dw, ir3);
+                const float2 term[10] = {jx, jy, jz, am, Gxx, Gyy, Gzz, Gxy, Gxz, Gyz};
+#pragma unroll
+                for (int i = 0; i < kAdjNodeTerms; ++i) {
+                    v[i] += term[i].x;
+                    v[kAdjNodeTerms + i] += term[i].y;
+                }
+            }
             const bool hasB = 2 * p + 1 < count;  // the padded last entry is no node
-            float v[32] = {jx.x,  jy.x,  jz.x,  am.x,  Gxx.x, Gyy.x, Gzz.x, Gxy.x, Gxz.x, Gyz.x, jx.y,
-                           jy.y,  jz.y,  am.y,  Gxx.y, Gyy.y, Gzz.y, Gxy.y, Gxz.y, Gyz.y, 0.f,  0.f,
-                           0.f,   0.f,   0.f,   0.f,   0.f,   0.f,   0.f,   0.f,   0.f,   0.f};
             reduce_scatter32(v, lane);
             if (lane < kAdjNodeTerms || (hasB && lane < 2 * kAdjNodeTerms)) {
                 const int e = 2 * p + (lane >= kAdjNodeTerms ? 1 : 0);
@@ -944,20 +957,23 @@ struct AdjSink {
                 atomicAdd(&nadj[int64_t(nidx[e]) * kAdjNodeTerms + term], double(v[0]));
             }
         }
-        a.gx -= double(gx.x) + double(gx.y);
-        a.gy -= double(gy.x) + double(gy.y);
-        a.gz -= double(gz.x) + double(gz.y);
+#pragma unroll
+        for (int q = 0; q < kS; ++q) {
+            aa[q].gx -= double(gx[q].x) + double(gx[q].y);
+            aa[q].gy -= double(gy[q].x) + double(gy[q].y);
+            aa[q].gz -= double(gz[q].x) + double(gz[q].y);
+        }
     }
 
     template <bool kExact, bool kSoft, int kS>
     __device__ __forceinline__ void sources(int count, const Target (&tt)[kS], float eps2, AdjAcc (&aa)[kS],
                                             int lane) {
-        static_assert(kS == 1 && kSoft, "the adjoint walk: one star a lane, softening");
+        static_assert(kSoft, "the adjoint walk: softening");
         using Lay = Layout<kExact>;
-        const Target &t = tt[0];
-        AdjAcc &a = aa[0];
-        const float2 e2 = f2(eps2), wx = f2(a.wx), wy = f2(a.wy), wz = f2(a.wz);
-        float2 gx = f2(0.f), gy = f2(0.f), gz = f2(0.f);
+        const float2 e2 = f2(eps2);
+        float2 gx[kS], gy[kS], gz[kS];
+#pragma unroll
+        for (int q = 0; q < kS; ++q) gx[q] = gy[q] = gz[q] = f2(0.f);
         const int np = (count + 1) >> 1;
         for (int p = 0; p < np; ++p) {
             const float4 *r = &sbuf[p * Lay::kSrcPair];
@@ -969,28 +985,44 @@ struct AdjSink {
                 ly = hi2(r2a);
                 lz = lo2(r3);
             }
-            const float2 dx = sep<kExact>(lo2(r0), lx, -t.tx, -t.hx, -t.lx);
-            const float2 dy = sep<kExact>(hi2(r0), ly, -t.ty, -t.hy, -t.ly);
-            const float2 dz = sep<kExact>(lo2(r1), lz, -t.tz, -t.hz, -t.lz);
-            const float2 rr = fma2(dz, dz, fma2(dy, dy, fma2(dx, dx, e2)));
-            const float2 ir = make_float2(rsqrtf(rr.x), rsqrtf(rr.y));
-            const float2 ir2 = mul2(ir, ir), ir3 = mul2(ir2, ir), ir5 = mul2(ir3, ir2);
             const bool hasB = 2 * p + 1 < count;
-            // a star and its own pair, and the padded last entry, contribute nothing
-            const float keepA = sidx[2 * p] == a.k ? 0.f : 1.f;
-            const float keepB = hasB && sidx[2 * p + 1] != a.k ? 1.f : 0.f;
-            const float2 m = mul2(hi2(r1), make_float2(keepA, keepB));
-            const float2 dw = fma2(dz, wz, fma2(dy, wy, mul2(dx, wx)));
-            // m K w = m (w / r^3 - 3 d dw / r^5)
-            const float2 c3 = mul2(mul2(ir5, dw), f2(-3.f));
-            const float2 kx = mul2(m, fma2(c3, dx, mul2(ir3, wx)));
-            const float2 ky = mul2(m, fma2(c3, dy, mul2(ir3, wy)));
-            const float2 kz = mul2(m, fma2(c3, dz, mul2(ir3, wz)));
-            gx = add2(gx, kx);
-            gy = add2(gy, ky);
-            gz = add2(gz, kz);
-            const float2 am = mul2(mul2(dw, ir3), make_float2(keepA, keepB));
-            float v[8] = {kx.x, ky.x, kz.x, am.x, kx.y, ky.y, kz.y, am.y};
+            const int32_t sA = sidx[2 * p], sB = hasB ? sidx[2 * p + 1] : -1;
+            float v[8];
+#pragma unroll
+            for (int i = 0; i < 8; ++i) v[i] = 0.f;
+#pragma unroll
+            for (int q = 0; q < kS; ++q) {
+                const Target &t = tt[q];
+                const float2 wx = f2(aa[q].wx), wy = f2(aa[q].wy), wz = f2(aa[q].wz);
+                const float2 dx = sep<kExact>(lo2(r0), lx, -t.tx, -t.hx, -t.lx);
+                const float2 dy = sep<kExact>(hi2(r0), ly, -t.ty, -t.hy, -t.ly);
+                const float2 dz = sep<kExact>(lo2(r1), lz, -t.tz, -t.hz, -t.lz);
+                const float2 rr = fma2(dz, dz, fma2(dy, dy, fma2(dx, dx, e2)));
+                const float2 ir = make_float2(rsqrtf(rr.x), rsqrtf(rr.y));
+                const float2 ir2 = mul2(ir, ir), ir3 = mul2(ir2, ir), ir5 = mul2(ir3, ir2);
+                // a star and its own pair, and the padded last entry, contribute nothing
+                const float keepA = sA == aa[q].k ? 0.f : 1.f;
+                const float keepB = hasB && sB != aa[q].k ? 1.f : 0.f;
+                const float2 m = mul2(hi2(r1), make_float2(keepA, keepB));
+                const float2 dw = fma2(dz, wz, fma2(dy, wy, mul2(dx, wx)));
+                // m K w = m (w / r^3 - 3 d dw / r^5)
+                const float2 c3 = mul2(mul2(ir5, dw), f2(-3.f));
+                const float2 kx = mul2(m, fma2(c3, dx, mul2(ir3, wx)));
+                const float2 ky = mul2(m, fma2(c3, dy, mul2(ir3, wy)));
+                const float2 kz = mul2(m, fma2(c3, dz, mul2(ir3, wz)));
+                gx[q] = add2(gx[q], kx);
+                gy[q] = add2(gy[q], ky);
+                gz[q] = add2(gz[q], kz);
+                const float2 am = mul2(mul2(dw, ir3), make_float2(keepA, keepB));
+                v[0] += kx.x;
+                v[1] += ky.x;
+                v[2] += kz.x;
+                v[3] += am.x;
+                v[4] += kx.y;
+                v[5] += ky.y;
+                v[6] += kz.y;
+                v[7] += am.y;
+            }
             reduce_scatter8(v, lane);
             if (lane < kAdjStarTerms || (hasB && lane < 2 * kAdjStarTerms)) {
                 const int e = 2 * p + (lane >= kAdjStarTerms ? 1 : 0);
@@ -998,9 +1030,12 @@ struct AdjSink {
                 atomicAdd(&sadj[int64_t(sidx[e]) * kAdjStarTerms + term], double(v[0]));
             }
         }
-        a.gx -= double(gx.x) + double(gx.y);
-        a.gy -= double(gy.x) + double(gy.y);
-        a.gz -= double(gz.x) + double(gz.y);
+#pragma unroll
+        for (int q = 0; q < kS; ++q) {
+            aa[q].gx -= double(gx[q].x) + double(gx[q].y);
+            aa[q].gy -= double(gy[q].x) + double(gy[q].y);
+            aa[q].gz -= double(gz[q].x) + double(gz[q].y);
+        }
     }
 };
 
@@ -1012,10 +1047,11 @@ struct __align__(16) AdjWarpMem {
     TravMem tm;
 };
 
-// The adjoint walk over 32-star groups (the forward's group size in adjoint mode): the same
-// traversal as k_walk_lists<quad, soft, 1>, with the adjoint sink. w: the weights in state order
-// (three arrays); tgt: each sorted star's own terms (3 doubles).
-template <bool kSplit>
+// The adjoint walk over groups of 32 kS stars (the forward's groups in adjoint mode): the same
+// traversal as k_walk_lists<quad, soft, kS, kSplit>, with the adjoint sink. w: the weights in
+// state order (three arrays); tgt: each sorted star's own terms (3 doubles), or with kSplit each
+// part's by sorted index in part_tgt (k_adj_part_combine adds the parts).
+template <int kS, bool kSplit>
 __global__ __launch_bounds__(kLwThreads) void k_walk_lists_adj(const DevInfo *info, const LNode *__restrict__ nodes,
                                                                const float4 *__restrict__ st_hi,
                                                                const float4 *__restrict__ st_lo,
@@ -1027,7 +1063,7 @@ __global__ __launch_bounds__(kLwThreads) void k_walk_lists_adj(const DevInfo *in
                                                                DevInfo *err_info, int node_depth, int src_depth,
                                                                int nparts, double *part_tgt, int64_t part_stride,
                                                                const int2 *__restrict__ ranges) {
-    constexpr int kS = 1, kG = 32;
+    constexpr int kG = 32 * kS;
     __shared__ AdjWarpMem smem[kLwWarps];
     AdjWarpMem &W = smem[threadIdx.x >> 5];
     const int lane = threadIdx.x & 31;
@@ -1050,14 +1086,17 @@ __global__ __launch_bounds__(kLwThreads) void k_walk_lists_adj(const DevInfo *in
         group_stars<kS>(lane, R, nullptr, st_hi, st_lo, G);
         const GroupBox B = group_box<kS>(lane, R.cnt, G.t, eps);
         __syncwarp();
-        AdjAcc a[1];
-        const int32_t o = order[G.k[0]];
-        // a lane beyond the group (a copy of the first star) weighs nothing: no source terms
-        a[0].wx = G.valid[0] ? float(wx[o]) : 0.f;
-        a[0].wy = G.valid[0] ? float(wy[o]) : 0.f;
-        a[0].wz = G.valid[0] ? float(wz[o]) : 0.f;
-        a[0].k = G.k[0];
-        a[0].gx = a[0].gy = a[0].gz = 0.0;
+        AdjAcc a[kS];
+#pragma unroll
+        for (int q = 0; q < kS; ++q) {
+            const int32_t o = order[G.k[q]];
+            // a star beyond the group (a copy of the first star) weighs nothing: no source terms
+            a[q].wx = G.valid[q] ? float(wx[o]) : 0.f;
+            a[q].wy = G.valid[q] ? float(wy[o]) : 0.f;
+            a[q].wz = G.valid[q] ? float(wz[o]) : 0.f;
+            a[q].k = G.k[q];
+            a[q].gx = a[q].gy = a[q].gz = 0.0;
+        }
         AdjSink sink{W.nbuf, W.sbuf, W.nidx, W.sidx, nadj, sadj};
         GroupOut r;
         if (B.exact)
@@ -1072,16 +1111,18 @@ __global__ __launch_bounds__(kLwThreads) void k_walk_lists_adj(const DevInfo *in
                                                           s_lo, s_hi);
         __syncwarp();
         if (!r.ok) break;
-        if (G.valid[0]) {
+#pragma unroll
+        for (int u = 0; u < kS; ++u) {
+            if (!G.valid[u]) continue;
             if constexpr (kSplit) {  // the part's own terms by sorted index; k_adj_part_combine adds them
                 double *q = part_tgt + int64_t(part) * 3 * part_stride;
-                q[G.k[0]] = a[0].gx;
-                q[part_stride + G.k[0]] = a[0].gy;
-                q[2 * part_stride + G.k[0]] = a[0].gz;
+                q[G.k[u]] = a[u].gx;
+                q[part_stride + G.k[u]] = a[u].gy;
+                q[2 * part_stride + G.k[u]] = a[u].gz;
             } else {
-                tgt[3 * int64_t(G.k[0])] = a[0].gx;
-                tgt[3 * int64_t(G.k[0]) + 1] = a[0].gy;
-                tgt[3 * int64_t(G.k[0]) + 2] = a[0].gz;
+                tgt[3 * int64_t(G.k[u])] = a[u].gx;
+                tgt[3 * int64_t(G.k[u]) + 1] = a[u].gy;
+                tgt[3 * int64_t(G.k[u]) + 2] = a[u].gz;
             }
         }
     }
@@ -1369,6 +1410,44 @@ cudaError_t walk_lists_potential(const Launch &L, const TreeBufs &b, float eps2,
     return quad ? launch_pot<true>(L, b, eps2, psi) : launch_pot<false>(L, b, eps2, psi);
 }
 
+template <int kS>
+static cudaError_t launch_adj(const Launch &L, const TreeBufs &b, int64_t n, float eps2, const double *wx,
+                              const double *wy, const double *wz, AdjTreeBufs &s) {
+    const int parts = split_parts(b, n, false, 32 * kS);
+    const int sms = L.num_sms > 0 ? L.num_sms : 152;
+    const int nd = kDefaultListDepth, sd = 2 * kDefaultListDepth;
+    cudaError_t e;
+    if (parts > 1) {
+        static int bps_split = 0;  // per instantiation
+        if (!bps_split) {
+            if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps_split, k_walk_lists_adj<kS, true>, kLwThreads,
+                                                                   0)))
+                return e;
+            if (bps_split < 1) bps_split = 1;
+        }
+        k_walk_lists_adj<kS, true><<<unsigned(sms * bps_split), kLwThreads, 0, L.stream>>>(
+            b.info, b.lnode, b.st_hi, b.st_lo, b.order, sqrtf(eps2), eps2, wx, wy, wz, s.tgt, s.nadj, s.sadj,
+            b.walk_ctr, b.info, nd, sd, parts, b.part_acc, n, b.mrange);
+        ++*L.count;
+        if ((e = cudaGetLastError())) return e;
+        k_adj_part_combine<<<unsigned((n + 255) / 256), 256, 0, L.stream>>>(b.info, parts, b.part_acc, n, s.tgt);
+        ++*L.count;
+        return cudaGetLastError();
+    }
+    static int blocks_per_sm = 0;  // per instantiation
+    if (!blocks_per_sm) {
+        if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_walk_lists_adj<kS, false>, kLwThreads,
+                                                               0)))
+            return e;
+        if (blocks_per_sm < 1) blocks_per_sm = 1;
+    }
+    k_walk_lists_adj<kS, false><<<unsigned(sms * blocks_per_sm), kLwThreads, 0, L.stream>>>(
+        b.info, b.lnode, b.st_hi, b.st_lo, b.order, sqrtf(eps2), eps2, wx, wy, wz, s.tgt, s.nadj, s.sadj, b.walk_ctr,
+        b.info, nd, sd, 1, nullptr, 0, nullptr);
+    ++*L.count;
+    return cudaGetLastError();
+}
+
 cudaError_t walk_lists_adjoint(const Launch &L, const TreeBufs &b, float eps2, const double *px, const double *py,
                                const double *pz, const double *mass, const double *wx, const double *wy,
                                const double *wz, int64_t n, AdjTreeBufs &s, double *out) {
@@ -1378,38 +1457,8 @@ cudaError_t walk_lists_adjoint(const Launch &L, const TreeBufs &b, float eps2, c
     if ((e = cudaMemsetAsync(s.star_leaf, 0xff, sizeof(int32_t) * size_t(b.cap_n), L.stream))) return e;
     if ((e = cudaMemsetAsync(b.walk_ctr, 0, sizeof(uint32_t), L.stream))) return e;
     // few groups: each group's walk shared among several warps, as the forward's (walk_lists)
-    const int parts = split_parts(b, n, false, 32);
-    const int sms = L.num_sms > 0 ? L.num_sms : 152;
-    const int nd = kDefaultListDepth, sd = 2 * kDefaultListDepth;
-    if (parts > 1) {
-        static int bps_split = 0;
-        if (!bps_split) {
-            if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps_split, k_walk_lists_adj<true>, kLwThreads, 0)))
-                return e;
-            if (bps_split < 1) bps_split = 1;
-        }
-        k_walk_lists_adj<true><<<unsigned(sms * bps_split), kLwThreads, 0, L.stream>>>(
-            b.info, b.lnode, b.st_hi, b.st_lo, b.order, sqrtf(eps2), eps2, wx, wy, wz, s.tgt, s.nadj, s.sadj,
-            b.walk_ctr, b.info, nd, sd, parts, b.part_acc, n, b.mrange);
-        ++*L.count;
-        if ((e = cudaGetLastError())) return e;
-        k_adj_part_combine<<<unsigned((n + 255) / 256), 256, 0, L.stream>>>(b.info, parts, b.part_acc, n, s.tgt);
-        ++*L.count;
-        if ((e = cudaGetLastError())) return e;
-    } else {
-        static int blocks_per_sm = 0;
-        if (!blocks_per_sm) {
-            if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_walk_lists_adj<false>, kLwThreads,
-                                                                   0)))
-                return e;
-            if (blocks_per_sm < 1) blocks_per_sm = 1;
-        }
-        k_walk_lists_adj<false><<<unsigned(sms * blocks_per_sm), kLwThreads, 0, L.stream>>>(
-            b.info, b.lnode, b.st_hi, b.st_lo, b.order, sqrtf(eps2), eps2, wx, wy, wz, s.tgt, s.nadj, s.sadj,
-            b.walk_ctr, b.info, nd, sd, 1, nullptr, 0, nullptr);
-        ++*L.count;
-        if ((e = cudaGetLastError())) return e;
-    }
+    if ((e = b.group == 64 ? launch_adj<2>(L, b, n, eps2, wx, wy, wz, s) : launch_adj<1>(L, b, n, eps2, wx, wy, wz, s)))
+        return e;
     const unsigned nbn = unsigned((b.cap_nodes + 255) / 256), nbs = unsigned((b.cap_n + 255) / 256);
     k_star_leaf<<<nbn < 1 ? 1 : nbn, 256, 0, L.stream>>>(b.info, b.lnode, s.star_leaf);
     ++*L.count;
