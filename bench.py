@@ -638,7 +638,7 @@ def run_adjoint(args):
             fd = (vals[0] - vals[1]) / (2 * hh)
             g = tdv[i, c] if q % 2 == 0 else tdm[i]
             terrs.append(abs(g - fd) / max(abs(fd), 1e-3 * (tscale_v if q % 2 == 0 else tscale_m)))
-        tree = {"theta": THETA, "leaf": ADJ_TREE_LEAF, "walk": "list walk, 64-star groups split among warps, quadrupoles",
+        tree = {"theta": THETA, "leaf": ADJ_TREE_LEAF, "walk": "list walk, 32-star groups split among warps, quadrupoles",
                 "ms_per_gradient": statistics.median(twalls) * 1e3,
                 "value": n * T / statistics.median(twalls), "unit": "particle-steps/s",
                 "fd_check": {"coords": len(terrs), "h_v": h, "h_m": "1e-2 m_i",

@@ -305,7 +305,7 @@ typedef struct {
                           GBH_ADJ_FP32: FP32 pairs, double-float separations, compensated sums */
     int32_t force;     /* GBH_ADJ_DIRECT: the softened direct sum (direct.go:18-48), every body a
                           source; GBH_ADJ_TREE (GBH_ADJ_FP32 only): the Barnes-Hut force of the
-                          mixed walk (quadrupoles, 64-star groups of the list walk, FP32 moments),
+                          mixed walk (quadrupoles, 32-star groups of the list walk, FP32 moments),
                           differentiated with each step's interaction lists and tree topology
                           frozen (the lists the forward builds at the same positions) */
     int32_t leaf_size; /* GBH_ADJ_TREE: max stars per leaf; 0 means 24 */

@@ -1,6 +1,6 @@
 """GPU tests of the tree adjoint (gbh_adjoint_params.force = GBH_ADJ_TREE): the gradient of a
 final-state loss through KDK steps of the Barnes-Hut force (the mixed list walk, quadrupoles,
-64-star groups, split among warps at these sizes), with each step's interaction lists and tree
+32-star groups, split among warps at these sizes), with each step's interaction lists and tree
 topology frozen.
 
 * With a tiny opening angle every node is opened and the tree force is the softened direct sum:
