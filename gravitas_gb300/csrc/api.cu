@@ -657,6 +657,7 @@ int run_block_steps(gbh_ctx *ctx, const gbh_params *p, double T, double eta, int
         CK(gbh::block_open(L, ctx->tb, n, T, levels, eta, eps, ctx->ax, ctx->ay, ctx->az, ctx->vx, ctx->vy, ctx->vz,
                            ctx->rung, ctx->end_tick));
         if ((rc = read_info(ctx))) return rc;
+        if (ctx->info_host.next_count > 0) ctx->active_hint = int64_t(ctx->info_host.next_count);
         int32_t t = 0;
         while (t < ticks) {
             int32_t tn = ctx->info_host.next_tick;
@@ -669,7 +670,8 @@ int run_block_steps(gbh_ctx *ctx, const gbh_params *p, double T, double eta, int
             CK(gbh::block_close(L, ctx->tb, n, t, T, levels, eta, eps, ctx->ax, ctx->ay, ctx->az, ctx->vx, ctx->vy,
                                 ctx->vz, ctx->rung, ctx->end_tick));
             if ((rc = read_info(ctx))) return rc;
-            if (ctx->info_host.ntargets > 0) ctx->active_hint = int64_t(ctx->info_host.ntargets);
+            // the next event walks the bodies due at its tick: size its walk (split or not) by them
+            if (ctx->info_host.next_count > 0) ctx->active_hint = int64_t(ctx->info_host.next_count);
             if (st) {
                 st->substeps += 1;
                 st->evaluations += ctx->info_host.ntargets;

@@ -43,6 +43,7 @@ struct DevInfo {
     uint32_t ntargets;        // entries of the target list (walks restricted to active stars)
     uint32_t ngroups;         // mixed-walk groups of a forest
     int32_t next_tick;        // block steps: the earliest step end over all bodies
+    uint32_t next_count;      // block steps: the bodies whose step ends at next_tick
     // FP32 views for the FP32 upsweep: min corner and side as hi + lo pairs, and the
     // opening base 2 * half_L / theta per level L
     float min_hi[3], min_lo[3];

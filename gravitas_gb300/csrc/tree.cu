@@ -2551,6 +2551,22 @@ __global__ __launch_bounds__(kThreads) void k_block_close(int64_t n, int32_t tic
     atomicMin(&info->next_tick, e);
 }
 
+// The bodies whose step ends at the next event tick (the host sizes that event's walk by them).
+__global__ __launch_bounds__(kThreads) void k_count_next(int64_t n, const int32_t *__restrict__ end, DevInfo *info) {
+    const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    const int32_t tn = info->next_tick;
+    const unsigned m = __ballot_sync(0xffffffffu, i < n && end[i] == tn);  // whole warps: no early return
+    if ((threadIdx.x & 31) == 0 && m) atomicAdd(&info->next_count, uint32_t(__popc(m)));
+}
+
+cudaError_t count_next(const Launch &L, const TreeBufs &b, int64_t n, const int32_t *end) {
+    cudaError_t e = cudaMemsetAsync(&b.info->next_count, 0, sizeof(uint32_t), L.stream);
+    if (e != cudaSuccess) return e;
+    k_count_next<<<blocks_for(n, kThreads), kThreads, 0, L.stream>>>(n, end, b.info);
+    GBH_LAUNCH_CHECK();
+    return cudaSuccess;
+}
+
 }  // namespace
 
 cudaError_t block_open(const Launch &L, const TreeBufs &b, int64_t n, double T, int levels, double eta, double eps,
@@ -2561,7 +2577,7 @@ cudaError_t block_open(const Launch &L, const TreeBufs &b, int64_t n, double T, 
     k_block_open<<<blocks_for(n, kThreads), kThreads, 0, L.stream>>>(n, T, 1 << (levels - 1), levels, eta, eps, ax, ay,
                                                                      az, vx, vy, vz, rung, end, b.info);
     GBH_LAUNCH_CHECK();
-    return cudaSuccess;
+    return count_next(L, b, n, end);
 }
 
 cudaError_t block_drift(const Launch &L, int64_t n, double dt, double c, double *px, double *py, double *pz,
@@ -2579,7 +2595,7 @@ cudaError_t block_close(const Launch &L, const TreeBufs &b, int64_t n, int32_t t
     k_block_close<<<blocks_for(n, kThreads), kThreads, 0, L.stream>>>(n, tick, 1 << (levels - 1), T, levels, eta, eps,
                                                                       ax, ay, az, vx, vy, vz, rung, end, b.info);
     GBH_LAUNCH_CHECK();
-    return cudaSuccess;
+    return count_next(L, b, n, end);
 }
 
 }  // namespace gbh
