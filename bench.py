@@ -296,7 +296,7 @@ def run(args):
     l0, l1 = np.array(diag[0]["angular_momentum"]), np.array(diag[1]["angular_momentum"])
     drift = {"steps": args.warmup + args.steps, "dt": DT, "energy_rel": abs((e1 - e0) / e0),
              "angular_momentum_rel": float(np.linalg.norm(l1 - l0) / np.linalg.norm(l0)),
-             "energy_method": "tree potential at theta 0.5 from the mixed walk in potential mode (FP32 "
+             "energy_method": "tree potential at theta 0.5 from the list walk with a potential sink (FP32 "
                               "interactions, compensated per-star sums, FP64 total) + FP64 kinetic "
                               "(gbh_state_diagnostics with the step's parameters)"}
     t_plain, w_plain, b_plain, _, _ = timed_steps("plain", args.steps, args.warmup)
