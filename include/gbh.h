@@ -301,7 +301,7 @@ typedef struct {
     double softening;  /* Plummer epsilon; must be > 0 */
     int64_t nsteps;    /* >= 1 */
     int64_t every;     /* checkpoint interval K >= 1: (x, v, a) saved every K steps */
-    int32_t precision; /* GBH_ADJ_FP64: pair sums bit-identical to the FP64 checker;
+    int32_t precision; /* GBH_ADJ_FP64: pair sums in the FP64 reference order (j ascending);
                           GBH_ADJ_FP32: FP32 pairs, double-float separations, compensated sums */
     int32_t force;     /* GBH_ADJ_DIRECT: the softened direct sum (direct.go:18-48), every body a
                           source; GBH_ADJ_TREE (GBH_ADJ_FP32 only): the Barnes-Hut force of the

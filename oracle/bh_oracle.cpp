@@ -1,5 +1,5 @@
 // bh_oracle.cpp — TEST INFRASTRUCTURE ONLY: the CPU restatement of gravitas'
-// Barnes-Hut path used as the parity checker and as the timed CPU baseline.
+// Barnes-Hut path used as the parity oracle and as the timed CPU baseline.
 // Every function cites the reference file:line it follows. Build with
 // -ffp-contract=off (see bh_oracle.h).
 #include "bh_oracle.h"

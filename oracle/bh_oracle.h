@@ -4,7 +4,7 @@
  * A CPU restatement, in C++, of gravitas' Barnes-Hut quadrupole force path
  * (internal/sim/bh/{morton,parallel,build,bh,potential}.go), its FP64 direct
  * sum (internal/sim/direct/direct.go) and its KDK leapfrog
- * (internal/sim/sim.go). It is the parity checker for the CUDA library and the
+ * (internal/sim/sim.go). It is the parity oracle for the CUDA library and the
  * timed CPU baseline; it is never linked into, or called by, the product path.
  * Only tests/, __graft_entry__.smoke() and bench.py (its CPU baseline legs)
  * load it.

@@ -2,7 +2,7 @@
 
 TEST INFRASTRUCTURE ONLY: a C++ restatement of gravitas' CPU Barnes-Hut path
 (internal/sim/bh/*.go, internal/sim/direct/direct.go, internal/sim/sim.go) used
-as the parity checker in tests/ and as the timed CPU baseline in bench.py. The
+as the parity oracle in tests/ and as the timed CPU baseline in bench.py. The
 product path (gravitas_gb300) never imports this module.
 """
 from __future__ import annotations
