@@ -608,7 +608,7 @@ def run_adjoint(args):
             vals.append(float(np.sum((x - targets) ** 2) / n))
         fd = (vals[0] - vals[1]) / (2 * h)
         tree_errs.append(abs(dv[i, c] - fd) / max(abs(fd), 1e-3 * scale))
-    # The tree force (config 4's theta 0.5): the adjoint of the list walk with each step's lists
+    # The tree force (theta 0.5): the adjoint of the list walk with each step's lists
     # frozen, timed like the direct-sum gradient and checked against central differences of the
     # same tree forward (velocities at h, masses at 1e-2 of their value)
     tree = None

@@ -1923,7 +1923,7 @@ cudaError_t tree_build(const Launch &L, TreeBufs &b, int64_t n, const double *px
     if (forest && (!sys_of || !sys_off)) return cudaErrorInvalidValue;
     cudaError_t e;
     // one-sweep sort and single-pass scans (capacity up to kOsMaxN bodies): histograms, tile
-    // counters and the look-back words of the passes this build runs start at zero
+    // counters and the look-back words of the passes this tree build runs start at zero
     const bool os = b.os_state != nullptr;
     // a forest then sorts stably by system id, one pass per byte: up to 256 systems the high
     // byte is 0 everywhere, and that pass (a stable pass over equal digits) is left out

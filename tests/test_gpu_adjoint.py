@@ -131,7 +131,7 @@ def test_gradient_matches_central_differences_of_the_tree_dynamics(ctx):
     library's own tree forward (mixed walk, theta 0.5, 200 KDK steps through gbh_step_kdk) agree
     with the direct-sum adjoint gradient at the median to 1e-4 relative and on nine in ten of 32
     velocity coordinates to 1e-3; a quotient that straddles a jump stays within 5e-3 (the full
-    config-4 run's worst coordinate was 2.4e-3)."""
+    32,768-body, 1,000-step run's worst coordinate was 2.4e-3)."""
     n, dt, eps, nsteps = 2048, 1e-3, 0.01, 200
     s, targets = ics.adjoint_problem(n, seed=15)
     _, _, dv, _ = sim.trajectory_loss_gradient(s, targets, dt, eps, nsteps, 50, abi.ADJ_FP32, ctx)
