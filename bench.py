@@ -469,7 +469,7 @@ def run_profile(args):
     if args.profile == "forest":
         from gravitas_gb300 import ics
         s, off = ics.forest(nsys=64, seed=0)
-        ctx = abi.Context(0)
+        ctx = abi.Context(0, abi.CFG_PAIRED if args.paired else 0)
         ctx.forest_upload(off, s["px"], s["py"], s["pz"], s["vx"], s["vy"], s["vz"], s["mass"], s["kind"],
                           s["alive"])
         # the autotuner's pick for this forest (theta 0.7, leaf 32, 64-star groups); --leaf overrides
@@ -483,7 +483,7 @@ def run_profile(args):
         return 0
     n = args.n
     s = make_workload(n, seed=0)
-    ctx = abi.Context(0)
+    ctx = abi.Context(0, abi.CFG_PAIRED if args.paired else 0)
     ctx.call("gbh_state_upload", n, *[P(s[k]) for k in ("px", "py", "pz", "vx", "vy", "vz")], None, None, None,
              P(s["mass"]), None, None)
     leaf = args.leaf or REFERENCE_LEAF
@@ -1015,6 +1015,9 @@ def main():
                          "JSON line")
     ap.add_argument("--group", type=int, default=0, choices=[0, 32, 64],
                     help="--profile mixed: the mixed walk's group size (0: the library's default)")
+    ap.add_argument("--paired", action="store_true",
+                    help="--profile mixed / forest: 64-star groups take the paired walk (GBH_CFG_PAIRED), for "
+                         "captures of k_walk_mixed2")
     ap.add_argument("--no-configs", action="store_true",
                     help="headline: leave out the short forest and galaxy runs reported beside it")
     ap.add_argument("--fd-coords", type=int, default=16, help="adjoint: coordinates checked by central differences")
