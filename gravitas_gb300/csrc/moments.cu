@@ -149,7 +149,10 @@ __device__ __forceinline__ void finish_fast(const SysGeo &inf, FMom &q, float rh
 }
 
 constexpr unsigned kFull = 0xffffffffu;
-constexpr int kGroup = 2;  // lanes per leaf and per inner node (measured: 2 beats 4 and 8 above 1M bodies)
+// Lanes per leaf and per inner node. Measured on the merger (whole build, CUDA events): 2, 4 and
+// 8 lanes tie at 16k bodies; from 1M to 4M 2 lanes are fastest (more lanes mean more warps for
+// the same leaves), and one thread per leaf was 3-20 % slower below 2M and 3 % faster at 4M.
+constexpr int kGroup = 2;
 constexpr int kMaxChildren = 8;
 
 // Sum over the kGroup lanes of a group: every lane ends with the same bits (each butterfly step
